@@ -1,0 +1,138 @@
+/*
+ * CPU oracle for the ps3d vorticity right-hand side and time steppers.
+ *
+ * TEST INFRASTRUCTURE ONLY.  This is a plain-C FP64 restatement of the
+ * reference Fortran (matt-frey/ps3d, BSD-3-Clause) used as the parity checker
+ * for the GPU library and as the timed CPU baseline.  Only tests/, the smoke
+ * entry point and the benchmark's CPU-baseline leg may load it; the product
+ * path never does.
+ *
+ * Parity pinning: the restatement is checked against every known-answer unit
+ * test the reference ships for this path (unit-tests/test_vor2vel_1..5,
+ * test_diffz_1..4, test_diffx, test_diffy, test_omp_collapse,
+ * test_implicit_rk), ported to tests/test_oracle_kat.py.  The reference
+ * itself cannot be compiled in this environment (no Fortran compiler, MPI or
+ * NetCDF), so no run of the reference is available as a further check.
+ *
+ * Array layout (the reference's, src/fields/fields.f90:17-79): a scalar field
+ * is (0:nz, 0:ny-1, 0:nx-1) with z fastest, offset iz + (nz+1)*(iy + ny*ix);
+ * a vector field appends a component index (3 consecutive scalar fields).
+ */
+#ifndef PS3D_ORACLE_H
+#define PS3D_ORACLE_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* 1-D transforms (oracle/stafft.c, restating src/fft/stafft.f90) */
+int ps3o_factorise(int n, int factors[5]);
+int ps3o_initfft(int n, int factors[5], double *trig);
+void ps3o_forfft(int m, int n, double *x, double *wk, const double *trig,
+                 const int factors[5]);
+void ps3o_revfft(int m, int n, double *x, double *wk, const double *trig,
+                 const int factors[5]);
+void ps3o_dct(int m, int n, double *x, double *wk, double *wk2,
+              const double *trig, const int factors[5]);
+void ps3o_dst(int m, int n, double *x1, double *wk, double *wk2,
+              const double *trig, const int factors[5]);
+
+/* Run configuration: the subset of the &PS3D namelist (src/utils/options.f90)
+ * and box (src/utils/parameters.f90) that the hot path consumes. */
+enum { PS3O_PRE_CONSTANT = 0, PS3O_PRE_VORCH = 1, PS3O_PRE_BFMAX = 2,
+       PS3O_PRE_ROLL_MEAN_MAX_STRAIN = 3, PS3O_PRE_MAX_STRAIN = 4,
+       PS3O_PRE_US_MAX_STRAIN = 5 };
+enum { PS3O_KOLMOGOROV = 0, PS3O_GEOPHYSICAL = 1 };
+enum { PS3O_HOU_LI = 0, PS3O_TWO_THIRDS = 1 };
+enum { PS3O_IMPL_DIFF_RK4 = 0, PS3O_CN2 = 1 };
+
+typedef struct {
+    int nx, ny, nz;
+    int nnu;
+    double lower[3];
+    double extent[3];
+    double prediss;
+    int pretype;
+    int length_scale;
+    int filtering;
+    int stepper;
+    double cflmax;
+    double alpha;
+    double time_limit;
+    int roll_mean_win_size;
+    int nthreads;            /* OpenMP threads (0: runtime default) */
+    int hold_source;         /* test hook: keep svorts fixed inside step()
+                                (unit-tests/test_implicit_rk.f90) */
+    double f_cor[3];
+} ps3o_config;
+
+/* Per-step diagnostics (adapt, src/stepper/advance.f90:109-377, plus the
+ * energy/enstrophy/helicity series). */
+typedef struct {
+    double t, dt;
+    double ke, en, hel;
+    double vortmax, vortrms, vorch;
+    double vormean[3];
+    double ggmax, usggmax, lsggmax;
+    double umax, vmax, wmax;
+    double bfmax, rmv, pref;
+} ps3o_diag;
+
+typedef struct ps3o_model ps3o_model;
+
+int ps3o_create(const ps3o_config *cfg, ps3o_model **out);
+void ps3o_destroy(ps3o_model *m);
+
+/* transforms on whole fields (single-rank semantics of src/fft/sta3dfft.f90) */
+void ps3o_fftxyp2s(ps3o_model *m, const double *fp, double *fs);
+void ps3o_fftxys2p(ps3o_model *m, const double *fs, double *fp);
+void ps3o_diffx(ps3o_model *m, const double *fs, double *ds);
+void ps3o_diffy(ps3o_model *m, const double *fs, double *ds);
+void ps3o_fftsine(ps3o_model *m, double *fs);
+void ps3o_fftcosine(ps3o_model *m, double *fs);
+void ps3o_central_diffz(ps3o_model *m, const double *fs, double *ds);
+void ps3o_decompose_semi_spectral(ps3o_model *m, double *sf);
+void ps3o_combine_semi_spectral(ps3o_model *m, double *sf);
+void ps3o_decompose_physical(ps3o_model *m, const double *fc, double *sf);
+void ps3o_combine_physical(ps3o_model *m, const double *sf, double *fc);
+
+/* tables: which = 0 k2l2, 1 k2l2i (ny*nx); 2 filt, 3 green, 4 phim, 5 phip,
+ * 6 thetam, 7 thetap, 8 dthetam, 9 dthetap (N); 10 gamtop, 11 gambot (nz+1);
+ * 12 vhdis (ny*nx); 13 rkx (nx), 14 rky (ny), 15 rkz (nz+1) */
+int ps3o_get_table(ps3o_model *m, int which, double *out);
+
+/* state access: which = 0 svor, 1 vor, 2 vel, 3 svel, 4 svorts (3N each) */
+int ps3o_get_field(ps3o_model *m, int which, double *out);
+int ps3o_set_field(ps3o_model *m, int which, const double *in);
+void ps3o_get_ini_vor_mean(ps3o_model *m, double out[2]);
+void ps3o_set_ini_vor_mean(ps3o_model *m, const double in[2]);
+double ps3o_get_vvisc(ps3o_model *m);
+
+/* setup_fields (src/utils/utils.f90:136-184) from physical vorticity (3N) */
+void ps3o_setup_fields(ps3o_model *m, const double *vor_phys, double *te, double *en);
+void ps3o_init_diffusion(ps3o_model *m, double te, double en);
+
+void ps3o_vor2vel(ps3o_model *m);
+void ps3o_source(ps3o_model *m);
+void ps3o_adapt(ps3o_model *m, double t, double *dt, ps3o_diag *d);
+void ps3o_step(ps3o_model *m, double *t, double dt);
+/* set_diffusion of the configured stepper with prefactor pref */
+void ps3o_set_diffusion(ps3o_model *m, double dt, double pref);
+/* one advance() (src/stepper/advance.f90:77-104): vor2vel, adapt, source, step */
+void ps3o_advance(ps3o_model *m, double *t, ps3o_diag *d);
+
+/* diagnostics of the current physical fields */
+void ps3o_energy_series(ps3o_model *m, double *ke, double *en, double *hel);
+void ps3o_calc_vorticity_mean(ps3o_model *m, double out[2]);
+void ps3o_adjust_vorticity_mean(ps3o_model *m);
+/* rolling mean of gamma_max (src/utils/rolling_mean.f90) exposed for tests */
+double ps3o_rolling_mean_next(ps3o_model *m, double v);
+
+/* Rutishauser Jacobi eigenvalues of a symmetric 3x3 (src/utils/jacobi.f90);
+ * a is column-major 3x3 (only the upper triangle is read), eigs descending. */
+int ps3o_jacobi_eigenvalues(double a[9], double eigs[3]);
+
+#ifdef __cplusplus
+}
+#endif
+#endif
