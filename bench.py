@@ -1,0 +1,351 @@
+"""Benchmark of the ps3d hot path on GB300: Mpts*steps/s at 512^3.
+
+One "step" is one advance() of the reference (vor2vel, adapt, source and an
+impl-diff-rk4 step: four right-hand-side evaluations) on the 512^3 Beltrami
+plus seeded-perturbation workload (prediss 30, nnu 3, vorch prefactor,
+Kolmogorov viscosity, Hou & Li filter, CFL 0.5).  The headline value is the
+mixed-precision form (FP32 transforms, products and stage arithmetic; FP64
+prognostic vorticity, RK accumulators, low-mode inversion and reductions);
+the plain FP64 form is timed beside it and the mixed form's relative L2
+vorticity error against it is reported.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+
+With --impl reference the CPU restatement of the reference's algorithm
+(oracle/, FP64, OpenMP over all host cores) is timed instead, one advance at
+256^3 per step (a bounded sample of the same workload, reported per grid
+point in the same unit).  Under torchrun every rank runs an independent
+replica (the path does not shard across GPUs: replicas only, weak scaling).
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+
+def log(*a):
+    print(*a, file=sys.stderr, flush=True)
+
+
+# ---------------------------------------------------------------- ranks
+def dist_init(n_gpus):
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    if ws <= 1:
+        return 0, 1, None
+    import torch.distributed as dist
+    os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+    dist.init_process_group("gloo")
+    return dist.get_rank(), dist.get_world_size(), dist
+
+
+def barrier(dist):
+    if dist is not None:
+        dist.barrier()
+
+
+def max_over_ranks(dist, v):
+    if dist is None:
+        return v
+    import torch
+    t = torch.tensor([v], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+# --------------------------------------------------------------- clocks
+class ClockSampler:
+    """nvidia-smi sampler for the timed region (SM clock, throttle reasons)."""
+
+    Q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.Q}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 8:
+                continue
+            try:
+                sm.append(float(f[0]))
+                mx = float(f[1])
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[4:8]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": mx,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# ------------------------------------------------------------ workloads
+def make_ic(n, seed=1):
+    from ps3d_gb300 import ic
+    return ic.beltrami_plus_perturbation(n, n, n, seed=seed, amplitude=1.0e-3)
+
+
+def model_kw():
+    return dict(nnu=3, prediss=30.0, pretype="vorch", length_scale="Kolmogorov",
+                filtering="Hou & Li", stepper="impl-diff-rk4", cflmax=0.5, alpha=0.1)
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            p = json.load(f)
+        return float(p["hbm_gbs"]), "measured"
+    except (OSError, KeyError, ValueError):
+        return 6800.0, "fallback"
+
+
+def cpu_sample(n_cpu, steps=1):
+    """Time the CPU oracle: `steps` advances at n_cpu^3 after one warm-up."""
+    import oracle
+    from ps3d_gb300 import ic
+    vor, pert = make_ic(n_cpu)
+    o = oracle.Oracle(n_cpu, n_cpu, n_cpu, ic.BASELINE_BOX["lower"], ic.BASELINE_BOX["extent"], **model_kw())
+    o.setup_fields(vor, pert)
+    t = 0.0
+    t, _ = o.advance(t)
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        t, _ = o.advance(t)
+    sec = (time.perf_counter() - t0) / steps
+    return sec, n_cpu ** 3 / sec / 1e6
+
+
+def run_reference(args, rank, world, dist):
+    """--impl reference: the reference's algorithm on the host cores."""
+    if rank != 0:
+        return
+    import oracle
+    from ps3d_gb300 import ic
+    n = args.cpu_n
+    cores = os.cpu_count()
+    vor, pert = make_ic(n)
+    o = oracle.Oracle(n, n, n, ic.BASELINE_BOX["lower"], ic.BASELINE_BOX["extent"], nthreads=cores,
+                      **model_kw())
+    o.setup_fields(vor, pert)
+    t = 0.0
+    for _ in range(args.warmup):
+        t, _ = o.advance(t)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        t, _ = o.advance(t)
+    sec = time.perf_counter() - t0
+    value = n ** 3 * args.steps / sec / 1e6
+    sample = f"{args.steps} advance() steps of the FP64 oracle at {n}^3 (same workload, per-point rate)"
+    line = {
+        "impl": "reference", "metric": "Mpts*steps/s", "value": value, "unit": "Mpts*steps/s",
+        "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": 1e3 * sec / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": f"beltrami+perturbation {args.n}^3 impl-diff-rk4 (sampled at {n}^3 on CPU)",
+                   "grid": [args.n] * 3, "sample_grid": [n] * 3, "parallelism": "replicas"},
+        "cpu_baseline": {"value": value, "unit": "Mpts*steps/s", "cores": cores, "kind": "port",
+                         "sample": sample},
+        "e2e": {"value": value, "unit": "Mpts*steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_gpu(args, rank, world, dist):
+    from ps3d_gb300 import Ps3dGpu, ic
+    n = args.n
+    dev = int(os.environ.get("LOCAL_RANK", "0"))
+    pts = float(n) ** 3
+    lower, extent = ic.BASELINE_BOX["lower"], ic.BASELINE_BOX["extent"]
+    t_ic = time.perf_counter()
+    vor, pert = make_ic(n, seed=1 + rank)
+    log(f"[bench] rank {rank}: IC {n}^3 in {time.perf_counter() - t_ic:.1f}s")
+
+    # ---- mixed precision (headline) ----------------------------------
+    gm = Ps3dGpu(n, n, n, lower, extent, precision="mixed", device=dev, **model_kw())
+    gm.setup_fields(vor, pert)
+    t_m = 0.0
+    for _ in range(args.warmup):
+        t_m, _ = gm.advance(t_m)
+    gm.synchronize()
+    launches0 = gm.launch_count
+    barrier(dist)
+    with ClockSampler(dev) as clk:
+        t_m, ms = gm.time_advance(t_m, args.steps)
+    barrier(dist)
+    launches = gm.launch_count - launches0
+    sec = max_over_ranks(dist, ms / 1e3)
+    value = world * pts * args.steps / sec / 1e6
+    clocks = clk.summary()
+
+    # dominant kernel probe inside real steps (same stream, CUDA events)
+    probe_steps = max(1, min(3, args.steps))
+    best = None
+    for kind, name in ((1, "k_lines (y)"), (2, "k_lines (x)"), (3, "k_columns")):
+        gm.probe(kind)
+        t_m, _ = gm.time_advance(t_m, probe_steps)
+        kms, nl, kbytes = gm.probe_result()
+        gm.probe(0)
+        share = kms / (ms / args.steps * probe_steps) if ms > 0 else 0.0
+        rec = {"kernel": name, "launches_per_step": nl / probe_steps, "ms_per_launch": kms / max(nl, 1),
+               "bytes_per_launch": kbytes / max(nl, 1), "share_of_step": share}
+        if best is None or kms > best[1]:
+            best = (rec, kms)
+    peak, peak_kind = peaks()
+    krec = best[0]
+    achieved = krec["bytes_per_launch"] / (krec["ms_per_launch"] * 1e-3) / 1e9
+    roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                "frac": achieved / peak, "traffic": None, "kernel": krec["kernel"],
+                "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured" else peak_kind,
+                "kernel_share_of_step": krec["share_of_step"]}
+    svor_mixed_steps = args.warmup + args.steps + 3 * probe_steps
+
+    # ---- FP64 form: timing and reference for the mixed error ------------
+    fp64 = None
+    if not args.skip_fp64:
+        g64 = Ps3dGpu(n, n, n, lower, extent, precision="fp64", device=dev, **model_kw())
+        g64.setup_fields(vor, pert)
+        # same number of steps as the mixed run so the states are comparable
+        t64 = 0.0
+        n_fp64_timed = max(1, min(args.fp64_steps, svor_mixed_steps))
+        pre = svor_mixed_steps - n_fp64_timed
+        if pre > 0:
+            t64, _ = g64.advance_n(t64, pre)
+        t64, ms64 = g64.time_advance(t64, n_fp64_timed)
+        sec64 = max_over_ranks(dist, ms64 / 1e3)
+        a = gm.get("svor")
+        b = g64.get("svor")
+        err = float(np.linalg.norm(a - b) / np.linalg.norm(b))
+        v64 = world * pts * n_fp64_timed / sec64 / 1e6
+        fp64 = {"value": v64, "unit": "Mpts*steps/s", "ms_per_step": 1e3 * sec64 / n_fp64_timed,
+                "steps": n_fp64_timed, "mixed_speedup": value / v64,
+                "mixed_rel_l2_vs_fp64": err, "after_steps": svor_mixed_steps,
+                "t_mixed": t_m, "t_fp64": t64}
+        del a, b
+        g64.close()
+
+    # ---- end to end through the public API with host buffers ------------
+    e2e = None
+    if not args.skip_e2e:
+        host = pinned_like((3, n, n, n + 1))
+        host[...] = gm.get("svor")
+        nb = host.nbytes
+        e2e_steps = max(1, min(args.steps, 5))
+        t_e = t_m
+        t_e, _ = gm.advance_host(host, t_e)   # warm
+        barrier(dist)
+        t0 = time.perf_counter()
+        for _ in range(e2e_steps):
+            t_e, _ = gm.advance_host(host, t_e)
+        esec = max_over_ranks(dist, time.perf_counter() - t0)
+        e2e = {"value": world * pts * e2e_steps / esec / 1e6, "unit": "Mpts*steps/s",
+               "h2d_bytes_per_step": nb, "d2h_bytes_per_step": nb, "steps": e2e_steps,
+               "api": "ps3d_gpu_advance_host (svor FP64 in/out, host pinned)"}
+
+    cpu = None
+    if rank == 0 and not args.skip_cpu:
+        csec, crate = cpu_sample(args.cpu_n)
+        cpu = {"value": crate, "unit": "Mpts*steps/s", "cores": os.cpu_count(), "kind": "port",
+               "sample": f"1 advance() at {args.cpu_n}^3 (FP64 oracle, OpenMP), {csec:.2f} s"}
+
+    if rank == 0:
+        line = {
+            "metric": "Mpts*steps/s", "value": value, "unit": "Mpts*steps/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * sec / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32 transforms / f64 state (mixed)", "data": "synthetic",
+            "config": {"workload": f"beltrami+perturbation {n}^3 impl-diff-rk4 advance (mixed precision)",
+                       "grid": [n, n, n], "stepper": "impl-diff-rk4", "prediss": 30, "nnu": 3,
+                       "cfl": 0.5, "parallelism": "replicas" if world > 1 else "single",
+                       "l2": "inputs larger than L2 (each field >= 0.5 GB)"},
+            "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "fp64": fp64,
+            "gpu_launches": launches, "clocks": clocks,
+            "device_bytes": gm.device_bytes,
+        }
+        print(json.dumps(line), flush=True)
+    gm.close()
+
+
+def pinned_like(shape):
+    """Page-locked host array (cudaHostAlloc through libcudart)."""
+    import ctypes
+    nbytes = int(np.prod(shape)) * 8
+    for name in ("libcudart.so", "libcudart.so.13", "/usr/local/cuda/lib64/libcudart.so"):
+        try:
+            rt = ctypes.CDLL(name)
+            break
+        except OSError:
+            rt = None
+    if rt is None:
+        return np.empty(shape)
+    p = ctypes.c_void_p()
+    if rt.cudaHostAlloc(ctypes.byref(p), ctypes.c_size_t(nbytes), 0) != 0:
+        return np.empty(shape)
+    buf = (ctypes.c_double * (nbytes // 8)).from_address(p.value)
+    arr = np.frombuffer(buf, dtype=np.float64).reshape(shape)
+    return arr
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gpu", choices=["gpu", "reference"])
+    ap.add_argument("--n", type=int, default=512)
+    ap.add_argument("--cpu-n", type=int, default=256)
+    ap.add_argument("--fp64-steps", type=int, default=3)
+    ap.add_argument("--skip-fp64", action="store_true")
+    ap.add_argument("--skip-e2e", action="store_true")
+    ap.add_argument("--skip-cpu", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        log("[bench] warm-up raised to 3 steps")
+        args.warmup = 3
+    rank, world, dist = dist_init(args.gpus)
+    if args.impl == "reference":
+        run_reference(args, rank, world, dist)
+    else:
+        run_gpu(args, rank, world, dist)
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

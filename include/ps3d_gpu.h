@@ -1,0 +1,190 @@
+/*
+ * ps3d_gpu.h - C ABI of the GB300 (sm_103a) implementation of the ps3d
+ * per-step vorticity right-hand side and time steppers.
+ *
+ * The reference (matt-frey/ps3d) keeps this path in Fortran module procedures
+ * that act on module-global arrays.  This header is the drop-in boundary a
+ * Fortran `iso_c_binding` interface (or ctypes/cffi) binds: plain pointers,
+ * sizes and int status codes, no C++ or torch types.  Every routine below
+ * names the reference procedure it replaces.
+ *
+ * Host arrays use the reference layout (src/fields/fields.f90:59-79): a
+ * scalar field is (0:nz, 0:ny-1, 0:nx-1), column-major, z fastest, i.e. the
+ * element (iz, iy, ix) sits at iz + (nz+1)*(iy + ny*ix); a vector field is
+ * three scalar fields back to back.  Host arrays are only read or written
+ * during a call; no host pointer is retained.
+ *
+ * Threading: one context per host thread; calls on one context are not
+ * thread-safe.  Each context owns its device buffers and its CUDA stream.
+ * Errors: every entry point returns PS3D_OK (0) or a PS3D_ERR_* code; the
+ * library never aborts the process and never traps on the device.
+ */
+#ifndef PS3D_GPU_H
+#define PS3D_GPU_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ------------------------------------------------------ */
+#define PS3D_OK 0
+#define PS3D_ERR_INVALID_ARG 1      /* bad pointer, enum or size            */
+#define PS3D_ERR_UNSUPPORTED_SIZE 2 /* grid the kernels do not implement    */
+#define PS3D_ERR_CUDA 3             /* CUDA runtime error (see last_error)  */
+#define PS3D_ERR_OUT_OF_MEMORY 4    /* device allocation failed             */
+#define PS3D_ERR_NOT_READY 5        /* e.g. step before init_diffusion      */
+#define PS3D_ERR_NONFINITE 6        /* NaN/Inf detected in a diagnostic     */
+#define PS3D_ERR_DEVICE_LIMIT 7     /* a bounded device loop hit its limit  */
+#define PS3D_ERR_NO_DEVICE 8        /* no CUDA device / wrong architecture  */
+
+/* ---- enums (string options of the &PS3D namelist, options.f90) --------- */
+#define PS3D_PRE_CONSTANT 0              /* pretype 'constant'             */
+#define PS3D_PRE_VORCH 1                 /* 'vorch'                        */
+#define PS3D_PRE_BFMAX 2                 /* 'bfmax' (0: no buoyancy)       */
+#define PS3D_PRE_ROLL_MEAN_MAX_STRAIN 3  /* 'roll-mean-max-strain'         */
+#define PS3D_PRE_MAX_STRAIN 4            /* 'max-strain'                   */
+#define PS3D_PRE_US_MAX_STRAIN 5         /* 'us-max-strain'                */
+#define PS3D_KOLMOGOROV 0                /* length_scale                   */
+#define PS3D_GEOPHYSICAL 1
+#define PS3D_HOU_LI 0                    /* filtering 'Hou & Li'           */
+#define PS3D_TWO_THIRDS 1                /* filtering '2/3-rule'           */
+#define PS3D_IMPL_DIFF_RK4 0             /* stepper 'impl-diff-rk4'        */
+#define PS3D_CN2 1                       /* stepper 'cn2'                  */
+#define PS3D_PRECISION_FP64 0            /* every field and transform FP64 */
+#define PS3D_PRECISION_MIXED 1           /* FP32 transforms/products/stage
+                                            arithmetic; FP64 prognostic
+                                            vorticity, RK accumulators,
+                                            low-mode inversion, reductions */
+
+/* Run configuration: the hot-path subset of the &PS3D namelist
+ * (src/utils/options.f90:11-96) and the box (src/utils/parameters.f90).
+ * The first 17 members match the oracle's ps3o_config field for field. */
+typedef struct {
+    int nx, ny, nz;             /* cells; nx, ny, nz powers of two, 8..2048  */
+    int nnu;                    /* vor_visc%nnu                              */
+    double lower[3];            /* box lower corner                          */
+    double extent[3];           /* box extent                                */
+    double prediss;             /* vor_visc%prediss                          */
+    int pretype;                /* PS3D_PRE_*                                */
+    int length_scale;           /* PS3D_KOLMOGOROV | PS3D_GEOPHYSICAL        */
+    int filtering;              /* PS3D_HOU_LI | PS3D_TWO_THIRDS             */
+    int stepper;                /* PS3D_IMPL_DIFF_RK4 | PS3D_CN2             */
+    double cflmax;              /* reference constant 0.8 (constants.f90:47) */
+    double alpha;               /* time%alpha                                */
+    double time_limit;          /* time%limit                                */
+    int roll_mean_win_size;     /* vor_visc%roll_mean_win_size               */
+    int nthreads;               /* unused on the GPU (oracle compatibility)  */
+    int hold_source;            /* test hook: keep svorts fixed in step()    */
+    double f_cor[3];            /* planetary vorticity (physics.f90:61)      */
+    int precision;              /* PS3D_PRECISION_*                          */
+    int device;                 /* CUDA device ordinal                       */
+} ps3d_gpu_config;
+
+/* Diagnostics of one adapt() call (src/stepper/advance.f90:109-377) plus the
+ * kinetic energy, enstrophy (field_diagnostics.f90:85-206) and helicity
+ * <u.omega> (no reference counterpart; same z-trapezoid weights). */
+typedef struct {
+    double t, dt;
+    double ke, en, hel;
+    double vortmax, vortrms, vorch;
+    double vormean[3];
+    double ggmax, usggmax, lsggmax;
+    double umax, vmax, wmax;
+    double bfmax, rmv, pref;
+} ps3d_gpu_diag;
+
+typedef struct ps3d_gpu_ctx ps3d_gpu_ctx;
+
+/* ---- lifetime ----------------------------------------------------------
+ * create: init_inversion (inversion_utils.f90:222-372) + initialise_fft
+ * (sta3dfft.f90:53-110) + field_alloc (fields.f90:45-84). */
+int ps3d_gpu_create(const ps3d_gpu_config *cfg, ps3d_gpu_ctx **ctx);
+int ps3d_gpu_destroy(ps3d_gpu_ctx *ctx);
+const char *ps3d_gpu_strerror(int status);
+const char *ps3d_gpu_last_error(const ps3d_gpu_ctx *ctx);
+/* device bytes held by the context */
+long long ps3d_gpu_device_bytes(const ps3d_gpu_ctx *ctx);
+
+/* ---- state transfer ----------------------------------------------------
+ * which: 0 svor (mixed-spectral vorticity), 1 vor, 2 vel (physical),
+ * 3 svel (semi-spectral velocity), 4 svorts (vorticity source); 3 fields each
+ * (fields.f90:17-23).  Mixed precision converts at the boundary. */
+#define PS3D_FIELD_SVOR 0
+#define PS3D_FIELD_VOR 1
+#define PS3D_FIELD_VEL 2
+#define PS3D_FIELD_SVEL 3
+#define PS3D_FIELD_SVORTS 4
+int ps3d_gpu_set_field(ps3d_gpu_ctx *ctx, int which, const double *host);
+int ps3d_gpu_get_field(ps3d_gpu_ctx *ctx, int which, double *host);
+int ps3d_gpu_set_ini_vor_mean(ps3d_gpu_ctx *ctx, const double v[2]);
+int ps3d_gpu_get_ini_vor_mean(ps3d_gpu_ctx *ctx, double v[2]);
+/* tables, numbering as the oracle: 0 k2l2, 1 k2l2i, 2 filt, 3 green, 4 phim,
+ * 5 phip, 6 thetam, 7 thetap, 8 dthetam, 9 dthetap, 10 gamtop, 11 gambot,
+ * 12 vhdis, 13 rkx, 14 rky, 15 rkz (inversion_utils.f90:222-372). */
+int ps3d_gpu_get_table(ps3d_gpu_ctx *ctx, int which, double *host);
+
+/* ---- reference procedures ---------------------------------------------- */
+/* setup_fields (utils.f90:136-184): decompose the physical vorticity
+ * vor_phys (3 fields), add the optional mixed-spectral perturbation pert
+ * (3 fields, may be NULL), record ini_vor_mean, vor2vel, then te = kinetic
+ * energy, en = enstrophy and init_diffusion(te, en). */
+int ps3d_gpu_setup_fields(ps3d_gpu_ctx *ctx, const double *vor_phys,
+                          const double *pert, double *te, double *en);
+/* init_diffusion (inversion_utils.f90:124-153) */
+int ps3d_gpu_init_diffusion(ps3d_gpu_ctx *ctx, double te, double en);
+/* vor2vel (inversion.f90:23-226) */
+int ps3d_gpu_vor2vel(ps3d_gpu_ctx *ctx);
+/* source / vorticity_tendency (inversion.f90:298-388) */
+int ps3d_gpu_source(ps3d_gpu_ctx *ctx);
+/* adapt (advance.f90:109-377) incl. set_diffusion of the stepper */
+int ps3d_gpu_adapt(ps3d_gpu_ctx *ctx, double t, double *dt, ps3d_gpu_diag *diag);
+/* base_stepper%set_diffusion (impl_rk4.f90:37-53, cn2.f90:40-77) */
+int ps3d_gpu_set_diffusion(ps3d_gpu_ctx *ctx, double dt, double pref);
+/* base_stepper%step (impl_rk4.f90:76-207, cn2.f90:92-181) */
+int ps3d_gpu_step(ps3d_gpu_ctx *ctx, double *t, double dt);
+/* advance (advance.f90:77-104) repeated nsteps times; diag (nullable) gets
+ * nsteps records, one per step, taken by adapt at the start of the step. */
+int ps3d_gpu_advance(ps3d_gpu_ctx *ctx, double *t, int nsteps, ps3d_gpu_diag *diag);
+/* One advance for a caller that owns the state on the host (the Fortran
+ * driver's arrays): upload svor (3 fields), advance once, download svor. */
+int ps3d_gpu_advance_host(ps3d_gpu_ctx *ctx, double *svor, double *t, ps3d_gpu_diag *diag);
+/* calc_vorticity_mean / adjust_vorticity_mean (field_diagnostics.f90:584-619) */
+int ps3d_gpu_calc_vorticity_mean(ps3d_gpu_ctx *ctx, double out[2]);
+int ps3d_gpu_adjust_vorticity_mean(ps3d_gpu_ctx *ctx);
+/* get_kinetic_energy, get_enstrophy and helicity of the current vel/vor */
+int ps3d_gpu_energy_series(ps3d_gpu_ctx *ctx, double *ke, double *en, double *hel);
+
+/* ---- single-field operators (host in/out, one scalar field) ------------ */
+#define PS3D_OP_FFTXYP2S 0        /* sta3dfft.f90:136-194                   */
+#define PS3D_OP_FFTXYS2P 1        /* sta3dfft.f90:202-260                   */
+#define PS3D_OP_DIFFX 2           /* sta3dfft.f90:304-339 + reverse_x       */
+#define PS3D_OP_DIFFY 3           /* sta3dfft.f90:345-377 + reverse_y       */
+#define PS3D_OP_FFTSINE 4         /* sta3dfft.f90:264-277                   */
+#define PS3D_OP_FFTCOSINE 5       /* sta3dfft.f90:282-298                   */
+#define PS3D_OP_CENTRAL_DIFFZ 6   /* inversion_utils.f90:653-673            */
+#define PS3D_OP_DECOMPOSE_SEMI 7  /* inversion_utils.f90:563-595            */
+#define PS3D_OP_COMBINE_SEMI 8    /* inversion_utils.f90:617-647            */
+#define PS3D_OP_DECOMPOSE_PHYS 9  /* inversion_utils.f90:549-557            */
+#define PS3D_OP_COMBINE_PHYS 10   /* inversion_utils.f90:599-611            */
+int ps3d_gpu_field_op(ps3d_gpu_ctx *ctx, int op, const double *in, double *out);
+
+/* ---- benchmark helpers ------------------------------------------------- */
+/* Time nsteps advance() calls on the context stream with CUDA events (the
+ * state stays resident); *ms is the elapsed device time. */
+int ps3d_gpu_time_advance(ps3d_gpu_ctx *ctx, double *t, int nsteps, double *ms);
+/* Kernel launches issued by this context since creation. */
+long long ps3d_gpu_launch_count(const ps3d_gpu_ctx *ctx);
+int ps3d_gpu_synchronize(ps3d_gpu_ctx *ctx);
+/* Kernel probe: bracket every launch of one kernel class with CUDA events on
+ * the context stream.  kind: 0 off, 1 y-line transforms, 2 x-line
+ * transforms, 3 column (z) transforms.  probe resets the counters;
+ * probe_result returns the summed device time, the number of bracketed
+ * launches and their algorithmic bytes (one read and one write of
+ * nx*ny*(nz+1) elements per launch). */
+int ps3d_gpu_probe(ps3d_gpu_ctx *ctx, int kind);
+int ps3d_gpu_probe_result(ps3d_gpu_ctx *ctx, double *total_ms, long long *launches, double *bytes);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

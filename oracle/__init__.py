@@ -81,7 +81,7 @@ def lib():
         L.ps3o_set_ini_vor_mean.argtypes = [vp, _dp]
         L.ps3o_get_vvisc.argtypes = [vp]
         L.ps3o_get_vvisc.restype = ctypes.c_double
-        L.ps3o_setup_fields.argtypes = [vp, _dp, _dp, _dp]
+        L.ps3o_setup_fields.argtypes = [vp, _dp, _dp, _dp, _dp]
         L.ps3o_init_diffusion.argtypes = [vp, ctypes.c_double, ctypes.c_double]
         L.ps3o_vor2vel.argtypes = [vp]
         L.ps3o_source.argtypes = [vp]
@@ -269,11 +269,16 @@ class Oracle:
     def vvisc(self):
         return lib().ps3o_get_vvisc(self._h)
 
-    def setup_fields(self, vor_phys):
+    def setup_fields(self, vor_phys, pert=None):
         vor_phys = np.ascontiguousarray(vor_phys, dtype=np.float64)
         assert vor_phys.shape == (3,) + self.shape
+        pp = None
+        if pert is not None:
+            pert = np.ascontiguousarray(pert, dtype=np.float64)
+            assert pert.shape == (3,) + self.shape
+            pp = _ptr(pert)
         te, en = ctypes.c_double(), ctypes.c_double()
-        lib().ps3o_setup_fields(self._h, _ptr(vor_phys), ctypes.byref(te), ctypes.byref(en))
+        lib().ps3o_setup_fields(self._h, _ptr(vor_phys), pp, ctypes.byref(te), ctypes.byref(en))
         return te.value, en.value
 
     def init_diffusion(self, te, en):

@@ -826,7 +826,8 @@ void ps3o_init_diffusion(ps3o_model *m, double te, double en)
 }
 
 /* setup_fields (utils.f90:136-184), without the NetCDF read */
-void ps3o_setup_fields(ps3o_model *m, const double *vor_phys, double *te_out, double *en_out)
+void ps3o_setup_fields(ps3o_model *m, const double *vor_phys, const double *pert, double *te_out,
+                       double *en_out)
 {
     const size_t N = m->nfield;
     memset(m->svor, 0, sizeof(double) * 3 * N);
@@ -836,6 +837,8 @@ void ps3o_setup_fields(ps3o_model *m, const double *vor_phys, double *te_out, do
     memset(m->vortsm, 0, sizeof(double) * 3 * N);
     memcpy(m->vor, vor_phys, sizeof(double) * 3 * N);
     for (int nc = 0; nc < 3; ++nc) ps3o_decompose_physical(m, m->vor + nc * N, m->svor + nc * N);
+    if (pert)
+        for (size_t i = 0; i < 3 * N; ++i) m->svor[i] += pert[i];
     ps3o_calc_vorticity_mean(m, m->ini_vor_mean);
     ps3o_vor2vel(m);
     double ke, en, hel;

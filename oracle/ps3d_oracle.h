@@ -108,8 +108,10 @@ void ps3o_get_ini_vor_mean(ps3o_model *m, double out[2]);
 void ps3o_set_ini_vor_mean(ps3o_model *m, const double in[2]);
 double ps3o_get_vvisc(ps3o_model *m);
 
-/* setup_fields (src/utils/utils.f90:136-184) from physical vorticity (3N) */
-void ps3o_setup_fields(ps3o_model *m, const double *vor_phys, double *te, double *en);
+/* setup_fields (src/utils/utils.f90:136-184) from physical vorticity (3N);
+ * pert (3N mixed-spectral, may be NULL) is added after the decomposition */
+void ps3o_setup_fields(ps3o_model *m, const double *vor_phys, const double *pert, double *te,
+                       double *en);
 void ps3o_init_diffusion(ps3o_model *m, double te, double en);
 
 void ps3o_vor2vel(ps3o_model *m);

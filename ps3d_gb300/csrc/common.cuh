@@ -1,0 +1,156 @@
+// Shared device helpers for the ps3d GB300 kernels: complex arithmetic,
+// radix-2/4/8 butterflies and the shared-memory Stockham FFT used by every
+// transform kernel.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace ps3d {
+
+template <typename T> struct cplx;
+template <> struct cplx<double> { using type = double2; };
+template <> struct cplx<float> { using type = float2; };
+
+template <typename C> __device__ __forceinline__ C mk(decltype(C::x) x, decltype(C::x) y)
+{
+    C c;
+    c.x = x;
+    c.y = y;
+    return c;
+}
+template <typename C> __device__ __forceinline__ C cadd(C a, C b) { return mk<C>(a.x + b.x, a.y + b.y); }
+template <typename C> __device__ __forceinline__ C csub(C a, C b) { return mk<C>(a.x - b.x, a.y - b.y); }
+template <typename C> __device__ __forceinline__ C cmul(C a, C b)
+{
+    return mk<C>(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+}
+// multiply by -i (forward) or +i (inverse)
+template <bool INV, typename C> __device__ __forceinline__ C mul_mi(C a)
+{
+    return INV ? mk<C>(-a.y, a.x) : mk<C>(a.y, -a.x);
+}
+
+// In-register DFTs with the sign of the forward (e^{-2 pi i/R}) or inverse
+// transform.
+template <bool INV, typename C> __device__ __forceinline__ void dft2(C &a, C &b)
+{
+    C t = a;
+    a = cadd(t, b);
+    b = csub(t, b);
+}
+
+template <bool INV, typename C> __device__ __forceinline__ void dft4(C &a0, C &a1, C &a2, C &a3)
+{
+    C t0 = cadd(a0, a2), t1 = csub(a0, a2);
+    C t2 = cadd(a1, a3), t3 = mul_mi<INV>(csub(a1, a3));
+    a0 = cadd(t0, t2);
+    a2 = csub(t0, t2);
+    a1 = cadd(t1, t3);
+    a3 = csub(t1, t3);
+}
+
+template <bool INV, typename C> __device__ __forceinline__ void dft8(C *v)
+{
+    using R = decltype(C::x);
+    const R h = (R)0.70710678118654752440084436210484903928483593768847;
+    // even / odd halves
+    dft4<INV>(v[0], v[2], v[4], v[6]);
+    dft4<INV>(v[1], v[3], v[5], v[7]);
+    // twiddle the odd half by w8^k, k = 0..3
+    C o1 = v[3], o2 = v[5], o3 = v[7];
+    if (!INV) {
+        o1 = mk<C>((o1.x + o1.y) * h, (o1.y - o1.x) * h);   // (1-i)/sqrt2
+        o2 = mk<C>(o2.y, -o2.x);                            // -i
+        o3 = mk<C>((o3.y - o3.x) * h, -(o3.x + o3.y) * h);  // (-1-i)/sqrt2
+    } else {
+        o1 = mk<C>((o1.x - o1.y) * h, (o1.x + o1.y) * h);   // (1+i)/sqrt2
+        o2 = mk<C>(-o2.y, o2.x);                            // +i
+        o3 = mk<C>(-(o3.x + o3.y) * h, (o3.x - o3.y) * h);  // (-1+i)/sqrt2
+    }
+    C e0 = v[0], e1 = v[2], e2 = v[4], e3 = v[6], o0 = v[1];
+    v[0] = cadd(e0, o0);
+    v[4] = csub(e0, o0);
+    v[1] = cadd(e1, o1);
+    v[5] = csub(e1, o1);
+    v[2] = cadd(e2, o2);
+    v[6] = csub(e2, o2);
+    v[3] = cadd(e3, o3);
+    v[7] = csub(e3, o3);
+}
+
+template <int R, bool INV, typename C> __device__ __forceinline__ void dft(C *v)
+{
+    if (R == 2) dft2<INV>(v[0], v[1]);
+    else if (R == 4) dft4<INV>(v[0], v[1], v[2], v[3]);
+    else dft8<INV>(v);
+}
+
+// One Stockham autosort pass of radix R over B interleaved sequences of
+// length n held in shared memory as buf[j*B + b].  Ns is the product of the
+// radices already applied.  tw[k] = exp(-2 pi i k / n).
+template <int R, bool INV, typename C>
+__device__ __forceinline__ void stockham_pass(const C *__restrict__ src, C *__restrict__ dst, int n,
+                                              int logB, int Ns, const C *__restrict__ tw)
+{
+    const int B = 1 << logB;
+    const int nR = n / R;
+    const int nbf = nR << logB;
+    const int twstride = n / (Ns * R);
+    for (int g = threadIdx.x; g < nbf; g += blockDim.x) {
+        const int b = g & (B - 1);
+        const int j = g >> logB;
+        const int k = j & (Ns - 1);
+        C v[R];
+#pragma unroll
+        for (int r = 0; r < R; ++r) v[r] = src[((j + r * nR) << logB) + b];
+        if (Ns > 1) {
+#pragma unroll
+            for (int r = 1; r < R; ++r) {
+                C w = tw[k * r * twstride];
+                if (INV) w.y = -w.y;
+                v[r] = cmul(v[r], w);
+            }
+        }
+        dft<R, INV>(v);
+        const int idxD = (j - k) * R + k;
+#pragma unroll
+        for (int r = 0; r < R; ++r) dst[((idxD + r * Ns) << logB) + b] = v[r];
+    }
+}
+
+// Complex FFT of B = 2^logB interleaved sequences of length n (a power of two,
+// 2..4096) in shared memory; buf0 holds the input, the result ends in the
+// returned buffer (buf0 or buf1).  All threads of the block take part; the
+// caller synchronises before the call.
+template <bool INV, typename C>
+__device__ C *smem_fft(C *buf0, C *buf1, int n, int logB, const C *__restrict__ tw)
+{
+    C *s = buf0, *d = buf1;
+    int Ns = 1, rem = n;
+    while (rem >= 8) {
+        stockham_pass<8, INV>(s, d, n, logB, Ns, tw);
+        __syncthreads();
+        C *t = s; s = d; d = t;
+        Ns *= 8;
+        rem /= 8;
+    }
+    if (rem == 4) {
+        stockham_pass<4, INV>(s, d, n, logB, Ns, tw);
+        __syncthreads();
+        C *t = s; s = d; d = t;
+    } else if (rem == 2) {
+        stockham_pass<2, INV>(s, d, n, logB, Ns, tw);
+        __syncthreads();
+        C *t = s; s = d; d = t;
+    }
+    return s;
+}
+
+__host__ __device__ inline int ilog2(int v)
+{
+    int r = 0;
+    while ((1 << r) < v) ++r;
+    return r;
+}
+
+}  // namespace ps3d

@@ -1,0 +1,155 @@
+// Internal launcher declarations shared by the translation units of
+// libps3d_gpu.so (not part of the public C ABI).
+#pragma once
+#include <cuda_runtime.h>
+
+#include "common.cuh"
+
+namespace ps3d {
+
+struct Dims {
+    int nx, ny, nz;
+    int P;                // padded column pitch (>= nz+1, multiple of 8)
+    long long ncol;       // nx*ny
+    long long nfield;     // P*ny*nx elements per scalar field
+};
+
+enum { COL_DST = 0, COL_DCT = 1, COL_DECOMP = 2, COL_COMBINE = 3 };
+
+// Optional timing probe: brackets every launch of one kernel class with CUDA
+// events on the launching stream (used by the benchmark to time the dominant
+// kernel inside a real step).  kind: 0 off, 1 y lines, 2 x lines, 3 columns.
+enum { PROBE_OFF = 0, PROBE_YLINES = 1, PROBE_XLINES = 2, PROBE_COLUMNS = 3 };
+struct Probe {
+    static constexpr int MAXP = 8192;
+    int kind = PROBE_OFF;
+    cudaEvent_t *ev = nullptr;  // 2*MAXP events
+    int used = 0;
+    long long launches = 0;
+    double bytes = 0.0;         // algorithmic bytes of the bracketed launches
+    void begin(int k, cudaStream_t st)
+    {
+        if (k == kind && ev && used + 2 <= 2 * MAXP) cudaEventRecord(ev[used++], st);
+    }
+    void end(int k, cudaStream_t st, double b)
+    {
+        if (k == kind && ev && (used & 1)) {
+            cudaEventRecord(ev[used++], st);
+            ++launches;
+            bytes += b;
+        }
+    }
+};
+
+// transforms.cu
+void transforms_init();
+template <typename T>
+void xy_forward(const Dims &d, cudaStream_t st, const T *in, T *out, const typename cplx<T>::type *twx,
+                const typename cplx<T>::type *twy, Probe *pr);
+template <typename T>
+void xy_inverse(const Dims &d, cudaStream_t st, const T *in, T *out, const typename cplx<T>::type *twx,
+                const typename cplx<T>::type *twy, Probe *pr);
+template <typename T>
+void columns(const Dims &d, cudaStream_t st, int mode, const T *in, T *out, const T *phim,
+             const T *phip, const typename cplx<T>::type *twz2, Probe *pr);
+
+// Spectral-horizontal derivative operators.  For a spectral index k along
+// x (or y) the reference's diffx/diffy (sta3dfft.f90:304-377, with the
+// single-rank reverse_x/y of mpi_reverse.f90) reduce to
+//    (D f)(k) = c[k] * f(src[k]),   src[k] = (n - k) mod n,
+// with c[k] = -hrk(2k) for 1 <= k < n/2, +hrk(2(n-k)) for k > n/2 and
+// c[0] = c[n/2] = 0.
+struct Deriv {
+    const double *cx;  // nx
+    const double *cy;  // ny
+};
+
+struct Tables {
+    // per (ky,kx) column (ny*nx, FP64)
+    const double *k2l2i, *filt0, *vhdis, *epq, *emq, *epq2, *emq2, *vdiss;
+    // per kz (nz+1, FP64)
+    const double *fz;       // vertical Hou-Li / 2/3 factor, fz[0] = fz[nz] = 1
+    const double *rkz, *rkzi, *gamtop, *gambot, *dstsum, *dctcos;
+};
+
+// ops.cu : elementwise / stencil kernels (T = transient field type, S = state)
+template <typename T> void op_diff(const Dims &d, cudaStream_t st, const Deriv &D, int axis, const T *in, T *out);
+template <typename T> void op_diffz(const Dims &d, cudaStream_t st, double dzi, const T *in, T *out);
+template <typename T, typename S>
+void op_v2v_ds(const Dims &d, cudaStream_t st, const Deriv &D, const S *A, const S *B, T *ds);
+template <typename T, typename S>
+void op_v2v_project(const Dims &d, cudaStream_t st, const Deriv &D, const double *k2l2i, const T *es,
+                    const T *ds, S *A, S *B);
+template <typename T, typename S>
+void op_v2v_wsrc(const Dims &d, cudaStream_t st, const Deriv &D, const S *A, const S *B, T *ds);
+template <typename T>
+void op_v2v_wprep(const Dims &d, cudaStream_t st, const T *ds, const T *thetam, const T *thetap,
+                  const T *dthetam, const T *dthetap, const T *green, const double *rkz, T *bs, T *es,
+                  T *dsg, T *as);
+template <typename T>
+void op_v2v_wfinish(const Dims &d, cudaStream_t st, const T *dsg, const T *bs, const T *as, T *w, T *es);
+template <typename S>
+void op_v2v_meanflow(const Dims &d, cudaStream_t st, const S *A, const S *B, const Tables &tb, double *ubar,
+                     double *vbar);
+template <typename T>
+void op_v2v_uv(const Dims &d, cudaStream_t st, const Deriv &D, const double *k2l2i, const T *es, const T *cs,
+               const double *ubar, const double *vbar, T *u, T *v);
+template <typename T>
+void op_add_const(const Dims &d, cudaStream_t st, T *f, double c);
+template <typename T>
+void op_products(const Dims &d, cudaStream_t st, const T *vel, const T *vor, T *r, T *q, T *p);
+template <typename T>
+void op_svorts(const Dims &d, cudaStream_t st, const Deriv &D, const T *r, const T *q, const T *p,
+               const T *gq, const T *gp, T *s1, T *s2, T *s3);
+template <typename T>
+void op_strain_fields(const Dims &d, cudaStream_t st, const Deriv &D, const T *svel, T *g5);
+template <typename T, typename S>
+void op_convert(const Dims &d, cudaStream_t st, const S *in, T *out, long long n);
+template <typename T, typename S>
+void op_add(const Dims &d, cudaStream_t st, S *acc, const T *add, long long n);
+
+// steppers
+template <typename T>
+void op_rk4_sub1(const Dims &d, cudaStream_t st, double *q, double *qdi, double *qdf, T *sqs,
+                 const double *filt0, const double *emq, double dt2, double dt6);
+template <typename T>
+void op_rk4_sub23(const Dims &d, cudaStream_t st, double *q, const double *qdi, double *qdf, const T *sqs,
+                  const double *epq, const double *emq, double c1, double dt3);
+template <typename T>
+void op_rk4_sub4(const Dims &d, cudaStream_t st, double *q, const double *qdf, const T *sqs,
+                 const double *epq, const double *emq, double dt6);
+void op_rk4_factors(const Dims &d, cudaStream_t st, const double *vdiss, const double *filt0, double *epq,
+                    double *emq, double *epq2, double *emq2);
+template <typename T>
+void op_cn2_init(const Dims &d, cudaStream_t st, double *vortsm, const double *svor, const T *svorts,
+                 double dt2);
+template <typename T>
+void op_cn2_update(const Dims &d, cudaStream_t st, double *svor, const double *vortsm, const T *svorts,
+                   const double *filt0, const double *fz, const double *vdiss, double dt2);
+void op_mean_fix(const Dims &d, cudaStream_t st, double *svor, const double *dstsum, double fnzi,
+                 const double *ini, double *savg_out, int apply);
+
+// reductions (adapt, energy series); results are FP64 partials per block
+struct RedOut {
+    double *part;     // scratch partials
+    double *result;   // final values
+};
+template <typename T>
+void red_pass1(const Dims &d, cudaStream_t st, const T *vel, const T *vor, double *part, double *result);
+template <typename T>
+void red_pass2(const Dims &d, cudaStream_t st, const T *vor, const T *g5, double vortrms, double *part,
+               double *result, int *flag);
+int red_nblocks(const Dims &d);
+constexpr int RED1_N = 12;  // values of pass 1
+constexpr int RED2_N = 5;   // values of pass 2
+
+// tables
+template <typename T>
+void op_hyperbolic_tables(const Dims &d, cudaStream_t st, const double *k2l2, const double *k2l2i,
+                          const double *rkz, const double *zm, const double *zp, double Lz, T *phim, T *phip,
+                          T *thetam, T *thetap, T *dthetam, T *dthetap, T *green);
+
+size_t lines_smem_bytes(int n, bool fp64);
+size_t columns_smem_bytes(int nz, bool fp64);
+
+}  // namespace ps3d

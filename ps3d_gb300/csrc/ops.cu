@@ -1,0 +1,864 @@
+// Elementwise, stencil, stepper and reduction kernels of the ps3d hot path.
+//
+// All kernels walk columns: a block is 32 x 8 threads, threadIdx.x runs along
+// z (coalesced: 32 consecutive z of one column per warp), threadIdx.y picks
+// one of 8 columns.  Spectral x/y derivatives read the partner column
+// src(k) = (n - k) mod n, which is itself a contiguous z run.  Arithmetic is
+// done in FP64 registers whatever the storage type, so the mixed-precision
+// form only rounds at loads and stores.
+#include <float.h>
+
+#include "kernels.h"
+
+namespace ps3d {
+
+#define COLS_PER_BLOCK 8
+
+__device__ __forceinline__ int xsrc(int kx, int nx) { return kx == 0 ? 0 : nx - kx; }
+
+#define COLUMN_HEADER                                                          \
+    const long long col = (long long)blockIdx.x * COLS_PER_BLOCK + threadIdx.y; \
+    if (col >= d.ncol) return;                                                 \
+    const int kx = (int)(col / d.ny);                                          \
+    const int ky = (int)(col - (long long)kx * d.ny);                          \
+    const long long o = col * d.P;                                             \
+    (void)kx; (void)ky;
+
+#define PARTNERS                                                               \
+    const long long ox = ((long long)ky + (long long)d.ny * xsrc(kx, d.nx)) * d.P; \
+    const long long oy = ((long long)xsrc(ky, d.ny) + (long long)d.ny * kx) * d.P; \
+    const double cxk = D.cx[kx], cyk = D.cy[ky];
+
+static inline dim3 col_grid(const Dims &d)
+{
+    return dim3((unsigned)((d.ncol + COLS_PER_BLOCK - 1) / COLS_PER_BLOCK));
+}
+static const dim3 COL_BLOCK(32, COLS_PER_BLOCK);
+
+// ---------------------------------------------------------------- diff x/y
+template <typename T>
+__global__ void k_diff(Dims d, Deriv D, int axis, const T *__restrict__ in, T *__restrict__ out)
+{
+    COLUMN_HEADER
+    PARTNERS
+    const long long os = axis == 0 ? ox : oy;
+    const double c = axis == 0 ? cxk : cyk;
+    for (int iz = threadIdx.x; iz <= d.nz; iz += 32) out[o + iz] = (T)(c * (double)in[os + iz]);
+}
+template <typename T> void op_diff(const Dims &d, cudaStream_t st, const Deriv &D, int axis, const T *in, T *out)
+{
+    k_diff<T><<<col_grid(d), COL_BLOCK, 0, st>>>(d, D, axis, in, out);
+}
+
+// ------------------------------------------------------------ central diffz
+template <typename T>
+__global__ void k_diffz(Dims d, double dzi, const T *__restrict__ in, T *__restrict__ out)
+{
+    COLUMN_HEADER
+    const int nz = d.nz;
+    const double hdzi = 0.5 * dzi;
+    for (int iz = threadIdx.x; iz <= nz; iz += 32) {
+        double v;
+        if (iz == 0) v = dzi * ((double)in[o + 1] - (double)in[o]);
+        else if (iz == nz) v = dzi * ((double)in[o + nz] - (double)in[o + nz - 1]);
+        else v = ((double)in[o + iz + 1] - (double)in[o + iz - 1]) * hdzi;
+        out[o + iz] = (T)v;
+    }
+}
+template <typename T> void op_diffz(const Dims &d, cudaStream_t st, double dzi, const T *in, T *out)
+{
+    k_diffz<T><<<col_grid(d), COL_BLOCK, 0, st>>>(d, dzi, in, out);
+}
+
+// ------------------------------------------------------------------ vor2vel
+// ds = D_x B - D_y A   (inversion.f90:39-42 and :86-90 with A, B swapped roles)
+template <typename T, typename S>
+__global__ void k_v2v_ds(Dims d, Deriv D, const S *__restrict__ A, const S *__restrict__ B, T *__restrict__ ds)
+{
+    COLUMN_HEADER
+    PARTNERS
+    for (int iz = threadIdx.x; iz <= d.nz; iz += 32)
+        ds[o + iz] = (T)(cxk * (double)B[ox + iz] - cyk * (double)A[oy + iz]);
+}
+template <typename T, typename S>
+void op_v2v_ds(const Dims &d, cudaStream_t st, const Deriv &D, const S *A, const S *B, T *ds)
+{
+    k_v2v_ds<T, S><<<col_grid(d), COL_BLOCK, 0, st>>>(d, D, A, B, ds);
+}
+
+// ds = D_y A - D_x B   (inversion.f90:86-90)
+template <typename T, typename S>
+__global__ void k_v2v_wsrc(Dims d, Deriv D, const S *__restrict__ A, const S *__restrict__ B, T *__restrict__ ds)
+{
+    COLUMN_HEADER
+    PARTNERS
+    for (int iz = threadIdx.x; iz <= d.nz; iz += 32)
+        ds[o + iz] = (T)(cyk * (double)A[oy + iz] - cxk * (double)B[ox + iz]);
+}
+template <typename T, typename S>
+void op_v2v_wsrc(const Dims &d, cudaStream_t st, const Deriv &D, const S *A, const S *B, T *ds)
+{
+    k_v2v_wsrc<T, S><<<col_grid(d), COL_BLOCK, 0, st>>>(d, D, A, B, ds);
+}
+
+// A = k2l2i (D_x es + D_y ds), B = k2l2i (D_y es - D_x ds); the (0,0) column
+// keeps its mean vorticity (inversion.f90:50-76)
+template <typename T, typename S>
+__global__ void k_v2v_project(Dims d, Deriv D, const double *__restrict__ k2l2i, const T *__restrict__ es,
+                              const T *__restrict__ ds, S *__restrict__ A, S *__restrict__ B)
+{
+    COLUMN_HEADER
+    if (col == 0) return;
+    PARTNERS
+    const double kk = k2l2i[col];
+    for (int iz = threadIdx.x; iz <= d.nz; iz += 32) {
+        const double a = kk * (cxk * (double)es[ox + iz] + cyk * (double)ds[oy + iz]);
+        const double b = kk * (cyk * (double)es[oy + iz] - cxk * (double)ds[ox + iz]);
+        A[o + iz] = (S)a;
+        B[o + iz] = (S)b;
+    }
+}
+template <typename T, typename S>
+void op_v2v_project(const Dims &d, cudaStream_t st, const Deriv &D, const double *k2l2i, const T *es,
+                    const T *ds, S *A, S *B)
+{
+    k_v2v_project<T, S><<<col_grid(d), COL_BLOCK, 0, st>>>(d, D, k2l2i, es, ds, A, B);
+}
+
+// boundary contributions and Green-function inversion for w
+// (inversion.f90:94-122)
+template <typename T>
+__global__ void k_v2v_wprep(Dims d, const T *__restrict__ ds, const T *__restrict__ thetam,
+                            const T *__restrict__ thetap, const T *__restrict__ dthetam,
+                            const T *__restrict__ dthetap, const T *__restrict__ green,
+                            const double *__restrict__ rkz, T *__restrict__ bs, T *__restrict__ es,
+                            T *__restrict__ dsg, T *__restrict__ as)
+{
+    COLUMN_HEADER
+    const int nz = d.nz;
+    const double d0 = ds[o], dn = ds[o + nz];
+    for (int iz = threadIdx.x; iz <= nz; iz += 32) {
+        const long long q = o + iz;
+        es[q] = (T)(d0 * (double)dthetam[q] + dn * (double)dthetap[q]);
+        if (iz > 0 && iz < nz) {
+            bs[q] = (T)(d0 * (double)thetam[q] + dn * (double)thetap[q]);
+            const double g = (double)green[q] * (double)ds[q];
+            dsg[q] = (T)g;
+            as[q] = (T)(rkz[iz] * (double)(T)g);
+        } else {
+            bs[q] = (T)0;
+            dsg[q] = (T)0;
+            as[q] = (T)0;
+        }
+    }
+}
+template <typename T>
+void op_v2v_wprep(const Dims &d, cudaStream_t st, const T *ds, const T *thetam, const T *thetap,
+                  const T *dthetam, const T *dthetap, const T *green, const double *rkz, T *bs, T *es,
+                  T *dsg, T *as)
+{
+    k_v2v_wprep<T><<<col_grid(d), COL_BLOCK, 0, st>>>(d, ds, thetam, thetap, dthetam, dthetap, green, rkz, bs,
+                                                      es, dsg, as);
+}
+
+// w = [0, dst(green ds) + bs, 0], dw/dz = es + dct(rkz green ds)
+// (inversion.f90:136-139)
+template <typename T>
+__global__ void k_v2v_wfinish(Dims d, const T *__restrict__ dsg, const T *__restrict__ bs,
+                              const T *__restrict__ as, T *__restrict__ w, T *__restrict__ es)
+{
+    COLUMN_HEADER
+    const int nz = d.nz;
+    for (int iz = threadIdx.x; iz <= nz; iz += 32) {
+        const long long q = o + iz;
+        w[q] = (iz > 0 && iz < nz) ? (T)((double)dsg[q] + (double)bs[q]) : (T)0;
+        es[q] = (T)((double)es[q] + (double)as[q]);
+    }
+}
+template <typename T>
+void op_v2v_wfinish(const Dims &d, cudaStream_t st, const T *dsg, const T *bs, const T *as, T *w, T *es)
+{
+    k_v2v_wfinish<T><<<col_grid(d), COL_BLOCK, 0, st>>>(d, dsg, bs, as, w, es);
+}
+
+// horizontally averaged flow from the (0,0) column (inversion.f90:150-165):
+// ubar = dct(-rkzi B) + B(nz) gamtop - B(0) gambot, vbar likewise.  One block;
+// the cosine transform of a single column is a direct O(nz^2) sum.
+template <typename S>
+__global__ void k_v2v_meanflow(int nz, const S *__restrict__ A, const S *__restrict__ B,
+                               const double *__restrict__ rkzi, const double *__restrict__ dctcos,
+                               const double *__restrict__ gamtop, const double *__restrict__ gambot,
+                               double *__restrict__ ubar, double *__restrict__ vbar)
+{
+    extern __shared__ double sh[];
+    double *xu = sh, *xv = sh + (nz + 1);
+    for (int iz = threadIdx.x; iz <= nz; iz += blockDim.x) {
+        const bool in = iz > 0 && iz < nz;
+        xu[iz] = in ? -rkzi[iz] * (double)B[iz] : 0.0;
+        xv[iz] = in ? rkzi[iz] * (double)A[iz] : 0.0;
+    }
+    __syncthreads();
+    const double s = sqrt(2.0 / (double)nz);
+    const double a0 = (double)A[0], an = (double)A[nz], b0 = (double)B[0], bn = (double)B[nz];
+    for (int k = threadIdx.x; k <= nz; k += blockDim.x) {
+        double su = 0.0, sv = 0.0;
+        for (int j = 1; j < nz; ++j) {
+            const double c = dctcos[(int)(((long long)j * k) % (2 * nz))];
+            su += xu[j] * c;
+            sv += xv[j] * c;
+        }
+        ubar[k] = s * su + bn * gamtop[k] - b0 * gambot[k];
+        vbar[k] = s * sv - an * gamtop[k] + a0 * gambot[k];
+    }
+}
+template <typename S>
+void op_v2v_meanflow(const Dims &d, cudaStream_t st, const S *A, const S *B, const Tables &tb, double *ubar,
+                     double *vbar)
+{
+    k_v2v_meanflow<S><<<1, 256, 2 * (d.nz + 1) * sizeof(double), st>>>(d.nz, A, B, tb.rkzi, tb.dctcos,
+                                                                         tb.gamtop, tb.gambot, ubar, vbar);
+}
+
+// u = k2l2i (D_x es + D_y cs), v = k2l2i (D_y es - D_x cs), (0,0) = ubar, vbar
+// (inversion.f90:169-213)
+template <typename T>
+__global__ void k_v2v_uv(Dims d, Deriv D, const double *__restrict__ k2l2i, const T *__restrict__ es,
+                         const T *__restrict__ cs, const double *__restrict__ ubar,
+                         const double *__restrict__ vbar, T *__restrict__ u, T *__restrict__ v)
+{
+    COLUMN_HEADER
+    if (col == 0) {
+        for (int iz = threadIdx.x; iz <= d.nz; iz += 32) {
+            u[iz] = (T)ubar[iz];
+            v[iz] = (T)vbar[iz];
+        }
+        return;
+    }
+    PARTNERS
+    const double kk = k2l2i[col];
+    for (int iz = threadIdx.x; iz <= d.nz; iz += 32) {
+        u[o + iz] = (T)(kk * (cxk * (double)es[ox + iz] + cyk * (double)cs[oy + iz]));
+        v[o + iz] = (T)(kk * (cyk * (double)es[oy + iz] - cxk * (double)cs[ox + iz]));
+    }
+}
+template <typename T>
+void op_v2v_uv(const Dims &d, cudaStream_t st, const Deriv &D, const double *k2l2i, const T *es, const T *cs,
+               const double *ubar, const double *vbar, T *u, T *v)
+{
+    k_v2v_uv<T><<<col_grid(d), COL_BLOCK, 0, st>>>(d, D, k2l2i, es, cs, ubar, vbar, u, v);
+}
+
+// ------------------------------------------------------------------- source
+template <typename T>
+__global__ void k_add_const(Dims d, T *__restrict__ f, double c)
+{
+    COLUMN_HEADER
+    for (int iz = threadIdx.x; iz <= d.nz; iz += 32) f[o + iz] = (T)((double)f[o + iz] + c);
+}
+template <typename T> void op_add_const(const Dims &d, cudaStream_t st, T *f, double c)
+{
+    k_add_const<T><<<col_grid(d), COL_BLOCK, 0, st>>>(d, f, c);
+}
+
+// r = u eta - v xi, q = w xi - u zeta, p = v zeta - w eta (inversion.f90:327-352)
+template <typename T>
+__global__ void k_products(Dims d, const T *__restrict__ vel, const T *__restrict__ vor, T *__restrict__ r,
+                           T *__restrict__ q, T *__restrict__ p)
+{
+    COLUMN_HEADER
+    const long long N = d.nfield;
+    for (int iz = threadIdx.x; iz <= d.nz; iz += 32) {
+        const long long i = o + iz;
+        const double u = vel[i], v = vel[N + i], w = vel[2 * N + i];
+        const double xi = vor[i], eta = vor[N + i], zeta = vor[2 * N + i];
+        r[i] = (T)(u * eta - v * xi);
+        q[i] = (T)(w * xi - u * zeta);
+        p[i] = (T)(v * zeta - w * eta);
+    }
+}
+template <typename T>
+void op_products(const Dims &d, cudaStream_t st, const T *vel, const T *vor, T *r, T *q, T *p)
+{
+    k_products<T><<<col_grid(d), COL_BLOCK, 0, st>>>(d, vel, vor, r, q, p);
+}
+
+// svorts = (D_y r - dq/dz, dp/dz - D_x r, D_x q - D_y p) (inversion.f90:341-367)
+template <typename T>
+__global__ void k_svorts(Dims d, Deriv D, const T *__restrict__ r, const T *__restrict__ q,
+                         const T *__restrict__ p, const T *__restrict__ gq, const T *__restrict__ gp,
+                         T *__restrict__ s1, T *__restrict__ s2, T *__restrict__ s3)
+{
+    COLUMN_HEADER
+    PARTNERS
+    for (int iz = threadIdx.x; iz <= d.nz; iz += 32) {
+        const long long i = o + iz;
+        s1[i] = (T)(cyk * (double)r[oy + iz] - (double)gq[i]);
+        s2[i] = (T)((double)gp[i] - cxk * (double)r[ox + iz]);
+        s3[i] = (T)(cxk * (double)q[ox + iz] - cyk * (double)p[oy + iz]);
+    }
+}
+template <typename T>
+void op_svorts(const Dims &d, cudaStream_t st, const Deriv &D, const T *r, const T *q, const T *p,
+               const T *gq, const T *gp, T *s1, T *s2, T *s3)
+{
+    k_svorts<T><<<col_grid(d), COL_BLOCK, 0, st>>>(d, D, r, q, p, gq, gp, s1, s2, s3);
+}
+
+// spectral velocity gradients for the strain (advance.f90:193-217):
+// du/dx, du/dy, dw/dx, dv/dy, dw/dy
+template <typename T>
+__global__ void k_strain_fields(Dims d, Deriv D, const T *__restrict__ svel, T *__restrict__ g5)
+{
+    COLUMN_HEADER
+    PARTNERS
+    const long long N = d.nfield;
+    for (int iz = threadIdx.x; iz <= d.nz; iz += 32) {
+        const long long i = o + iz;
+        g5[i] = (T)(cxk * (double)svel[ox + iz]);
+        g5[N + i] = (T)(cyk * (double)svel[oy + iz]);
+        g5[2 * N + i] = (T)(cxk * (double)svel[2 * N + ox + iz]);
+        g5[3 * N + i] = (T)(cyk * (double)svel[N + oy + iz]);
+        g5[4 * N + i] = (T)(cyk * (double)svel[2 * N + oy + iz]);
+    }
+}
+template <typename T>
+void op_strain_fields(const Dims &d, cudaStream_t st, const Deriv &D, const T *svel, T *g5)
+{
+    k_strain_fields<T><<<col_grid(d), COL_BLOCK, 0, st>>>(d, D, svel, g5);
+}
+
+// flat conversions / accumulation over n elements
+template <typename T, typename S>
+__global__ void k_convert(const S *__restrict__ in, T *__restrict__ out, long long n)
+{
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+        out[i] = (T)in[i];
+}
+template <typename T, typename S>
+void op_convert(const Dims &, cudaStream_t st, const S *in, T *out, long long n)
+{
+    k_convert<T, S><<<1216, 256, 0, st>>>(in, out, n);
+}
+template <typename T, typename S>
+__global__ void k_add(S *__restrict__ acc, const T *__restrict__ add, long long n)
+{
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+        acc[i] = (S)((double)acc[i] + (double)add[i]);
+}
+template <typename T, typename S>
+void op_add(const Dims &, cudaStream_t st, S *acc, const T *add, long long n)
+{
+    k_add<T, S><<<1216, 256, 0, st>>>(acc, add, n);
+}
+
+// ----------------------------------------------------------------- steppers
+// The reference wraps every column scaling of the steppers in
+// field_combine_semi_spectral ... field_decompose_semi_spectral
+// (impl_rk4.f90:232-238, 264-280, 307-323, 346-362; cn2.f90:110-116,
+// 128-134, 166-172).  Both are linear per column and the factors depend on
+// (ky, kx) only, so the sandwich equals the bare column scaling; it is
+// applied directly here (identical up to rounding).
+
+// integrating factors (impl_rk4.f90:87-89, 151, 185)
+__global__ void k_rk4_factors(long long ncol, const double *__restrict__ vdiss, const double *__restrict__ filt0,
+                              double *epq, double *emq, double *epq2, double *emq2)
+{
+    const long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= ncol) return;
+    const double e = exp(vdiss[c]);
+    const double m = 1.0 / e;
+    const double p = e * filt0[c];
+    epq[c] = p;
+    emq[c] = m;
+    epq2[c] = p * p;
+    emq2[c] = m * m;
+}
+void op_rk4_factors(const Dims &d, cudaStream_t st, const double *vdiss, const double *filt0, double *epq,
+                    double *emq, double *epq2, double *emq2)
+{
+    k_rk4_factors<<<(unsigned)((d.ncol + 255) / 256), 256, 0, st>>>(d.ncol, vdiss, filt0, epq, emq, epq2, emq2);
+}
+
+// substep 1 (impl_rk4.f90:212-242)
+template <typename T>
+__global__ void k_rk4_sub1(Dims d, double *__restrict__ q, double *__restrict__ qdi, double *__restrict__ qdf,
+                           T *__restrict__ sqs, const double *__restrict__ filt0, const double *__restrict__ emq,
+                           double dt2, double dt6)
+{
+    COLUMN_HEADER
+    const double f0 = filt0[col], m = emq[col];
+    for (int iz = threadIdx.x; iz <= d.nz; iz += 32) {
+        const long long i = o + iz;
+        const double s = f0 * (double)sqs[i];
+        const double q0 = q[i];
+        sqs[i] = (T)s;
+        qdi[i] = q0;
+        q[i] = (q0 + dt2 * s) * m;
+        qdf[i] = q0 + dt6 * s;
+    }
+}
+template <typename T>
+void op_rk4_sub1(const Dims &d, cudaStream_t st, double *q, double *qdi, double *qdf, T *sqs,
+                 const double *filt0, const double *emq, double dt2, double dt6)
+{
+    k_rk4_sub1<T><<<col_grid(d), COL_BLOCK, 0, st>>>(d, q, qdi, qdf, sqs, filt0, emq, dt2, dt6);
+}
+
+// substeps 2 and 3 (impl_rk4.f90:247-326): c1 = dt/2 or dt
+template <typename T>
+__global__ void k_rk4_sub23(Dims d, double *__restrict__ q, const double *__restrict__ qdi,
+                            double *__restrict__ qdf, const T *__restrict__ sqs, const double *__restrict__ epq,
+                            const double *__restrict__ emq, double c1, double dt3)
+{
+    COLUMN_HEADER
+    const double pp = epq[col], m = emq[col];
+    for (int iz = threadIdx.x; iz <= d.nz; iz += 32) {
+        const long long i = o + iz;
+        const double s = pp * (double)sqs[i];
+        q[i] = (qdi[i] + c1 * s) * m;
+        qdf[i] = qdf[i] + dt3 * s;
+    }
+}
+template <typename T>
+void op_rk4_sub23(const Dims &d, cudaStream_t st, double *q, const double *qdi, double *qdf, const T *sqs,
+                  const double *epq, const double *emq, double c1, double dt3)
+{
+    k_rk4_sub23<T><<<col_grid(d), COL_BLOCK, 0, st>>>(d, q, qdi, qdf, sqs, epq, emq, c1, dt3);
+}
+
+// substep 4 (impl_rk4.f90:331-364)
+template <typename T>
+__global__ void k_rk4_sub4(Dims d, double *__restrict__ q, const double *__restrict__ qdf,
+                           const T *__restrict__ sqs, const double *__restrict__ epq,
+                           const double *__restrict__ emq, double dt6)
+{
+    COLUMN_HEADER
+    const double pp = epq[col], m = emq[col];
+    for (int iz = threadIdx.x; iz <= d.nz; iz += 32) {
+        const long long i = o + iz;
+        q[i] = (qdf[i] + dt6 * (pp * (double)sqs[i])) * m;
+    }
+}
+template <typename T>
+void op_rk4_sub4(const Dims &d, cudaStream_t st, double *q, const double *qdf, const T *sqs,
+                 const double *epq, const double *emq, double dt6)
+{
+    k_rk4_sub4<T><<<col_grid(d), COL_BLOCK, 0, st>>>(d, q, qdf, sqs, epq, emq, dt6);
+}
+
+// cn2 (cn2.f90:119-175)
+template <typename T>
+__global__ void k_cn2_init(Dims d, double *__restrict__ vortsm, const double *__restrict__ svor,
+                           const T *__restrict__ svorts, double dt2)
+{
+    COLUMN_HEADER
+    for (int iz = threadIdx.x; iz <= d.nz; iz += 32) vortsm[o + iz] = svor[o + iz] + dt2 * (double)svorts[o + iz];
+}
+template <typename T>
+void op_cn2_init(const Dims &d, cudaStream_t st, double *vortsm, const double *svor, const T *svorts, double dt2)
+{
+    for (int c = 0; c < 3; ++c)
+        k_cn2_init<T><<<col_grid(d), COL_BLOCK, 0, st>>>(d, vortsm + c * d.nfield, svor + c * d.nfield,
+                                                         svorts + c * d.nfield, dt2);
+}
+template <typename T>
+__global__ void k_cn2_update(Dims d, double *__restrict__ svor, const double *__restrict__ vortsm,
+                             const T *__restrict__ svorts, const double *__restrict__ filt0,
+                             const double *__restrict__ fz, const double *__restrict__ vdiss, double dt2)
+{
+    COLUMN_HEADER
+    const double f0 = filt0[col], vd = vdiss[col];
+    for (int iz = threadIdx.x; iz <= d.nz; iz += 32) {
+        const long long i = o + iz;
+        double f = f0;
+        if (col == 0) f = 1.0;
+        else if (iz > 0 && iz < d.nz) f = f0 * fz[iz];
+        svor[i] = f * (vortsm[i] + dt2 * (double)svorts[i]) * vd;
+    }
+}
+template <typename T>
+void op_cn2_update(const Dims &d, cudaStream_t st, double *svor, const double *vortsm, const T *svorts,
+                   const double *filt0, const double *fz, const double *vdiss, double dt2)
+{
+    for (int c = 0; c < 3; ++c)
+        k_cn2_update<T><<<col_grid(d), COL_BLOCK, 0, st>>>(d, svor + c * d.nfield, vortsm + c * d.nfield,
+                                                           svorts + c * d.nfield, filt0, fz, vdiss, dt2);
+}
+
+// calc_vorticity_mean / adjust_vorticity_mean (field_diagnostics.f90:584-619).
+// The sum of the sine transform of the (0,0) column is the dot product with
+// dstsum[j] = sqrt(2/nz) sum_k sin(pi j k / nz).
+__global__ void k_mean_fix(int nz, long long nfield, double *svor, const double *__restrict__ dstsum, double fnzi,
+                           const double *__restrict__ ini, double *savg_out, int apply)
+{
+    __shared__ double red[2][256];
+    for (int nc = 0; nc < 2; ++nc) {
+        const double *s = svor + nc * nfield;
+        double acc = 0.0;
+        for (int j = 1 + threadIdx.x; j < nz; j += blockDim.x) acc += dstsum[j] * s[j];
+        red[nc][threadIdx.x] = acc;
+    }
+    __syncthreads();
+    for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+        if (threadIdx.x < w) {
+            red[0][threadIdx.x] += red[0][threadIdx.x + w];
+            red[1][threadIdx.x] += red[1][threadIdx.x + w];
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        for (int nc = 0; nc < 2; ++nc) {
+            double *s = svor + nc * nfield;
+            const double savg = 0.5 * (s[0] + s[nz]) + fnzi * red[nc][0];
+            if (savg_out) savg_out[nc] = savg;
+            if (apply) {
+                s[0] = s[0] + ini[nc] - savg;
+                s[nz] = s[nz] + ini[nc] - savg;
+            }
+        }
+    }
+}
+void op_mean_fix(const Dims &d, cudaStream_t st, double *svor, const double *dstsum, double fnzi,
+                 const double *ini, double *savg_out, int apply)
+{
+    k_mean_fix<<<1, 256, 0, st>>>(d.nz, d.nfield, svor, dstsum, fnzi, ini, savg_out, apply);
+}
+
+// --------------------------------------------------------------- reductions
+// Neumaier-compensated FP64 accumulation per thread, pairwise tree across
+// threads and blocks.
+struct KSum {
+    double s, c;
+    __device__ void add(double v)
+    {
+        const double t = s + v;
+        if (fabs(s) >= fabs(v)) c += (s - t) + v;
+        else c += (v - t) + s;
+        s = t;
+    }
+    __device__ double value() const { return s + c; }
+};
+
+int red_nblocks(const Dims &d)
+{
+    long long nb = (d.ncol + COLS_PER_BLOCK - 1) / COLS_PER_BLOCK;
+    if (nb > 1216) nb = 1216;
+    return (int)nb;
+}
+
+// block-level reduce of NV values: kinds[v] = 0 sum, 1 max
+template <int NV>
+__device__ void block_reduce_store(double (&vals)[NV], const int (&kinds)[NV], double *part)
+{
+    __shared__ double sh[NV][8];
+    const int lane = threadIdx.x, wy = threadIdx.y;  // 32 x 8 block: one warp per row
+#pragma unroll
+    for (int v = 0; v < NV; ++v) {
+        double x = vals[v];
+        for (int off = 16; off > 0; off >>= 1) {
+            const double y = __shfl_down_sync(0xffffffffu, x, off);
+            x = kinds[v] ? fmax(x, y) : x + y;
+        }
+        if (lane == 0) sh[v][wy] = x;
+    }
+    __syncthreads();
+    if (wy == 0 && lane < NV) {
+        double x = sh[lane][0];
+        for (int w = 1; w < COLS_PER_BLOCK; ++w) x = kinds[lane] ? fmax(x, sh[lane][w]) : x + sh[lane][w];
+        part[(long long)blockIdx.x * NV + lane] = x;
+    }
+}
+
+template <int NV>
+__global__ void k_finish(const double *__restrict__ part, int nblk, const int *kinds_in, double *result)
+{
+    // single block, one warp per value, fixed order
+    const int v = threadIdx.y;
+    if (v >= NV) return;
+    const int kind = kinds_in[v];
+    double x = kind ? -DBL_MAX : 0.0;
+    KSum ks{0.0, 0.0};
+    for (int b = threadIdx.x; b < nblk; b += 32) {
+        const double y = part[(long long)b * NV + v];
+        if (kind) x = fmax(x, y);
+        else ks.add(y);
+    }
+    if (!kind) x = ks.value();
+    for (int off = 16; off > 0; off >>= 1) {
+        const double y = __shfl_down_sync(0xffffffffu, x, off);
+        x = kind ? fmax(x, y) : x + y;
+    }
+    if (threadIdx.x == 0) result[v] = x;
+}
+
+__constant__ int c_kinds1[RED1_N] = {1, 0, 0, 0, 0, 0, 0, 1, 1, 1, 0, 0};
+__constant__ int c_kinds2[RED2_N] = {0, 0, 1, 1, 1};
+
+// pass 1: 0 max|w|^2, 1 sum_w |w|^2, 2 sum_w |u|^2, 3 sum_w u.w, 4..6 sum_w w_c,
+// 7..9 max u, v, w (signed)   (advance.f90:171-185, 285-288;
+// field_diagnostics.f90:85-206, 405-432, 549-579)
+template <typename T>
+__global__ void k_red1(Dims d, const T *__restrict__ vel, const T *__restrict__ vor, double *part)
+{
+    const long long N = d.nfield;
+    double vmx[3] = {-DBL_MAX, -DBL_MAX, -DBL_MAX};
+    double wmax2 = 0.0;
+    KSum s_w2{0, 0}, s_u2{0, 0}, s_h{0, 0}, s_m[3] = {{0, 0}, {0, 0}, {0, 0}};
+    for (long long col = (long long)blockIdx.x * COLS_PER_BLOCK + threadIdx.y; col < d.ncol;
+         col += (long long)gridDim.x * COLS_PER_BLOCK) {
+        const long long o = col * d.P;
+        for (int iz = threadIdx.x; iz <= d.nz; iz += 32) {
+            const long long i = o + iz;
+            const double wt = (iz == 0 || iz == d.nz) ? 0.5 : 1.0;
+            const double x = vor[i], y = vor[N + i], z = vor[2 * N + i];
+            const double u = vel[i], v = vel[N + i], w = vel[2 * N + i];
+            const double w2 = x * x + y * y + z * z;
+            wmax2 = fmax(wmax2, w2);
+            s_w2.add(wt * w2);
+            s_u2.add(wt * (u * u + v * v + w * w));
+            s_h.add(wt * (u * x + v * y + w * z));
+            s_m[0].add(wt * x);
+            s_m[1].add(wt * y);
+            s_m[2].add(wt * z);
+            vmx[0] = fmax(vmx[0], u);
+            vmx[1] = fmax(vmx[1], v);
+            vmx[2] = fmax(vmx[2], w);
+        }
+    }
+    double vals[RED1_N] = {wmax2, s_w2.value(), s_u2.value(), s_h.value(), s_m[0].value(), s_m[1].value(),
+                           s_m[2].value(), vmx[0], vmx[1], vmx[2], 0.0, 0.0};
+    const int kinds[RED1_N] = {1, 0, 0, 0, 0, 0, 0, 1, 1, 1, 0, 0};
+    block_reduce_store<RED1_N>(vals, kinds, part);
+}
+
+template <typename T>
+void red_pass1(const Dims &d, cudaStream_t st, const T *vel, const T *vor, double *part, double *result)
+{
+    const int nb = red_nblocks(d);
+    k_red1<T><<<nb, COL_BLOCK, 0, st>>>(d, vel, vor, part);
+    int *kinds;
+    cudaGetSymbolAddress((void **)&kinds, c_kinds1);
+    k_finish<RED1_N><<<1, dim3(32, RED1_N), 0, st>>>(part, nb, kinds, result);
+}
+
+// Rutishauser cyclic Jacobi eigenvalues of a symmetric 3x3 (jacobi.f90),
+// upper triangle a01 a02 a12, diagonal d0 d1 d2; returns max |lambda|.
+// The sweep count is bounded; *hit is set if the bound is reached.
+__device__ __forceinline__ void givens_rot(double aij, double di, double dj, double &c, double &s, double &t,
+                                           double &tau)
+{
+    const double g = 100.0 * fabs(aij);
+    const double h = dj - di;
+    if (fabs(h) + g == fabs(h)) {
+        t = aij / (h + copysign(DBL_EPSILON, h));
+    } else {
+        const double theta = 0.5 * h / (aij + copysign(DBL_EPSILON, aij));
+        t = 1.0 / (fabs(theta) + sqrt(1.0 + theta * theta));
+        if (theta < 0.0) t = -t;
+    }
+    c = 1.0 / sqrt(1.0 + t * t);
+    s = t * c;
+    tau = s / (1.0 + c);
+}
+
+__device__ double jacobi_maxabs(double a00, double a01, double a02, double a11, double a12, double a22, int *hit)
+{
+    double A[3][3] = {{a00, a01, a02}, {0.0, a11, a12}, {0.0, 0.0, a22}};
+    double D[3] = {a00, a11, a22}, Bv[3] = {a00, a11, a22}, Z[3] = {0.0, 0.0, 0.0};
+    double sm = fabs(A[0][1]) + fabs(A[0][2]) + fabs(A[1][2]);
+    int sweeps = 0;
+    while (sm > 1.0e-15) {
+        if (++sweeps > 100) {
+            *hit = 1;
+            break;
+        }
+#pragma unroll
+        for (int i = 0; i < 2; ++i) {
+#pragma unroll
+            for (int j = i + 1; j < 3; ++j) {
+                double c, s, t, tau;
+                givens_rot(A[i][j], D[i], D[j], c, s, t, tau);
+                double h = t * A[i][j];
+                Z[i] -= h;
+                Z[j] += h;
+                D[i] -= h;
+                D[j] += h;
+                A[i][j] = 0.0;
+#pragma unroll
+                for (int k = 0; k < 3; ++k) {
+                    if (k < i) {
+                        const double g = A[k][i], hh = A[k][j];
+                        A[k][i] = g - s * (hh + g * tau);
+                        A[k][j] = hh + s * (g - hh * tau);
+                    } else if (k > i && k < j) {
+                        const double g = A[i][k], hh = A[k][j];
+                        A[i][k] = g - s * (hh + g * tau);
+                        A[k][j] = hh + s * (g - hh * tau);
+                    } else if (k > j) {
+                        const double g = A[i][k], hh = A[j][k];
+                        A[i][k] = g - s * (hh + g * tau);
+                        A[j][k] = hh + s * (g - hh * tau);
+                    }
+                }
+            }
+        }
+        for (int k = 0; k < 3; ++k) {
+            Bv[k] += Z[k];
+            D[k] = Bv[k];
+            Z[k] = 0.0;
+        }
+        sm = fabs(A[0][1]) + fabs(A[0][2]) + fabs(A[1][2]);
+    }
+    return fmax(fmax(fabs(D[0]), fabs(D[1])), fabs(D[2]));
+}
+
+// pass 2: 0 vorl1, 1 vorl2 (characteristic vorticity, field_diagnostics.f90:
+// 501-545), 2 ggmax, 3 usggmax, 4 lsggmax (advance.f90:222-276)
+template <typename T>
+__global__ void k_red2(Dims d, const T *__restrict__ vor, const T *__restrict__ g5, double vortrms,
+                       double *part, int *flag)
+{
+    const long long N = d.nfield;
+    KSum l1{0, 0}, l2{0, 0};
+    double gg = DBL_EPSILON, us = 0.0, ls = 0.0;
+    int hit = 0;
+    for (long long col = (long long)blockIdx.x * COLS_PER_BLOCK + threadIdx.y; col < d.ncol;
+         col += (long long)gridDim.x * COLS_PER_BLOCK) {
+        const long long o = col * d.P;
+        for (int iz = threadIdx.x; iz <= d.nz; iz += 32) {
+            const long long i = o + iz;
+            const double x = vor[i], y = vor[N + i], z = vor[2 * N + i];
+            if (iz >= 1) {
+                const double v1 = 0.5 * fabs((double)vor[i - 1] + x);
+                const double v2 = 0.5 * fabs((double)vor[N + i - 1] + y);
+                const double v3 = 0.5 * fabs((double)vor[2 * N + i - 1] + z);
+                if (v1 + v2 + v3 > vortrms) {
+                    l1.add(v1 + v2 + v3);
+                    l2.add(v1 * v1 + v2 * v2 + v3 * v3);
+                }
+            }
+            const double dudx = g5[i], dudy = g5[N + i], dwdx = g5[2 * N + i], dvdy = g5[3 * N + i],
+                         dwdy = g5[4 * N + i];
+            const double lmax = jacobi_maxabs(dudx, dudy + 0.5 * z, dwdx + 0.5 * y, dvdy, dwdy - 0.5 * x,
+                                              -(dudx + dvdy), &hit);
+            gg = fmax(gg, lmax);
+            if (iz == d.nz) us = fmax(us, lmax);
+            if (iz == 0) ls = fmax(ls, lmax);
+        }
+    }
+    if (hit) atomicExch(flag, 1);
+    double vals[RED2_N] = {l1.value(), l2.value(), gg, us, ls};
+    const int kinds[RED2_N] = {0, 0, 1, 1, 1};
+    block_reduce_store<RED2_N>(vals, kinds, part);
+}
+
+template <typename T>
+void red_pass2(const Dims &d, cudaStream_t st, const T *vor, const T *g5, double vortrms, double *part,
+               double *result, int *flag)
+{
+    const int nb = red_nblocks(d);
+    k_red2<T><<<nb, COL_BLOCK, 0, st>>>(d, vor, g5, vortrms, part, flag);
+    int *kinds;
+    cudaGetSymbolAddress((void **)&kinds, c_kinds2);
+    k_finish<RED2_N><<<1, dim3(32, RED2_N), 0, st>>>(part, nb, kinds, result);
+}
+
+// ------------------------------------------------------------------- tables
+// phim, phip, thetam, thetap, dthetam, dthetap (inversion_utils.f90:484-542)
+// and the Green function (:281-288) per column
+template <typename T>
+__global__ void k_hyperbolic(Dims d, const double *__restrict__ k2l2, const double *__restrict__ k2l2i,
+                             const double *__restrict__ rkz, const double *__restrict__ zm,
+                             const double *__restrict__ zp, double Lz, T *phim, T *phip, T *thetam, T *thetap,
+                             T *dthetam, T *dthetap, T *green)
+{
+    COLUMN_HEADER
+    const int nz = d.nz;
+    const double kk = k2l2[col], ki = k2l2i[col];
+    if (col == 0) {
+        for (int iz = threadIdx.x; iz <= nz; iz += 32) {
+            const long long q = o + iz;
+            phim[q] = (T)(zm[iz] / Lz);
+            phip[q] = (T)(zp[iz] / Lz);
+            thetam[q] = thetap[q] = dthetam[q] = dthetap[q] = (T)0;
+            green[q] = (T)(iz == 0 ? -ki : -1.0 / (kk + rkz[iz] * rkz[iz]));
+        }
+        return;
+    }
+    const double kl = sqrt(kk);
+    const double ef = exp(-kl * Lz);
+    const double div = 1.0 / (1.0 - ef * ef);
+    const double k2ifac = 0.5 * ki;
+    const double Q = div * (1.0 + ef * ef);
+    const double R = div * 2.0 * ef;
+    for (int iz = threadIdx.x; iz <= nz; iz += 32) {
+        const long long q = o + iz;
+        const double Lm = kl * zm[iz], Lp = kl * zp[iz];
+        const double ep = exp(-Lp), em = exp(-Lm);
+        const double phm = div * (ep - ef * em);
+        const double php = div * (em - ef * ep);
+        const double dphm = -kl * div * (ep + ef * em);
+        const double dphp = kl * div * (em + ef * ep);
+        phim[q] = (T)phm;
+        phip[q] = (T)php;
+        thetam[q] = (T)(k2ifac * (R * Lm * php - Q * Lp * phm));
+        thetap[q] = (T)(k2ifac * (R * Lp * phm - Q * Lm * php));
+        dthetam[q] = (T)(-k2ifac * ((Q * Lp - 1.0) * dphm - R * Lm * dphp));
+        dthetap[q] = (T)(-k2ifac * ((Q * Lm - 1.0) * dphp - R * Lp * dphm));
+        green[q] = (T)(iz == 0 ? -ki : -1.0 / (kk + rkz[iz] * rkz[iz]));
+    }
+}
+template <typename T>
+void op_hyperbolic_tables(const Dims &d, cudaStream_t st, const double *k2l2, const double *k2l2i,
+                          const double *rkz, const double *zm, const double *zp, double Lz, T *phim, T *phip,
+                          T *thetam, T *thetap, T *dthetam, T *dthetap, T *green)
+{
+    k_hyperbolic<T><<<col_grid(d), COL_BLOCK, 0, st>>>(d, k2l2, k2l2i, rkz, zm, zp, Lz, phim, phip, thetam,
+                                                       thetap, dthetam, dthetap, green);
+}
+
+// ------------------------------------------------------------ instantiation
+#define INST_T(T)                                                                                              \
+    template void op_diff<T>(const Dims &, cudaStream_t, const Deriv &, int, const T *, T *);                   \
+    template void op_diffz<T>(const Dims &, cudaStream_t, double, const T *, T *);                              \
+    template void op_v2v_ds<T, double>(const Dims &, cudaStream_t, const Deriv &, const double *,              \
+                                       const double *, T *);                                                   \
+    template void op_v2v_project<T, double>(const Dims &, cudaStream_t, const Deriv &, const double *,         \
+                                            const T *, const T *, double *, double *);                         \
+    template void op_v2v_wsrc<T, double>(const Dims &, cudaStream_t, const Deriv &, const double *,            \
+                                         const double *, T *);                                                 \
+    template void op_v2v_wprep<T>(const Dims &, cudaStream_t, const T *, const T *, const T *, const T *,      \
+                                  const T *, const T *, const double *, T *, T *, T *, T *);                   \
+    template void op_v2v_wfinish<T>(const Dims &, cudaStream_t, const T *, const T *, const T *, T *, T *);    \
+    template void op_v2v_uv<T>(const Dims &, cudaStream_t, const Deriv &, const double *, const T *,           \
+                               const T *, const double *, const double *, T *, T *);                           \
+    template void op_add_const<T>(const Dims &, cudaStream_t, T *, double);                                    \
+    template void op_products<T>(const Dims &, cudaStream_t, const T *, const T *, T *, T *, T *);             \
+    template void op_svorts<T>(const Dims &, cudaStream_t, const Deriv &, const T *, const T *, const T *,     \
+                               const T *, const T *, T *, T *, T *);                                           \
+    template void op_strain_fields<T>(const Dims &, cudaStream_t, const Deriv &, const T *, T *);              \
+    template void op_add<T, double>(const Dims &, cudaStream_t, double *, const T *, long long);              \
+    template void op_rk4_sub1<T>(const Dims &, cudaStream_t, double *, double *, double *, T *,               \
+                                 const double *, const double *, double, double);                              \
+    template void op_rk4_sub23<T>(const Dims &, cudaStream_t, double *, const double *, double *, const T *,  \
+                                  const double *, const double *, double, double);                             \
+    template void op_rk4_sub4<T>(const Dims &, cudaStream_t, double *, const double *, const T *,             \
+                                 const double *, const double *, double);                                      \
+    template void op_cn2_init<T>(const Dims &, cudaStream_t, double *, const double *, const T *, double);    \
+    template void op_cn2_update<T>(const Dims &, cudaStream_t, double *, const double *, const T *,           \
+                                   const double *, const double *, const double *, double);                    \
+    template void red_pass1<T>(const Dims &, cudaStream_t, const T *, const T *, double *, double *);         \
+    template void red_pass2<T>(const Dims &, cudaStream_t, const T *, const T *, double, double *, double *,  \
+                               int *);                                                                         \
+    template void op_hyperbolic_tables<T>(const Dims &, cudaStream_t, const double *, const double *,         \
+                                          const double *, const double *, const double *, double, T *, T *,   \
+                                          T *, T *, T *, T *, T *);
+
+INST_T(double)
+INST_T(float)
+template void op_convert<float, double>(const Dims &, cudaStream_t, const double *, float *, long long);
+template void op_convert<double, float>(const Dims &, cudaStream_t, const float *, double *, long long);
+template void op_v2v_meanflow<double>(const Dims &, cudaStream_t, const double *, const double *, const Tables &,
+                                      double *, double *);
+
+}  // namespace ps3d

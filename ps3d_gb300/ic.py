@@ -1,0 +1,84 @@
+"""Initial conditions: the reference's Beltrami flow plus a seeded
+perturbation of the spectral vorticity.
+
+The Beltrami vorticity is src/beltrami.f90:162-181 evaluated on the grid
+points x = lower + i dx (both walls included, beltrami.f90:141-160).  The
+perturbation has no reference counterpart: Gaussian coefficients with a
+K^-2 envelope, K = |(k, l, m)|, placed in the interior sine modes of the
+mixed-spectral vorticity (boundary rows zero), from numpy's PCG64 generator
+seeded with `seed`, rescaled so that its grid rms (Parseval) is
+`amplitude * |omega|_rms` of the Beltrami field.  The first vor2vel of a run
+projects the sum onto a solenoidal field (inversion.f90:34-76).
+"""
+import numpy as np
+
+BASELINE_BOX = dict(lower=(0.0, 0.0, -0.5 * np.pi), extent=(2.0 * np.pi, 2.0 * np.pi, np.pi))
+
+
+def beltrami_vorticity(nx, ny, nz, lower, extent, k=2, l=2, m=1):
+    """(3, nx, ny, nz+1) FP64 physical vorticity of the Beltrami flow."""
+    kk, ll, mm = float(k), float(l), float(m)
+    alpha = np.sqrt(kk ** 2 + ll ** 2 + mm ** 2)
+    fk2l2 = alpha / float(k * k + l * l)
+    dx = np.array(extent, dtype=np.float64) / np.array([nx, ny, nz], dtype=np.float64)
+    x = lower[0] + dx[0] * np.arange(nx, dtype=np.float64)
+    y = lower[1] + dx[1] * np.arange(ny, dtype=np.float64)
+    z = lower[2] + dx[2] * np.arange(nz + 1, dtype=np.float64)
+    cosmz, sinmz = np.cos(mm * z), np.sin(mm * z)
+    phase = kk * x[:, None] + ll * y[None, :]
+    sinkxly, coskxly = np.sin(phase), np.cos(phase)
+    out = np.empty((3, nx, ny, nz + 1))
+    g1 = fk2l2 * (kk * mm * sinmz - ll * alpha * cosmz)
+    g2 = fk2l2 * (ll * mm * sinmz + kk * alpha * cosmz)
+    g3 = alpha * cosmz
+    np.multiply(sinkxly[:, :, None], g1[None, None, :], out=out[0])
+    np.multiply(sinkxly[:, :, None], g2[None, None, :], out=out[1])
+    np.multiply(coskxly[:, :, None], g3[None, None, :], out=out[2])
+    return out
+
+
+def wavenumbers(nx, ny, nz, extent):
+    """rkx, rky (Hermitian slot order, sta3dfft.f90:96-115), rkz (deriv1d.f90)."""
+    def horiz(n, L):
+        r = np.zeros(n)
+        h = n // 2
+        for kk in range(1, h):
+            r[kk] = r[n - kk] = 2.0 * np.pi * kk / L
+        r[h] = np.pi * n / L
+        return r
+    return horiz(nx, extent[0]), horiz(ny, extent[1]), np.pi * np.arange(nz + 1) / extent[2]
+
+
+def perturbation(nx, ny, nz, extent, seed, amplitude, vor_rms):
+    """(3, nx, ny, nz+1) mixed-spectral perturbation (see module docstring)."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    rkx, rky, rkz = wavenumbers(nx, ny, nz, extent)
+    K2 = rkx[:, None, None] ** 2 + rky[None, :, None] ** 2 + rkz[None, None, :] ** 2
+    env = np.zeros_like(K2)
+    np.divide(1.0, K2, out=env, where=K2 > 0)          # K^-2 envelope
+    env[:, :, 0] = 0.0
+    env[:, :, nz] = 0.0
+    env[nx // 2, :, :] = 0.0                            # no Nyquist modes
+    env[:, ny // 2, :] = 0.0
+    p = rng.standard_normal((3, nx, ny, nz + 1)) * env[None]
+    # grid mean square by Parseval: Hermitian slots other than 0 and n/2
+    # carry weight 2 in each horizontal direction; the sine transform is
+    # orthonormal over the nz-1 interior levels
+    wx = np.full(nx, 2.0); wx[0] = 1.0; wx[nx // 2] = 1.0
+    wy = np.full(ny, 2.0); wy[0] = 1.0; wy[ny // 2] = 1.0
+    w = wx[:, None, None] * wy[None, :, None]
+    ms = float(np.sum(w[None] * p * p)) / (nx * ny * (nz + 1))
+    scale = amplitude * vor_rms / np.sqrt(ms) if ms > 0 else 0.0
+    p *= scale
+    return p
+
+
+def beltrami_plus_perturbation(nx, ny, nz, seed=0, amplitude=1.0e-3, lower=None, extent=None):
+    """Physical Beltrami vorticity and the matching spectral perturbation,
+    on the box (2pi, 2pi, pi) with lower z = -pi/2 unless given."""
+    lower = BASELINE_BOX["lower"] if lower is None else lower
+    extent = BASELINE_BOX["extent"] if extent is None else extent
+    vor = beltrami_vorticity(nx, ny, nz, lower, extent)
+    rms = float(np.sqrt(np.mean(np.sum(vor * vor, axis=0))))
+    pert = perturbation(nx, ny, nz, extent, seed, amplitude, rms)
+    return vor, pert

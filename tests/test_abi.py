@@ -1,0 +1,66 @@
+"""CPU-side checks of the C ABI: the library builds, loads and exports every
+entry point include/ps3d_gpu.h declares; argument validation happens on the
+host before any device call."""
+import ctypes
+import os
+import re
+
+import pytest
+
+from ps3d_gb300 import _lib, build
+from ps3d_gb300.solver import make_config
+
+HEADER = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "include", "ps3d_gpu.h")
+
+
+def declared():
+    txt = open(HEADER).read()
+    return sorted(set(re.findall(r"\b(ps3d_gpu_\w+)\s*\(", txt)))
+
+
+def test_header_lists_match_binding():
+    assert declared() == sorted(_lib.EXPORTS)
+
+
+def test_library_exports_every_declared_symbol():
+    L = _lib.lib()
+    missing = [n for n in declared() if not hasattr(L, n)]
+    assert not missing, missing
+
+
+def test_library_is_built_for_sm_103a():
+    # the build recipe pins one -gencode target
+    assert build.ARCH == ["-gencode", "arch=compute_103a,code=sm_103a"]
+    assert os.path.exists(build.LIB)
+
+
+def test_strerror_codes():
+    L = _lib.lib()
+    for code in range(0, 9):
+        assert L.ps3d_gpu_strerror(code)
+    assert L.ps3d_gpu_strerror(999) == b"unknown status"
+
+
+@pytest.mark.parametrize("dims", [(30, 32, 32), (32, 32, 12), (4, 32, 32), (4096, 8, 8)])
+def test_unsupported_sizes_rejected_before_device(dims):
+    L = _lib.lib()
+    cfg = make_config(*dims, [0, 0, 0], [1, 1, 1])
+    h = ctypes.c_void_p()
+    assert L.ps3d_gpu_create(ctypes.byref(cfg), ctypes.byref(h)) == 2  # UNSUPPORTED_SIZE
+    assert not h.value
+
+
+def test_invalid_config_rejected():
+    L = _lib.lib()
+    h = ctypes.c_void_p()
+    cfg = make_config(32, 32, 32, [0, 0, 0], [1, 1, 1], precision=7)
+    assert L.ps3d_gpu_create(ctypes.byref(cfg), ctypes.byref(h)) == 1
+    cfg = make_config(32, 32, 32, [0, 0, 0], [1, 0, 1])
+    assert L.ps3d_gpu_create(ctypes.byref(cfg), ctypes.byref(h)) == 1
+    assert L.ps3d_gpu_create(None, ctypes.byref(h)) == 1
+
+
+def test_null_context_is_an_error_not_a_crash():
+    L = _lib.lib()
+    assert L.ps3d_gpu_vor2vel(None) == 1
+    assert L.ps3d_gpu_destroy(None) == 0
