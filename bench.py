@@ -249,6 +249,9 @@ def run_gpu(args, rank, world, dist):
             t64, _ = g64.advance_n(t64, pre)
         t64, ms64 = g64.time_advance(t64, n_fp64_timed)
         sec64 = max_over_ranks(dist, ms64 / 1e3)
+        # solenoidal states (the FP64 form projects svor in vor2vel)
+        g64.vor2vel()
+        gm.vor2vel()
         a = gm.get("svor")
         b = g64.get("svor")
         err = float(np.linalg.norm(a - b) / np.linalg.norm(b))

@@ -52,6 +52,10 @@ void xy_inverse(const Dims &d, cudaStream_t st, const T *in, T *out, const typen
 template <typename T>
 void columns(const Dims &d, cudaStream_t st, int mode, const T *in, T *out, const T *phim,
              const T *phip, const typename cplx<T>::type *twz2, Probe *pr);
+// column transform of an FP64 input field into a T field (mixed form)
+template <typename T, typename TIN>
+void columns_in(const Dims &d, cudaStream_t st, int mode, const TIN *in, T *out, const T *phim,
+                const T *phip, const typename cplx<T>::type *twz2, Probe *pr);
 
 // Spectral-horizontal derivative operators.  For a spectral index k along
 // x (or y) the reference's diffx/diffy (sta3dfft.f90:304-377, with the

@@ -42,8 +42,8 @@ __global__ void k_diff(Dims d, Deriv D, int axis, const T *__restrict__ in, T *_
     COLUMN_HEADER
     PARTNERS
     const long long os = axis == 0 ? ox : oy;
-    const double c = axis == 0 ? cxk : cyk;
-    for (int iz = threadIdx.x; iz <= d.nz; iz += 32) out[o + iz] = (T)(c * (double)in[os + iz]);
+    const T c = (T)(axis == 0 ? cxk : cyk);
+    for (int iz = threadIdx.x; iz <= d.nz; iz += 32) out[o + iz] = c * in[os + iz];
 }
 template <typename T> void op_diff(const Dims &d, cudaStream_t st, const Deriv &D, int axis, const T *in, T *out)
 {
@@ -56,13 +56,13 @@ __global__ void k_diffz(Dims d, double dzi, const T *__restrict__ in, T *__restr
 {
     COLUMN_HEADER
     const int nz = d.nz;
-    const double hdzi = 0.5 * dzi;
+    const T dz = (T)dzi, hdz = (T)(0.5 * dzi);
     for (int iz = threadIdx.x; iz <= nz; iz += 32) {
-        double v;
-        if (iz == 0) v = dzi * ((double)in[o + 1] - (double)in[o]);
-        else if (iz == nz) v = dzi * ((double)in[o + nz] - (double)in[o + nz - 1]);
-        else v = ((double)in[o + iz + 1] - (double)in[o + iz - 1]) * hdzi;
-        out[o + iz] = (T)v;
+        T v;
+        if (iz == 0) v = dz * (in[o + 1] - in[o]);
+        else if (iz == nz) v = dz * (in[o + nz] - in[o + nz - 1]);
+        else v = (in[o + iz + 1] - in[o + iz - 1]) * hdz;
+        out[o + iz] = v;
     }
 }
 template <typename T> void op_diffz(const Dims &d, cudaStream_t st, double dzi, const T *in, T *out)
@@ -77,8 +77,8 @@ __global__ void k_v2v_ds(Dims d, Deriv D, const S *__restrict__ A, const S *__re
 {
     COLUMN_HEADER
     PARTNERS
-    for (int iz = threadIdx.x; iz <= d.nz; iz += 32)
-        ds[o + iz] = (T)(cxk * (double)B[ox + iz] - cyk * (double)A[oy + iz]);
+    const T cx = (T)cxk, cy = (T)cyk;
+    for (int iz = threadIdx.x; iz <= d.nz; iz += 32) ds[o + iz] = cx * (T)B[ox + iz] - cy * (T)A[oy + iz];
 }
 template <typename T, typename S>
 void op_v2v_ds(const Dims &d, cudaStream_t st, const Deriv &D, const S *A, const S *B, T *ds)
@@ -92,8 +92,8 @@ __global__ void k_v2v_wsrc(Dims d, Deriv D, const S *__restrict__ A, const S *__
 {
     COLUMN_HEADER
     PARTNERS
-    for (int iz = threadIdx.x; iz <= d.nz; iz += 32)
-        ds[o + iz] = (T)(cyk * (double)A[oy + iz] - cxk * (double)B[ox + iz]);
+    const T cx = (T)cxk, cy = (T)cyk;
+    for (int iz = threadIdx.x; iz <= d.nz; iz += 32) ds[o + iz] = cy * (T)A[oy + iz] - cx * (T)B[ox + iz];
 }
 template <typename T, typename S>
 void op_v2v_wsrc(const Dims &d, cudaStream_t st, const Deriv &D, const S *A, const S *B, T *ds)
@@ -110,12 +110,10 @@ __global__ void k_v2v_project(Dims d, Deriv D, const double *__restrict__ k2l2i,
     COLUMN_HEADER
     if (col == 0) return;
     PARTNERS
-    const double kk = k2l2i[col];
+    const S kk = (S)k2l2i[col], cx = (S)cxk, cy = (S)cyk;
     for (int iz = threadIdx.x; iz <= d.nz; iz += 32) {
-        const double a = kk * (cxk * (double)es[ox + iz] + cyk * (double)ds[oy + iz]);
-        const double b = kk * (cyk * (double)es[oy + iz] - cxk * (double)ds[ox + iz]);
-        A[o + iz] = (S)a;
-        B[o + iz] = (S)b;
+        A[o + iz] = kk * (cx * (S)es[ox + iz] + cy * (S)ds[oy + iz]);
+        B[o + iz] = kk * (cy * (S)es[oy + iz] - cx * (S)ds[ox + iz]);
     }
 }
 template <typename T, typename S>
@@ -136,15 +134,15 @@ __global__ void k_v2v_wprep(Dims d, const T *__restrict__ ds, const T *__restric
 {
     COLUMN_HEADER
     const int nz = d.nz;
-    const double d0 = ds[o], dn = ds[o + nz];
+    const T d0 = ds[o], dn = ds[o + nz];
     for (int iz = threadIdx.x; iz <= nz; iz += 32) {
         const long long q = o + iz;
-        es[q] = (T)(d0 * (double)dthetam[q] + dn * (double)dthetap[q]);
+        es[q] = d0 * dthetam[q] + dn * dthetap[q];
         if (iz > 0 && iz < nz) {
-            bs[q] = (T)(d0 * (double)thetam[q] + dn * (double)thetap[q]);
-            const double g = (double)green[q] * (double)ds[q];
-            dsg[q] = (T)g;
-            as[q] = (T)(rkz[iz] * (double)(T)g);
+            bs[q] = d0 * thetam[q] + dn * thetap[q];
+            const T g = green[q] * ds[q];
+            dsg[q] = g;
+            as[q] = (T)rkz[iz] * g;
         } else {
             bs[q] = (T)0;
             dsg[q] = (T)0;
@@ -171,8 +169,8 @@ __global__ void k_v2v_wfinish(Dims d, const T *__restrict__ dsg, const T *__rest
     const int nz = d.nz;
     for (int iz = threadIdx.x; iz <= nz; iz += 32) {
         const long long q = o + iz;
-        w[q] = (iz > 0 && iz < nz) ? (T)((double)dsg[q] + (double)bs[q]) : (T)0;
-        es[q] = (T)((double)es[q] + (double)as[q]);
+        w[q] = (iz > 0 && iz < nz) ? dsg[q] + bs[q] : (T)0;
+        es[q] = es[q] + as[q];
     }
 }
 template <typename T>
@@ -235,10 +233,10 @@ __global__ void k_v2v_uv(Dims d, Deriv D, const double *__restrict__ k2l2i, cons
         return;
     }
     PARTNERS
-    const double kk = k2l2i[col];
+    const T kk = (T)k2l2i[col], cx = (T)cxk, cy = (T)cyk;
     for (int iz = threadIdx.x; iz <= d.nz; iz += 32) {
-        u[o + iz] = (T)(kk * (cxk * (double)es[ox + iz] + cyk * (double)cs[oy + iz]));
-        v[o + iz] = (T)(kk * (cyk * (double)es[oy + iz] - cxk * (double)cs[ox + iz]));
+        u[o + iz] = kk * (cx * es[ox + iz] + cy * cs[oy + iz]);
+        v[o + iz] = kk * (cy * es[oy + iz] - cx * cs[ox + iz]);
     }
 }
 template <typename T>
@@ -253,7 +251,8 @@ template <typename T>
 __global__ void k_add_const(Dims d, T *__restrict__ f, double c)
 {
     COLUMN_HEADER
-    for (int iz = threadIdx.x; iz <= d.nz; iz += 32) f[o + iz] = (T)((double)f[o + iz] + c);
+    const T cc = (T)c;
+    for (int iz = threadIdx.x; iz <= d.nz; iz += 32) f[o + iz] = f[o + iz] + cc;
 }
 template <typename T> void op_add_const(const Dims &d, cudaStream_t st, T *f, double c)
 {
@@ -269,11 +268,11 @@ __global__ void k_products(Dims d, const T *__restrict__ vel, const T *__restric
     const long long N = d.nfield;
     for (int iz = threadIdx.x; iz <= d.nz; iz += 32) {
         const long long i = o + iz;
-        const double u = vel[i], v = vel[N + i], w = vel[2 * N + i];
-        const double xi = vor[i], eta = vor[N + i], zeta = vor[2 * N + i];
-        r[i] = (T)(u * eta - v * xi);
-        q[i] = (T)(w * xi - u * zeta);
-        p[i] = (T)(v * zeta - w * eta);
+        const T u = vel[i], v = vel[N + i], w = vel[2 * N + i];
+        const T xi = vor[i], eta = vor[N + i], zeta = vor[2 * N + i];
+        r[i] = u * eta - v * xi;
+        q[i] = w * xi - u * zeta;
+        p[i] = v * zeta - w * eta;
     }
 }
 template <typename T>
@@ -290,11 +289,12 @@ __global__ void k_svorts(Dims d, Deriv D, const T *__restrict__ r, const T *__re
 {
     COLUMN_HEADER
     PARTNERS
+    const T cx = (T)cxk, cy = (T)cyk;
     for (int iz = threadIdx.x; iz <= d.nz; iz += 32) {
         const long long i = o + iz;
-        s1[i] = (T)(cyk * (double)r[oy + iz] - (double)gq[i]);
-        s2[i] = (T)((double)gp[i] - cxk * (double)r[ox + iz]);
-        s3[i] = (T)(cxk * (double)q[ox + iz] - cyk * (double)p[oy + iz]);
+        s1[i] = cy * r[oy + iz] - gq[i];
+        s2[i] = gp[i] - cx * r[ox + iz];
+        s3[i] = cx * q[ox + iz] - cy * p[oy + iz];
     }
 }
 template <typename T>
@@ -312,13 +312,14 @@ __global__ void k_strain_fields(Dims d, Deriv D, const T *__restrict__ svel, T *
     COLUMN_HEADER
     PARTNERS
     const long long N = d.nfield;
+    const T cx = (T)cxk, cy = (T)cyk;
     for (int iz = threadIdx.x; iz <= d.nz; iz += 32) {
         const long long i = o + iz;
-        g5[i] = (T)(cxk * (double)svel[ox + iz]);
-        g5[N + i] = (T)(cyk * (double)svel[oy + iz]);
-        g5[2 * N + i] = (T)(cxk * (double)svel[2 * N + ox + iz]);
-        g5[3 * N + i] = (T)(cyk * (double)svel[N + oy + iz]);
-        g5[4 * N + i] = (T)(cyk * (double)svel[2 * N + oy + iz]);
+        g5[i] = cx * svel[ox + iz];
+        g5[N + i] = cy * svel[oy + iz];
+        g5[2 * N + i] = cx * svel[2 * N + ox + iz];
+        g5[3 * N + i] = cy * svel[N + oy + iz];
+        g5[4 * N + i] = cy * svel[2 * N + oy + iz];
     }
 }
 template <typename T>
@@ -525,8 +526,10 @@ void op_mean_fix(const Dims &d, cudaStream_t st, double *svor, const double *dst
 }
 
 // --------------------------------------------------------------- reductions
-// Neumaier-compensated FP64 accumulation per thread, pairwise tree across
-// threads and blocks.
+// Compensated accumulation per thread (Neumaier in FP64 for the FP64 form;
+// Knuth two-sum in FP32 registers for the mixed form, so its error is that
+// of an FP64 sum without FP64 arithmetic per element), then an FP64 tree
+// across threads and a fixed-order FP64 compensated sum across blocks.
 struct KSum {
     double s, c;
     __device__ void add(double v)
@@ -537,6 +540,25 @@ struct KSum {
         s = t;
     }
     __device__ double value() const { return s + c; }
+};
+
+template <typename T> struct Acc;
+template <> struct Acc<double> {
+    KSum k{0.0, 0.0};
+    __device__ void add(double v) { k.add(v); }
+    __device__ double value() const { return k.value(); }
+};
+template <> struct Acc<float> {
+    float s = 0.0f, c = 0.0f;
+    __device__ void add(float v)
+    {
+        const float t = s + v;
+        const float bp = t - s;
+        const float err = (s - (t - bp)) + (v - bp);
+        s = t;
+        c += err;
+    }
+    __device__ double value() const { return (double)s + (double)c; }
 };
 
 int red_nblocks(const Dims &d)
@@ -601,32 +623,33 @@ template <typename T>
 __global__ void k_red1(Dims d, const T *__restrict__ vel, const T *__restrict__ vor, double *part)
 {
     const long long N = d.nfield;
-    double vmx[3] = {-DBL_MAX, -DBL_MAX, -DBL_MAX};
-    double wmax2 = 0.0;
-    KSum s_w2{0, 0}, s_u2{0, 0}, s_h{0, 0}, s_m[3] = {{0, 0}, {0, 0}, {0, 0}};
+    const T lowest = sizeof(T) == 8 ? (T)-DBL_MAX : (T)-FLT_MAX;
+    T vmx[3] = {lowest, lowest, lowest};
+    T wmax2 = 0;
+    Acc<T> s_w2, s_u2, s_h, s_m0, s_m1, s_m2;
     for (long long col = (long long)blockIdx.x * COLS_PER_BLOCK + threadIdx.y; col < d.ncol;
          col += (long long)gridDim.x * COLS_PER_BLOCK) {
         const long long o = col * d.P;
         for (int iz = threadIdx.x; iz <= d.nz; iz += 32) {
             const long long i = o + iz;
-            const double wt = (iz == 0 || iz == d.nz) ? 0.5 : 1.0;
-            const double x = vor[i], y = vor[N + i], z = vor[2 * N + i];
-            const double u = vel[i], v = vel[N + i], w = vel[2 * N + i];
-            const double w2 = x * x + y * y + z * z;
-            wmax2 = fmax(wmax2, w2);
+            const T wt = (iz == 0 || iz == d.nz) ? (T)0.5 : (T)1;
+            const T x = vor[i], y = vor[N + i], z = vor[2 * N + i];
+            const T u = vel[i], v = vel[N + i], w = vel[2 * N + i];
+            const T w2 = x * x + y * y + z * z;
+            wmax2 = w2 > wmax2 ? w2 : wmax2;
             s_w2.add(wt * w2);
             s_u2.add(wt * (u * u + v * v + w * w));
             s_h.add(wt * (u * x + v * y + w * z));
-            s_m[0].add(wt * x);
-            s_m[1].add(wt * y);
-            s_m[2].add(wt * z);
-            vmx[0] = fmax(vmx[0], u);
-            vmx[1] = fmax(vmx[1], v);
-            vmx[2] = fmax(vmx[2], w);
+            s_m0.add(wt * x);
+            s_m1.add(wt * y);
+            s_m2.add(wt * z);
+            vmx[0] = u > vmx[0] ? u : vmx[0];
+            vmx[1] = v > vmx[1] ? v : vmx[1];
+            vmx[2] = w > vmx[2] ? w : vmx[2];
         }
     }
-    double vals[RED1_N] = {wmax2, s_w2.value(), s_u2.value(), s_h.value(), s_m[0].value(), s_m[1].value(),
-                           s_m[2].value(), vmx[0], vmx[1], vmx[2], 0.0, 0.0};
+    double vals[RED1_N] = {(double)wmax2, s_w2.value(), s_u2.value(), s_h.value(), s_m0.value(), s_m1.value(),
+                           s_m2.value(), (double)vmx[0], (double)vmx[1], (double)vmx[2], 0.0, 0.0};
     const int kinds[RED1_N] = {1, 0, 0, 0, 0, 0, 0, 1, 1, 1, 0, 0};
     block_reduce_store<RED1_N>(vals, kinds, part);
 }
@@ -643,61 +666,68 @@ void red_pass1(const Dims &d, cudaStream_t st, const T *vel, const T *vor, doubl
 
 // Rutishauser cyclic Jacobi eigenvalues of a symmetric 3x3 (jacobi.f90),
 // upper triangle a01 a02 a12, diagonal d0 d1 d2; returns max |lambda|.
-// The sweep count is bounded; *hit is set if the bound is reached.
-__device__ __forceinline__ void givens_rot(double aij, double di, double dj, double &c, double &s, double &t,
-                                           double &tau)
+// FP64: the reference's absolute tolerance 1e-15 with a bounded sweep count
+// (*hit set if the bound is reached).  FP32: the same rotations stopped at
+// FP32 resolution (relative tolerance) after at most 12 sweeps.
+template <typename A>
+__device__ __forceinline__ void givens_rot(A aij, A di, A dj, A &c, A &s, A &t, A &tau)
 {
-    const double g = 100.0 * fabs(aij);
-    const double h = dj - di;
+    const A eps = sizeof(A) == 8 ? (A)DBL_EPSILON : (A)FLT_EPSILON;
+    const A g = (A)100 * fabs(aij);
+    const A h = dj - di;
     if (fabs(h) + g == fabs(h)) {
-        t = aij / (h + copysign(DBL_EPSILON, h));
+        t = aij / (h + copysign(eps, h));
     } else {
-        const double theta = 0.5 * h / (aij + copysign(DBL_EPSILON, aij));
-        t = 1.0 / (fabs(theta) + sqrt(1.0 + theta * theta));
-        if (theta < 0.0) t = -t;
+        const A theta = (A)0.5 * h / (aij + copysign(eps, aij));
+        t = (A)1 / (fabs(theta) + sqrt((A)1 + theta * theta));
+        if (theta < (A)0) t = -t;
     }
-    c = 1.0 / sqrt(1.0 + t * t);
+    c = (A)1 / sqrt((A)1 + t * t);
     s = t * c;
-    tau = s / (1.0 + c);
+    tau = s / ((A)1 + c);
 }
 
-__device__ double jacobi_maxabs(double a00, double a01, double a02, double a11, double a12, double a22, int *hit)
+template <typename A>
+__device__ A jacobi_maxabs(A a00, A a01, A a02, A a11, A a12, A a22, int *hit)
 {
-    double A[3][3] = {{a00, a01, a02}, {0.0, a11, a12}, {0.0, 0.0, a22}};
-    double D[3] = {a00, a11, a22}, Bv[3] = {a00, a11, a22}, Z[3] = {0.0, 0.0, 0.0};
-    double sm = fabs(A[0][1]) + fabs(A[0][2]) + fabs(A[1][2]);
+    A Am[3][3] = {{a00, a01, a02}, {0, a11, a12}, {0, 0, a22}};
+    A D[3] = {a00, a11, a22}, Bv[3] = {a00, a11, a22}, Z[3] = {0, 0, 0};
+    A sm = fabs(Am[0][1]) + fabs(Am[0][2]) + fabs(Am[1][2]);
+    const bool f64 = sizeof(A) == 8;
+    const int maxsweeps = f64 ? 100 : 12;
     int sweeps = 0;
-    while (sm > 1.0e-15) {
-        if (++sweeps > 100) {
-            *hit = 1;
+    while (f64 ? (sm > (A)1.0e-15)
+               : (sm > (A)1.0e-7 * (fabs(D[0]) + fabs(D[1]) + fabs(D[2])) && sm > (A)1.0e-30)) {
+        if (++sweeps > maxsweeps) {
+            if (f64) *hit = 1;
             break;
         }
 #pragma unroll
         for (int i = 0; i < 2; ++i) {
 #pragma unroll
             for (int j = i + 1; j < 3; ++j) {
-                double c, s, t, tau;
-                givens_rot(A[i][j], D[i], D[j], c, s, t, tau);
-                double h = t * A[i][j];
+                A c, s, t, tau;
+                givens_rot<A>(Am[i][j], D[i], D[j], c, s, t, tau);
+                A h = t * Am[i][j];
                 Z[i] -= h;
                 Z[j] += h;
                 D[i] -= h;
                 D[j] += h;
-                A[i][j] = 0.0;
+                Am[i][j] = 0;
 #pragma unroll
                 for (int k = 0; k < 3; ++k) {
                     if (k < i) {
-                        const double g = A[k][i], hh = A[k][j];
-                        A[k][i] = g - s * (hh + g * tau);
-                        A[k][j] = hh + s * (g - hh * tau);
+                        const A g = Am[k][i], hh = Am[k][j];
+                        Am[k][i] = g - s * (hh + g * tau);
+                        Am[k][j] = hh + s * (g - hh * tau);
                     } else if (k > i && k < j) {
-                        const double g = A[i][k], hh = A[k][j];
-                        A[i][k] = g - s * (hh + g * tau);
-                        A[k][j] = hh + s * (g - hh * tau);
+                        const A g = Am[i][k], hh = Am[k][j];
+                        Am[i][k] = g - s * (hh + g * tau);
+                        Am[k][j] = hh + s * (g - hh * tau);
                     } else if (k > j) {
-                        const double g = A[i][k], hh = A[j][k];
-                        A[i][k] = g - s * (hh + g * tau);
-                        A[j][k] = hh + s * (g - hh * tau);
+                        const A g = Am[i][k], hh = Am[j][k];
+                        Am[i][k] = g - s * (hh + g * tau);
+                        Am[j][k] = hh + s * (g - hh * tau);
                     }
                 }
             }
@@ -705,9 +735,9 @@ __device__ double jacobi_maxabs(double a00, double a01, double a02, double a11, 
         for (int k = 0; k < 3; ++k) {
             Bv[k] += Z[k];
             D[k] = Bv[k];
-            Z[k] = 0.0;
+            Z[k] = 0;
         }
-        sm = fabs(A[0][1]) + fabs(A[0][2]) + fabs(A[1][2]);
+        sm = fabs(Am[0][1]) + fabs(Am[0][2]) + fabs(Am[1][2]);
     }
     return fmax(fmax(fabs(D[0]), fabs(D[1])), fabs(D[2]));
 }
@@ -719,35 +749,36 @@ __global__ void k_red2(Dims d, const T *__restrict__ vor, const T *__restrict__ 
                        double *part, int *flag)
 {
     const long long N = d.nfield;
-    KSum l1{0, 0}, l2{0, 0};
-    double gg = DBL_EPSILON, us = 0.0, ls = 0.0;
+    const T vr = (T)vortrms;
+    Acc<T> l1, l2;
+    T gg = sizeof(T) == 8 ? (T)DBL_EPSILON : (T)FLT_EPSILON, us = 0, ls = 0;
     int hit = 0;
     for (long long col = (long long)blockIdx.x * COLS_PER_BLOCK + threadIdx.y; col < d.ncol;
          col += (long long)gridDim.x * COLS_PER_BLOCK) {
         const long long o = col * d.P;
         for (int iz = threadIdx.x; iz <= d.nz; iz += 32) {
             const long long i = o + iz;
-            const double x = vor[i], y = vor[N + i], z = vor[2 * N + i];
+            const T x = vor[i], y = vor[N + i], z = vor[2 * N + i];
             if (iz >= 1) {
-                const double v1 = 0.5 * fabs((double)vor[i - 1] + x);
-                const double v2 = 0.5 * fabs((double)vor[N + i - 1] + y);
-                const double v3 = 0.5 * fabs((double)vor[2 * N + i - 1] + z);
-                if (v1 + v2 + v3 > vortrms) {
+                const T v1 = (T)0.5 * fabs(vor[i - 1] + x);
+                const T v2 = (T)0.5 * fabs(vor[N + i - 1] + y);
+                const T v3 = (T)0.5 * fabs(vor[2 * N + i - 1] + z);
+                if (v1 + v2 + v3 > vr) {
                     l1.add(v1 + v2 + v3);
                     l2.add(v1 * v1 + v2 * v2 + v3 * v3);
                 }
             }
-            const double dudx = g5[i], dudy = g5[N + i], dwdx = g5[2 * N + i], dvdy = g5[3 * N + i],
-                         dwdy = g5[4 * N + i];
-            const double lmax = jacobi_maxabs(dudx, dudy + 0.5 * z, dwdx + 0.5 * y, dvdy, dwdy - 0.5 * x,
-                                              -(dudx + dvdy), &hit);
+            const T dudx = g5[i], dudy = g5[N + i], dwdx = g5[2 * N + i], dvdy = g5[3 * N + i],
+                    dwdy = g5[4 * N + i];
+            const T lmax = jacobi_maxabs<T>(dudx, dudy + (T)0.5 * z, dwdx + (T)0.5 * y, dvdy,
+                                             dwdy - (T)0.5 * x, -(dudx + dvdy), &hit);
             gg = fmax(gg, lmax);
             if (iz == d.nz) us = fmax(us, lmax);
             if (iz == 0) ls = fmax(ls, lmax);
         }
     }
     if (hit) atomicExch(flag, 1);
-    double vals[RED2_N] = {l1.value(), l2.value(), gg, us, ls};
+    double vals[RED2_N] = {l1.value(), l2.value(), (double)gg, (double)us, (double)ls};
     const int kinds[RED2_N] = {0, 0, 1, 1, 1};
     block_reduce_store<RED2_N>(vals, kinds, part);
 }
@@ -857,6 +888,10 @@ void op_hyperbolic_tables(const Dims &d, cudaStream_t st, const double *k2l2, co
 INST_T(double)
 INST_T(float)
 template void op_convert<float, double>(const Dims &, cudaStream_t, const double *, float *, long long);
+template void op_v2v_ds<float, float>(const Dims &, cudaStream_t, const Deriv &, const float *, const float *,
+                                      float *);
+template void op_v2v_project<float, float>(const Dims &, cudaStream_t, const Deriv &, const double *,
+                                           const float *, const float *, float *, float *);
 template void op_convert<double, float>(const Dims &, cudaStream_t, const float *, double *, long long);
 template void op_v2v_meanflow<double>(const Dims &, cudaStream_t, const double *, const double *, const Tables &,
                                       double *, double *);

@@ -77,6 +77,10 @@ struct ps3d_gpu_ctx {
     void *phim = nullptr, *phip = nullptr, *thetam = nullptr, *thetap = nullptr, *dthetam = nullptr,
          *dthetap = nullptr, *green = nullptr;
     void *twx = nullptr, *twy = nullptr, *twz2 = nullptr;
+    // FP64 transform tables for the FP64 set-up / projection of the mixed
+    // form (aliases of the above in the FP64 form)
+    double2 *twx64 = nullptr, *twy64 = nullptr, *twz2_64 = nullptr;
+    double *phim64 = nullptr, *phip64 = nullptr;
     // per-column and per-level FP64 tables
     double *k2l2 = nullptr, *k2l2i = nullptr, *filt0 = nullptr, *vhdis = nullptr, *vdiss = nullptr;
     double *epq = nullptr, *emq = nullptr, *epq2 = nullptr, *emq2 = nullptr;
@@ -228,10 +232,46 @@ template <typename T> void state_from_T(ps3d_gpu_ctx *c, const T *src, double *s
     c->launches += 1;
 }
 
+// FP64 scratch fields for the FP64 projection: the FP64 form uses its
+// transient temporaries, the mixed form the RK accumulator svorf (free
+// outside a step)
+double *scratch64(ps3d_gpu_ctx *c, int i)
+{
+    if (c->fp64) return tmpf<double>(c, i);
+    return c->svorf + (size_t)i * c->d.nfield;
+}
+
+// Solenoidal projection of the prognostic vorticity in FP64
+// (inversion.f90:34-76): ds = B_x - A_y, es = decompose(diffz(combine(C))),
+// A = k2l2i (es_x + ds_y), B = k2l2i (es_y - ds_x), (0,0) column kept.
+void project64(ps3d_gpu_ctx *c)
+{
+    const Dims &d = c->d;
+    const long long N = d.nfield;
+    double *A = c->svor, *B = c->svor + N, *Cc = c->svor + 2 * N;
+    double *cs = scratch64(c, 0), *es = scratch64(c, 1), *ds = scratch64(c, 2);
+    op_v2v_ds<double, double>(d, c->st, c->D(), A, B, ds);
+    columns<double>(d, c->st, COL_COMBINE, Cc, cs, c->phim64, c->phip64, c->twz2_64, nullptr);
+    op_diffz<double>(d, c->st, c->dzi, cs, es);
+    columns<double>(d, c->st, COL_DECOMP, es, es, c->phim64, c->phip64, c->twz2_64, nullptr);
+    op_v2v_project<double, double>(d, c->st, c->D(), c->k2l2i, es, ds, A, B);
+    c->launches += 5;
+}
+
 // ------------------------------------------------------------------ vor2vel
-// inversion.f90:23-226
+// inversion.f90:23-226.  The FP64 form follows the reference: the
+// solenoidal projection of svor, then the physical vorticity and the
+// velocity.  The mixed form keeps svor solenoidal by construction instead
+// (svor is projected in FP64 whenever it is set from outside, and every
+// source term is projected before the stage update; the projection is
+// linear and commutes with the per-column integrating factors, so the
+// projected trajectory is the reference's), which keeps FP32 rounding out of
+// the prognostic state; vor2vel then only evaluates vor, vel and svel.
+template <typename T> int vor2vel_mixed(ps3d_gpu_ctx *c);
+
 template <typename T> int vor2vel(ps3d_gpu_ctx *c)
 {
+    if (sizeof(T) == sizeof(float)) return vor2vel_mixed<T>(c);
     const Dims &d = c->d;
     const long long N = d.nfield;
     double *A = c->svor, *B = c->svor + N, *Cc = c->svor + 2 * N;
@@ -270,6 +310,57 @@ template <typename T> int vor2vel(ps3d_gpu_ctx *c)
     return check(c, "vor2vel");
 }
 
+template <typename T> int vor2vel_mixed(ps3d_gpu_ctx *c)
+{
+    const Dims &d = c->d;
+    const long long N = d.nfield;
+    const double *A = c->svor, *B = c->svor + N, *Cc = c->svor + 2 * N;
+    T *cs = tmpf<T>(c, 0), *es = tmpf<T>(c, 1), *ds = tmpf<T>(c, 2), *bs = tmpf<T>(c, 3), *dsg = tmpf<T>(c, 4),
+      *as = tmpf<T>(c, 5);
+    T *vor = tf<T>(c->vor), *vel = tf<T>(c->vel), *svel = tf<T>(c->svel);
+    const Deriv D = c->D();
+    auto colin = [&](int mode, const double *in, T *out) {
+        columns_in<T, double>(d, c->st, mode, in, out, tf<T>(c->phim), tf<T>(c->phip), tf<CT<T>>(c->twz2),
+                              &c->probe);
+        c->launches += 1;
+    };
+    // vorticity in physical space (field_combine_physical x3)
+    colin(COL_COMBINE, A, bs);
+    xyi<T>(c, bs, vor);
+    colin(COL_COMBINE, B, bs);
+    xyi<T>(c, bs, vor + N);
+    colin(COL_COMBINE, Cc, cs);
+    xyi<T>(c, cs, vor + 2 * N);
+    // vertical velocity, mean flow, u, v (inversion.f90:86-213)
+    op_v2v_wsrc<T, double>(d, c->st, D, A, B, ds);
+    op_v2v_wprep<T>(d, c->st, ds, tf<T>(c->thetam), tf<T>(c->thetap), tf<T>(c->dthetam), tf<T>(c->dthetap),
+                    tf<T>(c->green), c->rkz, bs, es, dsg, as);
+    col<T>(c, COL_DCT, as, as);
+    col<T>(c, COL_DST, dsg, dsg);
+    op_v2v_wfinish<T>(d, c->st, dsg, bs, as, svel + 2 * N, es);
+    op_v2v_meanflow<double>(d, c->st, A, B, c->tables(), c->ubar, c->vbar);
+    op_v2v_uv<T>(d, c->st, D, c->k2l2i, es, cs, c->ubar, c->vbar, svel, svel + N);
+    c->launches += 5;
+    for (int k = 0; k < 3; ++k) xyi<T>(c, svel + k * N, vel + k * N);
+    return check(c, "vor2vel");
+}
+
+// Projection of a source term (mixed form): the same operator as the
+// vor2vel projection, applied to svorts in FP32.
+template <typename T> void project_source(ps3d_gpu_ctx *c)
+{
+    const Dims &d = c->d;
+    const long long N = d.nfield;
+    T *S1 = tf<T>(c->svorts), *S2 = S1 + N, *S3 = S1 + 2 * N;
+    T *cs = tmpf<T>(c, 0), *es = tmpf<T>(c, 1), *ds = tmpf<T>(c, 2);
+    op_v2v_ds<T, T>(d, c->st, c->D(), S1, S2, ds);
+    col<T>(c, COL_COMBINE, S3, cs);
+    op_diffz<T>(d, c->st, c->dzi, cs, es);
+    col<T>(c, COL_DECOMP, es, es);
+    op_v2v_project<T, T>(d, c->st, c->D(), c->k2l2i, es, ds, S1, S2);
+    c->launches += 3;
+}
+
 // ------------------------------------------------------------------- source
 // vorticity_tendency (inversion.f90:298-371)
 template <typename T> int source(ps3d_gpu_ctx *c)
@@ -294,6 +385,7 @@ template <typename T> int source(ps3d_gpu_ctx *c)
     }
     op_svorts<T>(d, c->st, c->D(), r, q, p, gq, gp, svorts, svorts + N, svorts + 2 * N);
     c->launches += 1;
+    if (sizeof(T) == sizeof(float)) project_source<T>(c);
     return check(c, "source");
 }
 
@@ -457,15 +549,20 @@ template <typename T> int step_cn2(ps3d_gpu_ctx *c, double *t, double dt)
     T *sv = tf<T>(c->svorts);
     if (c->cfg.hold_source)
         cudaMemcpyAsync(c->held, c->svorts, 3 * d.nfield * sizeof(T), cudaMemcpyDeviceToDevice, c->st);
+    // the mixed form re-projects in FP64 after each update: the 3-D filter of
+    // cn2 does not commute with the projection
+    const bool mixed = sizeof(T) == sizeof(float);
     op_cn2_init<T>(d, c->st, c->vortsm, c->svor, sv, dt2);
     op_cn2_update<T>(d, c->st, c->svor, c->vortsm, sv, c->filt0, c->fz, c->vdiss, dt2);
     op_mean_fix(d, c->st, c->svor, c->dstsum, c->fnzi, c->ini, nullptr, 1);
+    if (mixed) project64(c);
     c->launches += 7;
     for (int it = 0; it < 2; ++it) {
         int rc = rhs_or_hold<T>(c);
         if (rc) return rc;
         op_cn2_update<T>(d, c->st, c->svor, c->vortsm, sv, c->filt0, c->fz, c->vdiss, dt2);
         op_mean_fix(d, c->st, c->svor, c->dstsum, c->fnzi, c->ini, nullptr, 1);
+        if (mixed) project64(c);
         c->launches += 4;
     }
     *t += dt;
@@ -497,13 +594,15 @@ template <typename T> int setup_fields(ps3d_gpu_ctx *c, const double *vor_phys, 
 {
     const Dims &d = c->d;
     const long long N = d.nfield;
-    int rc = upload(c, vor_phys, 3, c->vor, c->fp64);
+    // field_decompose_physical x3 in FP64 for both forms (the initial state
+    // carries no FP32 rounding)
+    int rc = upload(c, vor_phys, 3, c->svori, true);
     if (rc) return rc;
-    T *w = tmpf<T>(c, 0);
     for (int k = 0; k < 3; ++k) {
-        xyf<T>(c, tf<T>(c->vor) + k * N, w);
-        col<T>(c, COL_DECOMP, w, w);
-        state_from_T<T>(c, w, c->svor + k * N);
+        xy_forward<double>(d, c->st, c->svori + k * N, c->svori + k * N, c->twx64, c->twy64, nullptr);
+        columns<double>(d, c->st, COL_DECOMP, c->svori + k * N, c->svor + k * N, c->phim64, c->phip64,
+                        c->twz2_64, nullptr);
+        c->launches += 3;
     }
     if (pert) {
         rc = upload(c, pert, 3, c->svori, true);  // svori is free scratch here
@@ -515,6 +614,7 @@ template <typename T> int setup_fields(ps3d_gpu_ctx *c, const double *vor_phys, 
     cudaMemcpyAsync(c->ini, c->savg, 2 * sizeof(double), cudaMemcpyDeviceToDevice, c->st);
     cudaMemcpyAsync(c->ini_vor_mean, c->savg, 2 * sizeof(double), cudaMemcpyDeviceToHost, c->st);
     c->launches += 1;
+    if (sizeof(T) == sizeof(float)) project64(c);
     rc = vor2vel<T>(c);
     if (rc) return rc;
     double r1[RED1_N];
@@ -702,7 +802,10 @@ template <typename T> int allocate_fields(ps3d_gpu_ctx *c)
               dalloc(c, &c->dthetam, fb) && dalloc(c, &c->dthetap, fb) && dalloc(c, &c->green, fb);
     if (ok && c->cfg.stepper == PS3D_CN2) ok = dalloc(c, &c->vortsm, 3 * f64);
     if (ok && c->cfg.hold_source) ok = dalloc(c, &c->held, 3 * fb);
-    if (ok && !c->fp64) ok = dalloc(c, &c->stage64, f64);
+    if (ok && !c->fp64)
+        ok = dalloc(c, &c->stage64, f64) && dalloc(c, &c->phim64, f64) && dalloc(c, &c->phip64, f64) &&
+             dalloc(c, &c->twx64, d.nx * sizeof(double2)) && dalloc(c, &c->twy64, d.ny * sizeof(double2)) &&
+             dalloc(c, &c->twz2_64, 2 * d.nz * sizeof(double2));
     const size_t P2 = (size_t)d.ncol * sizeof(double), Z = (size_t)(d.nz + 1) * sizeof(double);
     ok = ok && dalloc(c, &c->twx, d.nx * sizeof(CT<T>)) && dalloc(c, &c->twy, d.ny * sizeof(CT<T>)) &&
          dalloc(c, &c->twz2, 2 * d.nz * sizeof(CT<T>));
@@ -721,11 +824,30 @@ template <typename T> int allocate_fields(ps3d_gpu_ctx *c)
     twiddles<T>(c, c->twx, d.nx);
     twiddles<T>(c, c->twy, d.ny);
     twiddles<T>(c, c->twz2, 2 * d.nz);
+    if (c->fp64) {
+        c->twx64 = tf<double2>(c->twx);
+        c->twy64 = tf<double2>(c->twy);
+        c->twz2_64 = tf<double2>(c->twz2);
+        c->phim64 = tf<double>(c->phim);
+        c->phip64 = tf<double>(c->phip);
+    } else {
+        twiddles<double>(c, c->twx64, d.nx);
+        twiddles<double>(c, c->twy64, d.ny);
+        twiddles<double>(c, c->twz2_64, 2 * d.nz);
+    }
     host_tables(c);
     op_hyperbolic_tables<T>(d, c->st, c->k2l2, c->k2l2i, c->rkz, c->zm, c->zp, c->cfg.extent[2], tf<T>(c->phim),
                             tf<T>(c->phip), tf<T>(c->thetam), tf<T>(c->thetap), tf<T>(c->dthetam),
                             tf<T>(c->dthetap), tf<T>(c->green));
     c->launches += 1;
+    if (!c->fp64) {
+        // FP64 harmonic functions for the FP64 set-up and projection; the
+        // remaining FP64 outputs go to scratch (svori, svorf)
+        double *s = c->svori, *s2 = c->svorf;
+        op_hyperbolic_tables<double>(d, c->st, c->k2l2, c->k2l2i, c->rkz, c->zm, c->zp, c->cfg.extent[2],
+                                     c->phim64, c->phip64, s, s + N, s + 2 * N, s2, s2 + N);
+        c->launches += 1;
+    }
     return sync_check(c, "create");
 }
 
@@ -845,7 +967,10 @@ int ps3d_gpu_set_field(ps3d_gpu_ctx *c, int which, const double *host)
     if (rc) return rc;
     if (!host) return PS3D_ERR_INVALID_ARG;
     switch (which) {
-    case PS3D_FIELD_SVOR: rc = upload(c, host, 3, c->svor, true); break;
+    case PS3D_FIELD_SVOR:
+        rc = upload(c, host, 3, c->svor, true);
+        if (!rc && !c->fp64) project64(c);
+        break;
     case PS3D_FIELD_VOR: rc = upload(c, host, 3, c->vor, c->fp64); break;
     case PS3D_FIELD_VEL: rc = upload(c, host, 3, c->vel, c->fp64); break;
     case PS3D_FIELD_SVEL: rc = upload(c, host, 3, c->svel, c->fp64); break;
@@ -1037,6 +1162,7 @@ int ps3d_gpu_advance_host(ps3d_gpu_ctx *c, double *svor, double *t, ps3d_gpu_dia
     if (!svor || !t) return PS3D_ERR_INVALID_ARG;
     rc = upload(c, svor, 3, c->svor, true);
     if (rc) return rc;
+    if (!c->fp64) project64(c);
     rc = ps3d_gpu_advance(c, t, 1, diag);
     if (rc) return rc;
     return download(c, c->svor, true, 3, svor);

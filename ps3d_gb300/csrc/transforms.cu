@@ -154,8 +154,8 @@ void xy_inverse(const Dims &d, cudaStream_t st, const T *in, T *out, const typen
 //       COL_DCT      plain dct of rows 0..nz
 //       COL_DECOMP   rows 1..nz-1 -= f0*phim + fnz*phip, then dst; rows 0, nz kept
 //       COL_COMBINE  dst of rows 1..nz-1, then += f0*phim + fnz*phip; rows 0, nz kept
-template <typename T, int MODE>
-__global__ void __launch_bounds__(256) k_columns(const T *__restrict__ in, T *__restrict__ out, int nz,
+template <typename T, int MODE, typename TIN>
+__global__ void __launch_bounds__(256) k_columns(const TIN *__restrict__ in, T *__restrict__ out, int nz,
                                                  int P, int logB, const T *__restrict__ phim,
                                                  const T *__restrict__ phip,
                                                  const typename cplx<T>::type *__restrict__ tw)
@@ -172,8 +172,8 @@ __global__ void __launch_bounds__(256) k_columns(const T *__restrict__ in, T *__
     // boundary values of the 2B columns
     for (int e = threadIdx.x; e < 2 * B; e += blockDim.x) {
         const long long c = col0 + e;
-        bnd[2 * e] = in[c * P];
-        bnd[2 * e + 1] = in[c * P + nz];
+        bnd[2 * e] = (T)in[c * P];
+        bnd[2 * e + 1] = (T)in[c * P + nz];
     }
     __syncthreads();
     // load the 2B columns into the extension buffer (column 2p -> .x, 2p+1 -> .y)
@@ -181,7 +181,7 @@ __global__ void __launch_bounds__(256) k_columns(const T *__restrict__ in, T *__
     for (int e = threadIdx.x; e < 2 * B * nrow; e += blockDim.x) {
         const int cl = e / nrow, iz = e - cl * nrow;
         const int p = cl >> 1, comp = cl & 1;
-        T v = in[(col0 + cl) * P + iz];
+        T v = (T)in[(col0 + cl) * P + iz];
         if (MODE == COL_DECOMP && iz > 0 && iz < nz) {
             const long long q = (col0 + cl) * P + iz;
             v = v - (bnd[2 * cl] * phim[q] + bnd[2 * cl + 1] * phip[q]);
@@ -215,7 +215,7 @@ __global__ void __launch_bounds__(256) k_columns(const T *__restrict__ in, T *__
         } else {
             if (iz == 0) {
                 v = bnd[2 * cl];
-                if (MODE == COL_DST) v = in[q];
+                if (MODE == COL_DST) v = (T)in[q];
             } else if (iz == nz) {
                 v = (MODE == COL_DST) ? (T)0 : bnd[2 * cl + 1];
             } else {
@@ -236,9 +236,9 @@ int column_lanes(int nz)
     return B;
 }
 
-template <typename T>
-void columns(const Dims &d, cudaStream_t st, int mode, const T *in, T *out, const T *phim,
-             const T *phip, const typename cplx<T>::type *twz2, Probe *pr)
+template <typename T, typename TIN>
+void columns_in(const Dims &d, cudaStream_t st, int mode, const TIN *in, T *out, const T *phim,
+                const T *phip, const typename cplx<T>::type *twz2, Probe *pr)
 {
     if (pr) pr->begin(PROBE_COLUMNS, st);
     int B = column_lanes<T>(d.nz);
@@ -249,19 +249,26 @@ void columns(const Dims &d, cudaStream_t st, int mode, const T *in, T *out, cons
     const size_t sm = 2 * (size_t)(2 * d.nz) * B * sizeof(typename cplx<T>::type) + 4 * B * sizeof(T);
     switch (mode) {
     case COL_DST:
-        k_columns<T, COL_DST><<<grid, 256, sm, st>>>(in, out, d.nz, d.P, logB, phim, phip, twz2);
+        k_columns<T, COL_DST, TIN><<<grid, 256, sm, st>>>(in, out, d.nz, d.P, logB, phim, phip, twz2);
         break;
     case COL_DCT:
-        k_columns<T, COL_DCT><<<grid, 256, sm, st>>>(in, out, d.nz, d.P, logB, phim, phip, twz2);
+        k_columns<T, COL_DCT, TIN><<<grid, 256, sm, st>>>(in, out, d.nz, d.P, logB, phim, phip, twz2);
         break;
     case COL_DECOMP:
-        k_columns<T, COL_DECOMP><<<grid, 256, sm, st>>>(in, out, d.nz, d.P, logB, phim, phip, twz2);
+        k_columns<T, COL_DECOMP, TIN><<<grid, 256, sm, st>>>(in, out, d.nz, d.P, logB, phim, phip, twz2);
         break;
     default:
-        k_columns<T, COL_COMBINE><<<grid, 256, sm, st>>>(in, out, d.nz, d.P, logB, phim, phip, twz2);
+        k_columns<T, COL_COMBINE, TIN><<<grid, 256, sm, st>>>(in, out, d.nz, d.P, logB, phim, phip, twz2);
         break;
     }
     if (pr) pr->end(PROBE_COLUMNS, st, pass_bytes<T>(d));
+}
+
+template <typename T>
+void columns(const Dims &d, cudaStream_t st, int mode, const T *in, T *out, const T *phim,
+             const T *phip, const typename cplx<T>::type *twz2, Probe *pr)
+{
+    columns_in<T, T>(d, st, mode, in, out, phim, phip, twz2, pr);
 }
 
 size_t lines_smem_bytes(int n, bool fp64)
@@ -276,21 +283,28 @@ size_t columns_smem_bytes(int nz, bool fp64)
     return 2 * (size_t)(2 * nz) * column_lanes<float>(nz) * sizeof(float2) + 4 * 16 * sizeof(float);
 }
 
+template <typename T, typename TIN>
+static void set_col_attrs()
+{
+    cudaFuncSetAttribute(k_columns<T, COL_DST, TIN>, cudaFuncAttributeMaxDynamicSharedMemorySize, 100 * 1024);
+    cudaFuncSetAttribute(k_columns<T, COL_DCT, TIN>, cudaFuncAttributeMaxDynamicSharedMemorySize, 100 * 1024);
+    cudaFuncSetAttribute(k_columns<T, COL_DECOMP, TIN>, cudaFuncAttributeMaxDynamicSharedMemorySize, 100 * 1024);
+    cudaFuncSetAttribute(k_columns<T, COL_COMBINE, TIN>, cudaFuncAttributeMaxDynamicSharedMemorySize, 100 * 1024);
+}
+
 template <typename T>
 static void set_smem_attrs()
 {
     cudaFuncSetAttribute(k_lines<T, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, 100 * 1024);
     cudaFuncSetAttribute(k_lines<T, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, 100 * 1024);
-    cudaFuncSetAttribute(k_columns<T, COL_DST>, cudaFuncAttributeMaxDynamicSharedMemorySize, 100 * 1024);
-    cudaFuncSetAttribute(k_columns<T, COL_DCT>, cudaFuncAttributeMaxDynamicSharedMemorySize, 100 * 1024);
-    cudaFuncSetAttribute(k_columns<T, COL_DECOMP>, cudaFuncAttributeMaxDynamicSharedMemorySize, 100 * 1024);
-    cudaFuncSetAttribute(k_columns<T, COL_COMBINE>, cudaFuncAttributeMaxDynamicSharedMemorySize, 100 * 1024);
+    set_col_attrs<T, T>();
 }
 
 void transforms_init()
 {
     set_smem_attrs<double>();
     set_smem_attrs<float>();
+    set_col_attrs<float, double>();
 }
 
 template void xy_forward<double>(const Dims &, cudaStream_t, const double *, double *, const double2 *,
@@ -305,5 +319,7 @@ template void columns<double>(const Dims &, cudaStream_t, int, const double *, d
                               const double *, const double2 *, Probe *);
 template void columns<float>(const Dims &, cudaStream_t, int, const float *, float *, const float *,
                              const float *, const float2 *, Probe *);
+template void columns_in<float, double>(const Dims &, cudaStream_t, int, const double *, float *, const float *,
+                                       const float *, const float2 *, Probe *);
 
 }  // namespace ps3d
