@@ -217,6 +217,7 @@ def run_gpu(args, rank, world, dist):
     # dominant kernel probe inside real steps (same stream, CUDA events)
     probe_steps = max(1, min(3, args.steps))
     best = None
+    probes = []
     for kind, name in ((1, "k_lines (y)"), (2, "k_lines (x)"), (3, "k_columns")):
         gm.probe(kind)
         t_m, _ = gm.time_advance(t_m, probe_steps)
@@ -225,6 +226,7 @@ def run_gpu(args, rank, world, dist):
         share = kms / (ms / args.steps * probe_steps) if ms > 0 else 0.0
         rec = {"kernel": name, "launches_per_step": nl / probe_steps, "ms_per_launch": kms / max(nl, 1),
                "bytes_per_launch": kbytes / max(nl, 1), "share_of_step": share}
+        probes.append(rec)
         if best is None or kms > best[1]:
             best = (rec, kms)
     peak, peak_kind = peaks()
@@ -233,7 +235,8 @@ def run_gpu(args, rank, world, dist):
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                 "frac": achieved / peak, "traffic": None, "kernel": krec["kernel"],
                 "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured" else peak_kind,
-                "kernel_share_of_step": krec["share_of_step"]}
+                "kernel_share_of_step": krec["share_of_step"],
+                "probes": probes}
     svor_mixed_steps = args.warmup + args.steps + 3 * probe_steps
 
     # ---- FP64 form: timing and reference for the mixed error ------------

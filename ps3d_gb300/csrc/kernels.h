@@ -52,6 +52,12 @@ void xy_inverse(const Dims &d, cudaStream_t st, const T *in, T *out, const typen
 template <typename T>
 void columns(const Dims &d, cudaStream_t st, int mode, const T *in, T *out, const T *phim,
              const T *phip, const typename cplx<T>::type *twz2, Probe *pr);
+// FP32 warp-per-column-pair transforms (columns32.cu), nz = 32..512
+bool col32_supported(int nz);
+void columns32_init();
+template <typename TIN>
+void columns32(const Dims &d, cudaStream_t st, int mode, const TIN *in, float *out, const double *k2l2, float dz,
+               float Lz, const float2 *twL, Probe *pr);
 // column transform of an FP64 input field into a T field (mixed form)
 template <typename T, typename TIN>
 void columns_in(const Dims &d, cudaStream_t st, int mode, const TIN *in, T *out, const T *phim,

@@ -208,11 +208,22 @@ template <typename T> void xyi(ps3d_gpu_ctx *c, const T *in, T *out)
     xy_inverse<T>(c->d, c->st, in, out, tf<CT<T>>(c->twx), tf<CT<T>>(c->twy), &c->probe);
     c->launches += NL_XY;
 }
-template <typename T> void col(ps3d_gpu_ctx *c, int mode, const T *in, T *out)
+template <typename T, typename TIN> void col_any(ps3d_gpu_ctx *c, int mode, const TIN *in, T *out)
 {
-    columns<T>(c->d, c->st, mode, in, out, tf<T>(c->phim), tf<T>(c->phip), tf<CT<T>>(c->twz2), &c->probe);
+    if (sizeof(T) == sizeof(float) && col32_supported(c->d.nz)) {
+        columns32<TIN>(c->d, c->st, mode, in, reinterpret_cast<float *>(out), c->k2l2, (float)c->dx[2],
+                       (float)c->cfg.extent[2], tf<float2>(c->twz2), &c->probe);
+    } else if (sizeof(TIN) == sizeof(T)) {
+        columns<T>(c->d, c->st, mode, reinterpret_cast<const T *>(in), out, tf<T>(c->phim), tf<T>(c->phip),
+                   tf<CT<T>>(c->twz2), &c->probe);
+    } else {
+        columns_in<float, double>(c->d, c->st, mode, reinterpret_cast<const double *>(in),
+                                  reinterpret_cast<float *>(out), tf<float>(c->phim), tf<float>(c->phip),
+                                  tf<float2>(c->twz2), &c->probe);
+    }
     c->launches += NL_COL;
 }
+template <typename T> void col(ps3d_gpu_ctx *c, int mode, const T *in, T *out) { col_any<T, T>(c, mode, in, out); }
 // a T view of an FP64 state component (copy for the mixed form)
 template <typename T> const T *state_as_T(ps3d_gpu_ctx *c, const double *s, T *scratch)
 {
@@ -319,11 +330,7 @@ template <typename T> int vor2vel_mixed(ps3d_gpu_ctx *c)
       *as = tmpf<T>(c, 5);
     T *vor = tf<T>(c->vor), *vel = tf<T>(c->vel), *svel = tf<T>(c->svel);
     const Deriv D = c->D();
-    auto colin = [&](int mode, const double *in, T *out) {
-        columns_in<T, double>(d, c->st, mode, in, out, tf<T>(c->phim), tf<T>(c->phip), tf<CT<T>>(c->twz2),
-                              &c->probe);
-        c->launches += 1;
-    };
+    auto colin = [&](int mode, const double *in, T *out) { col_any<T, double>(c, mode, in, out); };
     // vorticity in physical space (field_combine_physical x3)
     colin(COL_COMBINE, A, bs);
     xyi<T>(c, bs, vor);
@@ -918,6 +925,7 @@ int ps3d_gpu_create(const ps3d_gpu_config *cfg, ps3d_gpu_ctx **out)
     c->fp64 = cfg->precision == PS3D_PRECISION_FP64;
     cudaSetDevice(cfg->device);
     transforms_init();
+    columns32_init();
     cudaStreamCreateWithFlags(&c->st, cudaStreamNonBlocking);
     cudaEventCreate(&c->ev0);
     cudaEventCreate(&c->ev1);

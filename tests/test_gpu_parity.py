@@ -226,3 +226,22 @@ def test_advance_host_equals_resident_advance():
         t_b, _ = b.advance_host(host, t_b)
     assert np.array_equal(a.get("svor"), host)
     assert t_a == t_b
+
+
+MIXED_OP_TOL = 2.0e-6
+
+
+@pytest.mark.parametrize("nz", [16, 32, 64, 128, 256, 512])
+@pytest.mark.parametrize("op", ["fftsine", "fftcosine", "decompose_semi_spectral", "combine_semi_spectral",
+                                "fftxyp2s", "fftxys2p", "decompose_physical", "combine_physical",
+                                "central_diffz", "diffx", "diffy"])
+def test_mixed_field_operators_match_oracle(nz, op):
+    """FP32 operators of the mixed form (warp-per-column-pair z transforms
+    for nz = 32..512, shared-memory Stockham otherwise) against the FP64
+    oracle, relative L2 within 2e-6."""
+    grid = (16, 8, nz, [0.0, 0.0, -0.5], [2 * np.pi, 1.0, 1.0])
+    o = oracle.Oracle(*grid)
+    g = Ps3dGpu(*grid, precision="mixed")
+    f = np.random.default_rng(11).standard_normal(o.shape)
+    err = rel_l2(getattr(g, op)(f), getattr(o, op)(f))
+    assert err < MIXED_OP_TOL, (op, nz, err)
