@@ -184,6 +184,26 @@ int ps3d_gpu_synchronize(ps3d_gpu_ctx *ctx);
 int ps3d_gpu_probe(ps3d_gpu_ctx *ctx, int kind);
 int ps3d_gpu_probe_result(ps3d_gpu_ctx *ctx, double *total_ms, long long *launches, double *bytes);
 
+/* ---- energy series without device allocation ---------------------------
+ * No counterpart in the reference.  For callers that keep vel and vor in
+ * device arrays they manage themselves and cannot let the library allocate
+ * (a device-resident CUDA Fortran/OpenACC time loop, a fixed device-memory
+ * budget, or code that must not call cudaMalloc/cudaFree because they
+ * synchronise the device).  Computes the kinetic energy, enstrophy and
+ * helicity of ps3d_gpu_energy_series from caller-owned FP64 device fields:
+ * component c, level iz, column (iy, ix) at c*comp_stride + iz +
+ * pitch*(iy + ny*ix), pitch >= nz+1 (nz+1 is the reference layout).  Writes
+ * out[0..2] (device memory) on `stream` (a cudaStream_t, NULL for the legacy
+ * default stream) and returns without synchronising.
+ * Scratch: a fixed array in the library's device image (about 6 MB per GPU
+ * that loads the library), so nx*ny may not exceed 524288 (returns
+ * PS3D_ERR_UNSUPPORTED_SIZE beyond that).  The first call on a device looks
+ * up that array's address (cudaGetSymbolAddress) and should therefore come
+ * before any stream capture.  All calls share the array: calls that overlap
+ * on the GPU race.  No context is needed and nothing is allocated. */
+int ps3d_gpu_energy_series_noalloc(const double *vel, const double *vor, int nx, int ny, int nz,
+                                   long long pitch, long long comp_stride, void *stream, double *out);
+
 #ifdef __cplusplus
 }
 #endif

@@ -897,3 +897,83 @@ template void op_v2v_meanflow<double>(const Dims &, cudaStream_t, const double *
                                       double *, double *);
 
 }  // namespace ps3d
+
+// ======================================================================
+// Energy series without any device allocation.
+//
+// Some callers cannot let this library allocate device memory: a driver
+// that already keeps vel and vor resident in device arrays it manages itself
+// (a CUDA Fortran or OpenACC port of the reference's time loop), code running
+// under a fixed device-memory budget, or a loop that must not call
+// cudaMalloc/cudaFree because those synchronise the whole device.  For them
+// ps3d_gpu_energy_series_noalloc runs the same reduction kernels as
+// ps3d_gpu_energy_series, with the per-block partial sums kept in the
+// file-scope array below instead of in a context buffer.
+//
+// The array lives in every GPU that loads the library, for the life of the
+// process.  It holds the partials of at most NOALLOC_MAX_BLOCKS blocks (one
+// block per 8 columns), so nx*ny is limited to 8*NOALLOC_MAX_BLOCKS.  All
+// calls share it: every call overwrites the entries it uses before reading
+// them (nothing has to start at zero), and two calls that overlap on the GPU
+// (for example on two streams at once) race on it.
+// ======================================================================
+namespace ps3d {
+constexpr int NOALLOC_MAX_BLOCKS = 65536;
+static __device__ __align__(256) double g_noalloc_scratch[(size_t)NOALLOC_MAX_BLOCKS * RED1_N + 2 * RED1_N];
+
+__global__ void k_noalloc_energy_out(const double *res, double ncelli, double *out)
+{
+    if (threadIdx.x == 0 && blockIdx.x == 0) {
+        out[0] = 0.5 * res[2] * ncelli;  // kinetic energy
+        out[1] = 0.5 * res[1] * ncelli;  // enstrophy
+        out[2] = res[3] * ncelli;        // helicity
+    }
+}
+}  // namespace ps3d
+
+extern "C" int ps3d_gpu_energy_series_noalloc(const double *vel, const double *vor, int nx, int ny, int nz,
+                                              long long pitch, long long comp_stride, void *stream, double *out)
+{
+    using namespace ps3d;
+    if (!vel || !vor || !out || nx < 1 || ny < 1 || nz < 2 || pitch < nz + 1 ||
+        comp_stride < pitch * (long long)nx * ny)
+        return 1;  // PS3D_ERR_INVALID_ARG
+    const long long ncol = (long long)nx * ny;
+    const long long nblocks = (ncol + COLS_PER_BLOCK - 1) / COLS_PER_BLOCK;
+    if (nblocks > NOALLOC_MAX_BLOCKS) return 2;  // PS3D_ERR_UNSUPPORTED_SIZE: nx*ny above the scratch capacity
+    int dev = -1;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) {
+        cudaGetLastError();
+        return 8;  // PS3D_ERR_NO_DEVICE
+    }
+    // one-time set-up per device (on the first call made with that device
+    // current): the host-side address of the scratch array
+    static double *scratch_addr[64] = {nullptr};
+    if (!scratch_addr[dev]) {
+        double *p = nullptr;
+        if (cudaGetSymbolAddress((void **)&p, g_noalloc_scratch) != cudaSuccess || !p) {
+            cudaGetLastError();
+            return 3;  // PS3D_ERR_CUDA
+        }
+        scratch_addr[dev] = p;
+    }
+    double *part = scratch_addr[dev];
+    double *result = part + (size_t)NOALLOC_MAX_BLOCKS * RED1_N;
+    int *kinds = nullptr;
+    if (cudaGetSymbolAddress((void **)&kinds, c_kinds1) != cudaSuccess) {
+        cudaGetLastError();
+        return 3;
+    }
+    Dims d;
+    d.nx = nx;
+    d.ny = ny;
+    d.nz = nz;
+    d.P = (int)pitch;
+    d.ncol = ncol;
+    d.nfield = comp_stride;
+    cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+    k_red1<double><<<(unsigned)nblocks, COL_BLOCK, 0, st>>>(d, vel, vor, part);
+    k_finish<RED1_N><<<1, dim3(32, RED1_N), 0, st>>>(part, (int)nblocks, kinds, result);
+    k_noalloc_energy_out<<<1, 32, 0, st>>>(result, 1.0 / ((double)nx * (double)ny * (double)nz), out);
+    return cudaGetLastError() == cudaSuccess ? 0 : 3;
+}
