@@ -34,23 +34,57 @@ __device__ __forceinline__ float2 fmulc(float2 a, float2 b)
     return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
 }
 
-// harmonic functions of one (kx, ky) column at level iz (FP32)
+// harmonic functions of one (kx, ky) column at level iz (FP32):
+// ep = exp(-kl zp) = 2^(a iz), em = exp(-kl zm) = 2^(c - a iz) with
+// a = -kl dz log2(e), c = -kl Lz log2(e)
 struct Harm {
-    float kl, ef, div, dz, Lz;
+    float a, c, ef, div, dz, Lz;
     bool mean;  // (0,0) column: linear functions
+    __device__ static Harm make(float kl, float dz, float Lz, bool mean)
+    {
+        const float l2e = 1.4426950408889634f;
+        Harm h;
+        h.a = -kl * dz * l2e;
+        h.c = -kl * Lz * l2e;
+        h.ef = exp2f(h.c);
+        h.div = 1.0f / (1.0f - h.ef * h.ef);
+        h.dz = dz;
+        h.Lz = Lz;
+        h.mean = mean;
+        return h;
+    }
     __device__ void at(int iz, float &pm, float &pp) const
     {
-        const float zp = dz * (float)iz, zm = Lz - zp;
         if (mean) {
+            const float zp = dz * (float)iz, zm = Lz - zp;
             pm = zm / Lz;
             pp = zp / Lz;
         } else {
-            const float ep = expf(-kl * zp), em = expf(-kl * zm);
+            const float t = a * (float)iz;
+            const float ep = exp2f(t), em = exp2f(c - t);
             pm = div * (ep - ef * em);
             pp = div * (em - ef * ep);
         }
     }
 };
+
+// in-register DIF FFT of length M (output in bit-reversed order)
+template <int M> __device__ __forceinline__ void dif_regs(float2 *v)
+{
+#pragma unroll
+    for (int h = M / 2; h >= 1; h >>= 1) {
+#pragma unroll
+        for (int s0 = 0; s0 < M; s0 += 2 * h) {
+#pragma unroll
+            for (int i = 0; i < h; ++i) {
+                const float2 a = v[s0 + i], b = v[s0 + i + h];
+                v[s0 + i] = make_float2(a.x + b.x, a.y + b.y);
+                const float2 d = make_float2(a.x - b.x, a.y - b.y);
+                v[s0 + i + h] = (i == 0) ? d : fmulc(d, c_w32[i * (16 / h)]);
+            }
+        }
+    }
+}
 
 template <int MODE, int M, typename TIN>
 __global__ void __launch_bounds__(256) k_col32(const TIN *__restrict__ in, float *__restrict__ out, int nz, int P,
@@ -83,58 +117,89 @@ __global__ void __launch_bounds__(256) k_col32(const TIN *__restrict__ in, float
             fAn = (float)in[oA + nz];
             fB0 = (float)in[oB];
             fBn = (float)in[oB + nz];
-            const float kA = sqrtf((float)k2l2[cA]), kB = sqrtf((float)k2l2[cB]);
-            const float eA = expf(-kA * Lz), eB = expf(-kB * Lz);
-            hA = Harm{kA, eA, 1.0f / (1.0f - eA * eA), dz, Lz, cA == 0};
-            hB = Harm{kB, eB, 1.0f / (1.0f - eB * eB), dz, Lz, cB == 0};
+            hA = Harm::make(sqrtf((float)k2l2[cA]), dz, Lz, cA == 0);
+            hB = Harm::make(sqrtf((float)k2l2[cB]), dz, Lz, cB == 0);
         }
-        // ---- load the extension
+        // ---- load the extension (raw loads first)
         float2 v[M];
 #pragma unroll
         for (int m = 0; m < M; ++m) {
             const int j = lane + 32 * m;
+            const int jj = j <= nz ? j : L - j;
             float a = 0.f, b = 0.f;
-            if (MODE == COL_DCT) {
-                const int jj = j <= nz ? j : L - j;
+            if (MODE == COL_DCT || (j != 0 && j != nz)) {
                 a = (float)in[oA + jj];
                 b = (float)in[oB + jj];
-            } else if (j != 0 && j != nz) {
-                const int jj = j < nz ? j : L - j;
-                a = (float)in[oA + jj];
-                b = (float)in[oB + jj];
-                if (MODE == COL_DECOMP) {
-                    float pm, pp;
-                    hA.at(jj, pm, pp);
-                    a = a - (fA0 * pm + fAn * pp);
-                    hB.at(jj, pm, pp);
-                    b = b - (fB0 * pm + fBn * pp);
-                }
-                if (j > nz) {
-                    a = -a;
-                    b = -b;
-                }
             }
             v[m] = make_float2(a, b);
         }
-        // ---- M-point DIF FFT in registers (output in bit-reversed order)
+        if (MODE != COL_DCT) {
 #pragma unroll
-        for (int h = M / 2; h >= 1; h >>= 1) {
-#pragma unroll
-            for (int s0 = 0; s0 < M; s0 += 2 * h) {
-#pragma unroll
-                for (int i = 0; i < h; ++i) {
-                    const float2 a = v[s0 + i], b = v[s0 + i + h];
-                    v[s0 + i] = make_float2(a.x + b.x, a.y + b.y);
-                    const float2 d = make_float2(a.x - b.x, a.y - b.y);
-                    v[s0 + i + h] = (i == 0) ? d : fmulc(d, c_w32[i * (16 / h)]);
+            for (int m = 0; m < M; ++m) {
+                const int j = lane + 32 * m;
+                const int jj = j <= nz ? j : L - j;
+                if (MODE == COL_DECOMP && j != 0 && j != nz) {
+                    float pm, pp;
+                    hA.at(jj, pm, pp);
+                    v[m].x = v[m].x - (fA0 * pm + fAn * pp);
+                    hB.at(jj, pm, pp);
+                    v[m].y = v[m].y - (fB0 * pm + fBn * pp);
                 }
+                if (j > nz) v[m] = make_float2(-v[m].x, -v[m].y);
             }
         }
+        // ---- M-point DIF FFT in registers (output in bit-reversed order)
+        dif_regs<M>(v);
         // ---- twiddle wL^(lane * b), b = bitrev(r)
 #pragma unroll
         for (int r = 1; r < M; ++r) {
             const int b = bitrev<M>(r);
             v[r] = fmulc(v[r], __ldg(&twL[(lane * b) & (L - 1)]));
+        }
+        if constexpr (M == 32) {
+            // ---- transpose the 32 x 32 block through shared memory: lane b
+            // then holds Z[l][b] for l = 0..31
+            float2 *tr = reinterpret_cast<float2 *>(sm32) + (size_t)wib * 32 * 33;
+#pragma unroll
+            for (int r = 0; r < 32; ++r) tr[lane * 33 + bitrev<32>(r)] = v[r];
+            __syncwarp();
+#pragma unroll
+            for (int l = 0; l < 32; ++l) v[l] = tr[l * 33 + lane];
+            __syncwarp();
+            // ---- 32-point DIF over l: register r holds X[32 bitrev(r) + lane]
+            dif_regs<32>(v);
+            // ---- coalesced column stores (k = 32 a + lane)
+#pragma unroll
+            for (int r = 0; r < 32; ++r) {
+                const int a = bitrev<32>(r);
+                const int k = 32 * a + lane;
+                if (a <= 16 && k <= nz) {
+                    float ra, rb;
+                    if (MODE == COL_DCT) {
+                        ra = v[r].x * s;
+                        rb = v[r].y * s;
+                    } else if (k == 0) {
+                        ra = (MODE == COL_DST) ? (float)in[oA] : fA0;
+                        rb = (MODE == COL_DST) ? (float)in[oB] : fB0;
+                    } else if (k == nz) {
+                        ra = (MODE == COL_DST) ? 0.f : fAn;
+                        rb = (MODE == COL_DST) ? 0.f : fBn;
+                    } else {
+                        ra = -v[r].y * s;
+                        rb = v[r].x * s;
+                        if (MODE == COL_COMBINE) {
+                            float pm, pp;
+                            hA.at(k, pm, pp);
+                            ra = ra + fA0 * pm + fAn * pp;
+                            hB.at(k, pm, pp);
+                            rb = rb + fB0 * pm + fBn * pp;
+                        }
+                    }
+                    out[oA + k] = ra;
+                    out[oB + k] = rb;
+                }
+            }
+            continue;
         }
         // ---- 32-point DIF across lanes (lane l ends with index bitrev5(l))
 #pragma unroll
@@ -205,7 +270,9 @@ static void launch_m(int M, const TIN *in, float *out, const Dims &d, cudaStream
 {
     const long long npairs = d.ncol / 2;
     const int pad = d.nz + 1 + (d.nz + 1) / 32 + 1;
-    const size_t sm = 8 * 2 * pad * sizeof(float);
+    size_t per_warp = 2 * pad * sizeof(float);
+    if (M == 32 && per_warp < 32 * 33 * sizeof(float2)) per_warp = 32 * 33 * sizeof(float2);
+    const size_t sm = 8 * per_warp;
     long long nb = (npairs + 7) / 8;
     if (nb > 152 * 16) nb = 152 * 16;
     switch (M) {
@@ -234,8 +301,19 @@ void columns32(const Dims &d, cudaStream_t st, int mode, const TIN *in, float *o
     if (pr) pr->end(PROBE_COLUMNS, st, 2.0 * (double)d.ncol * (double)(d.nz + 1) * sizeof(float));
 }
 
+template <typename TIN> static void col32_attrs()
+{
+    const int bytes = 8 * 32 * 33 * (int)sizeof(float2);
+    cudaFuncSetAttribute(k_col32<COL_DST, 32, TIN>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+    cudaFuncSetAttribute(k_col32<COL_DCT, 32, TIN>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+    cudaFuncSetAttribute(k_col32<COL_DECOMP, 32, TIN>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+    cudaFuncSetAttribute(k_col32<COL_COMBINE, 32, TIN>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+}
+
 void columns32_init()
 {
+    col32_attrs<float>();
+    col32_attrs<double>();
     float2 w[32];
     for (int j = 0; j < 32; ++j) {
         const double a = 2.0 * 3.14159265358979323846 * (double)j / 32.0;

@@ -52,6 +52,11 @@ void xy_inverse(const Dims &d, cudaStream_t st, const T *in, T *out, const typen
 template <typename T>
 void columns(const Dims &d, cudaStream_t st, int mode, const T *in, T *out, const T *phim,
              const T *phip, const typename cplx<T>::type *twz2, Probe *pr);
+// FP32 bandwidth-tuned line FFTs (lines32.cu), n = 64..1024
+bool lines32_supported(int n);
+void lines32_init();
+void launch_lines32(cudaStream_t st, const float *in, float *out, int n, int P, long long line_stride,
+                    long long nbatch, long long batch_stride, bool inverse, const float2 *tw);
 // FP32 warp-per-column-pair transforms (columns32.cu), nz = 32..512
 bool col32_supported(int nz);
 void columns32_init();

@@ -1,0 +1,196 @@
+// FP32 line FFTs of the mixed form (fftxyp2s / fftxys2p of
+// src/fft/sta3dfft.f90:136-260 in the Hermitian storage of
+// src/fft/stafft.f90:55-58), tuned for HBM bandwidth.
+//
+// A block owns 32 consecutive z values (one 128-byte row segment per line
+// index) of one line set: 16 complex lanes, each packing two real lines
+// (z, z+1).  The Stockham passes keep their butterflies in registers:
+// the first pass of a forward transform loads its inputs straight from HBM
+// (coalesced 128-byte rows), the last pass of an inverse transform stores
+// straight to HBM, and the passes in between exchange through one shared
+// buffer laid out [line index][lane] so every access is bank-conflict free.
+// N (the line length) is a compile-time constant: 64..1024.
+#include "kernels.h"
+
+namespace ps3d {
+
+namespace {
+
+constexpr int LANES = 16;
+
+template <int N> struct LinePlan {
+    static constexpr int T = N >= 512 ? 512 : 256;  // threads per block
+    static constexpr int G = T / LANES;             // butterfly groups per lane
+};
+
+__device__ __forceinline__ float2 cm(float2 a, float2 b)
+{
+    return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+}
+
+template <int R, bool INV> __device__ __forceinline__ void dftR(float2 *v) { dft<R, INV, float2>(v); }
+
+// one radix-R Stockham pass with span NS over N points: inputs x[j + r N/R]
+// of butterfly j, outputs at (j - k) R + k + r NS, k = j mod NS
+template <int N, int R, int NS, bool INV, bool FROM_GLOBAL, bool TO_GLOBAL>
+__device__ __forceinline__ void pass(float2 *sm, const float2 *__restrict__ gin, float2 *__restrict__ gout,
+                                     long long gstride, bool valid, float scale, const float2 *__restrict__ tw)
+{
+    constexpr int G = LinePlan<N>::G;
+    constexpr int NB = N / R;                         // butterflies per lane
+    constexpr int NBT = (NB + G - 1) / G;             // per thread
+    const int p = threadIdx.x & (LANES - 1), g = threadIdx.x / LANES;
+    float2 v[NBT][R];
+#pragma unroll
+    for (int q = 0; q < NBT; ++q) {
+        const int j = g + G * q;
+        if (NB % G == 0 || j < NB) {
+#pragma unroll
+            for (int r = 0; r < R; ++r) {
+                const int row = j + r * NB;
+                if (FROM_GLOBAL) v[q][r] = valid ? gin[row * gstride] : make_float2(0.f, 0.f);
+                else v[q][r] = sm[row * LANES + p];
+            }
+        }
+    }
+    if (!FROM_GLOBAL) __syncthreads();
+#pragma unroll
+    for (int q = 0; q < NBT; ++q) {
+        const int j = g + G * q;
+        if (NB % G == 0 || j < NB) {
+            const int k = j & (NS - 1);
+            if (NS > 1) {
+#pragma unroll
+                for (int r = 1; r < R; ++r) {
+                    float2 w = __ldg(&tw[k * r * (N / (NS * R))]);
+                    if (INV) w.y = -w.y;
+                    v[q][r] = cm(v[q][r], w);
+                }
+            }
+            dftR<R, INV>(v[q]);
+#pragma unroll
+            for (int r = 0; r < R; ++r) {
+                const int row = (j - k) * R + k + r * NS;
+                if (TO_GLOBAL) {
+                    if (valid) gout[row * gstride] = make_float2(v[q][r].x * scale, v[q][r].y * scale);
+                } else {
+                    sm[row * LANES + p] = v[q][r];
+                }
+            }
+        }
+    }
+    __syncthreads();
+}
+
+// the complete pass sequence for N = 8^a * {1, 2, 4}
+template <int N, bool INV, bool FROM_GLOBAL, bool TO_GLOBAL>
+__device__ __forceinline__ void fft_passes(float2 *sm, const float2 *gin, float2 *gout, long long gs, bool valid,
+                                           float scale, const float2 *tw)
+{
+    if constexpr (N == 64) {
+        pass<N, 8, 1, INV, FROM_GLOBAL, false>(sm, gin, gout, gs, valid, scale, tw);
+        pass<N, 8, 8, INV, false, TO_GLOBAL>(sm, gin, gout, gs, valid, scale, tw);
+    } else if constexpr (N == 128) {
+        pass<N, 8, 1, INV, FROM_GLOBAL, false>(sm, gin, gout, gs, valid, scale, tw);
+        pass<N, 8, 8, INV, false, false>(sm, gin, gout, gs, valid, scale, tw);
+        pass<N, 2, 64, INV, false, TO_GLOBAL>(sm, gin, gout, gs, valid, scale, tw);
+    } else if constexpr (N == 256) {
+        pass<N, 8, 1, INV, FROM_GLOBAL, false>(sm, gin, gout, gs, valid, scale, tw);
+        pass<N, 8, 8, INV, false, false>(sm, gin, gout, gs, valid, scale, tw);
+        pass<N, 4, 64, INV, false, TO_GLOBAL>(sm, gin, gout, gs, valid, scale, tw);
+    } else if constexpr (N == 512) {
+        pass<N, 8, 1, INV, FROM_GLOBAL, false>(sm, gin, gout, gs, valid, scale, tw);
+        pass<N, 8, 8, INV, false, false>(sm, gin, gout, gs, valid, scale, tw);
+        pass<N, 8, 64, INV, false, TO_GLOBAL>(sm, gin, gout, gs, valid, scale, tw);
+    } else {  // 1024
+        pass<N, 8, 1, INV, FROM_GLOBAL, false>(sm, gin, gout, gs, valid, scale, tw);
+        pass<N, 8, 8, INV, false, false>(sm, gin, gout, gs, valid, scale, tw);
+        pass<N, 8, 64, INV, false, false>(sm, gin, gout, gs, valid, scale, tw);
+        pass<N, 2, 512, INV, false, TO_GLOBAL>(sm, gin, gout, gs, valid, scale, tw);
+    }
+}
+
+template <int N, bool INV>
+__global__ void __launch_bounds__(LinePlan<N>::T) k_lines32(const float *__restrict__ in, float *__restrict__ out,
+                                                            int P, long long line_stride, long long batch_stride,
+                                                            const float2 *__restrict__ tw)
+{
+    extern __shared__ __align__(16) float2 smL[];
+    constexpr int T = LinePlan<N>::T;
+    const int p = threadIdx.x & (LANES - 1);
+    const int z0 = blockIdx.x * 2 * LANES;
+    const bool valid = z0 + 2 * p < P;
+    const long long base = ((long long)blockIdx.y * batch_stride + z0 + 2 * p) >> 1;  // float2 units
+    const long long gs = line_stride >> 1;
+    const float2 *gin = reinterpret_cast<const float2 *>(in) + base;
+    float2 *gout = reinterpret_cast<float2 *>(out) + base;
+    const float s = rsqrtf((float)N);
+    constexpr int H = N / 2;
+    if (!INV) {
+        fft_passes<N, false, true, false>(smL, gin, gout, gs, valid, 1.0f, tw);
+        // split the two packed real transforms and store Hermitian rows
+        for (int e = threadIdx.x; e < (H + 1) * LANES; e += T) {
+            const int k = e / LANES, q = e & (LANES - 1);
+            if (z0 + 2 * q >= P) continue;
+            const float2 ck = smL[k * LANES + q];
+            const float2 cn = smL[((N - k) & (N - 1)) * LANES + q];
+            const float are = 0.5f * (ck.x + cn.x), aim = 0.5f * (ck.y - cn.y);
+            const float bre = 0.5f * (ck.y + cn.y), bim = -0.5f * (ck.x - cn.x);
+            float2 *o = reinterpret_cast<float2 *>(out) + (((long long)blockIdx.y * batch_stride + z0 + 2 * q) >> 1);
+            o[k * gs] = make_float2(are * s, bre * s);
+            if (k > 0 && k < H) o[(N - k) * gs] = make_float2(aim * s, bim * s);
+        }
+    } else {
+        // rebuild C_k = A_k + i B_k from the Hermitian rows of both lines
+        for (int e = threadIdx.x; e < (H + 1) * LANES; e += T) {
+            const int k = e / LANES, q = e & (LANES - 1);
+            float2 lo = make_float2(0.f, 0.f), hi = make_float2(0.f, 0.f);
+            if (z0 + 2 * q < P) {
+                const float2 *i2 =
+                    reinterpret_cast<const float2 *>(in) + (((long long)blockIdx.y * batch_stride + z0 + 2 * q) >> 1);
+                lo = i2[k * gs];
+                if (k > 0 && k < H) hi = i2[(N - k) * gs];
+            }
+            smL[k * LANES + q] = make_float2(lo.x - hi.y, hi.x + lo.y);
+            if (k > 0 && k < H) smL[(N - k) * LANES + q] = make_float2(lo.x + hi.y, lo.y - hi.x);
+        }
+        __syncthreads();
+        fft_passes<N, true, false, true>(smL, gin, gout, gs, valid, s, tw);
+    }
+}
+
+template <int N>
+void launch32(cudaStream_t st, const float *in, float *out, int P, long long ls, long long nbatch, long long bs,
+              bool inverse, const float2 *tw)
+{
+    dim3 grid((P + 2 * LANES - 1) / (2 * LANES), (unsigned)nbatch);
+    const size_t sm = (size_t)N * LANES * sizeof(float2);
+    if (inverse) k_lines32<N, true><<<grid, LinePlan<N>::T, sm, st>>>(in, out, P, ls, bs, tw);
+    else k_lines32<N, false><<<grid, LinePlan<N>::T, sm, st>>>(in, out, P, ls, bs, tw);
+}
+
+}  // namespace
+
+bool lines32_supported(int n) { return n == 64 || n == 128 || n == 256 || n == 512 || n == 1024; }
+
+void lines32_init()
+{
+    cudaFuncSetAttribute(k_lines32<1024, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, 1024 * LANES * 8);
+    cudaFuncSetAttribute(k_lines32<1024, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, 1024 * LANES * 8);
+    cudaFuncSetAttribute(k_lines32<512, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, 512 * LANES * 8);
+    cudaFuncSetAttribute(k_lines32<512, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, 512 * LANES * 8);
+}
+
+void launch_lines32(cudaStream_t st, const float *in, float *out, int n, int P, long long line_stride,
+                    long long nbatch, long long batch_stride, bool inverse, const float2 *tw)
+{
+    switch (n) {
+    case 64: launch32<64>(st, in, out, P, line_stride, nbatch, batch_stride, inverse, tw); break;
+    case 128: launch32<128>(st, in, out, P, line_stride, nbatch, batch_stride, inverse, tw); break;
+    case 256: launch32<256>(st, in, out, P, line_stride, nbatch, batch_stride, inverse, tw); break;
+    case 512: launch32<512>(st, in, out, P, line_stride, nbatch, batch_stride, inverse, tw); break;
+    default: launch32<1024>(st, in, out, P, line_stride, nbatch, batch_stride, inverse, tw); break;
+    }
+}
+
+}  // namespace ps3d

@@ -105,6 +105,13 @@ void launch_lines(cudaStream_t st, const T *in, T *out, int n, int P, long long 
                   long long nbatch, long long batch_stride, bool inverse,
                   const typename cplx<T>::type *tw)
 {
+    if constexpr (sizeof(T) == sizeof(float)) {
+        if (lines32_supported(n)) {
+            launch_lines32(st, reinterpret_cast<const float *>(in), reinterpret_cast<float *>(out), n, P,
+                           line_stride, nbatch, batch_stride, inverse, reinterpret_cast<const float2 *>(tw));
+            return;
+        }
+    }
     const int B = lines_lanes<T>(n);
     const int logB = ilog2(B);
     dim3 grid((P + 2 * B - 1) / (2 * B), (unsigned)nbatch);
@@ -302,6 +309,7 @@ static void set_smem_attrs()
 
 void transforms_init()
 {
+    lines32_init();
     set_smem_attrs<double>();
     set_smem_attrs<float>();
     set_col_attrs<float, double>();
