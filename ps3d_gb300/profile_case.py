@@ -15,19 +15,23 @@ from . import Ps3dGpu, ic
 def main(argv=None):
     ap = argparse.ArgumentParser()
     ap.add_argument("--n", type=int, default=256)
+    ap.add_argument("--nx", type=int, default=0)
+    ap.add_argument("--ny", type=int, default=0)
+    ap.add_argument("--nz", type=int, default=0)
     ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
     ap.add_argument("--steps", type=int, default=1)
     ap.add_argument("--warmup", type=int, default=1)
     a = ap.parse_args(argv)
-    vor, pert = ic.beltrami_plus_perturbation(a.n, a.n, a.n, seed=1)
-    g = Ps3dGpu(a.n, a.n, a.n, ic.BASELINE_BOX["lower"], ic.BASELINE_BOX["extent"], precision=a.precision,
+    nx, ny, nz = a.nx or a.n, a.ny or a.n, a.nz or a.n
+    vor, pert = ic.beltrami_plus_perturbation(nx, ny, nz, seed=1)
+    g = Ps3dGpu(nx, ny, nz, ic.BASELINE_BOX["lower"], ic.BASELINE_BOX["extent"], precision=a.precision,
                 nnu=3, prediss=30.0, pretype="vorch", cflmax=0.5)
     g.setup_fields(vor, pert)
     t = 0.0
     if a.warmup:
         t, _ = g.advance_n(t, a.warmup)
     t, ms = g.time_advance(t, a.steps)
-    print(f"profile_case n={a.n} {a.precision}: {ms / max(a.steps, 1):.3f} ms/advance, "
+    print(f"profile_case {nx}x{ny}x{nz} {a.precision}: {ms / max(a.steps, 1):.3f} ms/advance, "
           f"{g.launch_count} launches total", file=sys.stderr)
     g.close()
 
