@@ -1,0 +1,419 @@
+// FP32 column (z) transforms of the mixed form: one warp per pair of
+// columns, half-length algorithm.
+//
+// The reference computes its sine and cosine transforms (src/fft/stafft.f90:
+// 410-550) from one real FFT of length n = nz of a pre-processed sequence
+//   dst:  wk(j) = (x(j) - x(n-j))/2 + sin(j pi/n) (x(j) + x(n-j))
+//   dct:  wk(j) = (x(j) + x(n-j))/2 - sin(j pi/n) (x(j) - x(n-j))
+// followed by a running sum over the cosine (dst) or sine (dct) part of the
+// spectrum.  Here the two columns of a pair are packed as the real and
+// imaginary parts of one complex sequence, so one n-point complex FFT serves
+// both; the running sums become a warp scan.
+//
+// Warp FFT of n = 32*M points: lane l holds c[l + 32 m] (m < M); an M-point
+// DFT in registers, a twiddle, a transpose through the warp's shared buffer,
+// an M-point DFT over the other index, and S = 32/M lanes combined by
+// shuffles.  Inputs stored as FP64 (the prognostic state) are narrowed with
+// integer arithmetic, keeping GB300's FP64 pipe out of the kernel.
+#include "kernels.h"
+
+namespace ps3d {
+
+namespace {
+
+__constant__ float2 c_w32z[32];  // exp(-2 pi i j / 32)
+
+__device__ __forceinline__ float2 fm(float2 a, float2 b)
+{
+    return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+}
+
+template <int M> __device__ __forceinline__ int brev(int r)
+{
+    int o = 0;
+#pragma unroll
+    for (int b = 1; b < M; b <<= 1) {
+        o = (o << 1) | (r & 1);
+        r >>= 1;
+    }
+    return o;
+}
+
+// FP64 -> FP32 with round to nearest (ties away), values below the FP32
+// normal range flushed to zero, using only integer and FP32 instructions
+__device__ __forceinline__ float narrow(double x)
+{
+    const long long b = __double_as_longlong(x);
+    const unsigned hi = (unsigned)(b >> 32), lo = (unsigned)b;
+    const unsigned sign = hi & 0x80000000u;
+    const int e = (int)((hi >> 20) & 0x7ff) - 1023 + 127;
+    if (e <= 0) return __uint_as_float(sign);
+    if (e >= 255) return __uint_as_float(sign | 0x7f800000u);
+    // 23 mantissa bits: 20 from hi, 3 from lo; round on the next bit
+    unsigned m = ((hi & 0xfffffu) << 3) | (lo >> 29);
+    unsigned f = sign | ((unsigned)e << 23);
+    f += m;
+    f += (lo >> 28) & 1u;  // carries into the exponent when the mantissa overflows
+    return __uint_as_float(f);
+}
+__device__ __forceinline__ float ld(const float *p, long long i) { return p[i]; }
+__device__ __forceinline__ float ld(const double *p, long long i) { return narrow(p[i]); }
+
+// harmonic functions of one column (inversion_utils.f90:484-542):
+// phim(z) = div (ep - ef em), phip(z) = div (em - ef ep), ep = exp(-kl zp),
+// em = exp(-kl zm) = ep at the mirrored level; phip(iz) = phim(nz - iz)
+struct Harm {
+    float a, c, ef, div, inv_n;
+    bool mean;
+    __device__ static Harm make(float kl, float dz, float Lz, int nz, bool mean)
+    {
+        const float l2e = 1.4426950408889634f;
+        Harm h;
+        h.a = -kl * dz * l2e;
+        h.c = -kl * Lz * l2e;
+        h.ef = exp2f(h.c);
+        h.div = 1.0f / (1.0f - h.ef * h.ef);
+        h.inv_n = 1.0f / (float)nz;
+        h.mean = mean;
+        return h;
+    }
+    __device__ void at(int iz, int nz, float &pm, float &pp) const
+    {
+        if (mean) {
+            pp = (float)iz * inv_n;
+            pm = (float)(nz - iz) * inv_n;
+        } else {
+            const float t = a * (float)iz;
+            const float ep = exp2f(t), em = exp2f(c - t);
+            pm = div * (ep - ef * em);
+            pp = div * (em - ef * ep);
+        }
+    }
+};
+
+template <int M> __device__ __forceinline__ void dif(float2 *v)
+{
+#pragma unroll
+    for (int h = M / 2; h >= 1; h >>= 1) {
+#pragma unroll
+        for (int s0 = 0; s0 < M; s0 += 2 * h) {
+#pragma unroll
+            for (int i = 0; i < h; ++i) {
+                const float2 a = v[s0 + i], b = v[s0 + i + h];
+                v[s0 + i] = make_float2(a.x + b.x, a.y + b.y);
+                const float2 d = make_float2(a.x - b.x, a.y - b.y);
+                v[s0 + i + h] = (i == 0) ? d : fm(d, c_w32z[i * (16 / h)]);
+            }
+        }
+    }
+}
+
+// n = 32 M point forward FFT of the warp's sequence; on entry lane l holds
+// v[m] = c[l + 32 m]; on exit X[k] (natural order) is in xs[0..n).
+template <int M>
+__device__ __forceinline__ void warp_fft(float2 *v, float2 *xs, const float2 *__restrict__ twn, int lane)
+{
+    constexpr int S = 32 / M;
+    constexpr int n = 32 * M;
+    dif<M>(v);  // register r: Z_l[b], b = brev(r)
+#pragma unroll
+    for (int r = 1; r < M; ++r) v[r] = fm(v[r], __ldg(&twn[(lane * brev<M>(r)) & (n - 1)]));
+    // transpose: lane (b, h) = (lane / S, lane % S) gathers Z[h + S t][b]
+#pragma unroll
+    for (int r = 0; r < M; ++r) xs[lane * (M + 1) + brev<M>(r)] = v[r];
+    __syncwarp();
+    const int b = lane / S, h = lane % S;
+#pragma unroll
+    for (int t = 0; t < M; ++t) v[t] = xs[(h + S * t) * (M + 1) + b];
+    __syncwarp();
+    dif<M>(v);  // register r: F_h[a'], a' = brev(r)
+    if (S > 1) {
+#pragma unroll
+        for (int r = 1; r < M; ++r) v[r] = fm(v[r], c_w32z[(h * brev<M>(r)) & 31]);
+        // S-point DIF across the S lanes of the group
+#pragma unroll
+        for (int hs = S / 2; hs >= 1; hs >>= 1) {
+            const bool upper = (h & hs) != 0;
+            const float2 w = c_w32z[((h & (hs - 1)) * (16 / hs)) & 31];
+#pragma unroll
+            for (int r = 0; r < M; ++r) {
+                float2 u;
+                u.x = __shfl_xor_sync(0xffffffffu, v[r].x, hs);
+                u.y = __shfl_xor_sync(0xffffffffu, v[r].y, hs);
+                const float2 sum = make_float2(v[r].x + u.x, v[r].y + u.y);
+                const float2 dif2 = fm(make_float2(u.x - v[r].x, u.y - v[r].y), w);
+                v[r] = upper ? dif2 : sum;
+            }
+        }
+    }
+    const int e = brev<S>(h);
+#pragma unroll
+    for (int r = 0; r < M; ++r) xs[b + M * brev<M>(r) + M * M * e] = v[r];
+    __syncwarp();
+}
+
+__device__ __forceinline__ int zpad(int z) { return z + (z >> 4); }
+
+// inclusive warp scan of one value per lane
+__device__ __forceinline__ float warp_incl_scan(float x, int lane)
+{
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const float y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= o) x += y;
+    }
+    return x;
+}
+
+}  // namespace
+
+// MODE: COL_DST, COL_DCT, COL_DECOMP, COL_COMBINE (see kernels.h)
+template <int MODE, int M, typename TIN>
+__global__ void __launch_bounds__(256) k_colz(const TIN *__restrict__ in, float *__restrict__ out, int P,
+                                              long long npairs, const double *__restrict__ k2l2, float dz,
+                                              float Lz, const float2 *__restrict__ twn,
+                                              const float *__restrict__ sinz, const float *__restrict__ cosz)
+{
+    constexpr int n = 32 * M;  // = nz
+    constexpr int KPL = n / 64;  // spectrum indices per lane for the running sums
+    const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+    extern __shared__ __align__(16) unsigned char smz[];
+    constexpr int XS = (32 * (M + 1) > n ? 32 * (M + 1) : n);  // float2 per warp
+    constexpr int ZS = n + 1 + (n + 1) / 16 + 2;                // floats per output column
+    float2 *xs = reinterpret_cast<float2 *>(smz) + (size_t)wib * (XS + ZS);
+    float *zA = reinterpret_cast<float *>(xs + XS);
+    float *zB = zA + ZS;
+    const float s = rsqrtf((float)n);
+    const float r2s = 1.41421356237309505f * s;
+    const long long warps = (long long)gridDim.x * (blockDim.x >> 5);
+    for (long long pr = (long long)blockIdx.x * (blockDim.x >> 5) + wib; pr < npairs; pr += warps) {
+        const long long cA = 2 * pr, cB = cA + 1;
+        const long long oA = cA * P, oB = cB * P;
+        float fA0 = 0.f, fAn = 0.f, fB0 = 0.f, fBn = 0.f;
+        Harm hA{}, hB{};
+        if (MODE == COL_DECOMP || MODE == COL_COMBINE || MODE == COL_DCT) {
+            fA0 = ld(in, oA);
+            fAn = ld(in, oA + n);
+            fB0 = ld(in, oB);
+            fBn = ld(in, oB + n);
+        }
+        if (MODE == COL_DECOMP || MODE == COL_COMBINE) {
+            hA = Harm::make(sqrtf((float)k2l2[cA]), dz, Lz, n, cA == 0);
+            hB = Harm::make(sqrtf((float)k2l2[cB]), dz, Lz, n, cB == 0);
+        }
+        // ---- pre-processed sequence wk (both columns), lane l: j = l + 32 m
+        float2 v[M];
+        float dsumA = 0.f, dsumB = 0.f;  // DCT direct sum for x(1)
+#pragma unroll
+        for (int m = 0; m < M; ++m) {
+            const int j = lane + 32 * m;
+            float xa = 0.f, xb = 0.f, ya = 0.f, yb = 0.f;  // x(j), x(n-j)
+            if (j > 0) {
+                xa = ld(in, oA + j);
+                xb = ld(in, oB + j);
+                ya = ld(in, oA + n - j);
+                yb = ld(in, oB + n - j);
+            }
+            if (MODE == COL_DECOMP && j > 0) {
+                float pm, pp;
+                hA.at(j, n, pm, pp);
+                xa -= fA0 * pm + fAn * pp;
+                ya -= fA0 * pp + fAn * pm;
+                hB.at(j, n, pm, pp);
+                xb -= fB0 * pm + fBn * pp;
+                yb -= fB0 * pp + fBn * pm;
+            }
+            const float sj = __ldg(&sinz[j]);
+            if (MODE == COL_DCT) {
+                if (j == 0) {
+                    v[m] = make_float2(0.5f * (fA0 + fAn), 0.5f * (fB0 + fBn));
+                } else {
+                    const float cj = __ldg(&cosz[j]);
+                    dsumA += xa * cj;
+                    dsumB += xb * cj;
+                    v[m] = make_float2(0.5f * (xa + ya) - sj * (xa - ya), 0.5f * (xb + yb) - sj * (xb - yb));
+                }
+            } else {
+                v[m] = (j == 0) ? make_float2(0.f, 0.f)
+                                : make_float2(0.5f * (xa - ya) + sj * (xa + ya), 0.5f * (xb - yb) + sj * (xb + yb));
+            }
+        }
+        warp_fft<M>(v, xs, twn, lane);
+        // ---- split the packed spectra (k = lane + 32 i), running sums as
+        // warp scans with a carry, outputs to zA / zB
+        float x1A = 0.f, x1B = 0.f;
+        if (MODE == COL_DCT) {
+            x1A = dsumA;
+            x1B = dsumB;
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) {
+                x1A += __shfl_xor_sync(0xffffffffu, x1A, o);
+                x1B += __shfl_xor_sync(0xffffffffu, x1B, o);
+            }
+            x1A = r2s * (0.5f * fA0 + x1A - 0.5f * fAn);
+            x1B = r2s * (0.5f * fB0 + x1B - 0.5f * fBn);
+        }
+        float carryA = 0.f, carryB = 0.f;
+#pragma unroll
+        for (int i = 0; i < KPL; ++i) {
+            const int k = lane + 32 * i;
+            const float2 ck = xs[k], cn = xs[(n - k) & (n - 1)];
+            const float ReA = 0.5f * (ck.x + cn.x), ImA = 0.5f * (ck.y - cn.y);
+            const float ReB = 0.5f * (ck.y + cn.y), ImB = -0.5f * (ck.x - cn.x);
+            float va, vb;
+            if (MODE == COL_DCT) {
+                va = (k == 0) ? 0.f : ImA;
+                vb = (k == 0) ? 0.f : ImB;
+            } else {
+                va = (k == 0) ? 0.5f * ReA : ReA;
+                vb = (k == 0) ? 0.5f * ReB : ReB;
+            }
+            const float ia = warp_incl_scan(va, lane) + carryA;
+            const float ib = warp_incl_scan(vb, lane) + carryB;
+            carryA = __shfl_sync(0xffffffffu, ia, 31);
+            carryB = __shfl_sync(0xffffffffu, ib, 31);
+            if (MODE == COL_DCT) {
+                zA[zpad(2 * k)] = r2s * ReA;
+                zB[zpad(2 * k)] = r2s * ReB;
+                zA[zpad(2 * k + 1)] = x1A - r2s * ia;
+                zB[zpad(2 * k + 1)] = x1B - r2s * ib;
+            } else {
+                zA[zpad(2 * k + 1)] = r2s * ia;
+                zB[zpad(2 * k + 1)] = r2s * ib;
+                if (k > 0) {
+                    zA[zpad(2 * k)] = -r2s * ImA;
+                    zB[zpad(2 * k)] = -r2s * ImB;
+                }
+            }
+        }
+        if (MODE == COL_DCT && lane == 0) {
+            const float2 cm = xs[n / 2];
+            zA[zpad(n)] = r2s * cm.x;
+            zB[zpad(n)] = r2s * cm.y;
+        }
+        __syncwarp();
+        // ---- coalesced column stores with the mode's boundary rows
+        for (int iz = lane; iz <= n; iz += 32) {
+            float ra, rb;
+            if (MODE == COL_DCT) {
+                ra = zA[zpad(iz)];
+                rb = zB[zpad(iz)];
+            } else if (iz == 0) {
+                ra = (MODE == COL_DST) ? ld(in, oA) : fA0;
+                rb = (MODE == COL_DST) ? ld(in, oB) : fB0;
+            } else if (iz == n) {
+                ra = (MODE == COL_DST) ? 0.f : fAn;
+                rb = (MODE == COL_DST) ? 0.f : fBn;
+            } else {
+                ra = zA[zpad(iz)];
+                rb = zB[zpad(iz)];
+                if (MODE == COL_COMBINE) {
+                    float pm, pp;
+                    hA.at(iz, n, pm, pp);
+                    ra += fA0 * pm + fAn * pp;
+                    hB.at(iz, n, pm, pp);
+                    rb += fB0 * pm + fBn * pp;
+                }
+            }
+            out[oA + iz] = ra;
+            out[oB + iz] = rb;
+        }
+        __syncwarp();
+    }
+}
+
+namespace {
+template <int M> constexpr size_t colz_smem_per_warp()
+{
+    constexpr int n = 32 * M;
+    constexpr int XS = (32 * (M + 1) > n ? 32 * (M + 1) : n);
+    constexpr int ZS = n + 1 + (n + 1) / 16 + 2;
+    return XS * sizeof(float2) + 2 * ZS * sizeof(float);
+}
+
+template <int MODE, int M, typename TIN>
+void launch_colz_m(const TIN *in, float *out, const Dims &d, cudaStream_t st, const double *k2l2, float dz, float Lz,
+                   const float2 *twn, const float *sinz, const float *cosz)
+{
+    const long long npairs = d.ncol / 2;
+    const size_t sm = 8 * colz_smem_per_warp<M>();
+    long long nb = (npairs + 7) / 8;
+    if (nb > 152 * 24) nb = 152 * 24;
+    k_colz<MODE, M, TIN><<<(unsigned)nb, 256, sm, st>>>(in, out, d.P, npairs, k2l2, dz, Lz, twn, sinz, cosz);
+}
+
+template <int MODE, typename TIN>
+void launch_colz(const TIN *in, float *out, const Dims &d, cudaStream_t st, const double *k2l2, float dz, float Lz,
+                 const float2 *twn, const float *sinz, const float *cosz)
+{
+    switch (d.nz) {
+    case 64: launch_colz_m<MODE, 2, TIN>(in, out, d, st, k2l2, dz, Lz, twn, sinz, cosz); break;
+    case 128: launch_colz_m<MODE, 4, TIN>(in, out, d, st, k2l2, dz, Lz, twn, sinz, cosz); break;
+    case 256: launch_colz_m<MODE, 8, TIN>(in, out, d, st, k2l2, dz, Lz, twn, sinz, cosz); break;
+    case 512: launch_colz_m<MODE, 16, TIN>(in, out, d, st, k2l2, dz, Lz, twn, sinz, cosz); break;
+    default: launch_colz_m<MODE, 32, TIN>(in, out, d, st, k2l2, dz, Lz, twn, sinz, cosz); break;
+    }
+}
+
+template <int MODE, int M, typename TIN> void attr_m()
+{
+    cudaFuncSetAttribute(k_colz<MODE, M, TIN>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)(8 * colz_smem_per_warp<M>()));
+}
+template <int MODE, typename TIN> void attr_mode()
+{
+    attr_m<MODE, 2, TIN>();
+    attr_m<MODE, 4, TIN>();
+    attr_m<MODE, 8, TIN>();
+    attr_m<MODE, 16, TIN>();
+    attr_m<MODE, 32, TIN>();
+}
+template <typename TIN> void attr_all()
+{
+    attr_mode<COL_DST, TIN>();
+    attr_mode<COL_DCT, TIN>();
+    attr_mode<COL_DECOMP, TIN>();
+    attr_mode<COL_COMBINE, TIN>();
+}
+}  // namespace
+
+bool colz_supported(int nz) { return nz == 64 || nz == 128 || nz == 256 || nz == 512 || nz == 1024; }
+
+void colz_init()
+{
+    float2 w[32];
+    for (int j = 0; j < 32; ++j) {
+        const double a = 2.0 * 3.14159265358979323846 * (double)j / 32.0;
+        double c = cos(a), sn = sin(a);
+        if (j % 8 == 0) {
+            const int q = j / 8;
+            c = (q == 0) ? 1.0 : (q == 2 ? -1.0 : 0.0);
+            sn = (q == 1) ? 1.0 : (q == 3 ? -1.0 : 0.0);
+        }
+        w[j] = make_float2((float)c, (float)(-sn));
+    }
+    cudaMemcpyToSymbol(c_w32z, w, sizeof(w));
+    attr_all<float>();
+    attr_all<double>();
+}
+
+template <typename TIN>
+void columns_z(const Dims &d, cudaStream_t st, int mode, const TIN *in, float *out, const double *k2l2, float dz,
+               float Lz, const float2 *twn, const float *sinz, const float *cosz, Probe *pr)
+{
+    if (pr) pr->begin(PROBE_COLUMNS, st);
+    switch (mode) {
+    case COL_DST: launch_colz<COL_DST, TIN>(in, out, d, st, k2l2, dz, Lz, twn, sinz, cosz); break;
+    case COL_DCT: launch_colz<COL_DCT, TIN>(in, out, d, st, k2l2, dz, Lz, twn, sinz, cosz); break;
+    case COL_DECOMP: launch_colz<COL_DECOMP, TIN>(in, out, d, st, k2l2, dz, Lz, twn, sinz, cosz); break;
+    default: launch_colz<COL_COMBINE, TIN>(in, out, d, st, k2l2, dz, Lz, twn, sinz, cosz); break;
+    }
+    if (pr) pr->end(PROBE_COLUMNS, st, 2.0 * (double)d.ncol * (double)(d.nz + 1) * sizeof(float));
+}
+
+template void columns_z<float>(const Dims &, cudaStream_t, int, const float *, float *, const double *, float, float,
+                               const float2 *, const float *, const float *, Probe *);
+template void columns_z<double>(const Dims &, cudaStream_t, int, const double *, float *, const double *, float,
+                                float, const float2 *, const float *, const float *, Probe *);
+
+}  // namespace ps3d

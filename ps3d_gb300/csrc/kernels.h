@@ -57,6 +57,12 @@ bool lines32_supported(int n);
 void lines32_init();
 void launch_lines32(cudaStream_t st, const float *in, float *out, int n, int P, long long line_stride,
                     long long nbatch, long long batch_stride, bool inverse, const float2 *tw);
+// FP32 half-length warp z transforms (colz.cu), nz = 64..1024
+bool colz_supported(int nz);
+void colz_init();
+template <typename TIN>
+void columns_z(const Dims &d, cudaStream_t st, int mode, const TIN *in, float *out, const double *k2l2, float dz,
+               float Lz, const float2 *twn, const float *sinz, const float *cosz, Probe *pr);
 // FP32 warp-per-column-pair transforms (columns32.cu), nz = 32..512
 bool col32_supported(int nz);
 void columns32_init();

@@ -77,6 +77,10 @@ struct ps3d_gpu_ctx {
     void *phim = nullptr, *phip = nullptr, *thetam = nullptr, *thetap = nullptr, *dthetam = nullptr,
          *dthetap = nullptr, *green = nullptr;
     void *twx = nullptr, *twy = nullptr, *twz2 = nullptr;
+    // FP32 z-transform tables of the mixed form: exp(-2 pi i k/nz), sin and
+    // cos(j pi/nz)
+    float2 *twz32 = nullptr;
+    float *sinz32 = nullptr, *cosz32 = nullptr;
     // FP64 transform tables for the FP64 set-up / projection of the mixed
     // form (aliases of the above in the FP64 form)
     double2 *twx64 = nullptr, *twy64 = nullptr, *twz2_64 = nullptr;
@@ -210,7 +214,10 @@ template <typename T> void xyi(ps3d_gpu_ctx *c, const T *in, T *out)
 }
 template <typename T, typename TIN> void col_any(ps3d_gpu_ctx *c, int mode, const TIN *in, T *out)
 {
-    if (sizeof(T) == sizeof(float) && col32_supported(c->d.nz)) {
+    if (sizeof(T) == sizeof(float) && colz_supported(c->d.nz)) {
+        columns_z<TIN>(c->d, c->st, mode, in, reinterpret_cast<float *>(out), c->k2l2, (float)c->dx[2],
+                       (float)c->cfg.extent[2], c->twz32, c->sinz32, c->cosz32, &c->probe);
+    } else if (sizeof(T) == sizeof(float) && col32_supported(c->d.nz)) {
         columns32<TIN>(c->d, c->st, mode, in, reinterpret_cast<float *>(out), c->k2l2, (float)c->dx[2],
                        (float)c->cfg.extent[2], tf<float2>(c->twz2), &c->probe);
     } else if (sizeof(TIN) == sizeof(T)) {
@@ -810,7 +817,9 @@ template <typename T> int allocate_fields(ps3d_gpu_ctx *c)
     if (ok && c->cfg.stepper == PS3D_CN2) ok = dalloc(c, &c->vortsm, 3 * f64);
     if (ok && c->cfg.hold_source) ok = dalloc(c, &c->held, 3 * fb);
     if (ok && !c->fp64)
-        ok = dalloc(c, &c->stage64, f64) && dalloc(c, &c->phim64, f64) && dalloc(c, &c->phip64, f64) &&
+        ok = dalloc(c, &c->twz32, d.nz * sizeof(float2)) && dalloc(c, &c->sinz32, d.nz * sizeof(float)) &&
+             dalloc(c, &c->cosz32, d.nz * sizeof(float)) &&
+             dalloc(c, &c->stage64, f64) && dalloc(c, &c->phim64, f64) && dalloc(c, &c->phip64, f64) &&
              dalloc(c, &c->twx64, d.nx * sizeof(double2)) && dalloc(c, &c->twy64, d.ny * sizeof(double2)) &&
              dalloc(c, &c->twz2_64, 2 * d.nz * sizeof(double2));
     const size_t P2 = (size_t)d.ncol * sizeof(double), Z = (size_t)(d.nz + 1) * sizeof(double);
@@ -841,6 +850,15 @@ template <typename T> int allocate_fields(ps3d_gpu_ctx *c)
         twiddles<double>(c, c->twx64, d.nx);
         twiddles<double>(c, c->twy64, d.ny);
         twiddles<double>(c, c->twz2_64, 2 * d.nz);
+        twiddles<float>(c, c->twz32, d.nz);
+        std::vector<float> sn(d.nz), cs(d.nz);
+        for (int j = 0; j < d.nz; ++j) {
+            sn[j] = (float)sin(M_PI * (double)j / (double)d.nz);
+            cs[j] = (float)cos(M_PI * (double)j / (double)d.nz);
+        }
+        cudaMemcpyAsync(c->sinz32, sn.data(), d.nz * sizeof(float), cudaMemcpyHostToDevice, c->st);
+        cudaMemcpyAsync(c->cosz32, cs.data(), d.nz * sizeof(float), cudaMemcpyHostToDevice, c->st);
+        cudaStreamSynchronize(c->st);
     }
     host_tables(c);
     op_hyperbolic_tables<T>(d, c->st, c->k2l2, c->k2l2i, c->rkz, c->zm, c->zp, c->cfg.extent[2], tf<T>(c->phim),
@@ -926,6 +944,7 @@ int ps3d_gpu_create(const ps3d_gpu_config *cfg, ps3d_gpu_ctx **out)
     cudaSetDevice(cfg->device);
     transforms_init();
     columns32_init();
+    colz_init();
     cudaStreamCreateWithFlags(&c->st, cudaStreamNonBlocking);
     cudaEventCreate(&c->ev0);
     cudaEventCreate(&c->ev1);
