@@ -39,25 +39,16 @@ template <int M> __device__ __forceinline__ int brev(int r)
     return o;
 }
 
-// FP64 -> FP32 with round to nearest (ties away), values below the FP32
-// normal range flushed to zero, using only integer and FP32 instructions
-__device__ __forceinline__ float narrow(double x)
-{
-    const long long b = __double_as_longlong(x);
-    const unsigned hi = (unsigned)(b >> 32), lo = (unsigned)b;
-    const unsigned sign = hi & 0x80000000u;
-    const int e = (int)((hi >> 20) & 0x7ff) - 1023 + 127;
-    if (e <= 0) return __uint_as_float(sign);
-    if (e >= 255) return __uint_as_float(sign | 0x7f800000u);
-    // 23 mantissa bits: 20 from hi, 3 from lo; round on the next bit
-    unsigned m = ((hi & 0xfffffu) << 3) | (lo >> 29);
-    unsigned f = sign | ((unsigned)e << 23);
-    f += m;
-    f += (lo >> 28) & 1u;  // carries into the exponent when the mantissa overflows
-    return __uint_as_float(f);
-}
 __device__ __forceinline__ float ld(const float *p, long long i) { return p[i]; }
-__device__ __forceinline__ float ld(const double *p, long long i) { return narrow(p[i]); }
+__device__ __forceinline__ float ld(const double *p, long long i) { return narrow32(p[i]); }
+
+// 2^x on the special-function unit, results below the normal range flushed
+__device__ __forceinline__ float ex2(float x)
+{
+    float y;
+    asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
 
 // harmonic functions of one column (inversion_utils.f90:484-542):
 // phim(z) = div (ep - ef em), phip(z) = div (em - ef ep), ep = exp(-kl zp),
@@ -71,7 +62,7 @@ struct Harm {
         Harm h;
         h.a = -kl * dz * l2e;
         h.c = -kl * Lz * l2e;
-        h.ef = exp2f(h.c);
+        h.ef = ex2(h.c);
         h.div = 1.0f / (1.0f - h.ef * h.ef);
         h.inv_n = 1.0f / (float)nz;
         h.mean = mean;
@@ -84,7 +75,7 @@ struct Harm {
             pm = (float)(nz - iz) * inv_n;
         } else {
             const float t = a * (float)iz;
-            const float ep = exp2f(t), em = exp2f(c - t);
+            const float ep = ex2(t), em = ex2(c - t);
             pm = div * (ep - ef * em);
             pp = div * (em - ef * ep);
         }
@@ -169,7 +160,7 @@ __device__ __forceinline__ float warp_incl_scan(float x, int lane)
 
 // MODE: COL_DST, COL_DCT, COL_DECOMP, COL_COMBINE (see kernels.h)
 template <int MODE, int M, typename TIN>
-__global__ void __launch_bounds__(256) k_colz(const TIN *__restrict__ in, float *__restrict__ out, int P,
+__global__ void __launch_bounds__(256, 2) k_colz(const TIN *__restrict__ in, float *__restrict__ out, int P,
                                               long long npairs, const double *__restrict__ k2l2, float dz,
                                               float Lz, const float2 *__restrict__ twn,
                                               const float *__restrict__ sinz, const float *__restrict__ cosz)

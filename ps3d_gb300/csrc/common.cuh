@@ -154,3 +154,33 @@ __host__ __device__ inline int ilog2(int v)
 }
 
 }  // namespace ps3d
+
+namespace ps3d {
+// FP32 <-> FP64 conversions with integer instructions only (GB300 runs
+// F2F to or from FP64 on its narrow FP64 pipe).  narrow32 rounds to nearest
+// (ties away from zero) and flushes results below the FP32 normal range to
+// zero; widen64 is exact for normal FP32 values and flushes FP32 denormals.
+__device__ __forceinline__ float narrow32(double x)
+{
+    const long long b = __double_as_longlong(x);
+    const unsigned hi = (unsigned)(b >> 32), lo = (unsigned)b;
+    const unsigned sign = hi & 0x80000000u;
+    const int e = (int)((hi >> 20) & 0x7ff) - 1023 + 127;
+    if (e <= 0) return __uint_as_float(sign);
+    if (e >= 255) return __uint_as_float(sign | 0x7f800000u);
+    unsigned f = sign | ((unsigned)e << 23);
+    f += ((hi & 0xfffffu) << 3) | (lo >> 29);
+    f += (lo >> 28) & 1u;
+    return __uint_as_float(f);
+}
+
+__device__ __forceinline__ double widen64(float f)
+{
+    const unsigned u = __float_as_uint(f);
+    const unsigned e = (u >> 23) & 0xffu;
+    const unsigned long long s = (unsigned long long)(u & 0x80000000u) << 32;
+    if (e == 0) return __longlong_as_double((long long)s);
+    const unsigned long long de = (e == 255u) ? 2047ull : (unsigned long long)(e + 896u);
+    return __longlong_as_double((long long)(s | (de << 52) | ((unsigned long long)(u & 0x7fffffu) << 29)));
+}
+}  // namespace ps3d

@@ -447,6 +447,89 @@ void op_rk4_sub4(const Dims &d, cudaStream_t st, double *q, const double *qdf, c
     k_rk4_sub4<T><<<col_grid(d), COL_BLOCK, 0, st>>>(d, q, qdf, sqs, epq, emq, dt6);
 }
 
+// Mixed form: the increment (c1 * epq * sqs, an FP32 source term scaled by
+// per-column factors) is formed in FP32 and widened exactly; the state keeps
+// its FP64 accumulation with one fused multiply-add (q = qdi*m + inc) and one
+// add (qdf += inc) per element, and the FP32 copy of the new state that the
+// next vor2vel reads is written alongside.
+__global__ void k_rk4m_sub1(Dims d, double *__restrict__ q, double *__restrict__ qdi, double *__restrict__ qdf,
+                            float *__restrict__ sqs, float *__restrict__ q32, const double *__restrict__ filt0,
+                            const double *__restrict__ emq, double dt2, double dt6)
+{
+    COLUMN_HEADER
+    const double m = emq[col];
+    const float f0 = (float)filt0[col];
+    const float c2 = (float)(dt2 * m), c6 = (float)dt6;
+    for (int iz = threadIdx.x; iz <= d.nz; iz += 32) {
+        const long long i = o + iz;
+        const float s = f0 * sqs[i];
+        const double q0 = q[i];
+        sqs[i] = s;
+        qdi[i] = q0;
+        const double qn = fma(q0, m, widen64(c2 * s));
+        q[i] = qn;
+        q32[i] = narrow32(qn);
+        qdf[i] = q0 + widen64(c6 * s);
+    }
+}
+__global__ void k_rk4m_sub23(Dims d, double *__restrict__ q, const double *__restrict__ qdi,
+                             double *__restrict__ qdf, const float *__restrict__ sqs, float *__restrict__ q32,
+                             const double *__restrict__ epq, const double *__restrict__ emq, double c1, double dt3)
+{
+    COLUMN_HEADER
+    const double m = emq[col];
+    const float pp = (float)epq[col];
+    const float cq = (float)(c1 * m), c3 = (float)dt3;
+    for (int iz = threadIdx.x; iz <= d.nz; iz += 32) {
+        const long long i = o + iz;
+        const float s = pp * sqs[i];
+        const double qn = fma(qdi[i], m, widen64(cq * s));
+        q[i] = qn;
+        q32[i] = narrow32(qn);
+        qdf[i] = qdf[i] + widen64(c3 * s);
+    }
+}
+__global__ void k_rk4m_sub4(Dims d, double *__restrict__ q, const double *__restrict__ qdf,
+                            const float *__restrict__ sqs, float *__restrict__ q32, const double *__restrict__ epq,
+                            const double *__restrict__ emq, double dt6)
+{
+    COLUMN_HEADER
+    const double m = emq[col];
+    const float c = (float)(dt6 * epq[col] * m);
+    for (int iz = threadIdx.x; iz <= d.nz; iz += 32) {
+        const long long i = o + iz;
+        const double qn = fma(qdf[i], m, widen64(c * sqs[i]));
+        q[i] = qn;
+        q32[i] = narrow32(qn);
+    }
+}
+void op_rk4m_sub1(const Dims &d, cudaStream_t st, double *q, double *qdi, double *qdf, float *sqs, float *q32,
+                  const double *filt0, const double *emq, double dt2, double dt6)
+{
+    k_rk4m_sub1<<<col_grid(d), COL_BLOCK, 0, st>>>(d, q, qdi, qdf, sqs, q32, filt0, emq, dt2, dt6);
+}
+void op_rk4m_sub23(const Dims &d, cudaStream_t st, double *q, const double *qdi, double *qdf, const float *sqs,
+                   float *q32, const double *epq, const double *emq, double c1, double dt3)
+{
+    k_rk4m_sub23<<<col_grid(d), COL_BLOCK, 0, st>>>(d, q, qdi, qdf, sqs, q32, epq, emq, c1, dt3);
+}
+void op_rk4m_sub4(const Dims &d, cudaStream_t st, double *q, const double *qdf, const float *sqs, float *q32,
+                  const double *epq, const double *emq, double dt6)
+{
+    k_rk4m_sub4<<<col_grid(d), COL_BLOCK, 0, st>>>(d, q, qdf, sqs, q32, epq, emq, dt6);
+}
+
+// FP32 copy of an FP64 field (integer narrowing)
+__global__ void k_narrow(const double *__restrict__ in, float *__restrict__ out, long long n)
+{
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+        out[i] = narrow32(in[i]);
+}
+void op_narrow(cudaStream_t st, const double *in, float *out, long long n)
+{
+    k_narrow<<<2432, 256, 0, st>>>(in, out, n);
+}
+
 // cn2 (cn2.f90:119-175)
 template <typename T>
 __global__ void k_cn2_init(Dims d, double *__restrict__ vortsm, const double *__restrict__ svor,
@@ -490,7 +573,7 @@ void op_cn2_update(const Dims &d, cudaStream_t st, double *svor, const double *v
 // The sum of the sine transform of the (0,0) column is the dot product with
 // dstsum[j] = sqrt(2/nz) sum_k sin(pi j k / nz).
 __global__ void k_mean_fix(int nz, long long nfield, double *svor, const double *__restrict__ dstsum, double fnzi,
-                           const double *__restrict__ ini, double *savg_out, int apply)
+                           const double *__restrict__ ini, double *savg_out, int apply, float *svor32)
 {
     __shared__ double red[2][256];
     for (int nc = 0; nc < 2; ++nc) {
@@ -515,14 +598,18 @@ __global__ void k_mean_fix(int nz, long long nfield, double *svor, const double 
             if (apply) {
                 s[0] = s[0] + ini[nc] - savg;
                 s[nz] = s[nz] + ini[nc] - savg;
+                if (svor32) {
+                    svor32[nc * nfield] = narrow32(s[0]);
+                    svor32[nc * nfield + nz] = narrow32(s[nz]);
+                }
             }
         }
     }
 }
 void op_mean_fix(const Dims &d, cudaStream_t st, double *svor, const double *dstsum, double fnzi,
-                 const double *ini, double *savg_out, int apply)
+                 const double *ini, double *savg_out, int apply, float *svor32)
 {
-    k_mean_fix<<<1, 256, 0, st>>>(d.nz, d.nfield, svor, dstsum, fnzi, ini, savg_out, apply);
+    k_mean_fix<<<1, 256, 0, st>>>(d.nz, d.nfield, svor, dstsum, fnzi, ini, savg_out, apply, svor32);
 }
 
 // --------------------------------------------------------------- reductions
@@ -890,6 +977,8 @@ INST_T(float)
 template void op_convert<float, double>(const Dims &, cudaStream_t, const double *, float *, long long);
 template void op_v2v_ds<float, float>(const Dims &, cudaStream_t, const Deriv &, const float *, const float *,
                                       float *);
+template void op_v2v_wsrc<float, float>(const Dims &, cudaStream_t, const Deriv &, const float *, const float *,
+                                        float *);
 template void op_v2v_project<float, float>(const Dims &, cudaStream_t, const Deriv &, const double *,
                                            const float *, const float *, float *, float *);
 template void op_convert<double, float>(const Dims &, cudaStream_t, const float *, double *, long long);

@@ -71,6 +71,7 @@ struct ps3d_gpu_ctx {
     // FP64 prognostic state and RK accumulators
     double *svor = nullptr, *svori = nullptr, *svorf = nullptr, *vortsm = nullptr;
     double *stage64 = nullptr;   // FP64 staging field for mixed-precision transfers
+    float *svor32 = nullptr;     // FP32 copy of svor read by the mixed vor2vel
     // transient fields (storage type T)
     void *vor = nullptr, *vel = nullptr, *svel = nullptr, *svorts = nullptr, *held = nullptr;
     void *tmp = nullptr;         // NTMP consecutive fields
@@ -276,6 +277,21 @@ void project64(ps3d_gpu_ctx *c)
     c->launches += 5;
 }
 
+// FP32 copy of the prognostic state for the mixed form's vor2vel
+void refresh32(ps3d_gpu_ctx *c)
+{
+    if (c->fp64) return;
+    op_narrow(c->st, c->svor, c->svor32, 3 * c->d.nfield);
+    c->launches += 1;
+}
+
+// projection of an externally set state, then its FP32 copy (mixed form)
+void project_state_mixed(ps3d_gpu_ctx *c)
+{
+    project64(c);
+    refresh32(c);
+}
+
 // ------------------------------------------------------------------ vor2vel
 // inversion.f90:23-226.  The FP64 form follows the reference: the
 // solenoidal projection of svor, then the physical vorticity and the
@@ -332,21 +348,22 @@ template <typename T> int vor2vel_mixed(ps3d_gpu_ctx *c)
 {
     const Dims &d = c->d;
     const long long N = d.nfield;
-    const double *A = c->svor, *B = c->svor + N, *Cc = c->svor + 2 * N;
+    const double *A = c->svor, *B = c->svor + N;
+    const T *A32 = reinterpret_cast<const T *>(c->svor32), *B32 = A32 + N, *C32 = A32 + 2 * N;
     T *cs = tmpf<T>(c, 0), *es = tmpf<T>(c, 1), *ds = tmpf<T>(c, 2), *bs = tmpf<T>(c, 3), *dsg = tmpf<T>(c, 4),
       *as = tmpf<T>(c, 5);
     T *vor = tf<T>(c->vor), *vel = tf<T>(c->vel), *svel = tf<T>(c->svel);
     const Deriv D = c->D();
-    auto colin = [&](int mode, const double *in, T *out) { col_any<T, double>(c, mode, in, out); };
-    // vorticity in physical space (field_combine_physical x3)
-    colin(COL_COMBINE, A, bs);
+    // vorticity in physical space (field_combine_physical x3) from the FP32
+    // copy of the state
+    col<T>(c, COL_COMBINE, A32, bs);
     xyi<T>(c, bs, vor);
-    colin(COL_COMBINE, B, bs);
+    col<T>(c, COL_COMBINE, B32, bs);
     xyi<T>(c, bs, vor + N);
-    colin(COL_COMBINE, Cc, cs);
+    col<T>(c, COL_COMBINE, C32, cs);
     xyi<T>(c, cs, vor + 2 * N);
     // vertical velocity, mean flow, u, v (inversion.f90:86-213)
-    op_v2v_wsrc<T, double>(d, c->st, D, A, B, ds);
+    op_v2v_wsrc<T, T>(d, c->st, D, A32, B32, ds);
     op_v2v_wprep<T>(d, c->st, ds, tf<T>(c->thetam), tf<T>(c->thetap), tf<T>(c->dthetam), tf<T>(c->dthetap),
                     tf<T>(c->green), c->rkz, bs, es, dsg, as);
     col<T>(c, COL_DCT, as, as);
@@ -527,30 +544,52 @@ template <typename T> int step_rk4(ps3d_gpu_ctx *c, double *t, double dt)
         cudaMemcpyAsync(c->held, c->svorts, 3 * N * sizeof(T), cudaMemcpyDeviceToDevice, c->st);
     op_rk4_factors(d, c->st, c->vdiss, c->filt0, c->epq, c->emq, c->epq2, c->emq2);
     c->launches += 1;
-    for (int k = 0; k < 3; ++k)
-        op_rk4_sub1<T>(d, c->st, c->svor + k * N, c->svori + k * N, c->svorf + k * N, sv + k * N, c->filt0, c->emq,
-                       dt2, dt6);
+    const bool mixed = sizeof(T) == sizeof(float);
+    float *s32 = reinterpret_cast<float *>(sv), *q32 = c->svor32;
+    for (int k = 0; k < 3; ++k) {
+        if (mixed)
+            op_rk4m_sub1(d, c->st, c->svor + k * N, c->svori + k * N, c->svorf + k * N, s32 + k * N, q32 + k * N,
+                         c->filt0, c->emq, dt2, dt6);
+        else
+            op_rk4_sub1<T>(d, c->st, c->svor + k * N, c->svori + k * N, c->svorf + k * N, sv + k * N, c->filt0,
+                           c->emq, dt2, dt6);
+    }
     c->launches += 3;
     int rc = rhs_or_hold<T>(c);
     if (rc) return rc;
     *t += dt2;
-    for (int k = 0; k < 3; ++k)
-        op_rk4_sub23<T>(d, c->st, c->svor + k * N, c->svori + k * N, c->svorf + k * N, sv + k * N, c->epq, c->emq,
-                        dt2, dt3);
+    for (int k = 0; k < 3; ++k) {
+        if (mixed)
+            op_rk4m_sub23(d, c->st, c->svor + k * N, c->svori + k * N, c->svorf + k * N, s32 + k * N, q32 + k * N,
+                          c->epq, c->emq, dt2, dt3);
+        else
+            op_rk4_sub23<T>(d, c->st, c->svor + k * N, c->svori + k * N, c->svorf + k * N, sv + k * N, c->epq,
+                            c->emq, dt2, dt3);
+    }
     c->launches += 3;
     rc = rhs_or_hold<T>(c);
     if (rc) return rc;
     *t += dt2;
-    for (int k = 0; k < 3; ++k)
-        op_rk4_sub23<T>(d, c->st, c->svor + k * N, c->svori + k * N, c->svorf + k * N, sv + k * N, c->epq,
-                        c->emq2, dt, dt3);
+    for (int k = 0; k < 3; ++k) {
+        if (mixed)
+            op_rk4m_sub23(d, c->st, c->svor + k * N, c->svori + k * N, c->svorf + k * N, s32 + k * N, q32 + k * N,
+                          c->epq, c->emq2, dt, dt3);
+        else
+            op_rk4_sub23<T>(d, c->st, c->svor + k * N, c->svori + k * N, c->svorf + k * N, sv + k * N, c->epq,
+                            c->emq2, dt, dt3);
+    }
     c->launches += 3;
     rc = rhs_or_hold<T>(c);
     if (rc) return rc;
-    for (int k = 0; k < 3; ++k)
-        op_rk4_sub4<T>(d, c->st, c->svor + k * N, c->svorf + k * N, sv + k * N, c->epq2, c->emq2, dt6);
+    for (int k = 0; k < 3; ++k) {
+        if (mixed)
+            op_rk4m_sub4(d, c->st, c->svor + k * N, c->svorf + k * N, s32 + k * N, q32 + k * N, c->epq2, c->emq2,
+                         dt6);
+        else
+            op_rk4_sub4<T>(d, c->st, c->svor + k * N, c->svorf + k * N, sv + k * N, c->epq2, c->emq2, dt6);
+    }
     c->launches += 3;
-    op_mean_fix(d, c->st, c->svor, c->dstsum, c->fnzi, c->ini, nullptr, 1);
+    op_mean_fix(d, c->st, c->svor, c->dstsum, c->fnzi, c->ini, nullptr, 1, c->svor32);
     c->launches += 1;
     return check(c, "step");
 }
@@ -569,14 +608,14 @@ template <typename T> int step_cn2(ps3d_gpu_ctx *c, double *t, double dt)
     op_cn2_init<T>(d, c->st, c->vortsm, c->svor, sv, dt2);
     op_cn2_update<T>(d, c->st, c->svor, c->vortsm, sv, c->filt0, c->fz, c->vdiss, dt2);
     op_mean_fix(d, c->st, c->svor, c->dstsum, c->fnzi, c->ini, nullptr, 1);
-    if (mixed) project64(c);
+    if (mixed) project_state_mixed(c);
     c->launches += 7;
     for (int it = 0; it < 2; ++it) {
         int rc = rhs_or_hold<T>(c);
         if (rc) return rc;
         op_cn2_update<T>(d, c->st, c->svor, c->vortsm, sv, c->filt0, c->fz, c->vdiss, dt2);
         op_mean_fix(d, c->st, c->svor, c->dstsum, c->fnzi, c->ini, nullptr, 1);
-        if (mixed) project64(c);
+        if (mixed) project_state_mixed(c);
         c->launches += 4;
     }
     *t += dt;
@@ -628,7 +667,7 @@ template <typename T> int setup_fields(ps3d_gpu_ctx *c, const double *vor_phys, 
     cudaMemcpyAsync(c->ini, c->savg, 2 * sizeof(double), cudaMemcpyDeviceToDevice, c->st);
     cudaMemcpyAsync(c->ini_vor_mean, c->savg, 2 * sizeof(double), cudaMemcpyDeviceToHost, c->st);
     c->launches += 1;
-    if (sizeof(T) == sizeof(float)) project64(c);
+    if (sizeof(T) == sizeof(float)) project_state_mixed(c);
     rc = vor2vel<T>(c);
     if (rc) return rc;
     double r1[RED1_N];
@@ -817,7 +856,8 @@ template <typename T> int allocate_fields(ps3d_gpu_ctx *c)
     if (ok && c->cfg.stepper == PS3D_CN2) ok = dalloc(c, &c->vortsm, 3 * f64);
     if (ok && c->cfg.hold_source) ok = dalloc(c, &c->held, 3 * fb);
     if (ok && !c->fp64)
-        ok = dalloc(c, &c->twz32, d.nz * sizeof(float2)) && dalloc(c, &c->sinz32, d.nz * sizeof(float)) &&
+        ok = dalloc(c, &c->svor32, 3 * N * sizeof(float)) &&
+             dalloc(c, &c->twz32, d.nz * sizeof(float2)) && dalloc(c, &c->sinz32, d.nz * sizeof(float)) &&
              dalloc(c, &c->cosz32, d.nz * sizeof(float)) &&
              dalloc(c, &c->stage64, f64) && dalloc(c, &c->phim64, f64) && dalloc(c, &c->phip64, f64) &&
              dalloc(c, &c->twx64, d.nx * sizeof(double2)) && dalloc(c, &c->twy64, d.ny * sizeof(double2)) &&
@@ -996,7 +1036,7 @@ int ps3d_gpu_set_field(ps3d_gpu_ctx *c, int which, const double *host)
     switch (which) {
     case PS3D_FIELD_SVOR:
         rc = upload(c, host, 3, c->svor, true);
-        if (!rc && !c->fp64) project64(c);
+        if (!rc && !c->fp64) project_state_mixed(c);
         break;
     case PS3D_FIELD_VOR: rc = upload(c, host, 3, c->vor, c->fp64); break;
     case PS3D_FIELD_VEL: rc = upload(c, host, 3, c->vel, c->fp64); break;
@@ -1189,7 +1229,7 @@ int ps3d_gpu_advance_host(ps3d_gpu_ctx *c, double *svor, double *t, ps3d_gpu_dia
     if (!svor || !t) return PS3D_ERR_INVALID_ARG;
     rc = upload(c, svor, 3, c->svor, true);
     if (rc) return rc;
-    if (!c->fp64) project64(c);
+    if (!c->fp64) project_state_mixed(c);
     rc = ps3d_gpu_advance(c, t, 1, diag);
     if (rc) return rc;
     return download(c, c->svor, true, 3, svor);
@@ -1209,7 +1249,7 @@ int ps3d_gpu_adjust_vorticity_mean(ps3d_gpu_ctx *c)
 {
     int rc = enter(c);
     if (rc) return rc;
-    op_mean_fix(c->d, c->st, c->svor, c->dstsum, c->fnzi, c->ini, nullptr, 1);
+    op_mean_fix(c->d, c->st, c->svor, c->dstsum, c->fnzi, c->ini, nullptr, 1, c->svor32);
     c->launches += 1;
     return sync_check(c, "adjust_vorticity_mean");
 }
