@@ -156,6 +156,109 @@ __device__ __forceinline__ float warp_incl_scan(float x, int lane)
     return x;
 }
 
+
+// DST post-processing (stafft.f90:531-549 on the packed spectra in xs):
+// interior outputs z = 1..n-1 of both columns into zA / zB
+template <int M>
+__device__ __forceinline__ void post_dst(const float2 *xs, float *zA, float *zB, int lane, float r2s)
+{
+    constexpr int n = 32 * M, KPL = n / 64;
+    float carryA = 0.f, carryB = 0.f;
+#pragma unroll
+    for (int i = 0; i < KPL; ++i) {
+        const int k = lane + 32 * i;
+        const float2 ck = xs[k], cn = xs[(n - k) & (n - 1)];
+        const float ReA = 0.5f * (ck.x + cn.x), ImA = 0.5f * (ck.y - cn.y);
+        const float ReB = 0.5f * (ck.y + cn.y), ImB = -0.5f * (ck.x - cn.x);
+        const float ia = warp_incl_scan((k == 0) ? 0.5f * ReA : ReA, lane) + carryA;
+        const float ib = warp_incl_scan((k == 0) ? 0.5f * ReB : ReB, lane) + carryB;
+        carryA = __shfl_sync(0xffffffffu, ia, 31);
+        carryB = __shfl_sync(0xffffffffu, ib, 31);
+        zA[zpad(2 * k + 1)] = r2s * ia;
+        zB[zpad(2 * k + 1)] = r2s * ib;
+        if (k > 0) {
+            zA[zpad(2 * k)] = -r2s * ImA;
+            zB[zpad(2 * k)] = -r2s * ImB;
+        }
+    }
+}
+
+// DCT post-processing (stafft.f90:458-482): outputs z = 0..n; x1 = x(1)
+// from the direct sum
+template <int M>
+__device__ __forceinline__ void post_dct(const float2 *xs, float *zA, float *zB, int lane, float r2s, float x1A,
+                                         float x1B)
+{
+    constexpr int n = 32 * M, KPL = n / 64;
+    float carryA = 0.f, carryB = 0.f;
+#pragma unroll
+    for (int i = 0; i < KPL; ++i) {
+        const int k = lane + 32 * i;
+        const float2 ck = xs[k], cn = xs[(n - k) & (n - 1)];
+        const float ReA = 0.5f * (ck.x + cn.x), ImA = 0.5f * (ck.y - cn.y);
+        const float ReB = 0.5f * (ck.y + cn.y), ImB = -0.5f * (ck.x - cn.x);
+        const float ia = warp_incl_scan((k == 0) ? 0.f : ImA, lane) + carryA;
+        const float ib = warp_incl_scan((k == 0) ? 0.f : ImB, lane) + carryB;
+        carryA = __shfl_sync(0xffffffffu, ia, 31);
+        carryB = __shfl_sync(0xffffffffu, ib, 31);
+        zA[zpad(2 * k)] = r2s * ReA;
+        zB[zpad(2 * k)] = r2s * ReB;
+        zA[zpad(2 * k + 1)] = x1A - r2s * ia;
+        zB[zpad(2 * k + 1)] = x1B - r2s * ib;
+    }
+    if (lane == 0) {
+        const float2 cm = xs[n / 2];
+        zA[zpad(n)] = r2s * cm.x;
+        zB[zpad(n)] = r2s * cm.y;
+    }
+}
+
+__device__ __forceinline__ float warp_sum(float x)
+{
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
+    return x;
+}
+
+// Theta functions of the vertical-velocity inversion (inversion_utils.f90:
+// 484-542, Dritschel & Frey 2023 eqs 3.4, 3.10, 3.11) for one column
+struct Theta {
+    Harm h;
+    float kl, Q, R, k2ifac, dz, Lz;
+    bool zero;  // (0,0) column: all theta functions vanish
+    __device__ static Theta make(float kl, float k2i, float dz, float Lz, int nz, bool mean)
+    {
+        Theta t;
+        t.h = Harm::make(kl, dz, Lz, nz, mean);
+        t.kl = kl;
+        t.Q = t.h.div * (1.0f + t.h.ef * t.h.ef);
+        t.R = t.h.div * 2.0f * t.h.ef;
+        t.k2ifac = 0.5f * k2i;
+        t.dz = dz;
+        t.Lz = Lz;
+        t.zero = mean;
+        return t;
+    }
+    // thetam, thetap (z values of w) and dthetam, dthetap (dw/dz) at level iz
+    __device__ void at(int iz, float &tm, float &tp, float &dtm, float &dtp) const
+    {
+        if (zero) {
+            tm = tp = dtm = dtp = 0.f;
+            return;
+        }
+        const float zp = dz * (float)iz, zm = Lz - zp;
+        const float Lm = kl * zm, Lp = kl * zp;
+        const float t = h.a * (float)iz;
+        const float ep = ex2(t), em = ex2(h.c - t);
+        const float phm = h.div * (ep - h.ef * em), php = h.div * (em - h.ef * ep);
+        const float dphm = -kl * h.div * (ep + h.ef * em), dphp = kl * h.div * (em + h.ef * ep);
+        tm = k2ifac * (R * Lm * php - Q * Lp * phm);
+        tp = k2ifac * (R * Lp * phm - Q * Lm * php);
+        dtm = -k2ifac * ((Q * Lp - 1.0f) * dphm - R * Lm * dphp);
+        dtp = -k2ifac * ((Q * Lm - 1.0f) * dphp - R * Lp * dphm);
+    }
+};
+
 }  // namespace
 
 // MODE: COL_DST, COL_DCT, COL_DECOMP, COL_COMBINE (see kernels.h)
@@ -166,7 +269,6 @@ __global__ void __launch_bounds__(256, 2) k_colz(const TIN *__restrict__ in, flo
                                               const float *__restrict__ sinz, const float *__restrict__ cosz)
 {
     constexpr int n = 32 * M;  // = nz
-    constexpr int KPL = n / 64;  // spectrum indices per lane for the running sums
     const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
     extern __shared__ __align__(16) unsigned char smz[];
     constexpr int XS = (32 * (M + 1) > n ? 32 * (M + 1) : n);  // float2 per warp
@@ -230,57 +332,14 @@ __global__ void __launch_bounds__(256, 2) k_colz(const TIN *__restrict__ in, flo
             }
         }
         warp_fft<M>(v, xs, twn, lane);
-        // ---- split the packed spectra (k = lane + 32 i), running sums as
-        // warp scans with a carry, outputs to zA / zB
-        float x1A = 0.f, x1B = 0.f;
+        // ---- split the packed spectra, running sums as warp scans with a
+        // carry, outputs to zA / zB
         if (MODE == COL_DCT) {
-            x1A = dsumA;
-            x1B = dsumB;
-#pragma unroll
-            for (int o = 16; o > 0; o >>= 1) {
-                x1A += __shfl_xor_sync(0xffffffffu, x1A, o);
-                x1B += __shfl_xor_sync(0xffffffffu, x1B, o);
-            }
-            x1A = r2s * (0.5f * fA0 + x1A - 0.5f * fAn);
-            x1B = r2s * (0.5f * fB0 + x1B - 0.5f * fBn);
-        }
-        float carryA = 0.f, carryB = 0.f;
-#pragma unroll
-        for (int i = 0; i < KPL; ++i) {
-            const int k = lane + 32 * i;
-            const float2 ck = xs[k], cn = xs[(n - k) & (n - 1)];
-            const float ReA = 0.5f * (ck.x + cn.x), ImA = 0.5f * (ck.y - cn.y);
-            const float ReB = 0.5f * (ck.y + cn.y), ImB = -0.5f * (ck.x - cn.x);
-            float va, vb;
-            if (MODE == COL_DCT) {
-                va = (k == 0) ? 0.f : ImA;
-                vb = (k == 0) ? 0.f : ImB;
-            } else {
-                va = (k == 0) ? 0.5f * ReA : ReA;
-                vb = (k == 0) ? 0.5f * ReB : ReB;
-            }
-            const float ia = warp_incl_scan(va, lane) + carryA;
-            const float ib = warp_incl_scan(vb, lane) + carryB;
-            carryA = __shfl_sync(0xffffffffu, ia, 31);
-            carryB = __shfl_sync(0xffffffffu, ib, 31);
-            if (MODE == COL_DCT) {
-                zA[zpad(2 * k)] = r2s * ReA;
-                zB[zpad(2 * k)] = r2s * ReB;
-                zA[zpad(2 * k + 1)] = x1A - r2s * ia;
-                zB[zpad(2 * k + 1)] = x1B - r2s * ib;
-            } else {
-                zA[zpad(2 * k + 1)] = r2s * ia;
-                zB[zpad(2 * k + 1)] = r2s * ib;
-                if (k > 0) {
-                    zA[zpad(2 * k)] = -r2s * ImA;
-                    zB[zpad(2 * k)] = -r2s * ImB;
-                }
-            }
-        }
-        if (MODE == COL_DCT && lane == 0) {
-            const float2 cm = xs[n / 2];
-            zA[zpad(n)] = r2s * cm.x;
-            zB[zpad(n)] = r2s * cm.y;
+            const float x1A = r2s * (0.5f * fA0 + warp_sum(dsumA) - 0.5f * fAn);
+            const float x1B = r2s * (0.5f * fB0 + warp_sum(dsumB) - 0.5f * fBn);
+            post_dct<M>(xs, zA, zB, lane, r2s, x1A, x1B);
+        } else {
+            post_dst<M>(xs, zA, zB, lane, r2s);
         }
         __syncwarp();
         // ---- coalesced column stores with the mode's boundary rows
@@ -308,6 +367,265 @@ __global__ void __launch_bounds__(256, 2) k_colz(const TIN *__restrict__ in, flo
             }
             out[oA + iz] = ra;
             out[oB + iz] = rb;
+        }
+        __syncwarp();
+    }
+}
+
+// Per-column scalars of a column pair spread over the warp (lane i holds
+// scalar i): they stay out of the registers while the warp FFT runs and are
+// fetched with one shuffle each where needed.
+__device__ __forceinline__ float lane_get(float par, int i) { return __shfl_sync(0xffffffffu, par, i); }
+
+// ------------------------------------------------------------------------
+// Vertical velocity of vor2vel in one kernel (inversion.f90:94-139):
+//   bs = ds(0) thetam + ds(nz) thetap,  es = ds(0) dthetam + ds(nz) dthetap,
+//   dsg = green ds (interior), as = rkz dsg,
+//   w = [0, dst(dsg) + bs, 0],  dw/dz = es + dct(as),
+// with green(kz) = -1/(k^2 + l^2 + rkz^2) and the theta functions evaluated
+// in registers: one read of ds (the second transform re-reads it from L2),
+// one write each of w and dw/dz.
+template <int M>
+__global__ void __launch_bounds__(256, 2) k_colz_w(const float *__restrict__ ds, float *__restrict__ w,
+                                                   float *__restrict__ es, int P, long long npairs,
+                                                   const double *__restrict__ k2l2, const double *__restrict__ k2l2i,
+                                                   float dz, float Lz, const float2 *__restrict__ twn,
+                                                   const float *__restrict__ sinz, const float *__restrict__ cosz)
+{
+    constexpr int n = 32 * M;
+    const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+    extern __shared__ __align__(16) unsigned char smz[];
+    constexpr int XS = (32 * (M + 1) > n ? 32 * (M + 1) : n);
+    constexpr int ZS = n + 1 + (n + 1) / 16 + 2;
+    float2 *xs = reinterpret_cast<float2 *>(smz) + (size_t)wib * (XS + ZS);
+    float *zA = reinterpret_cast<float *>(xs + XS);
+    float *zB = zA + ZS;
+    const float r2s = 1.41421356237309505f * rsqrtf((float)n);
+    const float pk = 3.14159265358979324f / Lz;  // rkz(kz) = pk kz
+    const long long warps = (long long)gridDim.x * (blockDim.x >> 5);
+    for (long long pr = (long long)blockIdx.x * (blockDim.x >> 5) + wib; pr < npairs; pr += warps) {
+        const long long cA = 2 * pr, cB = cA + 1;
+        const long long oA = cA * P, oB = cB * P;
+        // lanes 0..3 (column A) and 8..11 (column B): k^2+l^2, 1/(k^2+l^2),
+        // ds(0), ds(nz)
+        float par = 0.f;
+        if (lane < 16 && (lane & 7) < 4) {
+            const long long c = lane < 8 ? cA : cB;
+            const int f = lane & 3;
+            par = f == 0 ? (float)k2l2[c] : f == 1 ? (float)k2l2i[c] : ds[c * P + (f == 2 ? 0 : n)];
+        }
+        // ---- dst of dsg = green ds
+        {
+            const float k2A = lane_get(par, 0), k2B = lane_get(par, 8);
+            float2 v[M];
+#pragma unroll
+            for (int m = 0; m < M; ++m) {
+                const int j = lane + 32 * m;
+                v[m] = make_float2(0.f, 0.f);
+                if (j > 0) {
+                    const float rj = pk * (float)j, rn = pk * (float)(n - j);
+                    const float rj2 = rj * rj, rn2 = rn * rn;
+                    const float xa = __fdividef(-ds[oA + j], k2A + rj2), ya = __fdividef(-ds[oA + n - j], k2A + rn2);
+                    const float xb = __fdividef(-ds[oB + j], k2B + rj2), yb = __fdividef(-ds[oB + n - j], k2B + rn2);
+                    const float sj = __ldg(&sinz[j]);
+                    v[m] = make_float2(0.5f * (xa - ya) + sj * (xa + ya), 0.5f * (xb - yb) + sj * (xb + yb));
+                }
+            }
+            warp_fft<M>(v, xs, twn, lane);
+        }
+        post_dst<M>(xs, zA, zB, lane, r2s);
+        __syncwarp();
+        {
+            const float d0A = lane_get(par, 2), dnA = lane_get(par, 3), d0B = lane_get(par, 10),
+                        dnB = lane_get(par, 11);
+            const Theta tA = Theta::make(sqrtf(lane_get(par, 0)), lane_get(par, 1), dz, Lz, n, cA == 0);
+            const Theta tB = Theta::make(sqrtf(lane_get(par, 8)), lane_get(par, 9), dz, Lz, n, cB == 0);
+            for (int iz = lane; iz <= n; iz += 32) {
+                float ra = 0.f, rb = 0.f;
+                if (iz > 0 && iz < n) {
+                    float tm, tp, dtm, dtp;
+                    tA.at(iz, tm, tp, dtm, dtp);
+                    ra = zA[zpad(iz)] + d0A * tm + dnA * tp;
+                    tB.at(iz, tm, tp, dtm, dtp);
+                    rb = zB[zpad(iz)] + d0B * tm + dnB * tp;
+                }
+                w[oA + iz] = ra;
+                w[oB + iz] = rb;
+            }
+        }
+        __syncwarp();
+        // ---- dct of as = rkz green ds (as(0) = as(nz) = 0)
+        {
+            const float k2A = lane_get(par, 0), k2B = lane_get(par, 8);
+            // opaque copies of the offsets keep the compiler from hoisting
+            // this phase's loads above the first transform (register spills)
+            long long oA = cA * P, oB = cB * P;
+            asm volatile("" : "+l"(oA), "+l"(oB));
+            float2 v[M];
+            float sA = 0.f, sB = 0.f;
+#pragma unroll
+            for (int m = 0; m < M; ++m) {
+                const int j = lane + 32 * m;
+                v[m] = make_float2(0.f, 0.f);
+                if (j > 0) {
+                    const float rj = pk * (float)j, rn = pk * (float)(n - j);
+                    const float rj2 = rj * rj, rn2 = rn * rn;
+                    const float xa = __fdividef(-rj * ds[oA + j], k2A + rj2);
+                    const float ya = __fdividef(-rn * ds[oA + n - j], k2A + rn2);
+                    const float xb = __fdividef(-rj * ds[oB + j], k2B + rj2);
+                    const float yb = __fdividef(-rn * ds[oB + n - j], k2B + rn2);
+                    const float sj = __ldg(&sinz[j]), cj = __ldg(&cosz[j]);
+                    sA += xa * cj;
+                    sB += xb * cj;
+                    v[m] = make_float2(0.5f * (xa + ya) - sj * (xa - ya), 0.5f * (xb + yb) - sj * (xb - yb));
+                }
+            }
+            const float x1A = r2s * warp_sum(sA), x1B = r2s * warp_sum(sB);
+            warp_fft<M>(v, xs, twn, lane);
+            post_dct<M>(xs, zA, zB, lane, r2s, x1A, x1B);
+        }
+        __syncwarp();
+        {
+            const float d0A = lane_get(par, 2), dnA = lane_get(par, 3), d0B = lane_get(par, 10),
+                        dnB = lane_get(par, 11);
+            const Theta tA = Theta::make(sqrtf(lane_get(par, 0)), lane_get(par, 1), dz, Lz, n, cA == 0);
+            const Theta tB = Theta::make(sqrtf(lane_get(par, 8)), lane_get(par, 9), dz, Lz, n, cB == 0);
+            for (int iz = lane; iz <= n; iz += 32) {
+                float tm, tp, dtm, dtp;
+                tA.at(iz, tm, tp, dtm, dtp);
+                const float ra = zA[zpad(iz)] + d0A * dtm + dnA * dtp;
+                tB.at(iz, tm, tp, dtm, dtp);
+                const float rb = zB[zpad(iz)] + d0B * dtm + dnB * dtp;
+                es[oA + iz] = ra;
+                es[oB + iz] = rb;
+            }
+        }
+        __syncwarp();
+    }
+}
+
+// ------------------------------------------------------------------------
+// es = decompose(central_diffz(combine(f))) in one kernel (the z part of
+// the solenoidal projection, inversion.f90:41-47): combine through the
+// warp FFT, the two-sided difference on the warp's z buffer, then the
+// decomposition; one read of f and one write of es.
+template <int M>
+__global__ void __launch_bounds__(256, 2) k_colz_proj(const float *__restrict__ f, float *__restrict__ es, int P,
+                                                      long long npairs, const double *__restrict__ k2l2, float dz,
+                                                      float Lz, const float2 *__restrict__ twn,
+                                                      const float *__restrict__ sinz)
+{
+    constexpr int n = 32 * M;
+    const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+    extern __shared__ __align__(16) unsigned char smz[];
+    constexpr int XS = (32 * (M + 1) > n ? 32 * (M + 1) : n);
+    constexpr int ZS = n + 1 + (n + 1) / 16 + 2;
+    float2 *xs = reinterpret_cast<float2 *>(smz) + (size_t)wib * (XS + ZS);
+    float *zA = reinterpret_cast<float *>(xs + XS);
+    float *zB = zA + ZS;
+    // the derivative columns reuse the FFT buffer: 2 (n + 1) <= 2 XS floats
+    float *gA = reinterpret_cast<float *>(xs), *gB = gA + (n + 1);
+    const float r2s = 1.41421356237309505f * rsqrtf((float)n);
+    const float dzi = 1.0f / dz, hdzi = 0.5f / dz;
+    const long long warps = (long long)gridDim.x * (blockDim.x >> 5);
+    for (long long pr = (long long)blockIdx.x * (blockDim.x >> 5) + wib; pr < npairs; pr += warps) {
+        const long long cA = 2 * pr, cB = cA + 1;
+        const long long oA = cA * P, oB = cB * P;
+        // lanes 0..2 (column A) and 8..10 (column B): k^2+l^2, f(0), f(nz)
+        float par = 0.f;
+        if (lane < 16 && (lane & 7) < 3) {
+            const long long c = lane < 8 ? cA : cB;
+            const int q = lane & 7;
+            par = q == 0 ? (float)k2l2[c] : f[c * P + (q == 1 ? 0 : n)];
+        }
+        // ---- combine: dst of the interior, plus the harmonic part
+        {
+            float2 v[M];
+#pragma unroll
+            for (int m = 0; m < M; ++m) {
+                const int j = lane + 32 * m;
+                v[m] = make_float2(0.f, 0.f);
+                if (j > 0) {
+                    const float xa = f[oA + j], ya = f[oA + n - j], xb = f[oB + j], yb = f[oB + n - j];
+                    const float sj = __ldg(&sinz[j]);
+                    v[m] = make_float2(0.5f * (xa - ya) + sj * (xa + ya), 0.5f * (xb - yb) + sj * (xb + yb));
+                }
+            }
+            warp_fft<M>(v, xs, twn, lane);
+        }
+        post_dst<M>(xs, zA, zB, lane, r2s);
+        __syncwarp();
+        {
+            const float f0A = lane_get(par, 1), fnA = lane_get(par, 2), f0B = lane_get(par, 9),
+                        fnB = lane_get(par, 10);
+            const Harm hA = Harm::make(sqrtf(lane_get(par, 0)), dz, Lz, n, cA == 0);
+            const Harm hB = Harm::make(sqrtf(lane_get(par, 8)), dz, Lz, n, cB == 0);
+            for (int iz = lane; iz <= n; iz += 32) {
+                float ca, cb;
+                if (iz == 0) {
+                    ca = f0A;
+                    cb = f0B;
+                } else if (iz == n) {
+                    ca = fnA;
+                    cb = fnB;
+                } else {
+                    float pm, pp;
+                    hA.at(iz, n, pm, pp);
+                    ca = zA[zpad(iz)] + f0A * pm + fnA * pp;
+                    hB.at(iz, n, pm, pp);
+                    cb = zB[zpad(iz)] + f0B * pm + fnB * pp;
+                }
+                zA[zpad(iz)] = ca;
+                zB[zpad(iz)] = cb;
+            }
+        }
+        __syncwarp();
+        // ---- central_diffz (inversion_utils.f90:653-673) into gA / gB
+        for (int iz = lane; iz <= n; iz += 32) {
+            const int lo = iz == 0 ? 0 : iz - 1, hi = iz == n ? n : iz + 1;
+            const float sc = (iz == 0 || iz == n) ? dzi : hdzi;
+            gA[iz] = (zA[zpad(hi)] - zA[zpad(lo)]) * sc;
+            gB[iz] = (zB[zpad(hi)] - zB[zpad(lo)]) * sc;
+        }
+        __syncwarp();
+        // ---- decompose: subtract the harmonic part, dst
+        {
+            const float g0A = gA[0], gnA = gA[n], g0B = gB[0], gnB = gB[n];
+            const Harm hA = Harm::make(sqrtf(lane_get(par, 0)), dz, Lz, n, cA == 0);
+            const Harm hB = Harm::make(sqrtf(lane_get(par, 8)), dz, Lz, n, cB == 0);
+            float2 v[M];
+#pragma unroll
+            for (int m = 0; m < M; ++m) {
+                const int j = lane + 32 * m;
+                v[m] = make_float2(0.f, 0.f);
+                if (j > 0) {
+                    float xa = gA[j], ya = gA[n - j], xb = gB[j], yb = gB[n - j];
+                    float pm, pp;
+                    hA.at(j, n, pm, pp);
+                    xa -= g0A * pm + gnA * pp;
+                    ya -= g0A * pp + gnA * pm;
+                    hB.at(j, n, pm, pp);
+                    xb -= g0B * pm + gnB * pp;
+                    yb -= g0B * pp + gnB * pm;
+                    const float sj = __ldg(&sinz[j]);
+                    v[m] = make_float2(0.5f * (xa - ya) + sj * (xa + ya), 0.5f * (xb - yb) + sj * (xb + yb));
+                }
+            }
+            // the boundary rows pass through unchanged
+            if (lane == 0) {
+                zA[zpad(0)] = g0A;
+                zB[zpad(0)] = g0B;
+                zA[zpad(n)] = gnA;
+                zB[zpad(n)] = gnB;
+            }
+            __syncwarp();
+            warp_fft<M>(v, xs, twn, lane);
+        }
+        post_dst<M>(xs, zA, zB, lane, r2s);
+        __syncwarp();
+        for (int iz = lane; iz <= n; iz += 32) {
+            es[oA + iz] = zA[zpad(iz)];
+            es[oB + iz] = zB[zpad(iz)];
         }
         __syncwarp();
     }
@@ -368,6 +686,56 @@ template <typename TIN> void attr_all()
 }
 }  // namespace
 
+template <int M>
+static void launch_w_m(const Dims &d, cudaStream_t st, const float *ds, float *w, float *es, const double *k2l2,
+                       const double *k2l2i, float dz, float Lz, const float2 *twn, const float *sinz, const float *cosz)
+{
+    const long long npairs = d.ncol / 2;
+    long long nb = (npairs + 7) / 8;
+    if (nb > 152 * 24) nb = 152 * 24;
+    k_colz_w<M><<<(unsigned)nb, 256, 8 * colz_smem_per_warp<M>(), st>>>(ds, w, es, d.P, npairs, k2l2, k2l2i, dz, Lz,
+                                                                         twn, sinz, cosz);
+}
+template <int M>
+static void launch_proj_m(const Dims &d, cudaStream_t st, const float *f, float *es, const double *k2l2, float dz,
+                          float Lz, const float2 *twn, const float *sinz)
+{
+    const long long npairs = d.ncol / 2;
+    long long nb = (npairs + 7) / 8;
+    if (nb > 152 * 24) nb = 152 * 24;
+    k_colz_proj<M><<<(unsigned)nb, 256, 8 * colz_smem_per_warp<M>(), st>>>(f, es, d.P, npairs, k2l2, dz, Lz, twn,
+                                                                            sinz);
+}
+
+void columns_w(const Dims &d, cudaStream_t st, const float *ds, float *w, float *es, const double *k2l2,
+               const double *k2l2i, float dz, float Lz, const float2 *twn, const float *sinz, const float *cosz,
+               Probe *pr)
+{
+    if (pr) pr->begin(PROBE_COLUMNS, st);
+    switch (d.nz) {
+    case 64: launch_w_m<2>(d, st, ds, w, es, k2l2, k2l2i, dz, Lz, twn, sinz, cosz); break;
+    case 128: launch_w_m<4>(d, st, ds, w, es, k2l2, k2l2i, dz, Lz, twn, sinz, cosz); break;
+    case 256: launch_w_m<8>(d, st, ds, w, es, k2l2, k2l2i, dz, Lz, twn, sinz, cosz); break;
+    case 512: launch_w_m<16>(d, st, ds, w, es, k2l2, k2l2i, dz, Lz, twn, sinz, cosz); break;
+    default: launch_w_m<32>(d, st, ds, w, es, k2l2, k2l2i, dz, Lz, twn, sinz, cosz); break;
+    }
+    if (pr) pr->end(PROBE_COLUMNS, st, 3.0 * (double)d.ncol * (double)(d.nz + 1) * sizeof(float));
+}
+
+void columns_proj(const Dims &d, cudaStream_t st, const float *f, float *es, const double *k2l2, float dz, float Lz,
+                  const float2 *twn, const float *sinz, Probe *pr)
+{
+    if (pr) pr->begin(PROBE_COLUMNS, st);
+    switch (d.nz) {
+    case 64: launch_proj_m<2>(d, st, f, es, k2l2, dz, Lz, twn, sinz); break;
+    case 128: launch_proj_m<4>(d, st, f, es, k2l2, dz, Lz, twn, sinz); break;
+    case 256: launch_proj_m<8>(d, st, f, es, k2l2, dz, Lz, twn, sinz); break;
+    case 512: launch_proj_m<16>(d, st, f, es, k2l2, dz, Lz, twn, sinz); break;
+    default: launch_proj_m<32>(d, st, f, es, k2l2, dz, Lz, twn, sinz); break;
+    }
+    if (pr) pr->end(PROBE_COLUMNS, st, 2.0 * (double)d.ncol * (double)(d.nz + 1) * sizeof(float));
+}
+
 bool colz_supported(int nz) { return nz == 64 || nz == 128 || nz == 256 || nz == 512 || nz == 1024; }
 
 void colz_init()
@@ -386,6 +754,12 @@ void colz_init()
     cudaMemcpyToSymbol(c_w32z, w, sizeof(w));
     attr_all<float>();
     attr_all<double>();
+    cudaFuncSetAttribute(k_colz_w<16>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)(8 * colz_smem_per_warp<16>()));
+    cudaFuncSetAttribute(k_colz_w<32>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)(8 * colz_smem_per_warp<32>()));
+    cudaFuncSetAttribute(k_colz_proj<16>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)(8 * colz_smem_per_warp<16>()));
+    cudaFuncSetAttribute(k_colz_proj<32>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)(8 * colz_smem_per_warp<32>()));
 }
 
 template <typename TIN>

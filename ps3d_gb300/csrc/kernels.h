@@ -63,6 +63,13 @@ void colz_init();
 template <typename TIN>
 void columns_z(const Dims &d, cudaStream_t st, int mode, const TIN *in, float *out, const double *k2l2, float dz,
                float Lz, const float2 *twn, const float *sinz, const float *cosz, Probe *pr);
+// fused column kernels of the mixed form (colz.cu): the vertical velocity
+// of vor2vel (w and dw/dz from ds) and the z part of the projection
+void columns_w(const Dims &d, cudaStream_t st, const float *ds, float *w, float *es, const double *k2l2,
+               const double *k2l2i, float dz, float Lz, const float2 *twn, const float *sinz, const float *cosz,
+               Probe *pr);
+void columns_proj(const Dims &d, cudaStream_t st, const float *f, float *es, const double *k2l2, float dz, float Lz,
+                  const float2 *twn, const float *sinz, Probe *pr);
 // FP32 warp-per-column-pair transforms (columns32.cu), nz = 32..512
 bool col32_supported(int nz);
 void columns32_init();

@@ -31,8 +31,11 @@ __device__ __forceinline__ float2 cm(float2 a, float2 b)
 template <int R, bool INV> __device__ __forceinline__ void dftR(float2 *v) { dft<R, INV, float2>(v); }
 
 // one radix-R Stockham pass with span NS over N points: inputs x[j + r N/R]
-// of butterfly j, outputs at (j - k) R + k + r NS, k = j mod NS
-template <int N, int R, int NS, bool INV, bool FROM_GLOBAL, bool TO_GLOBAL>
+// of butterfly j, outputs at (j - k) R + k + r NS, k = j mod NS.  HERM
+// (first pass of an inverse transform): the inputs C_k = A_k + i B_k of the
+// two packed lines are rebuilt from the Hermitian rows k and N - k as they
+// are loaded.
+template <int N, int R, int NS, bool INV, bool FROM_GLOBAL, bool TO_GLOBAL, bool HERM = false>
 __device__ __forceinline__ void pass(float2 *sm, const float2 *__restrict__ gin, float2 *__restrict__ gout,
                                      long long gstride, bool valid, float scale, const float2 *__restrict__ tw)
 {
@@ -48,8 +51,21 @@ __device__ __forceinline__ void pass(float2 *sm, const float2 *__restrict__ gin,
 #pragma unroll
             for (int r = 0; r < R; ++r) {
                 const int row = j + r * NB;
-                if (FROM_GLOBAL) v[q][r] = valid ? gin[row * gstride] : make_float2(0.f, 0.f);
-                else v[q][r] = sm[row * LANES + p];
+                if (FROM_GLOBAL && HERM) {
+                    const int mrow = (N - row) & (N - 1);
+                    const int klo = row < mrow ? row : mrow, khi = row < mrow ? mrow : row;
+                    float2 lo = make_float2(0.f, 0.f), hi = make_float2(0.f, 0.f);
+                    if (valid) {
+                        lo = gin[klo * gstride];
+                        if (khi != klo) hi = gin[khi * gstride];
+                    }
+                    v[q][r] = row <= N / 2 ? make_float2(lo.x - hi.y, hi.x + lo.y)
+                                           : make_float2(lo.x + hi.y, lo.y - hi.x);
+                } else if (FROM_GLOBAL) {
+                    v[q][r] = valid ? gin[row * gstride] : make_float2(0.f, 0.f);
+                } else {
+                    v[q][r] = sm[row * LANES + p];
+                }
             }
         }
     }
@@ -82,28 +98,30 @@ __device__ __forceinline__ void pass(float2 *sm, const float2 *__restrict__ gin,
     __syncthreads();
 }
 
-// the complete pass sequence for N = 8^a * {1, 2, 4}
+// the complete pass sequence for N = 8^a * {1, 2, 4}; an inverse
+// transform reads Hermitian rows (HERM first pass)
 template <int N, bool INV, bool FROM_GLOBAL, bool TO_GLOBAL>
 __device__ __forceinline__ void fft_passes(float2 *sm, const float2 *gin, float2 *gout, long long gs, bool valid,
                                            float scale, const float2 *tw)
 {
+    constexpr bool H = INV && FROM_GLOBAL;
     if constexpr (N == 64) {
-        pass<N, 8, 1, INV, FROM_GLOBAL, false>(sm, gin, gout, gs, valid, scale, tw);
+        pass<N, 8, 1, INV, FROM_GLOBAL, false, H>(sm, gin, gout, gs, valid, scale, tw);
         pass<N, 8, 8, INV, false, TO_GLOBAL>(sm, gin, gout, gs, valid, scale, tw);
     } else if constexpr (N == 128) {
-        pass<N, 8, 1, INV, FROM_GLOBAL, false>(sm, gin, gout, gs, valid, scale, tw);
+        pass<N, 8, 1, INV, FROM_GLOBAL, false, H>(sm, gin, gout, gs, valid, scale, tw);
         pass<N, 8, 8, INV, false, false>(sm, gin, gout, gs, valid, scale, tw);
         pass<N, 2, 64, INV, false, TO_GLOBAL>(sm, gin, gout, gs, valid, scale, tw);
     } else if constexpr (N == 256) {
-        pass<N, 8, 1, INV, FROM_GLOBAL, false>(sm, gin, gout, gs, valid, scale, tw);
+        pass<N, 8, 1, INV, FROM_GLOBAL, false, H>(sm, gin, gout, gs, valid, scale, tw);
         pass<N, 8, 8, INV, false, false>(sm, gin, gout, gs, valid, scale, tw);
         pass<N, 4, 64, INV, false, TO_GLOBAL>(sm, gin, gout, gs, valid, scale, tw);
     } else if constexpr (N == 512) {
-        pass<N, 8, 1, INV, FROM_GLOBAL, false>(sm, gin, gout, gs, valid, scale, tw);
+        pass<N, 8, 1, INV, FROM_GLOBAL, false, H>(sm, gin, gout, gs, valid, scale, tw);
         pass<N, 8, 8, INV, false, false>(sm, gin, gout, gs, valid, scale, tw);
         pass<N, 8, 64, INV, false, TO_GLOBAL>(sm, gin, gout, gs, valid, scale, tw);
     } else {  // 1024
-        pass<N, 8, 1, INV, FROM_GLOBAL, false>(sm, gin, gout, gs, valid, scale, tw);
+        pass<N, 8, 1, INV, FROM_GLOBAL, false, H>(sm, gin, gout, gs, valid, scale, tw);
         pass<N, 8, 8, INV, false, false>(sm, gin, gout, gs, valid, scale, tw);
         pass<N, 8, 64, INV, false, false>(sm, gin, gout, gs, valid, scale, tw);
         pass<N, 2, 512, INV, false, TO_GLOBAL>(sm, gin, gout, gs, valid, scale, tw);
@@ -141,21 +159,7 @@ __global__ void __launch_bounds__(LinePlan<N>::T) k_lines32(const float *__restr
             if (k > 0 && k < H) o[(N - k) * gs] = make_float2(aim * s, bim * s);
         }
     } else {
-        // rebuild C_k = A_k + i B_k from the Hermitian rows of both lines
-        for (int e = threadIdx.x; e < (H + 1) * LANES; e += T) {
-            const int k = e / LANES, q = e & (LANES - 1);
-            float2 lo = make_float2(0.f, 0.f), hi = make_float2(0.f, 0.f);
-            if (z0 + 2 * q < P) {
-                const float2 *i2 =
-                    reinterpret_cast<const float2 *>(in) + (((long long)blockIdx.y * batch_stride + z0 + 2 * q) >> 1);
-                lo = i2[k * gs];
-                if (k > 0 && k < H) hi = i2[(N - k) * gs];
-            }
-            smL[k * LANES + q] = make_float2(lo.x - hi.y, hi.x + lo.y);
-            if (k > 0 && k < H) smL[(N - k) * LANES + q] = make_float2(lo.x + hi.y, lo.y - hi.x);
-        }
-        __syncthreads();
-        fft_passes<N, true, false, true>(smL, gin, gout, gs, valid, s, tw);
+        fft_passes<N, true, true, true>(smL, gin, gout, gs, valid, s, tw);
     }
 }
 

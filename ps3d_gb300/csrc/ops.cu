@@ -180,31 +180,32 @@ void op_v2v_wfinish(const Dims &d, cudaStream_t st, const T *dsg, const T *bs, c
 }
 
 // horizontally averaged flow from the (0,0) column (inversion.f90:150-165):
-// ubar = dct(-rkzi B) + B(nz) gamtop - B(0) gambot, vbar likewise.  One block;
-// the cosine transform of a single column is a direct O(nz^2) sum.
+// ubar = dct(-rkzi B) + B(nz) gamtop - B(0) gambot, vbar likewise.  The
+// cosine transform of the single column is a direct O(nz^2) sum, one warp
+// per output level.
 template <typename S>
 __global__ void k_v2v_meanflow(int nz, const S *__restrict__ A, const S *__restrict__ B,
                                const double *__restrict__ rkzi, const double *__restrict__ dctcos,
                                const double *__restrict__ gamtop, const double *__restrict__ gambot,
                                double *__restrict__ ubar, double *__restrict__ vbar)
 {
-    extern __shared__ double sh[];
-    double *xu = sh, *xv = sh + (nz + 1);
-    for (int iz = threadIdx.x; iz <= nz; iz += blockDim.x) {
-        const bool in = iz > 0 && iz < nz;
-        xu[iz] = in ? -rkzi[iz] * (double)B[iz] : 0.0;
-        xv[iz] = in ? rkzi[iz] * (double)A[iz] : 0.0;
+    const int lane = threadIdx.x & 31;
+    const int k = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+    if (k > nz) return;
+    double su = 0.0, sv = 0.0;
+    for (int j = 1 + lane; j < nz; j += 32) {
+        const double c = dctcos[(int)(((long long)j * k) % (2 * nz))];
+        su -= rkzi[j] * (double)B[j] * c;
+        sv += rkzi[j] * (double)A[j] * c;
     }
-    __syncthreads();
-    const double s = sqrt(2.0 / (double)nz);
-    const double a0 = (double)A[0], an = (double)A[nz], b0 = (double)B[0], bn = (double)B[nz];
-    for (int k = threadIdx.x; k <= nz; k += blockDim.x) {
-        double su = 0.0, sv = 0.0;
-        for (int j = 1; j < nz; ++j) {
-            const double c = dctcos[(int)(((long long)j * k) % (2 * nz))];
-            su += xu[j] * c;
-            sv += xv[j] * c;
-        }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        su += __shfl_xor_sync(0xffffffffu, su, o);
+        sv += __shfl_xor_sync(0xffffffffu, sv, o);
+    }
+    if (lane == 0) {
+        const double s = sqrt(2.0 / (double)nz);
+        const double a0 = (double)A[0], an = (double)A[nz], b0 = (double)B[0], bn = (double)B[nz];
         ubar[k] = s * su + bn * gamtop[k] - b0 * gambot[k];
         vbar[k] = s * sv - an * gamtop[k] + a0 * gambot[k];
     }
@@ -213,8 +214,8 @@ template <typename S>
 void op_v2v_meanflow(const Dims &d, cudaStream_t st, const S *A, const S *B, const Tables &tb, double *ubar,
                      double *vbar)
 {
-    k_v2v_meanflow<S><<<1, 256, 2 * (d.nz + 1) * sizeof(double), st>>>(d.nz, A, B, tb.rkzi, tb.dctcos,
-                                                                         tb.gamtop, tb.gambot, ubar, vbar);
+    k_v2v_meanflow<S><<<(d.nz + 1 + 7) / 8, 256, 0, st>>>(d.nz, A, B, tb.rkzi, tb.dctcos, tb.gamtop, tb.gambot,
+                                                          ubar, vbar);
 }
 
 // u = k2l2i (D_x es + D_y cs), v = k2l2i (D_y es - D_x cs), (0,0) = ubar, vbar

@@ -364,14 +364,24 @@ template <typename T> int vor2vel_mixed(ps3d_gpu_ctx *c)
     xyi<T>(c, cs, vor + 2 * N);
     // vertical velocity, mean flow, u, v (inversion.f90:86-213)
     op_v2v_wsrc<T, T>(d, c->st, D, A32, B32, ds);
-    op_v2v_wprep<T>(d, c->st, ds, tf<T>(c->thetam), tf<T>(c->thetap), tf<T>(c->dthetam), tf<T>(c->dthetap),
-                    tf<T>(c->green), c->rkz, bs, es, dsg, as);
-    col<T>(c, COL_DCT, as, as);
-    col<T>(c, COL_DST, dsg, dsg);
-    op_v2v_wfinish<T>(d, c->st, dsg, bs, as, svel + 2 * N, es);
+    if (colz_supported(d.nz)) {
+        // w and dw/dz in one column kernel (theta functions and the Green
+        // function evaluated in registers)
+        columns_w(d, c->st, reinterpret_cast<const float *>(ds), reinterpret_cast<float *>(svel + 2 * N),
+                  reinterpret_cast<float *>(es), c->k2l2, c->k2l2i, (float)c->dx[2], (float)c->cfg.extent[2],
+                  c->twz32, c->sinz32, c->cosz32, &c->probe);
+        c->launches += 1;
+    } else {
+        op_v2v_wprep<T>(d, c->st, ds, tf<T>(c->thetam), tf<T>(c->thetap), tf<T>(c->dthetam), tf<T>(c->dthetap),
+                        tf<T>(c->green), c->rkz, bs, es, dsg, as);
+        col<T>(c, COL_DCT, as, as);
+        col<T>(c, COL_DST, dsg, dsg);
+        op_v2v_wfinish<T>(d, c->st, dsg, bs, as, svel + 2 * N, es);
+        c->launches += 2;
+    }
     op_v2v_meanflow<double>(d, c->st, A, B, c->tables(), c->ubar, c->vbar);
     op_v2v_uv<T>(d, c->st, D, c->k2l2i, es, cs, c->ubar, c->vbar, svel, svel + N);
-    c->launches += 5;
+    c->launches += 3;
     for (int k = 0; k < 3; ++k) xyi<T>(c, svel + k * N, vel + k * N);
     return check(c, "vor2vel");
 }
@@ -385,11 +395,18 @@ template <typename T> void project_source(ps3d_gpu_ctx *c)
     T *S1 = tf<T>(c->svorts), *S2 = S1 + N, *S3 = S1 + 2 * N;
     T *cs = tmpf<T>(c, 0), *es = tmpf<T>(c, 1), *ds = tmpf<T>(c, 2);
     op_v2v_ds<T, T>(d, c->st, c->D(), S1, S2, ds);
-    col<T>(c, COL_COMBINE, S3, cs);
-    op_diffz<T>(d, c->st, c->dzi, cs, es);
-    col<T>(c, COL_DECOMP, es, es);
+    if (colz_supported(d.nz)) {
+        columns_proj(d, c->st, reinterpret_cast<const float *>(S3), reinterpret_cast<float *>(es), c->k2l2,
+                     (float)c->dx[2], (float)c->cfg.extent[2], c->twz32, c->sinz32, &c->probe);
+        c->launches += 1;
+    } else {
+        col<T>(c, COL_COMBINE, S3, cs);
+        op_diffz<T>(d, c->st, c->dzi, cs, es);
+        col<T>(c, COL_DECOMP, es, es);
+        c->launches += 1;
+    }
     op_v2v_project<T, T>(d, c->st, c->D(), c->k2l2i, es, ds, S1, S2);
-    c->launches += 3;
+    c->launches += 2;
 }
 
 // ------------------------------------------------------------------- source
