@@ -13,8 +13,12 @@
 // Warp FFT of n = 32*M points: lane l holds c[l + 32 m] (m < M); an M-point
 // DFT in registers, a twiddle, a transpose through the warp's shared buffer,
 // an M-point DFT over the other index, and S = 32/M lanes combined by
-// shuffles.  Inputs stored as FP64 (the prognostic state) are narrowed with
-// integer arithmetic, keeping GB300's FP64 pipe out of the kernel.
+// shuffles.  Both shared-memory exchanges use XOR-swizzled layouts that keep
+// every access free of bank conflicts.  The post-processing produces output
+// levels 2k and 2k+1 in the same lane, so results leave as coalesced float2
+// stores straight from registers.  Inputs stored as FP64 (the prognostic
+// state) are narrowed with integer arithmetic, keeping GB300's FP64 pipe out
+// of the kernel.
 #include "kernels.h"
 
 namespace ps3d {
@@ -39,6 +43,8 @@ template <int M> __device__ __forceinline__ int brev(int r)
     return o;
 }
 
+template <int M> constexpr int lg2() { return M <= 1 ? 0 : 1 + lg2<M / 2>(); }
+
 __device__ __forceinline__ float ld(const float *p, long long i) { return p[i]; }
 __device__ __forceinline__ float ld(const double *p, long long i) { return narrow32(p[i]); }
 
@@ -52,18 +58,21 @@ __device__ __forceinline__ float ex2(float x)
 
 // harmonic functions of one column (inversion_utils.f90:484-542):
 // phim(z) = div (ep - ef em), phip(z) = div (em - ef ep), ep = exp(-kl zp),
-// em = exp(-kl zm) = ep at the mirrored level; phip(iz) = phim(nz - iz)
+// em = exp(-kl zm) = ep at the mirrored level; phip(iz) = phim(nz - iz).
+// Both exponents are a times an exact level count (iz or nz - iz), so the
+// exponential near either boundary carries one rounding of its argument.
+// The (0,0) column uses the linear functions (nz - iz)/nz and iz/nz.
 struct Harm {
-    float a, c, ef, div, inv_n;
+    float a, ef, div, g, inv_n;
     bool mean;
     __device__ static Harm make(float kl, float dz, float Lz, int nz, bool mean)
     {
         const float l2e = 1.4426950408889634f;
         Harm h;
         h.a = -kl * dz * l2e;
-        h.c = -kl * Lz * l2e;
-        h.ef = ex2(h.c);
+        h.ef = ex2(-kl * Lz * l2e);
         h.div = 1.0f / (1.0f - h.ef * h.ef);
+        h.g = ex2(h.a);  // ep(iz + 1) = g ep(iz)
         h.inv_n = 1.0f / (float)nz;
         h.mean = mean;
         return h;
@@ -74,10 +83,26 @@ struct Harm {
             pp = (float)iz * inv_n;
             pm = (float)(nz - iz) * inv_n;
         } else {
-            const float t = a * (float)iz;
-            const float ep = ex2(t), em = ex2(c - t);
+            const float ep = ex2(a * (float)iz), em = ex2(a * (float)(nz - iz));
             pm = div * (ep - ef * em);
             pp = div * (em - ef * ep);
+        }
+    }
+    // levels z0 and z0 + 1 from two exponentials
+    __device__ void at2(int z0, int nz, float &pm0, float &pp0, float &pm1, float &pp1) const
+    {
+        if (mean) {
+            pp0 = (float)z0 * inv_n;
+            pm0 = (float)(nz - z0) * inv_n;
+            pp1 = (float)(z0 + 1) * inv_n;
+            pm1 = (float)(nz - z0 - 1) * inv_n;
+        } else {
+            const float ep0 = ex2(a * (float)z0), em1 = ex2(a * (float)(nz - z0 - 1));
+            const float ep1 = ep0 * g, em0 = em1 * g;
+            pm0 = div * (ep0 - ef * em0);
+            pp0 = div * (em0 - ef * ep0);
+            pm1 = div * (ep1 - ef * em1);
+            pp1 = div * (em1 - ef * ep1);
         }
     }
 };
@@ -99,8 +124,32 @@ template <int M> __device__ __forceinline__ void dif(float2 *v)
     }
 }
 
+// Swizzles of the warp buffer (float2 slots; a half-warp of 8-byte accesses
+// is conflict free when its slots differ modulo 16).
+// Transpose slot of (lane l, column b < M): l M + (b ^ tsw(l)).  Writes (fixed
+// b, 16 consecutive l) and reads (lanes (b, h) of rows h + S t) both land on
+// 16 distinct slots modulo 16.
+template <int M> __device__ __forceinline__ int tsw(int l)
+{
+    if constexpr (M == 32) {
+        return l & 31;
+    } else {
+        constexpr int B = lg2<M>();
+        const int x = (l >> (4 - B)) & (M - 1);
+        return (x >> 1) | ((x & 1) << (B - 1));
+    }
+}
+// natural-order spectrum slot of X[x]: bit-field XOR with the high bits,
+// a bijection (the XOR source lies above its target)
+template <int M> __device__ __forceinline__ int nsw(int x)
+{
+    constexpr int B = lg2<M>(), S = 32 / M;
+    if constexpr (S == 1) return x;
+    else return x ^ (((x >> (2 * B)) & (S - 1)) << (B - 1));
+}
+
 // n = 32 M point forward FFT of the warp's sequence; on entry lane l holds
-// v[m] = c[l + 32 m]; on exit X[k] (natural order) is in xs[0..n).
+// v[m] = c[l + 32 m]; on exit X[k] (natural order) is in xs[nsw(k)].
 template <int M>
 __device__ __forceinline__ void warp_fft(float2 *v, float2 *xs, const float2 *__restrict__ twn, int lane)
 {
@@ -110,12 +159,16 @@ __device__ __forceinline__ void warp_fft(float2 *v, float2 *xs, const float2 *__
 #pragma unroll
     for (int r = 1; r < M; ++r) v[r] = fm(v[r], __ldg(&twn[(lane * brev<M>(r)) & (n - 1)]));
     // transpose: lane (b, h) = (lane / S, lane % S) gathers Z[h + S t][b]
+    const int swl = tsw<M>(lane);
 #pragma unroll
-    for (int r = 0; r < M; ++r) xs[lane * (M + 1) + brev<M>(r)] = v[r];
+    for (int r = 0; r < M; ++r) xs[lane * M + (brev<M>(r) ^ swl)] = v[r];
     __syncwarp();
     const int b = lane / S, h = lane % S;
 #pragma unroll
-    for (int t = 0; t < M; ++t) v[t] = xs[(h + S * t) * (M + 1) + b];
+    for (int t = 0; t < M; ++t) {
+        const int lp = h + S * t;
+        v[t] = xs[lp * M + (b ^ tsw<M>(lp))];
+    }
     __syncwarp();
     dif<M>(v);  // register r: F_h[a'], a' = brev(r)
     if (S > 1) {
@@ -139,11 +192,9 @@ __device__ __forceinline__ void warp_fft(float2 *v, float2 *xs, const float2 *__
     }
     const int e = brev<S>(h);
 #pragma unroll
-    for (int r = 0; r < M; ++r) xs[b + M * brev<M>(r) + M * M * e] = v[r];
+    for (int r = 0; r < M; ++r) xs[nsw<M>(b + M * brev<M>(r) + M * M * e)] = v[r];
     __syncwarp();
 }
-
-__device__ __forceinline__ int zpad(int z) { return z + (z >> 4); }
 
 // inclusive warp scan of one value per lane
 __device__ __forceinline__ float warp_incl_scan(float x, int lane)
@@ -156,63 +207,6 @@ __device__ __forceinline__ float warp_incl_scan(float x, int lane)
     return x;
 }
 
-
-// DST post-processing (stafft.f90:531-549 on the packed spectra in xs):
-// interior outputs z = 1..n-1 of both columns into zA / zB
-template <int M>
-__device__ __forceinline__ void post_dst(const float2 *xs, float *zA, float *zB, int lane, float r2s)
-{
-    constexpr int n = 32 * M, KPL = n / 64;
-    float carryA = 0.f, carryB = 0.f;
-#pragma unroll
-    for (int i = 0; i < KPL; ++i) {
-        const int k = lane + 32 * i;
-        const float2 ck = xs[k], cn = xs[(n - k) & (n - 1)];
-        const float ReA = 0.5f * (ck.x + cn.x), ImA = 0.5f * (ck.y - cn.y);
-        const float ReB = 0.5f * (ck.y + cn.y), ImB = -0.5f * (ck.x - cn.x);
-        const float ia = warp_incl_scan((k == 0) ? 0.5f * ReA : ReA, lane) + carryA;
-        const float ib = warp_incl_scan((k == 0) ? 0.5f * ReB : ReB, lane) + carryB;
-        carryA = __shfl_sync(0xffffffffu, ia, 31);
-        carryB = __shfl_sync(0xffffffffu, ib, 31);
-        zA[zpad(2 * k + 1)] = r2s * ia;
-        zB[zpad(2 * k + 1)] = r2s * ib;
-        if (k > 0) {
-            zA[zpad(2 * k)] = -r2s * ImA;
-            zB[zpad(2 * k)] = -r2s * ImB;
-        }
-    }
-}
-
-// DCT post-processing (stafft.f90:458-482): outputs z = 0..n; x1 = x(1)
-// from the direct sum
-template <int M>
-__device__ __forceinline__ void post_dct(const float2 *xs, float *zA, float *zB, int lane, float r2s, float x1A,
-                                         float x1B)
-{
-    constexpr int n = 32 * M, KPL = n / 64;
-    float carryA = 0.f, carryB = 0.f;
-#pragma unroll
-    for (int i = 0; i < KPL; ++i) {
-        const int k = lane + 32 * i;
-        const float2 ck = xs[k], cn = xs[(n - k) & (n - 1)];
-        const float ReA = 0.5f * (ck.x + cn.x), ImA = 0.5f * (ck.y - cn.y);
-        const float ReB = 0.5f * (ck.y + cn.y), ImB = -0.5f * (ck.x - cn.x);
-        const float ia = warp_incl_scan((k == 0) ? 0.f : ImA, lane) + carryA;
-        const float ib = warp_incl_scan((k == 0) ? 0.f : ImB, lane) + carryB;
-        carryA = __shfl_sync(0xffffffffu, ia, 31);
-        carryB = __shfl_sync(0xffffffffu, ib, 31);
-        zA[zpad(2 * k)] = r2s * ReA;
-        zB[zpad(2 * k)] = r2s * ReB;
-        zA[zpad(2 * k + 1)] = x1A - r2s * ia;
-        zB[zpad(2 * k + 1)] = x1B - r2s * ib;
-    }
-    if (lane == 0) {
-        const float2 cm = xs[n / 2];
-        zA[zpad(n)] = r2s * cm.x;
-        zB[zpad(n)] = r2s * cm.y;
-    }
-}
-
 __device__ __forceinline__ float warp_sum(float x)
 {
 #pragma unroll
@@ -220,48 +214,64 @@ __device__ __forceinline__ float warp_sum(float x)
     return x;
 }
 
-// Theta functions of the vertical-velocity inversion (inversion_utils.f90:
-// 484-542, Dritschel & Frey 2023 eqs 3.4, 3.10, 3.11) for one column
-struct Theta {
-    Harm h;
-    float kl, Q, R, k2ifac, dz, Lz;
-    bool zero;  // (0,0) column: all theta functions vanish
-    __device__ static Theta make(float kl, float k2i, float dz, float Lz, int nz, bool mean)
-    {
-        Theta t;
-        t.h = Harm::make(kl, dz, Lz, nz, mean);
-        t.kl = kl;
-        t.Q = t.h.div * (1.0f + t.h.ef * t.h.ef);
-        t.R = t.h.div * 2.0f * t.h.ef;
-        t.k2ifac = 0.5f * k2i;
-        t.dz = dz;
-        t.Lz = Lz;
-        t.zero = mean;
-        return t;
-    }
-    // thetam, thetap (z values of w) and dthetam, dthetap (dw/dz) at level iz
-    __device__ void at(int iz, float &tm, float &tp, float &dtm, float &dtp) const
-    {
-        if (zero) {
-            tm = tp = dtm = dtp = 0.f;
-            return;
+// Per-column scalars of a column pair spread over the warp (lane i holds
+// scalar i): they stay out of the registers while the warp FFT runs and are
+// fetched with one shuffle each where needed.
+__device__ __forceinline__ float lane_get(float par, int i) { return __shfl_sync(0xffffffffu, par, i); }
+
+// Post-processing of the packed spectra in xs (stafft.f90:458-482 cosine,
+// :531-549 sine): for k = lane + 32 i calls emit(k, eA, oA, eB, oB) with the
+// transform values of both columns at levels 2k and 2k+1 (sine: the value at
+// level 0 is meaningless; cosine: x1 is the direct sum giving level 1's
+// constant).  Running sums are warp scans with a carry.
+template <int M, bool COS, typename F>
+__device__ __forceinline__ void post(const float2 *xs, int lane, float r2s, float x1A, float x1B, F &&emit)
+{
+    constexpr int n = 32 * M, KPL = n / 64;
+    float carryA = 0.f, carryB = 0.f;
+#pragma unroll
+    for (int i = 0; i < KPL; ++i) {
+        const int k = lane + 32 * i;
+        const float2 ck = xs[nsw<M>(k)], cn = xs[nsw<M>((n - k) & (n - 1))];
+        const float ReA = 0.5f * (ck.x + cn.x), ImA = 0.5f * (ck.y - cn.y);
+        const float ReB = 0.5f * (ck.y + cn.y), ImB = -0.5f * (ck.x - cn.x);
+        float va, vb;
+        if (COS) {
+            va = (k == 0) ? 0.f : ImA;
+            vb = (k == 0) ? 0.f : ImB;
+        } else {
+            va = (k == 0) ? 0.5f * ReA : ReA;
+            vb = (k == 0) ? 0.5f * ReB : ReB;
         }
-        const float zp = dz * (float)iz, zm = Lz - zp;
-        const float Lm = kl * zm, Lp = kl * zp;
-        const float t = h.a * (float)iz;
-        const float ep = ex2(t), em = ex2(h.c - t);
-        const float phm = h.div * (ep - h.ef * em), php = h.div * (em - h.ef * ep);
-        const float dphm = -kl * h.div * (ep + h.ef * em), dphp = kl * h.div * (em + h.ef * ep);
-        tm = k2ifac * (R * Lm * php - Q * Lp * phm);
-        tp = k2ifac * (R * Lp * phm - Q * Lm * php);
-        dtm = -k2ifac * ((Q * Lp - 1.0f) * dphm - R * Lm * dphp);
-        dtp = -k2ifac * ((Q * Lm - 1.0f) * dphp - R * Lp * dphm);
+        const float ia = warp_incl_scan(va, lane) + carryA;
+        const float ib = warp_incl_scan(vb, lane) + carryB;
+        carryA = __shfl_sync(0xffffffffu, ia, 31);
+        carryB = __shfl_sync(0xffffffffu, ib, 31);
+        if (COS) emit(k, r2s * ReA, x1A - r2s * ia, r2s * ReB, x1B - r2s * ib);
+        else emit(k, -r2s * ImA, r2s * ia, -r2s * ImB, r2s * ib);
     }
-};
+}
+
+// dst pre-processing of x(j), x(n-j) of both columns
+__device__ __forceinline__ float2 pre_sine(float xa, float ya, float xb, float yb, float sj)
+{
+    return make_float2(0.5f * (xa - ya) + sj * (xa + ya), 0.5f * (xb - yb) + sj * (xb + yb));
+}
+// dct pre-processing
+__device__ __forceinline__ float2 pre_cosine(float xa, float ya, float xb, float yb, float sj)
+{
+    return make_float2(0.5f * (xa + ya) - sj * (xa - ya), 0.5f * (xb + yb) - sj * (xb - yb));
+}
+
+__device__ __forceinline__ void st2(float *col, int k, float e, float o)
+{
+    reinterpret_cast<float2 *>(col)[k] = make_float2(e, o);
+}
 
 }  // namespace
 
-// MODE: COL_DST, COL_DCT, COL_DECOMP, COL_COMBINE (see kernels.h)
+// MODE: COL_DST, COL_DCT, COL_DECOMP, COL_COMBINE (see kernels.h).  Safe in
+// place: a pair's inputs are all read before its outputs are written.
 template <int MODE, int M, typename TIN>
 __global__ void __launch_bounds__(256, 2) k_colz(const TIN *__restrict__ in, float *__restrict__ out, int P,
                                               long long npairs, const double *__restrict__ k2l2, float dz,
@@ -271,120 +281,187 @@ __global__ void __launch_bounds__(256, 2) k_colz(const TIN *__restrict__ in, flo
     constexpr int n = 32 * M;  // = nz
     const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
     extern __shared__ __align__(16) unsigned char smz[];
-    constexpr int XS = (32 * (M + 1) > n ? 32 * (M + 1) : n);  // float2 per warp
-    constexpr int ZS = n + 1 + (n + 1) / 16 + 2;                // floats per output column
-    float2 *xs = reinterpret_cast<float2 *>(smz) + (size_t)wib * (XS + ZS);
-    float *zA = reinterpret_cast<float *>(xs + XS);
-    float *zB = zA + ZS;
-    const float s = rsqrtf((float)n);
-    const float r2s = 1.41421356237309505f * s;
+    float2 *xs = reinterpret_cast<float2 *>(smz) + (size_t)wib * n;
+    const float r2s = 1.41421356237309505f * rsqrtf((float)n);
     const long long warps = (long long)gridDim.x * (blockDim.x >> 5);
     for (long long pr = (long long)blockIdx.x * (blockDim.x >> 5) + wib; pr < npairs; pr += warps) {
         const long long cA = 2 * pr, cB = cA + 1;
         const long long oA = cA * P, oB = cB * P;
-        float fA0 = 0.f, fAn = 0.f, fB0 = 0.f, fBn = 0.f;
-        Harm hA{}, hB{};
-        if (MODE == COL_DECOMP || MODE == COL_COMBINE || MODE == COL_DCT) {
-            fA0 = ld(in, oA);
-            fAn = ld(in, oA + n);
-            fB0 = ld(in, oB);
-            fBn = ld(in, oB + n);
-        }
-        if (MODE == COL_DECOMP || MODE == COL_COMBINE) {
-            hA = Harm::make(sqrtf((float)k2l2[cA]), dz, Lz, n, cA == 0);
-            hB = Harm::make(sqrtf((float)k2l2[cB]), dz, Lz, n, cB == 0);
+        // lanes 0..2 (column A) and 8..10 (column B): f(0), f(nz), kl
+        float par = 0.f;
+        if (lane < 16 && (lane & 7) < 3) {
+            const long long c = lane < 8 ? cA : cB;
+            const int q = lane & 7;
+            par = q == 2 ? sqrtf((float)k2l2[c]) : ld(in, c * P + (q == 0 ? 0 : n));
         }
         // ---- pre-processed sequence wk (both columns), lane l: j = l + 32 m
-        float2 v[M];
         float dsumA = 0.f, dsumB = 0.f;  // DCT direct sum for x(1)
+        {
+            float2 v[M];
+            const float f0A = lane_get(par, 0), fnA = lane_get(par, 1), f0B = lane_get(par, 8),
+                        fnB = lane_get(par, 9);
+            Harm hA{}, hB{};
+            if (MODE == COL_DECOMP) {
+                hA = Harm::make(lane_get(par, 2), dz, Lz, n, cA == 0);
+                hB = Harm::make(lane_get(par, 10), dz, Lz, n, cB == 0);
+            }
 #pragma unroll
-        for (int m = 0; m < M; ++m) {
-            const int j = lane + 32 * m;
-            float xa = 0.f, xb = 0.f, ya = 0.f, yb = 0.f;  // x(j), x(n-j)
-            if (j > 0) {
-                xa = ld(in, oA + j);
-                xb = ld(in, oB + j);
-                ya = ld(in, oA + n - j);
-                yb = ld(in, oB + n - j);
-            }
-            if (MODE == COL_DECOMP && j > 0) {
-                float pm, pp;
-                hA.at(j, n, pm, pp);
-                xa -= fA0 * pm + fAn * pp;
-                ya -= fA0 * pp + fAn * pm;
-                hB.at(j, n, pm, pp);
-                xb -= fB0 * pm + fBn * pp;
-                yb -= fB0 * pp + fBn * pm;
-            }
-            const float sj = __ldg(&sinz[j]);
-            if (MODE == COL_DCT) {
-                if (j == 0) {
-                    v[m] = make_float2(0.5f * (fA0 + fAn), 0.5f * (fB0 + fBn));
-                } else {
-                    const float cj = __ldg(&cosz[j]);
-                    dsumA += xa * cj;
-                    dsumB += xb * cj;
-                    v[m] = make_float2(0.5f * (xa + ya) - sj * (xa - ya), 0.5f * (xb + yb) - sj * (xb - yb));
+            for (int m = 0; m < M; ++m) {
+                const int j = lane + 32 * m;
+                float xa = 0.f, xb = 0.f, ya = 0.f, yb = 0.f;  // x(j), x(n-j)
+                if (j > 0) {
+                    xa = ld(in, oA + j);
+                    xb = ld(in, oB + j);
+                    ya = ld(in, oA + n - j);
+                    yb = ld(in, oB + n - j);
                 }
-            } else {
-                v[m] = (j == 0) ? make_float2(0.f, 0.f)
-                                : make_float2(0.5f * (xa - ya) + sj * (xa + ya), 0.5f * (xb - yb) + sj * (xb + yb));
-            }
-        }
-        warp_fft<M>(v, xs, twn, lane);
-        // ---- split the packed spectra, running sums as warp scans with a
-        // carry, outputs to zA / zB
-        if (MODE == COL_DCT) {
-            const float x1A = r2s * (0.5f * fA0 + warp_sum(dsumA) - 0.5f * fAn);
-            const float x1B = r2s * (0.5f * fB0 + warp_sum(dsumB) - 0.5f * fBn);
-            post_dct<M>(xs, zA, zB, lane, r2s, x1A, x1B);
-        } else {
-            post_dst<M>(xs, zA, zB, lane, r2s);
-        }
-        __syncwarp();
-        // ---- coalesced column stores with the mode's boundary rows
-        for (int iz = lane; iz <= n; iz += 32) {
-            float ra, rb;
-            if (MODE == COL_DCT) {
-                ra = zA[zpad(iz)];
-                rb = zB[zpad(iz)];
-            } else if (iz == 0) {
-                ra = (MODE == COL_DST) ? ld(in, oA) : fA0;
-                rb = (MODE == COL_DST) ? ld(in, oB) : fB0;
-            } else if (iz == n) {
-                ra = (MODE == COL_DST) ? 0.f : fAn;
-                rb = (MODE == COL_DST) ? 0.f : fBn;
-            } else {
-                ra = zA[zpad(iz)];
-                rb = zB[zpad(iz)];
-                if (MODE == COL_COMBINE) {
+                if (MODE == COL_DECOMP && j > 0) {
                     float pm, pp;
-                    hA.at(iz, n, pm, pp);
-                    ra += fA0 * pm + fAn * pp;
-                    hB.at(iz, n, pm, pp);
-                    rb += fB0 * pm + fBn * pp;
+                    hA.at(j, n, pm, pp);
+                    xa -= f0A * pm + fnA * pp;
+                    ya -= f0A * pp + fnA * pm;
+                    hB.at(j, n, pm, pp);
+                    xb -= f0B * pm + fnB * pp;
+                    yb -= f0B * pp + fnB * pm;
+                }
+                const float sj = __ldg(&sinz[j]);
+                if (MODE == COL_DCT) {
+                    if (j == 0) {
+                        v[m] = make_float2(0.5f * (f0A + fnA), 0.5f * (f0B + fnB));
+                    } else {
+                        const float cj = __ldg(&cosz[j]);
+                        dsumA += xa * cj;
+                        dsumB += xb * cj;
+                        v[m] = pre_cosine(xa, ya, xb, yb, sj);
+                    }
+                } else {
+                    v[m] = (j == 0) ? make_float2(0.f, 0.f) : pre_sine(xa, ya, xb, yb, sj);
                 }
             }
-            out[oA + iz] = ra;
-            out[oB + iz] = rb;
+            warp_fft<M>(v, xs, twn, lane);
+        }
+        // ---- split the packed spectra, store levels 2k, 2k+1 as float2
+        float *colA = out + oA, *colB = out + oB;
+        const float f0A = lane_get(par, 0), fnA = lane_get(par, 1), f0B = lane_get(par, 8),
+                    fnB = lane_get(par, 9);
+        if (MODE == COL_DCT) {
+            const float x1A = r2s * (0.5f * f0A + warp_sum(dsumA) - 0.5f * fnA);
+            const float x1B = r2s * (0.5f * f0B + warp_sum(dsumB) - 0.5f * fnB);
+            post<M, true>(xs, lane, r2s, x1A, x1B, [&](int k, float eA, float oA_, float eB, float oB_) {
+                st2(colA, k, eA, oA_);
+                st2(colB, k, eB, oB_);
+            });
+            if (lane == 0) {
+                const float2 cm = xs[nsw<M>(n / 2)];
+                colA[n] = r2s * cm.x;
+                colB[n] = r2s * cm.y;
+            }
+        } else if (MODE == COL_COMBINE) {
+            const Harm hA = Harm::make(lane_get(par, 2), dz, Lz, n, cA == 0);
+            const Harm hB = Harm::make(lane_get(par, 10), dz, Lz, n, cB == 0);
+            post<M, false>(xs, lane, r2s, 0.f, 0.f, [&](int k, float eA, float oA_, float eB, float oB_) {
+                float pm0, pp0, pm1, pp1;
+                hA.at2(2 * k, n, pm0, pp0, pm1, pp1);
+                eA = (k == 0) ? f0A : eA + f0A * pm0 + fnA * pp0;
+                oA_ += f0A * pm1 + fnA * pp1;
+                hB.at2(2 * k, n, pm0, pp0, pm1, pp1);
+                eB = (k == 0) ? f0B : eB + f0B * pm0 + fnB * pp0;
+                oB_ += f0B * pm1 + fnB * pp1;
+                st2(colA, k, eA, oA_);
+                st2(colB, k, eB, oB_);
+            });
+            if (lane == 0) {
+                colA[n] = fnA;
+                colB[n] = fnB;
+            }
+        } else {
+            // DST keeps the input's level 0 and zeroes level nz; DECOMP
+            // keeps both boundary values
+            const float bA = f0A, bB = f0B;
+            post<M, false>(xs, lane, r2s, 0.f, 0.f, [&](int k, float eA, float oA_, float eB, float oB_) {
+                st2(colA, k, (k == 0) ? bA : eA, oA_);
+                st2(colB, k, (k == 0) ? bB : eB, oB_);
+            });
+            if (lane == 0) {
+                colA[n] = (MODE == COL_DST) ? 0.f : fnA;
+                colB[n] = (MODE == COL_DST) ? 0.f : fnB;
+            }
         }
         __syncwarp();
     }
 }
 
-// Per-column scalars of a column pair spread over the warp (lane i holds
-// scalar i): they stay out of the registers while the warp FFT runs and are
-// fetched with one shuffle each where needed.
-__device__ __forceinline__ float lane_get(float par, int i) { return __shfl_sync(0xffffffffu, par, i); }
+namespace {
+// Boundary-driven part of the vertical-velocity inversion for one column
+// (inversion.f90:94-139 with the theta functions of inversion_utils.f90:
+// 484-542).  With Lp = kl zp, Lm = kl zm, ep = exp(-Lp), em = exp(-Lm),
+//   ds(0) thetam + ds(nz) thetap   (w) and
+//   ds(0) dthetam + ds(nz) dthetap (dw/dz)
+// are both em (c_mm Lm + c_mp Lp + c_mc) + ep (c_pm Lm + c_pp Lp + c_pc):
+// expanding thetam, thetap (and their z derivatives) in phim, phip leaves
+// terms linear in Lm and Lp times the two exponentials.  Lp and Lm are taken
+// as kl dz times the exact level counts iz and nz - iz.
+struct ThetaCol {
+    float a, g, kdz;
+    float c_mm, c_mp, c_mc, c_pm, c_pp, c_pc;
+    bool zero;  // (0,0) column: no boundary-driven part
+    __device__ static ThetaCol make(bool dwdz, float kl, float k2i, float d0, float dn, float dz, float Lz,
+                                    bool zero)
+    {
+        const float l2e = 1.4426950408889634f;
+        ThetaCol t;
+        t.zero = zero;
+        t.a = -kl * dz * l2e;
+        t.g = ex2(t.a);
+        t.kdz = kl * dz;
+        const float ef = ex2(-kl * Lz * l2e);
+        const float div = 1.0f / (1.0f - ef * ef);
+        const float Q = div * (1.0f + ef * ef), R = div * 2.0f * ef;
+        const float A = d0 * R - dn * Q, B = d0 * Q - dn * R;
+        if (!dwdz) {
+            const float s = 0.5f * k2i * div;
+            t.c_mm = s * A;
+            t.c_mp = s * ef * B;
+            t.c_mc = 0.f;
+            t.c_pm = -s * ef * A;
+            t.c_pp = -s * B;
+            t.c_pc = 0.f;
+        } else {
+            const float s = 0.5f * k2i * kl * div;
+            t.c_mm = s * A;
+            t.c_mp = s * ef * B;
+            t.c_mc = s * (dn - d0 * ef);
+            t.c_pm = s * ef * A;
+            t.c_pp = s * B;
+            t.c_pc = s * (dn * ef - d0);
+        }
+        return t;
+    }
+    // values at levels z0 and z0 + 1
+    __device__ void at2(int z0, int n, float &v0, float &v1) const
+    {
+        if (zero) {
+            v0 = v1 = 0.f;
+            return;
+        }
+        const float ep0 = ex2(a * (float)z0), em1 = ex2(a * (float)(n - z0 - 1));
+        const float ep1 = ep0 * g, em0 = em1 * g;
+        const float Lp0 = kdz * (float)z0, Lp1 = kdz * (float)(z0 + 1);
+        const float Lm0 = kdz * (float)(n - z0), Lm1 = kdz * (float)(n - z0 - 1);
+        v0 = em0 * (c_mm * Lm0 + c_mp * Lp0 + c_mc) + ep0 * (c_pm * Lm0 + c_pp * Lp0 + c_pc);
+        v1 = em1 * (c_mm * Lm1 + c_mp * Lp1 + c_mc) + ep1 * (c_pm * Lm1 + c_pp * Lp1 + c_pc);
+    }
+};
+}  // namespace
 
 // ------------------------------------------------------------------------
 // Vertical velocity of vor2vel in one kernel (inversion.f90:94-139):
 //   bs = ds(0) thetam + ds(nz) thetap,  es = ds(0) dthetam + ds(nz) dthetap,
 //   dsg = green ds (interior), as = rkz dsg,
 //   w = [0, dst(dsg) + bs, 0],  dw/dz = es + dct(as),
-// with green(kz) = -1/(k^2 + l^2 + rkz^2) and the theta functions evaluated
-// in registers: one read of ds (the second transform re-reads it from L2),
-// one write each of w and dw/dz.
+// with green(kz) = -1/(k^2 + l^2 + rkz^2) and the boundary-driven parts
+// evaluated in registers: one read of ds (the second transform re-reads it
+// from L2), one write each of w and dw/dz.
 template <int M>
 __global__ void __launch_bounds__(256, 2) k_colz_w(const float *__restrict__ ds, float *__restrict__ w,
                                                    float *__restrict__ es, int P, long long npairs,
@@ -395,11 +472,7 @@ __global__ void __launch_bounds__(256, 2) k_colz_w(const float *__restrict__ ds,
     constexpr int n = 32 * M;
     const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
     extern __shared__ __align__(16) unsigned char smz[];
-    constexpr int XS = (32 * (M + 1) > n ? 32 * (M + 1) : n);
-    constexpr int ZS = n + 1 + (n + 1) / 16 + 2;
-    float2 *xs = reinterpret_cast<float2 *>(smz) + (size_t)wib * (XS + ZS);
-    float *zA = reinterpret_cast<float *>(xs + XS);
-    float *zB = zA + ZS;
+    float2 *xs = reinterpret_cast<float2 *>(smz) + (size_t)wib * n;
     const float r2s = 1.41421356237309505f * rsqrtf((float)n);
     const float pk = 3.14159265358979324f / Lz;  // rkz(kz) = pk kz
     const long long warps = (long long)gridDim.x * (blockDim.x >> 5);
@@ -427,40 +500,39 @@ __global__ void __launch_bounds__(256, 2) k_colz_w(const float *__restrict__ ds,
                     const float rj2 = rj * rj, rn2 = rn * rn;
                     const float xa = __fdividef(-ds[oA + j], k2A + rj2), ya = __fdividef(-ds[oA + n - j], k2A + rn2);
                     const float xb = __fdividef(-ds[oB + j], k2B + rj2), yb = __fdividef(-ds[oB + n - j], k2B + rn2);
-                    const float sj = __ldg(&sinz[j]);
-                    v[m] = make_float2(0.5f * (xa - ya) + sj * (xa + ya), 0.5f * (xb - yb) + sj * (xb + yb));
+                    v[m] = pre_sine(xa, ya, xb, yb, __ldg(&sinz[j]));
                 }
             }
             warp_fft<M>(v, xs, twn, lane);
         }
-        post_dst<M>(xs, zA, zB, lane, r2s);
-        __syncwarp();
         {
-            const float d0A = lane_get(par, 2), dnA = lane_get(par, 3), d0B = lane_get(par, 10),
-                        dnB = lane_get(par, 11);
-            const Theta tA = Theta::make(sqrtf(lane_get(par, 0)), lane_get(par, 1), dz, Lz, n, cA == 0);
-            const Theta tB = Theta::make(sqrtf(lane_get(par, 8)), lane_get(par, 9), dz, Lz, n, cB == 0);
-            for (int iz = lane; iz <= n; iz += 32) {
-                float ra = 0.f, rb = 0.f;
-                if (iz > 0 && iz < n) {
-                    float tm, tp, dtm, dtp;
-                    tA.at(iz, tm, tp, dtm, dtp);
-                    ra = zA[zpad(iz)] + d0A * tm + dnA * tp;
-                    tB.at(iz, tm, tp, dtm, dtp);
-                    rb = zB[zpad(iz)] + d0B * tm + dnB * tp;
-                }
-                w[oA + iz] = ra;
-                w[oB + iz] = rb;
+            const float klA = sqrtf(lane_get(par, 0)), klB = sqrtf(lane_get(par, 8));
+            const ThetaCol tA =
+                ThetaCol::make(false, klA, lane_get(par, 1), lane_get(par, 2), lane_get(par, 3), dz, Lz, cA == 0);
+            const ThetaCol tB =
+                ThetaCol::make(false, klB, lane_get(par, 9), lane_get(par, 10), lane_get(par, 11), dz, Lz, cB == 0);
+            float *wA = w + oA, *wB = w + oB;
+            post<M, false>(xs, lane, r2s, 0.f, 0.f, [&](int k, float eA, float oA_, float eB, float oB_) {
+                float b0, b1;
+                tA.at2(2 * k, n, b0, b1);
+                st2(wA, k, (k == 0) ? 0.f : eA + b0, oA_ + b1);
+                tB.at2(2 * k, n, b0, b1);
+                st2(wB, k, (k == 0) ? 0.f : eB + b0, oB_ + b1);
+            });
+            if (lane == 0) {
+                wA[n] = 0.f;
+                wB[n] = 0.f;
             }
         }
         __syncwarp();
         // ---- dct of as = rkz green ds (as(0) = as(nz) = 0)
+        float x1A, x1B;
         {
             const float k2A = lane_get(par, 0), k2B = lane_get(par, 8);
             // opaque copies of the offsets keep the compiler from hoisting
             // this phase's loads above the first transform (register spills)
-            long long oA = cA * P, oB = cB * P;
-            asm volatile("" : "+l"(oA), "+l"(oB));
+            long long qA = oA, qB = oB;
+            asm volatile("" : "+l"(qA), "+l"(qB));
             float2 v[M];
             float sA = 0.f, sB = 0.f;
 #pragma unroll
@@ -470,45 +542,57 @@ __global__ void __launch_bounds__(256, 2) k_colz_w(const float *__restrict__ ds,
                 if (j > 0) {
                     const float rj = pk * (float)j, rn = pk * (float)(n - j);
                     const float rj2 = rj * rj, rn2 = rn * rn;
-                    const float xa = __fdividef(-rj * ds[oA + j], k2A + rj2);
-                    const float ya = __fdividef(-rn * ds[oA + n - j], k2A + rn2);
-                    const float xb = __fdividef(-rj * ds[oB + j], k2B + rj2);
-                    const float yb = __fdividef(-rn * ds[oB + n - j], k2B + rn2);
-                    const float sj = __ldg(&sinz[j]), cj = __ldg(&cosz[j]);
+                    const float xa = __fdividef(-rj * ds[qA + j], k2A + rj2);
+                    const float ya = __fdividef(-rn * ds[qA + n - j], k2A + rn2);
+                    const float xb = __fdividef(-rj * ds[qB + j], k2B + rj2);
+                    const float yb = __fdividef(-rn * ds[qB + n - j], k2B + rn2);
+                    const float cj = __ldg(&cosz[j]);
                     sA += xa * cj;
                     sB += xb * cj;
-                    v[m] = make_float2(0.5f * (xa + ya) - sj * (xa - ya), 0.5f * (xb + yb) - sj * (xb - yb));
+                    v[m] = pre_cosine(xa, ya, xb, yb, __ldg(&sinz[j]));
                 }
             }
-            const float x1A = r2s * warp_sum(sA), x1B = r2s * warp_sum(sB);
+            x1A = r2s * warp_sum(sA);
+            x1B = r2s * warp_sum(sB);
             warp_fft<M>(v, xs, twn, lane);
-            post_dct<M>(xs, zA, zB, lane, r2s, x1A, x1B);
         }
-        __syncwarp();
         {
-            const float d0A = lane_get(par, 2), dnA = lane_get(par, 3), d0B = lane_get(par, 10),
-                        dnB = lane_get(par, 11);
-            const Theta tA = Theta::make(sqrtf(lane_get(par, 0)), lane_get(par, 1), dz, Lz, n, cA == 0);
-            const Theta tB = Theta::make(sqrtf(lane_get(par, 8)), lane_get(par, 9), dz, Lz, n, cB == 0);
-            for (int iz = lane; iz <= n; iz += 32) {
-                float tm, tp, dtm, dtp;
-                tA.at(iz, tm, tp, dtm, dtp);
-                const float ra = zA[zpad(iz)] + d0A * dtm + dnA * dtp;
-                tB.at(iz, tm, tp, dtm, dtp);
-                const float rb = zB[zpad(iz)] + d0B * dtm + dnB * dtp;
-                es[oA + iz] = ra;
-                es[oB + iz] = rb;
+            const float klA = sqrtf(lane_get(par, 0)), klB = sqrtf(lane_get(par, 8));
+            const ThetaCol tA =
+                ThetaCol::make(true, klA, lane_get(par, 1), lane_get(par, 2), lane_get(par, 3), dz, Lz, cA == 0);
+            const ThetaCol tB =
+                ThetaCol::make(true, klB, lane_get(par, 9), lane_get(par, 10), lane_get(par, 11), dz, Lz, cB == 0);
+            float *eA_ = es + oA, *eB_ = es + oB;
+            post<M, true>(xs, lane, r2s, x1A, x1B, [&](int k, float eA, float oA_, float eB, float oB_) {
+                float b0, b1;
+                tA.at2(2 * k, n, b0, b1);
+                st2(eA_, k, eA + b0, oA_ + b1);
+                tB.at2(2 * k, n, b0, b1);
+                st2(eB_, k, eB + b0, oB_ + b1);
+            });
+            if (lane == 0) {
+                const float2 cm = xs[nsw<M>(n / 2)];
+                float b0, b1;
+                tA.at2(n - 1, n, b0, b1);
+                eA_[n] = r2s * cm.x + b1;
+                tB.at2(n - 1, n, b0, b1);
+                eB_[n] = r2s * cm.y + b1;
             }
         }
         __syncwarp();
     }
 }
 
+namespace {
+__device__ __forceinline__ int zpad(int z) { return z + (z >> 4); }
+template <int M> constexpr int zbuf_floats() { return 32 * M + 1 + (32 * M + 1) / 16 + 2; }
+}  // namespace
+
 // ------------------------------------------------------------------------
 // es = decompose(central_diffz(combine(f))) in one kernel (the z part of
 // the solenoidal projection, inversion.f90:41-47): combine through the
-// warp FFT, the two-sided difference on the warp's z buffer, then the
-// decomposition; one read of f and one write of es.
+// warp FFT into the warp's z buffers, the two-sided difference into the FFT
+// buffer, then the decomposition; one read of f and one write of es.
 template <int M>
 __global__ void __launch_bounds__(256, 2) k_colz_proj(const float *__restrict__ f, float *__restrict__ es, int P,
                                                       long long npairs, const double *__restrict__ k2l2, float dz,
@@ -516,27 +600,26 @@ __global__ void __launch_bounds__(256, 2) k_colz_proj(const float *__restrict__ 
                                                       const float *__restrict__ sinz)
 {
     constexpr int n = 32 * M;
+    constexpr int ZS = zbuf_floats<M>();
     const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
     extern __shared__ __align__(16) unsigned char smz[];
-    constexpr int XS = (32 * (M + 1) > n ? 32 * (M + 1) : n);
-    constexpr int ZS = n + 1 + (n + 1) / 16 + 2;
-    float2 *xs = reinterpret_cast<float2 *>(smz) + (size_t)wib * (XS + ZS);
-    float *zA = reinterpret_cast<float *>(xs + XS);
+    float2 *xs = reinterpret_cast<float2 *>(smz + (size_t)wib * (n * sizeof(float2) + 2 * ZS * sizeof(float)));
+    float *zA = reinterpret_cast<float *>(xs + n);
     float *zB = zA + ZS;
-    // the derivative columns reuse the FFT buffer: 2 (n + 1) <= 2 XS floats
-    float *gA = reinterpret_cast<float *>(xs), *gB = gA + (n + 1);
+    // derivative levels 0..n-1 reuse the FFT buffer; level n stays in registers
+    float *gA = reinterpret_cast<float *>(xs), *gB = gA + n;
     const float r2s = 1.41421356237309505f * rsqrtf((float)n);
     const float dzi = 1.0f / dz, hdzi = 0.5f / dz;
     const long long warps = (long long)gridDim.x * (blockDim.x >> 5);
     for (long long pr = (long long)blockIdx.x * (blockDim.x >> 5) + wib; pr < npairs; pr += warps) {
         const long long cA = 2 * pr, cB = cA + 1;
         const long long oA = cA * P, oB = cB * P;
-        // lanes 0..2 (column A) and 8..10 (column B): k^2+l^2, f(0), f(nz)
+        // lanes 0..2 (column A) and 8..10 (column B): f(0), f(nz), kl
         float par = 0.f;
         if (lane < 16 && (lane & 7) < 3) {
             const long long c = lane < 8 ? cA : cB;
             const int q = lane & 7;
-            par = q == 0 ? (float)k2l2[c] : f[c * P + (q == 1 ? 0 : n)];
+            par = q == 2 ? sqrtf((float)k2l2[c]) : f[c * P + (q == 0 ? 0 : n)];
         }
         // ---- combine: dst of the interior, plus the harmonic part
         {
@@ -545,54 +628,46 @@ __global__ void __launch_bounds__(256, 2) k_colz_proj(const float *__restrict__ 
             for (int m = 0; m < M; ++m) {
                 const int j = lane + 32 * m;
                 v[m] = make_float2(0.f, 0.f);
-                if (j > 0) {
-                    const float xa = f[oA + j], ya = f[oA + n - j], xb = f[oB + j], yb = f[oB + n - j];
-                    const float sj = __ldg(&sinz[j]);
-                    v[m] = make_float2(0.5f * (xa - ya) + sj * (xa + ya), 0.5f * (xb - yb) + sj * (xb + yb));
-                }
+                if (j > 0) v[m] = pre_sine(f[oA + j], f[oA + n - j], f[oB + j], f[oB + n - j], __ldg(&sinz[j]));
             }
             warp_fft<M>(v, xs, twn, lane);
         }
-        post_dst<M>(xs, zA, zB, lane, r2s);
-        __syncwarp();
         {
-            const float f0A = lane_get(par, 1), fnA = lane_get(par, 2), f0B = lane_get(par, 9),
-                        fnB = lane_get(par, 10);
-            const Harm hA = Harm::make(sqrtf(lane_get(par, 0)), dz, Lz, n, cA == 0);
-            const Harm hB = Harm::make(sqrtf(lane_get(par, 8)), dz, Lz, n, cB == 0);
-            for (int iz = lane; iz <= n; iz += 32) {
-                float ca, cb;
-                if (iz == 0) {
-                    ca = f0A;
-                    cb = f0B;
-                } else if (iz == n) {
-                    ca = fnA;
-                    cb = fnB;
-                } else {
-                    float pm, pp;
-                    hA.at(iz, n, pm, pp);
-                    ca = zA[zpad(iz)] + f0A * pm + fnA * pp;
-                    hB.at(iz, n, pm, pp);
-                    cb = zB[zpad(iz)] + f0B * pm + fnB * pp;
-                }
-                zA[zpad(iz)] = ca;
-                zB[zpad(iz)] = cb;
+            const float f0A = lane_get(par, 0), fnA = lane_get(par, 1), f0B = lane_get(par, 8),
+                        fnB = lane_get(par, 9);
+            const Harm hA = Harm::make(lane_get(par, 2), dz, Lz, n, cA == 0);
+            const Harm hB = Harm::make(lane_get(par, 10), dz, Lz, n, cB == 0);
+            post<M, false>(xs, lane, r2s, 0.f, 0.f, [&](int k, float eA, float oA_, float eB, float oB_) {
+                float pm0, pp0, pm1, pp1;
+                hA.at2(2 * k, n, pm0, pp0, pm1, pp1);
+                zA[zpad(2 * k)] = (k == 0) ? f0A : eA + f0A * pm0 + fnA * pp0;
+                zA[zpad(2 * k + 1)] = oA_ + f0A * pm1 + fnA * pp1;
+                hB.at2(2 * k, n, pm0, pp0, pm1, pp1);
+                zB[zpad(2 * k)] = (k == 0) ? f0B : eB + f0B * pm0 + fnB * pp0;
+                zB[zpad(2 * k + 1)] = oB_ + f0B * pm1 + fnB * pp1;
+            });
+            if (lane == 0) {
+                zA[zpad(n)] = fnA;
+                zB[zpad(n)] = fnB;
             }
         }
         __syncwarp();
-        // ---- central_diffz (inversion_utils.f90:653-673) into gA / gB
-        for (int iz = lane; iz <= n; iz += 32) {
-            const int lo = iz == 0 ? 0 : iz - 1, hi = iz == n ? n : iz + 1;
-            const float sc = (iz == 0 || iz == n) ? dzi : hdzi;
-            gA[iz] = (zA[zpad(hi)] - zA[zpad(lo)]) * sc;
-            gB[iz] = (zB[zpad(hi)] - zB[zpad(lo)]) * sc;
+        // ---- central_diffz (inversion_utils.f90:653-673): levels 0..n-1
+        // into gA / gB, level n in registers
+        for (int iz = lane; iz < n; iz += 32) {
+            const int lo = iz == 0 ? 0 : iz - 1;
+            const float sc = iz == 0 ? dzi : hdzi;
+            gA[iz] = (zA[zpad(iz + 1)] - zA[zpad(lo)]) * sc;
+            gB[iz] = (zB[zpad(iz + 1)] - zB[zpad(lo)]) * sc;
         }
+        const float gnA = dzi * (zA[zpad(n)] - zA[zpad(n - 1)]);
+        const float gnB = dzi * (zB[zpad(n)] - zB[zpad(n - 1)]);
         __syncwarp();
         // ---- decompose: subtract the harmonic part, dst
+        const float g0A = gA[0], g0B = gB[0];
         {
-            const float g0A = gA[0], gnA = gA[n], g0B = gB[0], gnB = gB[n];
-            const Harm hA = Harm::make(sqrtf(lane_get(par, 0)), dz, Lz, n, cA == 0);
-            const Harm hB = Harm::make(sqrtf(lane_get(par, 8)), dz, Lz, n, cB == 0);
+            const Harm hA = Harm::make(lane_get(par, 2), dz, Lz, n, cA == 0);
+            const Harm hB = Harm::make(lane_get(par, 10), dz, Lz, n, cB == 0);
             float2 v[M];
 #pragma unroll
             for (int m = 0; m < M; ++m) {
@@ -607,37 +682,38 @@ __global__ void __launch_bounds__(256, 2) k_colz_proj(const float *__restrict__ 
                     hB.at(j, n, pm, pp);
                     xb -= g0B * pm + gnB * pp;
                     yb -= g0B * pp + gnB * pm;
-                    const float sj = __ldg(&sinz[j]);
-                    v[m] = make_float2(0.5f * (xa - ya) + sj * (xa + ya), 0.5f * (xb - yb) + sj * (xb + yb));
+                    v[m] = pre_sine(xa, ya, xb, yb, __ldg(&sinz[j]));
                 }
-            }
-            // the boundary rows pass through unchanged
-            if (lane == 0) {
-                zA[zpad(0)] = g0A;
-                zB[zpad(0)] = g0B;
-                zA[zpad(n)] = gnA;
-                zB[zpad(n)] = gnB;
             }
             __syncwarp();
             warp_fft<M>(v, xs, twn, lane);
         }
-        post_dst<M>(xs, zA, zB, lane, r2s);
-        __syncwarp();
-        for (int iz = lane; iz <= n; iz += 32) {
-            es[oA + iz] = zA[zpad(iz)];
-            es[oB + iz] = zB[zpad(iz)];
+        {
+            float *eA_ = es + oA, *eB_ = es + oB;
+            post<M, false>(xs, lane, r2s, 0.f, 0.f, [&](int k, float eA, float oA_, float eB, float oB_) {
+                st2(eA_, k, (k == 0) ? g0A : eA, oA_);
+                st2(eB_, k, (k == 0) ? g0B : eB, oB_);
+            });
+            if (lane == 0) {
+                eA_[n] = gnA;
+                eB_[n] = gnB;
+            }
         }
         __syncwarp();
     }
 }
 
 namespace {
-template <int M> constexpr size_t colz_smem_per_warp()
+template <int M> constexpr size_t colz_smem_per_warp() { return 32 * M * sizeof(float2); }
+template <int M> constexpr size_t proj_smem_per_warp()
 {
-    constexpr int n = 32 * M;
-    constexpr int XS = (32 * (M + 1) > n ? 32 * (M + 1) : n);
-    constexpr int ZS = n + 1 + (n + 1) / 16 + 2;
-    return XS * sizeof(float2) + 2 * ZS * sizeof(float);
+    return 32 * M * sizeof(float2) + 2 * zbuf_floats<M>() * sizeof(float);
+}
+
+long long colz_blocks(long long npairs)
+{
+    long long nb = (npairs + 7) / 8;
+    return nb > 152 * 24 ? 152 * 24 : nb;
 }
 
 template <int MODE, int M, typename TIN>
@@ -645,10 +721,8 @@ void launch_colz_m(const TIN *in, float *out, const Dims &d, cudaStream_t st, co
                    const float2 *twn, const float *sinz, const float *cosz)
 {
     const long long npairs = d.ncol / 2;
-    const size_t sm = 8 * colz_smem_per_warp<M>();
-    long long nb = (npairs + 7) / 8;
-    if (nb > 152 * 24) nb = 152 * 24;
-    k_colz<MODE, M, TIN><<<(unsigned)nb, 256, sm, st>>>(in, out, d.P, npairs, k2l2, dz, Lz, twn, sinz, cosz);
+    k_colz<MODE, M, TIN><<<(unsigned)colz_blocks(npairs), 256, 8 * colz_smem_per_warp<M>(), st>>>(
+        in, out, d.P, npairs, k2l2, dz, Lz, twn, sinz, cosz);
 }
 
 template <int MODE, typename TIN>
@@ -664,48 +738,42 @@ void launch_colz(const TIN *in, float *out, const Dims &d, cudaStream_t st, cons
     }
 }
 
-template <int MODE, int M, typename TIN> void attr_m()
+template <int M>
+void launch_w_m(const Dims &d, cudaStream_t st, const float *ds, float *w, float *es, const double *k2l2,
+                const double *k2l2i, float dz, float Lz, const float2 *twn, const float *sinz, const float *cosz)
 {
-    cudaFuncSetAttribute(k_colz<MODE, M, TIN>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         (int)(8 * colz_smem_per_warp<M>()));
+    const long long npairs = d.ncol / 2;
+    k_colz_w<M><<<(unsigned)colz_blocks(npairs), 256, 8 * colz_smem_per_warp<M>(), st>>>(
+        ds, w, es, d.P, npairs, k2l2, k2l2i, dz, Lz, twn, sinz, cosz);
 }
-template <int MODE, typename TIN> void attr_mode()
-{
-    attr_m<MODE, 2, TIN>();
-    attr_m<MODE, 4, TIN>();
-    attr_m<MODE, 8, TIN>();
-    attr_m<MODE, 16, TIN>();
-    attr_m<MODE, 32, TIN>();
-}
-template <typename TIN> void attr_all()
-{
-    attr_mode<COL_DST, TIN>();
-    attr_mode<COL_DCT, TIN>();
-    attr_mode<COL_DECOMP, TIN>();
-    attr_mode<COL_COMBINE, TIN>();
-}
-}  // namespace
 
 template <int M>
-static void launch_w_m(const Dims &d, cudaStream_t st, const float *ds, float *w, float *es, const double *k2l2,
-                       const double *k2l2i, float dz, float Lz, const float2 *twn, const float *sinz, const float *cosz)
+void launch_proj_m(const Dims &d, cudaStream_t st, const float *f, float *es, const double *k2l2, float dz, float Lz,
+                   const float2 *twn, const float *sinz)
 {
     const long long npairs = d.ncol / 2;
-    long long nb = (npairs + 7) / 8;
-    if (nb > 152 * 24) nb = 152 * 24;
-    k_colz_w<M><<<(unsigned)nb, 256, 8 * colz_smem_per_warp<M>(), st>>>(ds, w, es, d.P, npairs, k2l2, k2l2i, dz, Lz,
-                                                                         twn, sinz, cosz);
+    k_colz_proj<M><<<(unsigned)colz_blocks(npairs), 256, 8 * proj_smem_per_warp<M>(), st>>>(f, es, d.P, npairs,
+                                                                                            k2l2, dz, Lz, twn, sinz);
 }
-template <int M>
-static void launch_proj_m(const Dims &d, cudaStream_t st, const float *f, float *es, const double *k2l2, float dz,
-                          float Lz, const float2 *twn, const float *sinz)
+
+template <typename K> void smem_attr(K kern, size_t bytes)
 {
-    const long long npairs = d.ncol / 2;
-    long long nb = (npairs + 7) / 8;
-    if (nb > 152 * 24) nb = 152 * 24;
-    k_colz_proj<M><<<(unsigned)nb, 256, 8 * colz_smem_per_warp<M>(), st>>>(f, es, d.P, npairs, k2l2, dz, Lz, twn,
-                                                                            sinz);
+    if (bytes > 48 * 1024) cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
 }
+template <int M> void attr_m()
+{
+    smem_attr(k_colz<COL_DST, M, float>, 8 * colz_smem_per_warp<M>());
+    smem_attr(k_colz<COL_DCT, M, float>, 8 * colz_smem_per_warp<M>());
+    smem_attr(k_colz<COL_DECOMP, M, float>, 8 * colz_smem_per_warp<M>());
+    smem_attr(k_colz<COL_COMBINE, M, float>, 8 * colz_smem_per_warp<M>());
+    smem_attr(k_colz<COL_DST, M, double>, 8 * colz_smem_per_warp<M>());
+    smem_attr(k_colz<COL_DCT, M, double>, 8 * colz_smem_per_warp<M>());
+    smem_attr(k_colz<COL_DECOMP, M, double>, 8 * colz_smem_per_warp<M>());
+    smem_attr(k_colz<COL_COMBINE, M, double>, 8 * colz_smem_per_warp<M>());
+    smem_attr(k_colz_w<M>, 8 * colz_smem_per_warp<M>());
+    smem_attr(k_colz_proj<M>, 8 * proj_smem_per_warp<M>());
+}
+}  // namespace
 
 void columns_w(const Dims &d, cudaStream_t st, const float *ds, float *w, float *es, const double *k2l2,
                const double *k2l2i, float dz, float Lz, const float2 *twn, const float *sinz, const float *cosz,
@@ -752,14 +820,11 @@ void colz_init()
         w[j] = make_float2((float)c, (float)(-sn));
     }
     cudaMemcpyToSymbol(c_w32z, w, sizeof(w));
-    attr_all<float>();
-    attr_all<double>();
-    cudaFuncSetAttribute(k_colz_w<16>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)(8 * colz_smem_per_warp<16>()));
-    cudaFuncSetAttribute(k_colz_w<32>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)(8 * colz_smem_per_warp<32>()));
-    cudaFuncSetAttribute(k_colz_proj<16>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         (int)(8 * colz_smem_per_warp<16>()));
-    cudaFuncSetAttribute(k_colz_proj<32>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         (int)(8 * colz_smem_per_warp<32>()));
+    attr_m<2>();
+    attr_m<4>();
+    attr_m<8>();
+    attr_m<16>();
+    attr_m<32>();
 }
 
 template <typename TIN>

@@ -31,11 +31,8 @@ __device__ __forceinline__ float2 cm(float2 a, float2 b)
 template <int R, bool INV> __device__ __forceinline__ void dftR(float2 *v) { dft<R, INV, float2>(v); }
 
 // one radix-R Stockham pass with span NS over N points: inputs x[j + r N/R]
-// of butterfly j, outputs at (j - k) R + k + r NS, k = j mod NS.  HERM
-// (first pass of an inverse transform): the inputs C_k = A_k + i B_k of the
-// two packed lines are rebuilt from the Hermitian rows k and N - k as they
-// are loaded.
-template <int N, int R, int NS, bool INV, bool FROM_GLOBAL, bool TO_GLOBAL, bool HERM = false>
+// of butterfly j, outputs at (j - k) R + k + r NS, k = j mod NS
+template <int N, int R, int NS, bool INV, bool FROM_GLOBAL, bool TO_GLOBAL>
 __device__ __forceinline__ void pass(float2 *sm, const float2 *__restrict__ gin, float2 *__restrict__ gout,
                                      long long gstride, bool valid, float scale, const float2 *__restrict__ tw)
 {
@@ -51,17 +48,7 @@ __device__ __forceinline__ void pass(float2 *sm, const float2 *__restrict__ gin,
 #pragma unroll
             for (int r = 0; r < R; ++r) {
                 const int row = j + r * NB;
-                if (FROM_GLOBAL && HERM) {
-                    const int mrow = (N - row) & (N - 1);
-                    const int klo = row < mrow ? row : mrow, khi = row < mrow ? mrow : row;
-                    float2 lo = make_float2(0.f, 0.f), hi = make_float2(0.f, 0.f);
-                    if (valid) {
-                        lo = gin[klo * gstride];
-                        if (khi != klo) hi = gin[khi * gstride];
-                    }
-                    v[q][r] = row <= N / 2 ? make_float2(lo.x - hi.y, hi.x + lo.y)
-                                           : make_float2(lo.x + hi.y, lo.y - hi.x);
-                } else if (FROM_GLOBAL) {
+                if (FROM_GLOBAL) {
                     v[q][r] = valid ? gin[row * gstride] : make_float2(0.f, 0.f);
                 } else {
                     v[q][r] = sm[row * LANES + p];
@@ -98,30 +85,105 @@ __device__ __forceinline__ void pass(float2 *sm, const float2 *__restrict__ gin,
     __syncthreads();
 }
 
-// the complete pass sequence for N = 8^a * {1, 2, 4}; an inverse
-// transform reads Hermitian rows (HERM first pass)
+
+// C_k = A_k + i B_k of the two packed lines from the Hermitian rows
+// lo = H[min(k, N-k)] and hi = H[max(k, N-k)] (stafft.f90:55-58 storage)
+__device__ __forceinline__ float2 herm_low(float2 lo, float2 hi) { return make_float2(lo.x - hi.y, hi.x + lo.y); }
+__device__ __forceinline__ float2 herm_high(float2 lo, float2 hi) { return make_float2(lo.x + hi.y, lo.y - hi.x); }
+
+// First radix-8 pass (span 1) of an inverse transform straight from the
+// Hermitian rows in HBM.  Butterfly j reads rows j + r N/8, whose mirrors
+// N - row are the rows of butterfly N/8 - j: a thread owns such a pair of
+// butterflies (slot s: s and N/8 - s; slot 0: butterflies 0 and N/16, each
+// its own mirror), so every row is loaded once and used for both C_k and
+// C_{N-k}.
+template <int N>
+__device__ __forceinline__ void herm_first_pass(float2 *sm, const float2 *__restrict__ gin, long long gs,
+                                                bool valid)
+{
+    constexpr int G = LinePlan<N>::G, NB = N / 8, SLOTS = NB / 2;
+    constexpr int SPT = (SLOTS + G - 1) / G;
+    const int p = threadIdx.x & (LANES - 1), g = threadIdx.x / LANES;
+#pragma unroll
+    for (int q = 0; q < SPT; ++q) {
+        const int s = g + G * q;
+        if (!(SLOTS % G == 0 || s < SLOTS)) continue;
+        const int j1 = s == 0 ? 0 : s, j2 = s == 0 ? NB / 2 : NB - s;
+        float2 h1[8], h2[8];
+#pragma unroll
+        for (int r = 0; r < 8; ++r) {
+            h1[r] = valid ? gin[(j1 + r * NB) * gs] : make_float2(0.f, 0.f);
+            h2[r] = valid ? gin[(j2 + r * NB) * gs] : make_float2(0.f, 0.f);
+        }
+        float2 a[8], b[8];
+        if (s == 0) {
+            // butterfly 0: rows r N/8, mirror index 8 - r; rows 0 and N/2 are
+            // their own mirrors (imaginary rows absent)
+#pragma unroll
+            for (int r = 0; r < 8; ++r) {
+                const int rm = (8 - r) & 7;
+                a[r] = (r == 0 || r == 4) ? h1[r] : (r < 4 ? herm_low(h1[r], h1[rm]) : herm_high(h1[rm], h1[r]));
+            }
+            // butterfly N/16: mirror index 7 - r
+#pragma unroll
+            for (int r = 0; r < 8; ++r)
+                b[r] = r < 4 ? herm_low(h2[r], h2[7 - r]) : herm_high(h2[7 - r], h2[r]);
+        } else {
+            // row j1 + r N/8 mirrors row j2 + (7 - r) N/8; it is the lower
+            // row of the pair for r < 4
+#pragma unroll
+            for (int r = 0; r < 8; ++r) {
+                if (r < 4) {
+                    a[r] = herm_low(h1[r], h2[7 - r]);
+                    b[7 - r] = herm_high(h1[r], h2[7 - r]);
+                } else {
+                    a[r] = herm_high(h2[7 - r], h1[r]);
+                    b[7 - r] = herm_low(h2[7 - r], h1[r]);
+                }
+            }
+        }
+        dftR<8, true>(a);
+        dftR<8, true>(b);
+#pragma unroll
+        for (int r = 0; r < 8; ++r) {
+            sm[(j1 * 8 + r) * LANES + p] = a[r];
+            sm[(j2 * 8 + r) * LANES + p] = b[r];
+        }
+    }
+    __syncthreads();
+}
+
+template <int N, bool INV, bool FROM_GLOBAL>
+__device__ __forceinline__ void first_pass(float2 *sm, const float2 *gin, float2 *gout, long long gs, bool valid,
+                                           float scale, const float2 *tw)
+{
+    if constexpr (INV && FROM_GLOBAL) herm_first_pass<N>(sm, gin, gs, valid);
+    else pass<N, 8, 1, INV, FROM_GLOBAL, false>(sm, gin, gout, gs, valid, scale, tw);
+}
+
+// the complete pass sequence for N = 8^a * {1, 2, 4}; the first pass of an
+// inverse transform reads the Hermitian rows
 template <int N, bool INV, bool FROM_GLOBAL, bool TO_GLOBAL>
 __device__ __forceinline__ void fft_passes(float2 *sm, const float2 *gin, float2 *gout, long long gs, bool valid,
                                            float scale, const float2 *tw)
 {
-    constexpr bool H = INV && FROM_GLOBAL;
     if constexpr (N == 64) {
-        pass<N, 8, 1, INV, FROM_GLOBAL, false, H>(sm, gin, gout, gs, valid, scale, tw);
+        first_pass<N, INV, FROM_GLOBAL>(sm, gin, gout, gs, valid, scale, tw);
         pass<N, 8, 8, INV, false, TO_GLOBAL>(sm, gin, gout, gs, valid, scale, tw);
     } else if constexpr (N == 128) {
-        pass<N, 8, 1, INV, FROM_GLOBAL, false, H>(sm, gin, gout, gs, valid, scale, tw);
+        first_pass<N, INV, FROM_GLOBAL>(sm, gin, gout, gs, valid, scale, tw);
         pass<N, 8, 8, INV, false, false>(sm, gin, gout, gs, valid, scale, tw);
         pass<N, 2, 64, INV, false, TO_GLOBAL>(sm, gin, gout, gs, valid, scale, tw);
     } else if constexpr (N == 256) {
-        pass<N, 8, 1, INV, FROM_GLOBAL, false, H>(sm, gin, gout, gs, valid, scale, tw);
+        first_pass<N, INV, FROM_GLOBAL>(sm, gin, gout, gs, valid, scale, tw);
         pass<N, 8, 8, INV, false, false>(sm, gin, gout, gs, valid, scale, tw);
         pass<N, 4, 64, INV, false, TO_GLOBAL>(sm, gin, gout, gs, valid, scale, tw);
     } else if constexpr (N == 512) {
-        pass<N, 8, 1, INV, FROM_GLOBAL, false, H>(sm, gin, gout, gs, valid, scale, tw);
+        first_pass<N, INV, FROM_GLOBAL>(sm, gin, gout, gs, valid, scale, tw);
         pass<N, 8, 8, INV, false, false>(sm, gin, gout, gs, valid, scale, tw);
         pass<N, 8, 64, INV, false, TO_GLOBAL>(sm, gin, gout, gs, valid, scale, tw);
     } else {  // 1024
-        pass<N, 8, 1, INV, FROM_GLOBAL, false, H>(sm, gin, gout, gs, valid, scale, tw);
+        first_pass<N, INV, FROM_GLOBAL>(sm, gin, gout, gs, valid, scale, tw);
         pass<N, 8, 8, INV, false, false>(sm, gin, gout, gs, valid, scale, tw);
         pass<N, 8, 64, INV, false, false>(sm, gin, gout, gs, valid, scale, tw);
         pass<N, 2, 512, INV, false, TO_GLOBAL>(sm, gin, gout, gs, valid, scale, tw);

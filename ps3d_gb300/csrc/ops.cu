@@ -755,8 +755,9 @@ void red_pass1(const Dims &d, cudaStream_t st, const T *vel, const T *vor, doubl
 // Rutishauser cyclic Jacobi eigenvalues of a symmetric 3x3 (jacobi.f90),
 // upper triangle a01 a02 a12, diagonal d0 d1 d2; returns max |lambda|.
 // FP64: the reference's absolute tolerance 1e-15 with a bounded sweep count
-// (*hit set if the bound is reached).  FP32: the same rotations stopped at
-// FP32 resolution (relative tolerance) after at most 12 sweeps.
+// (*hit set if the bound is reached).  FP32 (unused by the mixed form,
+// which takes the closed form below): the same rotations stopped at FP32
+// resolution after at most 12 sweeps.
 template <typename A>
 __device__ __forceinline__ void givens_rot(A aij, A di, A dj, A &c, A &s, A &t, A &tau)
 {
@@ -830,6 +831,43 @@ __device__ A jacobi_maxabs(A a00, A a01, A a02, A a11, A a12, A a22, int *hit)
     return fmax(fmax(fabs(D[0]), fabs(D[1])), fabs(D[2]));
 }
 
+// Largest |eigenvalue| of a symmetric 3x3 in closed form (FP32 path):
+// with m = tr/3 and B = A - m I, the eigenvalues are m + 2 s cos(psi/3 -
+// 2 pi k/3), s = sqrt(tr(B^2)/6), cos(psi) = det(B) / (2 s^3) (Smith 1961,
+// Commun. ACM 4:168).  The extreme eigenvalues (k = 0, 2) are well
+// conditioned in this form, which gives them to a few FP32 rounding units,
+// the resolution of the FP32 gradients they come from.
+__device__ __forceinline__ float sym3_maxabs(float a00, float a01, float a02, float a11, float a12, float a22)
+{
+    const float m = (a00 + a11 + a22) * (1.0f / 3.0f);
+    const float b00 = a00 - m, b11 = a11 - m, b22 = a22 - m;
+    const float p2 = b00 * b00 + b11 * b11 + b22 * b22 + 2.0f * (a01 * a01 + a02 * a02 + a12 * a12);
+    if (!(p2 > 0.0f)) return fabsf(m);
+    const float s = sqrtf(p2 * (1.0f / 6.0f));
+    const float det = b00 * (b11 * b22 - a12 * a12) - a01 * (a01 * b22 - a12 * a02) + a02 * (a01 * a12 - b11 * a02);
+    const float r = fminf(fmaxf(det / (2.0f * s * s * s), -1.0f), 1.0f);
+    const float th = acosf(r) * (1.0f / 3.0f);
+    float sn, cs;
+    sincosf(th, &sn, &cs);
+    const float lmax = m + 2.0f * s * cs;                                          // k = 0
+    const float lmin = m + 2.0f * s * (-0.5f * cs - 0.86602540378443865f * sn);   // k = 2
+    return fmaxf(fabsf(lmax), fabsf(lmin));
+}
+
+template <typename T> struct StrainMax;
+template <> struct StrainMax<double> {
+    __device__ static double get(double a00, double a01, double a02, double a11, double a12, double a22, int *hit)
+    {
+        return jacobi_maxabs<double>(a00, a01, a02, a11, a12, a22, hit);
+    }
+};
+template <> struct StrainMax<float> {
+    __device__ static float get(float a00, float a01, float a02, float a11, float a12, float a22, int *)
+    {
+        return sym3_maxabs(a00, a01, a02, a11, a12, a22);
+    }
+};
+
 // pass 2: 0 vorl1, 1 vorl2 (characteristic vorticity, field_diagnostics.f90:
 // 501-545), 2 ggmax, 3 usggmax, 4 lsggmax (advance.f90:222-276)
 template <typename T>
@@ -858,7 +896,7 @@ __global__ void k_red2(Dims d, const T *__restrict__ vor, const T *__restrict__ 
             }
             const T dudx = g5[i], dudy = g5[N + i], dwdx = g5[2 * N + i], dvdy = g5[3 * N + i],
                     dwdy = g5[4 * N + i];
-            const T lmax = jacobi_maxabs<T>(dudx, dudy + (T)0.5 * z, dwdx + (T)0.5 * y, dvdy,
+            const T lmax = StrainMax<T>::get(dudx, dudy + (T)0.5 * z, dwdx + (T)0.5 * y, dvdy,
                                              dwdy - (T)0.5 * x, -(dudx + dvdy), &hit);
             gg = fmax(gg, lmax);
             if (iz == d.nz) us = fmax(us, lmax);

@@ -316,3 +316,38 @@ def test_mixed_steps_track_fp64_at_fused_sizes(n):
     err = rel_l2(g.get("svor"), o.get("svor"))
     assert err < 1.0e-6, err
     assert abs(dg["ke"] - do["ke"]) < 1e-6 * do["ke"]
+
+
+@pytest.mark.parametrize("grid", [(64, 128, 8), (256, 64, 8), (512, 16, 8), (16, 512, 8), (1024, 8, 8),
+                                  (8, 1024, 8)], ids=lambda g: "x".join(map(str, g)))
+@pytest.mark.parametrize("op", ["fftxyp2s", "fftxys2p", "decompose_physical", "combine_physical"])
+def test_mixed_line_transforms_match_oracle(grid, op):
+    """FP32 register-butterfly line FFTs of the mixed form (x and y lines of
+    64..1024 points; the inverse reads the Hermitian rows in its first
+    pass) against the FP64 oracle, relative L2 within 2e-6."""
+    o = oracle.Oracle(*grid, [0.0, 0.0, 0.0], [1.0, 2.0, 0.5])
+    g = Ps3dGpu(*grid, [0.0, 0.0, 0.0], [1.0, 2.0, 0.5], precision="mixed")
+    f = np.random.default_rng(12).standard_normal(o.shape)
+    err = rel_l2(getattr(g, op)(f), getattr(o, op)(f))
+    assert err < MIXED_OP_TOL, (op, grid, err)
+
+
+@pytest.mark.parametrize("grid", [(32, 32, 32), (64, 32, 64)], ids=lambda g: "x".join(map(str, g)))
+def test_mixed_adapt_diagnostics_match_oracle(grid):
+    """Mixed-form adapt (FP32 strain eigenvalues in closed form, FP32
+    compensated sums) against the FP64 oracle's Jacobi eigenvalues: the time
+    step and every diagnostic within 2e-5 relative (the FP32 gradients carry
+    about 1e-6 relative rounding)."""
+    nx, ny, nz = grid
+    lo, ex = ic.BASELINE_BOX["lower"], ic.BASELINE_BOX["extent"]
+    vor, pert = ic.beltrami_plus_perturbation(nx, ny, nz, seed=8, amplitude=5.0e-2)
+    o = oracle.Oracle(nx, ny, nz, lo, ex, pretype="vorch")
+    g = Ps3dGpu(nx, ny, nz, lo, ex, pretype="vorch", precision="mixed")
+    o.setup_fields(vor, pert)
+    g.setup_fields(vor, pert)
+    dtg, dg = g.adapt(0.0)
+    dto, do = o.adapt(0.0)
+    assert abs(dtg - dto) <= 2e-5 * dto, (dtg, dto)
+    for k in ("ke", "en", "hel", "vortmax", "vortrms", "vorch", "ggmax", "usggmax", "lsggmax",
+              "umax", "vmax", "wmax", "pref"):
+        assert abs(dg[k] - do[k]) <= 2e-5 * max(abs(do[k]), 1e-300), (k, dg[k], do[k])
