@@ -270,10 +270,14 @@ __device__ __forceinline__ void st2(float *col, int k, float e, float o)
 
 }  // namespace
 
+// resident 256-thread blocks per SM: three up to nz = 512 (85 registers, a
+// few spilled), two at nz = 1024
+template <int M> constexpr int col_blocks_per_sm() { return M <= 16 ? 3 : 2; }
+
 // MODE: COL_DST, COL_DCT, COL_DECOMP, COL_COMBINE (see kernels.h).  Safe in
 // place: a pair's inputs are all read before its outputs are written.
 template <int MODE, int M, typename TIN>
-__global__ void __launch_bounds__(256, 2) k_colz(const TIN *__restrict__ in, float *__restrict__ out, int P,
+__global__ void __launch_bounds__(256, col_blocks_per_sm<M>()) k_colz(const TIN *__restrict__ in, float *__restrict__ out, int P,
                                               long long npairs, const double *__restrict__ k2l2, float dz,
                                               float Lz, const float2 *__restrict__ twn,
                                               const float *__restrict__ sinz, const float *__restrict__ cosz)

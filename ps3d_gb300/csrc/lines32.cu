@@ -21,6 +21,9 @@ constexpr int LANES = 16;
 template <int N> struct LinePlan {
     static constexpr int T = N >= 512 ? 512 : 256;  // threads per block
     static constexpr int G = T / LANES;             // butterfly groups per lane
+    // resident blocks per SM: two 512-thread blocks (64 registers each) at
+    // N = 512, three 256-thread blocks below (shared memory N * 128 bytes)
+    static constexpr int MINB = N >= 1024 ? 1 : (N >= 512 ? 2 : 3);
 };
 
 __device__ __forceinline__ float2 cm(float2 a, float2 b)
@@ -191,7 +194,7 @@ __device__ __forceinline__ void fft_passes(float2 *sm, const float2 *gin, float2
 }
 
 template <int N, bool INV>
-__global__ void __launch_bounds__(LinePlan<N>::T) k_lines32(const float *__restrict__ in, float *__restrict__ out,
+__global__ void __launch_bounds__(LinePlan<N>::T, LinePlan<N>::MINB) k_lines32(const float *__restrict__ in, float *__restrict__ out,
                                                             int P, long long line_stride, long long batch_stride,
                                                             const float2 *__restrict__ tw)
 {
