@@ -156,13 +156,14 @@ void op_cn2_update(const Dims &d, cudaStream_t st, double *svor, const double *v
                    const double *filt0, const double *fz, const double *vdiss, double dt2);
 void op_mean_fix(const Dims &d, cudaStream_t st, double *svor, const double *dstsum, double fnzi,
                  const double *ini, double *savg_out, int apply, float *svor32 = nullptr);
-// mixed-form stage updates (FP64 state, FP32 source and state copy)
-void op_rk4m_sub1(const Dims &d, cudaStream_t st, double *q, double *qdi, double *qdf, float *sqs, float *q32,
+// mixed-form stage updates (FP64 state, FP32 source, state copy and
+// accumulated source increments acc)
+void op_rk4m_sub1(const Dims &d, cudaStream_t st, double *q, double *qdi, float *acc, const float *sqs, float *q32,
                   const double *filt0, const double *emq, double dt2, double dt6);
-void op_rk4m_sub23(const Dims &d, cudaStream_t st, double *q, const double *qdi, double *qdf, const float *sqs,
+void op_rk4m_sub23(const Dims &d, cudaStream_t st, double *q, const double *qdi, float *acc, const float *sqs,
                    float *q32, const double *epq, const double *emq, double c1, double dt3);
-void op_rk4m_sub4(const Dims &d, cudaStream_t st, double *q, const double *qdf, const float *sqs, float *q32,
-                  const double *epq, const double *emq, double dt6);
+void op_rk4m_sub4(const Dims &d, cudaStream_t st, double *q, const double *qdi, const float *acc, const float *sqs,
+                  float *q32, const double *epq, const double *emq, double dt6);
 void op_narrow(cudaStream_t st, const double *in, float *out, long long n);
 
 // reductions (adapt, energy series); results are FP64 partials per block

@@ -450,11 +450,15 @@ void op_rk4_sub4(const Dims &d, cudaStream_t st, double *q, const double *qdf, c
 
 // Mixed form: the increment (c1 * epq * sqs, an FP32 source term scaled by
 // per-column factors) is formed in FP32 and widened exactly; the state keeps
-// its FP64 accumulation with one fused multiply-add (q = qdi*m + inc) and one
-// add (qdf += inc) per element, and the FP32 copy of the new state that the
-// next vor2vel reads is written alongside.
-__global__ void k_rk4m_sub1(Dims d, double *__restrict__ q, double *__restrict__ qdi, double *__restrict__ qdf,
-                            float *__restrict__ sqs, float *__restrict__ q32, const double *__restrict__ filt0,
+// its FP64 accumulation with one fused multiply-add (q = qdi*m + inc) per
+// element, and the FP32 copy of the new state that the next vor2vel reads is
+// written alongside.  The reference's FP64 accumulator qdf = qdi + d is kept
+// as its FP32 part d = dt/6 s1 + dt/3 s2 + dt/3 s3 alone (a source-sized
+// term, of order dt |s| against the state), and the last substep forms
+// qdf m + c s4 = qdi m + (d m + c s4).  The filtered stage-1 source is not
+// written back: the next source evaluation overwrites it.
+__global__ void k_rk4m_sub1(Dims d, double *__restrict__ q, double *__restrict__ qdi, float *__restrict__ acc,
+                            const float *__restrict__ sqs, float *__restrict__ q32, const double *__restrict__ filt0,
                             const double *__restrict__ emq, double dt2, double dt6)
 {
     COLUMN_HEADER
@@ -465,16 +469,15 @@ __global__ void k_rk4m_sub1(Dims d, double *__restrict__ q, double *__restrict__
         const long long i = o + iz;
         const float s = f0 * sqs[i];
         const double q0 = q[i];
-        sqs[i] = s;
         qdi[i] = q0;
         const double qn = fma(q0, m, widen64(c2 * s));
         q[i] = qn;
         q32[i] = narrow32(qn);
-        qdf[i] = q0 + widen64(c6 * s);
+        acc[i] = c6 * s;
     }
 }
 __global__ void k_rk4m_sub23(Dims d, double *__restrict__ q, const double *__restrict__ qdi,
-                             double *__restrict__ qdf, const float *__restrict__ sqs, float *__restrict__ q32,
+                             float *__restrict__ acc, const float *__restrict__ sqs, float *__restrict__ q32,
                              const double *__restrict__ epq, const double *__restrict__ emq, double c1, double dt3)
 {
     COLUMN_HEADER
@@ -487,37 +490,37 @@ __global__ void k_rk4m_sub23(Dims d, double *__restrict__ q, const double *__res
         const double qn = fma(qdi[i], m, widen64(cq * s));
         q[i] = qn;
         q32[i] = narrow32(qn);
-        qdf[i] = qdf[i] + widen64(c3 * s);
+        acc[i] = fmaf(c3, s, acc[i]);
     }
 }
-__global__ void k_rk4m_sub4(Dims d, double *__restrict__ q, const double *__restrict__ qdf,
-                            const float *__restrict__ sqs, float *__restrict__ q32, const double *__restrict__ epq,
-                            const double *__restrict__ emq, double dt6)
+__global__ void k_rk4m_sub4(Dims d, double *__restrict__ q, const double *__restrict__ qdi,
+                            const float *__restrict__ acc, const float *__restrict__ sqs, float *__restrict__ q32,
+                            const double *__restrict__ epq, const double *__restrict__ emq, double dt6)
 {
     COLUMN_HEADER
     const double m = emq[col];
-    const float c = (float)(dt6 * epq[col] * m);
+    const float mf = (float)m, c = (float)(dt6 * epq[col] * m);
     for (int iz = threadIdx.x; iz <= d.nz; iz += 32) {
         const long long i = o + iz;
-        const double qn = fma(qdf[i], m, widen64(c * sqs[i]));
+        const double qn = fma(qdi[i], m, widen64(fmaf(acc[i], mf, c * sqs[i])));
         q[i] = qn;
         q32[i] = narrow32(qn);
     }
 }
-void op_rk4m_sub1(const Dims &d, cudaStream_t st, double *q, double *qdi, double *qdf, float *sqs, float *q32,
+void op_rk4m_sub1(const Dims &d, cudaStream_t st, double *q, double *qdi, float *acc, const float *sqs, float *q32,
                   const double *filt0, const double *emq, double dt2, double dt6)
 {
-    k_rk4m_sub1<<<col_grid(d), COL_BLOCK, 0, st>>>(d, q, qdi, qdf, sqs, q32, filt0, emq, dt2, dt6);
+    k_rk4m_sub1<<<col_grid(d), COL_BLOCK, 0, st>>>(d, q, qdi, acc, sqs, q32, filt0, emq, dt2, dt6);
 }
-void op_rk4m_sub23(const Dims &d, cudaStream_t st, double *q, const double *qdi, double *qdf, const float *sqs,
+void op_rk4m_sub23(const Dims &d, cudaStream_t st, double *q, const double *qdi, float *acc, const float *sqs,
                    float *q32, const double *epq, const double *emq, double c1, double dt3)
 {
-    k_rk4m_sub23<<<col_grid(d), COL_BLOCK, 0, st>>>(d, q, qdi, qdf, sqs, q32, epq, emq, c1, dt3);
+    k_rk4m_sub23<<<col_grid(d), COL_BLOCK, 0, st>>>(d, q, qdi, acc, sqs, q32, epq, emq, c1, dt3);
 }
-void op_rk4m_sub4(const Dims &d, cudaStream_t st, double *q, const double *qdf, const float *sqs, float *q32,
-                  const double *epq, const double *emq, double dt6)
+void op_rk4m_sub4(const Dims &d, cudaStream_t st, double *q, const double *qdi, const float *acc, const float *sqs,
+                  float *q32, const double *epq, const double *emq, double dt6)
 {
-    k_rk4m_sub4<<<col_grid(d), COL_BLOCK, 0, st>>>(d, q, qdf, sqs, q32, epq, emq, dt6);
+    k_rk4m_sub4<<<col_grid(d), COL_BLOCK, 0, st>>>(d, q, qdi, acc, sqs, q32, epq, emq, dt6);
 }
 
 // FP32 copy of an FP64 field (integer narrowing)

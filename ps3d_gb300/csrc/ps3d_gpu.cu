@@ -423,6 +423,11 @@ template <typename T> int source(ps3d_gpu_ctx *c)
             c->launches += 1;
         }
     op_products<T>(d, c->st, vel, vor, r, q, p);
+    // the z derivatives are taken on the physical products, as in the
+    // reference: on the semi-spectral columns (where the difference commutes
+    // with the horizontal transform) the FP32 form would amplify the
+    // transform's rounding by 1/dz at every level, and in 256^3 and 512^3
+    // runs that seeded a growing top-boundary error within about 40 steps
     op_diffz<T>(d, c->st, c->dzi, q, gq);
     op_diffz<T>(d, c->st, c->dzi, p, gp);
     c->launches += 3;
@@ -563,9 +568,11 @@ template <typename T> int step_rk4(ps3d_gpu_ctx *c, double *t, double dt)
     c->launches += 1;
     const bool mixed = sizeof(T) == sizeof(float);
     float *s32 = reinterpret_cast<float *>(sv), *q32 = c->svor32;
+    // mixed: the accumulator's FP32 increments live in the (FP64-sized) svorf
+    float *acc = reinterpret_cast<float *>(c->svorf);
     for (int k = 0; k < 3; ++k) {
         if (mixed)
-            op_rk4m_sub1(d, c->st, c->svor + k * N, c->svori + k * N, c->svorf + k * N, s32 + k * N, q32 + k * N,
+            op_rk4m_sub1(d, c->st, c->svor + k * N, c->svori + k * N, acc + k * N, s32 + k * N, q32 + k * N,
                          c->filt0, c->emq, dt2, dt6);
         else
             op_rk4_sub1<T>(d, c->st, c->svor + k * N, c->svori + k * N, c->svorf + k * N, sv + k * N, c->filt0,
@@ -577,7 +584,7 @@ template <typename T> int step_rk4(ps3d_gpu_ctx *c, double *t, double dt)
     *t += dt2;
     for (int k = 0; k < 3; ++k) {
         if (mixed)
-            op_rk4m_sub23(d, c->st, c->svor + k * N, c->svori + k * N, c->svorf + k * N, s32 + k * N, q32 + k * N,
+            op_rk4m_sub23(d, c->st, c->svor + k * N, c->svori + k * N, acc + k * N, s32 + k * N, q32 + k * N,
                           c->epq, c->emq, dt2, dt3);
         else
             op_rk4_sub23<T>(d, c->st, c->svor + k * N, c->svori + k * N, c->svorf + k * N, sv + k * N, c->epq,
@@ -589,7 +596,7 @@ template <typename T> int step_rk4(ps3d_gpu_ctx *c, double *t, double dt)
     *t += dt2;
     for (int k = 0; k < 3; ++k) {
         if (mixed)
-            op_rk4m_sub23(d, c->st, c->svor + k * N, c->svori + k * N, c->svorf + k * N, s32 + k * N, q32 + k * N,
+            op_rk4m_sub23(d, c->st, c->svor + k * N, c->svori + k * N, acc + k * N, s32 + k * N, q32 + k * N,
                           c->epq, c->emq2, dt, dt3);
         else
             op_rk4_sub23<T>(d, c->st, c->svor + k * N, c->svori + k * N, c->svorf + k * N, sv + k * N, c->epq,
@@ -600,8 +607,8 @@ template <typename T> int step_rk4(ps3d_gpu_ctx *c, double *t, double dt)
     if (rc) return rc;
     for (int k = 0; k < 3; ++k) {
         if (mixed)
-            op_rk4m_sub4(d, c->st, c->svor + k * N, c->svorf + k * N, s32 + k * N, q32 + k * N, c->epq2, c->emq2,
-                         dt6);
+            op_rk4m_sub4(d, c->st, c->svor + k * N, c->svori + k * N, acc + k * N, s32 + k * N, q32 + k * N,
+                         c->epq2, c->emq2, dt6);
         else
             op_rk4_sub4<T>(d, c->st, c->svor + k * N, c->svorf + k * N, sv + k * N, c->epq2, c->emq2, dt6);
     }
