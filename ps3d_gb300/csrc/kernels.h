@@ -165,6 +165,9 @@ void op_rk4m_sub23(const Dims &d, cudaStream_t st, double *q, const double *qdi,
 void op_rk4m_sub4(const Dims &d, cudaStream_t st, double *q, const double *qdi, const float *acc, const float *sqs,
                   float *q32, const double *epq, const double *emq, double dt6);
 void op_narrow(cudaStream_t st, const double *in, float *out, long long n);
+// host-layout (nz+1)-pitched FP64 columns <-> device P-pitched columns
+void op_unpack_cols(const Dims &d, cudaStream_t st, const double *src, double *dst, int ncomp, int *changed);
+void op_pack_cols(const Dims &d, cudaStream_t st, const double *src, double *dst, int ncomp);
 
 // reductions (adapt, energy series); results are FP64 partials per block
 struct RedOut {

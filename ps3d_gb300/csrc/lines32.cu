@@ -4,46 +4,59 @@
 //
 // A block owns 32 consecutive z values (one 128-byte row segment per line
 // index) of one line set: 16 complex lanes, each packing two real lines
-// (z, z+1).  The Stockham passes keep their butterflies in registers:
+// (z, z+1).  A thread carries two adjacent lanes as one float4, so every
+// global and shared-memory access moves 16 bytes and eight threads cover a
+// 128-byte row.  The Stockham passes keep their butterflies in registers:
 // the first pass of a forward transform loads its inputs straight from HBM
 // (coalesced 128-byte rows), the last pass of an inverse transform stores
 // straight to HBM, and the passes in between exchange through one shared
 // buffer laid out [line index][lane] so every access is bank-conflict free.
-// N (the line length) is a compile-time constant: 64..1024.
+// The first pass of an inverse transform rebuilds the packed spectrum from
+// the Hermitian rows k and N - k as it loads them (one lane per thread
+// there, to bound the registers).  N (the line length) is a compile-time
+// constant: 64..1024.
 #include "kernels.h"
 
 namespace ps3d {
 
 namespace {
 
-constexpr int LANES = 16;
+constexpr int LANES = 16;  // complex lanes per block
+constexpr int PAIRS = 8;   // threads per row (two lanes each)
 
-template <int N> struct LinePlan {
-    static constexpr int T = N >= 512 ? 512 : 256;  // threads per block
-    static constexpr int G = T / LANES;             // butterfly groups per lane
-    // resident blocks per SM: two 512-thread blocks (64 registers each) at
-    // N = 512, three 256-thread blocks below (shared memory N * 128 bytes)
-    static constexpr int MINB = N >= 1024 ? 1 : (N >= 512 ? 2 : 3);
+template <int N, bool INV> struct LinePlan {
+    // threads per block: 512 for the forward transform at N >= 512; the
+    // inverse runs 256-thread blocks there (more registers per thread for
+    // its Hermitian first pass)
+    static constexpr int T = (N >= 1024 || (N >= 512 && !INV)) ? 512 : 256;
+    static constexpr int G = T / PAIRS;  // butterfly groups
+    // resident blocks per SM: N * 128 bytes of shared memory each, and the
+    // register file shared by T * MINB threads
+    static constexpr int MINB = N >= 1024 ? 1 : (N >= 512 ? (INV ? 3 : 2) : 3);
 };
 
 __device__ __forceinline__ float2 cm(float2 a, float2 b)
 {
     return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
 }
+__device__ __forceinline__ float2 lo2(float4 v) { return make_float2(v.x, v.y); }
+__device__ __forceinline__ float2 hi2(float4 v) { return make_float2(v.z, v.w); }
+__device__ __forceinline__ float4 f4(float2 a, float2 b) { return make_float4(a.x, a.y, b.x, b.y); }
 
 template <int R, bool INV> __device__ __forceinline__ void dftR(float2 *v) { dft<R, INV, float2>(v); }
 
 // one radix-R Stockham pass with span NS over N points: inputs x[j + r N/R]
-// of butterfly j, outputs at (j - k) R + k + r NS, k = j mod NS
+// of butterfly j, outputs at (j - k) R + k + r NS, k = j mod NS; each thread
+// applies it to its two lanes
 template <int N, int R, int NS, bool INV, bool FROM_GLOBAL, bool TO_GLOBAL>
-__device__ __forceinline__ void pass(float2 *sm, const float2 *__restrict__ gin, float2 *__restrict__ gout,
+__device__ __forceinline__ void pass(float4 *sm, const float4 *__restrict__ gin, float4 *__restrict__ gout,
                                      long long gstride, bool valid, float scale, const float2 *__restrict__ tw)
 {
-    constexpr int G = LinePlan<N>::G;
-    constexpr int NB = N / R;                         // butterflies per lane
-    constexpr int NBT = (NB + G - 1) / G;             // per thread
-    const int p = threadIdx.x & (LANES - 1), g = threadIdx.x / LANES;
-    float2 v[NBT][R];
+    constexpr int G = LinePlan<N, INV>::G;
+    constexpr int NB = N / R;              // butterflies per lane
+    constexpr int NBT = (NB + G - 1) / G;  // per thread
+    const int p = threadIdx.x & (PAIRS - 1), g = threadIdx.x / PAIRS;
+    float2 va[NBT][R], vb[NBT][R];
 #pragma unroll
     for (int q = 0; q < NBT; ++q) {
         const int j = g + G * q;
@@ -51,11 +64,11 @@ __device__ __forceinline__ void pass(float2 *sm, const float2 *__restrict__ gin,
 #pragma unroll
             for (int r = 0; r < R; ++r) {
                 const int row = j + r * NB;
-                if (FROM_GLOBAL) {
-                    v[q][r] = valid ? gin[row * gstride] : make_float2(0.f, 0.f);
-                } else {
-                    v[q][r] = sm[row * LANES + p];
-                }
+                float4 x;
+                if (FROM_GLOBAL) x = valid ? gin[row * gstride] : make_float4(0.f, 0.f, 0.f, 0.f);
+                else x = sm[row * PAIRS + p];
+                va[q][r] = lo2(x);
+                vb[q][r] = hi2(x);
             }
         }
     }
@@ -70,24 +83,27 @@ __device__ __forceinline__ void pass(float2 *sm, const float2 *__restrict__ gin,
                 for (int r = 1; r < R; ++r) {
                     float2 w = __ldg(&tw[k * r * (N / (NS * R))]);
                     if (INV) w.y = -w.y;
-                    v[q][r] = cm(v[q][r], w);
+                    va[q][r] = cm(va[q][r], w);
+                    vb[q][r] = cm(vb[q][r], w);
                 }
             }
-            dftR<R, INV>(v[q]);
+            dftR<R, INV>(va[q]);
+            dftR<R, INV>(vb[q]);
 #pragma unroll
             for (int r = 0; r < R; ++r) {
                 const int row = (j - k) * R + k + r * NS;
                 if (TO_GLOBAL) {
-                    if (valid) gout[row * gstride] = make_float2(v[q][r].x * scale, v[q][r].y * scale);
+                    if (valid)
+                        gout[row * gstride] = make_float4(va[q][r].x * scale, va[q][r].y * scale,
+                                                          vb[q][r].x * scale, vb[q][r].y * scale);
                 } else {
-                    sm[row * LANES + p] = v[q][r];
+                    sm[row * PAIRS + p] = f4(va[q][r], vb[q][r]);
                 }
             }
         }
     }
     __syncthreads();
 }
-
 
 // C_k = A_k + i B_k of the two packed lines from the Hermitian rows
 // lo = H[min(k, N-k)] and hi = H[max(k, N-k)] (stafft.f90:55-58 storage)
@@ -96,27 +112,29 @@ __device__ __forceinline__ float2 herm_high(float2 lo, float2 hi) { return make_
 
 // First radix-8 pass (span 1) of an inverse transform straight from the
 // Hermitian rows in HBM.  Butterfly j reads rows j + r N/8, whose mirrors
-// N - row are the rows of butterfly N/8 - j: a thread owns such a pair of
+// N - row are the rows of butterfly N/8 - j: one work item is such a pair of
 // butterflies (slot s: s and N/8 - s; slot 0: butterflies 0 and N/16, each
-// its own mirror), so every row is loaded once and used for both C_k and
-// C_{N-k}.
+// its own mirror) for one lane, so every row is loaded once and used for
+// both C_k and C_{N-k}.  Items: slots x 16 lanes over the block's threads.
 template <int N>
-__device__ __forceinline__ void herm_first_pass(float2 *sm, const float2 *__restrict__ gin, long long gs,
-                                                bool valid)
+__device__ __forceinline__ void herm_first_pass(float2 *sm2, const float2 *__restrict__ gin2, long long gs2,
+                                                int z0, int P)
 {
-    constexpr int G = LinePlan<N>::G, NB = N / 8, SLOTS = NB / 2;
-    constexpr int SPT = (SLOTS + G - 1) / G;
-    const int p = threadIdx.x & (LANES - 1), g = threadIdx.x / LANES;
-#pragma unroll
-    for (int q = 0; q < SPT; ++q) {
-        const int s = g + G * q;
-        if (!(SLOTS % G == 0 || s < SLOTS)) continue;
+    constexpr int T = LinePlan<N, true>::T, NB = N / 8, SLOTS = NB / 2;
+    constexpr int ITEMS = SLOTS * LANES, IPT = (ITEMS + T - 1) / T;
+#pragma unroll 1
+    for (int q = 0; q < IPT; ++q) {
+        const int it = threadIdx.x + T * q;
+        if (!(ITEMS % T == 0 || it < ITEMS)) continue;
+        const int lane = it & (LANES - 1), s = it / LANES;
+        const bool valid = z0 + 2 * lane < P;
+        const float2 *g = gin2 + lane;
         const int j1 = s == 0 ? 0 : s, j2 = s == 0 ? NB / 2 : NB - s;
         float2 h1[8], h2[8];
 #pragma unroll
         for (int r = 0; r < 8; ++r) {
-            h1[r] = valid ? gin[(j1 + r * NB) * gs] : make_float2(0.f, 0.f);
-            h2[r] = valid ? gin[(j2 + r * NB) * gs] : make_float2(0.f, 0.f);
+            h1[r] = valid ? g[(j1 + r * NB) * gs2] : make_float2(0.f, 0.f);
+            h2[r] = valid ? g[(j2 + r * NB) * gs2] : make_float2(0.f, 0.f);
         }
         float2 a[8], b[8];
         if (s == 0) {
@@ -149,82 +167,76 @@ __device__ __forceinline__ void herm_first_pass(float2 *sm, const float2 *__rest
         dftR<8, true>(b);
 #pragma unroll
         for (int r = 0; r < 8; ++r) {
-            sm[(j1 * 8 + r) * LANES + p] = a[r];
-            sm[(j2 * 8 + r) * LANES + p] = b[r];
+            sm2[(j1 * 8 + r) * LANES + lane] = a[r];
+            sm2[(j2 * 8 + r) * LANES + lane] = b[r];
         }
     }
     __syncthreads();
 }
 
-template <int N, bool INV, bool FROM_GLOBAL>
-__device__ __forceinline__ void first_pass(float2 *sm, const float2 *gin, float2 *gout, long long gs, bool valid,
-                                           float scale, const float2 *tw)
-{
-    if constexpr (INV && FROM_GLOBAL) herm_first_pass<N>(sm, gin, gs, valid);
-    else pass<N, 8, 1, INV, FROM_GLOBAL, false>(sm, gin, gout, gs, valid, scale, tw);
-}
-
-// the complete pass sequence for N = 8^a * {1, 2, 4}; the first pass of an
-// inverse transform reads the Hermitian rows
-template <int N, bool INV, bool FROM_GLOBAL, bool TO_GLOBAL>
-__device__ __forceinline__ void fft_passes(float2 *sm, const float2 *gin, float2 *gout, long long gs, bool valid,
-                                           float scale, const float2 *tw)
+// the passes after the first for N = 8^a * {1, 2, 4}
+template <int N, bool INV, bool TO_GLOBAL>
+__device__ __forceinline__ void later_passes(float4 *sm, float4 *gout, long long gs, bool valid, float scale,
+                                             const float2 *tw)
 {
     if constexpr (N == 64) {
-        first_pass<N, INV, FROM_GLOBAL>(sm, gin, gout, gs, valid, scale, tw);
-        pass<N, 8, 8, INV, false, TO_GLOBAL>(sm, gin, gout, gs, valid, scale, tw);
+        pass<N, 8, 8, INV, false, TO_GLOBAL>(sm, nullptr, gout, gs, valid, scale, tw);
     } else if constexpr (N == 128) {
-        first_pass<N, INV, FROM_GLOBAL>(sm, gin, gout, gs, valid, scale, tw);
-        pass<N, 8, 8, INV, false, false>(sm, gin, gout, gs, valid, scale, tw);
-        pass<N, 2, 64, INV, false, TO_GLOBAL>(sm, gin, gout, gs, valid, scale, tw);
+        pass<N, 8, 8, INV, false, false>(sm, nullptr, gout, gs, valid, scale, tw);
+        pass<N, 2, 64, INV, false, TO_GLOBAL>(sm, nullptr, gout, gs, valid, scale, tw);
     } else if constexpr (N == 256) {
-        first_pass<N, INV, FROM_GLOBAL>(sm, gin, gout, gs, valid, scale, tw);
-        pass<N, 8, 8, INV, false, false>(sm, gin, gout, gs, valid, scale, tw);
-        pass<N, 4, 64, INV, false, TO_GLOBAL>(sm, gin, gout, gs, valid, scale, tw);
+        pass<N, 8, 8, INV, false, false>(sm, nullptr, gout, gs, valid, scale, tw);
+        pass<N, 4, 64, INV, false, TO_GLOBAL>(sm, nullptr, gout, gs, valid, scale, tw);
     } else if constexpr (N == 512) {
-        first_pass<N, INV, FROM_GLOBAL>(sm, gin, gout, gs, valid, scale, tw);
-        pass<N, 8, 8, INV, false, false>(sm, gin, gout, gs, valid, scale, tw);
-        pass<N, 8, 64, INV, false, TO_GLOBAL>(sm, gin, gout, gs, valid, scale, tw);
+        pass<N, 8, 8, INV, false, false>(sm, nullptr, gout, gs, valid, scale, tw);
+        pass<N, 8, 64, INV, false, TO_GLOBAL>(sm, nullptr, gout, gs, valid, scale, tw);
     } else {  // 1024
-        first_pass<N, INV, FROM_GLOBAL>(sm, gin, gout, gs, valid, scale, tw);
-        pass<N, 8, 8, INV, false, false>(sm, gin, gout, gs, valid, scale, tw);
-        pass<N, 8, 64, INV, false, false>(sm, gin, gout, gs, valid, scale, tw);
-        pass<N, 2, 512, INV, false, TO_GLOBAL>(sm, gin, gout, gs, valid, scale, tw);
+        pass<N, 8, 8, INV, false, false>(sm, nullptr, gout, gs, valid, scale, tw);
+        pass<N, 8, 64, INV, false, false>(sm, nullptr, gout, gs, valid, scale, tw);
+        pass<N, 2, 512, INV, false, TO_GLOBAL>(sm, nullptr, gout, gs, valid, scale, tw);
     }
 }
 
 template <int N, bool INV>
-__global__ void __launch_bounds__(LinePlan<N>::T, LinePlan<N>::MINB) k_lines32(const float *__restrict__ in, float *__restrict__ out,
-                                                            int P, long long line_stride, long long batch_stride,
-                                                            const float2 *__restrict__ tw)
+__global__ void __launch_bounds__(LinePlan<N, INV>::T, LinePlan<N, INV>::MINB)
+    k_lines32(const float *__restrict__ in, float *__restrict__ out, int P, long long line_stride,
+              long long batch_stride, const float2 *__restrict__ tw)
 {
-    extern __shared__ __align__(16) float2 smL[];
-    constexpr int T = LinePlan<N>::T;
-    const int p = threadIdx.x & (LANES - 1);
+    extern __shared__ __align__(16) float4 smL[];
+    constexpr int T = LinePlan<N, INV>::T;
+    const int p = threadIdx.x & (PAIRS - 1);
     const int z0 = blockIdx.x * 2 * LANES;
-    const bool valid = z0 + 2 * p < P;
-    const long long base = ((long long)blockIdx.y * batch_stride + z0 + 2 * p) >> 1;  // float2 units
-    const long long gs = line_stride >> 1;
-    const float2 *gin = reinterpret_cast<const float2 *>(in) + base;
-    float2 *gout = reinterpret_cast<float2 *>(out) + base;
+    const bool valid = z0 + 4 * p < P;  // P is a multiple of 8: both lanes or neither
+    const long long base = (long long)blockIdx.y * batch_stride + z0;  // floats
     const float s = rsqrtf((float)N);
     constexpr int H = N / 2;
     if (!INV) {
-        fft_passes<N, false, true, false>(smL, gin, gout, gs, valid, 1.0f, tw);
-        // split the two packed real transforms and store Hermitian rows
-        for (int e = threadIdx.x; e < (H + 1) * LANES; e += T) {
-            const int k = e / LANES, q = e & (LANES - 1);
-            if (z0 + 2 * q >= P) continue;
-            const float2 ck = smL[k * LANES + q];
-            const float2 cn = smL[((N - k) & (N - 1)) * LANES + q];
-            const float are = 0.5f * (ck.x + cn.x), aim = 0.5f * (ck.y - cn.y);
-            const float bre = 0.5f * (ck.y + cn.y), bim = -0.5f * (ck.x - cn.x);
-            float2 *o = reinterpret_cast<float2 *>(out) + (((long long)blockIdx.y * batch_stride + z0 + 2 * q) >> 1);
-            o[k * gs] = make_float2(are * s, bre * s);
-            if (k > 0 && k < H) o[(N - k) * gs] = make_float2(aim * s, bim * s);
+        const long long gs = line_stride >> 2;  // float4 units
+        const float4 *gin = reinterpret_cast<const float4 *>(in + base) + p;
+        pass<N, 8, 1, false, true, false>(smL, gin, nullptr, gs, valid, 1.0f, tw);
+        later_passes<N, false, false>(smL, nullptr, gs, valid, 1.0f, tw);
+        // split the two packed real transforms of each lane and store the
+        // Hermitian rows k and N - k
+        float4 *o = reinterpret_cast<float4 *>(out + base);
+        for (int e = threadIdx.x; e < (H + 1) * PAIRS; e += T) {
+            const int k = e / PAIRS, q = e & (PAIRS - 1);
+            if (z0 + 4 * q >= P) continue;
+            const float4 ck = smL[k * PAIRS + q];
+            const float4 cn = smL[((N - k) & (N - 1)) * PAIRS + q];
+            // lane 0 in (x, y), lane 1 in (z, w); A = real line z, B = z + 1
+            const float4 re = make_float4(0.5f * (ck.x + cn.x) * s, 0.5f * (ck.y + cn.y) * s,
+                                          0.5f * (ck.z + cn.z) * s, 0.5f * (ck.w + cn.w) * s);
+            o[k * gs + q] = re;
+            if (k > 0 && k < H)
+                o[(N - k) * gs + q] = make_float4(0.5f * (ck.y - cn.y) * s, -0.5f * (ck.x - cn.x) * s,
+                                                  0.5f * (ck.w - cn.w) * s, -0.5f * (ck.z - cn.z) * s);
         }
     } else {
-        fft_passes<N, true, true, true>(smL, gin, gout, gs, valid, s, tw);
+        herm_first_pass<N>(reinterpret_cast<float2 *>(smL), reinterpret_cast<const float2 *>(in + base),
+                           line_stride >> 1, z0, P);
+        const long long gs = line_stride >> 2;
+        float4 *gout = reinterpret_cast<float4 *>(out + base) + p;
+        later_passes<N, true, true>(smL, gout, gs, valid, s, tw);
     }
 }
 
@@ -234,8 +246,8 @@ void launch32(cudaStream_t st, const float *in, float *out, int P, long long ls,
 {
     dim3 grid((P + 2 * LANES - 1) / (2 * LANES), (unsigned)nbatch);
     const size_t sm = (size_t)N * LANES * sizeof(float2);
-    if (inverse) k_lines32<N, true><<<grid, LinePlan<N>::T, sm, st>>>(in, out, P, ls, bs, tw);
-    else k_lines32<N, false><<<grid, LinePlan<N>::T, sm, st>>>(in, out, P, ls, bs, tw);
+    if (inverse) k_lines32<N, true><<<grid, LinePlan<N, true>::T, sm, st>>>(in, out, P, ls, bs, tw);
+    else k_lines32<N, false><<<grid, LinePlan<N, false>::T, sm, st>>>(in, out, P, ls, bs, tw);
 }
 
 }  // namespace

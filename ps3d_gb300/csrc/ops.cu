@@ -523,6 +523,48 @@ void op_rk4m_sub4(const Dims &d, cudaStream_t st, double *q, const double *qdi, 
     k_rk4m_sub4<<<col_grid(d), COL_BLOCK, 0, st>>>(d, q, qdi, acc, sqs, q32, epq, emq, dt6);
 }
 
+// Host-layout state (nz+1 values per column, the three components one after
+// another) <-> the device's P-pitched columns, FP64.  The unpack raises
+// *changed when any element differs bitwise from the device state it
+// overwrites.
+__global__ void k_unpack_cols(Dims d, const double *__restrict__ src, double *__restrict__ dst, long long ncols,
+                              int *__restrict__ changed)
+{
+    const long long c = (long long)blockIdx.x * COLS_PER_BLOCK + threadIdx.y;
+    if (c >= ncols) return;
+    const int n1 = d.nz + 1;
+    const double *s = src + c * n1;
+    double *t = dst + c * d.P;
+    bool diff = false;
+    for (int iz = threadIdx.x; iz < n1; iz += 32) {
+        const double v = s[iz];
+        diff |= __double_as_longlong(v) != __double_as_longlong(t[iz]);
+        t[iz] = v;
+    }
+    if (__any_sync(0xffffffffu, diff) && threadIdx.x == 0) atomicOr(changed, 1);
+}
+__global__ void k_pack_cols(Dims d, const double *__restrict__ src, double *__restrict__ dst, long long ncols)
+{
+    const long long c = (long long)blockIdx.x * COLS_PER_BLOCK + threadIdx.y;
+    if (c >= ncols) return;
+    const int n1 = d.nz + 1;
+    const double *s = src + c * d.P;
+    double *t = dst + c * n1;
+    for (int iz = threadIdx.x; iz < n1; iz += 32) t[iz] = s[iz];
+}
+void op_unpack_cols(const Dims &d, cudaStream_t st, const double *src, double *dst, int ncomp, int *changed)
+{
+    const long long ncols = (long long)ncomp * d.ncol;
+    k_unpack_cols<<<(unsigned)((ncols + COLS_PER_BLOCK - 1) / COLS_PER_BLOCK), COL_BLOCK, 0, st>>>(d, src, dst,
+                                                                                                   ncols, changed);
+}
+void op_pack_cols(const Dims &d, cudaStream_t st, const double *src, double *dst, int ncomp)
+{
+    const long long ncols = (long long)ncomp * d.ncol;
+    k_pack_cols<<<(unsigned)((ncols + COLS_PER_BLOCK - 1) / COLS_PER_BLOCK), COL_BLOCK, 0, st>>>(d, src, dst,
+                                                                                                 ncols);
+}
+
 // FP32 copy of an FP64 field (integer narrowing)
 __global__ void k_narrow(const double *__restrict__ in, float *__restrict__ out, long long n)
 {

@@ -1251,12 +1251,30 @@ int ps3d_gpu_advance_host(ps3d_gpu_ctx *c, double *svor, double *t, ps3d_gpu_dia
     int rc = enter(c);
     if (rc) return rc;
     if (!svor || !t) return PS3D_ERR_INVALID_ARG;
-    rc = upload(c, svor, 3, c->svor, true);
-    if (rc) return rc;
-    if (!c->fp64) project_state_mixed(c);
+    const Dims &d = c->d;
+    // one linear copy each way through a staging array in host layout (the
+    // RK accumulator svorf, free outside a step); the device re-pitches
+    const size_t bytes = (size_t)3 * d.ncol * (d.nz + 1) * sizeof(double);
+    double *stage = c->svorf;
+    cudaMemcpyAsync(stage, svor, bytes, cudaMemcpyHostToDevice, c->st);
+    cudaMemsetAsync(c->flag, 0, sizeof(int), c->st);
+    op_unpack_cols(d, c->st, stage, c->svor, 3, c->flag);
+    c->launches += 1;
+    if (!c->fp64) {
+        // a state bitwise equal to the device's (the previous step's result)
+        // is already solenoidal; any other state is projected in FP64 first
+        int changed = 0;
+        cudaMemcpyAsync(&changed, c->flag, sizeof(int), cudaMemcpyDeviceToHost, c->st);
+        rc = sync_check(c, "advance_host");
+        if (rc) return rc;
+        if (changed) project_state_mixed(c);
+    }
     rc = ps3d_gpu_advance(c, t, 1, diag);
     if (rc) return rc;
-    return download(c, c->svor, true, 3, svor);
+    op_pack_cols(d, c->st, c->svor, stage, 3);
+    c->launches += 1;
+    cudaMemcpyAsync(svor, stage, bytes, cudaMemcpyDeviceToHost, c->st);
+    return sync_check(c, "advance_host");
 }
 
 int ps3d_gpu_calc_vorticity_mean(ps3d_gpu_ctx *c, double out[2])

@@ -351,3 +351,29 @@ def test_mixed_adapt_diagnostics_match_oracle(grid):
     for k in ("ke", "en", "hel", "vortmax", "vortrms", "vorch", "ggmax", "usggmax", "lsggmax",
               "umax", "vmax", "wmax", "pref"):
         assert abs(dg[k] - do[k]) <= 2e-5 * max(abs(do[k]), 1e-300), (k, dg[k], do[k])
+
+
+def test_mixed_advance_host_matches_resident_and_projects_changes():
+    """advance_host in the mixed form: an unchanged host state continues the
+    resident trajectory bitwise; a changed one is projected first, exactly as
+    set_field does."""
+    lo, ex, vor, pert = beltrami_case(64, seed=9)
+    a = Ps3dGpu(64, 64, 64, lo, ex, precision="mixed")
+    b = Ps3dGpu(64, 64, 64, lo, ex, precision="mixed")
+    a.setup_fields(vor, pert)
+    b.setup_fields(vor, pert)
+    host = np.ascontiguousarray(b.get("svor"))
+    t_a = t_b = 0.0
+    for _ in range(3):
+        t_a, _ = a.advance(t_a)
+        t_b, _ = b.advance_host(host, t_b)
+    assert np.array_equal(a.get("svor"), host)
+    assert t_a == t_b
+    # a host-side change (not solenoidal) goes through the FP64 projection
+    kick = 1e-3 * np.random.default_rng(1).standard_normal(host.shape)
+    changed = host + kick
+    a.set("svor", changed)
+    t_a, _ = a.advance(t_a)
+    host[...] = changed
+    t_b, _ = b.advance_host(host, t_b)
+    assert np.array_equal(a.get("svor"), host)
