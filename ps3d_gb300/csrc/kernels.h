@@ -126,6 +126,10 @@ template <typename T>
 void op_add_const(const Dims &d, cudaStream_t st, T *f, double c);
 template <typename T>
 void op_products(const Dims &d, cudaStream_t st, const T *vel, const T *vor, T *r, T *q, T *p);
+// products and the z derivatives gq = dq/dz, gp = dp/dz in one pass
+template <typename T>
+void op_products_dz(const Dims &d, cudaStream_t st, double dzi, const T *vel, const T *vor, T *r, T *q, T *p,
+                    T *gq, T *gp);
 template <typename T>
 void op_svorts(const Dims &d, cudaStream_t st, const Deriv &D, const T *r, const T *q, const T *p,
                const T *gq, const T *gp, T *s1, T *s2, T *s3);

@@ -282,6 +282,81 @@ void op_products(const Dims &d, cudaStream_t st, const T *vel, const T *vor, T *
     k_products<T><<<col_grid(d), COL_BLOCK, 0, st>>>(d, vel, vor, r, q, p);
 }
 
+// The products together with the z derivatives of q and p (central_diffz,
+// inversion_utils.f90:653-673) in one pass over each column: the
+// neighbours iz -+ 1 come from the adjacent lanes, and across 32-level
+// chunks from the previous chunk (carried) or the next one (the last lane's
+// derivative is written one chunk later).  Same arithmetic as k_products
+// followed by k_diffz.
+template <typename T>
+__global__ void k_products_dz(Dims d, T dzi, T hdzi, const T *__restrict__ vel, const T *__restrict__ vor,
+                              T *__restrict__ r, T *__restrict__ q, T *__restrict__ p, T *__restrict__ gq,
+                              T *__restrict__ gp)
+{
+    COLUMN_HEADER
+    const long long N = d.nfield;
+    const int nz = d.nz, lane = threadIdx.x;
+    T q1 = 0, p1 = 0, q2 = 0, p2 = 0;  // levels 32c - 1 and 32c - 2 of the previous chunk
+    for (int c0 = 0; c0 <= nz; c0 += 32) {
+        const int iz = c0 + lane;
+        T qv = 0, pv = 0;
+        if (iz <= nz) {
+            const long long i = o + iz;
+            const T u = vel[i], v = vel[N + i], w = vel[2 * N + i];
+            const T xi = vor[i], eta = vor[N + i], zeta = vor[2 * N + i];
+            r[i] = u * eta - v * xi;
+            qv = w * xi - u * zeta;
+            pv = v * zeta - w * eta;
+            q[i] = qv;
+            p[i] = pv;
+        }
+        T qm = __shfl_up_sync(0xffffffffu, qv, 1), pm = __shfl_up_sync(0xffffffffu, pv, 1);
+        const T qn = __shfl_down_sync(0xffffffffu, qv, 1), pn = __shfl_down_sync(0xffffffffu, pv, 1);
+        const T q0 = __shfl_sync(0xffffffffu, qv, 0), p0 = __shfl_sync(0xffffffffu, pv, 0);
+        if (lane == 0) {
+            qm = q1;
+            pm = p1;
+        }
+        // the previous chunk's last level, now that its upper neighbour is known
+        if (c0 > 0 && lane == 31) {
+            gq[o + c0 - 1] = (q0 - q2) * hdzi;
+            gp[o + c0 - 1] = (p0 - p2) * hdzi;
+        }
+        if (iz <= nz) {
+            T a = 0, b = 0;
+            bool put = true;
+            if (iz == 0) {
+                a = (qn - qv) * dzi;
+                b = (pn - pv) * dzi;
+            } else if (iz == nz) {
+                a = (qv - qm) * dzi;
+                b = (pv - pm) * dzi;
+            } else if (lane < 31) {
+                a = (qn - qm) * hdzi;
+                b = (pn - pm) * hdzi;
+            } else {
+                put = false;
+            }
+            if (put) {
+                gq[o + iz] = a;
+                gp[o + iz] = b;
+            }
+        }
+        q1 = __shfl_sync(0xffffffffu, qv, 31);
+        p1 = __shfl_sync(0xffffffffu, pv, 31);
+        q2 = __shfl_sync(0xffffffffu, qv, 30);
+        p2 = __shfl_sync(0xffffffffu, pv, 30);
+    }
+}
+template <typename T>
+void op_products_dz(const Dims &d, cudaStream_t st, double dzi, const T *vel, const T *vor, T *r, T *q, T *p,
+                    T *gq, T *gp)
+{
+    k_products_dz<T><<<col_grid(d), COL_BLOCK, 0, st>>>(d, (T)dzi, (T)(0.5 * dzi), vel, vor, r, q, p, gq, gp);
+}
+template void op_products_dz<float>(const Dims &, cudaStream_t, double, const float *, const float *, float *,
+                                    float *, float *, float *, float *);
+
 // svorts = (D_y r - dq/dz, dp/dz - D_x r, D_x q - D_y p) (inversion.f90:341-367)
 template <typename T>
 __global__ void k_svorts(Dims d, Deriv D, const T *__restrict__ r, const T *__restrict__ q,
@@ -701,6 +776,20 @@ int red_nblocks(const Dims &d)
     return (int)nb;
 }
 
+// Reduction grid: at most red_nblocks, and no more blocks than fit on the
+// device at once (a partial second wave would leave most SMs idle while it
+// runs; the kernels stride over the columns)
+template <typename K> int red_grid(const Dims &d, K kern)
+{
+    int dev = 0, sms = 1, per = 1;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kern, COLS_PER_BLOCK * 32, 0);
+    const int cap = sms * (per > 0 ? per : 1);
+    const int nb = red_nblocks(d);
+    return nb < cap ? nb : cap;
+}
+
 // block-level reduce of NV values: kinds[v] = 0 sum, 1 max
 template <int NV>
 __device__ void block_reduce_store(double (&vals)[NV], const int (&kinds)[NV], double *part)
@@ -790,7 +879,7 @@ __global__ void k_red1(Dims d, const T *__restrict__ vel, const T *__restrict__ 
 template <typename T>
 void red_pass1(const Dims &d, cudaStream_t st, const T *vel, const T *vor, double *part, double *result)
 {
-    const int nb = red_nblocks(d);
+    const int nb = red_grid(d, k_red1<T>);
     k_red1<T><<<nb, COL_BLOCK, 0, st>>>(d, vel, vor, part);
     int *kinds;
     cudaGetSymbolAddress((void **)&kinds, c_kinds1);
@@ -958,7 +1047,7 @@ template <typename T>
 void red_pass2(const Dims &d, cudaStream_t st, const T *vor, const T *g5, double vortrms, double *part,
                double *result, int *flag)
 {
-    const int nb = red_nblocks(d);
+    const int nb = red_grid(d, k_red2<T>);
     k_red2<T><<<nb, COL_BLOCK, 0, st>>>(d, vor, g5, vortrms, part, flag);
     int *kinds;
     cudaGetSymbolAddress((void **)&kinds, c_kinds2);

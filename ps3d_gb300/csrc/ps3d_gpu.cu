@@ -422,15 +422,22 @@ template <typename T> int source(ps3d_gpu_ctx *c)
             op_add_const<T>(d, c->st, vor + k * N, c->cfg.f_cor[k]);
             c->launches += 1;
         }
-    op_products<T>(d, c->st, vel, vor, r, q, p);
     // the z derivatives are taken on the physical products, as in the
     // reference: on the semi-spectral columns (where the difference commutes
     // with the horizontal transform) the FP32 form would amplify the
     // transform's rounding by 1/dz at every level, and in 256^3 and 512^3
     // runs that seeded a growing top-boundary error within about 40 steps
-    op_diffz<T>(d, c->st, c->dzi, q, gq);
-    op_diffz<T>(d, c->st, c->dzi, p, gp);
-    c->launches += 3;
+    if (sizeof(T) == sizeof(float)) {
+        op_products_dz<float>(d, c->st, c->dzi, reinterpret_cast<const float *>(vel),
+                              reinterpret_cast<const float *>(vor), tf<float>(r), tf<float>(q), tf<float>(p),
+                              tf<float>(gq), tf<float>(gp));
+        c->launches += 1;
+    } else {
+        op_products<T>(d, c->st, vel, vor, r, q, p);
+        op_diffz<T>(d, c->st, c->dzi, q, gq);
+        op_diffz<T>(d, c->st, c->dzi, p, gp);
+        c->launches += 3;
+    }
     T *f5[5] = {r, q, p, gq, gp};
     for (int k = 0; k < 5; ++k) {
         xyf<T>(c, f5[k], f5[k]);
