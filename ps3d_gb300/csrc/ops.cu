@@ -101,26 +101,70 @@ void op_v2v_wsrc(const Dims &d, cudaStream_t st, const Deriv &D, const S *A, con
     k_v2v_wsrc<T, S><<<col_grid(d), COL_BLOCK, 0, st>>>(d, D, A, B, ds);
 }
 
-// A = k2l2i (D_x es + D_y ds), B = k2l2i (D_y es - D_x ds); the (0,0) column
-// keeps its mean vorticity (inversion.f90:50-76)
-template <typename T, typename S>
-__global__ void k_v2v_project(Dims d, Deriv D, const double *__restrict__ k2l2i, const T *__restrict__ es,
-                              const T *__restrict__ ds, S *__restrict__ A, S *__restrict__ B)
+// Orbit form of the two horizontal inversions below (the projection of
+// inversion.f90:50-76 and u, v of :169-213):
+//   a = k2l2i (D_x e + D_y f),  b = k2l2i (D_y e - D_x f),
+// D_x f at (kx, ky) reading f at (nx - kx, ky) and D_y at (kx, ny - ky).  The
+// columns (kx, ky), (nx-kx, ky), (kx, ny-ky), (nx-kx, ny-ky) read only one
+// another, so one warp takes the whole orbit: e and f are read once instead
+// of twice.  Same expression per output as the per-column form.  MEAN: the
+// (0,0) column gets ubar, vbar; otherwise it is left as it is.
+template <typename T, typename S, bool MEAN>
+__global__ void k_v2v_orbit(Dims d, Deriv D, const double *__restrict__ k2l2i, const T *__restrict__ e,
+                            const T *__restrict__ f, const double *__restrict__ ubar,
+                            const double *__restrict__ vbar, S *__restrict__ a, S *__restrict__ b)
 {
-    COLUMN_HEADER
-    if (col == 0) return;
-    PARTNERS
-    const S kk = (S)k2l2i[col], cx = (S)cxk, cy = (S)cyk;
+    const int hy = d.ny / 2 + 1;
+    const long long orb = (long long)blockIdx.x * COLS_PER_BLOCK + threadIdx.y;
+    if (orb >= (long long)(d.nx / 2 + 1) * hy) return;
+    const int kx = (int)(orb / hy), ky = (int)(orb - (long long)kx * hy);
+    const int x2 = xsrc(kx, d.nx), y2 = xsrc(ky, d.ny);
+    const long long o00 = ((long long)ky + (long long)d.ny * kx) * d.P, o10 = ((long long)ky + (long long)d.ny * x2) * d.P;
+    const long long o01 = ((long long)y2 + (long long)d.ny * kx) * d.P, o11 = ((long long)y2 + (long long)d.ny * x2) * d.P;
+    if (o00 == 0) {
+        if (MEAN)
+            for (int iz = threadIdx.x; iz <= d.nz; iz += 32) {
+                a[iz] = (S)ubar[iz];
+                b[iz] = (S)vbar[iz];
+            }
+        return;
+    }
+    const bool dx = x2 != kx, dy = y2 != ky;
+    const S cxa = (S)D.cx[kx], cxb = (S)D.cx[x2], cya = (S)D.cy[ky], cyb = (S)D.cy[y2];
+    const S k00 = (S)k2l2i[o00 / d.P], k10 = (S)k2l2i[o10 / d.P], k01 = (S)k2l2i[o01 / d.P],
+            k11 = (S)k2l2i[o11 / d.P];
     for (int iz = threadIdx.x; iz <= d.nz; iz += 32) {
-        A[o + iz] = kk * (cx * (S)es[ox + iz] + cy * (S)ds[oy + iz]);
-        B[o + iz] = kk * (cy * (S)es[oy + iz] - cx * (S)ds[ox + iz]);
+        const S e00 = (S)e[o00 + iz], e10 = (S)e[o10 + iz], e01 = (S)e[o01 + iz], e11 = (S)e[o11 + iz];
+        const S f00 = (S)f[o00 + iz], f10 = (S)f[o10 + iz], f01 = (S)f[o01 + iz], f11 = (S)f[o11 + iz];
+        a[o00 + iz] = k00 * (cxa * e10 + cya * f01);
+        b[o00 + iz] = k00 * (cya * e01 - cxa * f10);
+        if (dx) {
+            a[o10 + iz] = k10 * (cxb * e00 + cya * f11);
+            b[o10 + iz] = k10 * (cya * e11 - cxb * f00);
+        }
+        if (dy) {
+            a[o01 + iz] = k01 * (cxa * e11 + cyb * f00);
+            b[o01 + iz] = k01 * (cyb * e00 - cxa * f11);
+        }
+        if (dx && dy) {
+            a[o11 + iz] = k11 * (cxb * e01 + cyb * f10);
+            b[o11 + iz] = k11 * (cyb * e10 - cxb * f01);
+        }
     }
 }
+static inline dim3 orbit_grid(const Dims &d)
+{
+    const long long norb = (long long)(d.nx / 2 + 1) * (d.ny / 2 + 1);
+    return dim3((unsigned)((norb + COLS_PER_BLOCK - 1) / COLS_PER_BLOCK));
+}
+
+// A = k2l2i (D_x es + D_y ds), B = k2l2i (D_y es - D_x ds); the (0,0) column
+// keeps its mean vorticity (inversion.f90:50-76)
 template <typename T, typename S>
 void op_v2v_project(const Dims &d, cudaStream_t st, const Deriv &D, const double *k2l2i, const T *es,
                     const T *ds, S *A, S *B)
 {
-    k_v2v_project<T, S><<<col_grid(d), COL_BLOCK, 0, st>>>(d, D, k2l2i, es, ds, A, B);
+    k_v2v_orbit<T, S, false><<<orbit_grid(d), COL_BLOCK, 0, st>>>(d, D, k2l2i, es, ds, nullptr, nullptr, A, B);
 }
 
 // boundary contributions and Green-function inversion for w
@@ -221,30 +265,10 @@ void op_v2v_meanflow(const Dims &d, cudaStream_t st, const S *A, const S *B, con
 // u = k2l2i (D_x es + D_y cs), v = k2l2i (D_y es - D_x cs), (0,0) = ubar, vbar
 // (inversion.f90:169-213)
 template <typename T>
-__global__ void k_v2v_uv(Dims d, Deriv D, const double *__restrict__ k2l2i, const T *__restrict__ es,
-                         const T *__restrict__ cs, const double *__restrict__ ubar,
-                         const double *__restrict__ vbar, T *__restrict__ u, T *__restrict__ v)
-{
-    COLUMN_HEADER
-    if (col == 0) {
-        for (int iz = threadIdx.x; iz <= d.nz; iz += 32) {
-            u[iz] = (T)ubar[iz];
-            v[iz] = (T)vbar[iz];
-        }
-        return;
-    }
-    PARTNERS
-    const T kk = (T)k2l2i[col], cx = (T)cxk, cy = (T)cyk;
-    for (int iz = threadIdx.x; iz <= d.nz; iz += 32) {
-        u[o + iz] = kk * (cx * es[ox + iz] + cy * cs[oy + iz]);
-        v[o + iz] = kk * (cy * es[oy + iz] - cx * cs[ox + iz]);
-    }
-}
-template <typename T>
 void op_v2v_uv(const Dims &d, cudaStream_t st, const Deriv &D, const double *k2l2i, const T *es, const T *cs,
                const double *ubar, const double *vbar, T *u, T *v)
 {
-    k_v2v_uv<T><<<col_grid(d), COL_BLOCK, 0, st>>>(d, D, k2l2i, es, cs, ubar, vbar, u, v);
+    k_v2v_orbit<T, T, true><<<orbit_grid(d), COL_BLOCK, 0, st>>>(d, D, k2l2i, es, cs, ubar, vbar, u, v);
 }
 
 // ------------------------------------------------------------------- source
@@ -852,6 +876,7 @@ __global__ void k_red1(Dims d, const T *__restrict__ vel, const T *__restrict__ 
     for (long long col = (long long)blockIdx.x * COLS_PER_BLOCK + threadIdx.y; col < d.ncol;
          col += (long long)gridDim.x * COLS_PER_BLOCK) {
         const long long o = col * d.P;
+#pragma unroll 4
         for (int iz = threadIdx.x; iz <= d.nz; iz += 32) {
             const long long i = o + iz;
             const T wt = (iz == 0 || iz == d.nz) ? (T)0.5 : (T)1;
