@@ -214,11 +214,15 @@ def run_gpu(args, rank, world, dist):
     value = world * pts * args.steps / sec / 1e6
     clocks = clk.summary()
 
-    # dominant kernel probe inside real steps (same stream, CUDA events)
+    # dominant kernel probe inside real steps (same stream, CUDA events).
+    # k_lines32 (the line FFT, both directions) and the k_colz column-kernel
+    # family are the candidates; y and x lines are also reported apart.
     probe_steps = max(1, min(3, args.steps))
     best = None
     probes = []
-    for kind, name in ((1, "k_lines (y)"), (2, "k_lines (x)"), (3, "k_columns")):
+    kinds = ((4, "k_lines32 (x and y lines)", True), (3, "k_colz (column transforms)", True),
+             (1, "k_lines32 (y lines)", False), (2, "k_lines32 (x lines)", False))
+    for kind, name, candidate in kinds:
         gm.probe(kind)
         t_m, _ = gm.time_advance(t_m, probe_steps)
         kms, nl, kbytes = gm.probe_result()
@@ -227,17 +231,25 @@ def run_gpu(args, rank, world, dist):
         rec = {"kernel": name, "launches_per_step": nl / probe_steps, "ms_per_launch": kms / max(nl, 1),
                "bytes_per_launch": kbytes / max(nl, 1), "share_of_step": share}
         probes.append(rec)
-        if best is None or kms > best[1]:
-            best = (rec, kms)
+        if candidate and (best is None or kms > best[1]):
+            best = (rec, kms, kind)
     peak, peak_kind = peaks()
     krec = best[0]
     achieved = krec["bytes_per_launch"] / (krec["ms_per_launch"] * 1e-3) / 1e9
+    # DRAM traffic per launch from the committed ncu capture of the same
+    # kernel at 512^3 (profiles/k_lines32_512.md: read + write, mean of four
+    # launches); not measured for other kernels or sizes
+    traffic = 1.04e9 if (best[2] == 4 and n == 512) else None
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                "frac": achieved / peak, "traffic": None, "kernel": krec["kernel"],
+                "frac": achieved / peak, "traffic": traffic, "traffic_unit": "bytes per launch",
+                "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum, profiles/k_lines32_512.md"
+                if traffic else None,
+                "kernel": krec["kernel"],
+                "algorithmic_bytes_per_launch": krec["bytes_per_launch"],
                 "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured" else peak_kind,
                 "kernel_share_of_step": krec["share_of_step"],
                 "probes": probes}
-    svor_mixed_steps = args.warmup + args.steps + 3 * probe_steps
+    svor_mixed_steps = args.warmup + args.steps + len(kinds) * probe_steps
 
     # ---- FP64 form: timing, and the reference for the mixed error --------
     # Both forms run the same `accuracy_steps` advances from the same state;

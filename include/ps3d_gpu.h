@@ -177,7 +177,8 @@ long long ps3d_gpu_launch_count(const ps3d_gpu_ctx *ctx);
 int ps3d_gpu_synchronize(ps3d_gpu_ctx *ctx);
 /* Kernel probe: bracket every launch of one kernel class with CUDA events on
  * the context stream.  kind: 0 off, 1 y-line transforms, 2 x-line
- * transforms, 3 column (z) transforms.  probe resets the counters;
+ * transforms, 3 column (z) transforms, 4 line transforms of both
+ * directions.  probe resets the counters;
  * probe_result returns the summed device time, the number of bracketed
  * launches and their algorithmic bytes (one read and one write of
  * nx*ny*(nz+1) elements per launch). */

@@ -19,7 +19,8 @@ enum { COL_DST = 0, COL_DCT = 1, COL_DECOMP = 2, COL_COMBINE = 3 };
 // Optional timing probe: brackets every launch of one kernel class with CUDA
 // events on the launching stream (used by the benchmark to time the dominant
 // kernel inside a real step).  kind: 0 off, 1 y lines, 2 x lines, 3 columns.
-enum { PROBE_OFF = 0, PROBE_YLINES = 1, PROBE_XLINES = 2, PROBE_COLUMNS = 3 };
+// PROBE_LINES brackets the line transforms of both directions
+enum { PROBE_OFF = 0, PROBE_YLINES = 1, PROBE_XLINES = 2, PROBE_COLUMNS = 3, PROBE_LINES = 4 };
 struct Probe {
     static constexpr int MAXP = 8192;
     int kind = PROBE_OFF;
@@ -27,13 +28,17 @@ struct Probe {
     int used = 0;
     long long launches = 0;
     double bytes = 0.0;         // algorithmic bytes of the bracketed launches
+    bool match(int k) const
+    {
+        return k == kind || (kind == PROBE_LINES && (k == PROBE_YLINES || k == PROBE_XLINES));
+    }
     void begin(int k, cudaStream_t st)
     {
-        if (k == kind && ev && used + 2 <= 2 * MAXP) cudaEventRecord(ev[used++], st);
+        if (match(k) && ev && used + 2 <= 2 * MAXP) cudaEventRecord(ev[used++], st);
     }
     void end(int k, cudaStream_t st, double b)
     {
-        if (k == kind && ev && (used & 1)) {
+        if (match(k) && ev && (used & 1)) {
             cudaEventRecord(ev[used++], st);
             ++launches;
             bytes += b;

@@ -1350,7 +1350,7 @@ int ps3d_gpu_probe(ps3d_gpu_ctx *c, int kind)
 {
     int rc = enter(c);
     if (rc) return rc;
-    if (kind < PROBE_OFF || kind > PROBE_COLUMNS) return PS3D_ERR_INVALID_ARG;
+    if (kind < PROBE_OFF || kind > PROBE_LINES) return PS3D_ERR_INVALID_ARG;
     rc = sync_check(c, "probe");
     if (rc) return rc;
     if (kind != PROBE_OFF && !c->probe.ev) {

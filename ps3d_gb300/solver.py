@@ -246,7 +246,7 @@ class Ps3dGpu:
 
     def probe(self, kind):
         """Bracket launches of one kernel class with events (0 off, 1 y lines,
-        2 x lines, 3 columns)."""
+        2 x lines, 3 columns, 4 lines of both directions)."""
         self._chk(self.L.ps3d_gpu_probe(self._h, int(kind)))
 
     def probe_result(self):
