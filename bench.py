@@ -119,6 +119,8 @@ class ClockSampler:
 # ------------------------------------------------------------ workloads
 def make_ic(n, seed=1):
     from ps3d_gb300 import ic
+    if n >= 1024:  # 26 GB per vector field: build it slab by slab
+        return ic.beltrami_plus_perturbation_slabs(n, n, n, seed=seed, amplitude=1.0e-3)
     return ic.beltrami_plus_perturbation(n, n, n, seed=seed, amplitude=1.0e-3)
 
 

@@ -175,6 +175,21 @@ int ps3d_gpu_time_advance(ps3d_gpu_ctx *ctx, double *t, int nsteps, double *ms);
 /* Kernel launches issued by this context since creation. */
 long long ps3d_gpu_launch_count(const ps3d_gpu_ctx *ctx);
 int ps3d_gpu_synchronize(ps3d_gpu_ctx *ctx);
+/* Captured steps (no reference counterpart): nsteps advances of the mixed
+ * form with impl-diff-rk4, each one CUDA graph launch with adapt's scalar
+ * logic on the device (no host synchronisation inside a step).  Same
+ * arithmetic as ps3d_gpu_advance.  t in/out; diag (optional) receives the
+ * last step's diagnostics, ms (optional) the device time.  A non-finite
+ * diagnostic or a Jacobi limit is reported after the launches
+ * (PS3D_ERR_NONFINITE / PS3D_ERR_DEVICE_LIMIT; the state is then invalid).
+ * PS3D_ERR_INVALID_ARG for the FP64 form, cn2 or a held source. */
+int ps3d_gpu_advance_graph(ps3d_gpu_ctx *ctx, double *t, int nsteps, ps3d_gpu_diag *diag, double *ms);
+/* Batching (no reference counterpart): nsteps captured steps of n independent
+ * contexts (any grid sizes, one device), the runs' graphs interleaved on
+ * their own streams so they execute concurrently.  t[n] in/out; ms = device
+ * time of the whole batch. */
+int ps3d_gpu_batch_advance(ps3d_gpu_ctx *const *ctx, int n, double *t, int nsteps, double *ms);
+
 /* Kernel probe: bracket every launch of one kernel class with CUDA events on
  * the context stream.  kind: 0 off, 1 y-line transforms, 2 x-line
  * transforms, 3 column (z) transforms, 4 line transforms of both

@@ -6,7 +6,7 @@ time steppers behind a C ABI (include/ps3d_gpu.h, libps3d_gpu.so).
     m.setup_fields(vor_phys)
     t, diag = m.advance(0.0)
 """
-from .solver import Ps3dGpu, Ps3dError, make_config  # noqa: F401
+from .solver import Ps3dGpu, Ps3dError, batch_advance, make_config  # noqa: F401
 from . import ic  # noqa: F401
 
-__all__ = ["Ps3dGpu", "Ps3dError", "make_config", "ic"]
+__all__ = ["Ps3dGpu", "Ps3dError", "batch_advance", "make_config", "ic"]

@@ -167,12 +167,13 @@ void op_mean_fix(const Dims &d, cudaStream_t st, double *svor, const double *dst
                  const double *ini, double *savg_out, int apply, float *svor32 = nullptr);
 // mixed-form stage updates (FP64 state, FP32 source, state copy and
 // accumulated source increments acc)
+// (dtp: the step's dt in device memory; full: the third stage's full-step factor)
 void op_rk4m_sub1(const Dims &d, cudaStream_t st, double *q, double *qdi, float *acc, const float *sqs, float *q32,
-                  const double *filt0, const double *emq, double dt2, double dt6);
+                  const double *filt0, const double *emq, const double *dtp);
 void op_rk4m_sub23(const Dims &d, cudaStream_t st, double *q, const double *qdi, float *acc, const float *sqs,
-                   float *q32, const double *epq, const double *emq, double c1, double dt3);
+                   float *q32, const double *epq, const double *emq, const double *dtp, bool full);
 void op_rk4m_sub4(const Dims &d, cudaStream_t st, double *q, const double *qdi, const float *acc, const float *sqs,
-                  float *q32, const double *epq, const double *emq, double dt6);
+                  float *q32, const double *epq, const double *emq, const double *dtp);
 void op_narrow(cudaStream_t st, const double *in, float *out, long long n);
 // host-layout (nz+1)-pitched FP64 columns <-> device P-pitched columns
 void op_unpack_cols(const Dims &d, cudaStream_t st, const double *src, double *dst, int ncomp, int *changed);
@@ -186,8 +187,10 @@ struct RedOut {
 template <typename T>
 void red_pass1(const Dims &d, cudaStream_t st, const T *vel, const T *vor, double *part, double *result);
 template <typename T>
+// vortrms from the pass-1 results on the device when res1 is given:
+// sqrt(res1[1] / ncell)
 void red_pass2(const Dims &d, cudaStream_t st, const T *vor, const T *g5, double vortrms, double *part,
-               double *result, int *flag);
+               double *result, int *flag, const double *res1 = nullptr, double ncell = 1.0);
 int red_nblocks(const Dims &d);
 constexpr int RED1_N = 12;  // values of pass 1
 constexpr int RED2_N = 5;   // values of pass 2

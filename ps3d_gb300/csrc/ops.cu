@@ -558,9 +558,10 @@ void op_rk4_sub4(const Dims &d, cudaStream_t st, double *q, const double *qdf, c
 // written back: the next source evaluation overwrites it.
 __global__ void k_rk4m_sub1(Dims d, double *__restrict__ q, double *__restrict__ qdi, float *__restrict__ acc,
                             const float *__restrict__ sqs, float *__restrict__ q32, const double *__restrict__ filt0,
-                            const double *__restrict__ emq, double dt2, double dt6)
+                            const double *__restrict__ emq, const double *__restrict__ dtp)
 {
     COLUMN_HEADER
+    const double dt = *dtp, dt2 = 0.5 * dt, dt6 = dt / 6.0;
     const double m = emq[col];
     const float f0 = (float)filt0[col];
     const float c2 = (float)(dt2 * m), c6 = (float)dt6;
@@ -577,9 +578,11 @@ __global__ void k_rk4m_sub1(Dims d, double *__restrict__ q, double *__restrict__
 }
 __global__ void k_rk4m_sub23(Dims d, double *__restrict__ q, const double *__restrict__ qdi,
                              float *__restrict__ acc, const float *__restrict__ sqs, float *__restrict__ q32,
-                             const double *__restrict__ epq, const double *__restrict__ emq, double c1, double dt3)
+                             const double *__restrict__ epq, const double *__restrict__ emq,
+                             const double *__restrict__ dtp, int full)
 {
     COLUMN_HEADER
+    const double dt = *dtp, c1 = full ? dt : 0.5 * dt, dt3 = dt / 3.0;
     const double m = emq[col];
     const float pp = (float)epq[col];
     const float cq = (float)(c1 * m), c3 = (float)dt3;
@@ -594,9 +597,11 @@ __global__ void k_rk4m_sub23(Dims d, double *__restrict__ q, const double *__res
 }
 __global__ void k_rk4m_sub4(Dims d, double *__restrict__ q, const double *__restrict__ qdi,
                             const float *__restrict__ acc, const float *__restrict__ sqs, float *__restrict__ q32,
-                            const double *__restrict__ epq, const double *__restrict__ emq, double dt6)
+                            const double *__restrict__ epq, const double *__restrict__ emq,
+                            const double *__restrict__ dtp)
 {
     COLUMN_HEADER
+    const double dt6 = *dtp / 6.0;
     const double m = emq[col];
     const float mf = (float)m, c = (float)(dt6 * epq[col] * m);
     for (int iz = threadIdx.x; iz <= d.nz; iz += 32) {
@@ -607,19 +612,19 @@ __global__ void k_rk4m_sub4(Dims d, double *__restrict__ q, const double *__rest
     }
 }
 void op_rk4m_sub1(const Dims &d, cudaStream_t st, double *q, double *qdi, float *acc, const float *sqs, float *q32,
-                  const double *filt0, const double *emq, double dt2, double dt6)
+                  const double *filt0, const double *emq, const double *dtp)
 {
-    k_rk4m_sub1<<<col_grid(d), COL_BLOCK, 0, st>>>(d, q, qdi, acc, sqs, q32, filt0, emq, dt2, dt6);
+    k_rk4m_sub1<<<col_grid(d), COL_BLOCK, 0, st>>>(d, q, qdi, acc, sqs, q32, filt0, emq, dtp);
 }
 void op_rk4m_sub23(const Dims &d, cudaStream_t st, double *q, const double *qdi, float *acc, const float *sqs,
-                   float *q32, const double *epq, const double *emq, double c1, double dt3)
+                   float *q32, const double *epq, const double *emq, const double *dtp, bool full)
 {
-    k_rk4m_sub23<<<col_grid(d), COL_BLOCK, 0, st>>>(d, q, qdi, acc, sqs, q32, epq, emq, c1, dt3);
+    k_rk4m_sub23<<<col_grid(d), COL_BLOCK, 0, st>>>(d, q, qdi, acc, sqs, q32, epq, emq, dtp, full ? 1 : 0);
 }
 void op_rk4m_sub4(const Dims &d, cudaStream_t st, double *q, const double *qdi, const float *acc, const float *sqs,
-                  float *q32, const double *epq, const double *emq, double dt6)
+                  float *q32, const double *epq, const double *emq, const double *dtp)
 {
-    k_rk4m_sub4<<<col_grid(d), COL_BLOCK, 0, st>>>(d, q, qdi, acc, sqs, q32, epq, emq, dt6);
+    k_rk4m_sub4<<<col_grid(d), COL_BLOCK, 0, st>>>(d, q, qdi, acc, sqs, q32, epq, emq, dtp);
 }
 
 // Host-layout state (nz+1 values per column, the three components one after
@@ -1031,10 +1036,12 @@ template <> struct StrainMax<float> {
 // 501-545), 2 ggmax, 3 usggmax, 4 lsggmax (advance.f90:222-276)
 template <typename T>
 __global__ void k_red2(Dims d, const T *__restrict__ vor, const T *__restrict__ g5, double vortrms,
-                       double *part, int *flag)
+                       const double *__restrict__ res1, double ncell, double *part, int *flag)
 {
     const long long N = d.nfield;
-    const T vr = (T)vortrms;
+    // the characteristic-vorticity threshold from the pass-1 results when
+    // they stay on the device (sqrt(sum w^2 / ncell), as the host computes)
+    const T vr = (T)(res1 ? sqrt(res1[1] / ncell) : vortrms);
     Acc<T> l1, l2;
     T gg = sizeof(T) == 8 ? (T)DBL_EPSILON : (T)FLT_EPSILON, us = 0, ls = 0;
     int hit = 0;
@@ -1070,10 +1077,10 @@ __global__ void k_red2(Dims d, const T *__restrict__ vor, const T *__restrict__ 
 
 template <typename T>
 void red_pass2(const Dims &d, cudaStream_t st, const T *vor, const T *g5, double vortrms, double *part,
-               double *result, int *flag)
+               double *result, int *flag, const double *res1, double ncell)
 {
     const int nb = red_grid(d, k_red2<T>);
-    k_red2<T><<<nb, COL_BLOCK, 0, st>>>(d, vor, g5, vortrms, part, flag);
+    k_red2<T><<<nb, COL_BLOCK, 0, st>>>(d, vor, g5, vortrms, res1, ncell, part, flag);
     int *kinds;
     cudaGetSymbolAddress((void **)&kinds, c_kinds2);
     k_finish<RED2_N><<<1, dim3(32, RED2_N), 0, st>>>(part, nb, kinds, result);
@@ -1165,7 +1172,7 @@ void op_hyperbolic_tables(const Dims &d, cudaStream_t st, const double *k2l2, co
                                    const double *, const double *, const double *, double);                    \
     template void red_pass1<T>(const Dims &, cudaStream_t, const T *, const T *, double *, double *);         \
     template void red_pass2<T>(const Dims &, cudaStream_t, const T *, const T *, double, double *, double *,  \
-                               int *);                                                                         \
+                               int *, const double *, double);                                                 \
     template void op_hyperbolic_tables<T>(const Dims &, cudaStream_t, const double *, const double *,         \
                                           const double *, const double *, const double *, double, T *, T *,   \
                                           T *, T *, T *, T *, T *);

@@ -55,6 +55,19 @@ struct Rolling {
     }
 };
 
+// Per-step scalars in device memory.  The mixed stage kernels read dt here;
+// in a captured step (CUDA graph) adapt's scalar logic also runs on the
+// device and leaves the step's diagnostics here.
+struct StepScal {
+    double dt;         // time step of the current step
+    double t;          // model time at the start of the next step
+    double dfac;       // diffusion factor of vdiss (impl-diff-rk4: pref dt / 2)
+    double diag[20];   // ps3d_gpu_diag of the last step, field by field
+    double sma;        // rolling mean of the strain maximum (rolling_mean.f90)
+    int inew, iold, filled;
+    int err;           // 1 non-finite diagnostic, 2 Jacobi sweep limit
+};
+
 }  // namespace
 
 struct ps3d_gpu_ctx {
@@ -103,6 +116,11 @@ struct ps3d_gpu_ctx {
     double ini_vor_mean[2] = {0.0, 0.0};
     Rolling roll;
     Probe probe;
+    // device-side step scalars, rolling-mean history, captured step
+    StepScal *sc = nullptr;
+    double *roll_dev = nullptr;
+    cudaGraphExec_t graph = nullptr;
+    long long graph_launches = 0;  // kernels per captured step
 
     Deriv D() const { return Deriv{cx, cy}; }
     Tables tables() const
@@ -563,12 +581,21 @@ template <typename T> int rhs_or_hold(ps3d_gpu_ctx *c)
 }
 
 // impl_rk4_step (impl_rk4.f90:76-207)
+__global__ void k_set_dt(StepScal *sc, double dt) { sc->dt = dt; }
+
+// t == nullptr: a device-driven step (dt already in c->sc, the time kept on
+// the device); only the mixed form runs that way
 template <typename T> int step_rk4(ps3d_gpu_ctx *c, double *t, double dt)
 {
     const Dims &d = c->d;
     const long long N = d.nfield;
     const double dt2 = 0.5 * dt, dt3 = dt / 3.0, dt6 = dt / 6.0;
     T *sv = tf<T>(c->svorts);
+    const double *dtp = &c->sc->dt;
+    if (sizeof(T) == sizeof(float) && t) {
+        k_set_dt<<<1, 1, 0, c->st>>>(c->sc, dt);
+        c->launches += 1;
+    }
     if (c->cfg.hold_source)
         cudaMemcpyAsync(c->held, c->svorts, 3 * N * sizeof(T), cudaMemcpyDeviceToDevice, c->st);
     op_rk4_factors(d, c->st, c->vdiss, c->filt0, c->epq, c->emq, c->epq2, c->emq2);
@@ -580,7 +607,7 @@ template <typename T> int step_rk4(ps3d_gpu_ctx *c, double *t, double dt)
     for (int k = 0; k < 3; ++k) {
         if (mixed)
             op_rk4m_sub1(d, c->st, c->svor + k * N, c->svori + k * N, acc + k * N, s32 + k * N, q32 + k * N,
-                         c->filt0, c->emq, dt2, dt6);
+                         c->filt0, c->emq, dtp);
         else
             op_rk4_sub1<T>(d, c->st, c->svor + k * N, c->svori + k * N, c->svorf + k * N, sv + k * N, c->filt0,
                            c->emq, dt2, dt6);
@@ -588,11 +615,11 @@ template <typename T> int step_rk4(ps3d_gpu_ctx *c, double *t, double dt)
     c->launches += 3;
     int rc = rhs_or_hold<T>(c);
     if (rc) return rc;
-    *t += dt2;
+    if (t) *t += dt2;
     for (int k = 0; k < 3; ++k) {
         if (mixed)
             op_rk4m_sub23(d, c->st, c->svor + k * N, c->svori + k * N, acc + k * N, s32 + k * N, q32 + k * N,
-                          c->epq, c->emq, dt2, dt3);
+                          c->epq, c->emq, dtp, false);
         else
             op_rk4_sub23<T>(d, c->st, c->svor + k * N, c->svori + k * N, c->svorf + k * N, sv + k * N, c->epq,
                             c->emq, dt2, dt3);
@@ -600,11 +627,11 @@ template <typename T> int step_rk4(ps3d_gpu_ctx *c, double *t, double dt)
     c->launches += 3;
     rc = rhs_or_hold<T>(c);
     if (rc) return rc;
-    *t += dt2;
+    if (t) *t += dt2;
     for (int k = 0; k < 3; ++k) {
         if (mixed)
             op_rk4m_sub23(d, c->st, c->svor + k * N, c->svori + k * N, acc + k * N, s32 + k * N, q32 + k * N,
-                          c->epq, c->emq2, dt, dt3);
+                          c->epq, c->emq2, dtp, true);
         else
             op_rk4_sub23<T>(d, c->st, c->svor + k * N, c->svori + k * N, c->svorf + k * N, sv + k * N, c->epq,
                             c->emq2, dt, dt3);
@@ -615,7 +642,7 @@ template <typename T> int step_rk4(ps3d_gpu_ctx *c, double *t, double dt)
     for (int k = 0; k < 3; ++k) {
         if (mixed)
             op_rk4m_sub4(d, c->st, c->svor + k * N, c->svori + k * N, acc + k * N, s32 + k * N, q32 + k * N,
-                         c->epq2, c->emq2, dt6);
+                         c->epq2, c->emq2, dtp);
         else
             op_rk4_sub4<T>(d, c->st, c->svor + k * N, c->svorf + k * N, sv + k * N, c->epq2, c->emq2, dt6);
     }
@@ -670,6 +697,209 @@ template <typename T> int advance(ps3d_gpu_ctx *c, double *t, ps3d_gpu_diag *dia
     rc = source<T>(c);
     if (rc) return rc;
     return step<T>(c, t, dt);
+}
+
+// ------------------------------------------------- device-driven step
+// adapt's scalar logic (advance.f90:109-377, rolling_mean.f90:36-69) on the
+// device, one thread, the same operations in the same order as the host
+// version in adapt<T>; results stay in c->sc for the stage kernels.
+struct AdaptParams {
+    double cflmax, alpha, time_limit, dx0, dx1, dx2, ncell, ncelli;
+    int pretype, L;
+};
+
+__global__ void k_adapt_scalars(StepScal *sc, double *hist, const double *__restrict__ r1,
+                                const double *__restrict__ r2, const int *__restrict__ flag, AdaptParams p)
+{
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    const double t = sc->t;
+    const double small = 1.0e-12;
+    const double vortmax = sqrt(r1[0]);
+    const double vortrms = sqrt(r1[1] / p.ncell);
+    const double vorch = r2[1] / (small + r2[0]);
+    const double ggmax = r2[2], usggmax = r2[3], lsggmax = r2[4];
+    const double umax = r1[7], vmax = r1[8], wmax = r1[9];
+    const double bfmax = 0.0;
+    const double dtcfl =
+        p.cflmax * fmin(fmin(p.dx0 / (umax + small), p.dx1 / (vmax + small)), p.dx2 / (wmax + small));
+    const double dt = fmin(fmin(p.alpha / (ggmax + small), p.alpha / (bfmax + small)), fmin(dtcfl, p.time_limit - t));
+    double sma;
+    const int L = p.L;
+    if (sc->filled) {
+        const double vold = hist[sc->iold - 1];
+        sc->iold = sc->iold % L + 1;
+        sma = sc->sma + (ggmax - vold) / (double)L;
+        hist[sc->inew - 1] = ggmax;
+        sc->inew = sc->inew % L + 1;
+    } else {
+        hist[sc->inew - 1] = ggmax;
+        double sum = 0.0;
+        for (int i = 0; i < sc->inew; ++i) sum += hist[i];
+        sma = sum / (double)sc->inew;
+        sc->filled = (L == sc->inew);
+        sc->inew = sc->inew % L + 1;
+    }
+    sc->sma = sma;
+    double val;
+    switch (p.pretype) {
+    case PS3D_PRE_CONSTANT: val = 1.0; break;
+    case PS3D_PRE_VORCH: val = vorch; break;
+    case PS3D_PRE_BFMAX: val = bfmax; break;
+    case PS3D_PRE_MAX_STRAIN: val = ggmax; break;
+    case PS3D_PRE_US_MAX_STRAIN: val = usggmax; break;
+    default: val = sma; break;
+    }
+    if (*flag) sc->err |= 2;
+    if (!isfinite(dt) || !isfinite(r1[1]) || !isfinite(r1[2])) sc->err |= 1;
+    sc->dt = dt;
+    sc->dfac = 0.5 * val * dt;  // impl_rk4_set_diffusion (impl_rk4.f90:37-53)
+    double *g = sc->diag;
+    g[0] = t;
+    g[1] = dt;
+    g[2] = 0.5 * r1[2] * p.ncelli;
+    g[3] = 0.5 * r1[1] * p.ncelli;
+    g[4] = r1[3] * p.ncelli;
+    g[5] = vortmax;
+    g[6] = vortrms;
+    g[7] = vorch;
+    for (int k = 0; k < 3; ++k) g[8 + k] = r1[4 + k] * p.ncelli;
+    g[11] = ggmax;
+    g[12] = usggmax;
+    g[13] = lsggmax;
+    g[14] = umax;
+    g[15] = vmax;
+    g[16] = wmax;
+    g[17] = bfmax;
+    g[18] = sma;
+    g[19] = val;
+    // the stepper advances t by dt/2 twice (impl_rk4.f90)
+    const double dt2 = 0.5 * dt;
+    sc->t = (t + dt2) + dt2;
+}
+
+__global__ void k_vdiss_dev(long long n, const double *vhdis, double *vdiss, const StepScal *sc)
+{
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    vdiss[i] = sc->dfac * vhdis[i];
+}
+
+// One advance of the mixed form with impl-diff-rk4 and no host
+// synchronisation: what a CUDA graph captures.
+int advance_dev(ps3d_gpu_ctx *c)
+{
+    const Dims &d = c->d;
+    const long long N = d.nfield;
+    int rc = vor2vel<float>(c);
+    if (rc) return rc;
+    red_pass1<float>(d, c->st, tf<float>(c->vel), tf<float>(c->vor), c->part, c->res1);
+    float *g5 = tmpf<float>(c, 0);
+    op_strain_fields<float>(d, c->st, c->D(), tf<float>(c->svel), g5);
+    c->launches += 3;
+    for (int k = 0; k < 5; ++k) xyi<float>(c, g5 + k * N, g5 + k * N);
+    cudaMemsetAsync(c->flag, 0, sizeof(int), c->st);
+    red_pass2<float>(d, c->st, tf<float>(c->vor), g5, 0.0, c->part, c->res2, c->flag, c->res1, (double)c->ncell);
+    c->launches += 2;
+    AdaptParams ap;
+    ap.cflmax = c->cfg.cflmax;
+    ap.alpha = c->cfg.alpha;
+    ap.time_limit = c->cfg.time_limit;
+    ap.dx0 = c->dx[0];
+    ap.dx1 = c->dx[1];
+    ap.dx2 = c->dx[2];
+    ap.ncell = (double)c->ncell;
+    ap.ncelli = c->ncelli;
+    ap.pretype = c->cfg.pretype;
+    ap.L = (int)c->roll.hist.size();
+    k_adapt_scalars<<<1, 1, 0, c->st>>>(c->sc, c->roll_dev, c->res1, c->res2, c->flag, ap);
+    k_vdiss_dev<<<(unsigned)((d.ncol + 255) / 256), 256, 0, c->st>>>(d.ncol, c->vhdis, c->vdiss, c->sc);
+    c->launches += 2;
+    rc = source<float>(c);
+    if (rc) return rc;
+    return step_rk4<float>(c, nullptr, 0.0);
+}
+
+int graph_supported(ps3d_gpu_ctx *c)
+{
+    if (c->fp64 || c->cfg.stepper == PS3D_CN2 || c->cfg.hold_source)
+        return fail(c, PS3D_ERR_INVALID_ARG, "captured steps need the mixed form, impl-diff-rk4, no held source");
+    if (!c->diffusion_ready) return fail(c, PS3D_ERR_NOT_READY, "advance before init_diffusion");
+    return PS3D_OK;
+}
+
+// upload the model time and the rolling-mean state; capture the step once
+int graph_prepare(ps3d_gpu_ctx *c, double t)
+{
+    int rc = graph_supported(c);
+    if (rc) return rc;
+    StepScal h{};
+    h.t = t;
+    h.sma = c->roll.sma;
+    h.inew = c->roll.inew;
+    h.iold = c->roll.iold;
+    h.filled = c->roll.filled ? 1 : 0;
+    cudaMemcpyAsync(c->sc, &h, sizeof(h), cudaMemcpyHostToDevice, c->st);
+    cudaMemcpyAsync(c->roll_dev, c->roll.hist.data(), c->roll.hist.size() * sizeof(double),
+                    cudaMemcpyHostToDevice, c->st);
+    rc = sync_check(c, "graph_prepare");
+    if (rc) return rc;
+    if (c->graph) return PS3D_OK;
+    const int kind = c->probe.kind;
+    c->probe.kind = PROBE_OFF;  // no event records inside the graph
+    cudaGraph_t g = nullptr;
+    if (cudaStreamBeginCapture(c->st, cudaStreamCaptureModeThreadLocal) != cudaSuccess) {
+        c->probe.kind = kind;
+        return check(c, "graph capture");
+    }
+    const long long l0 = c->launches;
+    rc = advance_dev(c);
+    const cudaError_t e = cudaStreamEndCapture(c->st, &g);
+    c->probe.kind = kind;
+    if (rc || e != cudaSuccess) {
+        if (g) cudaGraphDestroy(g);
+        cudaGetLastError();
+        return rc ? rc : fail(c, PS3D_ERR_CUDA, std::string("graph capture: ") + cudaGetErrorString(e));
+    }
+    c->graph_launches = c->launches - l0;
+    c->launches = l0;
+    const cudaError_t ei = cudaGraphInstantiate(&c->graph, g, 0);
+    cudaGraphDestroy(g);
+    if (ei != cudaSuccess) {
+        c->graph = nullptr;
+        return fail(c, PS3D_ERR_CUDA, std::string("graph instantiate: ") + cudaGetErrorString(ei));
+    }
+    return PS3D_OK;
+}
+
+int graph_launch(ps3d_gpu_ctx *c, int nsteps)
+{
+    for (int s = 0; s < nsteps; ++s)
+        if (cudaGraphLaunch(c->graph, c->st) != cudaSuccess) return check(c, "graph launch");
+    c->launches += c->graph_launches * nsteps;
+    return PS3D_OK;
+}
+
+// read back the time, the last step's diagnostics and the rolling state
+int graph_finish(ps3d_gpu_ctx *c, double *t, ps3d_gpu_diag *diag)
+{
+    StepScal h;
+    cudaMemcpyAsync(&h, c->sc, sizeof(h), cudaMemcpyDeviceToHost, c->st);
+    cudaMemcpyAsync(c->roll.hist.data(), c->roll_dev, c->roll.hist.size() * sizeof(double),
+                    cudaMemcpyDeviceToHost, c->st);
+    int rc = sync_check(c, "graph_finish");
+    if (rc) return rc;
+    c->roll.sma = h.sma;
+    c->roll.inew = h.inew;
+    c->roll.iold = h.iold;
+    c->roll.filled = h.filled != 0;
+    *t = h.t;
+    if (diag) {
+        static_assert(sizeof(ps3d_gpu_diag) == 20 * sizeof(double), "diag layout");
+        memcpy(diag, h.diag, sizeof(h.diag));
+    }
+    if (h.err & 2) return fail(c, PS3D_ERR_DEVICE_LIMIT, "adapt: Jacobi sweep limit reached");
+    if (h.err & 1) return fail(c, PS3D_ERR_NONFINITE, "adapt: non-finite diagnostic");
+    return PS3D_OK;
 }
 
 // setup_fields (utils.f90:136-184)
@@ -906,7 +1136,8 @@ template <typename T> int allocate_fields(ps3d_gpu_ctx *c)
          dalloc(c, &c->ini, 2 * sizeof(double)) && dalloc(c, &c->savg, 2 * sizeof(double)) &&
          dalloc(c, &c->part, (size_t)red_nblocks(d) * RED1_N * sizeof(double)) &&
          dalloc(c, &c->res1, RED1_N * sizeof(double)) && dalloc(c, &c->res2, RED2_N * sizeof(double)) &&
-         dalloc(c, &c->flag, sizeof(int));
+         dalloc(c, &c->flag, sizeof(int)) && dalloc(c, &c->sc, sizeof(StepScal)) &&
+         dalloc(c, &c->roll_dev, c->roll.hist.size() * sizeof(double));
     if (!ok) return fail(c, PS3D_ERR_OUT_OF_MEMORY, "device allocation failed");
     twiddles<T>(c, c->twx, d.nx);
     twiddles<T>(c, c->twy, d.ny);
@@ -1047,6 +1278,7 @@ int ps3d_gpu_destroy(ps3d_gpu_ctx *c)
     if (!c) return PS3D_OK;
     cudaSetDevice(c->cfg.device);
     if (c->st) cudaStreamSynchronize(c->st);
+    if (c->graph) cudaGraphExecDestroy(c->graph);
     for (void *p : c->allocs) cudaFree(p);
     if (c->probe.ev) {
         for (int i = 0; i < 2 * Probe::MAXP; ++i) cudaEventDestroy(c->probe.ev[i]);
@@ -1344,6 +1576,68 @@ int ps3d_gpu_time_advance(ps3d_gpu_ctx *c, double *t, int nsteps, double *ms)
     cudaEventElapsedTime(&f, c->ev0, c->ev1);
     *ms = (double)f;
     return PS3D_OK;
+}
+
+int ps3d_gpu_advance_graph(ps3d_gpu_ctx *c, double *t, int nsteps, ps3d_gpu_diag *diag, double *ms)
+{
+    int rc = enter(c);
+    if (rc) return rc;
+    if (!t || nsteps < 0) return PS3D_ERR_INVALID_ARG;
+    rc = graph_prepare(c, *t);
+    if (rc) return rc;
+    cudaEventRecord(c->ev0, c->st);
+    rc = graph_launch(c, nsteps);
+    if (rc) return rc;
+    cudaEventRecord(c->ev1, c->st);
+    rc = graph_finish(c, t, diag);
+    if (ms) {
+        float f = 0.0f;
+        cudaEventElapsedTime(&f, c->ev0, c->ev1);
+        *ms = (double)f;
+    }
+    return rc;
+}
+
+int ps3d_gpu_batch_advance(ps3d_gpu_ctx *const *ctx, int n, double *t, int nsteps, double *ms)
+{
+    if (!ctx || !t || n <= 0 || nsteps < 0) return PS3D_ERR_INVALID_ARG;
+    for (int i = 0; i < n; ++i)
+        if (!ctx[i] || ctx[i]->cfg.device != ctx[0]->cfg.device) return PS3D_ERR_INVALID_ARG;
+    int rc = enter(ctx[0]);
+    if (rc) return rc;
+    for (int i = 0; i < n; ++i) {
+        rc = graph_prepare(ctx[i], t[i]);
+        if (rc) return rc;
+    }
+    // every run's step is one graph on its own stream; the streams start
+    // together after one event and the elapsed time ends when the last one
+    // has finished
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    cudaStream_t s0 = ctx[0]->st;
+    cudaEventRecord(e0, s0);
+    for (int i = 1; i < n; ++i) cudaStreamWaitEvent(ctx[i]->st, e0, 0);
+    for (int s = 0; s < nsteps && !rc; ++s)
+        for (int i = 0; i < n && !rc; ++i) rc = graph_launch(ctx[i], 1);
+    for (int i = 1; i < n; ++i) {
+        cudaEventRecord(ctx[i]->ev1, ctx[i]->st);
+        cudaStreamWaitEvent(s0, ctx[i]->ev1, 0);
+    }
+    cudaEventRecord(e1, s0);
+    int rf = PS3D_OK;
+    for (int i = 0; i < n; ++i) {
+        const int r = graph_finish(ctx[i], &t[i], nullptr);
+        if (r && !rf) rf = r;
+    }
+    if (ms) {
+        float f = 0.0f;
+        cudaEventElapsedTime(&f, e0, e1);
+        *ms = (double)f;
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    return rc ? rc : rf;
 }
 
 int ps3d_gpu_probe(ps3d_gpu_ctx *c, int kind)

@@ -82,3 +82,55 @@ def beltrami_plus_perturbation(nx, ny, nz, seed=0, amplitude=1.0e-3, lower=None,
     rms = float(np.sqrt(np.mean(np.sum(vor * vor, axis=0))))
     pert = perturbation(nx, ny, nz, extent, seed, amplitude, rms)
     return vor, pert
+
+
+def beltrami_plus_perturbation_slabs(nx, ny, nz, seed=0, amplitude=1.0e-3, lower=None, extent=None):
+    """Memory-lean variant for very large grids (1024^3: 26 GB per vector
+    field): the same Beltrami field and the same perturbation recipe, built
+    one x-slab at a time.  The Gaussian coefficients of slab ix come from
+    PCG64 seeded with (seed, ix), so for a given seed the field differs from
+    `beltrami_plus_perturbation`'s; host memory is the two output arrays plus
+    one slab."""
+    lower = BASELINE_BOX["lower"] if lower is None else lower
+    extent = BASELINE_BOX["extent"] if extent is None else extent
+    vor = np.empty((3, nx, ny, nz + 1))
+    kk, ll, mm = 2.0, 2.0, 1.0
+    alpha = np.sqrt(kk ** 2 + ll ** 2 + mm ** 2)
+    fk2l2 = alpha / (kk * kk + ll * ll)
+    dx = np.array(extent, dtype=np.float64) / np.array([nx, ny, nz], dtype=np.float64)
+    y = lower[1] + dx[1] * np.arange(ny, dtype=np.float64)
+    z = lower[2] + dx[2] * np.arange(nz + 1, dtype=np.float64)
+    cosmz, sinmz = np.cos(mm * z), np.sin(mm * z)
+    g = (fk2l2 * (kk * mm * sinmz - ll * alpha * cosmz), fk2l2 * (ll * mm * sinmz + kk * alpha * cosmz),
+         alpha * cosmz)
+    sq = 0.0
+    for ix in range(nx):
+        phase = kk * (lower[0] + dx[0] * ix) + ll * y
+        s, c = np.sin(phase), np.cos(phase)
+        vor[0, ix] = s[:, None] * g[0][None, :]
+        vor[1, ix] = s[:, None] * g[1][None, :]
+        vor[2, ix] = c[:, None] * g[2][None, :]
+        sq += float(np.sum(vor[:, ix] * vor[:, ix]))
+    rms = np.sqrt(sq / (nx * ny * (nz + 1)))
+    rkx, rky, rkz = wavenumbers(nx, ny, nz, extent)
+    wy = np.full(ny, 2.0); wy[0] = 1.0; wy[ny // 2] = 1.0
+    pert = np.empty((3, nx, ny, nz + 1))
+    ms = 0.0
+    for ix in range(nx):
+        K2 = rkx[ix] ** 2 + rky[:, None] ** 2 + rkz[None, :] ** 2
+        env = np.zeros_like(K2)
+        np.divide(1.0, K2, out=env, where=K2 > 0)
+        env[:, 0] = 0.0
+        env[:, nz] = 0.0
+        env[ny // 2, :] = 0.0
+        if ix == nx // 2:
+            env[:] = 0.0
+        rng = np.random.Generator(np.random.PCG64([seed, ix]))
+        pert[:, ix] = rng.standard_normal((3, ny, nz + 1)) * env[None]
+        wx = 1.0 if ix in (0, nx // 2) else 2.0
+        ms += wx * float(np.sum(wy[None, :, None] * pert[:, ix] * pert[:, ix]))
+    ms /= nx * ny * (nz + 1)
+    scale = amplitude * rms / np.sqrt(ms) if ms > 0 else 0.0
+    for ix in range(nx):
+        pert[:, ix] *= scale
+    return vor, pert

@@ -231,6 +231,17 @@ class Ps3dGpu:
         self._chk(self.L.ps3d_gpu_time_advance(self._h, ctypes.byref(tt), nsteps, ctypes.byref(ms)))
         return tt.value, ms.value
 
+    def advance_graph(self, t, nsteps):
+        """nsteps captured advances (mixed form, impl-diff-rk4): one CUDA graph
+        launch per step, adapt's scalars on the device.  Returns (t, diag of
+        the last step, device ms)."""
+        tt = ctypes.c_double(t)
+        ms = ctypes.c_double()
+        d = _lib.Diag()
+        self._chk(self.L.ps3d_gpu_advance_graph(self._h, ctypes.byref(tt), nsteps, ctypes.byref(d),
+                                                ctypes.byref(ms)))
+        return tt.value, d.as_dict(), ms.value
+
     def energy_series(self):
         a, b, c = ctypes.c_double(), ctypes.c_double(), ctypes.c_double()
         self._chk(self.L.ps3d_gpu_energy_series(self._h, ctypes.byref(a), ctypes.byref(b), ctypes.byref(c)))
@@ -256,3 +267,19 @@ class Ps3dGpu:
 
     def synchronize(self):
         self._chk(self.L.ps3d_gpu_synchronize(self._h))
+
+
+def batch_advance(models, ts, nsteps):
+    """Advance independent runs (Ps3dGpu objects, any sizes, one device) by
+    nsteps captured steps, their graphs interleaved on their own streams.
+    Returns (list of times, device ms of the batch)."""
+    n = len(models)
+    hs = (ctypes.c_void_p * n)(*[m._h.value for m in models])
+    tt = (ctypes.c_double * n)(*ts)
+    ms = ctypes.c_double()
+    L = models[0].L
+    rc = L.ps3d_gpu_batch_advance(hs, n, tt, nsteps, ctypes.byref(ms))
+    if rc:
+        msgs = [L.ps3d_gpu_last_error(m._h).decode() for m in models]
+        raise Ps3dError(rc, " | ".join(x for x in msgs if x))
+    return list(tt), ms.value
