@@ -12,6 +12,10 @@ struct Dims {
     int P;                // padded column pitch (>= nz+1, multiple of 8)
     long long ncol;       // nx*ny
     long long nfield;     // P*ny*nx elements per scalar field
+    // FP32 line-FFT block shape per pass, picked by the autotuner:
+    // [0] forward y, [1] forward x, [2] inverse y, [3] inverse x;
+    // -1 = the default shape of the line length
+    signed char line_shape[4] = {-1, -1, -1, -1};
 };
 
 enum { COL_DST = 0, COL_DCT = 1, COL_DECOMP = 2, COL_COMBINE = 3 };
@@ -60,8 +64,12 @@ void columns(const Dims &d, cudaStream_t st, int mode, const T *in, T *out, cons
 // FP32 bandwidth-tuned line FFTs (lines32.cu), n = 64..1024
 bool lines32_supported(int n);
 void lines32_init();
+// shape: -1 default, 0 512-thread blocks (two per SM), 1 256-thread blocks
+// (three per SM); the two differ only at n = 512
 void launch_lines32(cudaStream_t st, const float *in, float *out, int n, int P, long long line_stride,
-                    long long nbatch, long long batch_stride, bool inverse, const float2 *tw);
+                    long long nbatch, long long batch_stride, bool inverse, const float2 *tw, int shape = -1);
+// number of block shapes the autotuner can choose from at line length n
+int lines32_shapes(int n);
 // FP32 half-length warp z transforms (colz.cu), nz = 64..1024
 bool colz_supported(int nz);
 void colz_init();

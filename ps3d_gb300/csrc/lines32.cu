@@ -24,15 +24,17 @@ namespace {
 constexpr int LANES = 16;  // complex lanes per block
 constexpr int PAIRS = 8;   // threads per row (two lanes each)
 
-template <int N, bool INV> struct LinePlan {
-    // threads per block: 512 for the forward transform at N >= 512; the
-    // inverse runs 256-thread blocks there (more registers per thread for
-    // its Hermitian first pass)
-    static constexpr int T = (N >= 1024 || (N >= 512 && !INV)) ? 512 : 256;
-    static constexpr int G = T / PAIRS;  // butterfly groups
-    // resident blocks per SM: N * 128 bytes of shared memory each, and the
-    // register file shared by T * MINB threads
-    static constexpr int MINB = N >= 1024 ? 1 : (N >= 512 ? (INV ? 3 : 2) : 3);
+// Block shape W at N = 512: 0 = 512-thread blocks, two per SM (64
+// registers); 1 = 256-thread blocks, three per SM (85 registers).  The
+// autotuner picks one per pass; by default the forward transform takes 0
+// and the inverse (its Hermitian first pass needs more registers) takes 1.
+// N = 1024 always runs one 512-thread block per SM (128 KB of shared
+// memory), N <= 256 three 256-thread blocks.
+template <int N, bool INV, int W> struct LinePlan {
+    static constexpr bool BIG = N >= 1024 || (N == 512 && W == 0);
+    static constexpr int T = BIG ? 512 : 256;  // threads per block
+    static constexpr int G = T / PAIRS;        // butterfly groups
+    static constexpr int MINB = N >= 1024 ? 1 : (BIG ? 2 : 3);
 };
 
 __device__ __forceinline__ float2 cm(float2 a, float2 b)
@@ -48,11 +50,11 @@ template <int R, bool INV> __device__ __forceinline__ void dftR(float2 *v) { dft
 // one radix-R Stockham pass with span NS over N points: inputs x[j + r N/R]
 // of butterfly j, outputs at (j - k) R + k + r NS, k = j mod NS; each thread
 // applies it to its two lanes
-template <int N, int R, int NS, bool INV, bool FROM_GLOBAL, bool TO_GLOBAL>
+template <int N, int R, int NS, bool INV, int W, bool FROM_GLOBAL, bool TO_GLOBAL>
 __device__ __forceinline__ void pass(float4 *sm, const float4 *__restrict__ gin, float4 *__restrict__ gout,
                                      long long gstride, bool valid, float scale, const float2 *__restrict__ tw)
 {
-    constexpr int G = LinePlan<N, INV>::G;
+    constexpr int G = LinePlan<N, INV, W>::G;
     constexpr int NB = N / R;              // butterflies per lane
     constexpr int NBT = (NB + G - 1) / G;  // per thread
     const int p = threadIdx.x & (PAIRS - 1), g = threadIdx.x / PAIRS;
@@ -116,11 +118,11 @@ __device__ __forceinline__ float2 herm_high(float2 lo, float2 hi) { return make_
 // butterflies (slot s: s and N/8 - s; slot 0: butterflies 0 and N/16, each
 // its own mirror) for one lane, so every row is loaded once and used for
 // both C_k and C_{N-k}.  Items: slots x 16 lanes over the block's threads.
-template <int N>
+template <int N, int W>
 __device__ __forceinline__ void herm_first_pass(float2 *sm2, const float2 *__restrict__ gin2, long long gs2,
                                                 int z0, int P)
 {
-    constexpr int T = LinePlan<N, true>::T, NB = N / 8, SLOTS = NB / 2;
+    constexpr int T = LinePlan<N, true, W>::T, NB = N / 8, SLOTS = NB / 2;
     constexpr int ITEMS = SLOTS * LANES, IPT = (ITEMS + T - 1) / T;
 #pragma unroll 1
     for (int q = 0; q < IPT; ++q) {
@@ -175,35 +177,35 @@ __device__ __forceinline__ void herm_first_pass(float2 *sm2, const float2 *__res
 }
 
 // the passes after the first for N = 8^a * {1, 2, 4}
-template <int N, bool INV, bool TO_GLOBAL>
+template <int N, bool INV, int W, bool TO_GLOBAL>
 __device__ __forceinline__ void later_passes(float4 *sm, float4 *gout, long long gs, bool valid, float scale,
                                              const float2 *tw)
 {
     if constexpr (N == 64) {
-        pass<N, 8, 8, INV, false, TO_GLOBAL>(sm, nullptr, gout, gs, valid, scale, tw);
+        pass<N, 8, 8, INV, W, false, TO_GLOBAL>(sm, nullptr, gout, gs, valid, scale, tw);
     } else if constexpr (N == 128) {
-        pass<N, 8, 8, INV, false, false>(sm, nullptr, gout, gs, valid, scale, tw);
-        pass<N, 2, 64, INV, false, TO_GLOBAL>(sm, nullptr, gout, gs, valid, scale, tw);
+        pass<N, 8, 8, INV, W, false, false>(sm, nullptr, gout, gs, valid, scale, tw);
+        pass<N, 2, 64, INV, W, false, TO_GLOBAL>(sm, nullptr, gout, gs, valid, scale, tw);
     } else if constexpr (N == 256) {
-        pass<N, 8, 8, INV, false, false>(sm, nullptr, gout, gs, valid, scale, tw);
-        pass<N, 4, 64, INV, false, TO_GLOBAL>(sm, nullptr, gout, gs, valid, scale, tw);
+        pass<N, 8, 8, INV, W, false, false>(sm, nullptr, gout, gs, valid, scale, tw);
+        pass<N, 4, 64, INV, W, false, TO_GLOBAL>(sm, nullptr, gout, gs, valid, scale, tw);
     } else if constexpr (N == 512) {
-        pass<N, 8, 8, INV, false, false>(sm, nullptr, gout, gs, valid, scale, tw);
-        pass<N, 8, 64, INV, false, TO_GLOBAL>(sm, nullptr, gout, gs, valid, scale, tw);
+        pass<N, 8, 8, INV, W, false, false>(sm, nullptr, gout, gs, valid, scale, tw);
+        pass<N, 8, 64, INV, W, false, TO_GLOBAL>(sm, nullptr, gout, gs, valid, scale, tw);
     } else {  // 1024
-        pass<N, 8, 8, INV, false, false>(sm, nullptr, gout, gs, valid, scale, tw);
-        pass<N, 8, 64, INV, false, false>(sm, nullptr, gout, gs, valid, scale, tw);
-        pass<N, 2, 512, INV, false, TO_GLOBAL>(sm, nullptr, gout, gs, valid, scale, tw);
+        pass<N, 8, 8, INV, W, false, false>(sm, nullptr, gout, gs, valid, scale, tw);
+        pass<N, 8, 64, INV, W, false, false>(sm, nullptr, gout, gs, valid, scale, tw);
+        pass<N, 2, 512, INV, W, false, TO_GLOBAL>(sm, nullptr, gout, gs, valid, scale, tw);
     }
 }
 
-template <int N, bool INV>
-__global__ void __launch_bounds__(LinePlan<N, INV>::T, LinePlan<N, INV>::MINB)
+template <int N, bool INV, int W>
+__global__ void __launch_bounds__(LinePlan<N, INV, W>::T, LinePlan<N, INV, W>::MINB)
     k_lines32(const float *__restrict__ in, float *__restrict__ out, int P, long long line_stride,
               long long batch_stride, const float2 *__restrict__ tw)
 {
     extern __shared__ __align__(16) float4 smL[];
-    constexpr int T = LinePlan<N, INV>::T;
+    constexpr int T = LinePlan<N, INV, W>::T;
     const int p = threadIdx.x & (PAIRS - 1);
     const int z0 = blockIdx.x * 2 * LANES;
     const bool valid = z0 + 4 * p < P;  // P is a multiple of 8: both lanes or neither
@@ -213,8 +215,8 @@ __global__ void __launch_bounds__(LinePlan<N, INV>::T, LinePlan<N, INV>::MINB)
     if (!INV) {
         const long long gs = line_stride >> 2;  // float4 units
         const float4 *gin = reinterpret_cast<const float4 *>(in + base) + p;
-        pass<N, 8, 1, false, true, false>(smL, gin, nullptr, gs, valid, 1.0f, tw);
-        later_passes<N, false, false>(smL, nullptr, gs, valid, 1.0f, tw);
+        pass<N, 8, 1, false, W, true, false>(smL, gin, nullptr, gs, valid, 1.0f, tw);
+        later_passes<N, false, W, false>(smL, nullptr, gs, valid, 1.0f, tw);
         // split the two packed real transforms of each lane and store the
         // Hermitian rows k and N - k
         float4 *o = reinterpret_cast<float4 *>(out + base);
@@ -232,22 +234,40 @@ __global__ void __launch_bounds__(LinePlan<N, INV>::T, LinePlan<N, INV>::MINB)
                                                   0.5f * (ck.w - cn.w) * s, -0.5f * (ck.z - cn.z) * s);
         }
     } else {
-        herm_first_pass<N>(reinterpret_cast<float2 *>(smL), reinterpret_cast<const float2 *>(in + base),
-                           line_stride >> 1, z0, P);
+        herm_first_pass<N, W>(reinterpret_cast<float2 *>(smL), reinterpret_cast<const float2 *>(in + base),
+                              line_stride >> 1, z0, P);
         const long long gs = line_stride >> 2;
         float4 *gout = reinterpret_cast<float4 *>(out + base) + p;
-        later_passes<N, true, true>(smL, gout, gs, valid, s, tw);
+        later_passes<N, true, W, true>(smL, gout, gs, valid, s, tw);
     }
+}
+
+template <int N, bool INV, int W>
+void launch32w(cudaStream_t st, const float *in, float *out, int P, long long ls, long long nbatch, long long bs,
+               const float2 *tw)
+{
+    dim3 grid((P + 2 * LANES - 1) / (2 * LANES), (unsigned)nbatch);
+    const size_t sm = (size_t)N * LANES * sizeof(float2);
+    k_lines32<N, INV, W><<<grid, LinePlan<N, INV, W>::T, sm, st>>>(in, out, P, ls, bs, tw);
 }
 
 template <int N>
 void launch32(cudaStream_t st, const float *in, float *out, int P, long long ls, long long nbatch, long long bs,
-              bool inverse, const float2 *tw)
+              bool inverse, const float2 *tw, int shape)
 {
-    dim3 grid((P + 2 * LANES - 1) / (2 * LANES), (unsigned)nbatch);
-    const size_t sm = (size_t)N * LANES * sizeof(float2);
-    if (inverse) k_lines32<N, true><<<grid, LinePlan<N, true>::T, sm, st>>>(in, out, P, ls, bs, tw);
-    else k_lines32<N, false><<<grid, LinePlan<N, false>::T, sm, st>>>(in, out, P, ls, bs, tw);
+    if (N == 512) {
+        const int w = shape < 0 ? (inverse ? 1 : 0) : shape;
+        if (inverse) {
+            if (w) launch32w<N, true, 1>(st, in, out, P, ls, nbatch, bs, tw);
+            else launch32w<N, true, 0>(st, in, out, P, ls, nbatch, bs, tw);
+        } else {
+            if (w) launch32w<N, false, 1>(st, in, out, P, ls, nbatch, bs, tw);
+            else launch32w<N, false, 0>(st, in, out, P, ls, nbatch, bs, tw);
+        }
+        return;
+    }
+    if (inverse) launch32w<N, true, 0>(st, in, out, P, ls, nbatch, bs, tw);
+    else launch32w<N, false, 0>(st, in, out, P, ls, nbatch, bs, tw);
 }
 
 }  // namespace
@@ -256,21 +276,25 @@ bool lines32_supported(int n) { return n == 64 || n == 128 || n == 256 || n == 5
 
 void lines32_init()
 {
-    cudaFuncSetAttribute(k_lines32<1024, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, 1024 * LANES * 8);
-    cudaFuncSetAttribute(k_lines32<1024, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, 1024 * LANES * 8);
-    cudaFuncSetAttribute(k_lines32<512, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, 512 * LANES * 8);
-    cudaFuncSetAttribute(k_lines32<512, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, 512 * LANES * 8);
+    cudaFuncSetAttribute(k_lines32<1024, false, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, 1024 * LANES * 8);
+    cudaFuncSetAttribute(k_lines32<1024, true, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, 1024 * LANES * 8);
+    cudaFuncSetAttribute(k_lines32<512, false, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, 512 * LANES * 8);
+    cudaFuncSetAttribute(k_lines32<512, true, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, 512 * LANES * 8);
+    cudaFuncSetAttribute(k_lines32<512, false, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, 512 * LANES * 8);
+    cudaFuncSetAttribute(k_lines32<512, true, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, 512 * LANES * 8);
 }
 
+int lines32_shapes(int n) { return n == 512 ? 2 : 1; }
+
 void launch_lines32(cudaStream_t st, const float *in, float *out, int n, int P, long long line_stride,
-                    long long nbatch, long long batch_stride, bool inverse, const float2 *tw)
+                    long long nbatch, long long batch_stride, bool inverse, const float2 *tw, int shape)
 {
     switch (n) {
-    case 64: launch32<64>(st, in, out, P, line_stride, nbatch, batch_stride, inverse, tw); break;
-    case 128: launch32<128>(st, in, out, P, line_stride, nbatch, batch_stride, inverse, tw); break;
-    case 256: launch32<256>(st, in, out, P, line_stride, nbatch, batch_stride, inverse, tw); break;
-    case 512: launch32<512>(st, in, out, P, line_stride, nbatch, batch_stride, inverse, tw); break;
-    default: launch32<1024>(st, in, out, P, line_stride, nbatch, batch_stride, inverse, tw); break;
+    case 64: launch32<64>(st, in, out, P, line_stride, nbatch, batch_stride, inverse, tw, shape); break;
+    case 128: launch32<128>(st, in, out, P, line_stride, nbatch, batch_stride, inverse, tw, shape); break;
+    case 256: launch32<256>(st, in, out, P, line_stride, nbatch, batch_stride, inverse, tw, shape); break;
+    case 512: launch32<512>(st, in, out, P, line_stride, nbatch, batch_stride, inverse, tw, shape); break;
+    default: launch32<1024>(st, in, out, P, line_stride, nbatch, batch_stride, inverse, tw, shape); break;
     }
 }
 

@@ -121,6 +121,9 @@ struct ps3d_gpu_ctx {
     double *roll_dev = nullptr;
     cudaGraphExec_t graph = nullptr;
     long long graph_launches = 0;  // kernels per captured step
+    // line-FFT autotuner: ms per launch of each block shape for the passes
+    // forward y, forward x, inverse y, inverse x (0 where not timed)
+    double tune_ms[4][2] = {{0, 0}, {0, 0}, {0, 0}, {0, 0}};
 
     Deriv D() const { return Deriv{cx, cy}; }
     Tables tables() const
@@ -1104,6 +1107,42 @@ template <typename T> void twiddles(ps3d_gpu_ctx *c, void *dst, int n)
     cudaStreamSynchronize(c->st);
 }
 
+// Autotuner of the FP32 line FFTs: where a line length has more than one
+// block shape (lines32_shapes), every pass (forward / inverse, y / x) is
+// timed with each shape on a zeroed scratch field (one warm-up and three
+// timed launches, CUDA events) and keeps the fastest.
+int autotune_lines(ps3d_gpu_ctx *c)
+{
+    Dims &d = c->d;
+    if (lines32_shapes(d.nx) < 2 && lines32_shapes(d.ny) < 2) return PS3D_OK;
+    float *a = tmpf<float>(c, 0), *b = tmpf<float>(c, 1);
+    cudaMemsetAsync(a, 0, d.nfield * sizeof(float), c->st);
+    const float2 *twx = tf<float2>(c->twx), *twy = tf<float2>(c->twy);
+    for (int pass = 0; pass < 4; ++pass) {
+        const bool inv = pass >= 2, xl = (pass & 1) != 0;
+        const int n = xl ? d.nx : d.ny;
+        const int ns = lines32_shapes(n);
+        if (ns < 2) continue;
+        const long long ls = xl ? (long long)d.ny * d.P : d.P, nb = xl ? d.ny : d.nx,
+                        bs = xl ? d.P : (long long)d.ny * d.P;
+        int best = 0;
+        for (int w = 0; w < ns; ++w) {
+            launch_lines32(c->st, a, b, n, d.P, ls, nb, bs, inv, xl ? twx : twy, w);
+            cudaEventRecord(c->ev0, c->st);
+            for (int r = 0; r < 3; ++r) launch_lines32(c->st, a, b, n, d.P, ls, nb, bs, inv, xl ? twx : twy, w);
+            cudaEventRecord(c->ev1, c->st);
+            const int rc = sync_check(c, "autotune");
+            if (rc) return rc;
+            float f = 0.0f;
+            cudaEventElapsedTime(&f, c->ev0, c->ev1);
+            c->tune_ms[pass][w] = f / 3.0;
+            if (c->tune_ms[pass][w] < c->tune_ms[pass][best]) best = w;
+        }
+        d.line_shape[pass] = (signed char)best;
+    }
+    return PS3D_OK;
+}
+
 template <typename T> int allocate_fields(ps3d_gpu_ctx *c)
 {
     const Dims &d = c->d;
@@ -1175,7 +1214,9 @@ template <typename T> int allocate_fields(ps3d_gpu_ctx *c)
                                      c->phim64, c->phip64, s, s + N, s + 2 * N, s2, s2 + N);
         c->launches += 1;
     }
-    return sync_check(c, "create");
+    int rc = sync_check(c, "create");
+    if (rc) return rc;
+    return c->fp64 ? PS3D_OK : autotune_lines(c);
 }
 
 #define DISPATCH(c, fn, ...) ((c)->fp64 ? fn<double>(__VA_ARGS__) : fn<float>(__VA_ARGS__))
@@ -1638,6 +1679,36 @@ int ps3d_gpu_batch_advance(ps3d_gpu_ctx *const *ctx, int n, double *t, int nstep
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
     return rc ? rc : rf;
+}
+
+int ps3d_gpu_tuning(ps3d_gpu_ctx *c, int shape[4], double ms[8])
+{
+    int rc = enter(c);
+    if (rc) return rc;
+    if (!shape || !ms) return PS3D_ERR_INVALID_ARG;
+    for (int p = 0; p < 4; ++p) {
+        shape[p] = c->d.line_shape[p];
+        ms[2 * p] = c->tune_ms[p][0];
+        ms[2 * p + 1] = c->tune_ms[p][1];
+    }
+    return PS3D_OK;
+}
+
+int ps3d_gpu_set_tuning(ps3d_gpu_ctx *c, const int shape[4])
+{
+    int rc = enter(c);
+    if (rc) return rc;
+    if (!shape) return PS3D_ERR_INVALID_ARG;
+    for (int p = 0; p < 4; ++p) {
+        const int n = (p & 1) ? c->d.nx : c->d.ny;
+        if (shape[p] < -1 || shape[p] >= lines32_shapes(n)) return PS3D_ERR_INVALID_ARG;
+    }
+    if (c->graph) {  // a captured step holds the old shapes
+        cudaGraphExecDestroy(c->graph);
+        c->graph = nullptr;
+    }
+    for (int p = 0; p < 4; ++p) c->d.line_shape[p] = (signed char)shape[p];
+    return PS3D_OK;
 }
 
 int ps3d_gpu_probe(ps3d_gpu_ctx *c, int kind)

@@ -103,12 +103,12 @@ int lines_lanes(int n)
 template <typename T>
 void launch_lines(cudaStream_t st, const T *in, T *out, int n, int P, long long line_stride,
                   long long nbatch, long long batch_stride, bool inverse,
-                  const typename cplx<T>::type *tw)
+                  const typename cplx<T>::type *tw, int shape = -1)
 {
     if constexpr (sizeof(T) == sizeof(float)) {
         if (lines32_supported(n)) {
             launch_lines32(st, reinterpret_cast<const float *>(in), reinterpret_cast<float *>(out), n, P,
-                           line_stride, nbatch, batch_stride, inverse, reinterpret_cast<const float2 *>(tw));
+                           line_stride, nbatch, batch_stride, inverse, reinterpret_cast<const float2 *>(tw), shape);
             return;
         }
     }
@@ -134,11 +134,11 @@ void xy_forward(const Dims &d, cudaStream_t st, const T *in, T *out, const typen
 {
     // y lines: line stride P (one column), batches over x (stride ny*P)
     if (pr) pr->begin(PROBE_YLINES, st);
-    launch_lines<T>(st, in, out, d.ny, d.P, d.P, d.nx, (long long)d.ny * d.P, false, twy);
+    launch_lines<T>(st, in, out, d.ny, d.P, d.P, d.nx, (long long)d.ny * d.P, false, twy, d.line_shape[0]);
     if (pr) pr->end(PROBE_YLINES, st, pass_bytes<T>(d));
     // x lines: line stride ny*P, batches over y (stride P)
     if (pr) pr->begin(PROBE_XLINES, st);
-    launch_lines<T>(st, out, out, d.nx, d.P, (long long)d.ny * d.P, d.ny, d.P, false, twx);
+    launch_lines<T>(st, out, out, d.nx, d.P, (long long)d.ny * d.P, d.ny, d.P, false, twx, d.line_shape[1]);
     if (pr) pr->end(PROBE_XLINES, st, pass_bytes<T>(d));
 }
 
@@ -147,10 +147,10 @@ void xy_inverse(const Dims &d, cudaStream_t st, const T *in, T *out, const typen
                 const typename cplx<T>::type *twy, Probe *pr)
 {
     if (pr) pr->begin(PROBE_XLINES, st);
-    launch_lines<T>(st, in, out, d.nx, d.P, (long long)d.ny * d.P, d.ny, d.P, true, twx);
+    launch_lines<T>(st, in, out, d.nx, d.P, (long long)d.ny * d.P, d.ny, d.P, true, twx, d.line_shape[3]);
     if (pr) pr->end(PROBE_XLINES, st, pass_bytes<T>(d));
     if (pr) pr->begin(PROBE_YLINES, st);
-    launch_lines<T>(st, out, out, d.ny, d.P, d.P, d.nx, (long long)d.ny * d.P, true, twy);
+    launch_lines<T>(st, out, out, d.ny, d.P, d.P, d.nx, (long long)d.ny * d.P, true, twy, d.line_shape[2]);
     if (pr) pr->end(PROBE_YLINES, st, pass_bytes<T>(d));
 }
 

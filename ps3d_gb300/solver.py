@@ -231,6 +231,18 @@ class Ps3dGpu:
         self._chk(self.L.ps3d_gpu_time_advance(self._h, ctypes.byref(tt), nsteps, ctypes.byref(ms)))
         return tt.value, ms.value
 
+    def tuning(self):
+        """Line-FFT autotuner result: (shape per pass [fwd y, fwd x, inv y,
+        inv x], ms per launch of each shape per pass)."""
+        sh = (ctypes.c_int * 4)()
+        ms = (ctypes.c_double * 8)()
+        self._chk(self.L.ps3d_gpu_tuning(self._h, sh, ms))
+        return list(sh), [list(ms[2 * i:2 * i + 2]) for i in range(4)]
+
+    def set_tuning(self, shapes):
+        """Pin the line-FFT block shape per pass (-1 = default)."""
+        self._chk(self.L.ps3d_gpu_set_tuning(self._h, (ctypes.c_int * 4)(*shapes)))
+
     def advance_graph(self, t, nsteps):
         """nsteps captured advances (mixed form, impl-diff-rk4): one CUDA graph
         launch per step, adapt's scalars on the device.  Returns (t, diag of
