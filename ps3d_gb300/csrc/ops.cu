@@ -406,26 +406,46 @@ void op_svorts(const Dims &d, cudaStream_t st, const Deriv &D, const T *r, const
 
 // spectral velocity gradients for the strain (advance.f90:193-217):
 // du/dx, du/dy, dw/dx, dv/dy, dw/dy
+// Orbit form (as k_v2v_orbit): one warp per partner orbit, each velocity
+// column read once; same products as k_strain_fields.
 template <typename T>
-__global__ void k_strain_fields(Dims d, Deriv D, const T *__restrict__ svel, T *__restrict__ g5)
+__global__ void k_strain_orbit(Dims d, Deriv D, const T *__restrict__ svel, T *__restrict__ g5)
 {
-    COLUMN_HEADER
-    PARTNERS
+    const int hy = d.ny / 2 + 1;
+    const long long orb = (long long)blockIdx.x * COLS_PER_BLOCK + threadIdx.y;
+    if (orb >= (long long)(d.nx / 2 + 1) * hy) return;
     const long long N = d.nfield;
-    const T cx = (T)cxk, cy = (T)cyk;
+    const int kx = (int)(orb / hy), ky = (int)(orb - (long long)kx * hy);
+    const int x2 = xsrc(kx, d.nx), y2 = xsrc(ky, d.ny);
+    const long long o00 = ((long long)ky + (long long)d.ny * kx) * d.P, o10 = ((long long)ky + (long long)d.ny * x2) * d.P;
+    const long long o01 = ((long long)y2 + (long long)d.ny * kx) * d.P, o11 = ((long long)y2 + (long long)d.ny * x2) * d.P;
+    const bool dx = x2 != kx, dy = y2 != ky;
+    const T cxa = (T)D.cx[kx], cxb = (T)D.cx[x2], cya = (T)D.cy[ky], cyb = (T)D.cy[y2];
+    const T *u = svel, *v = svel + N, *w = svel + 2 * N;
     for (int iz = threadIdx.x; iz <= d.nz; iz += 32) {
-        const long long i = o + iz;
-        g5[i] = cx * svel[ox + iz];
-        g5[N + i] = cy * svel[oy + iz];
-        g5[2 * N + i] = cx * svel[2 * N + ox + iz];
-        g5[3 * N + i] = cy * svel[N + oy + iz];
-        g5[4 * N + i] = cy * svel[2 * N + oy + iz];
+        const T u00 = u[o00 + iz], u10 = u[o10 + iz], u01 = u[o01 + iz], u11 = u[o11 + iz];
+        const T v00 = v[o00 + iz], v10 = v[o10 + iz], v01 = v[o01 + iz], v11 = v[o11 + iz];
+        const T w00 = w[o00 + iz], w10 = w[o10 + iz], w01 = w[o01 + iz], w11 = w[o11 + iz];
+        // member (a, b): x partner / y partner reads as in k_strain_fields
+        auto put = [&](long long o, T cx, T cy, T ux, T uy, T vy, T wx, T wy) {
+            g5[o + iz] = cx * ux;
+            g5[N + o + iz] = cy * uy;
+            g5[2 * N + o + iz] = cx * wx;
+            g5[3 * N + o + iz] = cy * vy;
+            g5[4 * N + o + iz] = cy * wy;
+        };
+        put(o00, cxa, cya, u10, u01, v01, w10, w01);
+        if (dx) put(o10, cxb, cya, u00, u11, v11, w00, w11);
+        if (dy) put(o01, cxa, cyb, u11, u00, v00, w11, w00);
+        if (dx && dy) put(o11, cxb, cyb, u01, u10, v10, w01, w10);
     }
 }
 template <typename T>
 void op_strain_fields(const Dims &d, cudaStream_t st, const Deriv &D, const T *svel, T *g5)
 {
-    k_strain_fields<T><<<col_grid(d), COL_BLOCK, 0, st>>>(d, D, svel, g5);
+    const long long norb = (long long)(d.nx / 2 + 1) * (d.ny / 2 + 1);
+    k_strain_orbit<T><<<(unsigned)((norb + COLS_PER_BLOCK - 1) / COLS_PER_BLOCK), COL_BLOCK, 0, st>>>(d, D, svel,
+                                                                                                      g5);
 }
 
 // flat conversions / accumulation over n elements
