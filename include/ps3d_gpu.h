@@ -175,6 +175,13 @@ int ps3d_gpu_time_advance(ps3d_gpu_ctx *ctx, double *t, int nsteps, double *ms);
 /* Kernel launches issued by this context since creation. */
 long long ps3d_gpu_launch_count(const ps3d_gpu_ctx *ctx);
 int ps3d_gpu_synchronize(ps3d_gpu_ctx *ctx);
+/* Derived fields (src/fields/fields_derived.f90:67-182, buoyancy disabled)
+ * from the current vel, vor and svel (call after ps3d_gpu_vor2vel, as the
+ * reference's adapt does): pres solves Lap(p) = 2[J_xy(u,v) + J_yz(v,w) +
+ * J_zx(w,u)] with dp/dz = 0 on the walls; delta = du/dx + dv/dy.  Physical
+ * host arrays (nz+1, ny, nx) column-major; NULL skips one. */
+int ps3d_gpu_derived_fields(ps3d_gpu_ctx *ctx, double *pres, double *delta);
+
 /* Captured steps (no reference counterpart): nsteps advances of the mixed
  * form with impl-diff-rk4, each one CUDA graph launch with adapt's scalar
  * logic on the device (no host synchronisation inside a step).  Same

@@ -95,6 +95,8 @@ def lib():
         L.ps3o_rolling_mean_next.argtypes = [vp, ctypes.c_double]
         L.ps3o_rolling_mean_next.restype = ctypes.c_double
         L.ps3o_jacobi_eigenvalues.argtypes = [_dp, _dp]
+        L.ps3o_pressure.argtypes = [vp, _dp]
+        L.ps3o_horizontal_divergence.argtypes = [vp, _dp]
         L.ps3o_forfft.argtypes = [ctypes.c_int, ctypes.c_int, _dp, _dp, _dp, ctypes.POINTER(ctypes.c_int)]
         L.ps3o_revfft.argtypes = L.ps3o_forfft.argtypes
         L.ps3o_dct.argtypes = [ctypes.c_int, ctypes.c_int, _dp, _dp, _dp, _dp, ctypes.POINTER(ctypes.c_int)]
@@ -306,6 +308,16 @@ class Oracle:
         d = Diag()
         lib().ps3o_advance(self._h, ctypes.byref(tt), ctypes.byref(d))
         return tt.value, d.as_dict()
+
+    def pressure(self):
+        out = np.zeros(self.shape)
+        lib().ps3o_pressure(self._h, _ptr(out))
+        return out
+
+    def horizontal_divergence(self):
+        out = np.zeros(self.shape)
+        lib().ps3o_horizontal_divergence(self._h, _ptr(out))
+        return out
 
     def energy_series(self):
         a, b, c = ctypes.c_double(), ctypes.c_double(), ctypes.c_double()

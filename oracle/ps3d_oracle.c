@@ -1176,3 +1176,45 @@ void ps3o_set_ini_vor_mean(ps3o_model *m, const double in[2])
 }
 
 double ps3o_get_vvisc(ps3o_model *m) { return m->vvisc; }
+
+/* ====================================================================== */
+/* derived fields (fields_derived.f90:67-182, buoyancy disabled): pressure */
+/* from Lap(p) = 2[J_xy(u,v) + J_yz(v,w) + J_zx(w,u)] with dp/dz = 0 on the */
+/* walls (DCT - Green function - DCT), and the horizontal divergence       */
+/* ====================================================================== */
+void ps3o_pressure(ps3o_model *m, double *pres)
+{
+    const size_t N = m->nfield;
+    double *xs = dalloc(N), *rs = dalloc(N);
+    double *dudx = dalloc(N), *dudy = dalloc(N), *dvdy = dalloc(N), *dwdx = dalloc(N), *dwdy = dalloc(N);
+    /* velocity gradients as in adapt (advance.f90:193-217) */
+    ps3o_diffx(m, m->svel, xs);          ps3o_fftxys2p(m, xs, dudx);
+    ps3o_diffy(m, m->svel, xs);          ps3o_fftxys2p(m, xs, dudy);
+    ps3o_diffx(m, m->svel + 2 * N, xs);  ps3o_fftxys2p(m, xs, dwdx);
+    ps3o_diffy(m, m->svel + N, xs);      ps3o_fftxys2p(m, xs, dvdy);
+    ps3o_diffy(m, m->svel + 2 * N, xs);  ps3o_fftxys2p(m, xs, dwdy);
+    const double *xi = m->vor, *eta = m->vor + N, *zeta = m->vor + 2 * N;
+    for (size_t i = 0; i < N; ++i) {
+        const double dwdz = -(dudx[i] + dvdy[i]);
+        pres[i] = 2.0 * (dudx[i] * dvdy[i] - dudy[i] * (zeta[i] + dudy[i]) +
+                         dvdy[i] * dwdz - dwdy[i] * (dwdy[i] - xi[i]) +
+                         dwdz * dudx[i] - dwdx[i] * (dwdx[i] + eta[i]));
+    }
+    ps3o_fftxyp2s(m, pres, rs);
+    ps3o_fftcosine(m, rs);
+    for (size_t i = 0; i < N; ++i) rs[i] = m->green[i] * rs[i];
+    ps3o_fftcosine(m, rs);
+    ps3o_fftxys2p(m, rs, pres);
+    free(xs); free(rs); free(dudx); free(dudy); free(dvdy); free(dwdx); free(dwdy);
+}
+
+void ps3o_horizontal_divergence(ps3o_model *m, double *delta)
+{
+    const size_t N = m->nfield;
+    double *uxs = dalloc(N), *vys = dalloc(N);
+    ps3o_diffx(m, m->svel, uxs);
+    ps3o_diffy(m, m->svel + N, vys);
+    for (size_t i = 0; i < N; ++i) uxs[i] = uxs[i] + vys[i];
+    ps3o_fftxys2p(m, uxs, delta);
+    free(uxs); free(vys);
+}

@@ -183,6 +183,10 @@ void op_rk4m_sub23(const Dims &d, cudaStream_t st, double *q, const double *qdi,
 void op_rk4m_sub4(const Dims &d, cudaStream_t st, double *q, const double *qdi, const float *acc, const float *sqs,
                   float *q32, const double *epq, const double *emq, const double *dtp);
 void op_narrow(cudaStream_t st, const double *in, float *out, long long n);
+// derived fields (pressure right-hand side, table product, horizontal divergence)
+template <typename T> void op_pressure_rhs(const Dims &d, cudaStream_t st, const T *g5, const T *vor, T *out);
+template <typename T> void op_mul_field(const Dims &d, cudaStream_t st, const T *tab, T *f);
+template <typename T> void op_hdiv(const Dims &d, cudaStream_t st, const Deriv &D, const T *svel, T *out);
 // host-layout (nz+1)-pitched FP64 columns <-> device P-pitched columns
 void op_unpack_cols(const Dims &d, cudaStream_t st, const double *src, double *dst, int ncomp, int *changed);
 void op_pack_cols(const Dims &d, cudaStream_t st, const double *src, double *dst, int ncomp);

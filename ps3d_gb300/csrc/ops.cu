@@ -448,6 +448,61 @@ void op_strain_fields(const Dims &d, cudaStream_t st, const Deriv &D, const T *s
                                                                                                       g5);
 }
 
+// Derived fields (fields_derived.f90:67-182, buoyancy disabled).
+// Right-hand side of the pressure Poisson equation from the physical
+// velocity gradients g5 = (du/dx, du/dy, dw/dx, dv/dy, dw/dy) and the
+// vorticity: 2 [J_xy(u,v) + J_yz(v,w) + J_zx(w,u)] with dv/dx = zeta + du/dy,
+// du/dz = eta + dw/dx, dv/dz = dw/dy - xi, dw/dz = -(du/dx + dv/dy).
+template <typename T>
+__global__ void k_pressure_rhs(Dims d, const T *__restrict__ g5, const T *__restrict__ vor, T *__restrict__ out)
+{
+    COLUMN_HEADER
+    const long long N = d.nfield;
+    for (int iz = threadIdx.x; iz <= d.nz; iz += 32) {
+        const long long i = o + iz;
+        const T dudx = g5[i], dudy = g5[N + i], dwdx = g5[2 * N + i], dvdy = g5[3 * N + i], dwdy = g5[4 * N + i];
+        const T xi = vor[i], eta = vor[N + i], zeta = vor[2 * N + i];
+        const T dwdz = -(dudx + dvdy);
+        out[i] = (T)2 * (dudx * dvdy - dudy * (zeta + dudy) + dvdy * dwdz - dwdy * (dwdy - xi) + dwdz * dudx -
+                         dwdx * (dwdx + eta));
+    }
+}
+template <typename T> void op_pressure_rhs(const Dims &d, cudaStream_t st, const T *g5, const T *vor, T *out)
+{
+    k_pressure_rhs<T><<<col_grid(d), COL_BLOCK, 0, st>>>(d, g5, vor, out);
+}
+// f *= tab (a field-shaped table, e.g. the Green function)
+template <typename T>
+__global__ void k_mul_field(Dims d, const T *__restrict__ tab, T *__restrict__ f)
+{
+    COLUMN_HEADER
+    for (int iz = threadIdx.x; iz <= d.nz; iz += 32) f[o + iz] = tab[o + iz] * f[o + iz];
+}
+template <typename T> void op_mul_field(const Dims &d, cudaStream_t st, const T *tab, T *f)
+{
+    k_mul_field<T><<<col_grid(d), COL_BLOCK, 0, st>>>(d, tab, f);
+}
+// du/dx + dv/dy in spectral space (diffx, diffy of sta3dfft.f90:304-377)
+template <typename T>
+__global__ void k_hdiv(Dims d, Deriv D, const T *__restrict__ svel, T *__restrict__ out)
+{
+    COLUMN_HEADER
+    PARTNERS
+    const long long N = d.nfield;
+    const T cx = (T)cxk, cy = (T)cyk;
+    for (int iz = threadIdx.x; iz <= d.nz; iz += 32) out[o + iz] = cx * svel[ox + iz] + cy * svel[N + oy + iz];
+}
+template <typename T> void op_hdiv(const Dims &d, cudaStream_t st, const Deriv &D, const T *svel, T *out)
+{
+    k_hdiv<T><<<col_grid(d), COL_BLOCK, 0, st>>>(d, D, svel, out);
+}
+template void op_pressure_rhs<float>(const Dims &, cudaStream_t, const float *, const float *, float *);
+template void op_pressure_rhs<double>(const Dims &, cudaStream_t, const double *, const double *, double *);
+template void op_mul_field<float>(const Dims &, cudaStream_t, const float *, float *);
+template void op_mul_field<double>(const Dims &, cudaStream_t, const double *, double *);
+template void op_hdiv<float>(const Dims &, cudaStream_t, const Deriv &, const float *, float *);
+template void op_hdiv<double>(const Dims &, cudaStream_t, const Deriv &, const double *, double *);
+
 // flat conversions / accumulation over n elements
 template <typename T, typename S>
 __global__ void k_convert(const S *__restrict__ in, T *__restrict__ out, long long n)

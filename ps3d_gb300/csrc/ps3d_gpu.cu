@@ -917,6 +917,40 @@ int graph_finish(ps3d_gpu_ctx *c, double *t, ps3d_gpu_diag *diag)
     return PS3D_OK;
 }
 
+// ---------------------------------------------------------- derived fields
+// pressure and horizontal divergence (fields_derived.f90:67-182, buoyancy
+// disabled) from the current vel / vor / svel; physical fields to the host
+template <typename T> int derived_fields(ps3d_gpu_ctx *c, double *hp, double *hd)
+{
+    const Dims &d = c->d;
+    const long long N = d.nfield;
+    if (hp) {
+        T *g5 = tmpf<T>(c, 0), *pr = tmpf<T>(c, 5);
+        op_strain_fields<T>(d, c->st, c->D(), tf<T>(c->svel), g5);
+        c->launches += 1;
+        for (int k = 0; k < 5; ++k) xyi<T>(c, g5 + k * N, g5 + k * N);
+        op_pressure_rhs<T>(d, c->st, g5, tf<T>(c->vor), pr);
+        c->launches += 1;
+        xyf<T>(c, pr, pr);
+        col<T>(c, COL_DCT, pr, pr);
+        op_mul_field<T>(d, c->st, tf<T>(c->green), pr);
+        c->launches += 1;
+        col<T>(c, COL_DCT, pr, pr);
+        xyi<T>(c, pr, pr);
+        int rc = download(c, pr, sizeof(T) == sizeof(double), 1, hp);
+        if (rc) return rc;
+    }
+    if (hd) {
+        T *dl = tmpf<T>(c, 0);
+        op_hdiv<T>(d, c->st, c->D(), tf<T>(c->svel), dl);
+        c->launches += 1;
+        xyi<T>(c, dl, dl);
+        int rc = download(c, dl, sizeof(T) == sizeof(double), 1, hd);
+        if (rc) return rc;
+    }
+    return PS3D_OK;
+}
+
 // setup_fields (utils.f90:136-184)
 template <typename T> int setup_fields(ps3d_gpu_ctx *c, const double *vor_phys, const double *pert, double *te,
                                        double *en)
@@ -1721,6 +1755,13 @@ int ps3d_gpu_set_tuning(ps3d_gpu_ctx *c, const int shape[4])
     }
     for (int p = 0; p < 4; ++p) c->d.line_shape[p] = (signed char)shape[p];
     return PS3D_OK;
+}
+
+int ps3d_gpu_derived_fields(ps3d_gpu_ctx *c, double *pres, double *delta)
+{
+    int rc = enter(c);
+    if (rc) return rc;
+    return DISPATCH(c, derived_fields, c, pres, delta);
 }
 
 int ps3d_gpu_probe(ps3d_gpu_ctx *c, int kind)

@@ -231,6 +231,14 @@ class Ps3dGpu:
         self._chk(self.L.ps3d_gpu_time_advance(self._h, ctypes.byref(tt), nsteps, ctypes.byref(ms)))
         return tt.value, ms.value
 
+    def derived_fields(self):
+        """(pressure, horizontal divergence) of the current state, physical
+        (nx, ny, nz+1) arrays (fields_derived.f90:67-182)."""
+        shape = (self.nx, self.ny, self.nz + 1)
+        p, dl = np.zeros(shape), np.zeros(shape)
+        self._chk(self.L.ps3d_gpu_derived_fields(self._h, p.ctypes.data, dl.ctypes.data))
+        return p, dl
+
     def tuning(self):
         """Line-FFT autotuner result: (shape per pass [fwd y, fwd x, inv y,
         inv x], ms per launch of each shape per pass)."""

@@ -119,3 +119,38 @@ def test_transform_conventions():
         assert np.abs(oracle.dst(oracle.dst(y)) - y).max() < 1e-13
         z = rng.standard_normal(n + 1)
         assert np.abs(oracle.dct(oracle.dct(z)) - z).max() < 1e-13
+
+
+def _beltrami_state(n):
+    from ps3d_gb300 import ic
+    lo, ex = ic.BASELINE_BOX["lower"], ic.BASELINE_BOX["extent"]
+    o = oracle.Oracle(n, n, n, lo, ex)
+    o.setup_fields(ic.beltrami_vorticity(n, n, n, lo, ex), None)
+    o.vor2vel()
+    return o, lo, ex
+
+
+@pytest.mark.parametrize("n", [16, 32])
+def test_pressure_of_beltrami_flow_is_bernoulli(n):
+    """Derived pressure (fields_derived.f90:67-157): a Beltrami flow is a
+    steady Euler solution with u x omega = 0, so grad p = -grad |u|^2/2 and
+    p = -|u|^2/2 + const exactly."""
+    o, _, _ = _beltrami_state(n)
+    p = o.pressure()
+    ke = 0.5 * np.sum(o.get("vel") ** 2, axis=0)
+    a, b = p - p.mean(), -(ke - ke.mean())
+    assert np.linalg.norm(a - b) / np.linalg.norm(b) < 1e-12
+
+
+@pytest.mark.parametrize("n", [16, 32])
+def test_horizontal_divergence_of_beltrami_flow(n):
+    """Horizontal divergence (fields_derived.f90:161-182) against the analytic
+    -dw/dz of the Beltrami field (k = l = 2, m = 1, u = omega / alpha):
+    w = cos(mz) cos(kx + ly), so du/dx + dv/dy = m sin(mz) cos(kx + ly)."""
+    o, lo, ex = _beltrami_state(n)
+    d = o.horizontal_divergence()
+    x = lo[0] + ex[0] / n * np.arange(n)
+    y = lo[1] + ex[1] / n * np.arange(n)
+    z = lo[2] + ex[2] / n * np.arange(n + 1)
+    ref = np.sin(z)[None, None, :] * np.cos(2 * x[:, None] + 2 * y[None, :])[:, :, None]
+    assert np.abs(d - ref).max() < 1e-12
