@@ -182,6 +182,13 @@ int ps3d_gpu_synchronize(ps3d_gpu_ctx *ctx);
  * host arrays (nz+1, ny, nx) column-major; NULL skips one. */
 int ps3d_gpu_derived_fields(ps3d_gpu_ctx *ctx, double *pres, double *delta);
 
+/* Kinetic-energy shell spectrum (src/genspec.f90:42-123) of the current
+ * vel: squared spectral amplitudes (dct of u, v and dst of w along z) summed
+ * into shells of |K| = nint(sqrt(kx^2 + ky^2 + kz^2)), scaled by shell volume
+ * over count and normalised so that sum(spec) * dk is the domain-average
+ * kinetic energy.  nbins = kmax + 1 shells (at most nmax written). */
+int ps3d_gpu_ke_spectrum(ps3d_gpu_ctx *ctx, int nmax, double *spec, int *nbins, double *dk);
+
 /* Captured steps (no reference counterpart): nsteps advances of the mixed
  * form with impl-diff-rk4, each one CUDA graph launch with adapt's scalar
  * logic on the device (no host synchronisation inside a step).  Same

@@ -97,6 +97,7 @@ def lib():
         L.ps3o_jacobi_eigenvalues.argtypes = [_dp, _dp]
         L.ps3o_pressure.argtypes = [vp, _dp]
         L.ps3o_horizontal_divergence.argtypes = [vp, _dp]
+        L.ps3o_ke_spectrum.argtypes = [vp, ctypes.c_int, _dp, _dp]
         L.ps3o_forfft.argtypes = [ctypes.c_int, ctypes.c_int, _dp, _dp, _dp, ctypes.POINTER(ctypes.c_int)]
         L.ps3o_revfft.argtypes = L.ps3o_forfft.argtypes
         L.ps3o_dct.argtypes = [ctypes.c_int, ctypes.c_int, _dp, _dp, _dp, _dp, ctypes.POINTER(ctypes.c_int)]
@@ -318,6 +319,12 @@ class Oracle:
         out = np.zeros(self.shape)
         lib().ps3o_horizontal_divergence(self._h, _ptr(out))
         return out
+
+    def ke_spectrum(self, nmax=4096):
+        spec = np.zeros(nmax)
+        dk = ctypes.c_double()
+        nb = lib().ps3o_ke_spectrum(self._h, nmax, _ptr(spec), ctypes.byref(dk))
+        return spec[:nb], dk.value
 
     def energy_series(self):
         a, b, c = ctypes.c_double(), ctypes.c_double(), ctypes.c_double()

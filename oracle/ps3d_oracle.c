@@ -1218,3 +1218,59 @@ void ps3o_horizontal_divergence(ps3o_model *m, double *delta)
     ps3o_fftxys2p(m, uxs, delta);
     free(uxs); free(vys);
 }
+
+/* kinetic-energy shell spectrum (genspec.f90:42-123): svel = fftxyp2s(vel),  */
+/* dct of u and v, dst of w's interior per column, squared amplitudes summed */
+/* into shells m = int(nint(|K|) / dk), scaled by the shell volume over the   */
+/* count and normalised to the domain-average kinetic energy.  Returns the  */
+/* number of shells (kmax + 1, at most nmax written) and dk.                */
+int ps3o_ke_spectrum(ps3o_model *m, int nmax, double *spec, double *dk_out)
+{
+    const int nx = m->nx, ny = m->ny, nz = m->nz;
+    const size_t N = m->nfield;
+    double *sv = dalloc(3 * N);
+    for (int nc = 0; nc < 3; ++nc) ps3o_fftxyp2s(m, m->vel + nc * N, sv + nc * N);
+    double *w1 = dalloc(nz + 1), *w2 = dalloc(nz + 1);
+    for (size_t c = 0; c < m->ncol; ++c) {
+        const size_t o = c * m->nz1;
+        ps3o_dct(1, nz, sv + o, w1, w2, m->ztrig, m->zfac);
+        ps3o_dct(1, nz, sv + N + o, w1, w2, m->ztrig, m->zfac);
+        ps3o_dst(1, nz, sv + 2 * N + o + 1, w1, w2, m->ztrig, m->zfac);
+    }
+    int kmax = 0;
+    for (int kx = 0; kx < nx; ++kx)
+        for (int ky = 0; ky < ny; ++ky)
+            for (int kz = 0; kz <= nz; ++kz) {
+                const int km = (int)lround(sqrt(m->rkx[kx] * m->rkx[kx] + m->rky[ky] * m->rky[ky] +
+                                                m->rkz[kz] * m->rkz[kz]));
+                if (km > kmax) kmax = km;
+            }
+    const double dk = (double)kmax / sqrt((0.5 * nx) * (0.5 * nx) + (0.5 * ny) * (0.5 * ny) + (double)nz * nz);
+    const double dki = 1.0 / dk;
+    double *sp = dalloc(kmax + 1);
+    long *num = (long *)calloc((size_t)kmax + 1, sizeof(long));
+    for (int kx = 0; kx < nx; ++kx)
+        for (int ky = 0; ky < ny; ++ky)
+            for (int kz = 0; kz <= nz; ++kz) {
+                const int km = (int)lround(sqrt(m->rkx[kx] * m->rkx[kx] + m->rky[ky] * m->rky[ky] +
+                                                m->rkz[kz] * m->rkz[kz]));
+                int b = (int)((double)km * dki);
+                if (b > kmax) b = kmax;
+                const size_t q = IDX(m, kz, ky, kx);
+                sp[b] += sv[q] * sv[q] + sv[N + q] * sv[N + q] + sv[2 * N + q] * sv[2 * N + q];
+                num[b] += 1;
+            }
+    const double pi = 3.14159265358979323846;
+    const double pref = 4.0 / 3.0 * pi * dk * dk * dk;
+    for (int b = 0; b <= kmax; ++b)
+        if (num[b] > 0) sp[b] = sp[b] * pref * (double)((long)(b + 1) * (b + 1) * (b + 1) - (long)b * b * b) / (double)num[b];
+    double ke, en, hel;
+    ps3o_energy_series(m, &ke, &en, &hel);
+    double tot = 0.0;
+    for (int b = 0; b <= kmax; ++b) tot += sp[b] * dk;
+    const double snorm = ke / tot;
+    for (int b = 0; b <= kmax && b < nmax; ++b) spec[b] = sp[b] * snorm;
+    *dk_out = dk;
+    free(sv); free(w1); free(w2); free(sp); free(num);
+    return kmax + 1;
+}

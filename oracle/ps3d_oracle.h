@@ -138,6 +138,8 @@ int ps3o_jacobi_eigenvalues(double a[9], double eigs[3]);
  * current vel/vor/svel; outputs physical (nz+1, ny, nx) */
 void ps3o_pressure(ps3o_model *m, double *pres);
 void ps3o_horizontal_divergence(ps3o_model *m, double *delta);
+/* kinetic-energy shell spectrum (genspec.f90:42-123) of the current vel */
+int ps3o_ke_spectrum(ps3o_model *m, int nmax, double *spec, double *dk);
 
 #ifdef __cplusplus
 }

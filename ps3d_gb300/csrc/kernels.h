@@ -187,6 +187,10 @@ void op_narrow(cudaStream_t st, const double *in, float *out, long long n);
 template <typename T> void op_pressure_rhs(const Dims &d, cudaStream_t st, const T *g5, const T *vor, T *out);
 template <typename T> void op_mul_field(const Dims &d, cudaStream_t st, const T *tab, T *f);
 template <typename T> void op_hdiv(const Dims &d, cudaStream_t st, const Deriv &D, const T *svel, T *out);
+// kinetic-energy shell binning of the spectral velocity f (3 components)
+template <typename T>
+void op_spec_bins(const Dims &d, cudaStream_t st, const double *rkx, const double *rky, const double *rkz,
+                  const T *f, double dki, int kmax, double *bins, unsigned long long *cnt);
 // host-layout (nz+1)-pitched FP64 columns <-> device P-pitched columns
 void op_unpack_cols(const Dims &d, cudaStream_t st, const double *src, double *dst, int ncomp, int *changed);
 void op_pack_cols(const Dims &d, cudaStream_t st, const double *src, double *dst, int ncomp);

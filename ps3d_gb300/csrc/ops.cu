@@ -503,6 +503,58 @@ template void op_mul_field<double>(const Dims &, cudaStream_t, const double *, d
 template void op_hdiv<float>(const Dims &, cudaStream_t, const Deriv &, const float *, float *);
 template void op_hdiv<double>(const Dims &, cudaStream_t, const Deriv &, const double *, double *);
 
+// Kinetic-energy shell binning (genspec.f90:67-99): for every spectral
+// element, |K| = nint(sqrt(rkx^2 + rky^2 + rkz^2)), shell int(|K| / dk)
+// (clamped to kmax), sum of u^2 + v^2 + w^2 and a count per shell; block
+// histograms in shared memory, then global atomics.
+template <typename T>
+__global__ void k_spec_bins(Dims d, const double *__restrict__ rkx, const double *__restrict__ rky,
+                            const double *__restrict__ rkz, const T *__restrict__ f, double dki, int kmax,
+                            double *__restrict__ bins, unsigned long long *__restrict__ cnt)
+{
+    extern __shared__ double shb[];
+    unsigned long long *shc = reinterpret_cast<unsigned long long *>(shb + kmax + 1);
+    const int tid = threadIdx.y * 32 + threadIdx.x;
+    for (int b = tid; b <= kmax; b += 32 * COLS_PER_BLOCK) {
+        shb[b] = 0.0;
+        shc[b] = 0ull;
+    }
+    __syncthreads();
+    const long long N = d.nfield;
+    const long long col = (long long)blockIdx.x * COLS_PER_BLOCK + threadIdx.y;
+    if (col < d.ncol) {
+        const int kx = (int)(col / d.ny), ky = (int)(col - (long long)kx * d.ny);
+        const long long o = col * d.P;
+        const double h2 = rkx[kx] * rkx[kx] + rky[ky] * rky[ky];
+        for (int iz = threadIdx.x; iz <= d.nz; iz += 32) {
+            const int km = (int)llround(sqrt(h2 + rkz[iz] * rkz[iz]));
+            int b = (int)((double)km * dki);
+            b = b > kmax ? kmax : b;
+            const double u = (double)f[o + iz], v = (double)f[N + o + iz], w = (double)f[2 * N + o + iz];
+            atomicAdd(&shb[b], u * u + v * v + w * w);
+            atomicAdd(&shc[b], 1ull);
+        }
+    }
+    __syncthreads();
+    for (int b = tid; b <= kmax; b += 32 * COLS_PER_BLOCK) {
+        if (shc[b]) {
+            atomicAdd(&bins[b], shb[b]);
+            atomicAdd(&cnt[b], shc[b]);
+        }
+    }
+}
+template <typename T>
+void op_spec_bins(const Dims &d, cudaStream_t st, const double *rkx, const double *rky, const double *rkz,
+                  const T *f, double dki, int kmax, double *bins, unsigned long long *cnt)
+{
+    const size_t sm = (size_t)(kmax + 1) * (sizeof(double) + sizeof(unsigned long long));
+    k_spec_bins<T><<<col_grid(d), COL_BLOCK, sm, st>>>(d, rkx, rky, rkz, f, dki, kmax, bins, cnt);
+}
+template void op_spec_bins<float>(const Dims &, cudaStream_t, const double *, const double *, const double *,
+                                  const float *, double, int, double *, unsigned long long *);
+template void op_spec_bins<double>(const Dims &, cudaStream_t, const double *, const double *, const double *,
+                                   const double *, double, int, double *, unsigned long long *);
+
 // flat conversions / accumulation over n elements
 template <typename T, typename S>
 __global__ void k_convert(const S *__restrict__ in, T *__restrict__ out, long long n)

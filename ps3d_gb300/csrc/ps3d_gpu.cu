@@ -124,6 +124,10 @@ struct ps3d_gpu_ctx {
     // line-FFT autotuner: ms per launch of each block shape for the passes
     // forward y, forward x, inverse y, inverse x (0 where not timed)
     double tune_ms[4][2] = {{0, 0}, {0, 0}, {0, 0}, {0, 0}};
+    // kinetic-energy spectrum scratch (allocated on first use): rkx, rky,
+    // shell sums, shell counts
+    double *spec_buf = nullptr;
+    int spec_kmax = -1;
 
     Deriv D() const { return Deriv{cx, cy}; }
     Tables tables() const
@@ -951,6 +955,62 @@ template <typename T> int derived_fields(ps3d_gpu_ctx *c, double *hp, double *hd
     return PS3D_OK;
 }
 
+// kinetic-energy shell spectrum (genspec.f90:42-123) of the current vel
+template <typename T> int ke_spectrum(ps3d_gpu_ctx *c, int nmax, double *spec, int *nbins, double *dk_out)
+{
+    const Dims &d = c->d;
+    const long long N = d.nfield;
+    int kmax = 0;
+    for (int kx = 0; kx < d.nx; ++kx)
+        for (int ky = 0; ky < d.ny; ++ky)
+            for (int kz = 0; kz <= d.nz; ++kz) {
+                const int km = (int)std::lround(std::sqrt(c->h_rkx[kx] * c->h_rkx[kx] + c->h_rky[ky] * c->h_rky[ky] +
+                                                          c->h_rkz[kz] * c->h_rkz[kz]));
+                kmax = km > kmax ? km : kmax;
+            }
+    const double dk = (double)kmax / std::sqrt((0.5 * d.nx) * (0.5 * d.nx) + (0.5 * d.ny) * (0.5 * d.ny) +
+                                               (double)d.nz * d.nz);
+    const int nb = kmax + 1;
+    if (!c->spec_buf) {
+        if (!dalloc(c, &c->spec_buf, (size_t)(d.nx + d.ny + 2 * nb) * sizeof(double)))
+            return fail(c, PS3D_ERR_OUT_OF_MEMORY, "ke_spectrum: device allocation failed");
+        cudaMemcpyAsync(c->spec_buf, c->h_rkx.data(), d.nx * sizeof(double), cudaMemcpyHostToDevice, c->st);
+        cudaMemcpyAsync(c->spec_buf + d.nx, c->h_rky.data(), d.ny * sizeof(double), cudaMemcpyHostToDevice, c->st);
+    }
+    double *bins = c->spec_buf + d.nx + d.ny;
+    unsigned long long *cnt = reinterpret_cast<unsigned long long *>(bins + nb);
+    cudaMemsetAsync(bins, 0, 2 * (size_t)nb * sizeof(double), c->st);
+    T *f = tmpf<T>(c, 0);
+    for (int k = 0; k < 3; ++k) xyf<T>(c, tf<T>(c->vel) + k * N, f + k * N);
+    col<T>(c, COL_DCT, f, f);
+    col<T>(c, COL_DCT, f + N, f + N);
+    col<T>(c, COL_DST, f + 2 * N, f + 2 * N);
+    op_spec_bins<T>(d, c->st, c->spec_buf, c->spec_buf + d.nx, c->rkz, f, 1.0 / dk, kmax, bins, cnt);
+    c->launches += 1;
+    std::vector<double> hb(nb);
+    std::vector<unsigned long long> hc(nb);
+    cudaMemcpyAsync(hb.data(), bins, nb * sizeof(double), cudaMemcpyDeviceToHost, c->st);
+    cudaMemcpyAsync(hc.data(), cnt, nb * sizeof(unsigned long long), cudaMemcpyDeviceToHost, c->st);
+    double r1[RED1_N];
+    int rc = energy<T>(c, r1);  // synchronises
+    if (rc) return rc;
+    const double ke = 0.5 * r1[2] * c->ncelli;
+    const double pi = 3.14159265358979323846;
+    const double pref = 4.0 / 3.0 * pi * dk * dk * dk;
+    double tot = 0.0;
+    for (int b = 0; b < nb; ++b) {
+        if (hc[b] > 0)
+            hb[b] = hb[b] * pref * (double)((long long)(b + 1) * (b + 1) * (b + 1) - (long long)b * b * b) /
+                    (double)hc[b];
+        tot += hb[b] * dk;
+    }
+    const double snorm = ke / tot;
+    for (int b = 0; b < nb && b < nmax; ++b) spec[b] = hb[b] * snorm;
+    *nbins = nb;
+    *dk_out = dk;
+    return PS3D_OK;
+}
+
 // setup_fields (utils.f90:136-184)
 template <typename T> int setup_fields(ps3d_gpu_ctx *c, const double *vor_phys, const double *pert, double *te,
                                        double *en)
@@ -1762,6 +1822,14 @@ int ps3d_gpu_derived_fields(ps3d_gpu_ctx *c, double *pres, double *delta)
     int rc = enter(c);
     if (rc) return rc;
     return DISPATCH(c, derived_fields, c, pres, delta);
+}
+
+int ps3d_gpu_ke_spectrum(ps3d_gpu_ctx *c, int nmax, double *spec, int *nbins, double *dk)
+{
+    int rc = enter(c);
+    if (rc) return rc;
+    if (!spec || !nbins || !dk || nmax < 1) return PS3D_ERR_INVALID_ARG;
+    return DISPATCH(c, ke_spectrum, c, nmax, spec, nbins, dk);
 }
 
 int ps3d_gpu_probe(ps3d_gpu_ctx *c, int kind)

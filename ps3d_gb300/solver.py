@@ -239,6 +239,13 @@ class Ps3dGpu:
         self._chk(self.L.ps3d_gpu_derived_fields(self._h, p.ctypes.data, dl.ctypes.data))
         return p, dl
 
+    def ke_spectrum(self, nmax=8192):
+        """(shell spectrum, dk) of the current vel (genspec.f90:42-123)."""
+        spec = np.zeros(nmax)
+        nb, dk = ctypes.c_int(), ctypes.c_double()
+        self._chk(self.L.ps3d_gpu_ke_spectrum(self._h, nmax, _ptr(spec), ctypes.byref(nb), ctypes.byref(dk)))
+        return spec[:nb.value], dk.value
+
     def tuning(self):
         """Line-FFT autotuner result: (shape per pass [fwd y, fwd x, inv y,
         inv x], ms per launch of each shape per pass)."""

@@ -397,3 +397,26 @@ def test_derived_pressure_and_divergence_match_oracle(grid, precision, tol):
     p, dl = g.derived_fields()
     assert rel_l2(p, o.pressure()) < tol
     assert rel_l2(dl, o.horizontal_divergence()) < tol
+
+
+@pytest.mark.parametrize("precision,tol", [("fp64", 1e-10), ("mixed", 1e-5)])
+@pytest.mark.parametrize("grid", [(32, 32, 32), (16, 32, 64)], ids=lambda g: "x".join(map(str, g)))
+def test_ke_spectrum_matches_oracle(grid, precision, tol):
+    """Kinetic-energy shell spectrum (genspec.f90:42-123) against the oracle:
+    same shells and dk, every shell within tol of the largest, sum(spec) dk
+    equal to the domain-average kinetic energy."""
+    nx, ny, nz = grid
+    lo, ex = ic.BASELINE_BOX["lower"], ic.BASELINE_BOX["extent"]
+    vor, pert = ic.beltrami_plus_perturbation(nx, ny, nz, seed=6, amplitude=1e-2)
+    o = oracle.Oracle(nx, ny, nz, lo, ex)
+    g = Ps3dGpu(nx, ny, nz, lo, ex, precision=precision)
+    o.setup_fields(vor, pert)
+    g.setup_fields(vor, pert)
+    o.vor2vel()
+    g.vor2vel()
+    so, dko = o.ke_spectrum()
+    sg, dkg = g.ke_spectrum()
+    assert len(sg) == len(so) and dkg == dko
+    assert np.abs(sg - so).max() <= tol * so.max()
+    ke = o.energy_series()[0]
+    assert abs(sg.sum() * dkg - ke) <= 1e-6 * ke
