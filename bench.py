@@ -138,6 +138,59 @@ def peaks():
         return 6800.0, "fallback"
 
 
+def fp64_peak_tflops(dev):
+    """FP64 peak of this GPU as measured by a cuBLAS DGEMM through torch
+    (plumbing: 2 n^3 flops per 4096^3 product, best of 5)."""
+    try:
+        import torch
+        n = 4096
+        a = torch.randn(n, n, dtype=torch.float64, device=f"cuda:{dev}")
+        b = torch.randn(n, n, dtype=torch.float64, device=f"cuda:{dev}")
+        torch.matmul(a, b)
+        best = None
+        for _ in range(5):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            torch.matmul(a, b)
+            e1.record()
+            torch.cuda.synchronize()
+            ms = e0.elapsed_time(e1)
+            best = ms if best is None else min(best, ms)
+        del a, b
+        torch.cuda.empty_cache()
+        return 2.0 * n ** 3 / (best * 1e-3) / 1e12
+    except Exception:
+        return None
+
+
+def cufft_comparator(n, dev):
+    """cuFFT (torch.fft.rfft2 / irfft2 over x and y of an (n, n, P) FP32 field,
+    z contiguous as here) timed as a comparator for one forward and one
+    inverse horizontal transform."""
+    try:
+        import torch
+        P = (n + 1 + 7) // 8 * 8
+        x = torch.randn(n, n, P, dtype=torch.float32, device=f"cuda:{dev}")
+        def t(fn, reps=5):
+            fn()
+            torch.cuda.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            for _ in range(reps):
+                out = fn()
+            e1.record()
+            torch.cuda.synchronize()
+            return e0.elapsed_time(e1) / reps, out
+        fwd_ms, X = t(lambda: torch.fft.rfft2(x, dim=(0, 1)))
+        inv_ms, _ = t(lambda: torch.fft.irfft2(X, s=(n, n), dim=(0, 1)))
+        del x, X
+        torch.cuda.empty_cache()
+        return {"forward_xy_ms": fwd_ms, "inverse_xy_ms": inv_ms,
+                "how": "torch.fft.rfft2 / irfft2 (cuFFT) over dims 0, 1 of an (n, n, P) float32 field"}
+    except Exception as e:
+        return {"unavailable": str(e)[:200]}
+
+
 def cpu_sample(n_cpu, steps=1):
     """Time the CPU oracle: `steps` advances at n_cpu^3 after one warm-up."""
     import oracle
@@ -300,6 +353,25 @@ def run_gpu(args, rank, world, dist):
                "h2d_bytes_per_step": nb, "d2h_bytes_per_step": nb, "steps": e2e_steps,
                "api": "ps3d_gpu_advance_host (svor FP64 in/out)", "host_buffer": host_kind}
 
+    # FP64 form against the FP64 ALU roofline (SURVEY §8(d) flop model:
+    # 49 transforms at 2.5 N log2 n each plus ~300 flop per point for the
+    # eigen-solve) and cuFFT as a comparator for the horizontal transforms
+    if fp64 is not None:
+        pk = fp64_peak_tflops(dev)
+        N = float(n) ** 2 * (n + 1)
+        flops = 49 * 2.5 * N * (3 * np.log2(n)) + 300.0 * N
+        ach = flops / (fp64["ms_per_step"] * 1e-3) / 1e12
+        fp64["alu"] = {"flops_per_step": flops, "achieved_tflops": ach, "peak_tflops": pk,
+                       "frac": (ach / pk) if pk else None,
+                       "peak_source": "cuBLAS DGEMM 4096^3 through torch, best of 5"}
+    cufft = None
+    if rank == 0:
+        cufft = cufft_comparator(n, dev)
+        lp = {p["kernel"]: p["ms_per_launch"] for p in roofline["probes"]}
+        ours = lp.get("k_lines32 (y lines)", 0.0) + lp.get("k_lines32 (x lines)", 0.0)
+        if isinstance(cufft, dict) and "forward_xy_ms" in cufft:
+            cufft["ours_xy_pass_pair_ms"] = ours
+
     cpu = None
     if rank == 0 and not args.skip_cpu:
         csec, crate = cpu_sample(args.cpu_n)
@@ -321,6 +393,7 @@ def run_gpu(args, rank, world, dist):
             "gpu_launches": launches, "clocks": clocks,
             "device_bytes": gm.device_bytes,
             "line_fft_autotune": dict(zip(("shape", "ms_per_launch"), gm.tuning())),
+            "cufft_comparator": cufft,
         }
         print(json.dumps(line), flush=True)
     gm.close()

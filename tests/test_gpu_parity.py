@@ -420,3 +420,27 @@ def test_ke_spectrum_matches_oracle(grid, precision, tol):
     assert np.abs(sg - so).max() <= tol * so.max()
     ke = o.energy_series()[0]
     assert abs(sg.sum() * dkg - ke) <= 1e-6 * ke
+
+
+@pytest.mark.parametrize("grid,stepper", [((64, 64, 64), "cn2"), ((32, 32, 32), "cn2"),
+                                          ((64, 32, 128), "impl-diff-rk4")],
+                         ids=["cn2-64", "cn2-32", "rk4-64x32x128"])
+def test_mixed_steps_other_steppers_and_shapes(grid, stepper):
+    """Mixed form over ten steps against the FP64 oracle for the cn2 stepper
+    and a non-cubic grid: solenoidal state within 1e-6."""
+    nx, ny, nz = grid
+    lo, ex = ic.BASELINE_BOX["lower"], ic.BASELINE_BOX["extent"]
+    vor, pert = ic.beltrami_plus_perturbation(nx, ny, nz, seed=10)
+    o = oracle.Oracle(nx, ny, nz, lo, ex, cflmax=0.5, stepper=stepper)
+    g = Ps3dGpu(nx, ny, nz, lo, ex, cflmax=0.5, stepper=stepper, precision="mixed")
+    o.setup_fields(vor, pert)
+    g.setup_fields(vor, pert)
+    t_o = t_g = 0.0
+    for _ in range(10):
+        t_g, dg = g.advance(t_g)
+        t_o, do = o.advance(t_o)
+    o.vor2vel()
+    g.vor2vel()
+    err = rel_l2(g.get("svor"), o.get("svor"))
+    assert err < 1.0e-6, err
+    assert abs(t_g - t_o) <= 1e-6 * t_o
