@@ -400,9 +400,15 @@ def run_gpu(args, rank, world, dist):
 
 
 def pinned_like(shape):
-    """Page-locked host array: a pinned torch tensor viewed through numpy
-    (torch is plumbing here), else cudaHostAlloc through libcudart, else
-    pageable.  Returns (array, how, owner); keep owner alive with the array."""
+    """Page-locked host array: from the library (ps3d_gpu_host_alloc), else a
+    pinned torch tensor viewed through numpy, else cudaHostAlloc through
+    libcudart, else pageable.  Returns (array, how, owner); keep owner alive with the array."""
+    try:
+        from ps3d_gb300.solver import PinnedArray
+        pa = PinnedArray(shape)
+        return pa.array, "ps3d_gpu_host_alloc", pa
+    except Exception:
+        pass
     try:
         import torch
         t = torch.empty(tuple(shape), dtype=torch.float64, pin_memory=True)

@@ -189,6 +189,13 @@ int ps3d_gpu_derived_fields(ps3d_gpu_ctx *ctx, double *pres, double *delta);
  * kinetic energy.  nbins = kmax + 1 shells (at most nmax written). */
 int ps3d_gpu_ke_spectrum(ps3d_gpu_ctx *ctx, int nmax, double *spec, int *nbins, double *dk);
 
+/* Page-locked host memory from the library's CUDA runtime (no reference
+ * counterpart): host arrays passed to ps3d_gpu_advance_host (or any
+ * transfer) move at the full host-device bandwidth when allocated here; a
+ * Fortran driver can map its svor onto it with c_f_pointer. */
+int ps3d_gpu_host_alloc(size_t bytes, void **ptr);
+int ps3d_gpu_host_free(void *ptr);
+
 /* Captured steps (no reference counterpart): nsteps advances of the mixed
  * form with impl-diff-rk4, each one CUDA graph launch with adapt's scalar
  * logic on the device (no host synchronisation inside a step).  Same

@@ -28,7 +28,7 @@ EXPORTS = [
     "ps3d_gpu_launch_count", "ps3d_gpu_synchronize", "ps3d_gpu_probe", "ps3d_gpu_probe_result",
     "ps3d_gpu_energy_series_noalloc", "ps3d_gpu_advance_graph", "ps3d_gpu_batch_advance",
     "ps3d_gpu_tuning", "ps3d_gpu_set_tuning", "ps3d_gpu_derived_fields",
-    "ps3d_gpu_ke_spectrum",
+    "ps3d_gpu_ke_spectrum", "ps3d_gpu_host_alloc", "ps3d_gpu_host_free",
 ]
 
 
@@ -111,6 +111,8 @@ def lib(build_if_missing=True):
     L.ps3d_gpu_time_advance.argtypes = [_vp, _dp, ctypes.c_int, _dp]
     L.ps3d_gpu_tuning.argtypes = [_vp, ctypes.POINTER(ctypes.c_int), _dp]
     L.ps3d_gpu_derived_fields.argtypes = [_vp, ctypes.c_void_p, ctypes.c_void_p]
+    L.ps3d_gpu_host_alloc.argtypes = [ctypes.c_size_t, ctypes.POINTER(ctypes.c_void_p)]
+    L.ps3d_gpu_host_free.argtypes = [ctypes.c_void_p]
     L.ps3d_gpu_ke_spectrum.argtypes = [_vp, ctypes.c_int, _dp, ctypes.POINTER(ctypes.c_int), _dp]
     L.ps3d_gpu_set_tuning.argtypes = [_vp, ctypes.POINTER(ctypes.c_int)]
     L.ps3d_gpu_advance_graph.argtypes = [_vp, _dp, ctypes.c_int, ctypes.c_void_p, _dp]

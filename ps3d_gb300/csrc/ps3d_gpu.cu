@@ -1638,11 +1638,22 @@ int ps3d_gpu_advance_host(ps3d_gpu_ctx *c, double *svor, double *t, ps3d_gpu_dia
     if (rc) return rc;
     if (!svor || !t) return PS3D_ERR_INVALID_ARG;
     const Dims &d = c->d;
-    // one linear copy each way through a staging array in host layout (the
-    // RK accumulator svorf, free outside a step); the device re-pitches
     const size_t bytes = (size_t)3 * d.ncol * (d.nz + 1) * sizeof(double);
-    double *stage = c->svorf;
-    cudaMemcpyAsync(stage, svor, bytes, cudaMemcpyHostToDevice, c->st);
+    // Page-locked host memory is read and written by the re-pitching
+    // kernels themselves over the host link (zero copy); other host memory
+    // goes through one linear copy each way into a staging array in host
+    // layout (the RK accumulator svorf, free outside a step).
+    double *mapped = nullptr;
+    {
+        cudaPointerAttributes pa;
+        if (cudaPointerGetAttributes(&pa, svor) == cudaSuccess && pa.type == cudaMemoryTypeHost) {
+            void *dp = nullptr;
+            if (cudaHostGetDevicePointer(&dp, svor, 0) == cudaSuccess) mapped = static_cast<double *>(dp);
+        }
+        cudaGetLastError();
+    }
+    double *stage = mapped ? mapped : c->svorf;
+    if (!mapped) cudaMemcpyAsync(stage, svor, bytes, cudaMemcpyHostToDevice, c->st);
     cudaMemsetAsync(c->flag, 0, sizeof(int), c->st);
     op_unpack_cols(d, c->st, stage, c->svor, 3, c->flag);
     c->launches += 1;
@@ -1659,7 +1670,7 @@ int ps3d_gpu_advance_host(ps3d_gpu_ctx *c, double *svor, double *t, ps3d_gpu_dia
     if (rc) return rc;
     op_pack_cols(d, c->st, c->svor, stage, 3);
     c->launches += 1;
-    cudaMemcpyAsync(svor, stage, bytes, cudaMemcpyDeviceToHost, c->st);
+    if (!mapped) cudaMemcpyAsync(svor, stage, bytes, cudaMemcpyDeviceToHost, c->st);
     return sync_check(c, "advance_host");
 }
 
@@ -1830,6 +1841,27 @@ int ps3d_gpu_ke_spectrum(ps3d_gpu_ctx *c, int nmax, double *spec, int *nbins, do
     if (rc) return rc;
     if (!spec || !nbins || !dk || nmax < 1) return PS3D_ERR_INVALID_ARG;
     return DISPATCH(c, ke_spectrum, c, nmax, spec, nbins, dk);
+}
+
+int ps3d_gpu_host_alloc(size_t bytes, void **ptr)
+{
+    if (!ptr || bytes == 0) return PS3D_ERR_INVALID_ARG;
+    *ptr = nullptr;
+    if (cudaHostAlloc(ptr, bytes, cudaHostAllocPortable) != cudaSuccess) {
+        cudaGetLastError();
+        *ptr = nullptr;
+        return PS3D_ERR_OUT_OF_MEMORY;
+    }
+    return PS3D_OK;
+}
+
+int ps3d_gpu_host_free(void *ptr)
+{
+    if (ptr && cudaFreeHost(ptr) != cudaSuccess) {
+        cudaGetLastError();
+        return PS3D_ERR_CUDA;
+    }
+    return PS3D_OK;
 }
 
 int ps3d_gpu_probe(ps3d_gpu_ctx *c, int kind)

@@ -310,3 +310,30 @@ def batch_advance(models, ts, nsteps):
         msgs = [L.ps3d_gpu_last_error(m._h).decode() for m in models]
         raise Ps3dError(rc, " | ".join(x for x in msgs if x))
     return list(tt), ms.value
+
+
+class PinnedArray:
+    """A page-locked FP64 host array from the library (ps3d_gpu_host_alloc);
+    `.array` is the numpy view, valid until close()."""
+
+    def __init__(self, shape):
+        self.L = _lib.lib()
+        n = int(np.prod(shape)) * 8
+        self._p = ctypes.c_void_p()
+        rc = self.L.ps3d_gpu_host_alloc(n, ctypes.byref(self._p))
+        if rc:
+            raise Ps3dError(rc, "ps3d_gpu_host_alloc")
+        buf = (ctypes.c_double * (n // 8)).from_address(self._p.value)
+        self.array = np.frombuffer(buf, dtype=np.float64).reshape(shape)
+
+    def close(self):
+        if self._p:
+            self.array = None
+            self.L.ps3d_gpu_host_free(self._p)
+            self._p = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
