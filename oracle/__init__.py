@@ -31,6 +31,10 @@ class Config(ctypes.Structure):
         ("roll_mean_win_size", ctypes.c_int), ("nthreads", ctypes.c_int),
         ("hold_source", ctypes.c_int),
         ("f_cor", ctypes.c_double * 3),
+        ("buoyancy", ctypes.c_int), ("bfsq", ctypes.c_double), ("bfsq_given", ctypes.c_int),
+        ("buoy_nnu", ctypes.c_int), ("buoy_prediss", ctypes.c_double),
+        ("buoy_pretype", ctypes.c_int), ("buoy_length_scale", ctypes.c_int),
+        ("buoy_roll_mean_win_size", ctypes.c_int),
     ]
 
 
@@ -38,7 +42,8 @@ class Diag(ctypes.Structure):
     _fields_ = [(n, ctypes.c_double) for n in (
         "t", "dt", "ke", "en", "hel", "vortmax", "vortrms", "vorch")] + [
         ("vormean", ctypes.c_double * 3)] + [(n, ctypes.c_double) for n in (
-            "ggmax", "usggmax", "lsggmax", "umax", "vmax", "wmax", "bfmax", "rmv", "pref")]
+            "ggmax", "usggmax", "lsggmax", "umax", "vmax", "wmax", "bfmax", "rmv", "pref",
+            "rmb", "bpref")]
 
     def as_dict(self):
         d = {n: getattr(self, n) for n, _ in self._fields_ if n != "vormean"}
@@ -47,14 +52,17 @@ class Diag(ctypes.Structure):
 
 
 PRETYPES = {"constant": 0, "vorch": 1, "bfmax": 2, "roll-mean-max-strain": 3,
-            "max-strain": 4, "us-max-strain": 5}
+            "max-strain": 4, "us-max-strain": 5, "roll-mean-bfmax": 6}
 LENGTH_SCALES = {"Kolmogorov": 0, "geophysical": 1}
 FILTERS = {"Hou & Li": 0, "2/3-rule": 1}
 STEPPERS = {"impl-diff-rk4": 0, "cn2": 1}
 TABLES = {"k2l2": 0, "k2l2i": 1, "filt": 2, "green": 3, "phim": 4, "phip": 5,
           "thetam": 6, "thetap": 7, "dthetam": 8, "dthetap": 9, "gamtop": 10,
-          "gambot": 11, "vhdis": 12, "rkx": 13, "rky": 14, "rkz": 15}
-FIELDS = {"svor": 0, "vor": 1, "vel": 2, "svel": 3, "svorts": 4}
+          "gambot": 11, "vhdis": 12, "rkx": 13, "rky": 14, "rkz": 15,
+          "dphim": 16, "dphip": 17, "bhdis": 18, "bbarz": 19}
+FIELDS = {"svor": 0, "vor": 1, "vel": 2, "svel": 3, "svorts": 4,
+          "sbuoy": 5, "buoy": 6, "sbuoys": 7}
+SCALAR_FIELDS = ("sbuoy", "buoy", "sbuoys")
 
 _dp = ctypes.POINTER(ctypes.c_double)
 
@@ -98,6 +106,15 @@ def lib():
         L.ps3o_pressure.argtypes = [vp, _dp]
         L.ps3o_horizontal_divergence.argtypes = [vp, _dp]
         L.ps3o_ke_spectrum.argtypes = [vp, ctypes.c_int, _dp, _dp]
+        L.ps3o_setup_fields_buoyancy.argtypes = [vp, _dp, _dp, _dp, _dp, _dp]
+        L.ps3o_get_bfsq.argtypes = [vp]
+        L.ps3o_get_bfsq.restype = ctypes.c_double
+        L.ps3o_get_bvisc.argtypes = [vp]
+        L.ps3o_get_bvisc.restype = ctypes.c_double
+        L.ps3o_diffz.argtypes = [vp, _dp, _dp]
+        L.ps3o_buoyancy_tendency.argtypes = [vp]
+        L.ps3o_buoyancy_diagnostics.argtypes = [vp, _dp]
+        L.ps3o_set_diffusion_vb.argtypes = [vp, ctypes.c_double, ctypes.c_double, ctypes.c_double]
         L.ps3o_forfft.argtypes = [ctypes.c_int, ctypes.c_int, _dp, _dp, _dp, ctypes.POINTER(ctypes.c_int)]
         L.ps3o_revfft.argtypes = L.ps3o_forfft.argtypes
         L.ps3o_dct.argtypes = [ctypes.c_int, ctypes.c_int, _dp, _dp, _dp, _dp, ctypes.POINTER(ctypes.c_int)]
@@ -116,7 +133,9 @@ def make_config(nx, ny, nz, lower, extent, nnu=3, prediss=30.0, pretype="vorch",
                 length_scale="Kolmogorov", filtering="Hou & Li",
                 stepper="impl-diff-rk4", cflmax=0.8, alpha=0.1, time_limit=1.0e30,
                 roll_mean_win_size=1000, nthreads=0, hold_source=0,
-                f_cor=(0.0, 0.0, 0.0)):
+                f_cor=(0.0, 0.0, 0.0), buoyancy=False, bfsq=None, buoy_nnu=3,
+                buoy_prediss=30.0, buoy_pretype="bfmax", buoy_length_scale="Kolmogorov",
+                buoy_roll_mean_win_size=1000):
     c = Config()
     c.nx, c.ny, c.nz, c.nnu = nx, ny, nz, nnu
     c.lower[:] = list(lower)
@@ -130,6 +149,14 @@ def make_config(nx, ny, nz, lower, extent, nnu=3, prediss=30.0, pretype="vorch",
     c.roll_mean_win_size, c.nthreads = roll_mean_win_size, nthreads
     c.hold_source = int(hold_source)
     c.f_cor[:] = list(f_cor)
+    c.buoyancy = int(bool(buoyancy))
+    c.bfsq = 0.0 if bfsq is None else float(bfsq)
+    c.bfsq_given = int(bfsq is not None)
+    c.buoy_nnu, c.buoy_prediss = buoy_nnu, buoy_prediss
+    c.buoy_pretype = PRETYPES[buoy_pretype] if isinstance(buoy_pretype, str) else int(buoy_pretype)
+    c.buoy_length_scale = (LENGTH_SCALES[buoy_length_scale] if isinstance(buoy_length_scale, str)
+                           else int(buoy_length_scale))
+    c.buoy_roll_mean_win_size = buoy_roll_mean_win_size
     return c
 
 
@@ -238,24 +265,31 @@ class Oracle:
         w = TABLES[name]
         n = {0: self.nx * self.ny, 1: self.nx * self.ny, 12: self.nx * self.ny,
              10: self.nz + 1, 11: self.nz + 1, 13: self.nx, 14: self.ny,
-             15: self.nz + 1}.get(w, self.nx * self.ny * (self.nz + 1))
+             15: self.nz + 1, 18: self.nx * self.ny,
+             19: self.nz + 1}.get(w, self.nx * self.ny * (self.nz + 1))
         out = np.zeros(n)
-        lib().ps3o_get_table(self._h, w, _ptr(out))
+        if lib().ps3o_get_table(self._h, w, _ptr(out)) != 0:
+            raise ValueError(f"table {name} not available")
         if n == self.nx * self.ny * (self.nz + 1):
             return out.reshape(self.shape)
         if n == self.nx * self.ny:
             return out.reshape(self.nx, self.ny)
         return out
 
+    def _fshape(self, name):
+        return self.shape if name in SCALAR_FIELDS else (3,) + self.shape
+
     def get(self, name):
-        out = np.zeros((3,) + self.shape)
-        lib().ps3o_get_field(self._h, FIELDS[name], _ptr(out))
+        out = np.zeros(self._fshape(name))
+        if lib().ps3o_get_field(self._h, FIELDS[name], _ptr(out)) != 0:
+            raise ValueError(f"field {name} not available")
         return out
 
     def set(self, name, a):
         a = np.ascontiguousarray(a, dtype=np.float64)
-        assert a.shape == (3,) + self.shape
-        lib().ps3o_set_field(self._h, FIELDS[name], _ptr(a))
+        assert a.shape == self._fshape(name)
+        if lib().ps3o_set_field(self._h, FIELDS[name], _ptr(a)) != 0:
+            raise ValueError(f"field {name} not available")
 
     @property
     def ini_vor_mean(self):
@@ -272,7 +306,8 @@ class Oracle:
     def vvisc(self):
         return lib().ps3o_get_vvisc(self._h)
 
-    def setup_fields(self, vor_phys, pert=None):
+    def setup_fields(self, vor_phys, pert=None, buoy=None):
+        """setup_fields; buoy is the total physical buoyancy (buoyancy runs)."""
         vor_phys = np.ascontiguousarray(vor_phys, dtype=np.float64)
         assert vor_phys.shape == (3,) + self.shape
         pp = None
@@ -281,8 +316,39 @@ class Oracle:
             assert pert.shape == (3,) + self.shape
             pp = _ptr(pert)
         te, en = ctypes.c_double(), ctypes.c_double()
-        lib().ps3o_setup_fields(self._h, _ptr(vor_phys), pp, ctypes.byref(te), ctypes.byref(en))
+        if self.cfg.buoyancy:
+            buoy = np.zeros(self.shape) if buoy is None else np.ascontiguousarray(buoy, dtype=np.float64)
+            assert buoy.shape == self.shape
+            lib().ps3o_setup_fields_buoyancy(self._h, _ptr(vor_phys), pp, _ptr(buoy), ctypes.byref(te),
+                                             ctypes.byref(en))
+        else:
+            lib().ps3o_setup_fields(self._h, _ptr(vor_phys), pp, ctypes.byref(te), ctypes.byref(en))
         return te.value, en.value
+
+    @property
+    def bfsq(self):
+        return lib().ps3o_get_bfsq(self._h)
+
+    @property
+    def bvisc(self):
+        return lib().ps3o_get_bvisc(self._h)
+
+    def diffz(self, fs):
+        fs = self._s(fs)
+        out = np.zeros(self.shape)
+        if lib().ps3o_diffz(self._h, _ptr(fs), _ptr(out)) != 0:
+            raise ValueError("diffz needs a model built with buoyancy")
+        return out
+    def buoyancy_tendency(self): lib().ps3o_buoyancy_tendency(self._h)
+
+    def buoyancy_diagnostics(self):
+        """(ape, gradb integral, min static stability, min Richardson number)"""
+        out = np.zeros(4)
+        lib().ps3o_buoyancy_diagnostics(self._h, _ptr(out))
+        return tuple(out)
+
+    def set_diffusion_vb(self, dt, vpref, bpref):
+        lib().ps3o_set_diffusion_vb(self._h, dt, vpref, bpref)
 
     def init_diffusion(self, te, en):
         lib().ps3o_init_diffusion(self._h, te, en)

@@ -22,6 +22,13 @@
 
 #include "ps3d_oracle.h"
 
+/* rolling_mean_t (rolling_mean.f90:6-69) */
+typedef struct {
+    double *hist;
+    int inew, iold, filled, len;
+    double sma;
+} ps3o_roll;
+
 struct ps3o_model {
     ps3o_config cfg;
     int nx, ny, nz, nz1;
@@ -43,12 +50,14 @@ struct ps3o_model {
     double ini_vor_mean[2];
     /* impl-diff-rk4 stepper state */
     double *svori, *svorf, *epq, *emq;
-    /* rolling mean of gamma_max */
-    double *rm_hist;
-    int rm_inew, rm_iold, rm_filled, rm_len;
-    double rm_sma;
+    /* rolling means of gamma_max (vorticity) and bfmax (buoyancy) */
+    ps3o_roll rv, rb;
     /* diagnostics kept between adapt and set_diffusion */
-    double vorch, ggmax, usggmax, lsggmax, bfmax, rmv;
+    double vorch, ggmax, usggmax, lsggmax, bfmax, rmv, rmb;
+    /* buoyancy (ENABLE_BUOYANCY): tables, fields, stepper state */
+    double *dphim, *dphip, *bhdis, *bdiss, *bbarz;
+    double *sbuoy, *buoy, *sbuoys, *bsm, *sbuoyi, *sbuoyf, *bpq, *bmq;
+    double bfsq, bvisc;
 };
 
 #define IDX(m, iz, iy, ix) ((size_t)(iz) + (size_t)(m)->nz1 * ((size_t)(iy) + (size_t)(m)->ny * (size_t)(ix)))
@@ -71,6 +80,15 @@ static double ipow(double x, int p)
         e >>= 1;
     }
     return p < 0 ? 1.0 / r : r;
+}
+
+/* rolling_mean_t%alloc (rolling_mean.f90:21-31); default window 1000
+ * (options.f90:66) */
+static void roll_init(ps3o_roll *r, int len)
+{
+    r->len = len > 0 ? len : 1000;
+    r->hist = dalloc((size_t)r->len);
+    r->inew = 1; r->iold = 1; r->filled = 0; r->sma = 0.0;
 }
 
 /* ====================================================================== */
@@ -104,6 +122,10 @@ static void set_hyperbolic_functions(ps3o_model *m, int kx, int ky,
         m->thetap[q] = k2ifac * (R * Lp * phm - Q * Lm * php);
         m->dthetam[q] = -k2ifac * ((Q * Lp - 1.0) * dphm - R * Lm * dphp);
         m->dthetap[q] = -k2ifac * ((Q * Lm - 1.0) * dphp - R * Lp * dphm);
+        if (m->dphim) {
+            m->dphim[q] = dphm;
+            m->dphip[q] = dphp;
+        }
     }
 }
 
@@ -172,6 +194,9 @@ int ps3o_create(const ps3o_config *cfg, ps3o_model **out)
     m->thetam = dalloc(N); m->thetap = dalloc(N);
     m->dthetam = dalloc(N); m->dthetap = dalloc(N);
     m->gamtop = dalloc(nz + 1); m->gambot = dalloc(nz + 1);
+    if (cfg->buoyancy) {
+        m->dphim = dalloc(N); m->dphip = dalloc(N);
+    }
     for (int kx = 0; kx < nx; ++kx)
         for (int ky = 0; ky < ny; ++ky)
             m->k2l2[PIDX(m, ky, kx)] = m->rkx[kx] * m->rkx[kx] + m->rky[ky] * m->rky[ky];
@@ -242,6 +267,10 @@ int ps3o_create(const ps3o_config *cfg, ps3o_model **out)
             m->phim[q] = zm[iz] / m->extent[2];
             m->phip[q] = zp[iz] / m->extent[2];
             m->thetam[q] = m->thetap[q] = m->dthetam[q] = m->dthetap[q] = 0.0;
+            if (m->dphim) {
+                m->dphim[q] = -1.0 / m->extent[2];
+                m->dphip[q] = 1.0 / m->extent[2];
+            }
         }
         for (int iz = 0; iz <= nz; ++iz) {
             const double php = m->phip[IDX(m, iz, 0, 0)];
@@ -257,9 +286,22 @@ int ps3o_create(const ps3o_config *cfg, ps3o_model **out)
     m->vdiss = dalloc(P);
     m->svori = dalloc(3 * N); m->svorf = dalloc(3 * N);
     m->epq = dalloc(P); m->emq = dalloc(P);
-    m->rm_len = cfg->roll_mean_win_size > 0 ? cfg->roll_mean_win_size : 1000;
-    m->rm_hist = dalloc(m->rm_len);
-    m->rm_inew = 1; m->rm_iold = 1; m->rm_filled = 0; m->rm_sma = 0.0;
+    roll_init(&m->rv, cfg->roll_mean_win_size);
+    roll_init(&m->rb, cfg->buoy_roll_mean_win_size);
+    m->bfsq = cfg->bfsq;
+    m->bbarz = dalloc(nz + 1);
+    if (cfg->buoyancy) {
+        m->bhdis = dalloc(P); m->bdiss = dalloc(P);
+        m->sbuoy = dalloc(N); m->buoy = dalloc(N); m->sbuoys = dalloc(N); m->bsm = dalloc(N);
+        m->sbuoyi = dalloc(N); m->sbuoyf = dalloc(N);
+        m->bpq = dalloc(P); m->bmq = dalloc(P);
+        if (!m->dphim || !m->dphip || !m->sbuoy || !m->buoy || !m->sbuoys || !m->bsm || !m->sbuoyi ||
+            !m->sbuoyf) {
+            ps3o_destroy(m);
+            return 2;
+        }
+        for (int iz = 0; iz <= nz; ++iz) m->bbarz[iz] = m->bfsq * (m->lower[2] + m->dx[2] * (double)iz);
+    }
     if (!m->svor || !m->vor || !m->vel || !m->svel || !m->svorts || !m->vortsm ||
         !m->svori || !m->svorf || !m->phim || !m->dthetap) {
         ps3o_destroy(m);
@@ -276,7 +318,9 @@ void ps3o_destroy(ps3o_model *m)
                     m->rkz, m->rkzi, m->k2l2, m->k2l2i, m->filt, m->green, m->phim,
                     m->phip, m->thetam, m->thetap, m->dthetam, m->dthetap, m->gamtop,
                     m->gambot, m->vhdis, m->svor, m->vor, m->vel, m->svel, m->svorts,
-                    m->vortsm, m->vdiss, m->svori, m->svorf, m->epq, m->emq, m->rm_hist};
+                    m->vortsm, m->vdiss, m->svori, m->svorf, m->epq, m->emq, m->rv.hist,
+                    m->rb.hist, m->dphim, m->dphip, m->bhdis, m->bdiss, m->bbarz, m->sbuoy,
+                    m->buoy, m->sbuoys, m->bsm, m->sbuoyi, m->sbuoyf, m->bpq, m->bmq};
     for (size_t i = 0; i < sizeof(ps) / sizeof(ps[0]); ++i) free(ps[i]);
     free(m);
 }
@@ -594,9 +638,63 @@ void ps3o_vor2vel(ps3o_model *m)
 /* ====================================================================== */
 /* vorticity_tendency / source (inversion.f90:298-388)                     */
 /* ====================================================================== */
+/* diffz (inversion_utils.f90:683-719): the linear part from the boundary
+ * rows and dphim/dphip, the sine series differentiated into a cosine series
+ * and transformed to semi-spectral space, then decomposed */
+int ps3o_diffz(ps3o_model *m, const double *fs, double *ds)
+{
+    if (!m->dphim) return 1;
+    const int nz = m->nz;
+    const long nc = (long)m->ncol;
+    double *as = dalloc(m->nfield);
+#pragma omp parallel for schedule(static)
+    for (long c = 0; c < nc; ++c) {
+        const size_t o = (size_t)c * m->nz1;
+        const double f0 = fs[o], fn = fs[o + nz];
+        for (int iz = 0; iz <= nz; ++iz) ds[o + iz] = f0 * m->dphim[o + iz] + fn * m->dphip[o + iz];
+        as[o] = 0.0;
+        for (int kz = 1; kz < nz; ++kz) as[o + kz] = m->rkz[kz] * fs[o + kz];
+        as[o + nz] = 0.0;
+    }
+    ps3o_fftcosine(m, as);
+    for (size_t i = 0; i < m->nfield; ++i) ds[i] = ds[i] + as[i];
+    ps3o_decompose_semi_spectral(m, ds);
+    free(as);
+    return 0;
+}
+
+/* buoyancy_tendency (inversion.f90:232-292): b_t = -div(u b) - N^2 w in flux
+ * form, each flux decomposed, differentiated and combined back */
+void ps3o_buoyancy_tendency(ps3o_model *m)
+{
+    const size_t N = m->nfield;
+    double *fp = dalloc(N), *fs = dalloc(N), *ds = dalloc(N), *btend = dalloc(N);
+    const double *u = m->vel, *v = m->vel + N, *w = m->vel + 2 * N;
+    ps3o_combine_physical(m, m->sbuoy, m->buoy);
+    for (size_t i = 0; i < N; ++i) fp[i] = u[i] * m->buoy[i];
+    ps3o_decompose_physical(m, fp, fs);
+    ps3o_diffx(m, fs, ds);
+    ps3o_combine_physical(m, ds, btend);
+    for (size_t i = 0; i < N; ++i) fp[i] = v[i] * m->buoy[i];
+    ps3o_decompose_physical(m, fp, fs);
+    ps3o_diffy(m, fs, ds);
+    ps3o_combine_physical(m, ds, fp);
+    for (size_t i = 0; i < N; ++i) btend[i] = -btend[i] - fp[i];
+    for (size_t i = 0; i < N; ++i) fp[i] = w[i] * m->buoy[i];
+    ps3o_decompose_physical(m, fp, fs);
+    ps3o_diffz(m, fs, ds);
+    ps3o_combine_physical(m, ds, fp);
+    for (size_t i = 0; i < N; ++i) btend[i] = btend[i] - m->bfsq * w[i] - fp[i];
+    ps3o_decompose_physical(m, btend, m->sbuoys);
+    free(fp); free(fs); free(ds); free(btend);
+}
+
+/* source (inversion.f90:376-388): buoyancy_tendency, then
+ * vorticity_tendency (:298-371) */
 void ps3o_source(ps3o_model *m)
 {
     const size_t N = m->nfield;
+    if (m->cfg.buoyancy) ps3o_buoyancy_tendency(m);
     double *fp = dalloc(N), *gp = dalloc(N), *p = dalloc(N), *q = dalloc(N), *r = dalloc(N);
     double *u = m->vel, *v = m->vel + N, *w = m->vel + 2 * N;
     double *xi = m->vor, *eta = m->vor + N, *zeta = m->vor + 2 * N;
@@ -607,8 +705,11 @@ void ps3o_source(ps3o_model *m)
         double *vv = m->vor + nc * N;
         for (size_t i = 0; i < N; ++i) vv[i] = vv[i] + f;
     }
-    /* r = u*eta - v*xi */
+    /* r = u*eta - v*xi (+ b) */
+    if (m->cfg.buoyancy) ps3o_combine_physical(m, m->sbuoy, m->buoy);
     for (size_t i = 0; i < N; ++i) fp[i] = u[i] * eta[i] - v[i] * xi[i];
+    if (m->cfg.buoyancy)
+        for (size_t i = 0; i < N; ++i) fp[i] = fp[i] + m->buoy[i];
     ps3o_decompose_physical(m, fp, r);
     /* q = w*xi - u*zeta */
     for (size_t i = 0; i < N; ++i) fp[i] = w[i] * xi[i] - u[i] * zeta[i];
@@ -783,45 +884,57 @@ int ps3o_jacobi_eigenvalues(double a[9], double D[3])
 #undef AM
 
 /* rolling_mean_t%get_next (rolling_mean.f90:36-69), 1-based indices kept */
-double ps3o_rolling_mean_next(ps3o_model *m, double vnew)
+static double roll_next(ps3o_roll *r, double vnew)
 {
-    const int L = m->rm_len;
-    if (m->rm_filled) {
-        const double vold = m->rm_hist[m->rm_iold - 1];
-        m->rm_iold = m->rm_iold % L + 1;
-        m->rm_sma = m->rm_sma + (vnew - vold) / (double)L;
-        m->rm_hist[m->rm_inew - 1] = vnew;
-        m->rm_inew = m->rm_inew % L + 1;
+    const int L = r->len;
+    if (r->filled) {
+        const double vold = r->hist[r->iold - 1];
+        r->iold = r->iold % L + 1;
+        r->sma = r->sma + (vnew - vold) / (double)L;
+        r->hist[r->inew - 1] = vnew;
+        r->inew = r->inew % L + 1;
     } else {
-        m->rm_hist[m->rm_inew - 1] = vnew;
+        r->hist[r->inew - 1] = vnew;
         double s = 0.0;
-        for (int i = 0; i < m->rm_inew; ++i) s += m->rm_hist[i];
-        m->rm_sma = s / (double)m->rm_inew;
-        m->rm_filled = (L == m->rm_inew);
-        m->rm_inew = m->rm_inew % L + 1;
+        for (int i = 0; i < r->inew; ++i) s += r->hist[i];
+        r->sma = s / (double)r->inew;
+        r->filled = (L == r->inew);
+        r->inew = r->inew % L + 1;
     }
-    return m->rm_sma;
+    return r->sma;
 }
+
+double ps3o_rolling_mean_next(ps3o_model *m, double vnew) { return roll_next(&m->rv, vnew); }
 
 /* ====================================================================== */
 /* init_diffusion (inversion_utils.f90:124-218)                           */
 /* ====================================================================== */
-void ps3o_init_diffusion(ps3o_model *m, double te, double en)
+/* get_viscosity (:157-185) */
+static double get_viscosity(ps3o_model *m, int length_scale, double prediss, int p, double te, double en)
 {
     double rkxmax = 0.0, rkymax = 0.0;
     for (int i = 0; i < m->nx; ++i) rkxmax = fmax(rkxmax, m->rkx[i]);
     for (int i = 0; i < m->ny; ++i) rkymax = fmax(rkymax, m->rky[i]);
     const double k2max = ipow(fmax(rkxmax, rkymax), 2);
     const double rkmsi = 1.0 / k2max;
-    const int p = m->cfg.nnu;
-    double vis;
-    if (m->cfg.length_scale == PS3O_GEOPHYSICAL)
-        vis = m->cfg.prediss * ipow(rkmsi, p);
-    else
-        vis = m->cfg.prediss * pow(k2max * te / en, 1.0 / 3.0) * ipow(rkmsi, p);
-    m->vvisc = vis;
-    for (size_t i = 0; i < m->nplane; ++i)
-        m->vhdis[i] = (p == 1) ? vis * m->k2l2[i] : vis * ipow(m->k2l2[i], p);
+    if (length_scale == PS3O_GEOPHYSICAL) return prediss * ipow(rkmsi, p);
+    return prediss * pow(k2max * te / en, 1.0 / 3.0) * ipow(rkmsi, p);
+}
+
+/* init_dissipation (:189-218) */
+static void init_dissipation(ps3o_model *m, double vis, int p, double *hdis)
+{
+    for (size_t i = 0; i < m->nplane; ++i) hdis[i] = (p == 1) ? vis * m->k2l2[i] : vis * ipow(m->k2l2[i], p);
+}
+
+void ps3o_init_diffusion(ps3o_model *m, double te, double en)
+{
+    m->vvisc = get_viscosity(m, m->cfg.length_scale, m->cfg.prediss, m->cfg.nnu, te, en);
+    init_dissipation(m, m->vvisc, m->cfg.nnu, m->vhdis);
+    if (m->cfg.buoyancy) {
+        m->bvisc = get_viscosity(m, m->cfg.buoy_length_scale, m->cfg.buoy_prediss, m->cfg.buoy_nnu, te, en);
+        init_dissipation(m, m->bvisc, m->cfg.buoy_nnu, m->bhdis);
+    }
     m->diffusion_ready = 1;
 }
 
@@ -848,20 +961,175 @@ void ps3o_setup_fields(ps3o_model *m, const double *vor_phys, const double *pert
     if (en_out) *en_out = en;
 }
 
+/* ---- buoyancy diagnostics (field_diagnostics.f90) -------------------- */
+/* z-trapezoid sum of one field: interior levels 1, walls 1/2 */
+static double wsum_field(ps3o_model *m, const double *f)
+{
+    return wsum_fn(m, f_comp, (void *)f);
+}
+
+/* get_available_potential_energy (:29-60) with the linear-stratification
+ * density ape_den(b, z) = b^2 / (2 N^2) (ape_density.f90:10-34) */
+static double available_potential_energy(ps3o_model *m, const double *b)
+{
+    double *a = dalloc(m->nfield);
+    for (size_t i = 0; i < m->nfield; ++i) a[i] = b[i] * b[i] / (2.0 * m->bfsq);
+    const double ape = wsum_field(m, a) * m->ncelli;
+    free(a);
+    return ape;
+}
+
+/* get_gradb_integral (:351-397).  The reference's z term is overwritten
+ * before use (central_diffz writes mag, then fftxys2p(ds, mag) replaces it
+ * with the y derivative, :369-370), so |grad b| there is
+ * sqrt(b_x^2 + 2 b_y^2); restated as is.  sbuoy makes the combine /
+ * decompose round trip in place. */
+static double gradb_integral(ps3o_model *m)
+{
+    const size_t N = m->nfield;
+    double *ds = dalloc(N), *mag = dalloc(N), *bx = dalloc(N), *by = dalloc(N);
+    ps3o_combine_semi_spectral(m, m->sbuoy);
+    ps3o_diffx(m, m->sbuoy, ds);
+    ps3o_fftxys2p(m, ds, bx);
+    ps3o_diffy(m, m->sbuoy, ds);
+    ps3o_fftxys2p(m, ds, by);
+    ps3o_central_diffz(m, m->sbuoy, mag);
+    ps3o_fftxys2p(m, ds, mag);
+    ps3o_decompose_semi_spectral(m, m->sbuoy);
+    for (size_t i = 0; i < N; ++i) mag[i] = sqrt(bx[i] * bx[i] + by[i] * by[i] + mag[i] * mag[i]);
+    const double enb = wsum_field(m, mag) * m->ncelli;
+    free(ds); free(mag); free(bx); free(by);
+    return enb;
+}
+
+void ps3o_buoyancy_diagnostics(ps3o_model *m, double out[4])
+{
+    const size_t N = m->nfield;
+    out[0] = out[1] = out[2] = out[3] = 0.0;
+    if (!m->cfg.buoyancy) return;
+    ps3o_combine_physical(m, m->sbuoy, m->buoy);
+    out[0] = available_potential_energy(m, m->buoy);
+    out[1] = gradb_integral(m);
+    double *dbdz = dalloc(N);
+    ps3o_central_diffz(m, m->buoy, dbdz);
+    /* get_minimum_static_stability (:327-344) */
+    double mn = DBL_MAX;
+    for (size_t i = 0; i < N; ++i) mn = fmin(mn, dbdz[i]);
+    out[2] = 1.0 + mn / m->bfsq;
+    /* get_min_richardson_number (:268-287) */
+    double ri = DBL_MAX;
+    for (size_t i = 0; i < N; ++i)
+        ri = fmin(ri, (m->bfsq + dbdz[i]) / (m->vor[i] * m->vor[i] + m->vor[N + i] * m->vor[N + i]));
+    out[3] = ri;
+    free(dbdz);
+}
+
+void ps3o_setup_fields_buoyancy(ps3o_model *m, const double *vor_phys, const double *pert,
+                                const double *buoy_phys, double *te_out, double *en_out)
+{
+    const size_t N = m->nfield;
+    const int nz = m->nz;
+    if (!m->cfg.buoyancy) {
+        ps3o_setup_fields(m, vor_phys, pert, te_out, en_out);
+        return;
+    }
+    memset(m->svor, 0, sizeof(double) * 3 * N);
+    memset(m->vel, 0, sizeof(double) * 3 * N);
+    memset(m->svel, 0, sizeof(double) * 3 * N);
+    memset(m->svorts, 0, sizeof(double) * 3 * N);
+    memset(m->vortsm, 0, sizeof(double) * 3 * N);
+    memset(m->sbuoys, 0, sizeof(double) * N);
+    memset(m->bsm, 0, sizeof(double) * N);
+    memcpy(m->vor, vor_phys, sizeof(double) * 3 * N);
+    memcpy(m->buoy, buoy_phys, sizeof(double) * N);
+    /* calculate_basic_reference_state (physics.f90:310-340) */
+    if (!m->cfg.bfsq_given) {
+        double sum = 0.0;
+        for (size_t c = 0; c < m->ncol; ++c) sum += m->buoy[c * m->nz1 + nz] - m->buoy[c * m->nz1];
+        m->bfsq = sum / ((double)m->nx * (double)m->ny * m->extent[2]);
+    }
+    /* remove the basic state (utils.f90:152-158) */
+    for (int iz = 0; iz <= nz; ++iz) m->bbarz[iz] = m->bfsq * (m->lower[2] + (double)iz * m->dx[2]);
+    for (size_t c = 0; c < m->ncol; ++c)
+        for (int iz = 0; iz <= nz; ++iz) m->buoy[c * m->nz1 + iz] -= m->bbarz[iz];
+    ps3o_decompose_physical(m, m->buoy, m->sbuoy);
+    for (int nc = 0; nc < 3; ++nc) ps3o_decompose_physical(m, m->vor + nc * N, m->svor + nc * N);
+    if (pert)
+        for (size_t i = 0; i < 3 * N; ++i) m->svor[i] += pert[i];
+    ps3o_calc_vorticity_mean(m, m->ini_vor_mean);
+    ps3o_vor2vel(m);
+    double ke, en, hel;
+    ps3o_energy_series(m, &ke, &en, &hel);
+    const double ape = available_potential_energy(m, m->buoy);
+    const double te = ke + ape;
+    en = en + gradb_integral(m);
+    ps3o_init_diffusion(m, te, en);
+    if (te_out) *te_out = te;
+    if (en_out) *en_out = en;
+}
+
 /* ====================================================================== */
 /* adapt (advance.f90:109-377) and get_diffusion_pre_factor (:381-410)     */
 /* ====================================================================== */
-void ps3o_set_diffusion(ps3o_model *m, double dt, double vorch)
+void ps3o_set_diffusion_vb(ps3o_model *m, double dt, double vorch, double bf)
 {
+    const int buoy = m->cfg.buoyancy;
     if (m->cfg.stepper == PS3O_CN2) {
         /* cn2_set_diffusion (cn2.f90:40-77) */
         const double dfac = (m->cfg.nnu == 1) ? dt : vorch * dt;
         for (size_t i = 0; i < m->nplane; ++i) m->vdiss[i] = 1.0 / (1.0 + dfac * m->vhdis[i]);
+        if (buoy) {
+            const double dbac = (m->cfg.buoy_nnu == 1) ? dt : bf * dt;
+            for (size_t i = 0; i < m->nplane; ++i) m->bdiss[i] = 1.0 / (1.0 + dbac * m->bhdis[i]);
+        }
     } else {
         /* impl_rk4_set_diffusion (impl_rk4.f90:37-53) */
-        const double dfac = 0.5 * vorch * dt;
+        const double dfac = 0.5 * vorch * dt, dbac = 0.5 * bf * dt;
         for (size_t i = 0; i < m->nplane; ++i) m->vdiss[i] = dfac * m->vhdis[i];
+        if (buoy)
+            for (size_t i = 0; i < m->nplane; ++i) m->bdiss[i] = dbac * m->bhdis[i];
     }
+}
+
+void ps3o_set_diffusion(ps3o_model *m, double dt, double vorch) { ps3o_set_diffusion_vb(m, dt, vorch, 0.0); }
+
+/* get_diffusion_pre_factor (advance.f90:381-410) */
+static double pre_factor(int pretype, double vorch, double bfmax, double rmv, double rmb, double ggmax,
+                         double usggmax)
+{
+    switch (pretype) {
+    case PS3O_PRE_CONSTANT: return 1.0;
+    case PS3O_PRE_VORCH: return vorch;
+    case PS3O_PRE_BFMAX: return bfmax;
+    case PS3O_PRE_ROLL_MEAN_BFMAX: return rmb;
+    case PS3O_PRE_MAX_STRAIN: return ggmax;
+    case PS3O_PRE_US_MAX_STRAIN: return usggmax;
+    default: return rmv;
+    }
+}
+
+/* maximum buoyancy frequency (advance.f90:147-168): gradient of the
+ * buoyancy perturbation plus N^2 in z; sbuoy makes the reference's
+ * combine / decompose round trip in place */
+static double buoyancy_frequency_max(ps3o_model *m)
+{
+    const size_t N = m->nfield;
+    double *xs = dalloc(N), *xp = dalloc(N), *yp = dalloc(N), *zp = dalloc(N);
+    ps3o_combine_semi_spectral(m, m->sbuoy);
+    ps3o_diffx(m, m->sbuoy, xs);
+    ps3o_fftxys2p(m, xs, xp);
+    ps3o_diffy(m, m->sbuoy, xs);
+    ps3o_fftxys2p(m, xs, yp);
+    ps3o_central_diffz(m, m->sbuoy, xs);
+    ps3o_fftxys2p(m, xs, zp);
+    ps3o_decompose_semi_spectral(m, m->sbuoy);
+    double mx = -DBL_MAX;
+    for (size_t i = 0; i < N; ++i) {
+        const double zz = zp[i] + m->bfsq;
+        mx = fmax(mx, xp[i] * xp[i] + yp[i] * yp[i] + zz * zz);
+    }
+    free(xs); free(xp); free(yp); free(zp);
+    return sqrt(sqrt(mx));
 }
 
 void ps3o_adapt(ps3o_model *m, double t, double *dt_out, ps3o_diag *d)
@@ -933,24 +1201,22 @@ void ps3o_adapt(ps3o_model *m, double t, double *dt_out, ps3o_diag *d)
         vmax = fmax(vmax, m->vel[N + i]);
         wmax = fmax(wmax, m->vel[2 * N + i]);
     }
-    const double small = 1.0e-12, bfmax = 0.0;
+    const double small = 1.0e-12;
+    const double bfmax = m->cfg.buoyancy ? buoyancy_frequency_max(m) : 0.0;
     const double dtcfl = m->cfg.cflmax * fmin(fmin(m->dx[0] / (umax + small), m->dx[1] / (vmax + small)),
                                               m->dx[2] / (wmax + small));
     double dt = fmin(fmin(m->cfg.alpha / (ggmax + small), m->cfg.alpha / (bfmax + small)),
                      fmin(dtcfl, m->cfg.time_limit - t));
-    const double rmv = ps3o_rolling_mean_next(m, ggmax);
-    double val;
-    switch (m->cfg.pretype) {
-    case PS3O_PRE_CONSTANT: val = 1.0; break;
-    case PS3O_PRE_VORCH: val = vorch; break;
-    case PS3O_PRE_BFMAX: val = bfmax; break;
-    case PS3O_PRE_MAX_STRAIN: val = ggmax; break;
-    case PS3O_PRE_US_MAX_STRAIN: val = usggmax; break;
-    default: val = rmv; break;
-    }
-    ps3o_set_diffusion(m, dt, val);
+    /* the buoyancy rolling mean is updated before the vorticity one
+     * (advance.f90:358-366) */
+    const double rmb = m->cfg.buoyancy ? roll_next(&m->rb, bfmax) : 0.0;
+    const double rmv = roll_next(&m->rv, ggmax);
+    const double val = pre_factor(m->cfg.pretype, vorch, bfmax, rmv, rmb, ggmax, usggmax);
+    const double bval =
+        m->cfg.buoyancy ? pre_factor(m->cfg.buoy_pretype, vorch, bfmax, rmv, rmb, ggmax, usggmax) : 0.0;
+    ps3o_set_diffusion_vb(m, dt, val, bval);
     m->vorch = vorch; m->ggmax = ggmax; m->usggmax = usggmax; m->lsggmax = lsggmax;
-    m->bfmax = bfmax; m->rmv = rmv;
+    m->bfmax = bfmax; m->rmv = rmv; m->rmb = rmb;
     if (d) {
         d->t = t; d->dt = dt;
         ps3o_energy_series(m, &d->ke, &d->en, &d->hel);
@@ -959,6 +1225,7 @@ void ps3o_adapt(ps3o_model *m, double t, double *dt_out, ps3o_diag *d)
         d->ggmax = ggmax; d->usggmax = usggmax; d->lsggmax = lsggmax;
         d->umax = umax; d->vmax = vmax; d->wmax = wmax;
         d->bfmax = bfmax; d->rmv = rmv; d->pref = val;
+        d->rmb = rmb; d->bpref = bval;
     }
     *dt_out = dt;
     free(xp); free(xs); free(dudx); free(dudy); free(dvdy); free(dwdx); free(dwdy);
@@ -988,72 +1255,107 @@ static void stage_rhs(ps3o_model *m, const double *held)
 {
     if (held) {
         memcpy(m->svorts, held, sizeof(double) * 3 * m->nfield);
+        if (m->cfg.buoyancy) memcpy(m->sbuoys, held + 3 * m->nfield, sizeof(double) * m->nfield);
         return;
     }
     ps3o_vor2vel(m);
     ps3o_source(m);
 }
 
+/* impl_rk4_substep_one (impl_rk4.f90:211-240) */
+static void rk4_sub1(ps3o_model *m, double *q, double *sqs, double *qdi, double *qdf, const double *mq,
+                     double dt2, double dt6)
+{
+    const size_t N = m->nfield, P = m->nplane;
+    for (size_t c = 0; c < P; ++c) {
+        const double f0 = m->filt[c * m->nz1];
+        for (int iz = 0; iz < m->nz1; ++iz) sqs[c * m->nz1 + iz] *= f0;
+    }
+    memcpy(qdi, q, sizeof(double) * N);
+    for (size_t i = 0; i < N; ++i) q[i] = qdi[i] + dt2 * sqs[i];
+    sandwich(m, q, mq);
+    for (size_t i = 0; i < N; ++i) qdf[i] = qdi[i] + dt6 * sqs[i];
+}
+
+/* impl_rk4_substep_two / _three (impl_rk4.f90:245-324): dtq = dt/2, dt */
+static void rk4_sub23(ps3o_model *m, double *q, double *sqs, const double *qdi, double *qdf, const double *mq,
+                      const double *pq, double dtq, double dt3)
+{
+    const size_t N = m->nfield;
+    sandwich(m, sqs, pq);
+    for (size_t i = 0; i < N; ++i) q[i] = qdi[i] + dtq * sqs[i];
+    sandwich(m, q, mq);
+    for (size_t i = 0; i < N; ++i) qdf[i] = qdf[i] + dt3 * sqs[i];
+}
+
+/* impl_rk4_substep_four (impl_rk4.f90:329-362) */
+static void rk4_sub4(ps3o_model *m, double *q, double *sqs, const double *qdf, const double *mq, const double *pq,
+                     double dt6)
+{
+    const size_t N = m->nfield;
+    sandwich(m, sqs, pq);
+    for (size_t i = 0; i < N; ++i) q[i] = qdf[i] + dt6 * sqs[i];
+    sandwich(m, q, mq);
+}
+
+/* copy of the sources for the hold_source test hook */
+static double *hold_sources(ps3o_model *m)
+{
+    if (!m->cfg.hold_source) return NULL;
+    const size_t N = m->nfield;
+    double *held = dalloc(4 * N);
+    memcpy(held, m->svorts, sizeof(double) * 3 * N);
+    if (m->cfg.buoyancy) memcpy(held + 3 * N, m->sbuoys, sizeof(double) * N);
+    return held;
+}
+
 static void impl_rk4_step(ps3o_model *m, double *t, double dt)
 {
     const size_t N = m->nfield, P = m->nplane;
-    double *held = NULL;
-    if (m->cfg.hold_source) {
-        held = dalloc(3 * N);
-        memcpy(held, m->svorts, sizeof(double) * 3 * N);
-    }
+    const int buoy = m->cfg.buoyancy;
+    double *held = hold_sources(m);
     const double dt2 = 0.5 * dt, dt3 = dt / 3.0, dt6 = dt / 6.0;
     for (size_t i = 0; i < P; ++i) {
         m->epq[i] = exp(m->vdiss[i]);
         m->emq[i] = 1.0 / m->epq[i];
         m->epq[i] = m->epq[i] * m->filt[i * m->nz1]; /* filt(0, ky, kx) */
     }
-    /* substep 1 */
-    for (int nc = 0; nc < 3; ++nc) {
-        double *q = m->svor + nc * N, *sqs = m->svorts + nc * N;
-        double *qdi = m->svori + nc * N, *qdf = m->svorf + nc * N;
-        for (size_t c = 0; c < P; ++c) {
-            const double f0 = m->filt[c * m->nz1];
-            for (int iz = 0; iz < m->nz1; ++iz) sqs[c * m->nz1 + iz] *= f0;
+    if (buoy)
+        for (size_t i = 0; i < P; ++i) {
+            m->bpq[i] = exp(m->bdiss[i]);
+            m->bmq[i] = 1.0 / m->bpq[i];
+            m->bpq[i] = m->bpq[i] * m->filt[i * m->nz1];
         }
-        memcpy(qdi, q, sizeof(double) * N);
-        for (size_t i = 0; i < N; ++i) q[i] = qdi[i] + dt2 * sqs[i];
-        sandwich(m, q, m->emq);
-        for (size_t i = 0; i < N; ++i) qdf[i] = qdi[i] + dt6 * sqs[i];
-    }
+    /* substep 1 (buoyancy first, impl_rk4.f90:99-115) */
+    if (buoy) rk4_sub1(m, m->sbuoy, m->sbuoys, m->sbuoyi, m->sbuoyf, m->bmq, dt2, dt6);
+    for (int nc = 0; nc < 3; ++nc)
+        rk4_sub1(m, m->svor + nc * N, m->svorts + nc * N, m->svori + nc * N, m->svorf + nc * N, m->emq, dt2,
+                 dt6);
     stage_rhs(m, held);
     *t += dt2;
     /* substep 2 */
-    for (int nc = 0; nc < 3; ++nc) {
-        double *q = m->svor + nc * N, *sqs = m->svorts + nc * N;
-        double *qdi = m->svori + nc * N, *qdf = m->svorf + nc * N;
-        sandwich(m, sqs, m->epq);
-        for (size_t i = 0; i < N; ++i) q[i] = qdi[i] + dt2 * sqs[i];
-        sandwich(m, q, m->emq);
-        for (size_t i = 0; i < N; ++i) qdf[i] = qdf[i] + dt3 * sqs[i];
-    }
+    if (buoy) rk4_sub23(m, m->sbuoy, m->sbuoys, m->sbuoyi, m->sbuoyf, m->bmq, m->bpq, dt2, dt3);
+    for (int nc = 0; nc < 3; ++nc)
+        rk4_sub23(m, m->svor + nc * N, m->svorts + nc * N, m->svori + nc * N, m->svorf + nc * N, m->emq,
+                  m->epq, dt2, dt3);
     stage_rhs(m, held);
     *t += dt2;
     for (size_t i = 0; i < P; ++i) m->emq[i] = m->emq[i] * m->emq[i];
+    if (buoy)
+        for (size_t i = 0; i < P; ++i) m->bmq[i] = m->bmq[i] * m->bmq[i];
     /* substep 3 */
-    for (int nc = 0; nc < 3; ++nc) {
-        double *q = m->svor + nc * N, *sqs = m->svorts + nc * N;
-        double *qdi = m->svori + nc * N, *qdf = m->svorf + nc * N;
-        sandwich(m, sqs, m->epq);
-        for (size_t i = 0; i < N; ++i) q[i] = qdi[i] + dt * sqs[i];
-        sandwich(m, q, m->emq);
-        for (size_t i = 0; i < N; ++i) qdf[i] = qdf[i] + dt3 * sqs[i];
-    }
+    if (buoy) rk4_sub23(m, m->sbuoy, m->sbuoys, m->sbuoyi, m->sbuoyf, m->bmq, m->bpq, dt, dt3);
+    for (int nc = 0; nc < 3; ++nc)
+        rk4_sub23(m, m->svor + nc * N, m->svorts + nc * N, m->svori + nc * N, m->svorf + nc * N, m->emq,
+                  m->epq, dt, dt3);
     stage_rhs(m, held);
     for (size_t i = 0; i < P; ++i) m->epq[i] = m->epq[i] * m->epq[i];
+    if (buoy)
+        for (size_t i = 0; i < P; ++i) m->bpq[i] = m->bpq[i] * m->bpq[i];
     /* substep 4 */
-    for (int nc = 0; nc < 3; ++nc) {
-        double *q = m->svor + nc * N, *sqs = m->svorts + nc * N;
-        double *qdf = m->svorf + nc * N;
-        sandwich(m, sqs, m->epq);
-        for (size_t i = 0; i < N; ++i) q[i] = qdf[i] + dt6 * sqs[i];
-        sandwich(m, q, m->emq);
-    }
+    if (buoy) rk4_sub4(m, m->sbuoy, m->sbuoys, m->sbuoyf, m->bmq, m->bpq, dt6);
+    for (int nc = 0; nc < 3; ++nc)
+        rk4_sub4(m, m->svor + nc * N, m->svorts + nc * N, m->svorf + nc * N, m->emq, m->epq, dt6);
     ps3o_adjust_vorticity_mean(m);
     free(held);
 }
@@ -1061,6 +1363,11 @@ static void impl_rk4_step(ps3o_model *m, double *t, double dt)
 static void cn2_update(ps3o_model *m, double dt2)
 {
     const size_t N = m->nfield;
+    if (m->cfg.buoyancy) {
+        /* cn2.f90:107-117, 151-160 */
+        for (size_t i = 0; i < N; ++i) m->sbuoy[i] = m->filt[i] * (m->bsm[i] + dt2 * m->sbuoys[i]);
+        sandwich(m, m->sbuoy, m->bdiss);
+    }
     for (int nc = 0; nc < 3; ++nc) {
         double *q = m->svor + nc * N;
         const double *vs = m->vortsm + nc * N, *sqs = m->svorts + nc * N;
@@ -1074,13 +1381,11 @@ static void cn2_step(ps3o_model *m, double *t, double dt)
 {
     const size_t N = m->nfield;
     const double dt2 = 0.5 * dt;
+    if (m->cfg.buoyancy)
+        for (size_t i = 0; i < N; ++i) m->bsm[i] = m->sbuoy[i] + dt2 * m->sbuoys[i];
     for (size_t i = 0; i < 3 * N; ++i) m->vortsm[i] = m->svor[i] + dt2 * m->svorts[i];
     cn2_update(m, dt2);
-    double *held = NULL;
-    if (m->cfg.hold_source) {
-        held = dalloc(3 * N);
-        memcpy(held, m->svorts, sizeof(double) * 3 * N);
-    }
+    double *held = hold_sources(m);
     for (int iter = 0; iter < 2; ++iter) {
         stage_rhs(m, held);
         cn2_update(m, dt2);
@@ -1129,39 +1434,56 @@ int ps3o_get_table(ps3o_model *m, int which, double *out)
     case 13: src = m->rkx; n = m->nx; break;
     case 14: src = m->rky; n = m->ny; break;
     case 15: src = m->rkz; n = m->nz1; break;
+    case 16: src = m->dphim; n = N; break;
+    case 17: src = m->dphip; n = N; break;
+    case 18: src = m->bhdis; n = P; break;
+    case 19: src = m->bbarz; n = m->nz1; break;
     default: return 1;
     }
+    if (!src) return 1;
     memcpy(out, src, sizeof(double) * n);
     return 0;
 }
 
-static double *field_ptr(ps3o_model *m, int which)
+static double *field_ptr(ps3o_model *m, int which, size_t *n)
 {
+    *n = 3 * m->nfield;
     switch (which) {
     case 0: return m->svor;
     case 1: return m->vor;
     case 2: return m->vel;
     case 3: return m->svel;
     case 4: return m->svorts;
+    }
+    *n = m->nfield;
+    switch (which) {
+    case 5: return m->sbuoy;
+    case 6: return m->buoy;
+    case 7: return m->sbuoys;
     default: return NULL;
     }
 }
 
 int ps3o_get_field(ps3o_model *m, int which, double *out)
 {
-    double *p = field_ptr(m, which);
+    size_t n;
+    double *p = field_ptr(m, which, &n);
     if (!p) return 1;
-    memcpy(out, p, sizeof(double) * 3 * m->nfield);
+    memcpy(out, p, sizeof(double) * n);
     return 0;
 }
 
 int ps3o_set_field(ps3o_model *m, int which, const double *in)
 {
-    double *p = field_ptr(m, which);
+    size_t n;
+    double *p = field_ptr(m, which, &n);
     if (!p) return 1;
-    memcpy(p, in, sizeof(double) * 3 * m->nfield);
+    memcpy(p, in, sizeof(double) * n);
     return 0;
 }
+
+double ps3o_get_bfsq(ps3o_model *m) { return m->bfsq; }
+double ps3o_get_bvisc(ps3o_model *m) { return m->bvisc; }
 
 void ps3o_get_ini_vor_mean(ps3o_model *m, double out[2])
 {

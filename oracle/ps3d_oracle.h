@@ -41,7 +41,7 @@ void ps3o_dst(int m, int n, double *x1, double *wk, double *wk2,
  * and box (src/utils/parameters.f90) that the hot path consumes. */
 enum { PS3O_PRE_CONSTANT = 0, PS3O_PRE_VORCH = 1, PS3O_PRE_BFMAX = 2,
        PS3O_PRE_ROLL_MEAN_MAX_STRAIN = 3, PS3O_PRE_MAX_STRAIN = 4,
-       PS3O_PRE_US_MAX_STRAIN = 5 };
+       PS3O_PRE_US_MAX_STRAIN = 5, PS3O_PRE_ROLL_MEAN_BFMAX = 6 };
 enum { PS3O_KOLMOGOROV = 0, PS3O_GEOPHYSICAL = 1 };
 enum { PS3O_HOU_LI = 0, PS3O_TWO_THIRDS = 1 };
 enum { PS3O_IMPL_DIFF_RK4 = 0, PS3O_CN2 = 1 };
@@ -64,6 +64,18 @@ typedef struct {
     int hold_source;         /* test hook: keep svorts fixed inside step()
                                 (unit-tests/test_implicit_rk.f90) */
     double f_cor[3];
+    /* buoyancy (the reference built with ENABLE_BUOYANCY): N^2 of the basic
+     * state (physics.f90:90-94; computed from the initial buoyancy by
+     * calculate_basic_reference_state when bfsq_given is 0) and buoy_visc
+     * (options.f90:78-80) */
+    int buoyancy;
+    double bfsq;
+    int bfsq_given;
+    int buoy_nnu;
+    double buoy_prediss;
+    int buoy_pretype;
+    int buoy_length_scale;
+    int buoy_roll_mean_win_size;
 } ps3o_config;
 
 /* Per-step diagnostics (adapt, src/stepper/advance.f90:109-377, plus the
@@ -76,6 +88,7 @@ typedef struct {
     double ggmax, usggmax, lsggmax;
     double umax, vmax, wmax;
     double bfmax, rmv, pref;
+    double rmb, bpref;       /* buoyancy: rolling mean of bfmax, prefactor */
 } ps3o_diag;
 
 typedef struct ps3o_model ps3o_model;
@@ -98,10 +111,12 @@ void ps3o_combine_physical(ps3o_model *m, const double *sf, double *fc);
 
 /* tables: which = 0 k2l2, 1 k2l2i (ny*nx); 2 filt, 3 green, 4 phim, 5 phip,
  * 6 thetam, 7 thetap, 8 dthetam, 9 dthetap (N); 10 gamtop, 11 gambot (nz+1);
- * 12 vhdis (ny*nx); 13 rkx (nx), 14 rky (ny), 15 rkz (nz+1) */
+ * 12 vhdis (ny*nx); 13 rkx (nx), 14 rky (ny), 15 rkz (nz+1); buoyancy:
+ * 16 dphim, 17 dphip (N), 18 bhdis (ny*nx), 19 bbarz (nz+1) */
 int ps3o_get_table(ps3o_model *m, int which, double *out);
 
-/* state access: which = 0 svor, 1 vor, 2 vel, 3 svel, 4 svorts (3N each) */
+/* state access: which = 0 svor, 1 vor, 2 vel, 3 svel, 4 svorts (3N each);
+ * buoyancy: 5 sbuoy, 6 buoy (physical), 7 sbuoys (N each) */
 int ps3o_get_field(ps3o_model *m, int which, double *out);
 int ps3o_set_field(ps3o_model *m, int which, const double *in);
 void ps3o_get_ini_vor_mean(ps3o_model *m, double out[2]);
@@ -113,6 +128,24 @@ double ps3o_get_vvisc(ps3o_model *m);
 void ps3o_setup_fields(ps3o_model *m, const double *vor_phys, const double *pert, double *te,
                        double *en);
 void ps3o_init_diffusion(ps3o_model *m, double te, double en);
+/* setup_fields with buoyancy (utils.f90:136-184): buoy_phys is the total
+ * physical buoyancy (N); N^2 from calculate_basic_reference_state unless
+ * given, the basic state N^2 z removed, te = kinetic + available potential
+ * energy, en = enstrophy + the buoyancy-gradient integral */
+void ps3o_setup_fields_buoyancy(ps3o_model *m, const double *vor_phys, const double *pert,
+                                const double *buoy_phys, double *te, double *en);
+double ps3o_get_bfsq(ps3o_model *m);
+double ps3o_get_bvisc(ps3o_model *m);
+/* diffz (inversion_utils.f90:683-719): d/dz of a mixed-spectral field,
+ * returned mixed-spectral (1: model built without buoyancy) */
+int ps3o_diffz(ps3o_model *m, const double *fs, double *ds);
+/* buoyancy_tendency (inversion.f90:232-292): sbuoys from sbuoy and vel */
+void ps3o_buoyancy_tendency(ps3o_model *m);
+/* buoyancy diagnostics of the current fields (field_diagnostics.f90):
+ * out[0] available potential energy (:29-60, linear stratification),
+ * out[1] buoyancy-gradient integral (:351-397), out[2] minimum static
+ * stability (:327-344), out[3] minimum Richardson number (:268-287) */
+void ps3o_buoyancy_diagnostics(ps3o_model *m, double out[4]);
 
 void ps3o_vor2vel(ps3o_model *m);
 void ps3o_source(ps3o_model *m);
@@ -120,6 +153,9 @@ void ps3o_adapt(ps3o_model *m, double t, double *dt, ps3o_diag *d);
 void ps3o_step(ps3o_model *m, double *t, double dt);
 /* set_diffusion of the configured stepper with prefactor pref */
 void ps3o_set_diffusion(ps3o_model *m, double dt, double pref);
+/* set_diffusion(dt, vorch, bf) with both prefactors (impl_rk4.f90:37-53,
+ * cn2.f90:40-77) */
+void ps3o_set_diffusion_vb(ps3o_model *m, double dt, double vpref, double bpref);
 /* one advance() (src/stepper/advance.f90:77-104): vor2vel, adapt, source, step */
 void ps3o_advance(ps3o_model *m, double *t, ps3o_diag *d);
 

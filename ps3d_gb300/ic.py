@@ -134,3 +134,35 @@ def beltrami_plus_perturbation_slabs(nx, ny, nz, seed=0, amplitude=1.0e-3, lower
     for ix in range(nx):
         pert[:, ix] *= scale
     return vor, pert
+
+
+def grid(nx, ny, nz, lower, extent):
+    """Grid coordinates x (nx), y (ny), z (nz+1) of the reference's nodes."""
+    dx = np.array(extent, dtype=np.float64) / np.array([nx, ny, nz], dtype=np.float64)
+    return (lower[0] + dx[0] * np.arange(nx), lower[1] + dx[1] * np.arange(ny),
+            lower[2] + dx[2] * np.arange(nz + 1))
+
+
+def stratified_buoyancy(nx, ny, nz, lower, extent, bfsq=1.0, amplitude=1.0e-2, seed=0, kmax=3):
+    """(nx, ny, nz+1) total physical buoyancy: the basic state N^2 z plus a
+    perturbation (no reference counterpart; the reference reads its buoyancy
+    from a NetCDF file): a sum of modes cos(k x + l y + phase) sin(j pi (z -
+    lower_z) / L_z) with |k|, |l| <= kmax horizontal and 1 <= j <= kmax
+    vertical wave numbers, Gaussian amplitudes from PCG64(seed), rescaled so
+    that its grid rms is amplitude * N^2 * L_z.  The perturbation vanishes on
+    the walls, so calculate_basic_reference_state recovers N^2 exactly."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    x, y, z = grid(nx, ny, nz, lower, extent)
+    zeta = (z - lower[2]) / extent[2]
+    pert = np.zeros((nx, ny, nz + 1))
+    for k in range(0, kmax + 1):
+        for l in range(-kmax, kmax + 1):
+            if k == 0 and l <= 0:
+                continue
+            phase = 2.0 * np.pi * (k * (x[:, None] - lower[0]) / extent[0] + l * (y[None, :] - lower[1]) / extent[1])
+            for j in range(1, kmax + 1):
+                a, ph = rng.standard_normal(), rng.uniform(0.0, 2.0 * np.pi)
+                pert += a * np.cos(phase + ph)[:, :, None] * np.sin(j * np.pi * zeta)[None, None, :]
+    rms = np.sqrt(np.mean(pert ** 2))
+    pert *= amplitude * bfsq * extent[2] / rms
+    return bfsq * z[None, None, :] + pert

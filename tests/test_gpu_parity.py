@@ -379,6 +379,35 @@ def test_mixed_advance_host_matches_resident_and_projects_changes():
     assert np.array_equal(a.get("svor"), host)
 
 
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_advance_host_page_locked_equals_pageable(precision):
+    """A state buffer from ps3d_gpu_host_alloc is read and written in place by
+    the device (zero copy); a plain numpy buffer goes through the staging
+    copies.  Both give the same state bitwise, including a host-side change."""
+    from ps3d_gb300.solver import PinnedArray
+    lo, ex, vor, pert = beltrami_case(32, seed=12)
+    a = Ps3dGpu(32, 32, 32, lo, ex, precision=precision)
+    b = Ps3dGpu(32, 32, 32, lo, ex, precision=precision)
+    a.setup_fields(vor, pert)
+    b.setup_fields(vor, pert)
+    plain = np.ascontiguousarray(a.get("svor"))
+    locked = PinnedArray(plain.shape)
+    try:
+        locked.array[...] = plain
+        t_a = t_b = 0.0
+        for i in range(3):
+            if i == 2:
+                kick = 1e-3 * np.random.default_rng(2).standard_normal(plain.shape)
+                plain += kick
+                locked.array[...] += kick
+            t_a, da = a.advance_host(plain, t_a)
+            t_b, db = b.advance_host(locked.array, t_b)
+            assert np.array_equal(plain, locked.array)
+            assert t_a == t_b and da["ke"] == db["ke"]
+    finally:
+        locked.close()
+
+
 @pytest.mark.parametrize("precision,tol", [("fp64", 1e-12), ("mixed", 1e-4)])
 @pytest.mark.parametrize("grid", [(32, 32, 32), (16, 32, 64)], ids=lambda g: "x".join(map(str, g)))
 def test_derived_pressure_and_divergence_match_oracle(grid, precision, tol):
