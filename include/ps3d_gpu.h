@@ -44,6 +44,7 @@ extern "C" {
 #define PS3D_PRE_ROLL_MEAN_MAX_STRAIN 3  /* 'roll-mean-max-strain'         */
 #define PS3D_PRE_MAX_STRAIN 4            /* 'max-strain'                   */
 #define PS3D_PRE_US_MAX_STRAIN 5         /* 'us-max-strain'                */
+#define PS3D_PRE_ROLL_MEAN_BFMAX 6       /* 'roll-mean-bfmax' (buoyancy)   */
 #define PS3D_KOLMOGOROV 0                /* length_scale                   */
 #define PS3D_GEOPHYSICAL 1
 #define PS3D_HOU_LI 0                    /* filtering 'Hou & Li'           */
@@ -78,6 +79,18 @@ typedef struct {
     double f_cor[3];            /* planetary vorticity (physics.f90:61)      */
     int precision;              /* PS3D_PRECISION_*                          */
     int device;                 /* CUDA device ordinal                       */
+    /* Buoyancy (the reference configured with --enable-buoyancy,
+     * configure.ac:213-223): a Boussinesq buoyancy perturbation b' about the
+     * basic state N^2 z is stepped with the vorticity. */
+    int buoyancy;               /* 0: vorticity only                         */
+    double bfsq;                /* N^2 (physics.f90:90-94)                   */
+    int bfsq_given;             /* 0: N^2 from the initial buoyancy
+                                   (calculate_basic_reference_state)         */
+    int buoy_nnu;               /* buoy_visc%nnu (options.f90:78-80)         */
+    double buoy_prediss;        /* buoy_visc%prediss                         */
+    int buoy_pretype;           /* buoy_visc%pretype, PS3D_PRE_*             */
+    int buoy_length_scale;      /* buoy_visc%length_scale                    */
+    int buoy_roll_mean_win_size;/* buoy_visc%roll_mean_win_size              */
 } ps3d_gpu_config;
 
 /* Diagnostics of one adapt() call (src/stepper/advance.f90:109-377) plus the
@@ -91,6 +104,8 @@ typedef struct {
     double ggmax, usggmax, lsggmax;
     double umax, vmax, wmax;
     double bfmax, rmv, pref;
+    double rmb, bpref;          /* buoyancy: rolling mean of bfmax (advance.f90:358-361)
+                                   and the buoyancy prefactor (:370-373)     */
 } ps3d_gpu_diag;
 
 typedef struct ps3d_gpu_ctx ps3d_gpu_ctx;
@@ -114,13 +129,19 @@ long long ps3d_gpu_device_bytes(const ps3d_gpu_ctx *ctx);
 #define PS3D_FIELD_VEL 2
 #define PS3D_FIELD_SVEL 3
 #define PS3D_FIELD_SVORTS 4
+/* buoyancy contexts (one scalar field each, fields.f90:25-31): sbuoy
+ * (mixed-spectral b'), buoy (physical b'), sbuoys (its source) */
+#define PS3D_FIELD_SBUOY 5
+#define PS3D_FIELD_BUOY 6
+#define PS3D_FIELD_SBUOYS 7
 int ps3d_gpu_set_field(ps3d_gpu_ctx *ctx, int which, const double *host);
 int ps3d_gpu_get_field(ps3d_gpu_ctx *ctx, int which, double *host);
 int ps3d_gpu_set_ini_vor_mean(ps3d_gpu_ctx *ctx, const double v[2]);
 int ps3d_gpu_get_ini_vor_mean(ps3d_gpu_ctx *ctx, double v[2]);
 /* tables, numbering as the oracle: 0 k2l2, 1 k2l2i, 2 filt, 3 green, 4 phim,
  * 5 phip, 6 thetam, 7 thetap, 8 dthetam, 9 dthetap, 10 gamtop, 11 gambot,
- * 12 vhdis, 13 rkx, 14 rky, 15 rkz (inversion_utils.f90:222-372). */
+ * 12 vhdis, 13 rkx, 14 rky, 15 rkz (inversion_utils.f90:222-372); buoyancy
+ * contexts: 16 dphim, 17 dphip, 18 bhdis, 19 bbarz (N^2 z). */
 int ps3d_gpu_get_table(ps3d_gpu_ctx *ctx, int which, double *host);
 
 /* ---- reference procedures ---------------------------------------------- */
@@ -130,23 +151,39 @@ int ps3d_gpu_get_table(ps3d_gpu_ctx *ctx, int which, double *host);
  * energy, en = enstrophy and init_diffusion(te, en). */
 int ps3d_gpu_setup_fields(ps3d_gpu_ctx *ctx, const double *vor_phys,
                           const double *pert, double *te, double *en);
-/* init_diffusion (inversion_utils.f90:124-153) */
+/* setup_fields of a buoyancy context (utils.f90:136-184): buoy_phys is the
+ * total physical buoyancy (1 field); N^2 from it unless bfsq_given
+ * (physics.f90:310-340), the basic state N^2 z removed and decomposed into
+ * sbuoy, then as above with te = kinetic + available potential energy
+ * (linear stratification, ape_density.f90:31-32) and en = enstrophy + the
+ * buoyancy-gradient integral (field_diagnostics.f90:351-397).  On a context
+ * without buoyancy this is ps3d_gpu_setup_fields (buoy_phys ignored). */
+int ps3d_gpu_setup_fields_buoyancy(ps3d_gpu_ctx *ctx, const double *vor_phys, const double *pert,
+                                   const double *buoy_phys, double *te, double *en);
+/* N^2 and the buoyancy viscosity bvisc of a buoyancy context */
+int ps3d_gpu_buoyancy_params(ps3d_gpu_ctx *ctx, double *bfsq, double *bvisc);
+/* init_diffusion (inversion_utils.f90:124-153), vorticity and buoyancy */
 int ps3d_gpu_init_diffusion(ps3d_gpu_ctx *ctx, double te, double en);
 /* vor2vel (inversion.f90:23-226) */
 int ps3d_gpu_vor2vel(ps3d_gpu_ctx *ctx);
-/* source / vorticity_tendency (inversion.f90:298-388) */
+/* source (inversion.f90:376-388): buoyancy_tendency (:232-292) on buoyancy
+ * contexts, then vorticity_tendency (:298-371) */
 int ps3d_gpu_source(ps3d_gpu_ctx *ctx);
 /* adapt (advance.f90:109-377) incl. set_diffusion of the stepper */
 int ps3d_gpu_adapt(ps3d_gpu_ctx *ctx, double t, double *dt, ps3d_gpu_diag *diag);
-/* base_stepper%set_diffusion (impl_rk4.f90:37-53, cn2.f90:40-77) */
+/* base_stepper%set_diffusion (impl_rk4.f90:37-53, cn2.f90:40-77) with the
+ * vorticity prefactor (the buoyancy prefactor 0) */
 int ps3d_gpu_set_diffusion(ps3d_gpu_ctx *ctx, double dt, double pref);
+/* set_diffusion(dt, vorch, bf) with both prefactors */
+int ps3d_gpu_set_diffusion_vb(ps3d_gpu_ctx *ctx, double dt, double vpref, double bpref);
 /* base_stepper%step (impl_rk4.f90:76-207, cn2.f90:92-181) */
 int ps3d_gpu_step(ps3d_gpu_ctx *ctx, double *t, double dt);
 /* advance (advance.f90:77-104) repeated nsteps times; diag (nullable) gets
  * nsteps records, one per step, taken by adapt at the start of the step. */
 int ps3d_gpu_advance(ps3d_gpu_ctx *ctx, double *t, int nsteps, ps3d_gpu_diag *diag);
 /* One advance for a caller that owns the state on the host (the Fortran
- * driver's arrays): upload svor (3 fields), advance once, download svor. */
+ * driver's arrays): upload svor (3 fields), advance once, download svor.
+ * PS3D_ERR_INVALID_ARG on a buoyancy context (its state includes sbuoy). */
 int ps3d_gpu_advance_host(ps3d_gpu_ctx *ctx, double *svor, double *t, ps3d_gpu_diag *diag);
 /* calc_vorticity_mean / adjust_vorticity_mean (field_diagnostics.f90:584-619) */
 int ps3d_gpu_calc_vorticity_mean(ps3d_gpu_ctx *ctx, double out[2]);
@@ -166,6 +203,8 @@ int ps3d_gpu_energy_series(ps3d_gpu_ctx *ctx, double *ke, double *en, double *he
 #define PS3D_OP_COMBINE_SEMI 8    /* inversion_utils.f90:617-647            */
 #define PS3D_OP_DECOMPOSE_PHYS 9  /* inversion_utils.f90:549-557            */
 #define PS3D_OP_COMBINE_PHYS 10   /* inversion_utils.f90:599-611            */
+#define PS3D_OP_DIFFZ 11          /* inversion_utils.f90:683-719 (buoyancy
+                                     contexts only)                         */
 int ps3d_gpu_field_op(ps3d_gpu_ctx *ctx, int op, const double *in, double *out);
 
 /* ---- benchmark helpers ------------------------------------------------- */
@@ -175,12 +214,23 @@ int ps3d_gpu_time_advance(ps3d_gpu_ctx *ctx, double *t, int nsteps, double *ms);
 /* Kernel launches issued by this context since creation. */
 long long ps3d_gpu_launch_count(const ps3d_gpu_ctx *ctx);
 int ps3d_gpu_synchronize(ps3d_gpu_ctx *ctx);
-/* Derived fields (src/fields/fields_derived.f90:67-182, buoyancy disabled)
- * from the current vel, vor and svel (call after ps3d_gpu_vor2vel, as the
- * reference's adapt does): pres solves Lap(p) = 2[J_xy(u,v) + J_yz(v,w) +
- * J_zx(w,u)] with dp/dz = 0 on the walls; delta = du/dx + dv/dy.  Physical
- * host arrays (nz+1, ny, nx) column-major; NULL skips one. */
+/* Derived fields (src/fields/fields_derived.f90:67-182) from the current
+ * vel, vor and svel (call after ps3d_gpu_vor2vel, as the reference's adapt
+ * does): pres solves Lap(p) = 2[J_xy(u,v) + J_yz(v,w) + J_zx(w,u)] with
+ * dp/dz = 0 on the walls (buoyancy contexts add b'_z + f_z zeta to the
+ * right-hand side and the harmonic boundary terms of b', :108-151);
+ * delta = du/dx + dv/dy.  Physical host arrays (nz+1, ny, nx) column-major;
+ * NULL skips one. */
 int ps3d_gpu_derived_fields(ps3d_gpu_ctx *ctx, double *pres, double *delta);
+
+/* Buoyancy diagnostics of the current state (field_diagnostics.f90, buoyancy
+ * contexts): out[0] available potential energy (:29-60, linear
+ * stratification b'^2 / (2 N^2)), out[1] buoyancy-gradient integral
+ * (:351-397; the reference's |grad b| is sqrt(b_x^2 + 2 b_y^2), its z term
+ * being overwritten at :369-370), out[2] minimum static stability
+ * 1 + min(b'_z) / N^2 (:327-344), out[3] minimum Richardson number
+ * min((N^2 + b'_z) / (xi^2 + eta^2)) (:268-287, from the current vor). */
+int ps3d_gpu_buoyancy_diagnostics(ps3d_gpu_ctx *ctx, double out[4]);
 
 /* Kinetic-energy shell spectrum (src/genspec.f90:42-123) of the current
  * vel: squared spectral amplitudes (dct of u, v and dst of w along z) summed
@@ -203,7 +253,7 @@ int ps3d_gpu_host_free(void *ptr);
  * last step's diagnostics, ms (optional) the device time.  A non-finite
  * diagnostic or a Jacobi limit is reported after the launches
  * (PS3D_ERR_NONFINITE / PS3D_ERR_DEVICE_LIMIT; the state is then invalid).
- * PS3D_ERR_INVALID_ARG for the FP64 form, cn2 or a held source. */
+ * PS3D_ERR_INVALID_ARG for the FP64 form, cn2, a held source or buoyancy. */
 int ps3d_gpu_advance_graph(ps3d_gpu_ctx *ctx, double *t, int nsteps, ps3d_gpu_diag *diag, double *ms);
 /* Batching (no reference counterpart): nsteps captured steps of n independent
  * contexts (any grid sizes, one device), the runs' graphs interleaved on

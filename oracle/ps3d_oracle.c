@@ -1500,7 +1500,7 @@ void ps3o_set_ini_vor_mean(ps3o_model *m, const double in[2])
 double ps3o_get_vvisc(ps3o_model *m) { return m->vvisc; }
 
 /* ====================================================================== */
-/* derived fields (fields_derived.f90:67-182, buoyancy disabled): pressure */
+/* derived fields (fields_derived.f90:67-182): pressure                    */
 /* from Lap(p) = 2[J_xy(u,v) + J_yz(v,w) + J_zx(w,u)] with dp/dz = 0 on the */
 /* walls (DCT - Green function - DCT), and the horizontal divergence       */
 /* ====================================================================== */
@@ -1522,10 +1522,27 @@ void ps3o_pressure(ps3o_model *m, double *pres)
                          dvdy[i] * dwdz - dwdy[i] * (dwdy[i] - xi[i]) +
                          dwdz * dudx[i] - dwdx[i] * (dwdx[i] + eta[i]));
     }
+    if (m->cfg.buoyancy) {
+        /* fields_derived.f90:108-112 */
+        double *dbdz = dalloc(N);
+        ps3o_combine_physical(m, m->sbuoy, m->buoy);
+        ps3o_central_diffz(m, m->buoy, dbdz);
+        for (size_t i = 0; i < N; ++i) pres[i] = pres[i] + dbdz[i] + m->cfg.f_cor[2] * zeta[i];
+        free(dbdz);
+    }
     ps3o_fftxyp2s(m, pres, rs);
     ps3o_fftcosine(m, rs);
     for (size_t i = 0; i < N; ++i) rs[i] = m->green[i] * rs[i];
     ps3o_fftcosine(m, rs);
+    if (m->cfg.buoyancy) {
+        /* fields_derived.f90:142-151 */
+        for (size_t c = 0; c < m->ncol; ++c) {
+            const size_t o = c * m->nz1;
+            for (int iz = 0; iz <= m->nz; ++iz)
+                rs[o + iz] = rs[o + iz] + m->sbuoy[o + m->nz] * m->k2l2i[c] * m->dphip[o + iz] +
+                             m->sbuoy[o] * m->k2l2i[c] * m->dphim[o + iz];
+        }
+    }
     ps3o_fftxys2p(m, rs, pres);
     free(xs); free(rs); free(dudx); free(dudy); free(dvdy); free(dwdx); free(dwdy);
 }

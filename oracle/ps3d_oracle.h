@@ -170,7 +170,8 @@ double ps3o_rolling_mean_next(ps3o_model *m, double v);
  * a is column-major 3x3 (only the upper triangle is read), eigs descending. */
 int ps3o_jacobi_eigenvalues(double a[9], double eigs[3]);
 
-/* derived fields (fields_derived.f90:67-182, buoyancy disabled) from the
+/* derived fields (fields_derived.f90:67-182, with the buoyancy terms on
+ * buoyancy models) from the
  * current vel/vor/svel; outputs physical (nz+1, ny, nx) */
 void ps3o_pressure(ps3o_model *m, double *pres);
 void ps3o_horizontal_divergence(ps3o_model *m, double *delta);

@@ -29,6 +29,8 @@ EXPORTS = [
     "ps3d_gpu_energy_series_noalloc", "ps3d_gpu_advance_graph", "ps3d_gpu_batch_advance",
     "ps3d_gpu_tuning", "ps3d_gpu_set_tuning", "ps3d_gpu_derived_fields",
     "ps3d_gpu_ke_spectrum", "ps3d_gpu_host_alloc", "ps3d_gpu_host_free",
+    "ps3d_gpu_setup_fields_buoyancy", "ps3d_gpu_buoyancy_params", "ps3d_gpu_set_diffusion_vb",
+    "ps3d_gpu_buoyancy_diagnostics",
 ]
 
 
@@ -48,6 +50,10 @@ class Config(ctypes.Structure):
         ("hold_source", ctypes.c_int),
         ("f_cor", ctypes.c_double * 3),
         ("precision", ctypes.c_int), ("device", ctypes.c_int),
+        ("buoyancy", ctypes.c_int), ("bfsq", ctypes.c_double), ("bfsq_given", ctypes.c_int),
+        ("buoy_nnu", ctypes.c_int), ("buoy_prediss", ctypes.c_double),
+        ("buoy_pretype", ctypes.c_int), ("buoy_length_scale", ctypes.c_int),
+        ("buoy_roll_mean_win_size", ctypes.c_int),
     ]
 
 
@@ -57,7 +63,8 @@ class Diag(ctypes.Structure):
     _fields_ = [(n, ctypes.c_double) for n in (
         "t", "dt", "ke", "en", "hel", "vortmax", "vortrms", "vorch")] + [
         ("vormean", ctypes.c_double * 3)] + [(n, ctypes.c_double) for n in (
-            "ggmax", "usggmax", "lsggmax", "umax", "vmax", "wmax", "bfmax", "rmv", "pref")]
+            "ggmax", "usggmax", "lsggmax", "umax", "vmax", "wmax", "bfmax", "rmv", "pref",
+            "rmb", "bpref")]
 
     def as_dict(self):
         d = {n: getattr(self, n) for n, _ in self._fields_ if n != "vormean"}
@@ -101,6 +108,10 @@ def lib(build_if_missing=True):
     L.ps3d_gpu_source.argtypes = [_vp]
     L.ps3d_gpu_adapt.argtypes = [_vp, ctypes.c_double, _dp, ctypes.POINTER(Diag)]
     L.ps3d_gpu_set_diffusion.argtypes = [_vp, ctypes.c_double, ctypes.c_double]
+    L.ps3d_gpu_set_diffusion_vb.argtypes = [_vp, ctypes.c_double, ctypes.c_double, ctypes.c_double]
+    L.ps3d_gpu_setup_fields_buoyancy.argtypes = [_vp, _dp, _dp, _dp, _dp, _dp]
+    L.ps3d_gpu_buoyancy_params.argtypes = [_vp, _dp, _dp]
+    L.ps3d_gpu_buoyancy_diagnostics.argtypes = [_vp, _dp]
     L.ps3d_gpu_step.argtypes = [_vp, _dp, ctypes.c_double]
     L.ps3d_gpu_advance.argtypes = [_vp, _dp, ctypes.c_int, ctypes.POINTER(Diag)]
     L.ps3d_gpu_advance_host.argtypes = [_vp, _dp, _dp, ctypes.POINTER(Diag)]

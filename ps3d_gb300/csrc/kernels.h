@@ -167,10 +167,10 @@ void op_rk4_factors(const Dims &d, cudaStream_t st, const double *vdiss, const d
                     double *emq, double *epq2, double *emq2);
 template <typename T>
 void op_cn2_init(const Dims &d, cudaStream_t st, double *vortsm, const double *svor, const T *svorts,
-                 double dt2);
+                 double dt2, int ncomp = 3);
 template <typename T>
 void op_cn2_update(const Dims &d, cudaStream_t st, double *svor, const double *vortsm, const T *svorts,
-                   const double *filt0, const double *fz, const double *vdiss, double dt2);
+                   const double *filt0, const double *fz, const double *vdiss, double dt2, int ncomp = 3);
 void op_mean_fix(const Dims &d, cudaStream_t st, double *svor, const double *dstsum, double fnzi,
                  const double *ini, double *savg_out, int apply, float *svor32 = nullptr);
 // mixed-form stage updates (FP64 state, FP32 source, state copy and
@@ -208,6 +208,33 @@ template <typename T>
 void red_pass2(const Dims &d, cudaStream_t st, const T *vor, const T *g5, double vortrms, double *part,
                double *result, int *flag, const double *res1 = nullptr, double ncell = 1.0);
 int red_nblocks(const Dims &d);
+
+// buoyancy.cu: diffz pieces, flux products, tendency assembly, maximum
+// buoyancy frequency and buoyancy diagnostics
+template <typename T>
+void op_dphi_tables(const Dims &d, cudaStream_t st, const double *k2l2, const double *zm, const double *zp, double Lz,
+                    T *dphim, T *dphip);
+template <typename T> void op_dz_sine(const Dims &d, cudaStream_t st, const double *rkz, const T *fs, T *as);
+template <typename T>
+void op_dz_join(const Dims &d, cudaStream_t st, const T *fs, const T *dphim, const T *dphip, const T *as, T *ds);
+template <typename T> void op_bflux(const Dims &d, cudaStream_t st, const T *vel, const T *b, T *f);
+template <typename T>
+void op_btend(const Dims &d, cudaStream_t st, const Deriv &D, const T *fu, const T *fv, const T *wsemi, const T *zs,
+              double bfsq, T *out);
+template <typename T> void op_addf(const Dims &d, cudaStream_t st, T *f, const T *g);
+void op_sub_zprof(const Dims &d, cudaStream_t st, double *f, const double *prof);
+template <typename T>
+void op_pres_buoy_rhs(const Dims &d, cudaStream_t st, const T *b, const T *zeta, double dzi, double fz, T *out);
+template <typename T>
+void op_pres_buoy_bc(const Dims &d, cudaStream_t st, const T *sb, const double *k2l2i, const T *dphim, const T *dphip,
+                     T *rs);
+template <typename T>
+void op_bgrad_max(const Dims &d, cudaStream_t st, const T *bx, const T *by, const T *b, double dzi, double bfsq,
+                  unsigned long long *out);
+long long bdiag_blocks(const Dims &d);
+template <typename T>
+void op_bdiag(const Dims &d, cudaStream_t st, const T *b, const T *bx, const T *by, const T *vor, double dzi,
+              double bfsq, double *part, double *out);
 constexpr int RED1_N = 12;  // values of pass 1
 constexpr int RED2_N = 5;   // values of pass 2
 

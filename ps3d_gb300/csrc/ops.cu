@@ -816,9 +816,10 @@ __global__ void k_cn2_init(Dims d, double *__restrict__ vortsm, const double *__
     for (int iz = threadIdx.x; iz <= d.nz; iz += 32) vortsm[o + iz] = svor[o + iz] + dt2 * (double)svorts[o + iz];
 }
 template <typename T>
-void op_cn2_init(const Dims &d, cudaStream_t st, double *vortsm, const double *svor, const T *svorts, double dt2)
+void op_cn2_init(const Dims &d, cudaStream_t st, double *vortsm, const double *svor, const T *svorts, double dt2,
+                 int ncomp)
 {
-    for (int c = 0; c < 3; ++c)
+    for (int c = 0; c < ncomp; ++c)
         k_cn2_init<T><<<col_grid(d), COL_BLOCK, 0, st>>>(d, vortsm + c * d.nfield, svor + c * d.nfield,
                                                          svorts + c * d.nfield, dt2);
 }
@@ -839,9 +840,9 @@ __global__ void k_cn2_update(Dims d, double *__restrict__ svor, const double *__
 }
 template <typename T>
 void op_cn2_update(const Dims &d, cudaStream_t st, double *svor, const double *vortsm, const T *svorts,
-                   const double *filt0, const double *fz, const double *vdiss, double dt2)
+                   const double *filt0, const double *fz, const double *vdiss, double dt2, int ncomp)
 {
-    for (int c = 0; c < 3; ++c)
+    for (int c = 0; c < ncomp; ++c)
         k_cn2_update<T><<<col_grid(d), COL_BLOCK, 0, st>>>(d, svor + c * d.nfield, vortsm + c * d.nfield,
                                                            svorts + c * d.nfield, filt0, fz, vdiss, dt2);
 }
@@ -1294,9 +1295,9 @@ void op_hyperbolic_tables(const Dims &d, cudaStream_t st, const double *k2l2, co
                                   const double *, const double *, double, double);                             \
     template void op_rk4_sub4<T>(const Dims &, cudaStream_t, double *, const double *, const T *,             \
                                  const double *, const double *, double);                                      \
-    template void op_cn2_init<T>(const Dims &, cudaStream_t, double *, const double *, const T *, double);    \
+    template void op_cn2_init<T>(const Dims &, cudaStream_t, double *, const double *, const T *, double, int); \
     template void op_cn2_update<T>(const Dims &, cudaStream_t, double *, const double *, const T *,           \
-                                   const double *, const double *, const double *, double);                    \
+                                   const double *, const double *, const double *, double, int);               \
     template void red_pass1<T>(const Dims &, cudaStream_t, const T *, const T *, double *, double *);         \
     template void red_pass2<T>(const Dims &, cudaStream_t, const T *, const T *, double, double *, double *,  \
                                int *, const double *, double);                                                 \

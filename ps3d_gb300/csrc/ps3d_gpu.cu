@@ -62,7 +62,7 @@ struct StepScal {
     double dt;         // time step of the current step
     double t;          // model time at the start of the next step
     double dfac;       // diffusion factor of vdiss (impl-diff-rk4: pref dt / 2)
-    double diag[20];   // ps3d_gpu_diag of the last step, field by field
+    double diag[22];   // ps3d_gpu_diag of the last step, field by field
     double sma;        // rolling mean of the strain maximum (rolling_mean.f90)
     int inew, iold, filled;
     int err;           // 1 non-finite diagnostic, 2 Jacobi sweep limit
@@ -128,6 +128,19 @@ struct ps3d_gpu_ctx {
     // shell sums, shell counts
     double *spec_buf = nullptr;
     int spec_kmax = -1;
+    // buoyancy (the reference's ENABLE_BUOYANCY build): the FP64 state b'
+    // (mixed-spectral) with its RK accumulators (sbuoyf holds FP32
+    // increments in the mixed form) and cn2 predictor, the FP32 copy read by
+    // the mixed form, transient fields of type T, per-column factors
+    double *sbuoy = nullptr, *sbuoyi = nullptr, *sbuoyf = nullptr, *bsm = nullptr;
+    float *sbuoy32 = nullptr;
+    void *buoy = nullptr, *sbuoys = nullptr, *heldb = nullptr, *dphim = nullptr, *dphip = nullptr;
+    double *bhdis = nullptr, *bdiss = nullptr, *bpq = nullptr, *bmq = nullptr, *bpq2 = nullptr, *bmq2 = nullptr;
+    double *bpart = nullptr, *bres = nullptr, *bprof = nullptr;
+    unsigned long long *bmax = nullptr;
+    std::vector<double> h_bbarz;
+    double bfsq = 0.0, bvisc = 0.0;
+    Rolling roll_b;
 
     Deriv D() const { return Deriv{cx, cy}; }
     Tables tables() const
@@ -434,10 +447,127 @@ template <typename T> void project_source(ps3d_gpu_ctx *c)
     c->launches += 2;
 }
 
+// ----------------------------------------------------------------- buoyancy
+// The buoyancy state b' as read by the transforms (FP32 copy in the mixed form)
+template <typename T> const T *sbuoy_T(ps3d_gpu_ctx *c)
+{
+    if (sizeof(T) == sizeof(double)) return reinterpret_cast<const T *>(c->sbuoy);
+    return reinterpret_cast<const T *>(c->sbuoy32);
+}
+
+// FP32 copy of b' after an update from outside the stage kernels
+void refresh_b32(ps3d_gpu_ctx *c)
+{
+    if (c->fp64 || !c->cfg.buoyancy) return;
+    op_narrow(c->st, c->sbuoy, c->sbuoy32, c->d.nfield);
+    c->launches += 1;
+}
+
+// semi-spectral b' into bs and the physical b' into c->buoy
+// (field_combine_physical(sbuoy, buoy), inversion.f90:243)
+template <typename T> void buoy_physical(ps3d_gpu_ctx *c, T *bs)
+{
+    col<T>(c, COL_COMBINE, sbuoy_T<T>(c), bs);
+    xyi<T>(c, bs, tf<T>(c->buoy));
+}
+
+// semi-spectral z derivative of a mixed-spectral field before its
+// decomposition (diffz, inversion_utils.f90:683-719): the linear part from
+// the boundary rows and dphim / dphip plus the cosine transform of the
+// differentiated sine series; as is scratch
+template <typename T> void diffz_semi(ps3d_gpu_ctx *c, const T *fs, T *ds, T *as)
+{
+    const Dims &d = c->d;
+    op_dz_sine<T>(d, c->st, c->rkz, fs, as);
+    col<T>(c, COL_DCT, as, as);
+    op_dz_join<T>(d, c->st, fs, tf<T>(c->dphim), tf<T>(c->dphip), as, ds);
+    c->launches += 2;
+}
+
+// buoyancy_tendency (inversion.f90:232-292).  The reference decomposes each
+// flux, differentiates it, combines it back to physical space and finally
+// decomposes the sum.  D_x and D_y commute with the decomposition (the
+// harmonic functions depend on |k| only, equal at a column and its partner)
+// and decompose(combine(f)) = f, so the same tendency is
+//   sbuoys = decompose(-D_x F(u b) - D_y F(v b) - N^2 F(w) - Dz(decompose F(w b))),
+// F the forward horizontal transform, F(w) the semi-spectral w (svel) and Dz
+// the semi-spectral derivative of diffz: 4 horizontal and 4 column
+// transforms instead of 8 and 10.  Leaves the physical b' in c->buoy.
+template <typename T> void buoyancy_tendency(ps3d_gpu_ctx *c)
+{
+    const Dims &d = c->d;
+    const long long N = d.nfield;
+    T *bs = tmpf<T>(c, 0), *fl = tmpf<T>(c, 1), *as = tmpf<T>(c, 4);
+    T *fu = fl, *fv = fl + N, *fw = fl + 2 * N;
+    T *sb = tf<T>(c->sbuoys);
+    buoy_physical<T>(c, bs);
+    op_bflux<T>(d, c->st, tf<T>(c->vel), tf<T>(c->buoy), fl);
+    c->launches += 1;
+    for (int k = 0; k < 3; ++k) xyf<T>(c, fl + k * N, fl + k * N);
+    col<T>(c, COL_DECOMP, fw, fw);
+    diffz_semi<T>(c, fw, bs, as);
+    op_btend<T>(d, c->st, c->D(), fu, fv, tf<T>(c->svel) + 2 * N, bs, c->bfsq, sb);
+    c->launches += 1;
+    col<T>(c, COL_DECOMP, sb, sb);
+}
+
+// Maximum buoyancy frequency (advance.f90:147-168): sqrt(sqrt(max(b_x^2 +
+// b_y^2 + (b_z + N^2)^2))) from the horizontal derivatives of the
+// semi-spectral b' and the central z difference of the physical b'.
+template <typename T> int buoyancy_frequency_max(ps3d_gpu_ctx *c, double *bfmax)
+{
+    const Dims &d = c->d;
+    T *bs = tmpf<T>(c, 0), *bx = tmpf<T>(c, 1), *by = tmpf<T>(c, 2);
+    buoy_physical<T>(c, bs);
+    op_diff<T>(d, c->st, c->D(), 0, bs, bx);
+    op_diff<T>(d, c->st, c->D(), 1, bs, by);
+    c->launches += 2;
+    xyi<T>(c, bx, bx);
+    xyi<T>(c, by, by);
+    op_bgrad_max<T>(d, c->st, bx, by, tf<T>(c->buoy), c->dzi, c->bfsq, c->bmax);
+    c->launches += 1;
+    unsigned long long bits = 0;
+    cudaMemcpyAsync(&bits, c->bmax, sizeof(bits), cudaMemcpyDeviceToHost, c->st);
+    const int rc = sync_check(c, "bfmax");
+    if (rc) return rc;
+    double mx;
+    memcpy(&mx, &bits, sizeof(mx));
+    *bfmax = sqrt(sqrt(mx));
+    return PS3D_OK;
+}
+
+// Buoyancy diagnostics: available potential energy, buoyancy-gradient
+// integral, minimum static stability, minimum Richardson number
+// (field_diagnostics.f90:29-60, 351-397, 327-344, 268-287)
+template <typename T> int buoyancy_diagnostics(ps3d_gpu_ctx *c, double out[4])
+{
+    const Dims &d = c->d;
+    T *bs = tmpf<T>(c, 0), *bx = tmpf<T>(c, 1), *by = tmpf<T>(c, 2);
+    buoy_physical<T>(c, bs);
+    op_diff<T>(d, c->st, c->D(), 0, bs, bx);
+    op_diff<T>(d, c->st, c->D(), 1, bs, by);
+    c->launches += 2;
+    xyi<T>(c, bx, bx);
+    xyi<T>(c, by, by);
+    op_bdiag<T>(d, c->st, tf<T>(c->buoy), bx, by, tf<T>(c->vor), c->dzi, c->bfsq, c->bpart, c->bres);
+    c->launches += 2;
+    double r[4];
+    cudaMemcpyAsync(r, c->bres, sizeof(r), cudaMemcpyDeviceToHost, c->st);
+    const int rc = sync_check(c, "buoyancy diagnostics");
+    if (rc) return rc;
+    out[0] = r[0] / (2.0 * c->bfsq) * c->ncelli;
+    out[1] = r[1] * c->ncelli;
+    out[2] = 1.0 + r[2] / c->bfsq;
+    out[3] = r[3];
+    return PS3D_OK;
+}
+
 // ------------------------------------------------------------------- source
-// vorticity_tendency (inversion.f90:298-371)
+// source (inversion.f90:376-388): buoyancy_tendency, then vorticity_tendency
+// (:298-371) with the buoyancy in r = u eta - v xi + b
 template <typename T> int source(ps3d_gpu_ctx *c)
 {
+    if (c->cfg.buoyancy) buoyancy_tendency<T>(c);
     const Dims &d = c->d;
     const long long N = d.nfield;
     T *vor = tf<T>(c->vor), *vel = tf<T>(c->vel), *svorts = tf<T>(c->svorts);
@@ -462,6 +592,10 @@ template <typename T> int source(ps3d_gpu_ctx *c)
         op_diffz<T>(d, c->st, c->dzi, q, gq);
         op_diffz<T>(d, c->st, c->dzi, p, gp);
         c->launches += 3;
+    }
+    if (c->cfg.buoyancy) {
+        op_addf<T>(d, c->st, r, tf<T>(c->buoy));  // c->buoy from buoyancy_tendency
+        c->launches += 1;
     }
     T *f5[5] = {r, q, p, gq, gp};
     if (sizeof(T) == sizeof(float)) {
@@ -495,15 +629,35 @@ template <typename T> int energy(ps3d_gpu_ctx *c, double out[RED1_N])
     return sync_check(c, "energy");
 }
 
-int set_diffusion(ps3d_gpu_ctx *c, double dt, double pref);
+int set_diffusion(ps3d_gpu_ctx *c, double dt, double pref, double bpref);
 
-// adapt (advance.f90:109-377) and get_diffusion_pre_factor (:381-410)
+// get_diffusion_pre_factor (advance.f90:381-410)
+double pre_factor(int pretype, double vorch, double bfmax, double rmv, double rmb, double ggmax, double usggmax)
+{
+    switch (pretype) {
+    case PS3D_PRE_CONSTANT: return 1.0;
+    case PS3D_PRE_VORCH: return vorch;
+    case PS3D_PRE_BFMAX: return bfmax;
+    case PS3D_PRE_ROLL_MEAN_BFMAX: return rmb;
+    case PS3D_PRE_MAX_STRAIN: return ggmax;
+    case PS3D_PRE_US_MAX_STRAIN: return usggmax;
+    default: return rmv;
+    }
+}
+
+// adapt (advance.f90:109-377)
 template <typename T> int adapt(ps3d_gpu_ctx *c, double t, double *dt_out, ps3d_gpu_diag *diag)
 {
     const Dims &d = c->d;
     const long long N = d.nfield;
+    double bfmax = 0.0;
+    int rc;
+    if (c->cfg.buoyancy) {
+        rc = buoyancy_frequency_max<T>(c, &bfmax);
+        if (rc) return rc;
+    }
     double r1[RED1_N];
-    int rc = energy<T>(c, r1);
+    rc = energy<T>(c, r1);
     if (rc) return rc;
     const double vortmax = sqrt(r1[0]);
     const double vortrms = sqrt(r1[1] / (double)c->ncell);
@@ -526,24 +680,19 @@ template <typename T> int adapt(ps3d_gpu_ctx *c, double t, double *dt_out, ps3d_
     const double vorch = r2[1] / (small + r2[0]);
     const double ggmax = r2[2], usggmax = r2[3], lsggmax = r2[4];
     const double umax = r1[7], vmax = r1[8], wmax = r1[9];
-    const double bfmax = 0.0;
     const double dtcfl = c->cfg.cflmax * fmin(fmin(c->dx[0] / (umax + small), c->dx[1] / (vmax + small)),
                                               c->dx[2] / (wmax + small));
     const double dt = fmin(fmin(c->cfg.alpha / (ggmax + small), c->cfg.alpha / (bfmax + small)),
                            fmin(dtcfl, c->cfg.time_limit - t));
+    // the buoyancy rolling mean is taken before the strain one (:358-366)
+    const double rmb = c->cfg.buoyancy ? c->roll_b.next(bfmax) : 0.0;
     const double rmv = c->roll.next(ggmax);
-    double val;
-    switch (c->cfg.pretype) {
-    case PS3D_PRE_CONSTANT: val = 1.0; break;
-    case PS3D_PRE_VORCH: val = vorch; break;
-    case PS3D_PRE_BFMAX: val = bfmax; break;
-    case PS3D_PRE_MAX_STRAIN: val = ggmax; break;
-    case PS3D_PRE_US_MAX_STRAIN: val = usggmax; break;
-    default: val = rmv; break;
-    }
-    if (!std::isfinite(dt) || !std::isfinite(r1[1]) || !std::isfinite(r1[2]))
+    const double val = pre_factor(c->cfg.pretype, vorch, bfmax, rmv, rmb, ggmax, usggmax);
+    const double bval =
+        c->cfg.buoyancy ? pre_factor(c->cfg.buoy_pretype, vorch, bfmax, rmv, rmb, ggmax, usggmax) : 0.0;
+    if (!std::isfinite(dt) || !std::isfinite(r1[1]) || !std::isfinite(r1[2]) || !std::isfinite(bfmax))
         return fail(c, PS3D_ERR_NONFINITE, "adapt: non-finite diagnostic");
-    rc = set_diffusion(c, dt, val);
+    rc = set_diffusion(c, dt, val, bval);
     if (rc) return rc;
     if (diag) {
         diag->t = t;
@@ -564,6 +713,8 @@ template <typename T> int adapt(ps3d_gpu_ctx *c, double t, double *dt_out, ps3d_
         diag->bfmax = bfmax;
         diag->rmv = rmv;
         diag->pref = val;
+        diag->rmb = rmb;
+        diag->bpref = bval;
     }
     *dt_out = dt;
     return PS3D_OK;
@@ -577,14 +728,20 @@ __global__ void k_vdiss(long long n, const double *vhdis, double *vdiss, double 
     vdiss[i] = cn2 ? 1.0 / (1.0 + dfac * vhdis[i]) : dfac * vhdis[i];
 }
 
-int set_diffusion(ps3d_gpu_ctx *c, double dt, double pref)
+int set_diffusion(ps3d_gpu_ctx *c, double dt, double pref, double bpref)
 {
     if (!c->diffusion_ready) return fail(c, PS3D_ERR_NOT_READY, "set_diffusion before init_diffusion");
     const bool cn2 = c->cfg.stepper == PS3D_CN2;
+    const unsigned nb = (unsigned)((c->d.ncol + 255) / 256);
     // impl_rk4_set_diffusion (impl_rk4.f90:37-53), cn2_set_diffusion (cn2.f90:40-77)
     const double dfac = cn2 ? ((c->cfg.nnu == 1) ? dt : pref * dt) : 0.5 * pref * dt;
-    k_vdiss<<<(unsigned)((c->d.ncol + 255) / 256), 256, 0, c->st>>>(c->d.ncol, c->vhdis, c->vdiss, dfac, cn2);
+    k_vdiss<<<nb, 256, 0, c->st>>>(c->d.ncol, c->vhdis, c->vdiss, dfac, cn2);
     c->launches += 1;
+    if (c->cfg.buoyancy) {
+        const double dbac = cn2 ? ((c->cfg.buoy_nnu == 1) ? dt : bpref * dt) : 0.5 * bpref * dt;
+        k_vdiss<<<nb, 256, 0, c->st>>>(c->d.ncol, c->bhdis, c->bdiss, dbac, cn2);
+        c->launches += 1;
+    }
     return check(c, "set_diffusion");
 }
 
@@ -592,6 +749,8 @@ template <typename T> int rhs_or_hold(ps3d_gpu_ctx *c)
 {
     if (c->cfg.hold_source) {
         cudaMemcpyAsync(c->svorts, c->held, 3 * c->d.nfield * sizeof(T), cudaMemcpyDeviceToDevice, c->st);
+        if (c->cfg.buoyancy)
+            cudaMemcpyAsync(c->sbuoys, c->heldb, c->d.nfield * sizeof(T), cudaMemcpyDeviceToDevice, c->st);
         return check(c, "hold");
     }
     int rc = vor2vel<T>(c);
@@ -615,14 +774,31 @@ template <typename T> int step_rk4(ps3d_gpu_ctx *c, double *t, double dt)
         k_set_dt<<<1, 1, 0, c->st>>>(c->sc, dt);
         c->launches += 1;
     }
-    if (c->cfg.hold_source)
+    const bool buoy = c->cfg.buoyancy != 0;
+    if (c->cfg.hold_source) {
         cudaMemcpyAsync(c->held, c->svorts, 3 * N * sizeof(T), cudaMemcpyDeviceToDevice, c->st);
+        if (buoy) cudaMemcpyAsync(c->heldb, c->sbuoys, N * sizeof(T), cudaMemcpyDeviceToDevice, c->st);
+    }
     op_rk4_factors(d, c->st, c->vdiss, c->filt0, c->epq, c->emq, c->epq2, c->emq2);
     c->launches += 1;
+    if (buoy) {
+        op_rk4_factors(d, c->st, c->bdiss, c->filt0, c->bpq, c->bmq, c->bpq2, c->bmq2);
+        c->launches += 1;
+    }
     const bool mixed = sizeof(T) == sizeof(float);
     float *s32 = reinterpret_cast<float *>(sv), *q32 = c->svor32;
     // mixed: the accumulator's FP32 increments live in the (FP64-sized) svorf
     float *acc = reinterpret_cast<float *>(c->svorf);
+    // buoyancy: the same substeps with its own factors (impl_rk4.f90:99-195)
+    T *sb = tf<T>(c->sbuoys);
+    float *sb32 = reinterpret_cast<float *>(sb), *accb = reinterpret_cast<float *>(c->sbuoyf);
+    if (buoy) {
+        if (mixed)
+            op_rk4m_sub1(d, c->st, c->sbuoy, c->sbuoyi, accb, sb32, c->sbuoy32, c->filt0, c->bmq, dtp);
+        else
+            op_rk4_sub1<T>(d, c->st, c->sbuoy, c->sbuoyi, c->sbuoyf, sb, c->filt0, c->bmq, dt2, dt6);
+        c->launches += 1;
+    }
     for (int k = 0; k < 3; ++k) {
         if (mixed)
             op_rk4m_sub1(d, c->st, c->svor + k * N, c->svori + k * N, acc + k * N, s32 + k * N, q32 + k * N,
@@ -635,6 +811,13 @@ template <typename T> int step_rk4(ps3d_gpu_ctx *c, double *t, double dt)
     int rc = rhs_or_hold<T>(c);
     if (rc) return rc;
     if (t) *t += dt2;
+    if (buoy) {
+        if (mixed)
+            op_rk4m_sub23(d, c->st, c->sbuoy, c->sbuoyi, accb, sb32, c->sbuoy32, c->bpq, c->bmq, dtp, false);
+        else
+            op_rk4_sub23<T>(d, c->st, c->sbuoy, c->sbuoyi, c->sbuoyf, sb, c->bpq, c->bmq, dt2, dt3);
+        c->launches += 1;
+    }
     for (int k = 0; k < 3; ++k) {
         if (mixed)
             op_rk4m_sub23(d, c->st, c->svor + k * N, c->svori + k * N, acc + k * N, s32 + k * N, q32 + k * N,
@@ -647,6 +830,13 @@ template <typename T> int step_rk4(ps3d_gpu_ctx *c, double *t, double dt)
     rc = rhs_or_hold<T>(c);
     if (rc) return rc;
     if (t) *t += dt2;
+    if (buoy) {
+        if (mixed)
+            op_rk4m_sub23(d, c->st, c->sbuoy, c->sbuoyi, accb, sb32, c->sbuoy32, c->bpq, c->bmq2, dtp, true);
+        else
+            op_rk4_sub23<T>(d, c->st, c->sbuoy, c->sbuoyi, c->sbuoyf, sb, c->bpq, c->bmq2, dt, dt3);
+        c->launches += 1;
+    }
     for (int k = 0; k < 3; ++k) {
         if (mixed)
             op_rk4m_sub23(d, c->st, c->svor + k * N, c->svori + k * N, acc + k * N, s32 + k * N, q32 + k * N,
@@ -658,6 +848,13 @@ template <typename T> int step_rk4(ps3d_gpu_ctx *c, double *t, double dt)
     c->launches += 3;
     rc = rhs_or_hold<T>(c);
     if (rc) return rc;
+    if (buoy) {
+        if (mixed)
+            op_rk4m_sub4(d, c->st, c->sbuoy, c->sbuoyi, accb, sb32, c->sbuoy32, c->bpq2, c->bmq2, dtp);
+        else
+            op_rk4_sub4<T>(d, c->st, c->sbuoy, c->sbuoyf, sb, c->bpq2, c->bmq2, dt6);
+        c->launches += 1;
+    }
     for (int k = 0; k < 3; ++k) {
         if (mixed)
             op_rk4m_sub4(d, c->st, c->svor + k * N, c->svori + k * N, acc + k * N, s32 + k * N, q32 + k * N,
@@ -676,12 +873,22 @@ template <typename T> int step_cn2(ps3d_gpu_ctx *c, double *t, double dt)
 {
     const Dims &d = c->d;
     const double dt2 = 0.5 * dt;
-    T *sv = tf<T>(c->svorts);
-    if (c->cfg.hold_source)
+    T *sv = tf<T>(c->svorts), *sb = tf<T>(c->sbuoys);
+    const bool buoy = c->cfg.buoyancy != 0;
+    if (c->cfg.hold_source) {
         cudaMemcpyAsync(c->held, c->svorts, 3 * d.nfield * sizeof(T), cudaMemcpyDeviceToDevice, c->st);
+        if (buoy) cudaMemcpyAsync(c->heldb, c->sbuoys, d.nfield * sizeof(T), cudaMemcpyDeviceToDevice, c->st);
+    }
     // the mixed form re-projects in FP64 after each update: the 3-D filter of
     // cn2 does not commute with the projection
     const bool mixed = sizeof(T) == sizeof(float);
+    // buoyancy first (cn2.f90:107-117, 151-160)
+    if (buoy) {
+        op_cn2_init<T>(d, c->st, c->bsm, c->sbuoy, sb, dt2, 1);
+        op_cn2_update<T>(d, c->st, c->sbuoy, c->bsm, sb, c->filt0, c->fz, c->bdiss, dt2, 1);
+        refresh_b32(c);
+        c->launches += 2;
+    }
     op_cn2_init<T>(d, c->st, c->vortsm, c->svor, sv, dt2);
     op_cn2_update<T>(d, c->st, c->svor, c->vortsm, sv, c->filt0, c->fz, c->vdiss, dt2);
     op_mean_fix(d, c->st, c->svor, c->dstsum, c->fnzi, c->ini, nullptr, 1);
@@ -690,6 +897,11 @@ template <typename T> int step_cn2(ps3d_gpu_ctx *c, double *t, double dt)
     for (int it = 0; it < 2; ++it) {
         int rc = rhs_or_hold<T>(c);
         if (rc) return rc;
+        if (buoy) {
+            op_cn2_update<T>(d, c->st, c->sbuoy, c->bsm, sb, c->filt0, c->fz, c->bdiss, dt2, 1);
+            refresh_b32(c);
+            c->launches += 1;
+        }
         op_cn2_update<T>(d, c->st, c->svor, c->vortsm, sv, c->filt0, c->fz, c->vdiss, dt2);
         op_mean_fix(d, c->st, c->svor, c->dstsum, c->fnzi, c->ini, nullptr, 1);
         if (mixed) project_state_mixed(c);
@@ -791,6 +1003,8 @@ __global__ void k_adapt_scalars(StepScal *sc, double *hist, const double *__rest
     g[17] = bfmax;
     g[18] = sma;
     g[19] = val;
+    g[20] = 0.0;  // no buoyancy in captured steps
+    g[21] = 0.0;
     // the stepper advances t by dt/2 twice (impl_rk4.f90)
     const double dt2 = 0.5 * dt;
     sc->t = (t + dt2) + dt2;
@@ -840,8 +1054,9 @@ int advance_dev(ps3d_gpu_ctx *c)
 
 int graph_supported(ps3d_gpu_ctx *c)
 {
-    if (c->fp64 || c->cfg.stepper == PS3D_CN2 || c->cfg.hold_source)
-        return fail(c, PS3D_ERR_INVALID_ARG, "captured steps need the mixed form, impl-diff-rk4, no held source");
+    if (c->fp64 || c->cfg.stepper == PS3D_CN2 || c->cfg.hold_source || c->cfg.buoyancy)
+        return fail(c, PS3D_ERR_INVALID_ARG,
+                    "captured steps need the mixed form, impl-diff-rk4, no held source, no buoyancy");
     if (!c->diffusion_ready) return fail(c, PS3D_ERR_NOT_READY, "advance before init_diffusion");
     return PS3D_OK;
 }
@@ -913,7 +1128,7 @@ int graph_finish(ps3d_gpu_ctx *c, double *t, ps3d_gpu_diag *diag)
     c->roll.filled = h.filled != 0;
     *t = h.t;
     if (diag) {
-        static_assert(sizeof(ps3d_gpu_diag) == 20 * sizeof(double), "diag layout");
+        static_assert(sizeof(ps3d_gpu_diag) == 22 * sizeof(double), "diag layout");
         memcpy(diag, h.diag, sizeof(h.diag));
     }
     if (h.err & 2) return fail(c, PS3D_ERR_DEVICE_LIMIT, "adapt: Jacobi sweep limit reached");
@@ -922,8 +1137,9 @@ int graph_finish(ps3d_gpu_ctx *c, double *t, ps3d_gpu_diag *diag)
 }
 
 // ---------------------------------------------------------- derived fields
-// pressure and horizontal divergence (fields_derived.f90:67-182, buoyancy
-// disabled) from the current vel / vor / svel; physical fields to the host
+// pressure and horizontal divergence (fields_derived.f90:67-182) from the
+// current vel / vor / svel (and b' on buoyancy contexts); physical fields to
+// the host
 template <typename T> int derived_fields(ps3d_gpu_ctx *c, double *hp, double *hd)
 {
     const Dims &d = c->d;
@@ -935,11 +1151,20 @@ template <typename T> int derived_fields(ps3d_gpu_ctx *c, double *hp, double *hd
         for (int k = 0; k < 5; ++k) xyi<T>(c, g5 + k * N, g5 + k * N);
         op_pressure_rhs<T>(d, c->st, g5, tf<T>(c->vor), pr);
         c->launches += 1;
+        if (c->cfg.buoyancy) {
+            buoy_physical<T>(c, g5);
+            op_pres_buoy_rhs<T>(d, c->st, tf<T>(c->buoy), tf<T>(c->vor) + 2 * N, c->dzi, c->cfg.f_cor[2], pr);
+            c->launches += 1;
+        }
         xyf<T>(c, pr, pr);
         col<T>(c, COL_DCT, pr, pr);
         op_mul_field<T>(d, c->st, tf<T>(c->green), pr);
         c->launches += 1;
         col<T>(c, COL_DCT, pr, pr);
+        if (c->cfg.buoyancy) {
+            op_pres_buoy_bc<T>(d, c->st, sbuoy_T<T>(c), c->k2l2i, tf<T>(c->dphim), tf<T>(c->dphip), pr);
+            c->launches += 1;
+        }
         xyi<T>(c, pr, pr);
         int rc = download(c, pr, sizeof(T) == sizeof(double), 1, hp);
         if (rc) return rc;
@@ -1043,10 +1268,46 @@ template <typename T> int setup_fields(ps3d_gpu_ctx *c, const double *vor_phys, 
     double r1[RED1_N];
     rc = energy<T>(c, r1);
     if (rc) return rc;
-    const double ke = 0.5 * r1[2] * c->ncelli, ens = 0.5 * r1[1] * c->ncelli;
+    double ke = 0.5 * r1[2] * c->ncelli, ens = 0.5 * r1[1] * c->ncelli;
+    if (c->cfg.buoyancy) {
+        // te = ke + ape, en = enstrophy + buoyancy-gradient integral
+        // (utils.f90:169-180)
+        double bd[4];
+        rc = buoyancy_diagnostics<T>(c, bd);
+        if (rc) return rc;
+        ke = ke + bd[0];
+        ens = ens + bd[1];
+    }
     if (te) *te = ke;
     if (en) *en = ens;
     return ps3d_gpu_init_diffusion(c, ke, ens);
+}
+
+// buoyancy part of setup_fields (utils.f90:149-159): N^2 of the basic state
+// unless given (calculate_basic_reference_state, physics.f90:310-340), the
+// basic state N^2 z removed and the perturbation decomposed in FP64
+template <typename T> int setup_buoyancy(ps3d_gpu_ctx *c, const double *buoy_phys)
+{
+    const Dims &d = c->d;
+    if (!c->cfg.bfsq_given) {
+        double sum = 0.0;
+        const size_t nz1 = (size_t)d.nz + 1;
+        for (long long col = 0; col < d.ncol; ++col) sum += buoy_phys[col * nz1 + d.nz] - buoy_phys[col * nz1];
+        c->bfsq = sum / ((double)d.nx * (double)d.ny * c->cfg.extent[2]);
+    }
+    for (int iz = 0; iz <= d.nz; ++iz) c->h_bbarz[iz] = c->bfsq * (c->cfg.lower[2] + (double)iz * c->dx[2]);
+    cudaMemcpyAsync(c->bprof, c->h_bbarz.data(), (d.nz + 1) * sizeof(double), cudaMemcpyHostToDevice, c->st);
+    double *scratch = c->svori;  // FP64 scratch before the vorticity set-up
+    int rc = upload(c, buoy_phys, 1, scratch, true);
+    if (rc) return rc;
+    op_sub_zprof(d, c->st, scratch, c->bprof);
+    xy_forward<double>(d, c->st, scratch, scratch, c->twx64, c->twy64, nullptr);
+    columns<double>(d, c->st, COL_DECOMP, scratch, c->sbuoy, c->phim64, c->phip64, c->twz2_64, nullptr);
+    c->launches += 4;
+    cudaMemsetAsync(c->sbuoys, 0, d.nfield * sizeof(T), c->st);
+    if (c->bsm) cudaMemsetAsync(c->bsm, 0, d.nfield * sizeof(double), c->st);
+    refresh_b32(c);
+    return check(c, "setup_buoyancy");
 }
 
 template <typename T> int field_op(ps3d_gpu_ctx *c, int op, const double *in, double *out)
@@ -1068,6 +1329,11 @@ template <typename T> int field_op(ps3d_gpu_ctx *c, int op, const double *in, do
     case PS3D_OP_COMBINE_SEMI: col<T>(c, COL_COMBINE, a, b); break;
     case PS3D_OP_DECOMPOSE_PHYS: xyf<T>(c, a, b); col<T>(c, COL_DECOMP, b, b); break;
     case PS3D_OP_COMBINE_PHYS: col<T>(c, COL_COMBINE, a, a); xyi<T>(c, a, b); break;
+    case PS3D_OP_DIFFZ:
+        if (!c->cfg.buoyancy) return fail(c, PS3D_ERR_INVALID_ARG, "field_op: diffz needs a buoyancy context");
+        diffz_semi<T>(c, a, b, tmpf<T>(c, 3));
+        col<T>(c, COL_DECOMP, b, b);
+        break;
     default: return fail(c, PS3D_ERR_INVALID_ARG, "field_op: unknown op");
     }
     rc = check(c, "field_op");
@@ -1261,6 +1527,25 @@ template <typename T> int allocate_fields(ps3d_gpu_ctx *c)
               dalloc(c, &c->dthetam, fb) && dalloc(c, &c->dthetap, fb) && dalloc(c, &c->green, fb);
     if (ok && c->cfg.stepper == PS3D_CN2) ok = dalloc(c, &c->vortsm, 3 * f64);
     if (ok && c->cfg.hold_source) ok = dalloc(c, &c->held, 3 * fb);
+    if (ok && c->cfg.buoyancy) {
+        const size_t P2b = (size_t)d.ncol * sizeof(double);
+        ok = dalloc(c, &c->sbuoy, f64) && dalloc(c, &c->sbuoyi, f64) && dalloc(c, &c->sbuoyf, f64) &&
+             dalloc(c, &c->buoy, fb) && dalloc(c, &c->sbuoys, fb) && dalloc(c, &c->dphim, fb) &&
+             dalloc(c, &c->dphip, fb) && dalloc(c, &c->bhdis, P2b) && dalloc(c, &c->bdiss, P2b) &&
+             dalloc(c, &c->bpq, P2b) && dalloc(c, &c->bmq, P2b) && dalloc(c, &c->bpq2, P2b) &&
+             dalloc(c, &c->bmq2, P2b) && dalloc(c, &c->bpart, (size_t)bdiag_blocks(d) * 4 * sizeof(double)) &&
+             dalloc(c, &c->bres, 4 * sizeof(double)) && dalloc(c, &c->bprof, (d.nz + 1) * sizeof(double)) &&
+             dalloc(c, &c->bmax, sizeof(unsigned long long));
+        if (ok && c->cfg.stepper == PS3D_CN2) ok = dalloc(c, &c->bsm, f64);
+        if (ok && c->cfg.hold_source) ok = dalloc(c, &c->heldb, fb);
+        if (ok && !c->fp64) ok = dalloc(c, &c->sbuoy32, N * sizeof(float));
+        if (ok) {
+            cudaMemsetAsync(c->sbuoy, 0, f64, c->st);
+            cudaMemsetAsync(c->buoy, 0, fb, c->st);
+            cudaMemsetAsync(c->sbuoys, 0, fb, c->st);
+            if (c->sbuoy32) cudaMemsetAsync(c->sbuoy32, 0, N * sizeof(float), c->st);
+        }
+    }
     if (ok && !c->fp64)
         ok = dalloc(c, &c->svor32, 3 * N * sizeof(float)) &&
              dalloc(c, &c->twz32, d.nz * sizeof(float2)) && dalloc(c, &c->sinz32, d.nz * sizeof(float)) &&
@@ -1312,6 +1597,12 @@ template <typename T> int allocate_fields(ps3d_gpu_ctx *c)
                             tf<T>(c->phip), tf<T>(c->thetam), tf<T>(c->thetap), tf<T>(c->dthetam),
                             tf<T>(c->dthetap), tf<T>(c->green));
     c->launches += 1;
+    if (c->cfg.buoyancy) {
+        op_dphi_tables<T>(d, c->st, c->k2l2, c->zm, c->zp, c->cfg.extent[2], tf<T>(c->dphim), tf<T>(c->dphip));
+        c->launches += 1;
+        c->h_bbarz.assign(d.nz + 1, 0.0);
+        for (int iz = 0; iz <= d.nz; ++iz) c->h_bbarz[iz] = c->bfsq * (c->cfg.lower[2] + (double)iz * c->dx[2]);
+    }
     if (!c->fp64) {
         // FP64 harmonic functions for the FP64 set-up and projection; the
         // remaining FP64 outputs go to scratch (svori, svorf)
@@ -1374,8 +1665,12 @@ int ps3d_gpu_create(const ps3d_gpu_config *cfg, ps3d_gpu_ctx **out)
         return PS3D_ERR_UNSUPPORTED_SIZE;
     if (cfg->precision != PS3D_PRECISION_FP64 && cfg->precision != PS3D_PRECISION_MIXED) return PS3D_ERR_INVALID_ARG;
     if (cfg->stepper != PS3D_IMPL_DIFF_RK4 && cfg->stepper != PS3D_CN2) return PS3D_ERR_INVALID_ARG;
-    if (cfg->pretype < 0 || cfg->pretype > 5 || cfg->nnu < 1 || !(cfg->extent[0] > 0) || !(cfg->extent[1] > 0) ||
+    if (cfg->pretype < 0 || cfg->pretype > 6 || cfg->nnu < 1 || !(cfg->extent[0] > 0) || !(cfg->extent[1] > 0) ||
         !(cfg->extent[2] > 0))
+        return PS3D_ERR_INVALID_ARG;
+    // 'bfmax' / 'roll-mean-bfmax' need the buoyancy build (advance.f90:395-407)
+    if (!cfg->buoyancy && cfg->pretype == PS3D_PRE_ROLL_MEAN_BFMAX) return PS3D_ERR_INVALID_ARG;
+    if (cfg->buoyancy && (cfg->buoy_pretype < 0 || cfg->buoy_pretype > 6 || cfg->buoy_nnu < 1))
         return PS3D_ERR_INVALID_ARG;
     int ndev = 0;
     if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev <= cfg->device || cfg->device < 0) {
@@ -1411,6 +1706,8 @@ int ps3d_gpu_create(const ps3d_gpu_config *cfg, ps3d_gpu_ctx **out)
     c->fnzi = 1.0 / (double)nz;
     c->dzi = 1.0 / c->dx[2];
     c->roll.hist.assign(cfg->roll_mean_win_size > 0 ? cfg->roll_mean_win_size : 1000, 0.0);
+    c->roll_b.hist.assign(cfg->buoy_roll_mean_win_size > 0 ? cfg->buoy_roll_mean_win_size : 1000, 0.0);
+    c->bfsq = cfg->buoyancy ? cfg->bfsq : 0.0;
     const int rc = DISPATCH(c, allocate_fields, c);
     if (rc) {
         ps3d_gpu_destroy(c);
@@ -1452,6 +1749,17 @@ int ps3d_gpu_set_field(ps3d_gpu_ctx *c, int which, const double *host)
     case PS3D_FIELD_VEL: rc = upload(c, host, 3, c->vel, c->fp64); break;
     case PS3D_FIELD_SVEL: rc = upload(c, host, 3, c->svel, c->fp64); break;
     case PS3D_FIELD_SVORTS: rc = upload(c, host, 3, c->svorts, c->fp64); break;
+    case PS3D_FIELD_SBUOY:
+    case PS3D_FIELD_BUOY:
+    case PS3D_FIELD_SBUOYS:
+        if (!c->cfg.buoyancy) return fail(c, PS3D_ERR_INVALID_ARG, "set_field: no buoyancy in this context");
+        if (which == PS3D_FIELD_SBUOY) {
+            rc = upload(c, host, 1, c->sbuoy, true);
+            if (!rc) refresh_b32(c);
+        } else {
+            rc = upload(c, host, 1, which == PS3D_FIELD_BUOY ? c->buoy : c->sbuoys, c->fp64);
+        }
+        break;
     default: return fail(c, PS3D_ERR_INVALID_ARG, "set_field: unknown field");
     }
     if (rc) return rc;
@@ -1469,6 +1777,12 @@ int ps3d_gpu_get_field(ps3d_gpu_ctx *c, int which, double *host)
     case PS3D_FIELD_VEL: return download(c, c->vel, c->fp64, 3, host);
     case PS3D_FIELD_SVEL: return download(c, c->svel, c->fp64, 3, host);
     case PS3D_FIELD_SVORTS: return download(c, c->svorts, c->fp64, 3, host);
+    case PS3D_FIELD_SBUOY:
+    case PS3D_FIELD_BUOY:
+    case PS3D_FIELD_SBUOYS:
+        if (!c->cfg.buoyancy) return fail(c, PS3D_ERR_INVALID_ARG, "get_field: no buoyancy in this context");
+        if (which == PS3D_FIELD_SBUOY) return download(c, c->sbuoy, true, 1, host);
+        return download(c, which == PS3D_FIELD_BUOY ? c->buoy : c->sbuoys, c->fp64, 1, host);
     default: return fail(c, PS3D_ERR_INVALID_ARG, "get_field: unknown field");
     }
 }
@@ -1527,6 +1841,19 @@ int ps3d_gpu_get_table(ps3d_gpu_ctx *c, int which, double *host)
     case 13: put(c->h_rkx); return PS3D_OK;
     case 14: put(c->h_rky); return PS3D_OK;
     case 15: put(c->h_rkz); return PS3D_OK;
+    case 16:
+    case 17:
+    case 18:
+    case 19:
+        if (!c->cfg.buoyancy) return fail(c, PS3D_ERR_INVALID_ARG, "get_table: no buoyancy in this context");
+        if (which == 16) return download(c, c->dphim, c->fp64, 1, host);
+        if (which == 17) return download(c, c->dphip, c->fp64, 1, host);
+        if (which == 19) {
+            put(c->h_bbarz);
+            return PS3D_OK;
+        }
+        cudaMemcpyAsync(host, c->bhdis, d.ncol * sizeof(double), cudaMemcpyDeviceToHost, c->st);
+        return sync_check(c, "get_table");
     default: return fail(c, PS3D_ERR_INVALID_ARG, "get_table: unknown table");
     }
 }
@@ -1536,7 +1863,41 @@ int ps3d_gpu_setup_fields(ps3d_gpu_ctx *c, const double *vor_phys, const double 
     int rc = enter(c);
     if (rc) return rc;
     if (!vor_phys) return PS3D_ERR_INVALID_ARG;
+    if (c->cfg.buoyancy)
+        return fail(c, PS3D_ERR_INVALID_ARG, "setup_fields: a buoyancy context needs ps3d_gpu_setup_fields_buoyancy");
     return DISPATCH(c, setup_fields, c, vor_phys, pert, te, en);
+}
+
+int ps3d_gpu_setup_fields_buoyancy(ps3d_gpu_ctx *c, const double *vor_phys, const double *pert,
+                                   const double *buoy_phys, double *te, double *en)
+{
+    int rc = enter(c);
+    if (rc) return rc;
+    if (!vor_phys) return PS3D_ERR_INVALID_ARG;
+    if (!c->cfg.buoyancy) return DISPATCH(c, setup_fields, c, vor_phys, pert, te, en);
+    if (!buoy_phys) return PS3D_ERR_INVALID_ARG;
+    rc = DISPATCH(c, setup_buoyancy, c, buoy_phys);
+    if (rc) return rc;
+    return DISPATCH(c, setup_fields, c, vor_phys, pert, te, en);
+}
+
+int ps3d_gpu_buoyancy_params(ps3d_gpu_ctx *c, double *bfsq, double *bvisc)
+{
+    int rc = enter(c);
+    if (rc) return rc;
+    if (!c->cfg.buoyancy) return fail(c, PS3D_ERR_INVALID_ARG, "buoyancy_params: no buoyancy in this context");
+    if (bfsq) *bfsq = c->bfsq;
+    if (bvisc) *bvisc = c->bvisc;
+    return PS3D_OK;
+}
+
+int ps3d_gpu_buoyancy_diagnostics(ps3d_gpu_ctx *c, double out[4])
+{
+    int rc = enter(c);
+    if (rc) return rc;
+    if (!out) return PS3D_ERR_INVALID_ARG;
+    if (!c->cfg.buoyancy) return fail(c, PS3D_ERR_INVALID_ARG, "buoyancy_diagnostics: no buoyancy in this context");
+    return DISPATCH(c, buoyancy_diagnostics, c, out);
 }
 
 // init_diffusion (inversion_utils.f90:124-218)
@@ -1560,13 +1921,23 @@ int ps3d_gpu_init_diffusion(ps3d_gpu_ctx *c, double te, double en)
         }
         return r;
     };
-    double vis;
-    if (c->cfg.length_scale == PS3D_GEOPHYSICAL) vis = c->cfg.prediss * ipow(rkmsi, p);
-    else vis = c->cfg.prediss * pow(k2max * te / en, 1.0 / 3.0) * ipow(rkmsi, p);
-    c->vvisc = vis;
-    std::vector<double> vh(c->d.ncol);
-    for (long long i = 0; i < c->d.ncol; ++i) vh[i] = (p == 1) ? vis * c->h_k2l2[i] : vis * ipow(c->h_k2l2[i], p);
-    cudaMemcpyAsync(c->vhdis, vh.data(), vh.size() * sizeof(double), cudaMemcpyHostToDevice, c->st);
+    // get_viscosity (:157-185) and init_dissipation (:189-218)
+    auto viscosity = [&](int scale, double prediss, int pp) {
+        if (scale == PS3D_GEOPHYSICAL) return prediss * ipow(rkmsi, pp);
+        return prediss * pow(k2max * te / en, 1.0 / 3.0) * ipow(rkmsi, pp);
+    };
+    auto dissipation = [&](double vis, int pp, double *dst) {
+        std::vector<double> h(c->d.ncol);
+        for (long long i = 0; i < c->d.ncol; ++i) h[i] = (pp == 1) ? vis * c->h_k2l2[i] : vis * ipow(c->h_k2l2[i], pp);
+        cudaMemcpyAsync(dst, h.data(), h.size() * sizeof(double), cudaMemcpyHostToDevice, c->st);
+        cudaStreamSynchronize(c->st);
+    };
+    c->vvisc = viscosity(c->cfg.length_scale, c->cfg.prediss, p);
+    dissipation(c->vvisc, p, c->vhdis);
+    if (c->cfg.buoyancy) {
+        c->bvisc = viscosity(c->cfg.buoy_length_scale, c->cfg.buoy_prediss, c->cfg.buoy_nnu);
+        dissipation(c->bvisc, c->cfg.buoy_nnu, c->bhdis);
+    }
     rc = sync_check(c, "init_diffusion");
     if (rc) return rc;
     c->diffusion_ready = true;
@@ -1602,9 +1973,14 @@ int ps3d_gpu_adapt(ps3d_gpu_ctx *c, double t, double *dt, ps3d_gpu_diag *diag)
 
 int ps3d_gpu_set_diffusion(ps3d_gpu_ctx *c, double dt, double pref)
 {
+    return ps3d_gpu_set_diffusion_vb(c, dt, pref, 0.0);
+}
+
+int ps3d_gpu_set_diffusion_vb(ps3d_gpu_ctx *c, double dt, double vpref, double bpref)
+{
     int rc = enter(c);
     if (rc) return rc;
-    rc = set_diffusion(c, dt, pref);
+    rc = set_diffusion(c, dt, vpref, bpref);
     if (rc) return rc;
     return sync_check(c, "set_diffusion");
 }
@@ -1637,6 +2013,7 @@ int ps3d_gpu_advance_host(ps3d_gpu_ctx *c, double *svor, double *t, ps3d_gpu_dia
     int rc = enter(c);
     if (rc) return rc;
     if (!svor || !t) return PS3D_ERR_INVALID_ARG;
+    if (c->cfg.buoyancy) return fail(c, PS3D_ERR_INVALID_ARG, "advance_host: the state of a buoyancy context includes sbuoy");
     const Dims &d = c->d;
     const size_t bytes = (size_t)3 * d.ncol * (d.nz + 1) * sizeof(double);
     // Page-locked host memory is read and written by the re-pitching

@@ -14,18 +14,22 @@ import numpy as np
 from . import _lib
 
 PRETYPES = {"constant": 0, "vorch": 1, "bfmax": 2, "roll-mean-max-strain": 3,
-            "max-strain": 4, "us-max-strain": 5}
+            "max-strain": 4, "us-max-strain": 5, "roll-mean-bfmax": 6}
 LENGTH_SCALES = {"Kolmogorov": 0, "geophysical": 1}
 FILTERS = {"Hou & Li": 0, "2/3-rule": 1}
 STEPPERS = {"impl-diff-rk4": 0, "cn2": 1}
 PRECISIONS = {"fp64": 0, "mixed": 1}
-FIELDS = {"svor": 0, "vor": 1, "vel": 2, "svel": 3, "svorts": 4}
+FIELDS = {"svor": 0, "vor": 1, "vel": 2, "svel": 3, "svorts": 4,
+          "sbuoy": 5, "buoy": 6, "sbuoys": 7}
+SCALAR_FIELDS = ("sbuoy", "buoy", "sbuoys")
 TABLES = {"k2l2": 0, "k2l2i": 1, "filt": 2, "green": 3, "phim": 4, "phip": 5,
           "thetam": 6, "thetap": 7, "dthetam": 8, "dthetap": 9, "gamtop": 10,
-          "gambot": 11, "vhdis": 12, "rkx": 13, "rky": 14, "rkz": 15}
+          "gambot": 11, "vhdis": 12, "rkx": 13, "rky": 14, "rkz": 15,
+          "dphim": 16, "dphip": 17, "bhdis": 18, "bbarz": 19}
 OPS = {"fftxyp2s": 0, "fftxys2p": 1, "diffx": 2, "diffy": 3, "fftsine": 4,
        "fftcosine": 5, "central_diffz": 6, "decompose_semi_spectral": 7,
-       "combine_semi_spectral": 8, "decompose_physical": 9, "combine_physical": 10}
+       "combine_semi_spectral": 8, "decompose_physical": 9, "combine_physical": 10,
+       "diffz": 11}
 
 _dp = ctypes.POINTER(ctypes.c_double)
 
@@ -44,7 +48,9 @@ def _ptr(a):
 def make_config(nx, ny, nz, lower, extent, nnu=3, prediss=30.0, pretype="vorch",
                 length_scale="Kolmogorov", filtering="Hou & Li", stepper="impl-diff-rk4",
                 cflmax=0.8, alpha=0.1, time_limit=1.0e30, roll_mean_win_size=1000,
-                hold_source=0, f_cor=(0.0, 0.0, 0.0), precision="fp64", device=0, nthreads=0):
+                hold_source=0, f_cor=(0.0, 0.0, 0.0), precision="fp64", device=0, nthreads=0,
+                buoyancy=False, bfsq=None, buoy_nnu=3, buoy_prediss=30.0, buoy_pretype="bfmax",
+                buoy_length_scale="Kolmogorov", buoy_roll_mean_win_size=1000):
     c = _lib.Config()
     c.nx, c.ny, c.nz, c.nnu = nx, ny, nz, nnu
     c.lower[:] = list(lower)
@@ -59,6 +65,14 @@ def make_config(nx, ny, nz, lower, extent, nnu=3, prediss=30.0, pretype="vorch",
     c.f_cor[:] = list(f_cor)
     c.precision = PRECISIONS[precision] if isinstance(precision, str) else int(precision)
     c.device = device
+    c.buoyancy = int(bool(buoyancy))
+    c.bfsq = 0.0 if bfsq is None else float(bfsq)
+    c.bfsq_given = int(bfsq is not None)
+    c.buoy_nnu, c.buoy_prediss = buoy_nnu, buoy_prediss
+    c.buoy_pretype = PRETYPES[buoy_pretype] if isinstance(buoy_pretype, str) else int(buoy_pretype)
+    c.buoy_length_scale = (LENGTH_SCALES[buoy_length_scale] if isinstance(buoy_length_scale, str)
+                           else int(buoy_length_scale))
+    c.buoy_roll_mean_win_size = buoy_roll_mean_win_size
     return c
 
 
@@ -130,28 +144,32 @@ class Ps3dGpu:
     def combine_semi_spectral(self, sf): return self._op("combine_semi_spectral", sf)
     def decompose_physical(self, fc): return self._op("decompose_physical", fc)
     def combine_physical(self, sf): return self._op("combine_physical", sf)
+    def diffz(self, fs): return self._op("diffz", fs)
 
     # -------------------------------------------------------------- state
+    def _fshape(self, name):
+        return self.shape if name in SCALAR_FIELDS else (3,) + self.shape
+
     def get(self, name):
-        out = np.zeros((3,) + self.shape)
+        out = np.zeros(self._fshape(name))
         self._chk(self.L.ps3d_gpu_get_field(self._h, FIELDS[name], _ptr(out)))
         return out
 
     def set(self, name, a):
         a = np.ascontiguousarray(a, dtype=np.float64)
-        assert a.shape == (3,) + self.shape
+        assert a.shape == self._fshape(name)
         self._chk(self.L.ps3d_gpu_set_field(self._h, FIELDS[name], _ptr(a)))
 
     def table(self, name):
         w = TABLES[name]
         n2 = self.nx * self.ny
-        n = {0: n2, 1: n2, 12: n2, 10: self.nz + 1, 11: self.nz + 1, 13: self.nx,
-             14: self.ny, 15: self.nz + 1}.get(w, n2 * (self.nz + 1))
+        n = {0: n2, 1: n2, 12: n2, 18: n2, 10: self.nz + 1, 11: self.nz + 1, 13: self.nx,
+             14: self.ny, 15: self.nz + 1, 19: self.nz + 1}.get(w, n2 * (self.nz + 1))
         out = np.zeros(n)
         self._chk(self.L.ps3d_gpu_get_table(self._h, w, _ptr(out)))
         if n == n2 * (self.nz + 1):
             return out.reshape(self.shape)
-        if n == n2 and w in (0, 1, 12):
+        if n == n2 and w in (0, 1, 12, 18):
             return out.reshape(self.nx, self.ny)
         return out
 
@@ -167,7 +185,9 @@ class Ps3dGpu:
         self._chk(self.L.ps3d_gpu_set_ini_vor_mean(self._h, _ptr(v)))
 
     # ------------------------------------------------- reference routines
-    def setup_fields(self, vor_phys, pert=None):
+    def setup_fields(self, vor_phys, pert=None, buoy=None):
+        """setup_fields (utils.f90:136-184); buoy is the total physical
+        buoyancy of a buoyancy context (zero when omitted)."""
         vor_phys = np.ascontiguousarray(vor_phys, dtype=np.float64)
         assert vor_phys.shape == (3,) + self.shape
         pp = None
@@ -176,9 +196,30 @@ class Ps3dGpu:
             assert pert.shape == (3,) + self.shape
             pp = _ptr(pert)
         te, en = ctypes.c_double(), ctypes.c_double()
-        self._chk(self.L.ps3d_gpu_setup_fields(self._h, _ptr(vor_phys), pp, ctypes.byref(te),
-                                               ctypes.byref(en)))
+        if self.cfg.buoyancy:
+            buoy = np.zeros(self.shape) if buoy is None else np.ascontiguousarray(buoy, dtype=np.float64)
+            assert buoy.shape == self.shape
+            self._chk(self.L.ps3d_gpu_setup_fields_buoyancy(self._h, _ptr(vor_phys), pp, _ptr(buoy),
+                                                            ctypes.byref(te), ctypes.byref(en)))
+        else:
+            self._chk(self.L.ps3d_gpu_setup_fields(self._h, _ptr(vor_phys), pp, ctypes.byref(te),
+                                                   ctypes.byref(en)))
         return te.value, en.value
+
+    def buoyancy_params(self):
+        """(N^2, buoyancy viscosity) of a buoyancy context."""
+        b, v = ctypes.c_double(), ctypes.c_double()
+        self._chk(self.L.ps3d_gpu_buoyancy_params(self._h, ctypes.byref(b), ctypes.byref(v)))
+        return b.value, v.value
+
+    def buoyancy_diagnostics(self):
+        """(ape, gradb integral, min static stability, min Richardson number)"""
+        out = np.zeros(4)
+        self._chk(self.L.ps3d_gpu_buoyancy_diagnostics(self._h, _ptr(out)))
+        return tuple(out)
+
+    def set_diffusion_vb(self, dt, vpref, bpref):
+        self._chk(self.L.ps3d_gpu_set_diffusion_vb(self._h, dt, vpref, bpref))
 
     def init_diffusion(self, te, en):
         self._chk(self.L.ps3d_gpu_init_diffusion(self._h, te, en))
