@@ -302,6 +302,76 @@ int ps3d_gpu_probe_result(ps3d_gpu_ctx *ctx, double *total_ms, long long *launch
 int ps3d_gpu_energy_series_noalloc(const double *vel, const double *vor, int nx, int ny, int nz,
                                    long long pitch, long long comp_stride, void *stream, double *out);
 
+/* ---- learned sub-grid closure --------------------------------------------
+ * No counterpart in the reference, whose only sub-grid model is the
+ * horizontal hyperdiffusion of init_diffusion (inversion_utils.f90:124-218);
+ * that hyperdiffusion stays in force and is the fallback whenever no
+ * closure is attached.
+ *
+ * The network maps the physical vorticity and velocity of a run, each
+ * divided by its rms over the grid points (6 input channels), to a
+ * vorticity-tendency correction in physical space (3 channels): four
+ * 3x3x3 convolutions (periodic in x and y, zero-padded in z), widths
+ * 6 -> 32 -> 32 -> 32 -> 3, GELU after the first three.  Weights and
+ * activations are BF16 on tensor cores with FP32 accumulation; the FP32
+ * master parameters and the Adam moments stay on the device.  The output
+ * is scaled by ct * <|omega|^2> (ct fixed from the training targets), then
+ * taken to the mixed-spectral form and added to svorts.
+ *
+ * Parameter vector (FP32, PS3D_CLOSURE_NPARAM values): for each layer its
+ * weights W[tap][ci][co] (tap = (dx+1)*9 + (dy+1)*3 + (dz+1), the input
+ * point being (ix+dx, iy+dy, iz+dz)) followed by its bias[co].
+ * Host fields: component-major, each component in the reference layout
+ * (0:nz, 0:ny-1, 0:nx-1) column-major. */
+#define PS3D_CLOSURE_NPARAM 63171
+typedef struct ps3d_closure ps3d_closure;
+/* max_samples: training samples held on the device (9 fields each). */
+int ps3d_closure_create(int nx, int ny, int nz, int max_samples, int device, unsigned long long seed,
+                        ps3d_closure **cl);
+/* PS3D_ERR_INVALID_ARG while attached to a context (detach first). */
+int ps3d_closure_destroy(ps3d_closure *cl);
+const char *ps3d_closure_last_error(const ps3d_closure *cl);
+int ps3d_closure_get_params(ps3d_closure *cl, float *params);
+int ps3d_closure_set_params(ps3d_closure *cl, const float *params);
+/* ct: the output scale (0 until fixed by the first ps3d_closure_train or
+ * set here). */
+int ps3d_closure_get_scale(ps3d_closure *cl, double *ct);
+int ps3d_closure_set_scale(ps3d_closure *cl, double ct);
+/* One training sample: the coarse run's vor and vel (3 components each)
+ * and the target tendency correction (3 components), all physical. */
+int ps3d_closure_add_sample(ps3d_closure *cl, const double *vor, const double *vel, const double *target);
+int ps3d_closure_num_samples(ps3d_closure *cl, int *n);
+/* iters Adam steps (beta 0.9 / 0.999, eps 1e-8), one stored sample each,
+ * visiting the samples in a fresh seeded order every pass; the learning rate
+ * decays from lr0 to lr1 on a cosine.  Fixes ct on the first call when it
+ * is still 0.  loss[iters] (optional) receives each step's normalised mean
+ * squared error before the update. */
+int ps3d_closure_train(ps3d_closure *cl, int iters, double lr0, double lr1, unsigned long long seed,
+                       double *loss);
+/* Forward pass on host fields: the physical tendency correction (3
+ * components) that an attached closure would add for this state. */
+int ps3d_closure_predict(ps3d_closure *cl, const double *vor, const double *vel, double *corr);
+/* Test hook: forward, loss and backward on stored sample `sample` without
+ * an update.  out (optional): the normalised prediction, 3 x npts FP32;
+ * grad (optional): the PS3D_CLOSURE_NPARAM parameter gradients; loss
+ * (optional): the normalised mean squared error. */
+int ps3d_closure_gradients(ps3d_closure *cl, int sample, float *out, float *grad, double *loss);
+/* Attach a closure to a context of the same grid and device (NULL
+ * detaches: plain hyperdiffusion).  flags, an OR of:
+ *   PS3D_CLOSURE_EVERY_STAGE  evaluate the correction at every right-hand
+ *                             side (default: at the first right-hand side of
+ *                             each advance, and at every ps3d_gpu_source
+ *                             call, then held over the stepper's stages);
+ *   PS3D_CLOSURE_CLIP         zero the correction where it would raise the
+ *                             local enstrophy (omega . correction > 0);
+ *   PS3D_CLOSURE_WALLS        zero its horizontal components on the walls
+ *                             (free slip: xi = eta = 0 there).
+ * A closure serves one context at a time. */
+#define PS3D_CLOSURE_EVERY_STAGE 1
+#define PS3D_CLOSURE_CLIP 2
+#define PS3D_CLOSURE_WALLS 4
+int ps3d_gpu_set_closure(ps3d_gpu_ctx *ctx, ps3d_closure *cl, int flags);
+
 #ifdef __cplusplus
 }
 #endif

@@ -31,6 +31,10 @@ EXPORTS = [
     "ps3d_gpu_ke_spectrum", "ps3d_gpu_host_alloc", "ps3d_gpu_host_free",
     "ps3d_gpu_setup_fields_buoyancy", "ps3d_gpu_buoyancy_params", "ps3d_gpu_set_diffusion_vb",
     "ps3d_gpu_buoyancy_diagnostics",
+    "ps3d_closure_create", "ps3d_closure_destroy", "ps3d_closure_last_error",
+    "ps3d_closure_get_params", "ps3d_closure_set_params", "ps3d_closure_get_scale",
+    "ps3d_closure_set_scale", "ps3d_closure_add_sample", "ps3d_closure_num_samples",
+    "ps3d_closure_train", "ps3d_closure_predict", "ps3d_closure_gradients", "ps3d_gpu_set_closure",
 ]
 
 
@@ -133,5 +137,21 @@ def lib(build_if_missing=True):
     L.ps3d_gpu_probe_result.argtypes = [_vp, _dp, ctypes.POINTER(ctypes.c_longlong), _dp]
     L.ps3d_gpu_energy_series_noalloc.argtypes = [_vp, _vp, ctypes.c_int, ctypes.c_int, ctypes.c_int,
                                                  ctypes.c_longlong, ctypes.c_longlong, _vp, _vp]
+    _fp = ctypes.POINTER(ctypes.c_float)
+    L.ps3d_closure_create.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                      ctypes.c_ulonglong, ctypes.POINTER(_vp)]
+    L.ps3d_closure_destroy.argtypes = [_vp]
+    L.ps3d_closure_last_error.argtypes = [_vp]
+    L.ps3d_closure_last_error.restype = ctypes.c_char_p
+    L.ps3d_closure_get_params.argtypes = [_vp, _fp]
+    L.ps3d_closure_set_params.argtypes = [_vp, _fp]
+    L.ps3d_closure_get_scale.argtypes = [_vp, _dp]
+    L.ps3d_closure_set_scale.argtypes = [_vp, ctypes.c_double]
+    L.ps3d_closure_add_sample.argtypes = [_vp, _dp, _dp, _dp]
+    L.ps3d_closure_num_samples.argtypes = [_vp, ctypes.POINTER(ctypes.c_int)]
+    L.ps3d_closure_train.argtypes = [_vp, ctypes.c_int, ctypes.c_double, ctypes.c_double, ctypes.c_ulonglong, _dp]
+    L.ps3d_closure_predict.argtypes = [_vp, _dp, _dp, _dp]
+    L.ps3d_closure_gradients.argtypes = [_vp, ctypes.c_int, _fp, _fp, _dp]
+    L.ps3d_gpu_set_closure.argtypes = [_vp, _vp, ctypes.c_int]
     _LIB = L
     return L

@@ -15,7 +15,8 @@ CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(BUILD, "libps3d_gpu.so")
 INCLUDE = os.path.join(os.path.dirname(HERE), "include")
-SOURCES = ["transforms.cu", "lines32.cu", "columns32.cu", "colz.cu", "ops.cu", "buoyancy.cu", "ps3d_gpu.cu"]
+SOURCES = ["transforms.cu", "lines32.cu", "columns32.cu", "colz.cu", "ops.cu", "buoyancy.cu", "closure.cu",
+           "ps3d_gpu.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

@@ -1,0 +1,1136 @@
+// Learned sub-grid closure: a four-layer 3x3x3 convolution network on the
+// physical grid of a run, trained and evaluated on the device.
+//
+// No counterpart in the reference (its only sub-grid model is the horizontal
+// hyperdiffusion of inversion_utils.f90:124-218, which stays in force).
+//
+// Layout.  A grid point p = iz + Z*(iy + ny*ix), Z = nz+1 (the reference's
+// column-major order without padding).  Activations are channels-last BF16,
+// act[p*C + c], with C padded to 16 or 32 channels: the network input has 6
+// channels (3 vorticity + 3 velocity components over their rms) padded to 16,
+// the hidden layers 32, the output 3 padded to 8 (FP32), its gradient 16.
+//
+// Convolution = implicit GEMM on the tensor cores (mma.sync m16n8k16, BF16
+// in, FP32 accumulate): rows are 16 grid points, the reduction runs over 27
+// taps x the input channels, the columns are the output channels.  The
+// reduction index inside each 16-wide step is permuted so that a lane's A
+// fragment for a row is ONE contiguous 8- or 16-byte load of the input row
+// (lane t of a quad holds channels [C/4*t, C/4*(t+1))); the weight image in
+// shared memory is stored in the same permuted order, already in B-fragment
+// register order (one 8-byte shared load per fragment).  The output columns
+// are permuted the same way so that each lane stores a contiguous run of
+// C/4 channels per row.
+// Backward data = the same kernel with the mirrored, transposed weight image
+// (periodic x, y and zero padding in z make the adjoint another convolution
+// of the same shape), the GELU derivative fused in its epilogue.
+// Weight gradients: per tap, dW = X_tap^T dZ over the points, staged through
+// shared memory and read with ldmatrix.trans; per-chunk partial sums are
+// reduced by a second kernel (deterministic).  Tap 27 is the bias (a column
+// of ones).
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstdint>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/ps3d_gpu.h"
+#include "kernels.h"
+
+namespace {
+
+using bf16 = __nv_bfloat16;
+
+constexpr int NL = 4;
+constexpr int NTAP = 27;
+constexpr int CREAL_IN[NL] = {6, 32, 32, 32};
+constexpr int CREAL_OUT[NL] = {32, 32, 32, 3};
+constexpr int CPAD_IN[NL] = {16, 32, 32, 32};
+constexpr int CPAD_OUT[NL] = {32, 32, 32, 8};
+constexpr int CPAD_DZ4 = 16;  // output-layer gradient channels (a 16-wide k step)
+
+constexpr int woff(int l)
+{
+    int o = 0;
+    for (int i = 0; i < l; ++i) o += NTAP * CREAL_IN[i] * CREAL_OUT[i] + CREAL_OUT[i];
+    return o;
+}
+constexpr int NPARAM = woff(NL);
+static_assert(NPARAM == PS3D_CLOSURE_NPARAM, "parameter count");
+
+constexpr int CONV_THREADS = 128;  // 4 warps
+constexpr int CONV_ROWS = 128;     // grid points per block tile (32 per warp)
+constexpr int WG_KW = 32;          // 16-point k steps per warp in the weight gradient
+constexpr int WG_CHUNK = 4 * WG_KW * 16;
+constexpr int RED_THREADS = 256;
+constexpr int RED_BLOCKS = 256;
+
+enum { EPI_GELU = 0, EPI_OUT = 1, EPI_BWD = 2 };
+
+// ------------------------------------------------------------ device helpers
+__device__ __forceinline__ float gelu_f(float x) { return 0.5f * x * (1.0f + erff(x * 0.70710678118654752f)); }
+__device__ __forceinline__ float dgelu_f(float x)
+{
+    // d/dx [x Phi(x)] = Phi(x) + x phi(x)
+    return 0.5f * (1.0f + erff(x * 0.70710678118654752f)) + x * 0.39894228040143268f * expf(-0.5f * x * x);
+}
+__device__ __forceinline__ uint32_t pack2(float a, float b)
+{
+    __nv_bfloat162 h = __floats2bfloat162_rn(a, b);
+    return *reinterpret_cast<uint32_t *>(&h);
+}
+__device__ __forceinline__ float2 unpack2(uint32_t u)
+{
+    __nv_bfloat162 h = *reinterpret_cast<__nv_bfloat162 *>(&u);
+    return __bfloat1622float2(h);
+}
+__device__ __forceinline__ void mma16816(float *d, uint32_t a0, uint32_t a1, uint32_t a2, uint32_t a3, uint32_t b0,
+                                         uint32_t b1)
+{
+    asm volatile(
+        "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
+        "{%0,%1,%2,%3};\n"
+        : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
+        : "r"(a0), "r"(a1), "r"(a2), "r"(a3), "r"(b0), "r"(b1));
+}
+__device__ __forceinline__ void ldsm_x4_trans(uint32_t &r0, uint32_t &r1, uint32_t &r2, uint32_t &r3,
+                                              const void *smem_row)
+{
+    const uint32_t a = (uint32_t)__cvta_generic_to_shared(smem_row);
+    asm volatile("ldmatrix.sync.aligned.m8n8.x4.trans.shared.b16 {%0,%1,%2,%3}, [%4];\n"
+                 : "=r"(r0), "=r"(r1), "=r"(r2), "=r"(r3)
+                 : "r"(a));
+}
+
+// A-operand row slice of one lane: C/4 channels (CIN 32: 16 bytes, CIN 16: 8)
+template <int CIN> struct RowT;
+template <> struct RowT<32> {
+    using type = uint4;
+    __device__ static uint32_t reg(const uint4 &v, int i) { return i == 0 ? v.x : i == 1 ? v.y : i == 2 ? v.z : v.w; }
+    __device__ static uint4 zero() { return make_uint4(0u, 0u, 0u, 0u); }
+};
+template <> struct RowT<16> {
+    using type = uint2;
+    __device__ static uint32_t reg(const uint2 &v, int i) { return i == 0 ? v.x : v.y; }
+    __device__ static uint2 zero() { return make_uint2(0u, 0u); }
+};
+
+struct ConvArgs {
+    const bf16 *in;      // [npts][CIN]
+    const uint2 *wimg;   // fragment-ordered weights, NTAP*(CIN/16)*(COUT/8)*32 entries
+    const float *bias;   // [COUT] (EPI_GELU, EPI_OUT)
+    bf16 *z;             // EPI_GELU: pre-activation [npts][COUT]
+    bf16 *act;           // EPI_GELU: GELU(z); EPI_BWD: gradient of the layer below
+    float *outf;         // EPI_OUT: [npts][COUT]
+    const bf16 *zprev;   // EPI_BWD: pre-activation of the layer below [npts][COUT]
+    int nx, ny, Z;
+    long long npts;
+};
+
+// One 3x3x3 convolution over all grid points: a persistent grid of 4-warp
+// blocks walks tiles of 128 points, each warp 2 row tiles of 16 points x all
+// COUT output channels.
+template <int CIN, int COUT, int EPI>
+__global__ void __launch_bounds__(CONV_THREADS) k_conv(ConvArgs a)
+{
+    constexpr int S = CIN / 16, NT = COUT / 8, MT = 2;
+    constexpr int WIMG = NTAP * S * NT * 32;
+    using R = RowT<CIN>;
+    using LT = typename R::type;
+    extern __shared__ uint2 sw[];
+    for (int i = threadIdx.x; i < WIMG; i += CONV_THREADS) sw[i] = a.wimg[i];
+    __syncthreads();
+
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int g = lane >> 2, t = lane & 3;
+    const int nym = a.ny - 1, nxm = a.nx - 1, Z = a.Z;
+    const long long ntiles = (a.npts + CONV_ROWS - 1) / CONV_ROWS;
+    const LT *in = reinterpret_cast<const LT *>(a.in);
+
+    for (long long tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+        // the lane's four rows: r = 2*mt + half, row = base + 16 mt + 8 half + g
+        int iz[4], iy[4], ix[4];
+        bool ok[4];
+        long long prow[4];
+#pragma unroll
+        for (int r = 0; r < 4; ++r) {
+            const long long p = tile * CONV_ROWS + warp * 32 + (r >> 1) * 16 + (r & 1) * 8 + g;
+            ok[r] = p < a.npts;
+            prow[r] = p;
+            const long long pp = ok[r] ? p : 0;
+            const long long col = pp / Z;
+            iz[r] = (int)(pp - col * Z);
+            iy[r] = (int)(col & nym);
+            ix[r] = (int)(col / a.ny);
+        }
+        float acc[MT][NT][4];
+#pragma unroll
+        for (int m = 0; m < MT; ++m)
+#pragma unroll
+            for (int n = 0; n < NT; ++n)
+#pragma unroll
+                for (int q = 0; q < 4; ++q) acc[m][n][q] = 0.f;
+
+#pragma unroll
+        for (int dx = -1; dx <= 1; ++dx) {
+#pragma unroll
+            for (int dy = -1; dy <= 1; ++dy) {
+                long long cb[4];
+#pragma unroll
+                for (int r = 0; r < 4; ++r)
+                    cb[r] = (long long)Z * ((long long)((iy[r] + dy) & nym) + (long long)a.ny * ((ix[r] + dx) & nxm));
+#pragma unroll
+                for (int dz = -1; dz <= 1; ++dz) {
+                    const int tap = (dx + 1) * 9 + (dy + 1) * 3 + (dz + 1);
+                    LT v[4];
+#pragma unroll
+                    for (int r = 0; r < 4; ++r) {
+                        const int z2 = iz[r] + dz;
+                        v[r] = (ok[r] && z2 >= 0 && z2 < Z) ? __ldg(in + (cb[r] + z2) * 4 + t) : R::zero();
+                    }
+#pragma unroll
+                    for (int s = 0; s < S; ++s) {
+#pragma unroll
+                        for (int n = 0; n < NT; ++n) {
+                            const uint2 b = sw[((tap * S + s) * NT + n) * 32 + lane];
+#pragma unroll
+                            for (int m = 0; m < MT; ++m)
+                                mma16816(acc[m][n], R::reg(v[2 * m], 2 * s), R::reg(v[2 * m + 1], 2 * s),
+                                         R::reg(v[2 * m], 2 * s + 1), R::reg(v[2 * m + 1], 2 * s + 1), b.x, b.y);
+                        }
+                    }
+                }
+            }
+        }
+
+        // epilogue: the lane owns channels [COUT/4*t, COUT/4*(t+1)) of its rows
+        constexpr int CL = COUT / 4;
+#pragma unroll
+        for (int r = 0; r < 4; ++r) {
+            if (!ok[r]) continue;
+            const int m = r >> 1, h = r & 1;
+            float v[CL];
+#pragma unroll
+            for (int n = 0; n < NT; ++n) {
+                v[2 * n] = acc[m][n][2 * h];
+                v[2 * n + 1] = acc[m][n][2 * h + 1];
+            }
+            const long long p = prow[r];
+            const int c0 = CL * t;
+            if (EPI == EPI_GELU) {
+                uint32_t zz[CL / 2], aa[CL / 2];
+#pragma unroll
+                for (int j = 0; j < CL / 2; ++j) {
+                    const float z0 = v[2 * j] + a.bias[c0 + 2 * j], z1 = v[2 * j + 1] + a.bias[c0 + 2 * j + 1];
+                    // the activation is formed from the rounded pre-activation,
+                    // so that the backward pass differentiates what it reads
+                    const float2 zr = unpack2(pack2(z0, z1));
+                    zz[j] = pack2(z0, z1);
+                    aa[j] = pack2(gelu_f(zr.x), gelu_f(zr.y));
+                }
+                if (CL == 8) {
+                    *reinterpret_cast<uint4 *>(a.z + p * COUT + c0) = make_uint4(zz[0], zz[1], zz[2], zz[3]);
+                    *reinterpret_cast<uint4 *>(a.act + p * COUT + c0) = make_uint4(aa[0], aa[1], aa[2], aa[3]);
+                } else {
+#pragma unroll
+                    for (int j = 0; j < CL / 2; ++j) {
+                        reinterpret_cast<uint32_t *>(a.z + p * COUT + c0)[j] = zz[j];
+                        reinterpret_cast<uint32_t *>(a.act + p * COUT + c0)[j] = aa[j];
+                    }
+                }
+            } else if (EPI == EPI_OUT) {
+#pragma unroll
+                for (int j = 0; j < CL; ++j) a.outf[p * COUT + c0 + j] = v[j] + a.bias[c0 + j];
+            } else {
+                uint32_t gg[CL / 2];
+                const uint32_t *zp = reinterpret_cast<const uint32_t *>(a.zprev + p * COUT + c0);
+#pragma unroll
+                for (int j = 0; j < CL / 2; ++j) {
+                    const float2 zf = unpack2(__ldg(zp + j));
+                    gg[j] = pack2(v[2 * j] * dgelu_f(zf.x), v[2 * j + 1] * dgelu_f(zf.y));
+                }
+#pragma unroll
+                for (int j = 0; j < CL / 2; ++j) reinterpret_cast<uint32_t *>(a.act + p * COUT + c0)[j] = gg[j];
+            }
+        }
+    }
+}
+
+// Weight gradient of one layer, partial sums per chunk of WG_CHUNK points:
+// part[chunk][tap][ci][co] = sum_p X_tap[p][ci] dZ[p][co], tap 27 = bias.
+template <int CIN, int COUT>
+__global__ void __launch_bounds__(128) k_wgrad(const bf16 *__restrict__ act, const bf16 *__restrict__ dz,
+                                               float *__restrict__ part, int nx, int ny, int Z, long long npts)
+{
+    constexpr int XS = CIN * 2 + 16;  // padded row bytes: conflict-free ldmatrix
+    constexpr int GS = COUT * 2 + 16;
+    constexpr int MT = CIN / 16, NT = COUT / 8;
+    __shared__ __align__(16) unsigned char sx[4][16 * XS];
+    __shared__ __align__(16) unsigned char sg[4][16 * GS];
+    __shared__ float red[4][CIN * COUT];
+    const int tap = blockIdx.y;
+    const long long chunk = blockIdx.x;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int g = lane >> 2, t = lane & 3;
+    const int dx = tap / 9 - 1, dy = (tap / 3) % 3 - 1, dzz = tap % 3 - 1;
+    const int nym = ny - 1, nxm = nx - 1;
+    float acc[MT][NT][4];
+#pragma unroll
+    for (int m = 0; m < MT; ++m)
+#pragma unroll
+        for (int n = 0; n < NT; ++n)
+#pragma unroll
+            for (int q = 0; q < 4; ++q) acc[m][n][q] = 0.f;
+
+    const long long p0 = (chunk * 4 + warp) * (long long)(WG_KW * 16);
+    unsigned char *xs = sx[warp];
+    unsigned char *gs = sg[warp];
+    for (int k = 0; k < WG_KW; ++k) {
+        const long long pb = p0 + k * 16;
+        if (pb >= npts) break;  // warp-uniform
+        for (int e = lane; e < 16 * (CIN / 8); e += 32) {
+            const int row = e / (CIN / 8), q = e % (CIN / 8);
+            const long long p = pb + row;
+            uint4 v = make_uint4(0u, 0u, 0u, 0u);
+            if (p < npts) {
+                if (tap == NTAP) {
+                    if (q == 0) v.x = 0x3F80u;  // BF16 1.0 in channel 0
+                } else {
+                    const long long col = p / Z;
+                    const int iz = (int)(p - col * Z) + dzz;
+                    if (iz >= 0 && iz < Z) {
+                        const int iy = (int)(col & nym), ix = (int)(col / ny);
+                        const long long pn =
+                            iz + (long long)Z * ((long long)((iy + dy) & nym) + (long long)ny * ((ix + dx) & nxm));
+                        v = __ldg(reinterpret_cast<const uint4 *>(act + pn * CIN) + q);
+                    }
+                }
+            }
+            *reinterpret_cast<uint4 *>(xs + row * XS + q * 16) = v;
+        }
+        for (int e = lane; e < 16 * (COUT / 8); e += 32) {
+            const int row = e / (COUT / 8), q = e % (COUT / 8);
+            const long long p = pb + row;
+            uint4 v = make_uint4(0u, 0u, 0u, 0u);
+            if (p < npts) v = __ldg(reinterpret_cast<const uint4 *>(dz + p * COUT) + q);
+            *reinterpret_cast<uint4 *>(gs + row * GS + q * 16) = v;
+        }
+        __syncwarp();
+        const int mi = lane >> 3, mr = lane & 7;
+        uint32_t A[MT][4];
+#pragma unroll
+        for (int m = 0; m < MT; ++m)
+            ldsm_x4_trans(A[m][0], A[m][1], A[m][2], A[m][3],
+                          xs + (mr + 8 * (mi >> 1)) * XS + (m * 16 + 8 * (mi & 1)) * 2);
+        uint32_t B[NT][2];
+#pragma unroll
+        for (int n2 = 0; n2 < NT / 2; ++n2)
+            ldsm_x4_trans(B[2 * n2][0], B[2 * n2][1], B[2 * n2 + 1][0], B[2 * n2 + 1][1],
+                          gs + (mr + 8 * (mi & 1)) * GS + (n2 * 16 + 8 * (mi >> 1)) * 2);
+#pragma unroll
+        for (int m = 0; m < MT; ++m)
+#pragma unroll
+            for (int n = 0; n < NT; ++n) mma16816(acc[m][n], A[m][0], A[m][1], A[m][2], A[m][3], B[n][0], B[n][1]);
+        __syncwarp();
+    }
+#pragma unroll
+    for (int m = 0; m < MT; ++m)
+#pragma unroll
+        for (int n = 0; n < NT; ++n)
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                const int ci = m * 16 + g + 8 * (q >> 1), co = n * 8 + 2 * t + (q & 1);
+                red[warp][ci * COUT + co] = acc[m][n][q];
+            }
+    __syncthreads();
+    float *dst = part + (chunk * (NTAP + 1) + tap) * (long long)(CIN * COUT);
+    for (int e = threadIdx.x; e < CIN * COUT; e += 128) dst[e] = red[0][e] + red[1][e] + red[2][e] + red[3][e];
+}
+
+// grad[e] for e < 27*cin*cout + cout (weights then bias of one layer)
+__global__ void k_wgrad_reduce(const float *__restrict__ part, long long nchunk, int CIN, int COUT, int cin, int cout,
+                               float *__restrict__ grad)
+{
+    const int n = NTAP * cin * cout + cout;
+    const int e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= n) return;
+    long long src;
+    if (e < NTAP * cin * cout) {
+        const int tap = e / (cin * cout), rem = e % (cin * cout), ci = rem / cout, co = rem % cout;
+        src = ((long long)tap * CIN + ci) * COUT + co;
+    } else {
+        src = (long long)NTAP * CIN * COUT + (e - NTAP * cin * cout);
+    }
+    const long long stride = (long long)(NTAP + 1) * CIN * COUT;
+    float s = 0.f;
+    for (long long c = 0; c < nchunk; ++c) s += part[c * stride + src];
+    grad[e] = s;
+}
+
+// Fragment-ordered BF16 weight image of one layer (and its padded bias).
+// Image entry (tap, s, n, lane) holds the B fragment registers {b0b1, b2b3}
+// of k step s and n tile n: row k (0..15) of the step is input channel
+// CINP/4*(k%8/2) + 4s + 2(k/8) + k%2, column j (0..7) of the tile is output
+// channel COUTP/4*(j/2) + 2n + j%2.  transpose != 0 builds the backward-data
+// image: input channels of the image = the layer's outputs, outputs = the
+// layer's inputs, taps mirrored.
+__global__ void k_wimage(const float *__restrict__ W, const float *__restrict__ b, int cin, int cout, int CINP,
+                         int COUTP, int transpose, uint2 *__restrict__ img, float *__restrict__ bpad)
+{
+    const int S = CINP / 16, NT = COUTP / 8;
+    const int total = NTAP * S * NT * 32;
+    const int e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (bpad && e < COUTP) bpad[e] = (!transpose && e < cout) ? b[e] : 0.f;
+    if (e >= total) return;
+    const int lane = e & 31;
+    int rest = e >> 5;
+    const int n = rest % NT;
+    rest /= NT;
+    const int s = rest % S;
+    const int tap = rest / S;
+    const int t = lane & 3, gq = lane >> 2;
+    const int co = (COUTP / 4) * (gq >> 1) + 2 * n + (gq & 1);
+    float w[4];
+#pragma unroll
+    for (int r = 0; r < 2; ++r)
+#pragma unroll
+        for (int j = 0; j < 2; ++j) {
+            const int ci = (CINP / 4) * t + 4 * s + 2 * r + j;
+            float v = 0.f;
+            if (!transpose) {
+                if (ci < cin && co < cout) v = W[((long long)tap * cin + ci) * cout + co];
+            } else {
+                if (ci < cout && co < cin) v = W[((long long)(NTAP - 1 - tap) * cin + co) * cout + ci];
+            }
+            w[2 * r + j] = v;
+        }
+    img[e] = make_uint2(pack2(w[0], w[1]), pack2(w[2], w[3]));
+}
+
+// network input from 3 vorticity + 3 velocity fields of type T (pitch
+// `pitch` per column, component stride cstride): channels 0-2 vor*scal[0],
+// 3-5 vel*scal[1], 6-15 zero
+template <typename T>
+__global__ void k_pack(const T *__restrict__ vor, const T *__restrict__ vel, long long cstride, int pitch, int Z,
+                       long long npts, const float *__restrict__ scal, bf16 *__restrict__ a0)
+{
+    const float sw = scal[0], su = scal[1];
+    for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < npts;
+         p += (long long)gridDim.x * blockDim.x) {
+        const long long col = p / Z;
+        const long long src = (p - col * Z) + (long long)pitch * col;
+        const float v0 = (float)vor[src] * sw, v1 = (float)vor[src + cstride] * sw, v2 = (float)vor[src + 2 * cstride] * sw;
+        const float u0 = (float)vel[src] * su, u1 = (float)vel[src + cstride] * su, u2 = (float)vel[src + 2 * cstride] * su;
+        uint4 *dst = reinterpret_cast<uint4 *>(a0 + p * 16);
+        dst[0] = make_uint4(pack2(v0, v1), pack2(v2, u0), pack2(u1, u2), 0u);
+        dst[1] = make_uint4(0u, 0u, 0u, 0u);
+    }
+}
+
+// correction fields out[c] (type T, pitch, component stride) = outf[p][c] * scal[2].
+// flags (PS3D_CLOSURE_*): CLIP zeroes the correction at points where it
+// would raise the local enstrophy (vor . corr > 0, backscatter); WALLS
+// zeroes its horizontal components on the walls (free slip: xi = eta = 0)
+template <typename T>
+__global__ void k_unpack(const float *__restrict__ outf, const float *__restrict__ scal, const T *__restrict__ vor,
+                         long long vstride, int Z, long long npts, int pitch, long long ostride, int flags,
+                         T *__restrict__ out)
+{
+    const float s = scal[2];
+    for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < npts;
+         p += (long long)gridDim.x * blockDim.x) {
+        const long long col = p / Z;
+        const int iz = (int)(p - col * Z);
+        const long long dst = iz + (long long)pitch * col;
+        const float *o = outf + p * CPAD_OUT[NL - 1];
+        float c0 = o[0] * s, c1 = o[1] * s, c2 = o[2] * s;
+        if (flags & PS3D_CLOSURE_WALLS) {
+            if (iz == 0 || iz == Z - 1) c0 = c1 = 0.f;
+        }
+        if (flags & PS3D_CLOSURE_CLIP) {
+            const float w = (float)vor[dst] * c0 + (float)vor[dst + vstride] * c1 + (float)vor[dst + 2 * vstride] * c2;
+            if (w > 0.f) c0 = c1 = c2 = 0.f;
+        }
+        out[dst] = (T)c0;
+        out[dst + ostride] = (T)c1;
+        out[dst + 2 * ostride] = (T)c2;
+    }
+}
+
+__device__ __forceinline__ double block_sum(double v, double *sh)
+{
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+    __syncthreads();
+    if (l == 0) sh[w] = v;
+    __syncthreads();
+    double s = 0.0;
+    if (threadIdx.x == 0)
+        for (int i = 0; i < (int)(blockDim.x >> 5); ++i) s += sh[i];
+    return s;  // valid in thread 0
+}
+
+// sums of |vor|^2 and |vel|^2 over the grid points, per block
+template <typename T>
+__global__ void k_sumsq(const T *__restrict__ vor, const T *__restrict__ vel, long long cstride, int pitch, int Z,
+                        long long npts, double *__restrict__ part)
+{
+    __shared__ double sh[32];
+    double sw = 0.0, su = 0.0;
+    for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < npts;
+         p += (long long)gridDim.x * blockDim.x) {
+        const long long col = p / Z;
+        const long long src = (p - col * Z) + (long long)pitch * col;
+        for (int c = 0; c < 3; ++c) {
+            const double w = (double)vor[src + c * cstride], u = (double)vel[src + c * cstride];
+            sw += w * w;
+            su += u * u;
+        }
+    }
+    const double a = block_sum(sw, sh);
+    const double b = block_sum(su, sh);
+    if (threadIdx.x == 0) {
+        part[2 * blockIdx.x] = a;
+        part[2 * blockIdx.x + 1] = b;
+    }
+}
+
+// scal[0] = 1/rms(vor), scal[1] = 1/rms(vel), scal[2] = ct * <|vor|^2>
+// (ct read from device memory, so that captured launches follow a change)
+__global__ void k_scal_finish(const double *__restrict__ part, int nblocks, long long npts, const double *ctp,
+                              float *__restrict__ scal)
+{
+    __shared__ double sh[32];
+    double a = 0.0, b = 0.0;
+    for (int i = threadIdx.x; i < nblocks; i += blockDim.x) {
+        a += part[2 * i];
+        b += part[2 * i + 1];
+    }
+    a = block_sum(a, sh);
+    b = block_sum(b, sh);
+    if (threadIdx.x == 0) {
+        const double w2 = a / (double)npts, u2 = b / (double)npts;
+        scal[0] = w2 > 0.0 ? (float)(1.0 / sqrt(w2)) : 0.f;
+        scal[1] = u2 > 0.0 ? (float)(1.0 / sqrt(u2)) : 0.f;
+        scal[2] = (float)(*ctp * w2);
+    }
+}
+
+// mean squared error against the normalised target and its gradient dz4
+// (channels 0-2, the rest zero); per-block partial sums of the squares
+__global__ void k_loss(const float *__restrict__ outf, const float *__restrict__ tgt, const float *__restrict__ sscal,
+                       long long npts, bf16 *__restrict__ dz4, double *__restrict__ part)
+{
+    __shared__ double sh[32];
+    const float ts = sscal[2];
+    const float gs = 2.0f / (3.0f * (float)npts);
+    double acc = 0.0;
+    for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < npts;
+         p += (long long)gridDim.x * blockDim.x) {
+        const float *o = outf + p * CPAD_OUT[NL - 1];
+        const float d0 = o[0] - tgt[p] * ts, d1 = o[1] - tgt[npts + p] * ts, d2 = o[2] - tgt[2 * npts + p] * ts;
+        acc += (double)d0 * d0 + (double)d1 * d1 + (double)d2 * d2;
+        uint4 *dst = reinterpret_cast<uint4 *>(dz4 + p * CPAD_DZ4);
+        dst[0] = make_uint4(pack2(gs * d0, gs * d1), pack2(gs * d2, 0.f), 0u, 0u);
+        dst[1] = make_uint4(0u, 0u, 0u, 0u);
+    }
+    const double s = block_sum(acc, sh);
+    if (threadIdx.x == 0) part[blockIdx.x] = s;
+}
+
+__global__ void k_loss_finish(const double *__restrict__ part, int nblocks, double scale, double *__restrict__ out)
+{
+    __shared__ double sh[32];
+    double a = 0.0;
+    for (int i = threadIdx.x; i < nblocks; i += blockDim.x) a += part[i];
+    a = block_sum(a, sh);
+    if (threadIdx.x == 0) *out = a * scale;
+}
+
+__global__ void k_adam(float *__restrict__ w, const float *__restrict__ g, float *__restrict__ m,
+                       float *__restrict__ v, int n, float lr, float b1, float b2, float c1, float c2, float eps)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float gi = g[i];
+    const float mi = b1 * m[i] + (1.f - b1) * gi;
+    const float vi = b2 * v[i] + (1.f - b2) * gi * gi;
+    m[i] = mi;
+    v[i] = vi;
+    w[i] -= lr * (mi * c1) / (sqrtf(vi * c2) + eps);
+}
+
+// host-side SplitMix64 (parameter initialisation, sample order)
+struct SplitMix {
+    unsigned long long s;
+    unsigned long long next()
+    {
+        unsigned long long z = (s += 0x9E3779B97F4A7C15ull);
+        z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+        z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+        return z ^ (z >> 31);
+    }
+    double uniform() { return (double)(next() >> 11) * (1.0 / 9007199254740992.0); }
+};
+
+}  // namespace
+
+// ======================================================================
+struct ps3d_closure {
+    int nx = 0, ny = 0, nz = 0, Z = 0, device = 0, nsm = 0;
+    long long npts = 0, nchunk = 0;
+    cudaStream_t st = nullptr;
+    std::string err;
+    std::vector<void *> allocs;
+    const void *owner = nullptr;  // attached context
+    // parameters, gradients, Adam moments (FP32, NPARAM)
+    float *w = nullptr, *g = nullptr, *m = nullptr, *v = nullptr;
+    uint2 *imgf[NL] = {}, *imgb[NL] = {};  // forward images; backward-data images (layers 1..3)
+    float *bpad[NL] = {};
+    // activations
+    bf16 *a0 = nullptr, *z[3] = {}, *act[3] = {}, *dz4 = nullptr, *dzA = nullptr, *dzB = nullptr;
+    float *outf = nullptr, *wpart = nullptr, *scal = nullptr;
+    double *rpart = nullptr, *lpart = nullptr, *lossd = nullptr;
+    double *ctd = nullptr;   // ct in device memory; lpart[RED_BLOCKS]: one loss value
+    int occ[5] = {1, 1, 1, 1, 1};  // resident conv blocks per SM per instantiation
+    int loss_cap = 0;
+    double *host_out = nullptr;   // predict staging (device)
+    double *host_in = nullptr;    // 6 fields FP64 staging (device)
+    // training samples: per sample 9 fields FP32 [vor 3, vel 3, target 3][npts]
+    int max_samples = 0, nsamples = 0;
+    float *data = nullptr;
+    float *sscal = nullptr;  // per sample {1/rms(vor), 1/rms(vel), 1/(ct <|vor|^2>), 0}
+    std::vector<double> w2, u2, t2;
+    double ct = 0.0;
+    long long adam_t = 0;
+    SplitMix rng{0};
+};
+
+namespace {
+
+int cfail(ps3d_closure *cl, int code, const std::string &msg)
+{
+    if (cl) cl->err = msg;
+    return code;
+}
+int ccheck(ps3d_closure *cl, const char *where)
+{
+    const cudaError_t e = cudaGetLastError();
+    if (e == cudaSuccess) return PS3D_OK;
+    return cfail(cl, PS3D_ERR_CUDA, std::string(where) + ": " + cudaGetErrorString(e));
+}
+template <typename P> bool calloc_dev(ps3d_closure *cl, P **p, size_t bytes)
+{
+    void *q = nullptr;
+    if (cudaMalloc(&q, bytes) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    cudaMemset(q, 0, bytes);
+    cl->allocs.push_back(q);
+    *p = reinterpret_cast<P *>(q);
+    return true;
+}
+
+template <int CIN, int COUT, int EPI> size_t conv_smem() { return (size_t)NTAP * (CIN / 16) * (COUT / 8) * 32 * 8; }
+
+template <int CIN, int COUT, int EPI> constexpr int conv_slot()
+{
+    return EPI == EPI_OUT ? 2 : EPI == EPI_BWD ? (CIN == 16 ? 3 : 4) : (CIN == 16 ? 0 : 1);
+}
+
+template <int CIN, int COUT, int EPI> void conv_attr(ps3d_closure *cl)
+{
+    cudaFuncSetAttribute(k_conv<CIN, COUT, EPI>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)conv_smem<CIN, COUT, EPI>());
+    int nb = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_conv<CIN, COUT, EPI>, CONV_THREADS,
+                                                      conv_smem<CIN, COUT, EPI>()) != cudaSuccess || nb < 1) {
+        cudaGetLastError();
+        nb = 1;
+    }
+    cl->occ[conv_slot<CIN, COUT, EPI>()] = nb;
+}
+
+// persistent grid: at most one wave of resident blocks, the tiles spread
+// evenly over it
+template <int CIN, int COUT, int EPI> void conv(ps3d_closure *cl, cudaStream_t st, const ConvArgs &a)
+{
+    const long long ntiles = (cl->npts + CONV_ROWS - 1) / CONV_ROWS;
+    const long long maxb = (long long)cl->nsm * cl->occ[conv_slot<CIN, COUT, EPI>()];
+    const long long per = (ntiles + maxb - 1) / maxb;
+    const unsigned grid = (unsigned)((ntiles + per - 1) / per);
+    k_conv<CIN, COUT, EPI><<<grid, CONV_THREADS, conv_smem<CIN, COUT, EPI>(), st>>>(a);
+}
+
+ConvArgs base_args(ps3d_closure *cl)
+{
+    ConvArgs a{};
+    a.nx = cl->nx;
+    a.ny = cl->ny;
+    a.Z = cl->Z;
+    a.npts = cl->npts;
+    return a;
+}
+
+// four layers: a0 -> z1/a1 -> z2/a2 -> z3/a3 -> outf
+void forward(ps3d_closure *cl, cudaStream_t st)
+{
+    ConvArgs a = base_args(cl);
+    a.in = cl->a0;
+    a.wimg = cl->imgf[0];
+    a.bias = cl->bpad[0];
+    a.z = cl->z[0];
+    a.act = cl->act[0];
+    conv<16, 32, EPI_GELU>(cl, st, a);
+    for (int l = 1; l < 3; ++l) {
+        a.in = cl->act[l - 1];
+        a.wimg = cl->imgf[l];
+        a.bias = cl->bpad[l];
+        a.z = cl->z[l];
+        a.act = cl->act[l];
+        conv<32, 32, EPI_GELU>(cl, st, a);
+    }
+    a.in = cl->act[2];
+    a.wimg = cl->imgf[3];
+    a.bias = cl->bpad[3];
+    a.z = nullptr;
+    a.act = nullptr;
+    a.outf = cl->outf;
+    conv<32, 8, EPI_OUT>(cl, st, a);
+}
+
+template <int CIN, int COUT> void wgrad(ps3d_closure *cl, cudaStream_t st, const bf16 *act, const bf16 *dz, int l)
+{
+    dim3 grid((unsigned)cl->nchunk, NTAP + 1);
+    k_wgrad<CIN, COUT><<<grid, 128, 0, st>>>(act, dz, cl->wpart, cl->nx, cl->ny, cl->Z, cl->npts);
+    const int n = NTAP * CREAL_IN[l] * CREAL_OUT[l] + CREAL_OUT[l];
+    k_wgrad_reduce<<<(n + 255) / 256, 256, 0, st>>>(cl->wpart, cl->nchunk, CIN, COUT, CREAL_IN[l], CREAL_OUT[l],
+                                                    cl->g + woff(l));
+}
+
+// backward pass after forward + k_loss (dz4 holds dL/dout): all parameter
+// gradients into cl->g
+void backward(ps3d_closure *cl, cudaStream_t st)
+{
+    wgrad<32, 16>(cl, st, cl->act[2], cl->dz4, 3);
+    ConvArgs a = base_args(cl);
+    // dz3 = (W4^T * dz4) . gelu'(z3)
+    a.in = cl->dz4;
+    a.wimg = cl->imgb[3];
+    a.zprev = cl->z[2];
+    a.act = cl->dzA;
+    conv<16, 32, EPI_BWD>(cl, st, a);
+    wgrad<32, 32>(cl, st, cl->act[1], cl->dzA, 2);
+    // dz2 = (W3^T * dz3) . gelu'(z2)
+    a.in = cl->dzA;
+    a.wimg = cl->imgb[2];
+    a.zprev = cl->z[1];
+    a.act = cl->dzB;
+    conv<32, 32, EPI_BWD>(cl, st, a);
+    wgrad<32, 32>(cl, st, cl->act[0], cl->dzB, 1);
+    // dz1 = (W2^T * dz2) . gelu'(z1)
+    a.in = cl->dzB;
+    a.wimg = cl->imgb[1];
+    a.zprev = cl->z[0];
+    a.act = cl->dzA;
+    conv<32, 32, EPI_BWD>(cl, st, a);
+    wgrad<16, 32>(cl, st, cl->a0, cl->dzA, 0);
+}
+
+// rebuild the BF16 images from the FP32 master parameters
+void images(ps3d_closure *cl, cudaStream_t st)
+{
+    for (int l = 0; l < NL; ++l) {
+        const float *W = cl->w + woff(l);
+        const float *b = W + NTAP * CREAL_IN[l] * CREAL_OUT[l];
+        const int nf = NTAP * (CPAD_IN[l] / 16) * (CPAD_OUT[l] / 8) * 32;
+        k_wimage<<<(nf + 255) / 256, 256, 0, st>>>(W, b, CREAL_IN[l], CREAL_OUT[l], CPAD_IN[l], CPAD_OUT[l], 0,
+                                                  cl->imgf[l], cl->bpad[l]);
+        if (l > 0) {
+            const int cinp = l == NL - 1 ? CPAD_DZ4 : CPAD_OUT[l];
+            const int nb = NTAP * (cinp / 16) * (CPAD_IN[l] / 8) * 32;
+            k_wimage<<<(nb + 255) / 256, 256, 0, st>>>(W, b, CREAL_IN[l], CREAL_OUT[l], cinp, CPAD_IN[l], 1,
+                                                      cl->imgb[l], nullptr);
+        }
+    }
+}
+
+// pack stored sample s into a0
+void pack_sample(ps3d_closure *cl, cudaStream_t st, int s)
+{
+    const float *base = cl->data + (size_t)s * 9 * cl->npts;
+    k_pack<float><<<RED_BLOCKS * 4, RED_THREADS, 0, st>>>(base, base + 3 * cl->npts, cl->npts, cl->Z, cl->Z,
+                                                         cl->npts, cl->sscal + 4 * s, cl->a0);
+}
+
+void loss_and_grad(ps3d_closure *cl, cudaStream_t st, int s, double *loss_dst)
+{
+    const float *tgt = cl->data + (size_t)s * 9 * cl->npts + 6 * cl->npts;
+    k_loss<<<RED_BLOCKS, RED_THREADS, 0, st>>>(cl->outf, tgt, cl->sscal + 4 * s, cl->npts, cl->dz4, cl->lpart);
+    k_loss_finish<<<1, RED_THREADS, 0, st>>>(cl->lpart, RED_BLOCKS, 1.0 / (3.0 * (double)cl->npts), loss_dst);
+}
+
+// per-sample scalars from the current ct
+void upload_sample_scalars(ps3d_closure *cl)
+{
+    std::vector<float> h(4 * (size_t)cl->nsamples);
+    for (int s = 0; s < cl->nsamples; ++s) {
+        h[4 * s + 0] = cl->w2[s] > 0 ? (float)(1.0 / std::sqrt(cl->w2[s])) : 0.f;
+        h[4 * s + 1] = cl->u2[s] > 0 ? (float)(1.0 / std::sqrt(cl->u2[s])) : 0.f;
+        h[4 * s + 2] = (cl->ct > 0 && cl->w2[s] > 0) ? (float)(1.0 / (cl->ct * cl->w2[s])) : 0.f;
+        h[4 * s + 3] = 0.f;
+    }
+    if (!h.empty()) cudaMemcpy(cl->sscal, h.data(), h.size() * sizeof(float), cudaMemcpyHostToDevice);
+}
+
+int centre(ps3d_closure *cl)
+{
+    if (!cl) return PS3D_ERR_INVALID_ARG;
+    if (cudaSetDevice(cl->device) != cudaSuccess) return ccheck(cl, "cudaSetDevice");
+    return PS3D_OK;
+}
+
+// mean squares over the points of 3-component host fields
+double mean_sq3(const double *f, long long npts)
+{
+    double s = 0.0;
+    for (long long i = 0; i < 3 * npts; ++i) s += f[i] * f[i];
+    return s / (double)npts;
+}
+
+}  // namespace
+
+// ---------------------------------------------------- internal interface
+namespace ps3d {
+
+int closure_attach(ps3d_closure *cl, const void *owner, int nx, int ny, int nz, int device, std::string *err)
+{
+    if (cl->owner && cl->owner != owner) {
+        *err = "closure already attached to another context";
+        return PS3D_ERR_INVALID_ARG;
+    }
+    if (cl->nx != nx || cl->ny != ny || cl->nz != nz || cl->device != device) {
+        *err = "closure grid or device differs from the context's";
+        return PS3D_ERR_INVALID_ARG;
+    }
+    if (!(cl->ct > 0.0)) {
+        *err = "closure output scale not set (train or set_scale first)";
+        return PS3D_ERR_NOT_READY;
+    }
+    cl->owner = owner;
+    return PS3D_OK;
+}
+
+void closure_detach(ps3d_closure *cl, const void *owner)
+{
+    if (cl && cl->owner == owner) cl->owner = nullptr;
+}
+
+template <typename T>
+int closure_apply(ps3d_closure *cl, cudaStream_t st, const T *vor, const T *vel, long long cstride, int pitch, T *out,
+                  long long ostride, int flags)
+{
+    k_sumsq<T><<<RED_BLOCKS, RED_THREADS, 0, st>>>(vor, vel, cstride, pitch, cl->Z, cl->npts, cl->rpart);
+    k_scal_finish<<<1, RED_THREADS, 0, st>>>(cl->rpart, RED_BLOCKS, cl->npts, cl->ctd, cl->scal);
+    k_pack<T><<<RED_BLOCKS * 4, RED_THREADS, 0, st>>>(vor, vel, cstride, pitch, cl->Z, cl->npts, cl->scal, cl->a0);
+    forward(cl, st);
+    k_unpack<T><<<RED_BLOCKS * 4, RED_THREADS, 0, st>>>(cl->outf, cl->scal, vor, cstride, cl->Z, cl->npts, pitch,
+                                                       ostride, flags, out);
+    return cudaPeekAtLastError() == cudaSuccess ? PS3D_OK : PS3D_ERR_CUDA;
+}
+template int closure_apply<float>(ps3d_closure *, cudaStream_t, const float *, const float *, long long, int, float *,
+                                  long long, int);
+template int closure_apply<double>(ps3d_closure *, cudaStream_t, const double *, const double *, long long, int,
+                                   double *, long long, int);
+
+}  // namespace ps3d
+
+// ======================================================================
+extern "C" {
+
+int ps3d_closure_create(int nx, int ny, int nz, int max_samples, int device, unsigned long long seed,
+                        ps3d_closure **out)
+{
+    if (!out) return PS3D_ERR_INVALID_ARG;
+    *out = nullptr;
+    auto pow2 = [](int v) { return v >= 8 && (v & (v - 1)) == 0; };
+    if (!pow2(nx) || !pow2(ny) || !pow2(nz) || nx > 2048 || ny > 2048 || nz > 2048) return PS3D_ERR_UNSUPPORTED_SIZE;
+    if (max_samples < 0) return PS3D_ERR_INVALID_ARG;
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || device < 0 || device >= ndev) {
+        cudaGetLastError();
+        return PS3D_ERR_NO_DEVICE;
+    }
+    cudaDeviceProp prop;
+    if (cudaGetDeviceProperties(&prop, device) != cudaSuccess || prop.major != 10 || prop.minor != 3) {
+        cudaGetLastError();
+        return PS3D_ERR_NO_DEVICE;
+    }
+    ps3d_closure *cl = new ps3d_closure();
+    cl->nx = nx;
+    cl->ny = ny;
+    cl->nz = nz;
+    cl->Z = nz + 1;
+    cl->npts = (long long)nx * ny * (nz + 1);
+    cl->device = device;
+    cl->nsm = prop.multiProcessorCount;
+    cl->max_samples = max_samples;
+    cl->nchunk = (cl->npts + WG_CHUNK - 1) / WG_CHUNK;
+    cl->rng.s = seed;
+    cudaSetDevice(device);
+    cudaStreamCreateWithFlags(&cl->st, cudaStreamNonBlocking);
+    conv_attr<16, 32, EPI_GELU>(cl);
+    conv_attr<32, 32, EPI_GELU>(cl);
+    conv_attr<32, 8, EPI_OUT>(cl);
+    conv_attr<16, 32, EPI_BWD>(cl);
+    conv_attr<32, 32, EPI_BWD>(cl);
+    const long long P = cl->npts;
+    bool ok = calloc_dev(cl, &cl->w, NPARAM * 4) && calloc_dev(cl, &cl->g, NPARAM * 4) &&
+              calloc_dev(cl, &cl->m, NPARAM * 4) && calloc_dev(cl, &cl->v, NPARAM * 4);
+    for (int l = 0; l < NL && ok; ++l) {
+        ok = calloc_dev(cl, &cl->imgf[l], (size_t)NTAP * (CPAD_IN[l] / 16) * (CPAD_OUT[l] / 8) * 32 * 8) &&
+             calloc_dev(cl, &cl->bpad[l], 64 * 4);
+        if (ok && l > 0) {
+            const int cinp = l == NL - 1 ? CPAD_DZ4 : CPAD_OUT[l];
+            ok = calloc_dev(cl, &cl->imgb[l], (size_t)NTAP * (cinp / 16) * (CPAD_IN[l] / 8) * 32 * 8);
+        }
+    }
+    ok = ok && calloc_dev(cl, &cl->a0, P * 16 * 2);
+    for (int l = 0; l < 3 && ok; ++l) ok = calloc_dev(cl, &cl->z[l], P * 32 * 2) && calloc_dev(cl, &cl->act[l], P * 32 * 2);
+    ok = ok && calloc_dev(cl, &cl->dz4, P * CPAD_DZ4 * 2) && calloc_dev(cl, &cl->dzA, P * 32 * 2) &&
+         calloc_dev(cl, &cl->dzB, P * 32 * 2) && calloc_dev(cl, &cl->outf, P * CPAD_OUT[NL - 1] * 4) &&
+         calloc_dev(cl, &cl->wpart, (size_t)cl->nchunk * (NTAP + 1) * 32 * 32 * 4) &&
+         calloc_dev(cl, &cl->scal, 4 * 4) && calloc_dev(cl, &cl->rpart, 2 * RED_BLOCKS * 8) &&
+         calloc_dev(cl, &cl->lpart, (RED_BLOCKS + 1) * 8) && calloc_dev(cl, &cl->ctd, 8) && calloc_dev(cl, &cl->host_out, (size_t)3 * P * 8) &&
+         calloc_dev(cl, &cl->host_in, (size_t)6 * P * 8) && calloc_dev(cl, &cl->sscal, (size_t)(max_samples + 1) * 16);
+    if (ok && max_samples > 0) ok = calloc_dev(cl, &cl->data, (size_t)max_samples * 9 * P * 4);
+    if (!ok) {
+        cudaGetLastError();
+        ps3d_closure_destroy(cl);
+        return PS3D_ERR_OUT_OF_MEMORY;
+    }
+    // He-uniform weights (bound sqrt(6 / fan_in)), the output layer scaled by
+    // 0.1 so that an untrained closure starts as a small correction; zero bias
+    std::vector<float> h(NPARAM, 0.f);
+    for (int l = 0; l < NL; ++l) {
+        const double bound = std::sqrt(6.0 / (NTAP * CREAL_IN[l])) * (l == NL - 1 ? 0.1 : 1.0);
+        const int nw = NTAP * CREAL_IN[l] * CREAL_OUT[l];
+        for (int i = 0; i < nw; ++i) h[woff(l) + i] = (float)((2.0 * cl->rng.uniform() - 1.0) * bound);
+    }
+    cudaMemcpy(cl->w, h.data(), NPARAM * 4, cudaMemcpyHostToDevice);
+    images(cl, cl->st);
+    cudaStreamSynchronize(cl->st);
+    const int rc = ccheck(cl, "closure_create");
+    if (rc) {
+        ps3d_closure_destroy(cl);
+        return rc;
+    }
+    *out = cl;
+    return PS3D_OK;
+}
+
+int ps3d_closure_destroy(ps3d_closure *cl)
+{
+    if (!cl) return PS3D_OK;
+    if (cl->owner) return cfail(cl, PS3D_ERR_INVALID_ARG, "closure is attached to a context");
+    cudaSetDevice(cl->device);
+    if (cl->st) cudaStreamSynchronize(cl->st);
+    for (void *p : cl->allocs) cudaFree(p);
+    if (cl->st) cudaStreamDestroy(cl->st);
+    delete cl;
+    return PS3D_OK;
+}
+
+const char *ps3d_closure_last_error(const ps3d_closure *cl) { return cl ? cl->err.c_str() : ""; }
+
+int ps3d_closure_get_params(ps3d_closure *cl, float *params)
+{
+    int rc = centre(cl);
+    if (rc) return rc;
+    if (!params) return PS3D_ERR_INVALID_ARG;
+    cudaStreamSynchronize(cl->st);
+    cudaMemcpy(params, cl->w, NPARAM * 4, cudaMemcpyDeviceToHost);
+    return ccheck(cl, "get_params");
+}
+
+int ps3d_closure_set_params(ps3d_closure *cl, const float *params)
+{
+    int rc = centre(cl);
+    if (rc) return rc;
+    if (!params) return PS3D_ERR_INVALID_ARG;
+    cudaStreamSynchronize(cl->st);
+    cudaMemcpy(cl->w, params, NPARAM * 4, cudaMemcpyHostToDevice);
+    images(cl, cl->st);
+    cudaStreamSynchronize(cl->st);
+    return ccheck(cl, "set_params");
+}
+
+int ps3d_closure_get_scale(ps3d_closure *cl, double *ct)
+{
+    if (!cl || !ct) return PS3D_ERR_INVALID_ARG;
+    *ct = cl->ct;
+    return PS3D_OK;
+}
+
+int ps3d_closure_set_scale(ps3d_closure *cl, double ct)
+{
+    if (!cl || !(ct > 0.0) || !std::isfinite(ct)) return PS3D_ERR_INVALID_ARG;
+    int rc = centre(cl);
+    if (rc) return rc;
+    cl->ct = ct;
+    cudaStreamSynchronize(cl->st);
+    cudaMemcpy(cl->ctd, &cl->ct, 8, cudaMemcpyHostToDevice);
+    return ccheck(cl, "set_scale");
+}
+
+int ps3d_closure_add_sample(ps3d_closure *cl, const double *vor, const double *vel, const double *target)
+{
+    int rc = centre(cl);
+    if (rc) return rc;
+    if (!vor || !vel || !target) return PS3D_ERR_INVALID_ARG;
+    if (cl->nsamples >= cl->max_samples) return cfail(cl, PS3D_ERR_INVALID_ARG, "sample store full");
+    const long long P = cl->npts;
+    std::vector<float> h((size_t)9 * P);
+    for (long long i = 0; i < 3 * P; ++i) {
+        h[i] = (float)vor[i];
+        h[3 * P + i] = (float)vel[i];
+        h[6 * P + i] = (float)target[i];
+    }
+    cudaStreamSynchronize(cl->st);
+    cudaMemcpy(cl->data + (size_t)cl->nsamples * 9 * P, h.data(), h.size() * 4, cudaMemcpyHostToDevice);
+    rc = ccheck(cl, "add_sample");
+    if (rc) return rc;
+    cl->w2.push_back(mean_sq3(vor, P));
+    cl->u2.push_back(mean_sq3(vel, P));
+    cl->t2.push_back(mean_sq3(target, P));
+    cl->nsamples += 1;
+    return PS3D_OK;
+}
+
+int ps3d_closure_num_samples(ps3d_closure *cl, int *n)
+{
+    if (!cl || !n) return PS3D_ERR_INVALID_ARG;
+    *n = cl->nsamples;
+    return PS3D_OK;
+}
+
+int ps3d_closure_train(ps3d_closure *cl, int iters, double lr0, double lr1, unsigned long long seed, double *loss)
+{
+    int rc = centre(cl);
+    if (rc) return rc;
+    if (iters < 0 || cl->nsamples == 0) return cfail(cl, PS3D_ERR_NOT_READY, "no training samples");
+    if (!(cl->ct > 0.0)) {
+        // ct = mean over the samples of rms(target) / <|vor|^2>
+        double s = 0.0;
+        int n = 0;
+        for (int i = 0; i < cl->nsamples; ++i)
+            if (cl->w2[i] > 0) {
+                s += std::sqrt(cl->t2[i]) / cl->w2[i];
+                ++n;
+            }
+        if (!(s > 0.0)) return cfail(cl, PS3D_ERR_INVALID_ARG, "training targets are zero");
+        cl->ct = s / n;
+        cudaMemcpy(cl->ctd, &cl->ct, 8, cudaMemcpyHostToDevice);
+    }
+    upload_sample_scalars(cl);
+    if (cl->loss_cap < iters) {
+        void *q = nullptr;
+        if (cudaMalloc(&q, (size_t)(iters > 0 ? iters : 1) * 8) != cudaSuccess) {
+            cudaGetLastError();
+            return cfail(cl, PS3D_ERR_OUT_OF_MEMORY, "loss buffer");
+        }
+        if (cl->lossd) {
+            for (auto &p : cl->allocs)
+                if (p == cl->lossd) p = q;
+            cudaFree(cl->lossd);
+        } else {
+            cl->allocs.push_back(q);
+        }
+        cl->lossd = reinterpret_cast<double *>(q);
+        cl->loss_cap = iters;
+    }
+    SplitMix order{seed};
+    std::vector<int> perm(cl->nsamples);
+    int pos = cl->nsamples;
+    const float b1 = 0.9f, b2 = 0.999f;
+    for (int it = 0; it < iters; ++it) {
+        if (pos == cl->nsamples) {
+            for (int i = 0; i < cl->nsamples; ++i) perm[i] = i;
+            for (int i = cl->nsamples - 1; i > 0; --i) {
+                const int j = (int)(order.next() % (unsigned long long)(i + 1));
+                std::swap(perm[i], perm[j]);
+            }
+            pos = 0;
+        }
+        const int s = perm[pos++];
+        pack_sample(cl, cl->st, s);
+        forward(cl, cl->st);
+        loss_and_grad(cl, cl->st, s, cl->lossd + it);
+        backward(cl, cl->st);
+        cl->adam_t += 1;
+        const double frac = iters > 1 ? (double)it / (double)(iters - 1) : 0.0;
+        const double lr = lr1 + 0.5 * (lr0 - lr1) * (1.0 + std::cos(3.14159265358979323846 * frac));
+        const float c1 = (float)(1.0 / (1.0 - std::pow((double)b1, (double)cl->adam_t)));
+        const float c2 = (float)(1.0 / (1.0 - std::pow((double)b2, (double)cl->adam_t)));
+        k_adam<<<(NPARAM + 255) / 256, 256, 0, cl->st>>>(cl->w, cl->g, cl->m, cl->v, NPARAM, (float)lr, b1, b2, c1, c2,
+                                                         1e-8f);
+        images(cl, cl->st);
+        if ((it & 63) == 63) {
+            rc = ccheck(cl, "train");
+            if (rc) return rc;
+        }
+    }
+    if (cudaStreamSynchronize(cl->st) != cudaSuccess) return ccheck(cl, "train");
+    if (loss && iters > 0) cudaMemcpy(loss, cl->lossd, (size_t)iters * 8, cudaMemcpyDeviceToHost);
+    return ccheck(cl, "train");
+}
+
+int ps3d_closure_predict(ps3d_closure *cl, const double *vor, const double *vel, double *corr)
+{
+    int rc = centre(cl);
+    if (rc) return rc;
+    if (!vor || !vel || !corr) return PS3D_ERR_INVALID_ARG;
+    if (!(cl->ct > 0.0)) return cfail(cl, PS3D_ERR_NOT_READY, "closure output scale not set");
+    const long long P = cl->npts;
+    cudaMemcpyAsync(cl->host_in, vor, (size_t)3 * P * 8, cudaMemcpyHostToDevice, cl->st);
+    cudaMemcpyAsync(cl->host_in + 3 * P, vel, (size_t)3 * P * 8, cudaMemcpyHostToDevice, cl->st);
+    const double *dv = cl->host_in;
+    k_sumsq<double><<<RED_BLOCKS, RED_THREADS, 0, cl->st>>>(dv, dv + 3 * P, P, cl->Z, cl->Z, P, cl->rpart);
+    k_scal_finish<<<1, RED_THREADS, 0, cl->st>>>(cl->rpart, RED_BLOCKS, P, cl->ctd, cl->scal);
+    k_pack<double><<<RED_BLOCKS * 4, RED_THREADS, 0, cl->st>>>(dv, dv + 3 * P, P, cl->Z, cl->Z, P, cl->scal, cl->a0);
+    forward(cl, cl->st);
+    k_unpack<double><<<RED_BLOCKS * 4, RED_THREADS, 0, cl->st>>>(cl->outf, cl->scal, dv, P, cl->Z, P, cl->Z, P, 0,
+                                                                cl->host_out);
+    cudaMemcpyAsync(corr, cl->host_out, (size_t)3 * P * 8, cudaMemcpyDeviceToHost, cl->st);
+    if (cudaStreamSynchronize(cl->st) != cudaSuccess) return ccheck(cl, "predict");
+    return ccheck(cl, "predict");
+}
+
+int ps3d_closure_gradients(ps3d_closure *cl, int sample, float *out, float *grad, double *loss)
+{
+    int rc = centre(cl);
+    if (rc) return rc;
+    if (sample < 0 || sample >= cl->nsamples) return PS3D_ERR_INVALID_ARG;
+    if (!(cl->ct > 0.0)) return cfail(cl, PS3D_ERR_NOT_READY, "closure output scale not set");
+    upload_sample_scalars(cl);
+    const long long P = cl->npts;
+    pack_sample(cl, cl->st, sample);
+    forward(cl, cl->st);
+    loss_and_grad(cl, cl->st, sample, cl->lpart + RED_BLOCKS);
+    backward(cl, cl->st);
+    if (cudaStreamSynchronize(cl->st) != cudaSuccess) return ccheck(cl, "gradients");
+    if (grad) cudaMemcpy(grad, cl->g, NPARAM * 4, cudaMemcpyDeviceToHost);
+    if (loss) cudaMemcpy(loss, cl->lpart + RED_BLOCKS, 8, cudaMemcpyDeviceToHost);
+    if (out) {
+        std::vector<float> h((size_t)P * CPAD_OUT[NL - 1]);
+        cudaMemcpy(h.data(), cl->outf, h.size() * 4, cudaMemcpyDeviceToHost);
+        for (long long p = 0; p < P; ++p)
+            for (int c = 0; c < 3; ++c) out[c * P + p] = h[p * CPAD_OUT[NL - 1] + c];
+    }
+    return ccheck(cl, "gradients");
+}
+
+}  // extern "C"

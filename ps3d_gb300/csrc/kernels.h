@@ -3,7 +3,11 @@
 #pragma once
 #include <cuda_runtime.h>
 
+#include <string>
+
 #include "common.cuh"
+
+struct ps3d_closure;
 
 namespace ps3d {
 
@@ -243,6 +247,16 @@ template <typename T>
 void op_hyperbolic_tables(const Dims &d, cudaStream_t st, const double *k2l2, const double *k2l2i,
                           const double *rkz, const double *zm, const double *zp, double Lz, T *phim, T *phip,
                           T *thetam, T *thetap, T *dthetam, T *dthetap, T *green);
+
+// closure.cu: the learned sub-grid closure's side of a context
+int closure_attach(ps3d_closure *cl, const void *owner, int nx, int ny, int nz, int device, std::string *err);
+void closure_detach(ps3d_closure *cl, const void *owner);
+// physical correction out[c] (c*ostride + iz + pitch*col) from the physical
+// vor and vel of a run; no host synchronisation
+template <typename T>
+int closure_apply(ps3d_closure *cl, cudaStream_t st, const T *vor, const T *vel, long long cstride, int pitch, T *out,
+                  long long ostride, int flags);
+constexpr int CLOSURE_LAUNCHES = 9;
 
 size_t lines_smem_bytes(int n, bool fp64);
 size_t columns_smem_bytes(int nz, bool fp64);

@@ -141,6 +141,13 @@ struct ps3d_gpu_ctx {
     std::vector<double> h_bbarz;
     double bfsq = 0.0, bvisc = 0.0;
     Rolling roll_b;
+    // learned sub-grid closure (closure.cu): the attached network, its
+    // correction (3 fields of type T in the form svorts is assembled in)
+    // and whether the next source evaluates it afresh
+    ps3d_closure *closure = nullptr;
+    void *corr = nullptr;
+    int closure_flags = 0;  // PS3D_CLOSURE_*
+    bool closure_fresh = true;
 
     Deriv D() const { return Deriv{cx, cy}; }
     Tables tables() const
@@ -563,10 +570,41 @@ template <typename T> int buoyancy_diagnostics(ps3d_gpu_ctx *c, double out[4])
 }
 
 // ------------------------------------------------------------------- source
+// learned closure: the attached network's correction from the physical vor
+// and vel, taken to the form svorts is assembled in (semi-spectral in the
+// mixed form, mixed-spectral in FP64)
+template <typename T> int closure_correction(ps3d_gpu_ctx *c)
+{
+    const long long N = c->d.nfield;
+    T *corr = tf<T>(c->corr);
+    const int rc =
+        closure_apply<T>(c->closure, c->st, tf<T>(c->vor), tf<T>(c->vel), N, c->d.P, corr, N, c->closure_flags);
+    c->launches += CLOSURE_LAUNCHES;
+    if (rc) return check(c, "closure");
+    for (int k = 0; k < 3; ++k) {
+        xyf<T>(c, corr + k * N, corr + k * N);
+        if (sizeof(T) == sizeof(double)) col<T>(c, COL_DECOMP, corr + k * N, corr + k * N);
+    }
+    c->closure_fresh = false;
+    return PS3D_OK;
+}
+
+template <typename T> void closure_add(ps3d_gpu_ctx *c, T *svorts)
+{
+    const long long N = c->d.nfield;
+    for (int k = 0; k < 3; ++k) op_addf<T>(c->d, c->st, svorts + k * N, tf<T>(c->corr) + k * N);
+    c->launches += 3;
+}
+
 // source (inversion.f90:376-388): buoyancy_tendency, then vorticity_tendency
-// (:298-371) with the buoyancy in r = u eta - v xi + b
+// (:298-371) with the buoyancy in r = u eta - v xi + b; an attached closure's
+// correction is added to the tendency
 template <typename T> int source(ps3d_gpu_ctx *c)
 {
+    if (c->closure && ((c->closure_flags & PS3D_CLOSURE_EVERY_STAGE) || c->closure_fresh)) {
+        const int rc = closure_correction<T>(c);
+        if (rc) return rc;
+    }
     if (c->cfg.buoyancy) buoyancy_tendency<T>(c);
     const Dims &d = c->d;
     const long long N = d.nfield;
@@ -607,6 +645,7 @@ template <typename T> int source(ps3d_gpu_ctx *c)
         for (int k = 0; k < 5; ++k) xyf<T>(c, f5[k], f5[k]);
         op_svorts<T>(d, c->st, c->D(), r, q, p, gq, gp, svorts, svorts + N, svorts + 2 * N);
         c->launches += 1;
+        if (c->closure) closure_add<T>(c, svorts);
         for (int k = 0; k < 3; ++k) col<T>(c, COL_DECOMP, svorts + k * N, svorts + k * N);
         project_source<T>(c);
         return check(c, "source");
@@ -617,6 +656,7 @@ template <typename T> int source(ps3d_gpu_ctx *c)
     }
     op_svorts<T>(d, c->st, c->D(), r, q, p, gq, gp, svorts, svorts + N, svorts + 2 * N);
     c->launches += 1;
+    if (c->closure) closure_add<T>(c, svorts);
     return check(c, "source");
 }
 
@@ -925,6 +965,7 @@ template <typename T> int advance(ps3d_gpu_ctx *c, double *t, ps3d_gpu_diag *dia
     double dt;
     rc = adapt<T>(c, *t, &dt, diag);
     if (rc) return rc;
+    c->closure_fresh = true;
     rc = source<T>(c);
     if (rc) return rc;
     return step<T>(c, t, dt);
@@ -1047,6 +1088,7 @@ int advance_dev(ps3d_gpu_ctx *c)
     k_adapt_scalars<<<1, 1, 0, c->st>>>(c->sc, c->roll_dev, c->res1, c->res2, c->flag, ap);
     k_vdiss_dev<<<(unsigned)((d.ncol + 255) / 256), 256, 0, c->st>>>(d.ncol, c->vhdis, c->vdiss, c->sc);
     c->launches += 2;
+    c->closure_fresh = true;
     rc = source<float>(c);
     if (rc) return rc;
     return step_rk4<float>(c, nullptr, 0.0);
@@ -1722,6 +1764,7 @@ int ps3d_gpu_destroy(ps3d_gpu_ctx *c)
     if (!c) return PS3D_OK;
     cudaSetDevice(c->cfg.device);
     if (c->st) cudaStreamSynchronize(c->st);
+    if (c->closure) closure_detach(c->closure, c);
     if (c->graph) cudaGraphExecDestroy(c->graph);
     for (void *p : c->allocs) cudaFree(p);
     if (c->probe.ev) {
@@ -1957,9 +2000,41 @@ int ps3d_gpu_source(ps3d_gpu_ctx *c)
 {
     int rc = enter(c);
     if (rc) return rc;
+    c->closure_fresh = true;
     rc = DISPATCH(c, source, c);
     if (rc) return rc;
     return sync_check(c, "source");
+}
+
+int ps3d_gpu_set_closure(ps3d_gpu_ctx *c, ps3d_closure *cl, int flags)
+{
+    int rc = enter(c);
+    if (rc) return rc;
+    if (flags & ~(PS3D_CLOSURE_EVERY_STAGE | PS3D_CLOSURE_CLIP | PS3D_CLOSURE_WALLS)) return PS3D_ERR_INVALID_ARG;
+    cudaStreamSynchronize(c->st);
+    if (cl) {
+        std::string e;
+        rc = closure_attach(cl, c, c->d.nx, c->d.ny, c->d.nz, c->cfg.device, &e);
+        if (rc) return fail(c, rc, e);
+        if (!c->corr) {
+            const size_t bytes = 3 * (size_t)c->d.nfield * (c->fp64 ? sizeof(double) : sizeof(float));
+            if (!dalloc(c, &c->corr, bytes)) {
+                closure_detach(cl, c);
+                return fail(c, PS3D_ERR_OUT_OF_MEMORY, "closure correction fields");
+            }
+            cudaMemsetAsync(c->corr, 0, bytes, c->st);
+        }
+    }
+    if (c->closure && c->closure != cl) closure_detach(c->closure, c);
+    c->closure = cl;
+    c->closure_flags = flags;
+    c->closure_fresh = true;
+    // a captured step holds the launches of the previous configuration
+    if (c->graph) {
+        cudaGraphExecDestroy(c->graph);
+        c->graph = nullptr;
+    }
+    return sync_check(c, "set_closure");
 }
 
 int ps3d_gpu_adapt(ps3d_gpu_ctx *c, double t, double *dt, ps3d_gpu_diag *diag)

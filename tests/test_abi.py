@@ -15,7 +15,7 @@ HEADER = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))
 
 def declared():
     txt = open(HEADER).read()
-    return sorted(set(re.findall(r"\b(ps3d_gpu_\w+)\s*\(", txt)))
+    return sorted(set(re.findall(r"\b(ps3d_(?:gpu|closure)_\w+)\s*\(", txt)))
 
 
 def test_header_lists_match_binding():
