@@ -191,6 +191,54 @@ def cufft_comparator(n, dev):
         return {"unavailable": str(e)[:200]}
 
 
+def closure_timing(dev, n=64):
+    """The learned closure's forward pass (four BF16 tensor-core 3x3x3
+    convolutions, closure.cu) at n^3 against the measured bf16 peak, and its
+    cost inside a coarse step: one captured impl-diff-rk4 advance at n^3 with
+    and without a network evaluated at every stage."""
+    try:
+        from ps3d_gb300 import Ps3dGpu, ic
+        from ps3d_gb300.closure import Closure, attach, forward_flops, param_views
+        cl = Closure(n, n, n, device=dev, seed=3)
+        p = cl.get_params()
+        param_views(p)[-1][0][...] *= 10.0
+        cl.set_params(p)
+        cl.scale = 1e-3
+        rng = np.random.default_rng(0)
+        shape = (3, n, n, n + 1)
+        cl.predict(rng.standard_normal(shape), rng.standard_normal(shape))
+        ms = cl.time_forward(50)
+        npts = n * n * (n + 1)
+        tf = forward_flops(npts) / (ms * 1e9)
+        try:
+            with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+                pk, src = float(json.load(f)["bf16_tflops"]), "measured (MEASURED_PEAKS.json bf16_tflops)"
+        except (OSError, KeyError, ValueError):
+            pk, src = 1900.0, "fallback"
+        vor, pert = ic.beltrami_plus_perturbation(n, n, n, seed=1, amplitude=1.0e-2)
+        steps = {}
+        for name, net in (("plain", None), ("closure_every_stage", cl)):
+            m = Ps3dGpu(n, n, n, ic.BASELINE_BOX["lower"], ic.BASELINE_BOX["extent"], precision="mixed",
+                        device=dev, **model_kw())
+            m.setup_fields(vor, pert)
+            if net is not None:
+                attach(m, net, every_stage=True)
+            t, _, _ = m.advance_graph(0.0, 3)
+            _, _, mss = m.advance_graph(t, 20)
+            steps[name] = mss / 20
+            if net is not None:
+                attach(m, None)
+            m.close()
+        cl.close()
+        return {"grid": [n, n, n], "ms_per_forward": ms, "flops_per_forward": forward_flops(npts),
+                "roofline": {"bound": "tensor", "achieved": tf, "peak": pk, "unit": "TFLOP/s", "frac": tf / pk,
+                             "peak_source": src},
+                "tflops_padded_channels": forward_flops(npts, True) / (ms * 1e9),
+                "step_ms": steps}
+    except Exception as e:
+        return {"unavailable": str(e)[:200]}
+
+
 def cpu_sample(n_cpu, steps=1):
     """Time the CPU oracle: `steps` advances at n_cpu^3 after one warm-up."""
     import oracle
@@ -372,6 +420,8 @@ def run_gpu(args, rank, world, dist):
         if isinstance(cufft, dict) and "forward_xy_ms" in cufft:
             cufft["ours_xy_pass_pair_ms"] = ours
 
+    closure = closure_timing(dev) if rank == 0 and not args.skip_closure else None
+
     cpu = None
     if rank == 0 and not args.skip_cpu:
         csec, crate = cpu_sample(args.cpu_n)
@@ -394,6 +444,7 @@ def run_gpu(args, rank, world, dist):
             "device_bytes": gm.device_bytes,
             "line_fft_autotune": dict(zip(("shape", "ms_per_launch"), gm.tuning())),
             "cufft_comparator": cufft,
+            "closure": closure,
         }
         print(json.dumps(line), flush=True)
     gm.close()
@@ -443,6 +494,7 @@ def main():
     ap.add_argument("--skip-fp64", action="store_true")
     ap.add_argument("--skip-e2e", action="store_true")
     ap.add_argument("--skip-cpu", action="store_true")
+    ap.add_argument("--skip-closure", action="store_true")
     args = ap.parse_args()
     if args.warmup < 3:
         log("[bench] warm-up raised to 3 steps")

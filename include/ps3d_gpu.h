@@ -356,6 +356,10 @@ int ps3d_closure_predict(ps3d_closure *cl, const double *vor, const double *vel,
  * grad (optional): the PS3D_CLOSURE_NPARAM parameter gradients; loss
  * (optional): the normalised mean squared error. */
 int ps3d_closure_gradients(ps3d_closure *cl, int sample, float *out, float *grad, double *loss);
+/* Device time (CUDA events on the closure's stream) of one forward pass
+ * (the four convolutions) over the input of the last predict, averaged over
+ * reps passes after one untimed pass. */
+int ps3d_closure_time_forward(ps3d_closure *cl, int reps, double *ms);
 /* Attach a closure to a context of the same grid and device (NULL
  * detaches: plain hyperdiffusion).  flags, an OR of:
  *   PS3D_CLOSURE_EVERY_STAGE  evaluate the correction at every right-hand

@@ -35,6 +35,7 @@ EXPORTS = [
     "ps3d_closure_get_params", "ps3d_closure_set_params", "ps3d_closure_get_scale",
     "ps3d_closure_set_scale", "ps3d_closure_add_sample", "ps3d_closure_num_samples",
     "ps3d_closure_train", "ps3d_closure_predict", "ps3d_closure_gradients", "ps3d_gpu_set_closure",
+    "ps3d_closure_time_forward",
 ]
 
 
@@ -153,5 +154,6 @@ def lib(build_if_missing=True):
     L.ps3d_closure_predict.argtypes = [_vp, _dp, _dp, _dp]
     L.ps3d_closure_gradients.argtypes = [_vp, ctypes.c_int, _fp, _fp, _dp]
     L.ps3d_gpu_set_closure.argtypes = [_vp, _vp, ctypes.c_int]
+    L.ps3d_closure_time_forward.argtypes = [_vp, ctypes.c_int, _dp]
     _LIB = L
     return L

@@ -129,6 +129,12 @@ class Closure:
         self._chk(self.L.ps3d_closure_predict(self._h, _d(vor), _d(vel), _d(out)))
         return out
 
+    def time_forward(self, reps=20):
+        """device ms of one forward pass over the last predict's input"""
+        ms = ctypes.c_double()
+        self._chk(self.L.ps3d_closure_time_forward(self._h, int(reps), ctypes.byref(ms)))
+        return ms.value
+
     def gradients(self, sample):
         """(normalised prediction (3, npts) FP32, parameter gradients, loss)
         of stored sample `sample`, without an update."""
@@ -153,6 +159,13 @@ def attach(model, closure, every_stage=False, clip=False, walls=False):
 # ----------------------------------------------------------------- layout
 NTAP = 27
 LAYERS = ((6, 32), (32, 32), (32, 32), (32, 3))
+# channels the kernels compute with (inputs padded to 16, the output to 8)
+PADDED = ((16, 32), (32, 32), (32, 32), (32, 8))
+
+
+def forward_flops(npts, padded=False):
+    """multiply-add flops (2 per MAC) of one forward pass over npts points"""
+    return 2.0 * npts * NTAP * sum(ci * co for ci, co in (PADDED if padded else LAYERS))
 
 
 def param_views(p):

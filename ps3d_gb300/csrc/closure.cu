@@ -133,7 +133,7 @@ struct ConvArgs {
 // blocks walks tiles of 128 points, each warp 2 row tiles of 16 points x all
 // COUT output channels.
 template <int CIN, int COUT, int EPI>
-__global__ void __launch_bounds__(CONV_THREADS) k_conv(ConvArgs a)
+__global__ void __launch_bounds__(CONV_THREADS, 4) k_conv(ConvArgs a)
 {
     constexpr int S = CIN / 16, NT = COUT / 8, MT = 2;
     constexpr int WIMG = NTAP * S * NT * 32;
@@ -173,33 +173,36 @@ __global__ void __launch_bounds__(CONV_THREADS) k_conv(ConvArgs a)
 #pragma unroll
                 for (int q = 0; q < 4; ++q) acc[m][n][q] = 0.f;
 
+        // the nine (dx, dy) neighbour columns in a loop that stays rolled (a
+        // fully unrolled 27-tap body overflows the instruction cache); the
+        // three dz taps of a column issue their loads together
+#pragma unroll 1
+        for (int dxy = 0; dxy < 9; ++dxy) {
+            const int dx = dxy / 3 - 1, dy = dxy % 3 - 1;
+            long long cb[4];
 #pragma unroll
-        for (int dx = -1; dx <= 1; ++dx) {
+            for (int r = 0; r < 4; ++r)
+                cb[r] = (long long)Z * ((long long)((iy[r] + dy) & nym) + (long long)a.ny * ((ix[r] + dx) & nxm));
+            LT v[3][4];
 #pragma unroll
-            for (int dy = -1; dy <= 1; ++dy) {
-                long long cb[4];
+            for (int k = 0; k < 3; ++k)
 #pragma unroll
-                for (int r = 0; r < 4; ++r)
-                    cb[r] = (long long)Z * ((long long)((iy[r] + dy) & nym) + (long long)a.ny * ((ix[r] + dx) & nxm));
+                for (int r = 0; r < 4; ++r) {
+                    const int z2 = iz[r] + k - 1;
+                    v[k][r] = (ok[r] && z2 >= 0 && z2 < Z) ? __ldg(in + (cb[r] + z2) * 4 + t) : R::zero();
+                }
 #pragma unroll
-                for (int dz = -1; dz <= 1; ++dz) {
-                    const int tap = (dx + 1) * 9 + (dy + 1) * 3 + (dz + 1);
-                    LT v[4];
+            for (int k = 0; k < 3; ++k) {
+                const int tap = dxy * 3 + k;
 #pragma unroll
-                    for (int r = 0; r < 4; ++r) {
-                        const int z2 = iz[r] + dz;
-                        v[r] = (ok[r] && z2 >= 0 && z2 < Z) ? __ldg(in + (cb[r] + z2) * 4 + t) : R::zero();
-                    }
+                for (int s = 0; s < S; ++s) {
 #pragma unroll
-                    for (int s = 0; s < S; ++s) {
+                    for (int n = 0; n < NT; ++n) {
+                        const uint2 b = sw[((tap * S + s) * NT + n) * 32 + lane];
 #pragma unroll
-                        for (int n = 0; n < NT; ++n) {
-                            const uint2 b = sw[((tap * S + s) * NT + n) * 32 + lane];
-#pragma unroll
-                            for (int m = 0; m < MT; ++m)
-                                mma16816(acc[m][n], R::reg(v[2 * m], 2 * s), R::reg(v[2 * m + 1], 2 * s),
-                                         R::reg(v[2 * m], 2 * s + 1), R::reg(v[2 * m + 1], 2 * s + 1), b.x, b.y);
-                        }
+                        for (int m = 0; m < MT; ++m)
+                            mma16816(acc[m][n], R::reg(v[k][2 * m], 2 * s), R::reg(v[k][2 * m + 1], 2 * s),
+                                     R::reg(v[k][2 * m], 2 * s + 1), R::reg(v[k][2 * m + 1], 2 * s + 1), b.x, b.y);
                     }
                 }
             }
@@ -1107,6 +1110,28 @@ int ps3d_closure_predict(ps3d_closure *cl, const double *vor, const double *vel,
     cudaMemcpyAsync(corr, cl->host_out, (size_t)3 * P * 8, cudaMemcpyDeviceToHost, cl->st);
     if (cudaStreamSynchronize(cl->st) != cudaSuccess) return ccheck(cl, "predict");
     return ccheck(cl, "predict");
+}
+
+int ps3d_closure_time_forward(ps3d_closure *cl, int reps, double *ms)
+{
+    int rc = centre(cl);
+    if (rc) return rc;
+    if (reps < 1 || !ms) return PS3D_ERR_INVALID_ARG;
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    forward(cl, cl->st);  // warm-up
+    cudaEventRecord(e0, cl->st);
+    for (int i = 0; i < reps; ++i) forward(cl, cl->st);
+    cudaEventRecord(e1, cl->st);
+    cudaError_t e = cudaEventSynchronize(e1);
+    float t = 0.f;
+    if (e == cudaSuccess) e = cudaEventElapsedTime(&t, e0, e1);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (e != cudaSuccess) return cfail(cl, PS3D_ERR_CUDA, std::string("time_forward: ") + cudaGetErrorString(e));
+    *ms = (double)t / reps;
+    return ccheck(cl, "time_forward");
 }
 
 int ps3d_closure_gradients(ps3d_closure *cl, int sample, float *out, float *grad, double *loss)
