@@ -356,6 +356,20 @@ int ps3d_closure_predict(ps3d_closure *cl, const double *vor, const double *vel,
  * grad (optional): the PS3D_CLOSURE_NPARAM parameter gradients; loss
  * (optional): the normalised mean squared error. */
 int ps3d_closure_gradients(ps3d_closure *cl, int sample, float *out, float *grad, double *loss);
+/* Inference engine of the forward pass (predict, time_forward and an
+ * attached closure; training always uses the warp-level engine):
+ * PS3D_CLOSURE_ENGINE_MMA warp-level mma.sync on the plain channels-last
+ * activations; PS3D_CLOSURE_ENGINE_TCGEN05 tcgen05.mma with TMEM accumulators
+ * on padded activations fed by TMA bulk copies (PS3D_ERR_UNSUPPORTED_SIZE when
+ * a tile of the grid's columns does not fit shared memory: nz above 160).
+ * The default is TCGEN05 where the grid allows it, else MMA. */
+#define PS3D_CLOSURE_ENGINE_MMA 0
+#define PS3D_CLOSURE_ENGINE_TCGEN05 1
+int ps3d_closure_set_engine(ps3d_closure *cl, int engine);
+int ps3d_closure_get_engine(ps3d_closure *cl, int *engine);
+/* Synchronise and report a bounded device wait of the tcgen05 engine that ran
+ * out since the last check (PS3D_ERR_DEVICE_LIMIT; the word is cleared). */
+int ps3d_closure_check(ps3d_closure *cl);
 /* Device time (CUDA events on the closure's stream) of one forward pass
  * (the four convolutions) over the input of the last predict, averaged over
  * reps passes after one untimed pass. */

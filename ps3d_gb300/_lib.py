@@ -35,7 +35,7 @@ EXPORTS = [
     "ps3d_closure_get_params", "ps3d_closure_set_params", "ps3d_closure_get_scale",
     "ps3d_closure_set_scale", "ps3d_closure_add_sample", "ps3d_closure_num_samples",
     "ps3d_closure_train", "ps3d_closure_predict", "ps3d_closure_gradients", "ps3d_gpu_set_closure",
-    "ps3d_closure_time_forward",
+    "ps3d_closure_time_forward", "ps3d_closure_set_engine", "ps3d_closure_get_engine", "ps3d_closure_check",
 ]
 
 
@@ -155,5 +155,8 @@ def lib(build_if_missing=True):
     L.ps3d_closure_gradients.argtypes = [_vp, ctypes.c_int, _fp, _fp, _dp]
     L.ps3d_gpu_set_closure.argtypes = [_vp, _vp, ctypes.c_int]
     L.ps3d_closure_time_forward.argtypes = [_vp, ctypes.c_int, _dp]
+    L.ps3d_closure_set_engine.argtypes = [_vp, ctypes.c_int]
+    L.ps3d_closure_get_engine.argtypes = [_vp, ctypes.POINTER(ctypes.c_int)]
+    L.ps3d_closure_check.argtypes = [_vp]
     _LIB = L
     return L

@@ -24,6 +24,7 @@ import numpy as np
 from . import _lib
 
 NPARAM = 63171
+ENGINES = ("mma", "tcgen05")
 _fp = ctypes.POINTER(ctypes.c_float)
 _dp = ctypes.POINTER(ctypes.c_double)
 
@@ -128,6 +129,21 @@ class Closure:
         out = np.zeros(self.shape)
         self._chk(self.L.ps3d_closure_predict(self._h, _d(vor), _d(vel), _d(out)))
         return out
+
+    @property
+    def engine(self):
+        """"mma" (warp-level mma.sync) or "tcgen05" (inference engine)"""
+        e = ctypes.c_int()
+        self._chk(self.L.ps3d_closure_get_engine(self._h, ctypes.byref(e)))
+        return ENGINES[e.value]
+
+    @engine.setter
+    def engine(self, name):
+        self._chk(self.L.ps3d_closure_set_engine(self._h, ENGINES.index(name)))
+
+    def check(self):
+        """raise if a bounded device wait of the tcgen05 engine ran out"""
+        self._chk(self.L.ps3d_closure_check(self._h))
 
     def time_forward(self, reps=20):
         """device ms of one forward pass over the last predict's input"""

@@ -50,6 +50,7 @@ constexpr int CREAL_OUT[NL] = {32, 32, 32, 3};
 constexpr int CPAD_IN[NL] = {16, 32, 32, 32};
 constexpr int CPAD_OUT[NL] = {32, 32, 32, 8};
 constexpr int CPAD_DZ4 = 16;  // output-layer gradient channels (a 16-wide k step)
+constexpr int OUTC = 8;       // = CPAD_OUT[NL - 1], usable in device code
 
 constexpr int woff(int l)
 {
@@ -453,8 +454,9 @@ __global__ void k_unpack(const float *__restrict__ outf, const float *__restrict
             if (iz == 0 || iz == Z - 1) c0 = c1 = 0.f;
         }
         if (flags & PS3D_CLOSURE_CLIP) {
-            const float w = (float)vor[dst] * c0 + (float)vor[dst + vstride] * c1 + (float)vor[dst + 2 * vstride] * c2;
-            if (w > 0.f) c0 = c1 = c2 = 0.f;
+            // the sign test in the field's precision
+            const T w = vor[dst] * (T)c0 + vor[dst + vstride] * (T)c1 + vor[dst + 2 * vstride] * (T)c2;
+            if (w > (T)0) c0 = c1 = c2 = 0.f;
         }
         out[dst] = (T)c0;
         out[dst + ostride] = (T)c1;
@@ -565,6 +567,374 @@ __global__ void k_adam(float *__restrict__ w, const float *__restrict__ g, float
     w[i] -= lr * (mi * c1) / (sqrtf(vi * c2) + eps);
 }
 
+// ===================================================== tcgen05 inference path
+// The forward pass on the 5th-generation tensor cores.  Activations live in a
+// padded, channel-chunk-planar layout: padded row r = GUARD + (iz+1) +
+// ZP*((iy+1) + YP*(ix+1)) (ZP = nz+3, YP = ny+2), chunk plane kc (8 channels,
+// 16 bytes) at byte (kc*RTOT + r)*16.  Ghost rows at iz = -1, nz+1 stay zero
+// (the z zero padding); ghost rows at iy = -1, ny and ix = -1, nx hold the
+// periodic copies, written by the producer of each activation; GUARD rows
+// before and after keep every load of a tile in bounds.  Every tap is then a
+// uniform shift of the row index, so one tile of 128 output rows needs, per x
+// shift dx, one contiguous run of 128 + 2(ZP+1) rows per chunk plane: 3 x KC
+// one-dimensional TMA bulk copies.  The 27 taps x CIN/16 k-steps are
+// tcgen05.mma (M 128, N = COUT, K 16, BF16 in, FP32 accumulate in TMEM)
+// issued by one thread from shared-memory descriptors shifted by
+// (ZP*dy + dz) rows (no-swizzle K-major core matrices: 8 rows x 16 bytes,
+// SBO 128 bytes between row groups, LBO one chunk plane); the epilogue reads
+// the accumulator with tcgen05.ld (one TMEM lane per thread = one output row).
+
+struct TcArgs {
+    const unsigned char *in;   // padded chunk-planar input (CIN/8 planes)
+    const uint4 *wimg;         // [tap][kc][co] x 16 bytes
+    const float *bias;         // [COUT]
+    unsigned char *out;        // EPI_GELU: padded chunk-planar activation
+    float *outf;               // EPI_OUT: [npts][CPAD_OUT] FP32
+    int *err;                  // device error word (bounded waits)
+    int nx, ny, Z, ZP, YP;
+    long long QN, RTOT, GUARD, npts;
+};
+
+__device__ __forceinline__ uint32_t smem_u32(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ uint64_t tc_desc(uint32_t saddr, uint32_t lbo, uint32_t sbo)
+{
+    // sm_100-family shared-memory matrix descriptor, no swizzle
+    uint64_t d = (uint64_t)((saddr >> 4) & 0x3FFFu);
+    d |= (uint64_t)((lbo >> 4) & 0x3FFFu) << 16;
+    d |= (uint64_t)((sbo >> 4) & 0x3FFFu) << 32;
+    d |= (uint64_t)1 << 46;  // descriptor version
+    return d;
+}
+
+template <int COUT> __host__ __device__ constexpr uint32_t tc_idesc()
+{
+    // kind::f16: D F32 (bits 4-5 = 1), A BF16 (7-9 = 1), B BF16 (10-12 = 1),
+    // both K-major, N >> 3 at 17-22, M >> 4 at 24-28 (M = 128)
+    return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(COUT >> 3) << 17) | ((uint32_t)(128 >> 4) << 24);
+}
+
+__device__ __forceinline__ void mbar_init(uint32_t a, uint32_t count)
+{
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;\n" ::"r"(a), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(uint32_t a, uint32_t bytes)
+{
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(a), "r"(bytes) : "memory");
+}
+// bounded wait for the completion of the phase with the given parity: a
+// non-blocking test with a short sleep, at most 2^21 rounds (about a second)
+__device__ __forceinline__ bool mbar_wait(uint32_t a, uint32_t parity)
+{
+    for (int i = 0; i < (1 << 21); ++i) {
+        uint32_t ok;
+        asm volatile(
+            "{\n.reg .pred p;\nmbarrier.test_wait.parity.shared::cta.b64 p, [%1], %2;\nselp.u32 %0, 1, 0, p;\n}\n"
+            : "=r"(ok)
+            : "r"(a), "r"(parity)
+            : "memory");
+        if (ok) return true;
+        if (i > 64) __nanosleep(256);
+    }
+    return false;
+}
+__device__ __forceinline__ void bulk_g2s(uint32_t dst, const void *src, uint32_t bytes, uint32_t mbar)
+{
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];\n" ::"r"(dst),
+                 "l"(src), "r"(bytes), "r"(mbar)
+                 : "memory");
+}
+__device__ __forceinline__ void tc_mma(uint32_t tmem, uint64_t ad, uint64_t bd, uint32_t idesc, uint32_t acc)
+{
+    asm volatile(
+        "{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\ntcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem),
+        "l"(ad), "l"(bd), "r"(idesc), "r"(acc));
+}
+__device__ __forceinline__ void tc_commit(uint32_t mbar)
+{
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(mbar) : "memory");
+}
+__device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory"); }
+__device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory"); }
+
+// 16 / 8 consecutive FP32 columns of this thread's TMEM lane
+__device__ __forceinline__ void tc_ld16(uint32_t taddr, float *v)
+{
+    uint32_t r[16];
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];\n"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]),
+          "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+        : "r"(taddr));
+    asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
+#pragma unroll
+    for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
+}
+
+__device__ __forceinline__ void tc_ld8(uint32_t taddr, float *v)
+{
+    uint32_t r[8];
+    asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];\n"
+                 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7])
+                 : "r"(taddr));
+    asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
+#pragma unroll
+    for (int i = 0; i < 8; ++i) v[i] = __uint_as_float(r[i]);
+}
+
+// padded row of point (ix, iy, iz) with x / y shifts (ghost copies)
+__device__ __forceinline__ long long tc_row(long long G, int ZP, int YP, int ixp, int iyp, int iz)
+{
+    return G + (iz + 1) + (long long)ZP * (iyp + (long long)YP * ixp);
+}
+
+// write the 16-byte chunks v[kc] of interior point (ix, iy, iz) to its row
+// and to the periodic ghost rows that mirror it
+template <int KC>
+__device__ __forceinline__ void tc_store_point(unsigned char *base, long long RTOT, long long G, int ZP, int YP, int nx,
+                                               int ny, int ix, int iy, int iz, const uint4 *v, int kc0 = 0)
+{
+    int xs[2], ys[2], nxs = 1, nys = 1;
+    xs[0] = ix + 1;
+    ys[0] = iy + 1;
+    if (ix == 0) xs[nxs++] = nx + 1;
+    else if (ix == nx - 1) xs[nxs++] = 0;
+    if (iy == 0) ys[nys++] = ny + 1;
+    else if (iy == ny - 1) ys[nys++] = 0;
+    for (int a = 0; a < nxs; ++a)
+        for (int b = 0; b < nys; ++b) {
+            const long long r = tc_row(G, ZP, YP, xs[a], ys[b], iz);
+#pragma unroll
+            for (int kc = 0; kc < KC; ++kc)
+                *reinterpret_cast<uint4 *>(base + ((long long)(kc0 + kc) * RTOT + r) * 16) = v[kc];
+        }
+}
+
+// network input in the padded layout (channels 0-2 vor*scal[0], 3-5
+// vel*scal[1], 6-15 zero; two chunk planes)
+template <typename T>
+__global__ void k_pack_pad(const T *__restrict__ vor, const T *__restrict__ vel, long long cstride, int pitch, int nx,
+                           int ny, int Z, int ZP, int YP, long long RTOT, long long G, long long npts,
+                           const float *__restrict__ scal, unsigned char *__restrict__ a0)
+{
+    const float sw = scal[0], su = scal[1];
+    for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < npts;
+         p += (long long)gridDim.x * blockDim.x) {
+        const long long col = p / Z;
+        const int iz = (int)(p - col * Z), iy = (int)(col % ny), ix = (int)(col / ny);
+        const long long src = iz + (long long)pitch * col;
+        const float v0 = (float)vor[src] * sw, v1 = (float)vor[src + cstride] * sw, v2 = (float)vor[src + 2 * cstride] * sw;
+        const float u0 = (float)vel[src] * su, u1 = (float)vel[src + cstride] * su, u2 = (float)vel[src + 2 * cstride] * su;
+        uint4 v[2];
+        v[0] = make_uint4(pack2(v0, v1), pack2(v2, u0), pack2(u1, u2), 0u);
+        v[1] = make_uint4(0u, 0u, 0u, 0u);
+        tc_store_point<2>(a0, RTOT, G, ZP, YP, nx, ny, ix, iy, iz, v);
+    }
+}
+
+// [tap][kc][co] x 8 BF16 weight image of one layer for the tcgen05 kernel
+__global__ void k_wimage_tc(const float *__restrict__ W, int cin, int cout, int CINP, int COUTP, uint4 *__restrict__ img)
+{
+    const int KC = CINP / 8;
+    const int total = NTAP * KC * COUTP;
+    const int e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= total) return;
+    const int co = e % COUTP, kc = (e / COUTP) % KC, tap = e / (COUTP * KC);
+    float w[8];
+#pragma unroll
+    for (int j = 0; j < 8; ++j) {
+        const int ci = kc * 8 + j;
+        w[j] = (ci < cin && co < cout) ? W[((long long)tap * cin + ci) * cout + co] : 0.f;
+    }
+    img[e] = make_uint4(pack2(w[0], w[1]), pack2(w[2], w[3]), pack2(w[4], w[5]), pack2(w[6], w[7]));
+}
+
+template <int CIN, int COUT> __host__ __device__ constexpr int tc_wbytes() { return NTAP * (CIN / 8) * COUT * 16; }
+__host__ __device__ inline int tc_seg(int ZP) { return 128 + 2 * (ZP + 1); }
+// weights + two tile buffers of 3 x CIN/8 chunk planes
+template <int CIN, int COUT> __host__ __device__ inline size_t tc_smem(int ZP)
+{
+    return (size_t)tc_wbytes<CIN, COUT>() + (size_t)2 * 3 * (CIN / 8) * tc_seg(ZP) * 16;
+}
+
+// epilogue of one tile for one output row and one half of the accumulator
+// columns (v: COUT/2 values from column half*COUT/2): bias + GELU into the
+// padded activation (with its ghost copies), or, for half 0 of the output
+// layer, bias only into the FP32 output
+template <int COUT, int EPI>
+__device__ __forceinline__ void tc_epilogue(const TcArgs &a, const float *bias, unsigned q, int half, const float *v)
+{
+    if ((long long)q >= a.QN) return;
+    const unsigned ZP = (unsigned)a.ZP, YP = (unsigned)a.YP;
+    const unsigned t1 = q / ZP;
+    const int iz = (int)(q - t1 * ZP) - 1, iy = (int)(t1 % YP) - 1, ix = (int)(t1 / YP) - 1;
+    if (iz < 0 || iz >= a.Z || iy < 0 || iy >= a.ny || ix < 0 || ix >= a.nx) return;
+    constexpr int H = COUT / 2;
+    if (EPI == EPI_GELU) {
+        uint4 o[H / 8];
+#pragma unroll
+        for (int k = 0; k < H / 8; ++k) {
+            uint32_t w4[4];
+#pragma unroll
+            for (int j = 0; j < 4; ++j) {
+                const int c = half * H + 8 * k + 2 * j;
+                const float2 zr = unpack2(pack2(v[8 * k + 2 * j] + bias[c], v[8 * k + 2 * j + 1] + bias[c + 1]));
+                w4[j] = pack2(gelu_f(zr.x), gelu_f(zr.y));
+            }
+            o[k] = make_uint4(w4[0], w4[1], w4[2], w4[3]);
+        }
+        tc_store_point<H / 8>(a.out, a.RTOT, a.GUARD, a.ZP, a.YP, a.nx, a.ny, ix, iy, iz, o, half * (H / 8));
+    } else if (half == 0) {
+        const long long p = iz + (long long)a.Z * (iy + (long long)a.ny * ix);
+        float *o = a.outf + p * OUTC;
+#pragma unroll
+        for (int j = 0; j < OUTC; ++j) o[j] = v[j] + bias[j];
+    }
+}
+
+// One convolution layer over the padded grid.  Persistent CTAs of 8 warps
+// walk tiles of 128 padded rows with a two-deep pipeline: thread 0 issues the
+// products of tile k into TMEM accumulator k%2; once the products of tile
+// k-1 are complete it starts the TMA copies of tile k+1 into the shared
+// buffer they used, and meanwhile all 256 threads read accumulator (k-1)%2
+// for the epilogue of tile k-1 (warp w: TMEM lanes 32(w%4).., column half
+// w/4).  Every wait is bounded; a wait that runs out raises the error word,
+// lets the operations in flight finish (bounded) and frees the accumulator.
+template <int CIN, int COUT, int EPI>
+__global__ void __launch_bounds__(256, 1) k_conv_tc(TcArgs a)
+{
+    constexpr int KC = CIN / 8, S = CIN / 16;
+    constexpr int WB = tc_wbytes<CIN, COUT>();
+    constexpr uint32_t IDESC = tc_idesc<COUT>();
+    extern __shared__ __align__(1024) unsigned char smem[];
+    __shared__ __align__(8) uint64_t mbar[4];  // loads of buffers 0, 1; products into accumulators 0, 1
+    __shared__ uint32_t tmem_slot;
+    __shared__ int bad;
+    __shared__ float sbias[32];
+    unsigned char *sW = smem;
+    unsigned char *sA = smem + WB;
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int ZP = a.ZP;
+    const uint32_t segb = (uint32_t)tc_seg(ZP) * 16u;
+    if (tid < 32) sbias[tid] = tid < COUT ? a.bias[tid] : 0.f;
+    const uint32_t abuf = (uint32_t)(3 * KC) * segb;
+    const long long plane = (long long)ZP * a.YP;
+
+    if (tid == 0) {
+        for (int i = 0; i < 4; ++i) mbar_init(smem_u32(&mbar[i]), 1);
+        bad = 0;
+        asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+    }
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 64;\n" ::"r"(smem_u32(&tmem_slot))
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n" ::: "memory");
+    }
+    for (int i = tid; i < WB / 16; i += 256) reinterpret_cast<uint4 *>(sW)[i] = __ldg(a.wimg + i);
+    asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = tmem_slot;
+    const uint32_t sAu = smem_u32(sA), sWu = smem_u32(sW);
+    uint32_t ph[4] = {0u, 0u, 0u, 0u};
+    bool pend[4] = {false, false, false, false};
+    const long long ntiles = (a.QN + 127) / 128;
+    const long long nk = ntiles > (long long)blockIdx.x ? (ntiles - 1 - blockIdx.x) / gridDim.x + 1 : 0;
+    auto tile_q0 = [&](long long k) { return ((long long)blockIdx.x + k * (long long)gridDim.x) * 128; };
+    auto issue_load = [&](long long k) {
+        const int b = (int)(k & 1);
+        const uint32_t mb = smem_u32(&mbar[b]);
+        mbar_expect_tx(mb, abuf);
+        const long long q0 = tile_q0(k);
+        for (int dxi = 0; dxi < 3; ++dxi) {
+            const long long r0 = a.GUARD + q0 + (dxi - 1) * plane - (ZP + 1);
+            for (int kc = 0; kc < KC; ++kc)
+                bulk_g2s(sAu + (uint32_t)b * abuf + (uint32_t)(dxi * KC + kc) * segb,
+                         a.in + ((long long)kc * a.RTOT + r0) * 16, segb, mb);
+        }
+    };
+    auto wait_bar = [&](int i) {
+        if (mbar_wait(smem_u32(&mbar[i]), ph[i])) {
+            ph[i] ^= 1u;
+            pend[i] = false;
+        } else {
+            bad = 1;
+        }
+    };
+    auto epilogue = [&](long long k) {
+        const int b = (int)(k & 1), quarter = warp & 3, half = warp >> 2;
+        float v[16];
+        const uint32_t taddr = tmem + (uint32_t)(b * 32 + half * (COUT / 2)) + ((uint32_t)(quarter * 32) << 16);
+        if (COUT == 32) tc_ld16(taddr, v);
+        else tc_ld8(taddr, v);
+        tc_epilogue<COUT, EPI>(a, sbias, (unsigned)(tile_q0(k) + quarter * 32 + lane), half, v);
+    };
+
+    if (nk > 0) {
+        pend[0] = true;
+        if (tid == 0) issue_load(0);
+    }
+    for (long long k = 0; k < nk; ++k) {
+        const int b = (int)(k & 1);
+        wait_bar(b);  // tile k in shared memory
+        __syncthreads();
+        if (bad) break;
+        pend[2 + b] = true;
+        if (tid == 0) {
+            tc_fence_after();
+            const uint32_t acc = tmem + (uint32_t)(b * 32);
+            // descriptors = base descriptor + start offset in 16-byte units
+            // (the 14-bit start field cannot carry below 256 KB)
+            const uint64_t ad0 = tc_desc(sAu + (uint32_t)b * abuf, segb, 128u);
+            const uint64_t bd0 = tc_desc(sWu, COUT * 16u, 128u);
+            const int seg = (int)(segb >> 4);
+#pragma unroll
+            for (int dxi = 0; dxi < 3; ++dxi)
+#pragma unroll
+                for (int dyi = 0; dyi < 3; ++dyi)
+#pragma unroll
+                    for (int dzi = 0; dzi < 3; ++dzi)
+#pragma unroll
+                        for (int s2 = 0; s2 < S; ++s2) {
+                            const int tap = dxi * 9 + dyi * 3 + dzi;
+                            // row offset of the tap in the tile buffer, >= 0
+                            const int off = (dxi * KC + 2 * s2) * seg + (ZP + 1) + ZP * (dyi - 1) + (dzi - 1);
+                            const uint64_t ad = ad0 + (uint64_t)(uint32_t)off;
+                            const uint64_t bd = bd0 + (uint64_t)((tap * KC + 2 * s2) * COUT);
+                            tc_mma(acc, ad, bd, IDESC, (tap | s2) != 0 ? 1u : 0u);
+                        }
+            tc_commit(smem_u32(&mbar[2 + b]));
+        }
+        if (k >= 1) wait_bar(2 + (int)((k - 1) & 1));  // products of tile k-1 done: its buffer is free
+        if (k + 1 < nk) {
+            pend[(k + 1) & 1] = true;
+            if (tid == 0) issue_load(k + 1);
+        }
+        if (k >= 1) {
+            tc_fence_after();
+            epilogue(k - 1);
+        }
+        tc_fence_before();
+        __syncthreads();
+        if (bad) break;
+    }
+    if (!bad && nk > 0) {  // uniform: read after a barrier
+        wait_bar(2 + (int)((nk - 1) & 1));
+        tc_fence_after();
+        epilogue(nk - 1);  // warp-collective TMEM load, whatever the wait gave
+    }
+    if (bad) {
+        if (tid == 0) atomicOr(a.err, 1);
+        for (int i = 0; i < 4; ++i)
+            if (pend[i]) mbar_wait(smem_u32(&mbar[i]), ph[i]);
+    }
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 64;\n" ::"r"(tmem) : "memory");
+}
+
 // host-side SplitMix64 (parameter initialisation, sample order)
 struct SplitMix {
     unsigned long long s;
@@ -597,6 +967,14 @@ struct ps3d_closure {
     float *outf = nullptr, *wpart = nullptr, *scal = nullptr;
     double *rpart = nullptr, *lpart = nullptr, *lossd = nullptr;
     double *ctd = nullptr;   // ct in device memory; lpart[RED_BLOCKS]: one loss value
+    // tcgen05 inference path: padded chunk-planar activations (input, two
+    // ping-pong hidden buffers), weight images, device error word
+    int engine = 0, tc_ok = 0, tc_occ[3] = {1, 1, 1};
+    int ZP = 0, YP = 0;
+    long long QN = 0, RTOT = 0, GUARD = 0;
+    unsigned char *pa0 = nullptr, *pact[2] = {};
+    uint4 *imgtc[NL] = {};
+    int *derr = nullptr;
     int occ[5] = {1, 1, 1, 1, 1};  // resident conv blocks per SM per instantiation
     int loss_cap = 0;
     double *host_out = nullptr;   // predict staging (device)
@@ -676,6 +1054,94 @@ ConvArgs base_args(ps3d_closure *cl)
     a.Z = cl->Z;
     a.npts = cl->npts;
     return a;
+}
+
+void forward(ps3d_closure *cl, cudaStream_t st);
+
+TcArgs tc_args(ps3d_closure *cl)
+{
+    TcArgs a{};
+    a.err = cl->derr;
+    a.nx = cl->nx;
+    a.ny = cl->ny;
+    a.Z = cl->Z;
+    a.ZP = cl->ZP;
+    a.YP = cl->YP;
+    a.QN = cl->QN;
+    a.RTOT = cl->RTOT;
+    a.GUARD = cl->GUARD;
+    a.npts = cl->npts;
+    return a;
+}
+
+template <int CIN, int COUT, int EPI> constexpr int tc_slot() { return EPI == EPI_OUT ? 2 : (CIN == 16 ? 0 : 1); }
+
+template <int CIN, int COUT, int EPI> bool tc_attr(ps3d_closure *cl)
+{
+    const size_t sm = tc_smem<CIN, COUT>(cl->ZP);
+    if (cudaFuncSetAttribute(k_conv_tc<CIN, COUT, EPI>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm) !=
+        cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    int nb = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_conv_tc<CIN, COUT, EPI>, 256, sm) != cudaSuccess ||
+        nb < 1) {
+        cudaGetLastError();
+        return false;
+    }
+    cl->tc_occ[tc_slot<CIN, COUT, EPI>()] = nb;
+    return true;
+}
+
+template <int CIN, int COUT, int EPI> void conv_tc(ps3d_closure *cl, cudaStream_t st, const TcArgs &a)
+{
+    const long long ntiles = (cl->QN + 127) / 128;
+    const long long maxb = (long long)cl->nsm * cl->tc_occ[tc_slot<CIN, COUT, EPI>()];
+    const long long per = (ntiles + maxb - 1) / maxb;
+    const unsigned grid = (unsigned)((ntiles + per - 1) / per);
+    k_conv_tc<CIN, COUT, EPI><<<grid, 256, tc_smem<CIN, COUT>(cl->ZP), st>>>(a);
+}
+
+// tcgen05 forward pass: pa0 -> pact[0] -> pact[1] -> pact[0] -> outf
+void forward_tc(ps3d_closure *cl, cudaStream_t st)
+{
+    TcArgs a = tc_args(cl);
+    a.in = cl->pa0;
+    a.wimg = cl->imgtc[0];
+    a.bias = cl->bpad[0];
+    a.out = cl->pact[0];
+    conv_tc<16, 32, EPI_GELU>(cl, st, a);
+    a.in = cl->pact[0];
+    a.wimg = cl->imgtc[1];
+    a.bias = cl->bpad[1];
+    a.out = cl->pact[1];
+    conv_tc<32, 32, EPI_GELU>(cl, st, a);
+    a.in = cl->pact[1];
+    a.wimg = cl->imgtc[2];
+    a.bias = cl->bpad[2];
+    a.out = cl->pact[0];
+    conv_tc<32, 32, EPI_GELU>(cl, st, a);
+    a.in = cl->pact[0];
+    a.wimg = cl->imgtc[3];
+    a.bias = cl->bpad[3];
+    a.out = nullptr;
+    a.outf = cl->outf;
+    conv_tc<32, 16, EPI_OUT>(cl, st, a);
+}
+
+// input packing and forward pass of the selected engine
+template <typename T>
+void pack_forward(ps3d_closure *cl, cudaStream_t st, const T *vor, const T *vel, long long cstride, int pitch)
+{
+    if (cl->engine == 1) {
+        k_pack_pad<T><<<RED_BLOCKS * 4, RED_THREADS, 0, st>>>(vor, vel, cstride, pitch, cl->nx, cl->ny, cl->Z, cl->ZP,
+                                                            cl->YP, cl->RTOT, cl->GUARD, cl->npts, cl->scal, cl->pa0);
+        forward_tc(cl, st);
+    } else {
+        k_pack<T><<<RED_BLOCKS * 4, RED_THREADS, 0, st>>>(vor, vel, cstride, pitch, cl->Z, cl->npts, cl->scal, cl->a0);
+        forward(cl, st);
+    }
 }
 
 // four layers: a0 -> z1/a1 -> z2/a2 -> z3/a3 -> outf
@@ -758,6 +1224,12 @@ void images(ps3d_closure *cl, cudaStream_t st)
             k_wimage<<<(nb + 255) / 256, 256, 0, st>>>(W, b, CREAL_IN[l], CREAL_OUT[l], cinp, CPAD_IN[l], 1,
                                                       cl->imgb[l], nullptr);
         }
+        if (cl->tc_ok) {
+            const int coutp = l == NL - 1 ? 16 : CPAD_OUT[l];
+            const int nt = NTAP * (CPAD_IN[l] / 8) * coutp;
+            k_wimage_tc<<<(nt + 255) / 256, 256, 0, st>>>(W, CREAL_IN[l], CREAL_OUT[l], CPAD_IN[l], coutp,
+                                                         cl->imgtc[l]);
+        }
     }
 }
 
@@ -838,8 +1310,7 @@ int closure_apply(ps3d_closure *cl, cudaStream_t st, const T *vor, const T *vel,
 {
     k_sumsq<T><<<RED_BLOCKS, RED_THREADS, 0, st>>>(vor, vel, cstride, pitch, cl->Z, cl->npts, cl->rpart);
     k_scal_finish<<<1, RED_THREADS, 0, st>>>(cl->rpart, RED_BLOCKS, cl->npts, cl->ctd, cl->scal);
-    k_pack<T><<<RED_BLOCKS * 4, RED_THREADS, 0, st>>>(vor, vel, cstride, pitch, cl->Z, cl->npts, cl->scal, cl->a0);
-    forward(cl, st);
+    pack_forward<T>(cl, st, vor, vel, cstride, pitch);
     k_unpack<T><<<RED_BLOCKS * 4, RED_THREADS, 0, st>>>(cl->outf, cl->scal, vor, cstride, cl->Z, cl->npts, pitch,
                                                        ostride, flags, out);
     return cudaPeekAtLastError() == cudaSuccess ? PS3D_OK : PS3D_ERR_CUDA;
@@ -890,6 +1361,16 @@ int ps3d_closure_create(int nx, int ny, int nz, int max_samples, int device, uns
     conv_attr<32, 8, EPI_OUT>(cl);
     conv_attr<16, 32, EPI_BWD>(cl);
     conv_attr<32, 32, EPI_BWD>(cl);
+    // tcgen05 path: padded geometry; available when a tile's shared memory
+    // (weights + 3 x 4 chunk planes of 128 + 2(ZP+1) rows) fits a block
+    cl->ZP = nz + 3;
+    cl->YP = ny + 2;
+    cl->QN = (long long)(nx + 2) * cl->YP * cl->ZP;
+    cl->GUARD = (long long)cl->YP * cl->ZP + cl->ZP + 256;
+    cl->RTOT = (cl->QN + 2 * cl->GUARD + 7) / 8 * 8;
+    cl->tc_ok = tc_smem<32, 32>(cl->ZP) + 2048 <= (size_t)prop.sharedMemPerBlockOptin && tc_attr<16, 32, EPI_GELU>(cl) &&
+                tc_attr<32, 32, EPI_GELU>(cl) && tc_attr<32, 16, EPI_OUT>(cl);
+    cl->engine = cl->tc_ok ? PS3D_CLOSURE_ENGINE_TCGEN05 : PS3D_CLOSURE_ENGINE_MMA;
     const long long P = cl->npts;
     bool ok = calloc_dev(cl, &cl->w, NPARAM * 4) && calloc_dev(cl, &cl->g, NPARAM * 4) &&
               calloc_dev(cl, &cl->m, NPARAM * 4) && calloc_dev(cl, &cl->v, NPARAM * 4);
@@ -910,6 +1391,16 @@ int ps3d_closure_create(int nx, int ny, int nz, int max_samples, int device, uns
          calloc_dev(cl, &cl->lpart, (RED_BLOCKS + 1) * 8) && calloc_dev(cl, &cl->ctd, 8) && calloc_dev(cl, &cl->host_out, (size_t)3 * P * 8) &&
          calloc_dev(cl, &cl->host_in, (size_t)6 * P * 8) && calloc_dev(cl, &cl->sscal, (size_t)(max_samples + 1) * 16);
     if (ok && max_samples > 0) ok = calloc_dev(cl, &cl->data, (size_t)max_samples * 9 * P * 4);
+    ok = ok && calloc_dev(cl, &cl->derr, 16);
+    if (ok && cl->tc_ok) {
+        ok = calloc_dev(cl, &cl->pa0, (size_t)2 * cl->RTOT * 16) &&
+             calloc_dev(cl, &cl->pact[0], (size_t)4 * cl->RTOT * 16) &&
+             calloc_dev(cl, &cl->pact[1], (size_t)4 * cl->RTOT * 16);
+        for (int l = 0; l < NL && ok; ++l) {
+            const int coutp = l == NL - 1 ? 16 : CPAD_OUT[l];
+            ok = calloc_dev(cl, &cl->imgtc[l], (size_t)NTAP * (CPAD_IN[l] / 8) * coutp * 16);
+        }
+    }
     if (!ok) {
         cudaGetLastError();
         ps3d_closure_destroy(cl);
@@ -1103,13 +1594,46 @@ int ps3d_closure_predict(ps3d_closure *cl, const double *vor, const double *vel,
     const double *dv = cl->host_in;
     k_sumsq<double><<<RED_BLOCKS, RED_THREADS, 0, cl->st>>>(dv, dv + 3 * P, P, cl->Z, cl->Z, P, cl->rpart);
     k_scal_finish<<<1, RED_THREADS, 0, cl->st>>>(cl->rpart, RED_BLOCKS, P, cl->ctd, cl->scal);
-    k_pack<double><<<RED_BLOCKS * 4, RED_THREADS, 0, cl->st>>>(dv, dv + 3 * P, P, cl->Z, cl->Z, P, cl->scal, cl->a0);
-    forward(cl, cl->st);
+    pack_forward<double>(cl, cl->st, dv, dv + 3 * P, P, cl->Z);
     k_unpack<double><<<RED_BLOCKS * 4, RED_THREADS, 0, cl->st>>>(cl->outf, cl->scal, dv, P, cl->Z, P, cl->Z, P, 0,
                                                                 cl->host_out);
     cudaMemcpyAsync(corr, cl->host_out, (size_t)3 * P * 8, cudaMemcpyDeviceToHost, cl->st);
     if (cudaStreamSynchronize(cl->st) != cudaSuccess) return ccheck(cl, "predict");
-    return ccheck(cl, "predict");
+    rc = ccheck(cl, "predict");
+    return rc ? rc : ps3d_closure_check(cl);
+}
+
+int ps3d_closure_set_engine(ps3d_closure *cl, int engine)
+{
+    if (!cl || (engine != PS3D_CLOSURE_ENGINE_MMA && engine != PS3D_CLOSURE_ENGINE_TCGEN05))
+        return PS3D_ERR_INVALID_ARG;
+    if (engine == PS3D_CLOSURE_ENGINE_TCGEN05 && !cl->tc_ok)
+        return cfail(cl, PS3D_ERR_UNSUPPORTED_SIZE, "tcgen05 tile does not fit shared memory at this nz");
+    cl->engine = engine;
+    return PS3D_OK;
+}
+
+int ps3d_closure_get_engine(ps3d_closure *cl, int *engine)
+{
+    if (!cl || !engine) return PS3D_ERR_INVALID_ARG;
+    *engine = cl->engine;
+    return PS3D_OK;
+}
+
+int ps3d_closure_check(ps3d_closure *cl)
+{
+    int rc = centre(cl);
+    if (rc) return rc;
+    int h = 0;
+    cudaStreamSynchronize(cl->st);
+    cudaMemcpy(&h, cl->derr, sizeof(int), cudaMemcpyDeviceToHost);
+    rc = ccheck(cl, "check");
+    if (rc) return rc;
+    if (h) {
+        cudaMemset(cl->derr, 0, sizeof(int));
+        return cfail(cl, PS3D_ERR_DEVICE_LIMIT, "tcgen05 convolution: a bounded wait ran out");
+    }
+    return PS3D_OK;
 }
 
 int ps3d_closure_time_forward(ps3d_closure *cl, int reps, double *ms)
@@ -1120,9 +1644,13 @@ int ps3d_closure_time_forward(ps3d_closure *cl, int reps, double *ms)
     cudaEvent_t e0, e1;
     cudaEventCreate(&e0);
     cudaEventCreate(&e1);
-    forward(cl, cl->st);  // warm-up
+    auto fwd = [cl]() {
+        if (cl->engine == 1) forward_tc(cl, cl->st);
+        else forward(cl, cl->st);
+    };
+    fwd();  // warm-up
     cudaEventRecord(e0, cl->st);
-    for (int i = 0; i < reps; ++i) forward(cl, cl->st);
+    for (int i = 0; i < reps; ++i) fwd();
     cudaEventRecord(e1, cl->st);
     cudaError_t e = cudaEventSynchronize(e1);
     float t = 0.f;
@@ -1131,7 +1659,8 @@ int ps3d_closure_time_forward(ps3d_closure *cl, int reps, double *ms)
     cudaEventDestroy(e1);
     if (e != cudaSuccess) return cfail(cl, PS3D_ERR_CUDA, std::string("time_forward: ") + cudaGetErrorString(e));
     *ms = (double)t / reps;
-    return ccheck(cl, "time_forward");
+    rc = ccheck(cl, "time_forward");
+    return rc ? rc : ps3d_closure_check(cl);
 }
 
 int ps3d_closure_gradients(ps3d_closure *cl, int sample, float *out, float *grad, double *loss)

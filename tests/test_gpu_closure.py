@@ -212,16 +212,21 @@ def test_clip_and_wall_options_shape_the_correction():
         m.vor2vel()
         m.source()
     vor = b.get("vor")
-    corr = cl.predict(vor, b.get("vel"))
+    raw = cl.predict(vor, b.get("vel"))
+    corr = raw.copy()
     corr[0:2, :, :, 0] = 0.0
     corr[0:2, :, :, -1] = 0.0
-    corr[:, np.sum(vor * corr, axis=0) > 0.0] = 0.0
-    expect = np.stack([a.decompose_physical(corr[k]) for k in range(3)])
+    w = np.sum(vor * corr, axis=0)
+    # points whose vor . corr lies within rounding of zero may fall either way
+    ambiguous = np.abs(w) <= 1e-9 * np.sqrt(np.sum(vor * vor, axis=0) * np.sum(corr * corr, axis=0))
+    corr[:, w > 0.0] = 0.0
     diff = b.get("svorts") - a.get("svorts")
-    err = np.linalg.norm(diff - expect) / np.linalg.norm(expect)
-    # the sign test runs in FP32 on the device: points with vor . corr
-    # within rounding of zero may fall either way
-    assert err < 1e-3, err
+    added = np.stack([a.combine_physical(diff[k]) for k in range(3)])  # the correction the run added
+    mism = np.max(np.abs(added - corr), axis=0) > 1e-8 * np.max(np.abs(raw))
+    bad = mism & ~ambiguous
+    assert not np.any(bad), (int(bad.sum()), int(mism.sum()), int(ambiguous.sum()))
+    assert np.all(np.abs(added[0:2, :, :, 0]) < 1e-8 * np.max(np.abs(raw)))
+    assert 0.1 < np.mean(w > 0.0) < 0.9  # the clip removed a part, not all
     attach(b, None)
     cl.close()
 
@@ -283,3 +288,66 @@ def test_subgrid_sample_of_a_resolved_flow_is_small():
     coarse.vor2vel()
     assert np.allclose(coarse.get("vor"), vc)
     assert np.linalg.norm(tgt) < 0.1 * np.linalg.norm(vc) ** 2 / np.sqrt(vc[0].size)
+
+
+@pytest.mark.parametrize("dims", [(16, 16, 16), (32, 16, 32), (64, 64, 64)])
+def test_tcgen05_engine_matches_warp_engine_and_torch(dims):
+    nx, ny, nz = dims
+    shape = (nx, ny, nz + 1)
+    vor, vel, _ = random_fields(shape, 7)
+    cl = Closure(nx, ny, nz, seed=6)
+    p = boosted_params(cl)
+    cl.set_params(p)
+    cl.scale = 1.0
+    assert cl.engine == "tcgen05"  # the default where the grid allows it
+    cl.engine = "mma"
+    ref = cl.predict(vor, vel)
+    cl.engine = "tcgen05"
+    out = cl.predict(vor, vel)
+    cl.check()
+    err = np.linalg.norm(out - ref) / np.linalg.norm(ref)
+    assert err < TOL_EMU_OUT, err
+    w2 = float(np.sum(vor * vor)) / vor[0].size
+    r, _, _ = reference(p, vor, vel, emulate=True)
+    r = r[0].detach().numpy() * w2  # ct = 1: correction = output * <|vor|^2>
+    e = np.linalg.norm(out - r) / np.linalg.norm(r)
+    assert e < TOL_EMU_OUT, e
+    cl.close()
+
+
+def test_tcgen05_engine_in_a_run():
+    a, b = _pair(32, "fp64")
+    cl = Closure(32, 32, 32, seed=2)
+    cl.set_params(boosted_params(cl))
+    cl.scale = 0.05
+    cl.engine = "tcgen05"
+    attach(b, cl)
+    for m in (a, b):
+        m.vor2vel()
+        m.source()
+    cl.check()
+    corr = cl.predict(b.get("vor"), b.get("vel"))
+    expect = np.stack([a.decompose_physical(corr[k]) for k in range(3)])
+    diff = b.get("svorts") - a.get("svorts")
+    err = np.linalg.norm(diff - expect) / np.linalg.norm(expect)
+    assert err < 1e-10, err
+    attach(b, None)
+    # captured steps with the tcgen05 engine equal host-driven ones
+    c, d = _pair(32, "mixed")
+    cl2 = Closure(32, 32, 32, seed=9)
+    cl2.set_params(cl.get_params())
+    cl2.scale = 0.05
+    cl2.engine = "tcgen05"
+    cl.set_params(cl2.get_params())
+    attach(c, cl, every_stage=True)
+    attach(d, cl2, every_stage=True)
+    tc, _ = c.advance_n(0.0, 3)
+    td, _, _ = d.advance_graph(0.0, 3)
+    cl.check()
+    cl2.check()
+    assert tc == td
+    assert np.array_equal(c.get("svor"), d.get("svor"))
+    attach(c, None)
+    attach(d, None)
+    cl.close()
+    cl2.close()
