@@ -694,20 +694,18 @@ template <int KC>
 __device__ __forceinline__ void tc_store_point(unsigned char *base, long long RTOT, long long G, int ZP, int YP, int nx,
                                                int ny, int ix, int iy, int iz, const uint4 *v, int kc0 = 0)
 {
-    int xs[2], ys[2], nxs = 1, nys = 1;
-    xs[0] = ix + 1;
-    ys[0] = iy + 1;
-    if (ix == 0) xs[nxs++] = nx + 1;
-    else if (ix == nx - 1) xs[nxs++] = 0;
-    if (iy == 0) ys[nys++] = ny + 1;
-    else if (iy == ny - 1) ys[nys++] = 0;
-    for (int a = 0; a < nxs; ++a)
-        for (int b = 0; b < nys; ++b) {
-            const long long r = tc_row(G, ZP, YP, xs[a], ys[b], iz);
+    // the point itself, then its ghost copies (x edge, y edge, corner)
+    const int xg = ix == 0 ? nx + 1 : (ix == nx - 1 ? 0 : -1);
+    const int yg = iy == 0 ? ny + 1 : (iy == ny - 1 ? 0 : -1);
+    auto put = [&](int xp, int yp) {
+        const long long r = tc_row(G, ZP, YP, xp, yp, iz);
 #pragma unroll
-            for (int kc = 0; kc < KC; ++kc)
-                *reinterpret_cast<uint4 *>(base + ((long long)(kc0 + kc) * RTOT + r) * 16) = v[kc];
-        }
+        for (int kc = 0; kc < KC; ++kc) *reinterpret_cast<uint4 *>(base + ((long long)(kc0 + kc) * RTOT + r) * 16) = v[kc];
+    };
+    put(ix + 1, iy + 1);
+    if (xg >= 0) put(xg, iy + 1);
+    if (yg >= 0) put(ix + 1, yg);
+    if (xg >= 0 && yg >= 0) put(xg, yg);
 }
 
 // network input in the padded layout (channels 0-2 vor*scal[0], 3-5
@@ -792,147 +790,167 @@ __device__ __forceinline__ void tc_epilogue(const TcArgs &a, const float *bias, 
     }
 }
 
-// One convolution layer over the padded grid.  Persistent CTAs of 8 warps
-// walk tiles of 128 padded rows with a two-deep pipeline: thread 0 issues the
-// products of tile k into TMEM accumulator k%2; once the products of tile
-// k-1 are complete it starts the TMA copies of tile k+1 into the shared
-// buffer they used, and meanwhile all 256 threads read accumulator (k-1)%2
-// for the epilogue of tile k-1 (warp w: TMEM lanes 32(w%4).., column half
-// w/4).  Every wait is bounded; a wait that runs out raises the error word,
-// lets the operations in flight finish (bounded) and frees the accumulator.
+__device__ __forceinline__ void mbar_arrive(uint32_t a)
+{
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];\n" ::"r"(a) : "memory");
+}
+
+// One convolution layer over the padded grid, warp-specialised.  Persistent
+// CTAs of 9 warps walk tiles of 128 padded rows.  Warp 8 (one elected lane)
+// is the producer and issuer: TMA copies of tile k+1 into the shared buffer
+// freed by the products of tile k-1, and the 27 x CIN/16 tcgen05.mma of tile
+// k into TMEM accumulator k%2 once the epilogue has released it.  Warps 0-7
+// are the epilogue: they wait for the products of tile k, read their lane
+// quarter (warp % 4) and column half (warp / 4) of the accumulator, release
+// it, and apply bias + GELU and the stores.  The roles meet only on
+// mbarriers: full[b] (copies landed), done[b] (products complete, tcgen05.
+// commit), free[b] (256 epilogue arrivals).  Every wait is bounded; a wait
+// that runs out sets a shared flag that stops both roles, raises the error
+// word, and the issuer lets its operations in flight finish (bounded) before
+// the accumulator is released.
 template <int CIN, int COUT, int EPI>
-__global__ void __launch_bounds__(256, 1) k_conv_tc(TcArgs a)
+__global__ void __launch_bounds__(288, 1) k_conv_tc(TcArgs a)
 {
     constexpr int KC = CIN / 8, S = CIN / 16;
     constexpr int WB = tc_wbytes<CIN, COUT>();
     constexpr uint32_t IDESC = tc_idesc<COUT>();
     extern __shared__ __align__(1024) unsigned char smem[];
-    __shared__ __align__(8) uint64_t mbar[4];  // loads of buffers 0, 1; products into accumulators 0, 1
+    __shared__ __align__(8) uint64_t mbar[6];  // full[0..1], done[2..3], free[4..5]
     __shared__ uint32_t tmem_slot;
-    __shared__ int bad;
+    __shared__ volatile int bad;
     __shared__ float sbias[32];
     unsigned char *sW = smem;
     unsigned char *sA = smem + WB;
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const int ZP = a.ZP;
     const uint32_t segb = (uint32_t)tc_seg(ZP) * 16u;
-    if (tid < 32) sbias[tid] = tid < COUT ? a.bias[tid] : 0.f;
     const uint32_t abuf = (uint32_t)(3 * KC) * segb;
     const long long plane = (long long)ZP * a.YP;
 
+    if (tid < 32) sbias[tid] = tid < COUT ? a.bias[tid] : 0.f;
     if (tid == 0) {
         for (int i = 0; i < 4; ++i) mbar_init(smem_u32(&mbar[i]), 1);
+        mbar_init(smem_u32(&mbar[4]), 256);
+        mbar_init(smem_u32(&mbar[5]), 256);
         bad = 0;
         asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
     }
-    if (warp == 0) {
+    if (warp == 8) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 64;\n" ::"r"(smem_u32(&tmem_slot))
                      : "memory");
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n" ::: "memory");
     }
-    for (int i = tid; i < WB / 16; i += 256) reinterpret_cast<uint4 *>(sW)[i] = __ldg(a.wimg + i);
+    for (int i = tid; i < WB / 16; i += 288) reinterpret_cast<uint4 *>(sW)[i] = __ldg(a.wimg + i);
     asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
     tc_fence_before();
     __syncthreads();
     tc_fence_after();
     const uint32_t tmem = tmem_slot;
-    const uint32_t sAu = smem_u32(sA), sWu = smem_u32(sW);
-    uint32_t ph[4] = {0u, 0u, 0u, 0u};
-    bool pend[4] = {false, false, false, false};
     const long long ntiles = (a.QN + 127) / 128;
     const long long nk = ntiles > (long long)blockIdx.x ? (ntiles - 1 - blockIdx.x) / gridDim.x + 1 : 0;
     auto tile_q0 = [&](long long k) { return ((long long)blockIdx.x + k * (long long)gridDim.x) * 128; };
-    auto issue_load = [&](long long k) {
-        const int b = (int)(k & 1);
-        const uint32_t mb = smem_u32(&mbar[b]);
-        mbar_expect_tx(mb, abuf);
-        const long long q0 = tile_q0(k);
-        for (int dxi = 0; dxi < 3; ++dxi) {
-            const long long r0 = a.GUARD + q0 + (dxi - 1) * plane - (ZP + 1);
-            for (int kc = 0; kc < KC; ++kc)
-                bulk_g2s(sAu + (uint32_t)b * abuf + (uint32_t)(dxi * KC + kc) * segb,
-                         a.in + ((long long)kc * a.RTOT + r0) * 16, segb, mb);
-        }
-    };
-    auto wait_bar = [&](int i) {
-        if (mbar_wait(smem_u32(&mbar[i]), ph[i])) {
-            ph[i] ^= 1u;
-            pend[i] = false;
-        } else {
-            bad = 1;
-        }
-    };
-    auto epilogue = [&](long long k) {
-        const int b = (int)(k & 1), quarter = warp & 3, half = warp >> 2;
-        float v[16];
-        const uint32_t taddr = tmem + (uint32_t)(b * 32 + half * (COUT / 2)) + ((uint32_t)(quarter * 32) << 16);
-        if (COUT == 32) tc_ld16(taddr, v);
-        else tc_ld8(taddr, v);
-        tc_epilogue<COUT, EPI>(a, sbias, (unsigned)(tile_q0(k) + quarter * 32 + lane), half, v);
-    };
 
-    if (nk > 0) {
-        pend[0] = true;
-        if (tid == 0) issue_load(0);
-    }
-    for (long long k = 0; k < nk; ++k) {
-        const int b = (int)(k & 1);
-        wait_bar(b);  // tile k in shared memory
-        __syncthreads();
-        if (bad) break;
-        pend[2 + b] = true;
-        if (tid == 0) {
-            tc_fence_after();
-            const uint32_t acc = tmem + (uint32_t)(b * 32);
-            // descriptors = base descriptor + start offset in 16-byte units
-            // (the 14-bit start field cannot carry below 256 KB)
-            const uint64_t ad0 = tc_desc(sAu + (uint32_t)b * abuf, segb, 128u);
+    if (warp == 8) {
+        if (lane == 0) {
+            const uint32_t sAu = smem_u32(sA), sWu = smem_u32(sW);
             const uint64_t bd0 = tc_desc(sWu, COUT * 16u, 128u);
             const int seg = (int)(segb >> 4);
+            // phase parities and pending operations as bit masks (bit i:
+            // barrier i; pending bits 0-3: copies into buffer 0/1, products
+            // into accumulator 0/1), kept in registers
+            uint32_t ph = 0u, pend = 0u;
+            auto wait_bar = [&](int i) {
+                if (mbar_wait(smem_u32(&mbar[i]), (ph >> i) & 1u)) {
+                    ph ^= 1u << i;
+                    pend &= ~(1u << i);
+                    return true;
+                }
+                bad = 1;
+                return false;
+            };
+            auto issue_load = [&](long long k) {
+                const int b = (int)(k & 1);
+                const uint32_t mb = smem_u32(&mbar[b]);
+                pend |= 1u << b;
+                mbar_expect_tx(mb, abuf);
+                const long long q0 = tile_q0(k);
+                for (int dxi = 0; dxi < 3; ++dxi) {
+                    const long long r0 = a.GUARD + q0 + (dxi - 1) * plane - (ZP + 1);
+                    for (int kc = 0; kc < KC; ++kc)
+                        bulk_g2s(sAu + (uint32_t)b * abuf + (uint32_t)(dxi * KC + kc) * segb,
+                                 a.in + ((long long)kc * a.RTOT + r0) * 16, segb, mb);
+                }
+            };
+            if (nk > 0) issue_load(0);
+            for (long long k = 0; k < nk && !bad; ++k) {
+                const int b = (int)(k & 1);
+                if (!wait_bar(b)) break;                          // tile k in shared memory
+                if (k >= 2 && !wait_bar(4 + b)) break;            // epilogue of tile k-2 released accumulator b
+                tc_fence_after();
+                const uint32_t acc = tmem + (uint32_t)(b * 32);
+                // descriptors = base descriptor + start offset in 16-byte units
+                // (the 14-bit start field cannot carry below 256 KB)
+                const uint64_t ad0 = tc_desc(sAu + (uint32_t)b * abuf, segb, 128u);
 #pragma unroll
-            for (int dxi = 0; dxi < 3; ++dxi)
+                for (int dxi = 0; dxi < 3; ++dxi)
 #pragma unroll
-                for (int dyi = 0; dyi < 3; ++dyi)
+                    for (int dyi = 0; dyi < 3; ++dyi)
 #pragma unroll
-                    for (int dzi = 0; dzi < 3; ++dzi)
+                        for (int dzi = 0; dzi < 3; ++dzi)
 #pragma unroll
-                        for (int s2 = 0; s2 < S; ++s2) {
-                            const int tap = dxi * 9 + dyi * 3 + dzi;
-                            // row offset of the tap in the tile buffer, >= 0
-                            const int off = (dxi * KC + 2 * s2) * seg + (ZP + 1) + ZP * (dyi - 1) + (dzi - 1);
-                            const uint64_t ad = ad0 + (uint64_t)(uint32_t)off;
-                            const uint64_t bd = bd0 + (uint64_t)((tap * KC + 2 * s2) * COUT);
-                            tc_mma(acc, ad, bd, IDESC, (tap | s2) != 0 ? 1u : 0u);
-                        }
-            tc_commit(smem_u32(&mbar[2 + b]));
+                            for (int s2 = 0; s2 < S; ++s2) {
+                                const int tap = dxi * 9 + dyi * 3 + dzi;
+                                // row offset of the tap in the tile buffer, >= 0
+                                const int off = (dxi * KC + 2 * s2) * seg + (ZP + 1) + ZP * (dyi - 1) + (dzi - 1);
+                                const uint64_t ad = ad0 + (uint64_t)(uint32_t)off;
+                                const uint64_t bd = bd0 + (uint64_t)((tap * KC + 2 * s2) * COUT);
+                                tc_mma(acc, ad, bd, IDESC, (tap | s2) != 0 ? 1u : 0u);
+                            }
+                pend |= 1u << (2 + b);
+                tc_commit(smem_u32(&mbar[2 + b]));
+                if (k + 1 < nk) {
+                    // buffer 1-b is free once the products of tile k-1 are complete
+                    if (k >= 1 && !wait_bar(2 + (1 - b))) break;
+                    issue_load(k + 1);
+                }
+            }
+            if (bad) {
+                atomicOr(a.err, 1);
+                for (int i = 0; i < 4; ++i)
+                    if ((pend >> i) & 1u) mbar_wait(smem_u32(&mbar[i]), (ph >> i) & 1u);
+            } else if (nk > 0) {
+                // the last tile's products (the epilogue waits for them too)
+                const int b = (int)((nk - 1) & 1);
+                if ((pend >> (2 + b)) & 1u) wait_bar(2 + b);
+            }
         }
-        if (k >= 1) wait_bar(2 + (int)((k - 1) & 1));  // products of tile k-1 done: its buffer is free
-        if (k + 1 < nk) {
-            pend[(k + 1) & 1] = true;
-            if (tid == 0) issue_load(k + 1);
-        }
-        if (k >= 1) {
+    } else {
+        const int quarter = warp & 3, half = warp >> 2;
+        uint32_t ph_done = 0u;  // bit b: phase parity of done[b]
+        for (long long k = 0; k < nk; ++k) {
+            // warp-uniform decisions: the TMEM load below is warp-collective
+            if (__any_sync(0xffffffffu, bad != 0)) break;
+            const int b = (int)(k & 1);
+            const bool ok = mbar_wait(smem_u32(&mbar[2 + b]), (ph_done >> b) & 1u);
+            if (!__all_sync(0xffffffffu, ok)) {
+                bad = 1;
+                break;
+            }
+            ph_done ^= 1u << b;
             tc_fence_after();
-            epilogue(k - 1);
+            float v[16];
+            const uint32_t taddr = tmem + (uint32_t)(b * 32 + half * (COUT / 2)) + ((uint32_t)(quarter * 32) << 16);
+            if (COUT == 32) tc_ld16(taddr, v);
+            else tc_ld8(taddr, v);
+            tc_fence_before();
+            mbar_arrive(smem_u32(&mbar[4 + b]));  // accumulator b may take the products of tile k+2
+            tc_epilogue<COUT, EPI>(a, sbias, (unsigned)(tile_q0(k) + quarter * 32 + lane), half, v);
         }
-        tc_fence_before();
-        __syncthreads();
-        if (bad) break;
-    }
-    if (!bad && nk > 0) {  // uniform: read after a barrier
-        wait_bar(2 + (int)((nk - 1) & 1));
-        tc_fence_after();
-        epilogue(nk - 1);  // warp-collective TMEM load, whatever the wait gave
-    }
-    if (bad) {
-        if (tid == 0) atomicOr(a.err, 1);
-        for (int i = 0; i < 4; ++i)
-            if (pend[i]) mbar_wait(smem_u32(&mbar[i]), ph[i]);
     }
     tc_fence_before();
     __syncthreads();
     tc_fence_after();
-    if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 64;\n" ::"r"(tmem) : "memory");
+    if (warp == 8) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 64;\n" ::"r"(tmem) : "memory");
 }
 
 // host-side SplitMix64 (parameter initialisation, sample order)
@@ -1085,7 +1103,7 @@ template <int CIN, int COUT, int EPI> bool tc_attr(ps3d_closure *cl)
         return false;
     }
     int nb = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_conv_tc<CIN, COUT, EPI>, 256, sm) != cudaSuccess ||
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_conv_tc<CIN, COUT, EPI>, 288, sm) != cudaSuccess ||
         nb < 1) {
         cudaGetLastError();
         return false;
@@ -1100,7 +1118,7 @@ template <int CIN, int COUT, int EPI> void conv_tc(ps3d_closure *cl, cudaStream_
     const long long maxb = (long long)cl->nsm * cl->tc_occ[tc_slot<CIN, COUT, EPI>()];
     const long long per = (ntiles + maxb - 1) / maxb;
     const unsigned grid = (unsigned)((ntiles + per - 1) / per);
-    k_conv_tc<CIN, COUT, EPI><<<grid, 256, tc_smem<CIN, COUT>(cl->ZP), st>>>(a);
+    k_conv_tc<CIN, COUT, EPI><<<grid, 288, tc_smem<CIN, COUT>(cl->ZP), st>>>(a);
 }
 
 // tcgen05 forward pass: pa0 -> pact[0] -> pact[1] -> pact[0] -> outf
