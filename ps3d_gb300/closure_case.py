@@ -36,8 +36,8 @@ import numpy as np
 from . import Ps3dGpu, ic
 from .closure import Closure, attach, shell_error, spectral_cut, subgrid_sample
 
-DEFAULT_VARIANTS = ("plain=30,nomodel0=0,net0=0:net,net0_clip=0:net+clip+walls,"
-                    "net10_clip=10:net+clip+walls,net30_clip=30:net+clip+walls,net0_clip_every=0:net+clip+walls+every")
+DEFAULT_VARIANTS = ("plain=30,net30_every=30:net+every,net10_every=10:net+every,net30_held=30:net,"
+                    "net30_clip=30:net+clip+walls,net0_every=0:net+every,nomodel0=0")
 
 PHYS = dict(prediss=30.0, nnu=3, pretype="vorch", length_scale="Kolmogorov", filtering="Hou & Li", cflmax=0.5)
 
@@ -112,7 +112,8 @@ def main(argv=None):
     ap.add_argument("--lr-final", type=float, default=5e-5)
     ap.add_argument("--variants", default=DEFAULT_VARIANTS,
                     help="coarse runs: name=prediss[:option+option...], options net, every, clip, walls, "
-                         "g<gain> (the correction times gain); the first variant with net is timed")
+                         "g<gain> (the correction times gain), mma (warp-level inference engine instead of "
+                         "tcgen05); the first variant with net is timed")
     ap.add_argument("--fp64-cost", action="store_true")
     ap.add_argument("--params-out", default="", help="save the trained network (.npz: params, ct)")
     ap.add_argument("--params-in", default="", help="load a trained network instead of generating data")
@@ -164,6 +165,7 @@ def main(argv=None):
     # --closure-prediss value, and the same without the network
     probe = model(nc, "mixed")
     ct0 = net.scale
+    engine0 = net.engine
     variants = []
     for item in a.variants.split(","):
         name, spec = item.split("=")
@@ -217,6 +219,7 @@ def main(argv=None):
             gain = [float(o[1:]) for o in opts if o.startswith("g")]
             if use_net:
                 net.scale = ct0 * (gain[0] if gain else 1.0)
+                net.engine = "mma" if "mma" in opts else engine0
                 attach(m, net, "every" in opts, "clip" in opts, "walls" in opts)
             try:
                 sp = coarse_spectra(m, times[-1])
@@ -238,6 +241,7 @@ def main(argv=None):
                 f"{errs[-1][0]:.4f} / {errs[-1][1]:.4f} in {len(sp) - 1} steps")
         evals.append(res)
     net.scale = ct0
+    net.engine = engine0
 
     # ---------------------------------------------------------------- cost
     f = fine_run(nf, 900, a.amplitude, "mixed")
