@@ -91,6 +91,16 @@ def at_time(series, t):
     return (1 - w) * a[:k] + w * b[:k]
 
 
+def parse_variants(spec):
+    """'name=prediss[:opt+opt...],...' -> [(name, prediss, {opts})]"""
+    out = []
+    for item in spec.split(","):
+        name, rest = item.split("=")
+        pd, _, opts = rest.partition(":")
+        out.append((name.strip(), float(pd), set(o for o in opts.split("+") if o)))
+    return out
+
+
 def cost_per_time(m, t0, nsteps):
     """(device ms per step, mean dt) of nsteps captured steps"""
     t1, _, ms = m.advance_graph(t0, nsteps)
@@ -166,12 +176,7 @@ def main(argv=None):
     probe = model(nc, "mixed")
     ct0 = net.scale
     engine0 = net.engine
-    variants = []
-    for item in a.variants.split(","):
-        name, spec = item.split("=")
-        pd, _, opts = spec.partition(":")
-        opts = set(o for o in opts.split("+") if o)
-        variants.append((name, float(pd), opts))
+    variants = parse_variants(a.variants)
     evals = []
     cache = {}
     if a.truth_cache and os.path.exists(a.truth_cache):

@@ -70,3 +70,27 @@ def test_parameter_layout():
     views = closure.param_views(p)
     assert [w.shape for w, _ in views] == [(27, 6, 32), (27, 32, 32), (27, 32, 32), (27, 32, 3)]
     assert views[-1][1][-1] == closure.NPARAM - 1
+
+
+def test_spectrum_interpolation_and_shell_error():
+    from ps3d_gb300 import closure_case as cc
+    k = np.arange(30, dtype=float)
+    series = [(0.0, 1.0 + k), (0.5, 3.0 + k), (1.5, 5.0 + k)]
+    assert np.allclose(cc.at_time(series, 0.25), 2.0 + k)
+    assert np.allclose(cc.at_time(series, 1.0), 4.0 + k)
+    assert np.allclose(cc.at_time(series, -1.0), 1.0 + k)   # before the first sample
+    assert np.allclose(cc.at_time(series, 9.0), 5.0 + k)    # after the last
+    truth = 1.0 + k
+    model = truth.copy()
+    model[3] *= 1.5
+    model[21] *= 0.9
+    model[25] *= 10.0                                        # beyond shell 21: ignored
+    mx, mean = closure.shell_error(model, truth, kmax=21)
+    assert abs(mx - 0.5) < 1e-12 and abs(mean - 0.6 / 21) < 1e-12
+
+
+def test_variant_parsing():
+    from ps3d_gb300 import closure_case as cc
+    v = cc.parse_variants("plain=30,net=10:net+every+g0.5,m=0:net+mma")
+    assert v == [("plain", 30.0, set()), ("net", 10.0, {"net", "every", "g0.5"}), ("m", 0.0, {"net", "mma"})]
+    assert [x[0] for x in cc.parse_variants(cc.DEFAULT_VARIANTS)][0] == "plain"
