@@ -6,8 +6,9 @@ carry a small convolution network (libps3d_gpu.so, closure.cu) that adds a
 vorticity-tendency correction to svorts at each advance; with no network
 attached the run is the plain hyperdiffusive method.
 
-Training data come from fine runs of the plain method: at a fine state
-omega_f, the target is the exact sub-grid tendency
+Training data come from fine runs (FP64 or the mixed form, which stays
+within 1e-6 of it): at a fine state omega_f, the target is the exact
+sub-grid tendency
 
     target = cut(T_f(omega_f)) - T_c(cut(omega_f))
 
@@ -236,7 +237,7 @@ def spectral_cut(f, nxc, nyc, nzc):
     return out
 
 
-def subgrid_sample(fine, coarse, closure_free=True):
+def subgrid_sample(fine, coarse):
     """(vor_c, vel_c, target) at the fine model's current state.
 
     fine, coarse: Ps3dGpu models on the same box; the coarse model must have
