@@ -36,6 +36,7 @@ EXPORTS = [
     "ps3d_closure_set_scale", "ps3d_closure_add_sample", "ps3d_closure_num_samples",
     "ps3d_closure_train", "ps3d_closure_predict", "ps3d_closure_gradients", "ps3d_gpu_set_closure",
     "ps3d_closure_time_forward", "ps3d_closure_set_engine", "ps3d_closure_get_engine", "ps3d_closure_check",
+    "ps3d_gpu_save_state", "ps3d_gpu_load_state",
 ]
 
 
@@ -158,5 +159,7 @@ def lib(build_if_missing=True):
     L.ps3d_closure_set_engine.argtypes = [_vp, ctypes.c_int]
     L.ps3d_closure_get_engine.argtypes = [_vp, ctypes.POINTER(ctypes.c_int)]
     L.ps3d_closure_check.argtypes = [_vp]
+    L.ps3d_gpu_save_state.argtypes = [_vp, ctypes.c_char_p, ctypes.c_double]
+    L.ps3d_gpu_load_state.argtypes = [_vp, ctypes.c_char_p, _dp]
     _LIB = L
     return L

@@ -2360,3 +2360,191 @@ int ps3d_gpu_synchronize(ps3d_gpu_ctx *c)
 }
 
 }  // extern "C"
+
+// ------------------------------------------------------------ checkpoint
+// Raw-binary checkpoint of everything a run carries from one step to the
+// next: the prognostic state (FP64, and in the mixed form its FP32 copy), the
+// buoyancy state, the rolling means of adapt, the initial mean vorticity, the
+// viscosities and hyperdiffusion tables, N^2 and the model time.  Restored
+// without re-projection; the continuation agrees with an uninterrupted run to
+// rounding level (the line transforms pair the top z row with a padding row
+// of a transient buffer, whose leftover content enters that row's last bit;
+// a fresh context's padding is zero).  The reference restarts
+// from the physical vorticity of a NetCDF field file (utils.f90:102-116);
+// its rolling means start afresh, so its restarts are not bit-continuous.
+
+namespace {
+
+struct CkptHeader {
+    char magic[8];
+    int32_t version, nx, ny, nz, precision, buoyancy, nnu, roll_len, rollb_len, diffusion_ready;
+    int32_t roll_inew, roll_iold, roll_filled, rollb_inew, rollb_iold, rollb_filled;
+    double t, lower[3], extent[3], ini_vor_mean[2], vvisc, bvisc, bfsq, roll_sma, rollb_sma;
+};
+constexpr char CKPT_MAGIC[8] = {'P', 'S', '3', 'D', 'G', 'P', 'U', 'S'};
+constexpr int32_t CKPT_VERSION = 1;
+
+// raw FP32 fields between device (P-pitched) and host ((nz+1)-pitched)
+int f32_transfer(ps3d_gpu_ctx *c, float *dev, float *host, int ncomp, bool to_host)
+{
+    const Dims &d = c->d;
+    const size_t hp = (size_t)(d.nz + 1) * sizeof(float);
+    for (int k = 0; k < ncomp; ++k) {
+        float *dk = dev + (size_t)k * d.nfield;
+        float *hk = host + (size_t)k * (d.nz + 1) * d.ncol;
+        const cudaError_t e =
+            to_host ? cudaMemcpy2DAsync(hk, hp, dk, d.P * sizeof(float), hp, d.ncol, cudaMemcpyDeviceToHost, c->st)
+                    : cudaMemcpy2DAsync(dk, d.P * sizeof(float), hk, hp, hp, d.ncol, cudaMemcpyHostToDevice, c->st);
+        if (e != cudaSuccess) return check(c, "checkpoint transfer");
+    }
+    return sync_check(c, "checkpoint transfer");
+}
+
+struct File {
+    FILE *f = nullptr;
+    ~File()
+    {
+        if (f) fclose(f);
+    }
+};
+
+}  // namespace
+
+extern "C" {
+
+int ps3d_gpu_save_state(ps3d_gpu_ctx *c, const char *path, double t)
+{
+    int rc = enter(c);
+    if (rc) return rc;
+    if (!path) return PS3D_ERR_INVALID_ARG;
+    const Dims &d = c->d;
+    const size_t n1 = (size_t)(d.nz + 1) * d.ncol;
+    CkptHeader h{};
+    memcpy(h.magic, CKPT_MAGIC, 8);
+    h.version = CKPT_VERSION;
+    h.nx = d.nx;
+    h.ny = d.ny;
+    h.nz = d.nz;
+    h.precision = c->cfg.precision;
+    h.buoyancy = c->cfg.buoyancy ? 1 : 0;
+    h.nnu = c->cfg.nnu;
+    h.roll_len = (int32_t)c->roll.hist.size();
+    h.rollb_len = (int32_t)c->roll_b.hist.size();
+    h.diffusion_ready = c->diffusion_ready ? 1 : 0;
+    h.roll_inew = c->roll.inew;
+    h.roll_iold = c->roll.iold;
+    h.roll_filled = c->roll.filled ? 1 : 0;
+    h.rollb_inew = c->roll_b.inew;
+    h.rollb_iold = c->roll_b.iold;
+    h.rollb_filled = c->roll_b.filled ? 1 : 0;
+    h.t = t;
+    for (int k = 0; k < 3; ++k) {
+        h.lower[k] = c->cfg.lower[k];
+        h.extent[k] = c->cfg.extent[k];
+    }
+    h.ini_vor_mean[0] = c->ini_vor_mean[0];
+    h.ini_vor_mean[1] = c->ini_vor_mean[1];
+    h.vvisc = c->vvisc;
+    h.bvisc = c->bvisc;
+    h.bfsq = c->bfsq;
+    h.roll_sma = c->roll.sma;
+    h.rollb_sma = c->roll_b.sma;
+    std::vector<double> vh(d.ncol, 0.0), bh(c->cfg.buoyancy ? d.ncol : 0, 0.0), sv(3 * n1), sb(c->cfg.buoyancy ? n1 : 0);
+    std::vector<float> sv32(c->fp64 ? 0 : 3 * n1), sb32((!c->fp64 && c->cfg.buoyancy) ? n1 : 0);
+    cudaMemcpyAsync(vh.data(), c->vhdis, d.ncol * sizeof(double), cudaMemcpyDeviceToHost, c->st);
+    if (c->cfg.buoyancy) cudaMemcpyAsync(bh.data(), c->bhdis, d.ncol * sizeof(double), cudaMemcpyDeviceToHost, c->st);
+    rc = download(c, c->svor, true, 3, sv.data());
+    if (!rc && c->cfg.buoyancy) rc = download(c, c->sbuoy, true, 1, sb.data());
+    if (!rc && !c->fp64) rc = f32_transfer(c, c->svor32, sv32.data(), 3, true);
+    if (!rc && !c->fp64 && c->cfg.buoyancy) rc = f32_transfer(c, c->sbuoy32, sb32.data(), 1, true);
+    if (!rc) rc = sync_check(c, "save_state");
+    if (rc) return rc;
+    File fh;
+    fh.f = fopen(path, "wb");
+    if (!fh.f) return fail(c, PS3D_ERR_INVALID_ARG, std::string("save_state: cannot open ") + path);
+    bool ok = fwrite(&h, sizeof(h), 1, fh.f) == 1;
+    auto put = [&](const void *p, size_t bytes) {
+        if (ok && bytes) ok = fwrite(p, 1, bytes, fh.f) == bytes;
+    };
+    put(c->roll.hist.data(), c->roll.hist.size() * sizeof(double));
+    put(c->roll_b.hist.data(), c->roll_b.hist.size() * sizeof(double));
+    put(vh.data(), vh.size() * sizeof(double));
+    put(bh.data(), bh.size() * sizeof(double));
+    put(sv.data(), sv.size() * sizeof(double));
+    put(sb.data(), sb.size() * sizeof(double));
+    put(sv32.data(), sv32.size() * sizeof(float));
+    put(sb32.data(), sb32.size() * sizeof(float));
+    if (!ok) return fail(c, PS3D_ERR_INVALID_ARG, std::string("save_state: write failed for ") + path);
+    return PS3D_OK;
+}
+
+int ps3d_gpu_load_state(ps3d_gpu_ctx *c, const char *path, double *t)
+{
+    int rc = enter(c);
+    if (rc) return rc;
+    if (!path || !t) return PS3D_ERR_INVALID_ARG;
+    const Dims &d = c->d;
+    const size_t n1 = (size_t)(d.nz + 1) * d.ncol;
+    File fh;
+    fh.f = fopen(path, "rb");
+    if (!fh.f) return fail(c, PS3D_ERR_INVALID_ARG, std::string("load_state: cannot open ") + path);
+    CkptHeader h{};
+    if (fread(&h, sizeof(h), 1, fh.f) != 1 || memcmp(h.magic, CKPT_MAGIC, 8) != 0 || h.version != CKPT_VERSION)
+        return fail(c, PS3D_ERR_INVALID_ARG, "load_state: not a checkpoint of this library version");
+    bool same_box = true;
+    for (int k = 0; k < 3; ++k)
+        same_box = same_box && h.lower[k] == c->cfg.lower[k] && h.extent[k] == c->cfg.extent[k];
+    if (h.nx != d.nx || h.ny != d.ny || h.nz != d.nz || h.precision != c->cfg.precision ||
+        h.buoyancy != (c->cfg.buoyancy ? 1 : 0) || h.nnu != c->cfg.nnu || !same_box ||
+        h.roll_len != (int32_t)c->roll.hist.size() || h.rollb_len != (int32_t)c->roll_b.hist.size())
+        return fail(c, PS3D_ERR_INVALID_ARG, "load_state: checkpoint of another grid, box, form or configuration");
+    std::vector<double> rh(h.roll_len), rbh(h.rollb_len), vh(d.ncol), bh(h.buoyancy ? d.ncol : 0), sv(3 * n1),
+        sb(h.buoyancy ? n1 : 0);
+    std::vector<float> sv32(c->fp64 ? 0 : 3 * n1), sb32((!c->fp64 && h.buoyancy) ? n1 : 0);
+    bool ok = true;
+    auto get = [&](void *p, size_t bytes) {
+        if (ok && bytes) ok = fread(p, 1, bytes, fh.f) == bytes;
+    };
+    get(rh.data(), rh.size() * sizeof(double));
+    get(rbh.data(), rbh.size() * sizeof(double));
+    get(vh.data(), vh.size() * sizeof(double));
+    get(bh.data(), bh.size() * sizeof(double));
+    get(sv.data(), sv.size() * sizeof(double));
+    get(sb.data(), sb.size() * sizeof(double));
+    get(sv32.data(), sv32.size() * sizeof(float));
+    get(sb32.data(), sb32.size() * sizeof(float));
+    if (!ok) return fail(c, PS3D_ERR_INVALID_ARG, "load_state: truncated checkpoint");
+    // the state as saved: no projection, the FP32 copies verbatim
+    rc = upload(c, sv.data(), 3, c->svor, true);
+    if (!rc && !c->fp64) rc = f32_transfer(c, c->svor32, sv32.data(), 3, false);
+    if (!rc && h.buoyancy) rc = upload(c, sb.data(), 1, c->sbuoy, true);
+    if (!rc && h.buoyancy && !c->fp64) rc = f32_transfer(c, c->sbuoy32, sb32.data(), 1, false);
+    if (rc) return rc;
+    cudaMemcpyAsync(c->vhdis, vh.data(), d.ncol * sizeof(double), cudaMemcpyHostToDevice, c->st);
+    if (h.buoyancy) {
+        cudaMemcpyAsync(c->bhdis, bh.data(), d.ncol * sizeof(double), cudaMemcpyHostToDevice, c->st);
+        c->bfsq = h.bfsq;
+        for (int iz = 0; iz <= d.nz; ++iz) c->h_bbarz[iz] = c->bfsq * (c->cfg.lower[2] + (double)iz * c->dx[2]);
+        cudaMemcpyAsync(c->bprof, c->h_bbarz.data(), (d.nz + 1) * sizeof(double), cudaMemcpyHostToDevice, c->st);
+    }
+    c->vvisc = h.vvisc;
+    c->bvisc = h.bvisc;
+    c->diffusion_ready = h.diffusion_ready != 0;
+    c->roll.hist = rh;
+    c->roll.inew = h.roll_inew;
+    c->roll.iold = h.roll_iold;
+    c->roll.filled = h.roll_filled != 0;
+    c->roll.sma = h.roll_sma;
+    c->roll_b.hist = rbh;
+    c->roll_b.inew = h.rollb_inew;
+    c->roll_b.iold = h.rollb_iold;
+    c->roll_b.filled = h.rollb_filled != 0;
+    c->roll_b.sma = h.rollb_sma;
+    c->closure_fresh = true;
+    *t = h.t;
+    rc = sync_check(c, "load_state");
+    if (rc) return rc;
+    return ps3d_gpu_set_ini_vor_mean(c, h.ini_vor_mean);
+}
+
+}  // extern "C"

@@ -333,6 +333,16 @@ class Ps3dGpu:
         self._chk(self.L.ps3d_gpu_probe_result(self._h, ctypes.byref(ms), ctypes.byref(n), ctypes.byref(b)))
         return ms.value, n.value, b.value
 
+    def save_state(self, path, t):
+        """Checkpoint the run state at model time t (ps3d_gpu_save_state)."""
+        self._chk(self.L.ps3d_gpu_save_state(self._h, str(path).encode(), float(t)))
+
+    def load_state(self, path):
+        """Restore a checkpoint of this configuration; returns its model time."""
+        t = ctypes.c_double()
+        self._chk(self.L.ps3d_gpu_load_state(self._h, str(path).encode(), ctypes.byref(t)))
+        return t.value
+
     def synchronize(self):
         self._chk(self.L.ps3d_gpu_synchronize(self._h))
 
