@@ -64,3 +64,23 @@ def test_null_context_is_an_error_not_a_crash():
     L = _lib.lib()
     assert L.ps3d_gpu_vor2vel(None) == 1
     assert L.ps3d_gpu_destroy(None) == 0
+
+
+def test_closure_and_checkpoint_entry_points_validate_on_the_host():
+    L = _lib.lib()
+    h = ctypes.c_void_p()
+    # sizes are checked before any device call
+    assert L.ps3d_closure_create(12, 16, 16, 0, 0, 0, ctypes.byref(h)) == 2
+    assert L.ps3d_closure_create(16, 16, 16, -1, 0, 0, ctypes.byref(h)) in (1, 8)
+    assert L.ps3d_closure_create(16, 16, 16, 0, 0, 0, None) == 1
+    assert not h.value
+    assert L.ps3d_closure_destroy(None) == 0
+    assert L.ps3d_closure_set_scale(None, 1.0) == 1
+    assert L.ps3d_closure_get_scale(None, None) == 1
+    assert L.ps3d_closure_set_engine(None, 1) == 1
+    assert L.ps3d_closure_num_samples(None, None) == 1
+    assert L.ps3d_closure_last_error(None) == b""
+    t = ctypes.c_double()
+    assert L.ps3d_gpu_save_state(None, b"x", 0.0) == 1
+    assert L.ps3d_gpu_load_state(None, b"x", ctypes.byref(t)) == 1
+    assert L.ps3d_gpu_set_closure(None, None, 0) == 1
