@@ -306,11 +306,8 @@ int ps3d_gpu_energy_series_noalloc(const double *vel, const double *vor, int nx,
  * Raw-binary checkpoint of a context's run state: svor (FP64, and the FP32
  * copy of the mixed form), sbuoy, the rolling means of adapt, ini_vor_mean,
  * the viscosities and hyperdiffusion tables, N^2 and the model time t.  A
- * context of the same grid, box, form and configuration that loads it holds
- * the saved state bitwise and continues the run to rounding level: the line
- * transforms pair the top z row with a padding row of their (transient)
- * input, whose leftover content enters that row's last bit.  Replaces, for
- * the GPU state, the reference's
+ * context of the same grid, box, form and configuration that loads it
+ * continues the run bitwise.  Replaces, for the GPU state, the reference's
  * restart from a NetCDF field file (utils.f90:102-116, field_netcdf.f90:
  * 276-300), which starts its rolling means afresh.  Errors: PS3D_ERR_INVALID_ARG
  * for an unreadable, truncated or mismatched file (see last_error). */

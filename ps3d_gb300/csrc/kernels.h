@@ -70,7 +70,8 @@ bool lines32_supported(int n);
 void lines32_init();
 // shape: -1 default, 0 512-thread blocks (two per SM), 1 256-thread blocks
 // (three per SM); the two differ only at n = 512
-void launch_lines32(cudaStream_t st, const float *in, float *out, int n, int P, long long line_stride,
+// zv = nz+1 valid z rows; rows zv..P-1 (padding) are read as zero
+void launch_lines32(cudaStream_t st, const float *in, float *out, int n, int P, int zv, long long line_stride,
                     long long nbatch, long long batch_stride, bool inverse, const float2 *tw, int shape = -1);
 // number of block shapes the autotuner can choose from at line length n
 int lines32_shapes(int n);

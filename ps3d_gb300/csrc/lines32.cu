@@ -52,7 +52,8 @@ template <int R, bool INV> __device__ __forceinline__ void dftR(float2 *v) { dft
 // applies it to its two lanes
 template <int N, int R, int NS, bool INV, int W, bool FROM_GLOBAL, bool TO_GLOBAL>
 __device__ __forceinline__ void pass(float4 *sm, const float4 *__restrict__ gin, float4 *__restrict__ gout,
-                                     long long gstride, bool valid, float scale, const float2 *__restrict__ tw)
+                                     long long gstride, bool valid, float scale, const float2 *__restrict__ tw,
+                                     int nval = 4)
 {
     constexpr int G = LinePlan<N, INV, W>::G;
     constexpr int NB = N / R;              // butterflies per lane
@@ -67,8 +68,19 @@ __device__ __forceinline__ void pass(float4 *sm, const float4 *__restrict__ gin,
             for (int r = 0; r < R; ++r) {
                 const int row = j + r * NB;
                 float4 x;
-                if (FROM_GLOBAL) x = valid ? gin[row * gstride] : make_float4(0.f, 0.f, 0.f, 0.f);
-                else x = sm[row * PAIRS + p];
+                if (FROM_GLOBAL) {
+                    x = valid ? gin[row * gstride] : make_float4(0.f, 0.f, 0.f, 0.f);
+                    // z rows beyond the top wall (padding) enter as zero: the
+                    // paired real line must not pick up leftover content
+                    if (nval < 4) {
+                        x.w = 0.f;
+                        if (nval < 3) x.z = 0.f;
+                        if (nval < 2) x.y = 0.f;
+                        if (nval < 1) x.x = 0.f;
+                    }
+                } else {
+                    x = sm[row * PAIRS + p];
+                }
                 va[q][r] = lo2(x);
                 vb[q][r] = hi2(x);
             }
@@ -120,7 +132,7 @@ __device__ __forceinline__ float2 herm_high(float2 lo, float2 hi) { return make_
 // both C_k and C_{N-k}.  Items: slots x 16 lanes over the block's threads.
 template <int N, int W>
 __device__ __forceinline__ void herm_first_pass(float2 *sm2, const float2 *__restrict__ gin2, long long gs2,
-                                                int z0, int P)
+                                                int z0, int P, int zv)
 {
     constexpr int T = LinePlan<N, true, W>::T, NB = N / 8, SLOTS = NB / 2;
     constexpr int ITEMS = SLOTS * LANES, IPT = (ITEMS + T - 1) / T;
@@ -137,6 +149,19 @@ __device__ __forceinline__ void herm_first_pass(float2 *sm2, const float2 *__res
         for (int r = 0; r < 8; ++r) {
             h1[r] = valid ? g[(j1 + r * NB) * gs2] : make_float2(0.f, 0.f);
             h2[r] = valid ? g[(j2 + r * NB) * gs2] : make_float2(0.f, 0.f);
+        }
+        // padding rows (z >= zv) enter as zero
+        const int nv = zv - (z0 + 2 * lane);
+        if (nv < 2) {
+#pragma unroll
+            for (int r = 0; r < 8; ++r) {
+                h1[r].y = 0.f;
+                h2[r].y = 0.f;
+                if (nv < 1) {
+                    h1[r].x = 0.f;
+                    h2[r].x = 0.f;
+                }
+            }
         }
         float2 a[8], b[8];
         if (s == 0) {
@@ -201,7 +226,7 @@ __device__ __forceinline__ void later_passes(float4 *sm, float4 *gout, long long
 
 template <int N, bool INV, int W>
 __global__ void __launch_bounds__(LinePlan<N, INV, W>::T, LinePlan<N, INV, W>::MINB)
-    k_lines32(const float *__restrict__ in, float *__restrict__ out, int P, long long line_stride,
+    k_lines32(const float *__restrict__ in, float *__restrict__ out, int P, int zv, long long line_stride,
               long long batch_stride, const float2 *__restrict__ tw)
 {
     extern __shared__ __align__(16) float4 smL[];
@@ -215,7 +240,7 @@ __global__ void __launch_bounds__(LinePlan<N, INV, W>::T, LinePlan<N, INV, W>::M
     if (!INV) {
         const long long gs = line_stride >> 2;  // float4 units
         const float4 *gin = reinterpret_cast<const float4 *>(in + base) + p;
-        pass<N, 8, 1, false, W, true, false>(smL, gin, nullptr, gs, valid, 1.0f, tw);
+        pass<N, 8, 1, false, W, true, false>(smL, gin, nullptr, gs, valid, 1.0f, tw, zv - (z0 + 4 * p));
         later_passes<N, false, W, false>(smL, nullptr, gs, valid, 1.0f, tw);
         // split the two packed real transforms of each lane and store the
         // Hermitian rows k and N - k
@@ -235,7 +260,7 @@ __global__ void __launch_bounds__(LinePlan<N, INV, W>::T, LinePlan<N, INV, W>::M
         }
     } else {
         herm_first_pass<N, W>(reinterpret_cast<float2 *>(smL), reinterpret_cast<const float2 *>(in + base),
-                              line_stride >> 1, z0, P);
+                              line_stride >> 1, z0, P, zv);
         const long long gs = line_stride >> 2;
         float4 *gout = reinterpret_cast<float4 *>(out + base) + p;
         later_passes<N, true, W, true>(smL, gout, gs, valid, s, tw);
@@ -243,31 +268,31 @@ __global__ void __launch_bounds__(LinePlan<N, INV, W>::T, LinePlan<N, INV, W>::M
 }
 
 template <int N, bool INV, int W>
-void launch32w(cudaStream_t st, const float *in, float *out, int P, long long ls, long long nbatch, long long bs,
-               const float2 *tw)
+void launch32w(cudaStream_t st, const float *in, float *out, int P, int zv, long long ls, long long nbatch,
+               long long bs, const float2 *tw)
 {
     dim3 grid((P + 2 * LANES - 1) / (2 * LANES), (unsigned)nbatch);
     const size_t sm = (size_t)N * LANES * sizeof(float2);
-    k_lines32<N, INV, W><<<grid, LinePlan<N, INV, W>::T, sm, st>>>(in, out, P, ls, bs, tw);
+    k_lines32<N, INV, W><<<grid, LinePlan<N, INV, W>::T, sm, st>>>(in, out, P, zv, ls, bs, tw);
 }
 
 template <int N>
-void launch32(cudaStream_t st, const float *in, float *out, int P, long long ls, long long nbatch, long long bs,
-              bool inverse, const float2 *tw, int shape)
+void launch32(cudaStream_t st, const float *in, float *out, int P, int zv, long long ls, long long nbatch,
+              long long bs, bool inverse, const float2 *tw, int shape)
 {
     if (N == 512) {
         const int w = shape < 0 ? (inverse ? 1 : 0) : shape;
         if (inverse) {
-            if (w) launch32w<N, true, 1>(st, in, out, P, ls, nbatch, bs, tw);
-            else launch32w<N, true, 0>(st, in, out, P, ls, nbatch, bs, tw);
+            if (w) launch32w<N, true, 1>(st, in, out, P, zv, ls, nbatch, bs, tw);
+            else launch32w<N, true, 0>(st, in, out, P, zv, ls, nbatch, bs, tw);
         } else {
-            if (w) launch32w<N, false, 1>(st, in, out, P, ls, nbatch, bs, tw);
-            else launch32w<N, false, 0>(st, in, out, P, ls, nbatch, bs, tw);
+            if (w) launch32w<N, false, 1>(st, in, out, P, zv, ls, nbatch, bs, tw);
+            else launch32w<N, false, 0>(st, in, out, P, zv, ls, nbatch, bs, tw);
         }
         return;
     }
-    if (inverse) launch32w<N, true, 0>(st, in, out, P, ls, nbatch, bs, tw);
-    else launch32w<N, false, 0>(st, in, out, P, ls, nbatch, bs, tw);
+    if (inverse) launch32w<N, true, 0>(st, in, out, P, zv, ls, nbatch, bs, tw);
+    else launch32w<N, false, 0>(st, in, out, P, zv, ls, nbatch, bs, tw);
 }
 
 }  // namespace
@@ -286,15 +311,15 @@ void lines32_init()
 
 int lines32_shapes(int n) { return n == 512 ? 2 : 1; }
 
-void launch_lines32(cudaStream_t st, const float *in, float *out, int n, int P, long long line_stride,
+void launch_lines32(cudaStream_t st, const float *in, float *out, int n, int P, int zv, long long line_stride,
                     long long nbatch, long long batch_stride, bool inverse, const float2 *tw, int shape)
 {
     switch (n) {
-    case 64: launch32<64>(st, in, out, P, line_stride, nbatch, batch_stride, inverse, tw, shape); break;
-    case 128: launch32<128>(st, in, out, P, line_stride, nbatch, batch_stride, inverse, tw, shape); break;
-    case 256: launch32<256>(st, in, out, P, line_stride, nbatch, batch_stride, inverse, tw, shape); break;
-    case 512: launch32<512>(st, in, out, P, line_stride, nbatch, batch_stride, inverse, tw, shape); break;
-    default: launch32<1024>(st, in, out, P, line_stride, nbatch, batch_stride, inverse, tw, shape); break;
+    case 64: launch32<64>(st, in, out, P, zv, line_stride, nbatch, batch_stride, inverse, tw, shape); break;
+    case 128: launch32<128>(st, in, out, P, zv, line_stride, nbatch, batch_stride, inverse, tw, shape); break;
+    case 256: launch32<256>(st, in, out, P, zv, line_stride, nbatch, batch_stride, inverse, tw, shape); break;
+    case 512: launch32<512>(st, in, out, P, zv, line_stride, nbatch, batch_stride, inverse, tw, shape); break;
+    default: launch32<1024>(st, in, out, P, zv, line_stride, nbatch, batch_stride, inverse, tw, shape); break;
     }
 }
 

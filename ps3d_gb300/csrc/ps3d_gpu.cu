@@ -1541,9 +1541,9 @@ int autotune_lines(ps3d_gpu_ctx *c)
                         bs = xl ? d.P : (long long)d.ny * d.P;
         int best = 0;
         for (int w = 0; w < ns; ++w) {
-            launch_lines32(c->st, a, b, n, d.P, ls, nb, bs, inv, xl ? twx : twy, w);
+            launch_lines32(c->st, a, b, n, d.P, d.nz + 1, ls, nb, bs, inv, xl ? twx : twy, w);
             cudaEventRecord(c->ev0, c->st);
-            for (int r = 0; r < 3; ++r) launch_lines32(c->st, a, b, n, d.P, ls, nb, bs, inv, xl ? twx : twy, w);
+            for (int r = 0; r < 3; ++r) launch_lines32(c->st, a, b, n, d.P, d.nz + 1, ls, nb, bs, inv, xl ? twx : twy, w);
             cudaEventRecord(c->ev1, c->st);
             const int rc = sync_check(c, "autotune");
             if (rc) return rc;
@@ -2366,10 +2366,9 @@ int ps3d_gpu_synchronize(ps3d_gpu_ctx *c)
 // next: the prognostic state (FP64, and in the mixed form its FP32 copy), the
 // buoyancy state, the rolling means of adapt, the initial mean vorticity, the
 // viscosities and hyperdiffusion tables, N^2 and the model time.  Restored
-// without re-projection; the continuation agrees with an uninterrupted run to
-// rounding level (the line transforms pair the top z row with a padding row
-// of a transient buffer, whose leftover content enters that row's last bit;
-// a fresh context's padding is zero).  The reference restarts
+// without re-projection, a run continues bitwise (no result depends on the
+// leftover content of padding rows: the line transforms read them as zero).
+// The reference restarts
 // from the physical vorticity of a NetCDF field file (utils.f90:102-116);
 // its rolling means start afresh, so its restarts are not bit-continuous.
 

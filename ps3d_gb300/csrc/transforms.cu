@@ -2,8 +2,9 @@
 //
 // Device layout of a scalar field: z fastest with a padded column pitch P
 // (P >= nz+1, a multiple of 8), element (iz, iy, ix) at iz + P*(iy + ny*ix).
-// Rows nz+1..P-1 are padding; they hold zeros and are ignored by every
-// column operation.
+// Rows nz+1..P-1 are padding: every column operation ignores them, and the
+// line transforms read them as zero (two z rows share one complex line, so
+// leftover content would otherwise reach the top row's last bit).
 //
 //  * lines kernels (fftxyp2s / fftxys2p of src/fft/sta3dfft.f90:136-260):
 //    real FFTs along y (or x) in the reference's Hermitian storage
@@ -27,7 +28,7 @@ namespace ps3d {
 // ------------------------------------------------------------------------
 template <typename T, bool INV>
 __global__ void __launch_bounds__(256) k_lines(const T *__restrict__ in, T *__restrict__ out, int n,
-                                               int logB, int P, long long line_stride,
+                                               int logB, int P, int zv, long long line_stride,
                                                long long batch_stride,
                                                const typename cplx<T>::type *__restrict__ tw)
 {
@@ -47,6 +48,10 @@ __global__ void __launch_bounds__(256) k_lines(const T *__restrict__ in, T *__re
             const int i = e >> logB, p = e & (B - 1);
             C v = mk<C>(0, 0);
             if (z0 + 2 * p < P) v = inC[(base + i * line_stride + 2 * p) >> 1];
+            // padding rows (z >= zv) enter as zero: the paired real line
+            // must not pick up leftover content
+            if (z0 + 2 * p + 1 >= zv) v.y = 0;
+            if (z0 + 2 * p >= zv) v.x = 0;
             buf0[e] = v;
         }
     } else {
@@ -60,6 +65,8 @@ __global__ void __launch_bounds__(256) k_lines(const T *__restrict__ in, T *__re
                 lo = inC[(base + k * line_stride + 2 * p) >> 1];
                 if (k > 0 && k < h) hi = inC[(base + (n - k) * line_stride + 2 * p) >> 1];
             }
+            if (z0 + 2 * p + 1 >= zv) lo.y = hi.y = 0;
+            if (z0 + 2 * p >= zv) lo.x = hi.x = 0;
             // A_k = (lo.x, hi.x), B_k = (lo.y, hi.y)
             buf0[(k << logB) + p] = mk<C>(lo.x - hi.y, hi.x + lo.y);
             if (k > 0 && k < h) buf0[((n - k) << logB) + p] = mk<C>(lo.x + hi.y, lo.y - hi.x);
@@ -101,13 +108,13 @@ int lines_lanes(int n)
 }
 
 template <typename T>
-void launch_lines(cudaStream_t st, const T *in, T *out, int n, int P, long long line_stride,
+void launch_lines(cudaStream_t st, const T *in, T *out, int n, int P, int zv, long long line_stride,
                   long long nbatch, long long batch_stride, bool inverse,
                   const typename cplx<T>::type *tw, int shape = -1)
 {
     if constexpr (sizeof(T) == sizeof(float)) {
         if (lines32_supported(n)) {
-            launch_lines32(st, reinterpret_cast<const float *>(in), reinterpret_cast<float *>(out), n, P,
+            launch_lines32(st, reinterpret_cast<const float *>(in), reinterpret_cast<float *>(out), n, P, zv,
                            line_stride, nbatch, batch_stride, inverse, reinterpret_cast<const float2 *>(tw), shape);
             return;
         }
@@ -117,9 +124,9 @@ void launch_lines(cudaStream_t st, const T *in, T *out, int n, int P, long long 
     dim3 grid((P + 2 * B - 1) / (2 * B), (unsigned)nbatch);
     const size_t sm = 2 * (size_t)n * B * sizeof(typename cplx<T>::type);
     if (inverse)
-        k_lines<T, true><<<grid, 256, sm, st>>>(in, out, n, logB, P, line_stride, batch_stride, tw);
+        k_lines<T, true><<<grid, 256, sm, st>>>(in, out, n, logB, P, zv, line_stride, batch_stride, tw);
     else
-        k_lines<T, false><<<grid, 256, sm, st>>>(in, out, n, logB, P, line_stride, batch_stride, tw);
+        k_lines<T, false><<<grid, 256, sm, st>>>(in, out, n, logB, P, zv, line_stride, batch_stride, tw);
 }
 
 // algorithmic bytes of one pass over a field: read + write nx*ny*(nz+1)
@@ -134,11 +141,11 @@ void xy_forward(const Dims &d, cudaStream_t st, const T *in, T *out, const typen
 {
     // y lines: line stride P (one column), batches over x (stride ny*P)
     if (pr) pr->begin(PROBE_YLINES, st);
-    launch_lines<T>(st, in, out, d.ny, d.P, d.P, d.nx, (long long)d.ny * d.P, false, twy, d.line_shape[0]);
+    launch_lines<T>(st, in, out, d.ny, d.P, d.nz + 1, d.P, d.nx, (long long)d.ny * d.P, false, twy, d.line_shape[0]);
     if (pr) pr->end(PROBE_YLINES, st, pass_bytes<T>(d));
     // x lines: line stride ny*P, batches over y (stride P)
     if (pr) pr->begin(PROBE_XLINES, st);
-    launch_lines<T>(st, out, out, d.nx, d.P, (long long)d.ny * d.P, d.ny, d.P, false, twx, d.line_shape[1]);
+    launch_lines<T>(st, out, out, d.nx, d.P, d.nz + 1, (long long)d.ny * d.P, d.ny, d.P, false, twx, d.line_shape[1]);
     if (pr) pr->end(PROBE_XLINES, st, pass_bytes<T>(d));
 }
 
@@ -147,10 +154,10 @@ void xy_inverse(const Dims &d, cudaStream_t st, const T *in, T *out, const typen
                 const typename cplx<T>::type *twy, Probe *pr)
 {
     if (pr) pr->begin(PROBE_XLINES, st);
-    launch_lines<T>(st, in, out, d.nx, d.P, (long long)d.ny * d.P, d.ny, d.P, true, twx, d.line_shape[3]);
+    launch_lines<T>(st, in, out, d.nx, d.P, d.nz + 1, (long long)d.ny * d.P, d.ny, d.P, true, twx, d.line_shape[3]);
     if (pr) pr->end(PROBE_XLINES, st, pass_bytes<T>(d));
     if (pr) pr->begin(PROBE_YLINES, st);
-    launch_lines<T>(st, out, out, d.ny, d.P, d.P, d.nx, (long long)d.ny * d.P, true, twy, d.line_shape[2]);
+    launch_lines<T>(st, out, out, d.ny, d.P, d.nz + 1, d.P, d.nx, (long long)d.ny * d.P, true, twy, d.line_shape[2]);
     if (pr) pr->end(PROBE_YLINES, st, pass_bytes<T>(d));
 }
 
