@@ -84,3 +84,27 @@ def test_closure_and_checkpoint_entry_points_validate_on_the_host():
     assert L.ps3d_gpu_save_state(None, b"x", 0.0) == 1
     assert L.ps3d_gpu_load_state(None, b"x", ctypes.byref(t)) == 1
     assert L.ps3d_gpu_set_closure(None, None, 0) == 1
+
+
+def test_c_driver_builds_and_runs_against_the_c_abi(tmp_path):
+    """tests/c_driver.c uses the ABI from plain C99 (-Wall -Wextra -Werror):
+    the header needs no C++, the library links, and without a device the
+    driver ends cleanly with PS3D_ERR_NO_DEVICE (with one it runs two steps
+    and writes a checkpoint)."""
+    import shutil
+    import subprocess
+    gcc = shutil.which("gcc")
+    if gcc is None:
+        pytest.skip("no C compiler")
+    _lib.lib()  # built
+    src = os.path.join(os.path.dirname(os.path.abspath(__file__)), "c_driver.c")
+    exe = str(tmp_path / "c_driver")
+    libdir = os.path.dirname(build.LIB)
+    cmd = [gcc, "-std=c99", "-Wall", "-Wextra", "-Werror", "-O1", "-I", os.path.dirname(HEADER), src,
+           "-o", exe, "-L", libdir, "-lps3d_gpu", "-lm", "-Wl,-rpath," + libdir]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    r = subprocess.run([exe, "16", "2", str(tmp_path / "state.bin")], capture_output=True, text=True,
+                       timeout=300)
+    assert r.returncode == 0, r.stdout + r.stderr
+    assert r.stdout.startswith("c_driver:")
