@@ -230,7 +230,7 @@ def closure_timing(dev, n=64):
         vor, pert = ic.beltrami_plus_perturbation(n, n, n, seed=1, amplitude=1.0e-2)
         steps = {}
         for name, net in (("plain", None), ("closure_every_stage", cl)):
-            m = Ps3dGpu(n, n, n, ic.BASELINE_BOX["lower"], ic.BASELINE_BOX["extent"], precision="mixed",
+            m = Ps3dGpu(n, n, n, ic.BELTRAMI_BOX["lower"], ic.BELTRAMI_BOX["extent"], precision="mixed",
                         device=dev, **model_kw())
             m.setup_fields(vor, pert)
             if net is not None:
@@ -257,7 +257,7 @@ def cpu_sample(n_cpu, steps=1):
     import oracle
     from ps3d_gb300 import ic
     vor, pert = make_ic(n_cpu)
-    o = oracle.Oracle(n_cpu, n_cpu, n_cpu, ic.BASELINE_BOX["lower"], ic.BASELINE_BOX["extent"], **model_kw())
+    o = oracle.Oracle(n_cpu, n_cpu, n_cpu, ic.BELTRAMI_BOX["lower"], ic.BELTRAMI_BOX["extent"], **model_kw())
     o.setup_fields(vor, pert)
     t = 0.0
     t, _ = o.advance(t)
@@ -277,7 +277,7 @@ def run_reference(args, rank, world, dist):
     n = args.cpu_n
     cores = os.cpu_count()
     vor, pert = make_ic(n)
-    o = oracle.Oracle(n, n, n, ic.BASELINE_BOX["lower"], ic.BASELINE_BOX["extent"], nthreads=cores,
+    o = oracle.Oracle(n, n, n, ic.BELTRAMI_BOX["lower"], ic.BELTRAMI_BOX["extent"], nthreads=cores,
                       **model_kw())
     o.setup_fields(vor, pert)
     t = 0.0
@@ -308,7 +308,7 @@ def run_gpu(args, rank, world, dist):
     n = args.n
     dev = int(os.environ.get("LOCAL_RANK", "0"))
     pts = float(n) ** 3
-    lower, extent = ic.BASELINE_BOX["lower"], ic.BASELINE_BOX["extent"]
+    lower, extent = ic.BELTRAMI_BOX["lower"], ic.BELTRAMI_BOX["extent"]
     t_ic = time.perf_counter()
     vor, pert = make_ic(n, seed=1 + rank)
     log(f"[bench] rank {rank}: IC {n}^3 in {time.perf_counter() - t_ic:.1f}s")
@@ -414,9 +414,10 @@ def run_gpu(args, rank, world, dist):
                "h2d_bytes_per_step": nb, "d2h_bytes_per_step": nb, "steps": e2e_steps,
                "api": "ps3d_gpu_advance_host (svor FP64 in/out)", "host_buffer": host_kind}
 
-    # FP64 form against the FP64 ALU roofline (SURVEY §8(d) flop model:
-    # 49 transforms at 2.5 N log2 n each plus ~300 flop per point for the
-    # eigen-solve) and cuFFT as a comparator for the horizontal transforms
+    # FP64 form against the FP64 ALU roofline (flop model: 49 transforms per
+    # impl-diff-rk4 step at 2.5 N log2 n each, plus ~300 flop per point for
+    # the strain eigen-solve) and cuFFT as a comparator for the horizontal
+    # transforms
     if fp64 is not None:
         pk = fp64_peak_tflops(dev)
         N = float(n) ** 2 * (n + 1)

@@ -30,7 +30,7 @@ def build(counts, seed):
             amp = float(10.0 ** rng.uniform(-4.0, -2.0))
             pre = float(rng.choice([10.0, 30.0, 60.0, 90.0]))
             vor, pert = ic.beltrami_plus_perturbation(n, n, n, seed=1000 + k, amplitude=amp)
-            m = Ps3dGpu(n, n, n, ic.BASELINE_BOX["lower"], ic.BASELINE_BOX["extent"], precision="mixed",
+            m = Ps3dGpu(n, n, n, ic.BELTRAMI_BOX["lower"], ic.BELTRAMI_BOX["extent"], precision="mixed",
                         prediss=pre, cflmax=0.5, nnu=3, pretype="vorch")
             m.setup_fields(vor, pert)
             runs.append((n, amp, pre, m))

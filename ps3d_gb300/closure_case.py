@@ -49,7 +49,7 @@ def log(*a):
 def model(n, precision, **kw):
     args = dict(PHYS)
     args.update(kw)
-    return Ps3dGpu(n, n, n, ic.BASELINE_BOX["lower"], ic.BASELINE_BOX["extent"], precision=precision, **args)
+    return Ps3dGpu(n, n, n, ic.BELTRAMI_BOX["lower"], ic.BELTRAMI_BOX["extent"], precision=precision, **args)
 
 
 def fine_run(n, seed, amplitude, precision):

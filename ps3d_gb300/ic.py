@@ -12,7 +12,7 @@ projects the sum onto a solenoidal field (inversion.f90:34-76).
 """
 import numpy as np
 
-BASELINE_BOX = dict(lower=(0.0, 0.0, -0.5 * np.pi), extent=(2.0 * np.pi, 2.0 * np.pi, np.pi))
+BELTRAMI_BOX = dict(lower=(0.0, 0.0, -0.5 * np.pi), extent=(2.0 * np.pi, 2.0 * np.pi, np.pi))
 
 
 def beltrami_vorticity(nx, ny, nz, lower, extent, k=2, l=2, m=1):
@@ -76,8 +76,8 @@ def perturbation(nx, ny, nz, extent, seed, amplitude, vor_rms):
 def beltrami_plus_perturbation(nx, ny, nz, seed=0, amplitude=1.0e-3, lower=None, extent=None):
     """Physical Beltrami vorticity and the matching spectral perturbation,
     on the box (2pi, 2pi, pi) with lower z = -pi/2 unless given."""
-    lower = BASELINE_BOX["lower"] if lower is None else lower
-    extent = BASELINE_BOX["extent"] if extent is None else extent
+    lower = BELTRAMI_BOX["lower"] if lower is None else lower
+    extent = BELTRAMI_BOX["extent"] if extent is None else extent
     vor = beltrami_vorticity(nx, ny, nz, lower, extent)
     rms = float(np.sqrt(np.mean(np.sum(vor * vor, axis=0))))
     pert = perturbation(nx, ny, nz, extent, seed, amplitude, rms)
@@ -91,8 +91,8 @@ def beltrami_plus_perturbation_slabs(nx, ny, nz, seed=0, amplitude=1.0e-3, lower
     PCG64 seeded with (seed, ix), so for a given seed the field differs from
     `beltrami_plus_perturbation`'s; host memory is the two output arrays plus
     one slab."""
-    lower = BASELINE_BOX["lower"] if lower is None else lower
-    extent = BASELINE_BOX["extent"] if extent is None else extent
+    lower = BELTRAMI_BOX["lower"] if lower is None else lower
+    extent = BELTRAMI_BOX["extent"] if extent is None else extent
     vor = np.empty((3, nx, ny, nz + 1))
     kk, ll, mm = 2.0, 2.0, 1.0
     alpha = np.sqrt(kk ** 2 + ll ** 2 + mm ** 2)

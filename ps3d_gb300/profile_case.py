@@ -24,7 +24,7 @@ def main(argv=None):
     a = ap.parse_args(argv)
     nx, ny, nz = a.nx or a.n, a.ny or a.n, a.nz or a.n
     vor, pert = ic.beltrami_plus_perturbation(nx, ny, nz, seed=1)
-    g = Ps3dGpu(nx, ny, nz, ic.BASELINE_BOX["lower"], ic.BASELINE_BOX["extent"], precision=a.precision,
+    g = Ps3dGpu(nx, ny, nz, ic.BELTRAMI_BOX["lower"], ic.BELTRAMI_BOX["extent"], precision=a.precision,
                 nnu=3, prediss=30.0, pretype="vorch", cflmax=0.5)
     g.setup_fields(vor, pert)
     t = 0.0

@@ -17,7 +17,7 @@ def pair(nx, ny, nz, lower, extent, precision="fp64", **kw):
 
 
 def beltrami_case(n, seed=1, amplitude=1.0e-3, **kw):
-    lower, extent = ic.BASELINE_BOX["lower"], ic.BASELINE_BOX["extent"]
+    lower, extent = ic.BELTRAMI_BOX["lower"], ic.BELTRAMI_BOX["extent"]
     vor, pert = ic.beltrami_plus_perturbation(n, n, n, seed=seed, amplitude=amplitude)
     return lower, extent, vor, pert
 

@@ -12,7 +12,7 @@ import pytest
 import oracle
 from ps3d_gb300 import closure, ic
 
-LO, EX = ic.BASELINE_BOX["lower"], ic.BASELINE_BOX["extent"]
+LO, EX = ic.BELTRAMI_BOX["lower"], ic.BELTRAMI_BOX["extent"]
 
 
 def band_limited(nx, ny, nz):

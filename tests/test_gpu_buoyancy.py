@@ -16,7 +16,7 @@ from tests.parity_util import rel_l2
 
 pytestmark = pytest.mark.gpu
 
-BOX = ic.BASELINE_BOX
+BOX = ic.BELTRAMI_BOX
 
 
 def _case(n, seed=3, bfsq=2.0, amp=2e-2):

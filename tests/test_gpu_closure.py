@@ -20,7 +20,7 @@ F = torch.nn.functional
 
 pytestmark = pytest.mark.gpu
 
-LO, EX = ic.BASELINE_BOX["lower"], ic.BASELINE_BOX["extent"]
+LO, EX = ic.BELTRAMI_BOX["lower"], ic.BELTRAMI_BOX["extent"]
 # tolerances: relative L2 against the reference with the BF16 roundings
 # emulated / against plain FP64
 TOL_EMU_OUT, TOL_FP64_OUT = 5e-3, 3e-2

@@ -12,7 +12,7 @@ pytestmark = pytest.mark.gpu
 def _model(n, seed, nz=None, prediss=30.0, amplitude=1e-3):
     nz = nz or n
     vor, pert = ic.beltrami_plus_perturbation(n, n, nz, seed=seed, amplitude=amplitude)
-    m = Ps3dGpu(n, n, nz, ic.BASELINE_BOX["lower"], ic.BASELINE_BOX["extent"], precision="mixed",
+    m = Ps3dGpu(n, n, nz, ic.BELTRAMI_BOX["lower"], ic.BELTRAMI_BOX["extent"], precision="mixed",
                 prediss=prediss, cflmax=0.5)
     m.setup_fields(vor, pert)
     return m
@@ -52,7 +52,7 @@ def test_batch_of_uneven_runs_matches_individual_runs():
 
 def test_graph_refused_for_fp64_form():
     vor, pert = ic.beltrami_plus_perturbation(32, 32, 32, seed=1)
-    m = Ps3dGpu(32, 32, 32, ic.BASELINE_BOX["lower"], ic.BASELINE_BOX["extent"], precision="fp64")
+    m = Ps3dGpu(32, 32, 32, ic.BELTRAMI_BOX["lower"], ic.BELTRAMI_BOX["extent"], precision="fp64")
     m.setup_fields(vor, pert)
     with pytest.raises(Exception):
         m.advance_graph(0.0, 1)

@@ -260,7 +260,7 @@ def test_mixed_vor2vel_and_source_match_oracle(grid):
     equal products: rounding vel and vor alone to FP32 moves the oracle's
     tendency by about 1e-5 (relative L2) at these sizes."""
     nx, ny, nz = grid
-    lo, ex = ic.BASELINE_BOX["lower"], ic.BASELINE_BOX["extent"]
+    lo, ex = ic.BELTRAMI_BOX["lower"], ic.BELTRAMI_BOX["extent"]
     vor, pert = ic.beltrami_plus_perturbation(nx, ny, nz, seed=5, amplitude=1.0e-2)
     o = oracle.Oracle(nx, ny, nz, lo, ex)
     g = Ps3dGpu(nx, ny, nz, lo, ex, precision="mixed")
@@ -339,7 +339,7 @@ def test_mixed_adapt_diagnostics_match_oracle(grid):
     step and every diagnostic within 2e-5 relative (the FP32 gradients carry
     about 1e-6 relative rounding)."""
     nx, ny, nz = grid
-    lo, ex = ic.BASELINE_BOX["lower"], ic.BASELINE_BOX["extent"]
+    lo, ex = ic.BELTRAMI_BOX["lower"], ic.BELTRAMI_BOX["extent"]
     vor, pert = ic.beltrami_plus_perturbation(nx, ny, nz, seed=8, amplitude=5.0e-2)
     o = oracle.Oracle(nx, ny, nz, lo, ex, pretype="vorch")
     g = Ps3dGpu(nx, ny, nz, lo, ex, pretype="vorch", precision="mixed")
@@ -415,7 +415,7 @@ def test_derived_pressure_and_divergence_match_oracle(grid, precision, tol):
     perturbed Beltrami state against the oracle: 1e-12 in FP64, 1e-4 in the
     mixed form (FP32 products of the velocity gradients)."""
     nx, ny, nz = grid
-    lo, ex = ic.BASELINE_BOX["lower"], ic.BASELINE_BOX["extent"]
+    lo, ex = ic.BELTRAMI_BOX["lower"], ic.BELTRAMI_BOX["extent"]
     vor, pert = ic.beltrami_plus_perturbation(nx, ny, nz, seed=4, amplitude=1e-2)
     o = oracle.Oracle(nx, ny, nz, lo, ex)
     g = Ps3dGpu(nx, ny, nz, lo, ex, precision=precision)
@@ -435,7 +435,7 @@ def test_ke_spectrum_matches_oracle(grid, precision, tol):
     same shells and dk, every shell within tol of the largest, sum(spec) dk
     equal to the domain-average kinetic energy."""
     nx, ny, nz = grid
-    lo, ex = ic.BASELINE_BOX["lower"], ic.BASELINE_BOX["extent"]
+    lo, ex = ic.BELTRAMI_BOX["lower"], ic.BELTRAMI_BOX["extent"]
     vor, pert = ic.beltrami_plus_perturbation(nx, ny, nz, seed=6, amplitude=1e-2)
     o = oracle.Oracle(nx, ny, nz, lo, ex)
     g = Ps3dGpu(nx, ny, nz, lo, ex, precision=precision)
@@ -458,7 +458,7 @@ def test_mixed_steps_other_steppers_and_shapes(grid, stepper):
     """Mixed form over ten steps against the FP64 oracle for the cn2 stepper
     and a non-cubic grid: solenoidal state within 1e-6."""
     nx, ny, nz = grid
-    lo, ex = ic.BASELINE_BOX["lower"], ic.BASELINE_BOX["extent"]
+    lo, ex = ic.BELTRAMI_BOX["lower"], ic.BELTRAMI_BOX["extent"]
     vor, pert = ic.beltrami_plus_perturbation(nx, ny, nz, seed=10)
     o = oracle.Oracle(nx, ny, nz, lo, ex, cflmax=0.5, stepper=stepper)
     g = Ps3dGpu(nx, ny, nz, lo, ex, cflmax=0.5, stepper=stepper, precision="mixed")

@@ -15,7 +15,7 @@ from ps3d_gb300.solver import Ps3dError
 
 pytestmark = pytest.mark.gpu
 
-BOX = ic.BASELINE_BOX
+BOX = ic.BELTRAMI_BOX
 
 
 def rel(x, y):

@@ -18,7 +18,7 @@ import pytest
 import oracle
 from ps3d_gb300 import ic
 
-BOX = ic.BASELINE_BOX
+BOX = ic.BELTRAMI_BOX
 
 
 def _model(n=(16, 16, 16), lower=BOX["lower"], extent=BOX["extent"], **kw):

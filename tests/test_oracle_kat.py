@@ -123,7 +123,7 @@ def test_transform_conventions():
 
 def _beltrami_state(n):
     from ps3d_gb300 import ic
-    lo, ex = ic.BASELINE_BOX["lower"], ic.BASELINE_BOX["extent"]
+    lo, ex = ic.BELTRAMI_BOX["lower"], ic.BELTRAMI_BOX["extent"]
     o = oracle.Oracle(n, n, n, lo, ex)
     o.setup_fields(ic.beltrami_vorticity(n, n, n, lo, ex), None)
     o.vor2vel()

@@ -38,7 +38,7 @@ def test_energy_series_noalloc_matches_context_path():
     rt = _cudart()
     L = _lib.lib()
     n = 32
-    lo, ex = ic.BASELINE_BOX["lower"], ic.BASELINE_BOX["extent"]
+    lo, ex = ic.BELTRAMI_BOX["lower"], ic.BELTRAMI_BOX["extent"]
     vor0, pert = ic.beltrami_plus_perturbation(n, n, n, seed=3)
     g = Ps3dGpu(n, n, n, lo, ex)
     out = ctypes.c_void_p()
