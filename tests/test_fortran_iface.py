@@ -70,3 +70,22 @@ def test_named_constants_match_the_header():
 
 def test_lines_fit_free_form_fortran():
     assert max(len(line) for line in FORTRAN.splitlines()) <= 132
+
+
+STEPPER = open(os.path.join(os.path.dirname(INC), "ps3d_gb300", "fortran", "gpu_stepper.f90")).read()
+
+
+def test_gpu_stepper_uses_bound_procedures_and_overrides_the_deferred_bindings():
+    bound = set(re.findall(r"bind\(c, name='(\w+)'\)", FORTRAN))
+    called = set(re.findall(r"\b(ps3d_(?:gpu|closure)_\w+)\(", STEPPER))
+    assert called and not (called - bound), called - bound
+    # base_stepper's deferred bindings (src/stepper/advance.f90:31-59), with
+    # their dummy arguments
+    bindings = dict(re.findall(r"procedure :: (\w+) => (\w+)", STEPPER))
+    assert {"set_diffusion", "setup", "step"} <= set(bindings)
+    args = {k: re.search(r"subroutine " + v + r"\(([^)]*)\)", STEPPER).group(1).replace(" ", "")
+            for k, v in bindings.items()}
+    assert args["set_diffusion"] == "self,dt,vorch,bf"
+    assert args["setup"] == "self"
+    assert args["step"] == "self,t,dt"
+    assert max(len(line) for line in STEPPER.splitlines()) <= 132
