@@ -295,10 +295,13 @@ int ps3d_gpu_probe_result(ps3d_gpu_ctx *ctx, double *total_ms, long long *launch
  * default stream) and returns without synchronising.
  * Scratch: a fixed array in the library's device image (about 6 MB per GPU
  * that loads the library), so nx*ny may not exceed 524288 (returns
- * PS3D_ERR_UNSUPPORTED_SIZE beyond that).  The first call on a device looks
- * up that array's address (cudaGetSymbolAddress) and should therefore come
- * before any stream capture.  All calls share the array: calls that overlap
- * on the GPU race.  No context is needed and nothing is allocated. */
+ * PS3D_ERR_UNSUPPORTED_SIZE beyond that).  Every call looks up that array's
+ * address in the current device's context (cudaGetSymbolAddress); the first
+ * call on a device may load the library's device code into the context and
+ * should therefore come before any stream capture.  pitch above INT_MAX or
+ * comp_stride below pitch*nx*ny is PS3D_ERR_INVALID_ARG.  All calls share
+ * the array: calls that overlap on the GPU race.  No context is needed and
+ * nothing is allocated. */
 int ps3d_gpu_energy_series_noalloc(const double *vel, const double *vor, int nx, int ny, int nz,
                                    long long pitch, long long comp_stride, void *stream, double *out);
 

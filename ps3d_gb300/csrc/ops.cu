@@ -7,6 +7,7 @@
 // done in FP64 registers whatever the storage type, so the mixed-precision
 // form only rounds at loads and stores.
 #include <float.h>
+#include <limits.h>
 
 #include "kernels.h"
 
@@ -1357,35 +1358,27 @@ extern "C" int ps3d_gpu_energy_series_noalloc(const double *vel, const double *v
                                               long long pitch, long long comp_stride, void *stream, double *out)
 {
     using namespace ps3d;
-    if (!vel || !vor || !out || nx < 1 || ny < 1 || nz < 2 || pitch < nz + 1 ||
-        comp_stride < pitch * (long long)nx * ny)
+    if (!vel || !vor || !out || nx < 1 || ny < 1 || nz < 2 || pitch < nz + 1 || pitch > INT_MAX)
         return 1;  // PS3D_ERR_INVALID_ARG
     const long long ncol = (long long)nx * ny;
+    // comp_stride >= pitch * ncol, checked by division (no overflow)
+    if (comp_stride < 1 || comp_stride / ncol < pitch) return 1;
     const long long nblocks = (ncol + COLS_PER_BLOCK - 1) / COLS_PER_BLOCK;
     if (nblocks > NOALLOC_MAX_BLOCKS) return 2;  // PS3D_ERR_UNSUPPORTED_SIZE: nx*ny above the scratch capacity
-    int dev = -1;
-    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) {
-        cudaGetLastError();
-        return 8;  // PS3D_ERR_NO_DEVICE
-    }
-    // one-time set-up per device (on the first call made with that device
-    // current): the host-side address of the scratch array
-    static double *scratch_addr[64] = {nullptr};
-    if (!scratch_addr[dev]) {
-        double *p = nullptr;
-        if (cudaGetSymbolAddress((void **)&p, g_noalloc_scratch) != cudaSuccess || !p) {
-            cudaGetLastError();
-            return 3;  // PS3D_ERR_CUDA
-        }
-        scratch_addr[dev] = p;
-    }
-    double *part = scratch_addr[dev];
-    double *result = part + (size_t)NOALLOC_MAX_BLOCKS * RED1_N;
+    // Set-up: the device address of the scratch array in the current
+    // device's context.  It is looked up on every call (a table lookup in
+    // the runtime, no allocation), so it is right after cudaDeviceReset or
+    // when the caller switches contexts.  The very first call on a device
+    // may load this library's device code into the context, which is not
+    // allowed during stream capture: make that first call outside a capture.
+    double *part = nullptr;
     int *kinds = nullptr;
-    if (cudaGetSymbolAddress((void **)&kinds, c_kinds1) != cudaSuccess) {
-        cudaGetLastError();
-        return 3;
+    if (cudaGetSymbolAddress((void **)&part, g_noalloc_scratch) != cudaSuccess || !part ||
+        cudaGetSymbolAddress((void **)&kinds, c_kinds1) != cudaSuccess || !kinds) {
+        const cudaError_t e = cudaGetLastError();
+        return (e == cudaErrorNoDevice || e == cudaErrorInsufficientDriver) ? 8 : 3;  // NO_DEVICE or CUDA
     }
+    double *result = part + (size_t)NOALLOC_MAX_BLOCKS * RED1_N;
     Dims d;
     d.nx = nx;
     d.ny = ny;

@@ -2363,9 +2363,15 @@ int ps3d_gpu_synchronize(ps3d_gpu_ctx *c)
 
 // ------------------------------------------------------------ checkpoint
 // Raw-binary checkpoint of everything a run carries from one step to the
-// next: the prognostic state (FP64, and in the mixed form its FP32 copy), the
-// buoyancy state, the rolling means of adapt, the initial mean vorticity, the
-// viscosities and hyperdiffusion tables, N^2 and the model time.  Restored
+// next.  Stored: the prognostic state svor (FP64, and in the mixed form its
+// FP32 copy), the buoyancy state sbuoy (likewise), the rolling-mean rings of
+// adapt with their indices, fill flags and running means, the initial mean
+// vorticity, the viscosities vvisc / bvisc, the hyperdiffusion tables vhdis
+// / bhdis, N^2 and the model time.  Not stored, because every step rebuilds
+// them before use: vdiss / bdiss and the integrating factors epq, emq, epq2,
+// emq2 (set_diffusion and the stepper's factor kernel recompute them from
+// vhdis / bhdis, dt and the prefactor), and the grid tables of context
+// creation (wavenumbers, filters, harmonic functions).  Restored
 // without re-projection, a run continues bitwise (no result depends on the
 // leftover content of padding rows: the line transforms read them as zero).
 // The reference restarts
@@ -2497,6 +2503,11 @@ int ps3d_gpu_load_state(ps3d_gpu_ctx *c, const char *path, double *t)
         h.buoyancy != (c->cfg.buoyancy ? 1 : 0) || h.nnu != c->cfg.nnu || !same_box ||
         h.roll_len != (int32_t)c->roll.hist.size() || h.rollb_len != (int32_t)c->roll_b.hist.size())
         return fail(c, PS3D_ERR_INVALID_ARG, "load_state: checkpoint of another grid, box, form or configuration");
+    // the ring indices address hist[inew-1] and hist[iold-1] on the next step
+    // (rolling_mean.f90:36-69): a file with an index outside 1..len is refused
+    if (h.roll_inew < 1 || h.roll_inew > h.roll_len || h.roll_iold < 1 || h.roll_iold > h.roll_len ||
+        h.rollb_inew < 1 || h.rollb_inew > h.rollb_len || h.rollb_iold < 1 || h.rollb_iold > h.rollb_len)
+        return fail(c, PS3D_ERR_INVALID_ARG, "load_state: rolling-mean index outside its ring");
     std::vector<double> rh(h.roll_len), rbh(h.rollb_len), vh(d.ncol), bh(h.buoyancy ? d.ncol : 0), sv(3 * n1),
         sb(h.buoyancy ? n1 : 0);
     std::vector<float> sv32(c->fp64 ? 0 : 3 * n1), sb32((!c->fp64 && h.buoyancy) ? n1 : 0);

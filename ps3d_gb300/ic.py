@@ -136,6 +136,41 @@ def beltrami_plus_perturbation_slabs(nx, ny, nz, seed=0, amplitude=1.0e-3, lower
     return vor, pert
 
 
+def kolmogorov_spectral_vorticity(nx, ny, nz, extent, seed=0):
+    """(3, nx, ny, nz+1) seeded random mixed-spectral vorticity for the
+    standalone vor2vel / diffz workloads: amplitude K^(-5/3), K = |(k, l, m)|
+    from the reference's wavenumber tables (zero at K = 0), with uniform
+    random phases.  In each horizontal direction a mode k has a cosine slot
+    k and a sine slot n-k of the Hermitian layout (stafft.f90:55-58); the
+    slot pair of mode k in x (and likewise in y) takes cos(phi), sin(phi) of
+    a phase phi drawn uniformly in [0, 2pi) per component, mode and level
+    (PCG64(seed)), and the coefficient is the product of the x and y
+    factors.  Every level is filled, the wall rows (semi-spectral boundary
+    values) included.  Normalised to unit rms over the stored values."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    rkx, rky, rkz = wavenumbers(nx, ny, nz, extent)
+    K2 = rkx[:, None, None] ** 2 + rky[None, :, None] ** 2 + rkz[None, None, :] ** 2
+    amp = np.zeros_like(K2)
+    np.power(K2, -5.0 / 6.0, out=amp, where=K2 > 0)
+
+    def slots(n):
+        j = np.arange(n)
+        mode = np.where(j <= n // 2, j, n - j)
+        return mode, j > n // 2
+
+    mx, sx = slots(nx)
+    my, sy = slots(ny)
+    phx = rng.uniform(0.0, 2.0 * np.pi, size=(3, nx // 2 + 1, ny // 2 + 1, nz + 1))
+    phy = rng.uniform(0.0, 2.0 * np.pi, size=(3, nx // 2 + 1, ny // 2 + 1, nz + 1))
+    ax = phx[:, mx[:, None], my[None, :], :]
+    ay = phy[:, mx[:, None], my[None, :], :]
+    fx = np.where(sx[None, :, None, None], np.sin(ax), np.cos(ax))
+    fy = np.where(sy[None, None, :, None], np.sin(ay), np.cos(ay))
+    out = amp[None] * fx * fy
+    out /= np.sqrt(np.mean(out * out))
+    return out
+
+
 def grid(nx, ny, nz, lower, extent):
     """Grid coordinates x (nx), y (ny), z (nz+1) of the reference's nodes."""
     dx = np.array(extent, dtype=np.float64) / np.array([nx, ny, nz], dtype=np.float64)

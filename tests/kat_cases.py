@@ -3,7 +3,7 @@
 Each function returns the grid/box of the reference test, the analytic input
 and the analytic expected output, plus the tolerance the reference uses.
 The same cases run against the CPU oracle (test_oracle_kat.py) and against
-the GPU library (test_gpu_kat.py).
+the GPU library (the known-answer tests of test_gpu_parity.py).
 
 Arrays follow the reference layout: a scalar field is shaped (nx, ny, nz+1)
 in C order (z fastest), a vector field (3, nx, ny, nz+1).

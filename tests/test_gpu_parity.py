@@ -155,7 +155,7 @@ def test_one_step_matches_oracle(stepper):
         assert rel_l2(g.get("svor")[c], o.get("svor")[c]) < FIELD_TOL
 
 
-@pytest.mark.parametrize("n,nsteps", [(32, 200), (128, 10)])
+@pytest.mark.parametrize("n,nsteps", [(32, 200)])
 def test_multi_step_parity_per_step(n, nsteps):
     """Per-step relative L2 of each vorticity component and the energy /
     enstrophy / helicity series over nsteps steps (Beltrami + perturbation,
@@ -165,7 +165,9 @@ def test_multi_step_parity_per_step(n, nsteps):
     grows by ~1e4 over 200 steps at 32^3 whatever produced it.  The oracle run
     against itself from an initial field perturbed by 1e-15 (relative) gives
     that rounding floor step by step; the GPU must stay within 1e-12 of the
-    oracle while the floor is below 1e-13 and within 10x the floor after."""
+    oracle while the floor is below 1e-13 and within 10x the floor after.
+    The worst ratio of GPU error to floor is printed.  (128^3 over 200 steps:
+    test_gpu_parity_config2.py.)"""
     o, g = _setup_both(n)
     lo, ex, vor, pert = beltrami_case(n, seed=1)
     f = oracle.Oracle(n, n, n, lo, ex, cflmax=0.5)
@@ -173,6 +175,7 @@ def test_multi_step_parity_per_step(n, nsteps):
     f.setup_fields(vor * jitter, pert)
     t_o = t_g = t_f = 0.0
     worst_series = 0.0
+    worst_ratio, worst_at = 0.0, None
     checked = 0
     for s in range(nsteps):
         t_g, dg = g.advance(t_g)
@@ -187,7 +190,11 @@ def test_multi_step_parity_per_step(n, nsteps):
                 floor = rel_l2(c_[c], b[c])
                 bound = FIELD_TOL if floor < 1.0e-13 else 10.0 * floor
                 assert err < bound, (s, c, err, floor)
+                if floor > 0 and err / floor > worst_ratio:
+                    worst_ratio, worst_at = err / floor, (s, c, err, floor)
                 checked += 1
+    print(f"{n}^3 x {nsteps} steps: worst GPU/floor ratio {worst_ratio:.3g} at (step, comp, err, floor) "
+          f"{worst_at}; worst series error {worst_series:.3g}")
     assert checked > 0
     assert worst_series < SERIES_TOL, worst_series
     assert abs(t_g - t_o) <= 1e-10 * t_o

@@ -88,6 +88,18 @@ def test_mismatched_and_damaged_checkpoints_are_refused(tmp_path):
     (tmp_path / "bad.bin").write_bytes(b"XXXXXXXX" + raw[8:])
     with pytest.raises(Ps3dError):
         a.load_state(tmp_path / "bad.bin")
+    # rolling-mean ring indices outside 1..len (header: int32 roll_len at
+    # byte 36, rollb_len 40, roll_inew 48, roll_iold 52, rollb_inew 60,
+    # rollb_iold 64) are refused before anything is read into the context
+    roll_len = int(np.frombuffer(raw[36:40], dtype=np.int32)[0])
+    rollb_len = int(np.frombuffer(raw[40:44], dtype=np.int32)[0])
+    for off, val in ((48, roll_len + 1), (52, 0), (60, rollb_len + 1), (64, -3)):
+        patched = bytearray(raw)
+        patched[off:off + 4] = np.int32(val).tobytes()
+        (tmp_path / "idx.bin").write_bytes(bytes(patched))
+        with pytest.raises(Ps3dError) as e:
+            a.load_state(tmp_path / "idx.bin")
+        assert e.value.code == 1, (off, val, e.value.code)  # PS3D_ERR_INVALID_ARG
     # the context still works after the refusals
     t, _ = a.advance(0.0)
     assert t > 0.0
