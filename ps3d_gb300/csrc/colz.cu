@@ -593,14 +593,18 @@ template <int M> constexpr int zbuf_floats() { return 32 * M + 1 + (32 * M + 1) 
 }  // namespace
 
 // ------------------------------------------------------------------------
-// es = decompose(central_diffz(combine(f))) in one kernel (the z part of
-// the solenoidal projection, inversion.f90:41-47): combine through the
-// warp FFT into the warp's z buffers, the two-sided difference into the FFT
-// buffer, then the decomposition; one read of f and one write of es.
+// The third tendency component's two decompositions in one kernel (mixed
+// form): from the semi-spectral S3 of a column pair,
+//   out = decompose(S3)                 (the mixed-spectral tendency), and
+//   es  = decompose(central_diffz(S3))  (the z part of its solenoidal
+//                                        projection, inversion.f90:41-47),
+// one read of S3 into the warp's z buffers, two warp FFTs, one write each.
+// Safe in place (out == f): the pair is read whole before anything is
+// written.
 template <int M>
-__global__ void __launch_bounds__(256, 2) k_colz_proj(const float *__restrict__ f, float *__restrict__ es, int P,
-                                                      long long npairs, const double *__restrict__ k2l2, float dz,
-                                                      float Lz, const float2 *__restrict__ twn,
+__global__ void __launch_bounds__(256, 2) k_colz_dec2(const float *__restrict__ f, float *out, float *__restrict__ es,
+                                                      int P, long long npairs, const double *__restrict__ k2l2,
+                                                      float dz, float Lz, const float2 *__restrict__ twn,
                                                       const float *__restrict__ sinz)
 {
     constexpr int n = 32 * M;
@@ -610,7 +614,6 @@ __global__ void __launch_bounds__(256, 2) k_colz_proj(const float *__restrict__ 
     float2 *xs = reinterpret_cast<float2 *>(smz + (size_t)wib * (n * sizeof(float2) + 2 * ZS * sizeof(float)));
     float *zA = reinterpret_cast<float *>(xs + n);
     float *zB = zA + ZS;
-    // derivative levels 0..n-1 reuse the FFT buffer; level n stays in registers
     float *gA = reinterpret_cast<float *>(xs), *gB = gA + n;
     const float r2s = 1.41421356237309505f * rsqrtf((float)n);
     const float dzi = 1.0f / dz, hdzi = 0.5f / dz;
@@ -618,46 +621,54 @@ __global__ void __launch_bounds__(256, 2) k_colz_proj(const float *__restrict__ 
     for (long long pr = (long long)blockIdx.x * (blockDim.x >> 5) + wib; pr < npairs; pr += warps) {
         const long long cA = 2 * pr, cB = cA + 1;
         const long long oA = cA * P, oB = cB * P;
-        // lanes 0..2 (column A) and 8..10 (column B): f(0), f(nz), kl
-        float par = 0.f;
-        if (lane < 16 && (lane & 7) < 3) {
-            const long long c = lane < 8 ? cA : cB;
-            const int q = lane & 7;
-            par = q == 2 ? sqrtf((float)k2l2[c]) : f[c * P + (q == 0 ? 0 : n)];
+        // the pair into the z buffers (levels 0..n)
+        for (int iz = lane; iz <= n; iz += 32) {
+            zA[zpad(iz)] = f[oA + iz];
+            zB[zpad(iz)] = f[oB + iz];
         }
-        // ---- combine: dst of the interior, plus the harmonic part
+        // lanes 0 / 8: kl of columns A / B
+        float par = 0.f;
+        if (lane == 0 || lane == 8) par = sqrtf((float)k2l2[lane == 0 ? cA : cB]);
+        __syncwarp();
+        // ---- decompose S3: subtract the harmonic part, dst
         {
+            const Harm hA = Harm::make(lane_get(par, 0), dz, Lz, n, cA == 0);
+            const Harm hB = Harm::make(lane_get(par, 8), dz, Lz, n, cB == 0);
+            const float f0A = zA[zpad(0)], fnA = zA[zpad(n)], f0B = zB[zpad(0)], fnB = zB[zpad(n)];
             float2 v[M];
 #pragma unroll
             for (int m = 0; m < M; ++m) {
                 const int j = lane + 32 * m;
                 v[m] = make_float2(0.f, 0.f);
-                if (j > 0) v[m] = pre_sine(f[oA + j], f[oA + n - j], f[oB + j], f[oB + n - j], __ldg(&sinz[j]));
+                if (j > 0) {
+                    float xa = zA[zpad(j)], ya = zA[zpad(n - j)], xb = zB[zpad(j)], yb = zB[zpad(n - j)];
+                    float pm, pp;
+                    hA.at(j, n, pm, pp);
+                    xa -= f0A * pm + fnA * pp;
+                    ya -= f0A * pp + fnA * pm;
+                    hB.at(j, n, pm, pp);
+                    xb -= f0B * pm + fnB * pp;
+                    yb -= f0B * pp + fnB * pm;
+                    v[m] = pre_sine(xa, ya, xb, yb, __ldg(&sinz[j]));
+                }
             }
             warp_fft<M>(v, xs, twn, lane);
         }
         {
-            const float f0A = lane_get(par, 0), fnA = lane_get(par, 1), f0B = lane_get(par, 8),
-                        fnB = lane_get(par, 9);
-            const Harm hA = Harm::make(lane_get(par, 2), dz, Lz, n, cA == 0);
-            const Harm hB = Harm::make(lane_get(par, 10), dz, Lz, n, cB == 0);
+            const float f0A = zA[zpad(0)], fnA = zA[zpad(n)], f0B = zB[zpad(0)], fnB = zB[zpad(n)];
+            float *colA = out + oA, *colB = out + oB;
             post<M, false>(xs, lane, r2s, 0.f, 0.f, [&](int k, float eA, float oA_, float eB, float oB_) {
-                float pm0, pp0, pm1, pp1;
-                hA.at2(2 * k, n, pm0, pp0, pm1, pp1);
-                zA[zpad(2 * k)] = (k == 0) ? f0A : eA + f0A * pm0 + fnA * pp0;
-                zA[zpad(2 * k + 1)] = oA_ + f0A * pm1 + fnA * pp1;
-                hB.at2(2 * k, n, pm0, pp0, pm1, pp1);
-                zB[zpad(2 * k)] = (k == 0) ? f0B : eB + f0B * pm0 + fnB * pp0;
-                zB[zpad(2 * k + 1)] = oB_ + f0B * pm1 + fnB * pp1;
+                st2(colA, k, (k == 0) ? f0A : eA, oA_);
+                st2(colB, k, (k == 0) ? f0B : eB, oB_);
             });
             if (lane == 0) {
-                zA[zpad(n)] = fnA;
-                zB[zpad(n)] = fnB;
+                colA[n] = fnA;
+                colB[n] = fnB;
             }
         }
         __syncwarp();
         // ---- central_diffz (inversion_utils.f90:653-673): levels 0..n-1
-        // into gA / gB, level n in registers
+        // into gA / gB (the FFT buffer), level n in registers
         for (int iz = lane; iz < n; iz += 32) {
             const int lo = iz == 0 ? 0 : iz - 1;
             const float sc = iz == 0 ? dzi : hdzi;
@@ -667,11 +678,11 @@ __global__ void __launch_bounds__(256, 2) k_colz_proj(const float *__restrict__ 
         const float gnA = dzi * (zA[zpad(n)] - zA[zpad(n - 1)]);
         const float gnB = dzi * (zB[zpad(n)] - zB[zpad(n - 1)]);
         __syncwarp();
-        // ---- decompose: subtract the harmonic part, dst
+        // ---- decompose the derivative
         const float g0A = gA[0], g0B = gB[0];
         {
-            const Harm hA = Harm::make(lane_get(par, 2), dz, Lz, n, cA == 0);
-            const Harm hB = Harm::make(lane_get(par, 10), dz, Lz, n, cB == 0);
+            const Harm hA = Harm::make(lane_get(par, 0), dz, Lz, n, cA == 0);
+            const Harm hB = Harm::make(lane_get(par, 8), dz, Lz, n, cB == 0);
             float2 v[M];
 #pragma unroll
             for (int m = 0; m < M; ++m) {
@@ -752,12 +763,12 @@ void launch_w_m(const Dims &d, cudaStream_t st, const float *ds, float *w, float
 }
 
 template <int M>
-void launch_proj_m(const Dims &d, cudaStream_t st, const float *f, float *es, const double *k2l2, float dz, float Lz,
-                   const float2 *twn, const float *sinz)
+void launch_dec2_m(const Dims &d, cudaStream_t st, const float *f, float *out, float *es, const double *k2l2,
+                   float dz, float Lz, const float2 *twn, const float *sinz)
 {
     const long long npairs = d.ncol / 2;
-    k_colz_proj<M><<<(unsigned)colz_blocks(npairs), 256, 8 * proj_smem_per_warp<M>(), st>>>(f, es, d.P, npairs,
-                                                                                            k2l2, dz, Lz, twn, sinz);
+    k_colz_dec2<M><<<(unsigned)colz_blocks(npairs), 256, 8 * proj_smem_per_warp<M>(), st>>>(
+        f, out, es, d.P, npairs, k2l2, dz, Lz, twn, sinz);
 }
 
 template <typename K> void smem_attr(K kern, size_t bytes)
@@ -775,7 +786,7 @@ template <int M> void attr_m()
     smem_attr(k_colz<COL_DECOMP, M, double>, 8 * colz_smem_per_warp<M>());
     smem_attr(k_colz<COL_COMBINE, M, double>, 8 * colz_smem_per_warp<M>());
     smem_attr(k_colz_w<M>, 8 * colz_smem_per_warp<M>());
-    smem_attr(k_colz_proj<M>, 8 * proj_smem_per_warp<M>());
+    smem_attr(k_colz_dec2<M>, 8 * proj_smem_per_warp<M>());
 }
 }  // namespace
 
@@ -794,18 +805,18 @@ void columns_w(const Dims &d, cudaStream_t st, const float *ds, float *w, float 
     if (pr) pr->end(PROBE_COLUMNS, st, 3.0 * (double)d.ncol * (double)(d.nz + 1) * sizeof(float));
 }
 
-void columns_proj(const Dims &d, cudaStream_t st, const float *f, float *es, const double *k2l2, float dz, float Lz,
-                  const float2 *twn, const float *sinz, Probe *pr)
+void columns_dec2(const Dims &d, cudaStream_t st, const float *f, float *out, float *es, const double *k2l2,
+                  float dz, float Lz, const float2 *twn, const float *sinz, Probe *pr)
 {
     if (pr) pr->begin(PROBE_COLUMNS, st);
     switch (d.nz) {
-    case 64: launch_proj_m<2>(d, st, f, es, k2l2, dz, Lz, twn, sinz); break;
-    case 128: launch_proj_m<4>(d, st, f, es, k2l2, dz, Lz, twn, sinz); break;
-    case 256: launch_proj_m<8>(d, st, f, es, k2l2, dz, Lz, twn, sinz); break;
-    case 512: launch_proj_m<16>(d, st, f, es, k2l2, dz, Lz, twn, sinz); break;
-    default: launch_proj_m<32>(d, st, f, es, k2l2, dz, Lz, twn, sinz); break;
+    case 64: launch_dec2_m<2>(d, st, f, out, es, k2l2, dz, Lz, twn, sinz); break;
+    case 128: launch_dec2_m<4>(d, st, f, out, es, k2l2, dz, Lz, twn, sinz); break;
+    case 256: launch_dec2_m<8>(d, st, f, out, es, k2l2, dz, Lz, twn, sinz); break;
+    case 512: launch_dec2_m<16>(d, st, f, out, es, k2l2, dz, Lz, twn, sinz); break;
+    default: launch_dec2_m<32>(d, st, f, out, es, k2l2, dz, Lz, twn, sinz); break;
     }
-    if (pr) pr->end(PROBE_COLUMNS, st, 2.0 * (double)d.ncol * (double)(d.nz + 1) * sizeof(float));
+    if (pr) pr->end(PROBE_COLUMNS, st, 3.0 * (double)d.ncol * (double)(d.nz + 1) * sizeof(float));
 }
 
 bool colz_supported(int nz) { return nz == 64 || nz == 128 || nz == 256 || nz == 512 || nz == 1024; }

@@ -82,12 +82,14 @@ template <typename TIN>
 void columns_z(const Dims &d, cudaStream_t st, int mode, const TIN *in, float *out, const double *k2l2, float dz,
                float Lz, const float2 *twn, const float *sinz, const float *cosz, Probe *pr);
 // fused column kernels of the mixed form (colz.cu): the vertical velocity
-// of vor2vel (w and dw/dz from ds) and the z part of the projection
+// of vor2vel (w and dw/dz from ds), and the decomposition of the third
+// tendency component together with the z part of its solenoidal projection
+// (out = decompose(f), es = decompose(central_diffz(f)); out may be f)
 void columns_w(const Dims &d, cudaStream_t st, const float *ds, float *w, float *es, const double *k2l2,
                const double *k2l2i, float dz, float Lz, const float2 *twn, const float *sinz, const float *cosz,
                Probe *pr);
-void columns_proj(const Dims &d, cudaStream_t st, const float *f, float *es, const double *k2l2, float dz, float Lz,
-                  const float2 *twn, const float *sinz, Probe *pr);
+void columns_dec2(const Dims &d, cudaStream_t st, const float *f, float *out, float *es, const double *k2l2,
+                  float dz, float Lz, const float2 *twn, const float *sinz, Probe *pr);
 // FP32 warp-per-column-pair transforms (columns32.cu), nz = 32..512
 bool col32_supported(int nz);
 void columns32_init();
@@ -188,6 +190,15 @@ void op_rk4m_sub23(const Dims &d, cudaStream_t st, double *q, const double *qdi,
 void op_rk4m_sub4(const Dims &d, cudaStream_t st, double *q, const double *qdi, const float *acc, const float *sqs,
                   float *q32, const double *epq, const double *emq, const double *dtp);
 void op_narrow(cudaStream_t st, const double *in, float *out, long long n);
+// mixed form, impl-diff-rk4: the solenoidal projection of the tendency
+// (S: the three decomposed components; es: decompose(diffz(S3))), the
+// filter and substep sub (1..4) of the integrating-factor RK4 in one pass;
+// fp, fm: the substep's column factors (1: filt0, emq; 2: epq, emq;
+// 3: epq, emq2; 4: epq2, emq2).  The FP64 state q is rewritten by substep 4
+// only; mf receives the (0,0) column of each stage state (components 1, 2)
+void op_stage_orbit(const Dims &d, cudaStream_t st, int sub, const Deriv &D, const double *k2l2i, const float *S,
+                    const float *es, double *q, float *acc, float *q32, double *mf, const double *fp,
+                    const double *fm, const double *dtp);
 // derived fields (pressure right-hand side, table product, horizontal divergence)
 template <typename T> void op_pressure_rhs(const Dims &d, cudaStream_t st, const T *g5, const T *vor, T *out);
 template <typename T> void op_mul_field(const Dims &d, cudaStream_t st, const T *tab, T *f);

@@ -755,6 +755,140 @@ void op_rk4m_sub4(const Dims &d, cudaStream_t st, double *q, const double *qdi, 
     k_rk4m_sub4<<<col_grid(d), COL_BLOCK, 0, st>>>(d, q, qdi, acc, sqs, q32, epq, emq, dtp);
 }
 
+// ------------------------------------------------ fused stage update (mixed)
+// The solenoidal projection of the tendency, the horizontal filter and one
+// integrating-factor substep of impl_rk4.f90:212-364 in one pass over the
+// tendency.  The projection is vor2vel's (inversion.f90:34-76) applied to
+// svorts:
+//   ds = D_x S2 - D_y S1,  S1 <- k2l2i (D_x es + D_y ds),
+//   S2 <- k2l2i (D_y es - D_x ds),  S3 unchanged,  (0,0) column kept,
+// es = decompose(diffz(S3)) from the source.  The projection is linear and
+// commutes with the per-column factors, so projecting each source term keeps
+// the state on the reference's projected trajectory.  One warp per partner
+// orbit (as k_v2v_orbit): the four columns (kx, ky), (nx-kx, ky), (kx, ny-ky),
+// (nx-kx, ny-ky) read only one another, so ds never leaves registers.
+//
+// State traffic: the FP64 state q is the step's initial state (qdi of the
+// reference) throughout substeps 1-3 and is not rewritten until substep 4.
+// Each substep writes the FP32 copy q32 of its stage state (what the next
+// vor2vel reads) and the FP32 source accumulator acc (the reference's qdf
+// minus qdi, see k_rk4m_sub1); the stage state of the (0,0) column also goes
+// to mf in FP64 (components 1 and 2, pitch P) for the mean-flow inversion of
+// the next vor2vel.  Substep 4 writes q.  Per element and substep, the same
+// FP32 increments and FP64 fused multiply-adds as k_rk4m_sub1/23/4.
+//   SUB 1: factors filt0, emq;           s = f s,  q' = q m + (dt/2 m) s,  acc  = dt/6 s
+//   SUB 2: factors epq, emq,  c1 = dt/2: s = p s,  q' = q m + (c1 m) s,    acc += dt/3 s
+//   SUB 3: factors epq, emq2, c1 = dt:   (as SUB 2)
+//   SUB 4: factors epq2, emq2:           q' = q m + (acc m + (dt/6 p m) s)
+template <int SUB> struct StageCol {
+    double m;
+    float a, b, c;
+    __device__ __forceinline__ void make(double dt, const double *fp, const double *fm, long long col)
+    {
+        m = fm[col];
+        if (SUB == 1) {
+            a = (float)fp[col];
+            b = (float)(0.5 * dt * m);
+            c = (float)(dt / 6.0);
+        } else if (SUB == 4) {
+            a = (float)m;
+            b = (float)(dt / 6.0 * fp[col] * m);
+        } else {
+            a = (float)fp[col];
+            b = (float)((SUB == 3 ? dt : 0.5 * dt) * m);
+            c = (float)(dt / 3.0);
+        }
+    }
+    // one element: s the projected source, q0 the step's initial state
+    __device__ __forceinline__ double apply(float s, double q0, float *acc) const
+    {
+        if (SUB == 4) return fma(q0, m, widen64(fmaf(*acc, a, b * s)));
+        const float fs = a * s;
+        const double qn = fma(q0, m, widen64(b * fs));
+        *acc = (SUB == 1) ? c * fs : fmaf(c, fs, *acc);
+        return qn;
+    }
+};
+
+template <int SUB>
+__global__ void k_stage_orbit(Dims d, Deriv D, const double *__restrict__ k2l2i, const float *__restrict__ S,
+                              const float *__restrict__ es, double *__restrict__ q, float *__restrict__ acc,
+                              float *__restrict__ q32, double *__restrict__ mf, const double *__restrict__ fp,
+                              const double *__restrict__ fm, const double *__restrict__ dtp)
+{
+    const int hy = d.ny / 2 + 1;
+    const long long orb = (long long)blockIdx.x * COLS_PER_BLOCK + threadIdx.y;
+    if (orb >= (long long)(d.nx / 2 + 1) * hy) return;
+    const long long N = d.nfield;
+    const int kx = (int)(orb / hy), ky = (int)(orb - (long long)kx * hy);
+    const int x2 = xsrc(kx, d.nx), y2 = xsrc(ky, d.ny);
+    const long long c00 = (long long)ky + (long long)d.ny * kx, c10 = (long long)ky + (long long)d.ny * x2;
+    const long long c01 = (long long)y2 + (long long)d.ny * kx, c11 = (long long)y2 + (long long)d.ny * x2;
+    const long long o00 = c00 * d.P, o10 = c10 * d.P, o01 = c01 * d.P, o11 = c11 * d.P;
+    const bool dx = x2 != kx, dy = y2 != ky, mean = c00 == 0;
+    const float cxa = (float)D.cx[kx], cxb = (float)D.cx[x2], cya = (float)D.cy[ky], cyb = (float)D.cy[y2];
+    const float k00 = (float)k2l2i[c00], k10 = (float)k2l2i[c10], k01 = (float)k2l2i[c01],
+                k11 = (float)k2l2i[c11];
+    const double dt = *dtp;
+    StageCol<SUB> f00, f10, f01, f11;
+    f00.make(dt, fp, fm, c00);
+    f10.make(dt, fp, fm, c10);
+    f01.make(dt, fp, fm, c01);
+    f11.make(dt, fp, fm, c11);
+    const float *S1 = S, *S2 = S + N, *S3 = S + 2 * N;
+    // one member column at level i: the three projected components
+    auto update = [&](const StageCol<SUB> &f, long long i, float s1, float s2, float s3, bool mean_col) {
+        const float sv[3] = {s1, s2, s3};
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            const long long ik = (long long)k * N + i;
+            float a = (SUB == 1) ? 0.f : acc[ik];
+            const double qn = f.apply(sv[k], q[ik], &a);
+            if (SUB == 4) q[ik] = qn;
+            else acc[ik] = a;
+            q32[ik] = narrow32(qn);
+            if (mean_col && k < 2) mf[(long long)k * d.P + i] = qn;
+        }
+    };
+    for (int iz = threadIdx.x; iz <= d.nz; iz += 32) {
+        if (mean) {
+            // the (0,0) column keeps its mean vorticity (no projection)
+            update(f00, iz, S1[iz], S2[iz], S3[iz], true);
+            continue;
+        }
+        const float a00 = S1[o00 + iz], a10 = S1[o10 + iz], a01 = S1[o01 + iz], a11 = S1[o11 + iz];
+        const float b00 = S2[o00 + iz], b10 = S2[o10 + iz], b01 = S2[o01 + iz], b11 = S2[o11 + iz];
+        const float e00 = es[o00 + iz], e10 = es[o10 + iz], e01 = es[o01 + iz], e11 = es[o11 + iz];
+        // ds = D_x S2 - D_y S1 at the four members (k_v2v_ds)
+        const float d00 = cxa * b10 - cya * a01, d10 = cxb * b00 - cya * a11;
+        const float d01 = cxa * b11 - cyb * a00, d11 = cxb * b01 - cyb * a10;
+        // projected S1, S2 (k_v2v_orbit with e = es, f = ds)
+        update(f00, o00 + iz, k00 * (cxa * e10 + cya * d01), k00 * (cya * e01 - cxa * d10), S3[o00 + iz], false);
+        if (dx)
+            update(f10, o10 + iz, k10 * (cxb * e00 + cya * d11), k10 * (cya * e11 - cxb * d00), S3[o10 + iz],
+                   false);
+        if (dy)
+            update(f01, o01 + iz, k01 * (cxa * e11 + cyb * d00), k01 * (cyb * e00 - cxa * d11), S3[o01 + iz],
+                   false);
+        if (dx && dy)
+            update(f11, o11 + iz, k11 * (cxb * e01 + cyb * d10), k11 * (cyb * e10 - cxb * d01), S3[o11 + iz],
+                   false);
+    }
+}
+
+void op_stage_orbit(const Dims &d, cudaStream_t st, int sub, const Deriv &D, const double *k2l2i, const float *S,
+                    const float *es, double *q, float *acc, float *q32, double *mf, const double *fp,
+                    const double *fm, const double *dtp)
+{
+    const dim3 g = orbit_grid(d);
+    switch (sub) {
+    case 1: k_stage_orbit<1><<<g, COL_BLOCK, 0, st>>>(d, D, k2l2i, S, es, q, acc, q32, mf, fp, fm, dtp); break;
+    case 2: k_stage_orbit<2><<<g, COL_BLOCK, 0, st>>>(d, D, k2l2i, S, es, q, acc, q32, mf, fp, fm, dtp); break;
+    case 3: k_stage_orbit<3><<<g, COL_BLOCK, 0, st>>>(d, D, k2l2i, S, es, q, acc, q32, mf, fp, fm, dtp); break;
+    default: k_stage_orbit<4><<<g, COL_BLOCK, 0, st>>>(d, D, k2l2i, S, es, q, acc, q32, mf, fp, fm, dtp); break;
+    }
+}
+
 // Host-layout state (nz+1 values per column, the three components one after
 // another) <-> the device's P-pitched columns, FP64.  The unpack raises
 // *changed when any element differs bitwise from the device state it

@@ -85,6 +85,15 @@ struct ps3d_gpu_ctx {
     double *svor = nullptr, *svori = nullptr, *svorf = nullptr, *vortsm = nullptr;
     double *stage64 = nullptr;   // FP64 staging field for mixed-precision transfers
     float *svor32 = nullptr;     // FP32 copy of svor read by the mixed vor2vel
+    // mixed form: es = decompose(diffz(svorts(3))), the z part of the
+    // tendency's solenoidal projection, left by source for the fused stage
+    // update; the FP64 (0,0) column of the current stage state (components
+    // 1 and 2, pitch P), read by the mean-flow inversion while the FP64
+    // state still holds the step's initial state (mf_a: where vor2vel reads
+    // that column from; null = svor itself)
+    float *es_src = nullptr;
+    double *mf64 = nullptr;
+    const double *mf_a = nullptr;
     // transient fields (storage type T)
     void *vor = nullptr, *vel = nullptr, *svel = nullptr, *svorts = nullptr, *held = nullptr;
     void *tmp = nullptr;         // NTMP consecutive fields
@@ -424,34 +433,40 @@ template <typename T> int vor2vel_mixed(ps3d_gpu_ctx *c)
         op_v2v_wfinish<T>(d, c->st, dsg, bs, as, svel + 2 * N, es);
         c->launches += 2;
     }
-    op_v2v_meanflow<double>(d, c->st, A, B, c->tables(), c->ubar, c->vbar);
+    // the (0,0) column of the stage state: FP64 (mf64) inside a step
+    const double *mA = c->mf_a ? c->mf_a : A, *mB = c->mf_a ? c->mf_a + d.P : B;
+    op_v2v_meanflow<double>(d, c->st, mA, mB, c->tables(), c->ubar, c->vbar);
     op_v2v_uv<T>(d, c->st, D, c->k2l2i, es, cs, c->ubar, c->vbar, svel, svel + N);
     c->launches += 3;
     for (int k = 0; k < 3; ++k) xyi<T>(c, svel + k * N, vel + k * N);
     return check(c, "vor2vel");
 }
 
-// Projection of a source term (mixed form): the same operator as the
-// vor2vel projection, applied to svorts in FP32.
-template <typename T> void project_source(ps3d_gpu_ctx *c)
+// The tail of the mixed source: the three tendency components decomposed
+// (field_decompose_semi_spectral, inversion_utils.f90:614-647) and es =
+// decompose(central_diffz(S3)), the z part of the tendency's solenoidal
+// projection (inversion.f90:41-47), for the fused stage update.  The
+// tendency itself stays unprojected, as the reference's source leaves it.
+template <typename T> void source_decompose_mixed(ps3d_gpu_ctx *c)
 {
     const Dims &d = c->d;
     const long long N = d.nfield;
     T *S1 = tf<T>(c->svorts), *S2 = S1 + N, *S3 = S1 + 2 * N;
-    T *cs = tmpf<T>(c, 0), *es = tmpf<T>(c, 1), *ds = tmpf<T>(c, 2);
-    op_v2v_ds<T, T>(d, c->st, c->D(), S1, S2, ds);
+    T *es = reinterpret_cast<T *>(c->es_src);
+    col<T>(c, COL_DECOMP, S1, S1);
+    col<T>(c, COL_DECOMP, S2, S2);
     if (colz_supported(d.nz)) {
-        columns_proj(d, c->st, reinterpret_cast<const float *>(S3), reinterpret_cast<float *>(es), c->k2l2,
-                     (float)c->dx[2], (float)c->cfg.extent[2], c->twz32, c->sinz32, &c->probe);
+        columns_dec2(d, c->st, reinterpret_cast<const float *>(S3), reinterpret_cast<float *>(S3),
+                     reinterpret_cast<float *>(es), c->k2l2, (float)c->dx[2], (float)c->cfg.extent[2], c->twz32,
+                     c->sinz32, &c->probe);
         c->launches += 1;
     } else {
-        col<T>(c, COL_COMBINE, S3, cs);
-        op_diffz<T>(d, c->st, c->dzi, cs, es);
-        col<T>(c, COL_DECOMP, es, es);
+        T *g = tmpf<T>(c, 0);
+        op_diffz<T>(d, c->st, c->dzi, S3, g);
         c->launches += 1;
+        col<T>(c, COL_DECOMP, g, es);
+        col<T>(c, COL_DECOMP, S3, S3);
     }
-    op_v2v_project<T, T>(d, c->st, c->D(), c->k2l2i, es, ds, S1, S2);
-    c->launches += 2;
 }
 
 // ----------------------------------------------------------------- buoyancy
@@ -646,8 +661,7 @@ template <typename T> int source(ps3d_gpu_ctx *c)
         op_svorts<T>(d, c->st, c->D(), r, q, p, gq, gp, svorts, svorts + N, svorts + 2 * N);
         c->launches += 1;
         if (c->closure) closure_add<T>(c, svorts);
-        for (int k = 0; k < 3; ++k) col<T>(c, COL_DECOMP, svorts + k * N, svorts + k * N);
-        project_source<T>(c);
+        source_decompose_mixed<T>(c);
         return check(c, "source");
     }
     for (int k = 0; k < 5; ++k) {
@@ -789,6 +803,9 @@ template <typename T> int rhs_or_hold(ps3d_gpu_ctx *c)
 {
     if (c->cfg.hold_source) {
         cudaMemcpyAsync(c->svorts, c->held, 3 * c->d.nfield * sizeof(T), cudaMemcpyDeviceToDevice, c->st);
+        if (!c->fp64)
+            cudaMemcpyAsync(c->es_src, tf<T>(c->held) + 3 * c->d.nfield, c->d.nfield * sizeof(T),
+                            cudaMemcpyDeviceToDevice, c->st);
         if (c->cfg.buoyancy)
             cudaMemcpyAsync(c->sbuoys, c->heldb, c->d.nfield * sizeof(T), cudaMemcpyDeviceToDevice, c->st);
         return check(c, "hold");
@@ -817,6 +834,8 @@ template <typename T> int step_rk4(ps3d_gpu_ctx *c, double *t, double dt)
     const bool buoy = c->cfg.buoyancy != 0;
     if (c->cfg.hold_source) {
         cudaMemcpyAsync(c->held, c->svorts, 3 * N * sizeof(T), cudaMemcpyDeviceToDevice, c->st);
+        if (!c->fp64)
+            cudaMemcpyAsync(tf<T>(c->held) + 3 * N, c->es_src, N * sizeof(T), cudaMemcpyDeviceToDevice, c->st);
         if (buoy) cudaMemcpyAsync(c->heldb, c->sbuoys, N * sizeof(T), cudaMemcpyDeviceToDevice, c->st);
     }
     op_rk4_factors(d, c->st, c->vdiss, c->filt0, c->epq, c->emq, c->epq2, c->emq2);
@@ -839,15 +858,27 @@ template <typename T> int step_rk4(ps3d_gpu_ctx *c, double *t, double dt)
             op_rk4_sub1<T>(d, c->st, c->sbuoy, c->sbuoyi, c->sbuoyf, sb, c->filt0, c->bmq, dt2, dt6);
         c->launches += 1;
     }
-    for (int k = 0; k < 3; ++k) {
-        if (mixed)
-            op_rk4m_sub1(d, c->st, c->svor + k * N, c->svori + k * N, acc + k * N, s32 + k * N, q32 + k * N,
-                         c->filt0, c->emq, dtp);
-        else
+    // the mixed form: projection, filter and stage update in one pass per
+    // substep (op_stage_orbit); the FP64 state keeps the step's initial
+    // state until substep 4, and vor2vel reads the stage state's (0,0)
+    // column from mf64 meanwhile
+    struct MeanFlowSource {
+        ps3d_gpu_ctx *c;
+        ~MeanFlowSource() { c->mf_a = nullptr; }
+    } mf_guard{c};
+    auto stage = [&](int sub, const double *fp, const double *fm) {
+        op_stage_orbit(d, c->st, sub, c->D(), c->k2l2i, s32, c->es_src, c->svor, acc, q32, c->mf64, fp, fm, dtp);
+        c->launches += 1;
+        c->mf_a = sub < 4 ? c->mf64 : nullptr;
+    };
+    if (mixed) {
+        stage(1, c->filt0, c->emq);
+    } else {
+        for (int k = 0; k < 3; ++k)
             op_rk4_sub1<T>(d, c->st, c->svor + k * N, c->svori + k * N, c->svorf + k * N, sv + k * N, c->filt0,
                            c->emq, dt2, dt6);
+        c->launches += 3;
     }
-    c->launches += 3;
     int rc = rhs_or_hold<T>(c);
     if (rc) return rc;
     if (t) *t += dt2;
@@ -858,15 +889,14 @@ template <typename T> int step_rk4(ps3d_gpu_ctx *c, double *t, double dt)
             op_rk4_sub23<T>(d, c->st, c->sbuoy, c->sbuoyi, c->sbuoyf, sb, c->bpq, c->bmq, dt2, dt3);
         c->launches += 1;
     }
-    for (int k = 0; k < 3; ++k) {
-        if (mixed)
-            op_rk4m_sub23(d, c->st, c->svor + k * N, c->svori + k * N, acc + k * N, s32 + k * N, q32 + k * N,
-                          c->epq, c->emq, dtp, false);
-        else
+    if (mixed) {
+        stage(2, c->epq, c->emq);
+    } else {
+        for (int k = 0; k < 3; ++k)
             op_rk4_sub23<T>(d, c->st, c->svor + k * N, c->svori + k * N, c->svorf + k * N, sv + k * N, c->epq,
                             c->emq, dt2, dt3);
+        c->launches += 3;
     }
-    c->launches += 3;
     rc = rhs_or_hold<T>(c);
     if (rc) return rc;
     if (t) *t += dt2;
@@ -877,15 +907,14 @@ template <typename T> int step_rk4(ps3d_gpu_ctx *c, double *t, double dt)
             op_rk4_sub23<T>(d, c->st, c->sbuoy, c->sbuoyi, c->sbuoyf, sb, c->bpq, c->bmq2, dt, dt3);
         c->launches += 1;
     }
-    for (int k = 0; k < 3; ++k) {
-        if (mixed)
-            op_rk4m_sub23(d, c->st, c->svor + k * N, c->svori + k * N, acc + k * N, s32 + k * N, q32 + k * N,
-                          c->epq, c->emq2, dtp, true);
-        else
+    if (mixed) {
+        stage(3, c->epq, c->emq2);
+    } else {
+        for (int k = 0; k < 3; ++k)
             op_rk4_sub23<T>(d, c->st, c->svor + k * N, c->svori + k * N, c->svorf + k * N, sv + k * N, c->epq,
                             c->emq2, dt, dt3);
+        c->launches += 3;
     }
-    c->launches += 3;
     rc = rhs_or_hold<T>(c);
     if (rc) return rc;
     if (buoy) {
@@ -895,14 +924,13 @@ template <typename T> int step_rk4(ps3d_gpu_ctx *c, double *t, double dt)
             op_rk4_sub4<T>(d, c->st, c->sbuoy, c->sbuoyf, sb, c->bpq2, c->bmq2, dt6);
         c->launches += 1;
     }
-    for (int k = 0; k < 3; ++k) {
-        if (mixed)
-            op_rk4m_sub4(d, c->st, c->svor + k * N, c->svori + k * N, acc + k * N, s32 + k * N, q32 + k * N,
-                         c->epq2, c->emq2, dtp);
-        else
+    if (mixed) {
+        stage(4, c->epq2, c->emq2);
+    } else {
+        for (int k = 0; k < 3; ++k)
             op_rk4_sub4<T>(d, c->st, c->svor + k * N, c->svorf + k * N, sv + k * N, c->epq2, c->emq2, dt6);
+        c->launches += 3;
     }
-    c->launches += 3;
     op_mean_fix(d, c->st, c->svor, c->dstsum, c->fnzi, c->ini, nullptr, 1, c->svor32);
     c->launches += 1;
     return check(c, "step");
@@ -1568,7 +1596,8 @@ template <typename T> int allocate_fields(ps3d_gpu_ctx *c)
               dalloc(c, &c->phip, fb) && dalloc(c, &c->thetam, fb) && dalloc(c, &c->thetap, fb) &&
               dalloc(c, &c->dthetam, fb) && dalloc(c, &c->dthetap, fb) && dalloc(c, &c->green, fb);
     if (ok && c->cfg.stepper == PS3D_CN2) ok = dalloc(c, &c->vortsm, 3 * f64);
-    if (ok && c->cfg.hold_source) ok = dalloc(c, &c->held, 3 * fb);
+    // the mixed form holds es beside the three tendency components
+    if (ok && c->cfg.hold_source) ok = dalloc(c, &c->held, (c->fp64 ? 3 : 4) * fb);
     if (ok && c->cfg.buoyancy) {
         const size_t P2b = (size_t)d.ncol * sizeof(double);
         ok = dalloc(c, &c->sbuoy, f64) && dalloc(c, &c->sbuoyi, f64) && dalloc(c, &c->sbuoyf, f64) &&
@@ -1589,7 +1618,8 @@ template <typename T> int allocate_fields(ps3d_gpu_ctx *c)
         }
     }
     if (ok && !c->fp64)
-        ok = dalloc(c, &c->svor32, 3 * N * sizeof(float)) &&
+        ok = dalloc(c, &c->svor32, 3 * N * sizeof(float)) && dalloc(c, &c->es_src, N * sizeof(float)) &&
+             dalloc(c, &c->mf64, 2 * (size_t)d.P * sizeof(double)) &&
              dalloc(c, &c->twz32, d.nz * sizeof(float2)) && dalloc(c, &c->sinz32, d.nz * sizeof(float)) &&
              dalloc(c, &c->cosz32, d.nz * sizeof(float)) &&
              dalloc(c, &c->stage64, f64) && dalloc(c, &c->phim64, f64) && dalloc(c, &c->phip64, f64) &&

@@ -12,7 +12,8 @@ For each combination: the filter and hyperdiffusion tables and the initial
 energy after setup_fields, adapt's time step and diagnostics at t = 0, and 20
 impl-diff-rk4 steps with dt, the rolling mean and the prefactor compared per
 step and the state at the end.  Tolerances: FP64 1e-12 (state), 1e-11
-(diagnostics); mixed form 1e-6 (solenoidal state), 2e-5 (diagnostics).  The
+(diagnostics), 1e-10 (initial energy); mixed form 1e-6 (solenoidal state),
+2e-5 (diagnostics), 2e-6 (initial energy, from the FP32 fields).  The
 captured (CUDA-graph) step of the mixed form runs the prefactor logic on the
 device; it is checked bitwise against the host-driven step for every pretype.
 """
@@ -28,8 +29,8 @@ pytestmark = pytest.mark.gpu
 PRETYPES = ["constant", "vorch", "max-strain", "us-max-strain", "roll-mean-max-strain"]
 FILTERS = ["Hou & Li", "2/3-rule"]
 LENGTHS = ["Kolmogorov", "geophysical"]
-TOL = {"fp64": dict(state=1e-12, diag=1e-11, table=1e-13),
-       "mixed": dict(state=1e-6, diag=2e-5, table=1e-13)}
+TOL = {"fp64": dict(state=1e-12, diag=1e-11, table=1e-13, energy=1e-10),
+       "mixed": dict(state=1e-6, diag=2e-5, table=1e-13, energy=2e-6)}
 
 
 def _pair(n, precision, **kw):
@@ -49,10 +50,12 @@ def _pair(n, precision, **kw):
 def test_option_branches_match_oracle(pretype, filtering, length_scale, precision):
     tol = TOL[precision]
     o, g, eo, eg = _pair(32, precision, pretype=pretype, filtering=filtering, length_scale=length_scale)
+    # initial energy and enstrophy (FP32 velocity and vorticity in the mixed form)
     for a, b in zip(eg, eo):
-        assert abs(a - b) <= 1e-10 * abs(b)
-    for name in ("filt", "vhdis"):
-        assert rel_l2(g.table(name), o.table(name)) < tol["table"], name
+        assert abs(a - b) <= tol["energy"] * abs(b), (a, b)
+    assert rel_l2(g.table("filt"), o.table("filt")) < tol["table"]
+    # the Kolmogorov viscosity scales with (te/en)^(1/3) of the set-up fields
+    assert rel_l2(g.table("vhdis"), o.table("vhdis")) < tol["energy"]
     dtg, dg = g.adapt(0.0)
     dto, do = o.adapt(0.0)
     assert abs(dtg - dto) <= tol["diag"] * dto

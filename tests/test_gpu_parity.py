@@ -261,11 +261,14 @@ MIXED_GRIDS = [(32, 32, 64), (16, 16, 128), (16, 8, 256), (8, 8, 512)]
 @pytest.mark.parametrize("grid", MIXED_GRIDS, ids=lambda g: "x".join(map(str, g)))
 def test_mixed_vor2vel_and_source_match_oracle(grid):
     """Mixed-form vor2vel (fused vertical-velocity column kernel) and
-    source (fused z projection of the tendency) against the FP64 oracle on
-    the same state: velocity and vorticity within 2e-6, the tendency within
-    2e-4.  The tendency of a near-Beltrami flow is a difference of nearly
-    equal products: rounding vel and vor alone to FP32 moves the oracle's
-    tendency by about 1e-5 (relative L2) at these sizes."""
+    source (the tendency's decompositions, the third fused with the z part
+    of its solenoidal projection) against the FP64 oracle on the same state:
+    velocity and vorticity within 2e-6, the tendency within 2e-4.  The
+    tendency of a near-Beltrami flow is a difference of nearly equal
+    products: rounding vel and vor alone to FP32 moves the oracle's tendency
+    by about 1e-5 (relative L2) at these sizes.  Like the reference's source,
+    the mixed source leaves the tendency unprojected; the projection happens
+    in the stage update."""
     nx, ny, nz = grid
     lo, ex = ic.BELTRAMI_BOX["lower"], ic.BELTRAMI_BOX["extent"]
     vor, pert = ic.beltrami_plus_perturbation(nx, ny, nz, seed=5, amplitude=1.0e-2)
@@ -284,25 +287,8 @@ def test_mixed_vor2vel_and_source_match_oracle(grid):
         assert err < tol, (name, err)
     o.source()
     g.source()
-    err = rel_l2(g.get("svorts"), _project_like_vor2vel(o, o.get("svorts")))
+    err = rel_l2(g.get("svorts"), o.get("svorts"))
     assert err < 2.0e-4, err
-
-
-def _project_like_vor2vel(o, S):
-    """The solenoidal projection of vor2vel (inversion.f90:34-76) applied to a
-    spectral vector field with the oracle's operators.  The mixed form
-    projects each tendency (the FP64 form projects the state at the next
-    vor2vel instead; both reach the same projected state), so its svorts is
-    compared with the projected oracle tendency."""
-    k = o.table("k2l2i")[:, :, None]
-    S1, S2, S3 = S
-    ds = o.diffx(S2) - o.diffy(S1)
-    es = o.decompose_semi_spectral(o.central_diffz(o.combine_semi_spectral(S3)))
-    P1 = k * (o.diffx(es) + o.diffy(ds))
-    P2 = k * (o.diffy(es) - o.diffx(ds))
-    P1[0, 0, :] = S1[0, 0, :]
-    P2[0, 0, :] = S2[0, 0, :]
-    return np.stack([P1, P2, S3])
 
 
 @pytest.mark.parametrize("n", [64])
@@ -480,3 +466,24 @@ def test_mixed_steps_other_steppers_and_shapes(grid, stepper):
     err = rel_l2(g.get("svor"), o.get("svor"))
     assert err < 1.0e-6, err
     assert abs(t_g - t_o) <= 1e-6 * t_o
+
+
+@pytest.mark.parametrize("n", [32, 64])
+def test_mixed_held_source_step_matches_oracle(n):
+    """hold_source in the mixed form: the source of the first right-hand side
+    (with the z part of its projection) is held over the four substeps; the
+    stepped state against the oracle's within 1e-6 (32^3: the
+    shared-memory column transforms, 64^3: the warp column kernels)."""
+    lo, ex, vor, pert = beltrami_case(n, seed=13, amplitude=1e-2)
+    o = oracle.Oracle(n, n, n, lo, ex, hold_source=1)
+    g = Ps3dGpu(n, n, n, lo, ex, hold_source=1, precision="mixed")
+    o.setup_fields(vor, pert)
+    g.setup_fields(vor, pert)
+    for m in (o, g):
+        m.vor2vel()
+        m.source()
+        dt, _ = m.adapt(0.0)
+        m.step(0.0, dt)
+        m.vor2vel()
+    err = rel_l2(g.get("svor"), o.get("svor"))
+    assert err < 1.0e-6, err
