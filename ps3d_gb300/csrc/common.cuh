@@ -5,6 +5,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <type_traits>
+
 namespace ps3d {
 
 template <typename T> struct cplx;
@@ -78,16 +80,61 @@ template <bool INV, typename C> __device__ __forceinline__ void dft8(C *v)
     v[7] = csub(e3, o3);
 }
 
+// radix 3: X1, X2 = m -/+ i (sqrt3/2) (a1 - a2), m = a0 - (a1 + a2)/2
+// (forward; the inverse swaps the signs of the imaginary terms)
+template <bool INV, typename C> __device__ __forceinline__ void dft3(C *v)
+{
+    using R = decltype(C::x);
+    const R h = (R)0.86602540378443864676372317075293618347140262690519;  // sqrt(3)/2
+    const C t1 = cadd(v[1], v[2]), t2 = csub(v[1], v[2]);
+    const C m = mk<C>(v[0].x - (R)0.5 * t1.x, v[0].y - (R)0.5 * t1.y);
+    // -i h t2 (forward) or +i h t2 (inverse)
+    const C s = INV ? mk<C>(-h * t2.y, h * t2.x) : mk<C>(h * t2.y, -h * t2.x);
+    v[0] = cadd(v[0], t1);
+    v[1] = cadd(m, s);
+    v[2] = csub(m, s);
+}
+
+// radix 5 from the real and imaginary parts of w = exp(-2 pi i / 5):
+// t1 = a1 + a4, t2 = a2 + a3, t3 = a1 - a4, t4 = a2 - a3,
+// X1, X4 = (a0 + c1 t1 + c2 t2) -/+ i (s1 t3 + s2 t4),
+// X2, X3 = (a0 + c2 t1 + c1 t2) -/+ i (s2 t3 - s1 t4),
+// c1 = cos(2 pi/5), c2 = cos(4 pi/5), s1 = sin(2 pi/5), s2 = sin(4 pi/5)
+template <bool INV, typename C> __device__ __forceinline__ void dft5(C *v)
+{
+    using R = decltype(C::x);
+    const R c1 = (R)0.30901699437494742410229341718281905886436448684277;
+    const R c2 = (R)-0.80901699437494742410229341718281905886436448684277;
+    const R s1 = (R)0.95105651629515357211643933337938214340569863412575;
+    const R s2 = (R)0.58778525229247312916870595463907276859765243764314;
+    const C t1 = cadd(v[1], v[4]), t2 = cadd(v[2], v[3]), t3 = csub(v[1], v[4]), t4 = csub(v[2], v[3]);
+    const C m1 = mk<C>(v[0].x + c1 * t1.x + c2 * t2.x, v[0].y + c1 * t1.y + c2 * t2.y);
+    const C m2 = mk<C>(v[0].x + c2 * t1.x + c1 * t2.x, v[0].y + c2 * t1.y + c1 * t2.y);
+    const C n1 = mk<C>(s1 * t3.x + s2 * t4.x, s1 * t3.y + s2 * t4.y);
+    const C n2 = mk<C>(s2 * t3.x - s1 * t4.x, s2 * t3.y - s1 * t4.y);
+    // -i n (forward) or +i n (inverse)
+    const C j1 = INV ? mk<C>(-n1.y, n1.x) : mk<C>(n1.y, -n1.x);
+    const C j2 = INV ? mk<C>(-n2.y, n2.x) : mk<C>(n2.y, -n2.x);
+    v[0] = cadd(v[0], cadd(t1, t2));
+    v[1] = cadd(m1, j1);
+    v[4] = csub(m1, j1);
+    v[2] = cadd(m2, j2);
+    v[3] = csub(m2, j2);
+}
+
 template <int R, bool INV, typename C> __device__ __forceinline__ void dft(C *v)
 {
     if (R == 2) dft2<INV>(v[0], v[1]);
+    else if (R == 3) dft3<INV>(v);
     else if (R == 4) dft4<INV>(v[0], v[1], v[2], v[3]);
+    else if (R == 5) dft5<INV>(v);
     else dft8<INV>(v);
 }
 
 // One Stockham autosort pass of radix R over B interleaved sequences of
 // length n held in shared memory as buf[j*B + b].  Ns is the product of the
-// radices already applied.  tw[k] = exp(-2 pi i k / n).
+// radices already applied (any order of the factors of n).
+// tw[k] = exp(-2 pi i k / n).
 template <int R, bool INV, typename C>
 __device__ __forceinline__ void stockham_pass(const C *__restrict__ src, C *__restrict__ dst, int n,
                                               int logB, int Ns, const C *__restrict__ tw)
@@ -99,7 +146,7 @@ __device__ __forceinline__ void stockham_pass(const C *__restrict__ src, C *__re
     for (int g = threadIdx.x; g < nbf; g += blockDim.x) {
         const int b = g & (B - 1);
         const int j = g >> logB;
-        const int k = j & (Ns - 1);
+        const int k = ((Ns & (Ns - 1)) == 0) ? (j & (Ns - 1)) : (j % Ns);
         C v[R];
 #pragma unroll
         for (int r = 0; r < R; ++r) v[r] = src[((j + r * nR) << logB) + b];
@@ -118,32 +165,43 @@ __device__ __forceinline__ void stockham_pass(const C *__restrict__ src, C *__re
     }
 }
 
-// Complex FFT of B = 2^logB interleaved sequences of length n (a power of two,
-// 2..4096) in shared memory; buf0 holds the input, the result ends in the
-// returned buffer (buf0 or buf1).  All threads of the block take part; the
-// caller synchronises before the call.
+// Complex FFT of B = 2^logB interleaved sequences of length n = 2^a 3^b 5^c
+// (2..4096) in shared memory: radix-8 passes while 8 divides what is left,
+// one radix-4 or radix-2 pass for the rest of the power of two, then the
+// radix-3 and radix-5 passes (the factorisation of stafft.f90:128-187, in
+// its own order).  buf0 holds the input, the result ends in the returned
+// buffer (buf0 or buf1).  All threads of the block take part; the caller
+// synchronises before the call.
 template <bool INV, typename C>
 __device__ C *smem_fft(C *buf0, C *buf1, int n, int logB, const C *__restrict__ tw)
 {
     C *s = buf0, *d = buf1;
     int Ns = 1, rem = n;
-    while (rem >= 8) {
-        stockham_pass<8, INV>(s, d, n, logB, Ns, tw);
+    auto step = [&](auto radix) {
+        constexpr int R = decltype(radix)::value;
+        stockham_pass<R, INV>(s, d, n, logB, Ns, tw);
         __syncthreads();
-        C *t = s; s = d; d = t;
-        Ns *= 8;
-        rem /= 8;
-    }
-    if (rem == 4) {
-        stockham_pass<4, INV>(s, d, n, logB, Ns, tw);
-        __syncthreads();
-        C *t = s; s = d; d = t;
-    } else if (rem == 2) {
-        stockham_pass<2, INV>(s, d, n, logB, Ns, tw);
-        __syncthreads();
-        C *t = s; s = d; d = t;
-    }
+        C *t = s;
+        s = d;
+        d = t;
+        Ns *= R;
+        rem /= R;
+    };
+    while (rem % 8 == 0) step(std::integral_constant<int, 8>());
+    if (rem % 4 == 0) step(std::integral_constant<int, 4>());
+    else if (rem % 2 == 0) step(std::integral_constant<int, 2>());
+    while (rem % 3 == 0) step(std::integral_constant<int, 3>());
+    while (rem % 5 == 0) step(std::integral_constant<int, 5>());
     return s;
+}
+
+// n = 2^a 3^b 5^c
+__host__ __device__ inline bool radix235(int n)
+{
+    if (n < 1) return false;
+    for (int p : {2, 3, 5})
+        while (n % p == 0) n /= p;
+    return n == 1;
 }
 
 __host__ __device__ inline int ilog2(int v)

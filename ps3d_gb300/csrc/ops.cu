@@ -800,79 +800,99 @@ template <int SUB> struct StageCol {
         }
     }
     // one element: s the projected source, q0 the step's initial state
-    __device__ __forceinline__ double apply(float s, double q0, float *acc) const
+    __device__ __forceinline__ double apply(float s, double q0, float &acc) const
     {
-        if (SUB == 4) return fma(q0, m, widen64(fmaf(*acc, a, b * s)));
+        if (SUB == 4) return fma(q0, m, widen64(fmaf(acc, a, b * s)));
         const float fs = a * s;
         const double qn = fma(q0, m, widen64(b * fs));
-        *acc = (SUB == 1) ? c * fs : fmaf(c, fs, *acc);
+        acc = (SUB == 1) ? c * fs : fmaf(c, fs, acc);
         return qn;
     }
 };
 
+// One block of four warps per partner orbit, warp w on member (x partner if
+// w & 1, y partner if w & 2) over 32 levels at a time: the members' S1, S2,
+// es and then ds meet in shared memory (two buffers, alternating), so each
+// value is read from HBM once and every warp keeps only its own column in
+// registers.  All global loads of the next 32 levels are issued before the
+// current levels' barriers.
+template <int SUB> struct StageLoads {
+    float a, b, e, s3, acc[3];
+    double q[3];
+};
+
 template <int SUB>
-__global__ void k_stage_orbit(Dims d, Deriv D, const double *__restrict__ k2l2i, const float *__restrict__ S,
-                              const float *__restrict__ es, double *__restrict__ q, float *__restrict__ acc,
-                              float *__restrict__ q32, double *__restrict__ mf, const double *__restrict__ fp,
-                              const double *__restrict__ fm, const double *__restrict__ dtp)
+__device__ __forceinline__ void stage_load(StageLoads<SUB> &v, bool on, long long N, long long i,
+                                           const float *__restrict__ S, const float *__restrict__ es,
+                                           const double *__restrict__ q, const float *__restrict__ acc)
 {
+    v.a = on ? S[i] : 0.f;
+    v.b = on ? S[N + i] : 0.f;
+    v.e = on ? es[i] : 0.f;
+    v.s3 = on ? S[2 * N + i] : 0.f;
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        v.q[k] = on ? q[(long long)k * N + i] : 0.0;
+        v.acc[k] = (on && SUB != 1) ? acc[(long long)k * N + i] : 0.f;
+    }
+}
+
+template <int SUB>
+__global__ void __launch_bounds__(128) k_stage_orbit(Dims d, Deriv D, const double *__restrict__ k2l2i,
+                                                     const float *__restrict__ S, const float *__restrict__ es,
+                                                     double *__restrict__ q, float *__restrict__ acc,
+                                                     float *__restrict__ q32, double *__restrict__ mf,
+                                                     const double *__restrict__ fp, const double *__restrict__ fm,
+                                                     const double *__restrict__ dtp)
+{
+    __shared__ float sh_a[2][4][32], sh_b[2][4][32], sh_e[2][4][32], sh_d[2][4][32];
     const int hy = d.ny / 2 + 1;
-    const long long orb = (long long)blockIdx.x * COLS_PER_BLOCK + threadIdx.y;
-    if (orb >= (long long)(d.nx / 2 + 1) * hy) return;
+    const long long orb = blockIdx.x;
     const long long N = d.nfield;
     const int kx = (int)(orb / hy), ky = (int)(orb - (long long)kx * hy);
     const int x2 = xsrc(kx, d.nx), y2 = xsrc(ky, d.ny);
-    const long long c00 = (long long)ky + (long long)d.ny * kx, c10 = (long long)ky + (long long)d.ny * x2;
-    const long long c01 = (long long)y2 + (long long)d.ny * kx, c11 = (long long)y2 + (long long)d.ny * x2;
-    const long long o00 = c00 * d.P, o10 = c10 * d.P, o01 = c01 * d.P, o11 = c11 * d.P;
-    const bool dx = x2 != kx, dy = y2 != ky, mean = c00 == 0;
-    const float cxa = (float)D.cx[kx], cxb = (float)D.cx[x2], cya = (float)D.cy[ky], cyb = (float)D.cy[y2];
-    const float k00 = (float)k2l2i[c00], k10 = (float)k2l2i[c10], k01 = (float)k2l2i[c01],
-                k11 = (float)k2l2i[c11];
-    const double dt = *dtp;
-    StageCol<SUB> f00, f10, f01, f11;
-    f00.make(dt, fp, fm, c00);
-    f10.make(dt, fp, fm, c10);
-    f01.make(dt, fp, fm, c01);
-    f11.make(dt, fp, fm, c11);
-    const float *S1 = S, *S2 = S + N, *S3 = S + 2 * N;
-    // one member column at level i: the three projected components
-    auto update = [&](const StageCol<SUB> &f, long long i, float s1, float s2, float s3, bool mean_col) {
-        const float sv[3] = {s1, s2, s3};
-#pragma unroll
-        for (int k = 0; k < 3; ++k) {
-            const long long ik = (long long)k * N + i;
-            float a = (SUB == 1) ? 0.f : acc[ik];
-            const double qn = f.apply(sv[k], q[ik], &a);
-            if (SUB == 4) q[ik] = qn;
-            else acc[ik] = a;
-            q32[ik] = narrow32(qn);
-            if (mean_col && k < 2) mf[(long long)k * d.P + i] = qn;
-        }
-    };
-    for (int iz = threadIdx.x; iz <= d.nz; iz += 32) {
-        if (mean) {
-            // the (0,0) column keeps its mean vorticity (no projection)
-            update(f00, iz, S1[iz], S2[iz], S3[iz], true);
-            continue;
-        }
-        const float a00 = S1[o00 + iz], a10 = S1[o10 + iz], a01 = S1[o01 + iz], a11 = S1[o11 + iz];
-        const float b00 = S2[o00 + iz], b10 = S2[o10 + iz], b01 = S2[o01 + iz], b11 = S2[o11 + iz];
-        const float e00 = es[o00 + iz], e10 = es[o10 + iz], e01 = es[o01 + iz], e11 = es[o11 + iz];
-        // ds = D_x S2 - D_y S1 at the four members (k_v2v_ds)
-        const float d00 = cxa * b10 - cya * a01, d10 = cxb * b00 - cya * a11;
-        const float d01 = cxa * b11 - cyb * a00, d11 = cxb * b01 - cyb * a10;
+    const bool dx = x2 != kx, dy = y2 != ky;
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const bool active = (!(w & 1) || dx) && (!(w & 2) || dy);
+    const int mx = (w & 1) ? x2 : kx, my = (w & 2) ? y2 : ky;
+    const int xw = dx ? (w ^ 1) : w, yw = dy ? (w ^ 2) : w;  // partner members
+    const long long col = (long long)my + (long long)d.ny * mx, o = col * d.P;
+    const bool mean = col == 0;  // the (0,0) column keeps its mean vorticity
+    const float cx = (float)D.cx[mx], cy = (float)D.cy[my], kk = (float)k2l2i[col];
+    StageCol<SUB> f;
+    f.make(*dtp, fp, fm, col);
+    StageLoads<SUB> cur, nxt;
+    stage_load<SUB>(cur, active && lane <= d.nz, N, o + lane, S, es, q, acc);
+    int buf = 0;
+    for (int z0 = 0; z0 <= d.nz; z0 += 32, buf ^= 1) {
+        const int iz = z0 + lane;
+        const bool on = active && iz <= d.nz;
+        sh_a[buf][w][lane] = cur.a;
+        sh_b[buf][w][lane] = cur.b;
+        sh_e[buf][w][lane] = cur.e;
+        if (z0 + 32 <= d.nz) stage_load<SUB>(nxt, active && iz + 32 <= d.nz, N, o + iz + 32, S, es, q, acc);
+        __syncthreads();
+        // ds = D_x S2 - D_y S1 (k_v2v_ds)
+        sh_d[buf][w][lane] = cx * sh_b[buf][xw][lane] - cy * sh_a[buf][yw][lane];
+        __syncthreads();
         // projected S1, S2 (k_v2v_orbit with e = es, f = ds)
-        update(f00, o00 + iz, k00 * (cxa * e10 + cya * d01), k00 * (cya * e01 - cxa * d10), S3[o00 + iz], false);
-        if (dx)
-            update(f10, o10 + iz, k10 * (cxb * e00 + cya * d11), k10 * (cya * e11 - cxb * d00), S3[o10 + iz],
-                   false);
-        if (dy)
-            update(f01, o01 + iz, k01 * (cxa * e11 + cyb * d00), k01 * (cyb * e00 - cxa * d11), S3[o01 + iz],
-                   false);
-        if (dx && dy)
-            update(f11, o11 + iz, k11 * (cxb * e01 + cyb * d10), k11 * (cyb * e10 - cxb * d01), S3[o11 + iz],
-                   false);
+        const float p1 = mean ? cur.a : kk * (cx * sh_e[buf][xw][lane] + cy * sh_d[buf][yw][lane]);
+        const float p2 = mean ? cur.b : kk * (cy * sh_e[buf][yw][lane] - cx * sh_d[buf][xw][lane]);
+        if (on) {
+            const float sv[3] = {p1, p2, cur.s3};
+            const long long i = o + iz;
+#pragma unroll
+            for (int k = 0; k < 3; ++k) {
+                const long long ik = (long long)k * N + i;
+                float a = cur.acc[k];
+                const double qn = f.apply(sv[k], cur.q[k], a);
+                if (SUB == 4) q[ik] = qn;
+                else acc[ik] = a;
+                q32[ik] = narrow32(qn);
+                if (mean && k < 2) mf[(long long)k * d.P + iz] = qn;
+            }
+        }
+        cur = nxt;
     }
 }
 
@@ -880,12 +900,12 @@ void op_stage_orbit(const Dims &d, cudaStream_t st, int sub, const Deriv &D, con
                     const float *es, double *q, float *acc, float *q32, double *mf, const double *fp,
                     const double *fm, const double *dtp)
 {
-    const dim3 g = orbit_grid(d);
+    const dim3 g((unsigned)((long long)(d.nx / 2 + 1) * (d.ny / 2 + 1)));
     switch (sub) {
-    case 1: k_stage_orbit<1><<<g, COL_BLOCK, 0, st>>>(d, D, k2l2i, S, es, q, acc, q32, mf, fp, fm, dtp); break;
-    case 2: k_stage_orbit<2><<<g, COL_BLOCK, 0, st>>>(d, D, k2l2i, S, es, q, acc, q32, mf, fp, fm, dtp); break;
-    case 3: k_stage_orbit<3><<<g, COL_BLOCK, 0, st>>>(d, D, k2l2i, S, es, q, acc, q32, mf, fp, fm, dtp); break;
-    default: k_stage_orbit<4><<<g, COL_BLOCK, 0, st>>>(d, D, k2l2i, S, es, q, acc, q32, mf, fp, fm, dtp); break;
+    case 1: k_stage_orbit<1><<<g, 128, 0, st>>>(d, D, k2l2i, S, es, q, acc, q32, mf, fp, fm, dtp); break;
+    case 2: k_stage_orbit<2><<<g, 128, 0, st>>>(d, D, k2l2i, S, es, q, acc, q32, mf, fp, fm, dtp); break;
+    case 3: k_stage_orbit<3><<<g, 128, 0, st>>>(d, D, k2l2i, S, es, q, acc, q32, mf, fp, fm, dtp); break;
+    default: k_stage_orbit<4><<<g, 128, 0, st>>>(d, D, k2l2i, S, es, q, acc, q32, mf, fp, fm, dtp); break;
     }
 }
 

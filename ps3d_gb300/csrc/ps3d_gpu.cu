@@ -26,7 +26,6 @@ namespace {
 
 constexpr int NTMP = 6;
 
-bool is_pow2(int v) { return v > 0 && (v & (v - 1)) == 0; }
 
 struct Rolling {
     std::vector<double> hist;
@@ -1732,9 +1731,10 @@ int ps3d_gpu_create(const ps3d_gpu_config *cfg, ps3d_gpu_ctx **out)
     *out = nullptr;
     const int nx = cfg->nx, ny = cfg->ny, nz = cfg->nz;
     const int zmax = cfg->precision == PS3D_PRECISION_FP64 ? 1024 : 2048;
-    if (!is_pow2(nx) || !is_pow2(ny) || !is_pow2(nz) || nx < 8 || ny < 8 || nz < 8 || nx > 2048 || ny > 2048 ||
-        nz > zmax)
-        return PS3D_ERR_UNSUPPORTED_SIZE;
+    // even lengths with factors 2, 3 and 5 only (the factorisation of
+    // stafft.f90:128-187 with its radices 2..6)
+    auto ok_len = [](int n, int lo, int hi) { return n >= lo && n <= hi && n % 2 == 0 && radix235(n); };
+    if (!ok_len(nx, 8, 2048) || !ok_len(ny, 8, 2048) || !ok_len(nz, 8, zmax)) return PS3D_ERR_UNSUPPORTED_SIZE;
     if (cfg->precision != PS3D_PRECISION_FP64 && cfg->precision != PS3D_PRECISION_MIXED) return PS3D_ERR_INVALID_ARG;
     if (cfg->stepper != PS3D_IMPL_DIFF_RK4 && cfg->stepper != PS3D_CN2) return PS3D_ERR_INVALID_ARG;
     if (cfg->pretype < 0 || cfg->pretype > 6 || cfg->nnu < 1 || !(cfg->extent[0] > 0) || !(cfg->extent[1] > 0) ||

@@ -81,7 +81,7 @@ __global__ void __launch_bounds__(256) k_lines(const T *__restrict__ in, T *__re
             const int k = e >> logB, p = e & (B - 1);
             if (z0 + 2 * p >= P) continue;
             const C ck = res[(k << logB) + p];
-            const C cn = res[(((n - k) & (n - 1)) << logB) + p];
+            const C cn = res[((k == 0 ? 0 : n - k) << logB) + p];
             const T are = half * (ck.x + cn.x), aim = half * (ck.y - cn.y);
             const T bre = half * (ck.y + cn.y), bim = -half * (ck.x - cn.x);
             outC[(base + k * line_stride + 2 * p) >> 1] = mk<C>(are * s, bre * s);

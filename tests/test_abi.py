@@ -41,13 +41,29 @@ def test_strerror_codes():
     assert L.ps3d_gpu_strerror(999) == b"unknown status"
 
 
-@pytest.mark.parametrize("dims", [(30, 32, 32), (32, 32, 12), (4, 32, 32), (4096, 8, 8)])
+@pytest.mark.parametrize("dims", [(14, 32, 32), (32, 32, 15), (32, 22, 32), (4, 32, 32), (4096, 8, 8),
+                                  (32, 32, 2048)])
 def test_unsupported_sizes_rejected_before_device(dims):
+    """Lengths must be even with factors 2, 3 and 5 only (the factorisation of
+    stafft.f90:128-187), 8..2048 (z up to 1024 in FP64)."""
     L = _lib.lib()
     cfg = make_config(*dims, [0, 0, 0], [1, 1, 1])
     h = ctypes.c_void_p()
     assert L.ps3d_gpu_create(ctypes.byref(cfg), ctypes.byref(h)) == 2  # UNSUPPORTED_SIZE
     assert not h.value
+
+
+@pytest.mark.parametrize("dims", [(30, 32, 32), (32, 32, 12), (48, 40, 24), (384, 8, 96)])
+def test_mixed_radix_sizes_pass_the_size_check(dims):
+    """n = 2^a 3^b 5^c passes the size check: without a device the call gets
+    as far as the device query (NO_DEVICE); with one it creates a context."""
+    L = _lib.lib()
+    cfg = make_config(*dims, [0, 0, 0], [1, 1, 1])
+    h = ctypes.c_void_p()
+    rc = L.ps3d_gpu_create(ctypes.byref(cfg), ctypes.byref(h))
+    assert rc in (0, 8), rc
+    if rc == 0:
+        L.ps3d_gpu_destroy(h)
 
 
 def test_invalid_config_rejected():
