@@ -252,6 +252,32 @@ def closure_timing(dev, n=64):
         return {"unavailable": str(e)[:200]}
 
 
+def batch_timing(steps, warmup=3):
+    """The batched workload: 96 independent runs of uneven sizes (48 x 32^3,
+    32 x 64^3, 16 x 128^3), each Beltrami plus its own seeded perturbation
+    (amplitude log-uniform in [1e-4, 1e-2]) and prediss from {10, 30, 60,
+    90}, mixed form; every batch step is one CUDA graph with one persistent
+    launch per stage update for all runs (ps3d_gpu_batch_advance)."""
+    try:
+        from ps3d_gb300 import batch_advance, batch_case
+        counts = [(32, 48), (64, 32), (128, 16)]
+        runs = batch_case.build(counts, seed=7)
+        models = [r[3] for r in runs]
+        pts = sum(n ** 3 for n, _, _, _ in runs)
+        ts = [0.0] * len(models)
+        ts, _ = batch_advance(models, ts, warmup)
+        ts, ms = batch_advance(models, ts, steps)
+        out = {"runs": len(models), "counts": {f"{n}^3": c for n, c in counts}, "points_per_step": pts,
+               "steps": steps, "ms_per_step": ms / steps, "value": pts * steps / (ms * 1e-3) / 1e6,
+               "unit": "Mpts*steps/s",
+               "how": "one CUDA graph per batch step; one persistent stage-update launch per RK stage"}
+        for m in models:
+            m.close()
+        return out
+    except Exception as e:
+        return {"unavailable": str(e)[:200]}
+
+
 def cpu_sample(n_cpu, steps=1):
     """Time the CPU oracle: `steps` advances at n_cpu^3 after one warm-up."""
     import oracle
@@ -435,6 +461,7 @@ def run_gpu(args, rank, world, dist):
             cufft["ours_xy_pass_pair_ms"] = ours
 
     closure = closure_timing(dev) if rank == 0 and not args.skip_closure else None
+    batch = batch_timing(args.batch_steps) if rank == 0 and not args.skip_batch else None
 
     cpu = None
     if rank == 0 and not args.skip_cpu:
@@ -459,6 +486,7 @@ def run_gpu(args, rank, world, dist):
             "line_fft_autotune": dict(zip(("shape", "ms_per_launch"), gm.tuning())),
             "cufft_comparator": cufft,
             "closure": closure,
+            "batch": batch,
         }
         print(json.dumps(line), flush=True)
     gm.close()
@@ -509,6 +537,8 @@ def main():
     ap.add_argument("--skip-e2e", action="store_true")
     ap.add_argument("--skip-cpu", action="store_true")
     ap.add_argument("--skip-closure", action="store_true")
+    ap.add_argument("--skip-batch", action="store_true")
+    ap.add_argument("--batch-steps", type=int, default=500)
     args = ap.parse_args()
     if args.warmup < 3:
         log("[bench] warm-up raised to 3 steps")

@@ -199,6 +199,25 @@ void op_narrow(cudaStream_t st, const double *in, float *out, long long n);
 void op_stage_orbit(const Dims &d, cudaStream_t st, int sub, const Deriv &D, const double *k2l2i, const float *S,
                     const float *es, double *q, float *acc, float *q32, double *mf, const double *fp,
                     const double *fm, const double *dtp);
+// one run of a batch for op_batch_stage: the arguments of op_stage_orbit,
+// the column factors of the four substeps, and the number of the run's
+// first work item (one item per partner orbit, runs numbered in order)
+struct StageRun {
+    Dims d;
+    Deriv D;
+    const double *k2l2i;
+    const float *S, *es;
+    double *q;
+    float *acc, *q32;
+    double *mf;
+    const double *fp[4], *fm[4];
+    const double *dtp;
+    long long item0;
+};
+// the stage update of every run of a batch in one persistent launch
+// (runs: device array of nruns entries; nitems: all runs' orbits)
+void op_batch_stage(cudaStream_t st, int sub, const StageRun *runs, int nruns, long long nitems, int blocks);
+int batch_stage_blocks();
 // derived fields (pressure right-hand side, table product, horizontal divergence)
 template <typename T> void op_pressure_rhs(const Dims &d, cudaStream_t st, const T *g5, const T *vor, T *out);
 template <typename T> void op_mul_field(const Dims &d, cudaStream_t st, const T *tab, T *f);

@@ -837,17 +837,24 @@ __device__ __forceinline__ void stage_load(StageLoads<SUB> &v, bool on, long lon
     }
 }
 
+struct StageShared {
+    float a[2][4][32], b[2][4][32], e[2][4][32], d[2][4][32];
+};
+
+// the stage update of partner orbit orb by the block's 128 threads
 template <int SUB>
-__global__ void __launch_bounds__(128) k_stage_orbit(Dims d, Deriv D, const double *__restrict__ k2l2i,
-                                                     const float *__restrict__ S, const float *__restrict__ es,
-                                                     double *__restrict__ q, float *__restrict__ acc,
-                                                     float *__restrict__ q32, double *__restrict__ mf,
-                                                     const double *__restrict__ fp, const double *__restrict__ fm,
-                                                     const double *__restrict__ dtp)
+__device__ __forceinline__ void stage_orbit(const Dims &d, const Deriv &D, const double *__restrict__ k2l2i,
+                                            const float *__restrict__ S, const float *__restrict__ es,
+                                            double *__restrict__ q, float *__restrict__ acc,
+                                            float *__restrict__ q32, double *__restrict__ mf,
+                                            const double *__restrict__ fp, const double *__restrict__ fm,
+                                            double dt, long long orb, StageShared &sh)
 {
-    __shared__ float sh_a[2][4][32], sh_b[2][4][32], sh_e[2][4][32], sh_d[2][4][32];
+    auto &sh_a = sh.a;
+    auto &sh_b = sh.b;
+    auto &sh_e = sh.e;
+    auto &sh_d = sh.d;
     const int hy = d.ny / 2 + 1;
-    const long long orb = blockIdx.x;
     const long long N = d.nfield;
     const int kx = (int)(orb / hy), ky = (int)(orb - (long long)kx * hy);
     const int x2 = xsrc(kx, d.nx), y2 = xsrc(ky, d.ny);
@@ -860,7 +867,7 @@ __global__ void __launch_bounds__(128) k_stage_orbit(Dims d, Deriv D, const doub
     const bool mean = col == 0;  // the (0,0) column keeps its mean vorticity
     const float cx = (float)D.cx[mx], cy = (float)D.cy[my], kk = (float)k2l2i[col];
     StageCol<SUB> f;
-    f.make(*dtp, fp, fm, col);
+    f.make(dt, fp, fm, col);
     StageLoads<SUB> cur, nxt;
     stage_load<SUB>(cur, active && lane <= d.nz, N, o + lane, S, es, q, acc);
     int buf = 0;
@@ -893,6 +900,61 @@ __global__ void __launch_bounds__(128) k_stage_orbit(Dims d, Deriv D, const doub
             }
         }
         cur = nxt;
+    }
+}
+
+
+template <int SUB>
+__global__ void __launch_bounds__(128) k_stage_orbit(Dims d, Deriv D, const double *__restrict__ k2l2i,
+                                                     const float *__restrict__ S, const float *__restrict__ es,
+                                                     double *__restrict__ q, float *__restrict__ acc,
+                                                     float *__restrict__ q32, double *__restrict__ mf,
+                                                     const double *__restrict__ fp, const double *__restrict__ fm,
+                                                     const double *__restrict__ dtp)
+{
+    __shared__ StageShared sh;
+    stage_orbit<SUB>(d, D, k2l2i, S, es, q, acc, q32, mf, fp, fm, *dtp, blockIdx.x, sh);
+}
+
+// The stage update of every run of a batch in one persistent launch: the
+// work items are (run, partner orbit), numbered run by run (item0), and the
+// blocks take items item b, b + gridDim.x, ...; each item is the same
+// computation as the single-run kernel above, so a batch and the runs
+// stepped alone agree bitwise.
+template <int SUB>
+__global__ void __launch_bounds__(128) k_batch_stage(const StageRun *__restrict__ runs, int nruns, long long nitems)
+{
+    __shared__ StageShared sh;
+    for (long long it = blockIdx.x; it < nitems; it += gridDim.x) {
+        int lo = 0, hi = nruns - 1;  // the run whose items contain it
+        while (lo < hi) {
+            const int mid = (lo + hi + 1) >> 1;
+            if (runs[mid].item0 <= it) lo = mid;
+            else hi = mid - 1;
+        }
+        const StageRun &r = runs[lo];
+        stage_orbit<SUB>(r.d, r.D, r.k2l2i, r.S, r.es, r.q, r.acc, r.q32, r.mf, r.fp[SUB - 1], r.fm[SUB - 1],
+                         *r.dtp, it - r.item0, sh);
+        __syncthreads();
+    }
+}
+
+int batch_stage_blocks()
+{
+    int dev = 0, sms = 1, per = 1;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_batch_stage<2>, 128, 0);
+    return sms * (per > 0 ? per : 1);
+}
+
+void op_batch_stage(cudaStream_t st, int sub, const StageRun *runs, int nruns, long long nitems, int blocks)
+{
+    switch (sub) {
+    case 1: k_batch_stage<1><<<blocks, 128, 0, st>>>(runs, nruns, nitems); break;
+    case 2: k_batch_stage<2><<<blocks, 128, 0, st>>>(runs, nruns, nitems); break;
+    case 3: k_batch_stage<3><<<blocks, 128, 0, st>>>(runs, nruns, nitems); break;
+    default: k_batch_stage<4><<<blocks, 128, 0, st>>>(runs, nruns, nitems); break;
     }
 }
 

@@ -11,6 +11,7 @@
 // low-mode inversion and reductions).
 #include <cuda_runtime.h>
 
+#include <atomic>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -66,6 +67,8 @@ struct StepScal {
     int inew, iold, filled;
     int err;           // 1 non-finite diagnostic, 2 Jacobi sweep limit
 };
+
+struct BatchPlan;
 
 }  // namespace
 
@@ -129,6 +132,10 @@ struct ps3d_gpu_ctx {
     double *roll_dev = nullptr;
     cudaGraphExec_t graph = nullptr;
     long long graph_launches = 0;  // kernels per captured step
+    // the captured batch step this context leads (ps3d_gpu_batch_advance),
+    // and the serial number that identifies the context in another's batch
+    BatchPlan *batch = nullptr;
+    unsigned long long serial = 0;
     // line-FFT autotuner: ms per launch of each block shape for the passes
     // forward y, forward x, inverse y, inverse x (0 where not timed)
     double tune_ms[4][2] = {{0, 0}, {0, 0}, {0, 0}, {0, 0}};
@@ -817,6 +824,28 @@ template <typename T> int rhs_or_hold(ps3d_gpu_ctx *c)
 // impl_rk4_step (impl_rk4.f90:76-207)
 __global__ void k_set_dt(StepScal *sc, double dt) { sc->dt = dt; }
 
+// column factors of impl-diff-rk4 substep sub (impl_rk4.f90:212-364):
+// the multiplier of the source (fp) and the integrating factor (fm)
+void stage_factors(ps3d_gpu_ctx *c, int sub, const double **fp, const double **fm)
+{
+    switch (sub) {
+    case 1: *fp = c->filt0; *fm = c->emq; break;
+    case 2: *fp = c->epq; *fm = c->emq; break;
+    case 3: *fp = c->epq; *fm = c->emq2; break;
+    default: *fp = c->epq2; *fm = c->emq2; break;
+    }
+}
+
+// the mixed form's fused projection, filter and stage update of substep sub
+void stage_mixed(ps3d_gpu_ctx *c, int sub)
+{
+    const double *fp, *fm;
+    stage_factors(c, sub, &fp, &fm);
+    op_stage_orbit(c->d, c->st, sub, c->D(), c->k2l2i, tf<float>(c->svorts), c->es_src, c->svor,
+                   reinterpret_cast<float *>(c->svorf), c->svor32, c->mf64, fp, fm, &c->sc->dt);
+    c->launches += 1;
+}
+
 // t == nullptr: a device-driven step (dt already in c->sc, the time kept on
 // the device); only the mixed form runs that way
 template <typename T> int step_rk4(ps3d_gpu_ctx *c, double *t, double dt)
@@ -865,9 +894,8 @@ template <typename T> int step_rk4(ps3d_gpu_ctx *c, double *t, double dt)
         ps3d_gpu_ctx *c;
         ~MeanFlowSource() { c->mf_a = nullptr; }
     } mf_guard{c};
-    auto stage = [&](int sub, const double *fp, const double *fm) {
-        op_stage_orbit(d, c->st, sub, c->D(), c->k2l2i, s32, c->es_src, c->svor, acc, q32, c->mf64, fp, fm, dtp);
-        c->launches += 1;
+    auto stage = [&](int sub, const double *, const double *) {
+        stage_mixed(c, sub);
         c->mf_a = sub < 4 ? c->mf64 : nullptr;
     };
     if (mixed) {
@@ -1086,8 +1114,13 @@ __global__ void k_vdiss_dev(long long n, const double *vhdis, double *vdiss, con
 }
 
 // One advance of the mixed form with impl-diff-rk4 and no host
-// synchronisation: what a CUDA graph captures.
-int advance_dev(ps3d_gpu_ctx *c)
+// synchronisation, in the pieces a batch interleaves with the stage updates
+// of its other runs: dev_pre (vor2vel, adapt on the device, the first
+// source and the integrating factors), then for substeps 1..4 the stage
+// update, with dev_rhs (vor2vel and source of the stage state) between
+// them, and dev_end (the vorticity-mean fix).  The same kernels in the same
+// order as advance<float> with step_rk4<float>.
+int dev_pre(ps3d_gpu_ctx *c)
 {
     const Dims &d = c->d;
     const long long N = d.nfield;
@@ -1118,7 +1151,36 @@ int advance_dev(ps3d_gpu_ctx *c)
     c->closure_fresh = true;
     rc = source<float>(c);
     if (rc) return rc;
-    return step_rk4<float>(c, nullptr, 0.0);
+    op_rk4_factors(d, c->st, c->vdiss, c->filt0, c->epq, c->emq, c->epq2, c->emq2);
+    c->launches += 1;
+    return check(c, "advance");
+}
+
+int dev_rhs(ps3d_gpu_ctx *c)
+{
+    c->mf_a = c->mf64;
+    int rc = vor2vel<float>(c);
+    if (!rc) rc = source<float>(c);
+    c->mf_a = nullptr;
+    return rc;
+}
+
+void dev_end(ps3d_gpu_ctx *c)
+{
+    op_mean_fix(c->d, c->st, c->svor, c->dstsum, c->fnzi, c->ini, nullptr, 1, c->svor32);
+    c->launches += 1;
+}
+
+int advance_dev(ps3d_gpu_ctx *c)
+{
+    int rc = dev_pre(c);
+    for (int sub = 1; sub <= 4 && !rc; ++sub) {
+        stage_mixed(c, sub);
+        if (sub < 4) rc = dev_rhs(c);
+    }
+    if (rc) return rc;
+    dev_end(c);
+    return check(c, "advance");
 }
 
 int graph_supported(ps3d_gpu_ctx *c)
@@ -1130,8 +1192,8 @@ int graph_supported(ps3d_gpu_ctx *c)
     return PS3D_OK;
 }
 
-// upload the model time and the rolling-mean state; capture the step once
-int graph_prepare(ps3d_gpu_ctx *c, double t)
+// upload the model time and the rolling-mean state for device-driven steps
+int graph_upload(ps3d_gpu_ctx *c, double t)
 {
     int rc = graph_supported(c);
     if (rc) return rc;
@@ -1144,7 +1206,13 @@ int graph_prepare(ps3d_gpu_ctx *c, double t)
     cudaMemcpyAsync(c->sc, &h, sizeof(h), cudaMemcpyHostToDevice, c->st);
     cudaMemcpyAsync(c->roll_dev, c->roll.hist.data(), c->roll.hist.size() * sizeof(double),
                     cudaMemcpyHostToDevice, c->st);
-    rc = sync_check(c, "graph_prepare");
+    return sync_check(c, "graph_prepare");
+}
+
+// upload the scalars; capture the step once
+int graph_prepare(ps3d_gpu_ctx *c, double t)
+{
+    int rc = graph_upload(c, t);
     if (rc) return rc;
     if (c->graph) return PS3D_OK;
     const int kind = c->probe.kind;
@@ -1202,6 +1270,133 @@ int graph_finish(ps3d_gpu_ctx *c, double *t, ps3d_gpu_diag *diag)
     }
     if (h.err & 2) return fail(c, PS3D_ERR_DEVICE_LIMIT, "adapt: Jacobi sweep limit reached");
     if (h.err & 1) return fail(c, PS3D_ERR_NONFINITE, "adapt: non-finite diagnostic");
+    return PS3D_OK;
+}
+
+// ------------------------------------------------------------ batch step
+// A batch of independent runs (any grid sizes, mixed form, impl-diff-rk4)
+// advanced one whole step per CUDA graph launch: every run's pieces of the
+// device-driven advance run on the run's own stream, and each of the four
+// stage updates is one persistent launch over the (run, partner orbit) work
+// items of all runs (op_batch_stage), between a join of all runs' streams
+// and a fork back to them.
+struct BatchPlan {
+    std::vector<ps3d_gpu_ctx *> runs;
+    std::vector<unsigned long long> serials;
+    std::vector<cudaEvent_t> ev;  // fork (0) and one join event per run
+    cudaGraphExec_t exec = nullptr;
+    StageRun *dev_runs = nullptr;
+    long long nitems = 0, kernels = 0;
+    int blocks = 0;
+    ~BatchPlan()
+    {
+        if (exec) cudaGraphExecDestroy(exec);
+        if (dev_runs) cudaFree(dev_runs);
+        for (cudaEvent_t e : ev) cudaEventDestroy(e);
+    }
+    bool same(ps3d_gpu_ctx *const *ctx, int n) const
+    {
+        if ((int)runs.size() != n) return false;
+        for (int i = 0; i < n; ++i)
+            if (runs[i] != ctx[i] || serials[i] != ctx[i]->serial) return false;
+        return true;
+    }
+};
+
+int batch_capture(BatchPlan *bp)
+{
+    const int n = (int)bp->runs.size();
+    ps3d_gpu_ctx *c0 = bp->runs[0];
+    cudaStream_t s0 = c0->st;
+    std::vector<StageRun> h(n);
+    long long items = 0;
+    for (int i = 0; i < n; ++i) {
+        ps3d_gpu_ctx *c = bp->runs[i];
+        StageRun &r = h[i];
+        r.d = c->d;
+        r.D = c->D();
+        r.k2l2i = c->k2l2i;
+        r.S = tf<float>(c->svorts);
+        r.es = c->es_src;
+        r.q = c->svor;
+        r.acc = reinterpret_cast<float *>(c->svorf);
+        r.q32 = c->svor32;
+        r.mf = c->mf64;
+        for (int sub = 1; sub <= 4; ++sub) stage_factors(c, sub, &r.fp[sub - 1], &r.fm[sub - 1]);
+        r.dtp = &c->sc->dt;
+        r.item0 = items;
+        items += (long long)(c->d.nx / 2 + 1) * (c->d.ny / 2 + 1);
+    }
+    bp->nitems = items;
+    bp->blocks = batch_stage_blocks();
+    if (cudaMalloc(&bp->dev_runs, n * sizeof(StageRun)) != cudaSuccess) {
+        cudaGetLastError();
+        return fail(c0, PS3D_ERR_OUT_OF_MEMORY, "batch: run table");
+    }
+    cudaMemcpyAsync(bp->dev_runs, h.data(), n * sizeof(StageRun), cudaMemcpyHostToDevice, s0);
+    bp->ev.assign(n + 1, nullptr);
+    for (auto &e : bp->ev) cudaEventCreateWithFlags(&e, cudaEventDisableTiming);
+    int rc = sync_check(c0, "batch set-up");
+    if (rc) return rc;
+    std::vector<int> kinds(n);
+    for (int i = 0; i < n; ++i) {
+        kinds[i] = bp->runs[i]->probe.kind;
+        bp->runs[i]->probe.kind = PROBE_OFF;  // no event records inside the graph
+    }
+    std::vector<long long> l0(n);
+    for (int i = 0; i < n; ++i) l0[i] = bp->runs[i]->launches;
+    cudaGraph_t g = nullptr;
+    if (cudaStreamBeginCapture(s0, cudaStreamCaptureModeThreadLocal) != cudaSuccess) rc = check(c0, "batch capture");
+    auto fork = [&]() {
+        cudaEventRecord(bp->ev[0], s0);
+        for (int i = 1; i < n; ++i) cudaStreamWaitEvent(bp->runs[i]->st, bp->ev[0], 0);
+    };
+    auto join = [&]() {
+        for (int i = 1; i < n; ++i) {
+            cudaEventRecord(bp->ev[i], bp->runs[i]->st);
+            cudaStreamWaitEvent(s0, bp->ev[i], 0);
+        }
+    };
+    long long stage_launches = 0;
+    if (!rc) {
+        fork();
+        for (int i = 0; i < n && !rc; ++i) rc = dev_pre(bp->runs[i]);
+        join();
+        for (int sub = 1; sub <= 4 && !rc; ++sub) {
+            op_batch_stage(s0, sub, bp->dev_runs, n, bp->nitems, bp->blocks);
+            ++stage_launches;
+            if (sub < 4) {
+                fork();
+                for (int i = 0; i < n && !rc; ++i) rc = dev_rhs(bp->runs[i]);
+                join();
+            }
+        }
+        if (!rc) {
+            fork();
+            for (int i = 0; i < n; ++i) dev_end(bp->runs[i]);
+            join();
+        }
+        const cudaError_t e = cudaStreamEndCapture(s0, &g);
+        if (!rc && e != cudaSuccess) rc = fail(c0, PS3D_ERR_CUDA, std::string("batch capture: ") + cudaGetErrorString(e));
+    }
+    long long kernels = stage_launches;
+    for (int i = 0; i < n; ++i) {
+        bp->runs[i]->probe.kind = kinds[i];
+        kernels += bp->runs[i]->launches - l0[i];
+        bp->runs[i]->launches = l0[i];
+    }
+    bp->kernels = kernels;
+    if (rc) {
+        if (g) cudaGraphDestroy(g);
+        cudaGetLastError();
+        return rc;
+    }
+    const cudaError_t ei = cudaGraphInstantiate(&bp->exec, g, 0);
+    cudaGraphDestroy(g);
+    if (ei != cudaSuccess) {
+        bp->exec = nullptr;
+        return fail(c0, PS3D_ERR_CUDA, std::string("batch instantiate: ") + cudaGetErrorString(ei));
+    }
     return PS3D_OK;
 }
 
@@ -1755,6 +1950,8 @@ int ps3d_gpu_create(const ps3d_gpu_config *cfg, ps3d_gpu_ctx **out)
         return PS3D_ERR_NO_DEVICE;
     }
     ps3d_gpu_ctx *c = new ps3d_gpu_ctx();
+    static std::atomic<unsigned long long> next_serial{0};
+    c->serial = ++next_serial;
     c->cfg = *cfg;
     c->fp64 = cfg->precision == PS3D_PRECISION_FP64;
     cudaSetDevice(cfg->device);
@@ -1796,6 +1993,7 @@ int ps3d_gpu_destroy(ps3d_gpu_ctx *c)
     if (c->st) cudaStreamSynchronize(c->st);
     if (c->closure) closure_detach(c->closure, c);
     if (c->graph) cudaGraphExecDestroy(c->graph);
+    delete c->batch;
     for (void *p : c->allocs) cudaFree(p);
     if (c->probe.ev) {
         for (int i = 0; i < 2 * Probe::MAXP; ++i) cudaEventDestroy(c->probe.ev[i]);
@@ -2241,42 +2439,48 @@ int ps3d_gpu_advance_graph(ps3d_gpu_ctx *c, double *t, int nsteps, ps3d_gpu_diag
 int ps3d_gpu_batch_advance(ps3d_gpu_ctx *const *ctx, int n, double *t, int nsteps, double *ms)
 {
     if (!ctx || !t || n <= 0 || nsteps < 0) return PS3D_ERR_INVALID_ARG;
-    for (int i = 0; i < n; ++i)
+    for (int i = 0; i < n; ++i) {
         if (!ctx[i] || ctx[i]->cfg.device != ctx[0]->cfg.device) return PS3D_ERR_INVALID_ARG;
+        for (int j = 0; j < i; ++j)
+            if (ctx[j] == ctx[i]) return fail(ctx[0], PS3D_ERR_INVALID_ARG, "batch: a context appears twice");
+    }
     int rc = enter(ctx[0]);
     if (rc) return rc;
     for (int i = 0; i < n; ++i) {
-        rc = graph_prepare(ctx[i], t[i]);
+        rc = graph_upload(ctx[i], t[i]);
         if (rc) return rc;
     }
-    // every run's step is one graph on its own stream; the streams start
-    // together after one event and the elapsed time ends when the last one
-    // has finished
-    cudaEvent_t e0, e1;
-    cudaEventCreate(&e0);
-    cudaEventCreate(&e1);
-    cudaStream_t s0 = ctx[0]->st;
-    cudaEventRecord(e0, s0);
-    for (int i = 1; i < n; ++i) cudaStreamWaitEvent(ctx[i]->st, e0, 0);
-    for (int s = 0; s < nsteps && !rc; ++s)
-        for (int i = 0; i < n && !rc; ++i) rc = graph_launch(ctx[i], 1);
-    for (int i = 1; i < n; ++i) {
-        cudaEventRecord(ctx[i]->ev1, ctx[i]->st);
-        cudaStreamWaitEvent(s0, ctx[i]->ev1, 0);
+    ps3d_gpu_ctx *c0 = ctx[0];
+    if (!c0->batch || !c0->batch->same(ctx, n)) {
+        delete c0->batch;
+        c0->batch = new BatchPlan();
+        c0->batch->runs.assign(ctx, ctx + n);
+        for (int i = 0; i < n; ++i) c0->batch->serials.push_back(ctx[i]->serial);
+        rc = batch_capture(c0->batch);
+        if (rc) {
+            delete c0->batch;
+            c0->batch = nullptr;
+            return rc;
+        }
     }
-    cudaEventRecord(e1, s0);
+    cudaStream_t s0 = c0->st;
+    cudaEventRecord(c0->ev0, s0);
+    for (int s = 0; s < nsteps && !rc; ++s)
+        if (cudaGraphLaunch(c0->batch->exec, s0) != cudaSuccess) rc = check(c0, "batch launch");
+    cudaEventRecord(c0->ev1, s0);
+    c0->launches += c0->batch->kernels * nsteps;
     int rf = PS3D_OK;
     for (int i = 0; i < n; ++i) {
+        // the runs' streams joined s0 inside the graph
+        if (i > 0) cudaStreamWaitEvent(ctx[i]->st, c0->ev1, 0);
         const int r = graph_finish(ctx[i], &t[i], nullptr);
         if (r && !rf) rf = r;
     }
     if (ms) {
         float f = 0.0f;
-        cudaEventElapsedTime(&f, e0, e1);
+        cudaEventElapsedTime(&f, c0->ev0, c0->ev1);
         *ms = (double)f;
     }
-    cudaEventDestroy(e0);
-    cudaEventDestroy(e1);
     return rc ? rc : rf;
 }
 

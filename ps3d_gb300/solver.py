@@ -348,8 +348,10 @@ class Ps3dGpu:
 
 
 def batch_advance(models, ts, nsteps):
-    """Advance independent runs (Ps3dGpu objects, any sizes, one device) by
-    nsteps captured steps, their graphs interleaved on their own streams.
+    """Advance independent runs (Ps3dGpu objects, any sizes, one device,
+    mixed form, impl-diff-rk4) by nsteps steps, each step one CUDA graph for
+    the whole batch: every run's right-hand sides on its own stream and one
+    persistent launch per stage update for all runs (ps3d_gpu_batch_advance).
     Returns (list of times, device ms of the batch)."""
     n = len(models)
     hs = (ctypes.c_void_p * n)(*[m._h.value for m in models])

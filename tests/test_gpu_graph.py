@@ -37,10 +37,16 @@ def test_graph_advance_matches_host_driven_advance(n):
 
 
 def test_batch_of_uneven_runs_matches_individual_runs():
-    specs = [(32, 11, 10.0), (64, 12, 60.0), (32, 13, 90.0)]
+    """The batch step (every run's pieces on its own stream, one persistent
+    launch per stage update over all runs' partner orbits, one CUDA graph per
+    step) against the same runs advanced one by one: bitwise, over two
+    calls (the second reuses the captured batch) and for a reordered subset
+    (captured afresh)."""
+    specs = [(32, 11, 10.0), (64, 12, 60.0), (128, 14, 30.0), (32, 13, 90.0)]
     batch = [_model(n, s, prediss=p) for n, s, p in specs]
     single = [_model(n, s, prediss=p) for n, s, p in specs]
-    ts, ms = batch_advance(batch, [0.0] * len(batch), 3)
+    ts, ms = batch_advance(batch, [0.0] * len(batch), 2)
+    ts, ms = batch_advance(batch, ts, 1)
     assert ms > 0
     for m, b, t in zip(single, batch, ts):
         tt = 0.0
@@ -48,6 +54,12 @@ def test_batch_of_uneven_runs_matches_individual_runs():
             tt, _ = m.advance(tt)
         assert tt == t
         assert np.array_equal(m.get("svor"), b.get("svor"))
+    sub = [batch[2], batch[0]]
+    ts2, _ = batch_advance(sub, [ts[2], ts[0]], 1)
+    for k, i in enumerate((2, 0)):
+        tt, _ = single[i].advance(ts[i])
+        assert tt == ts2[k]
+        assert np.array_equal(single[i].get("svor"), batch[i].get("svor"))
 
 
 def test_graph_refused_for_fp64_form():
