@@ -284,7 +284,8 @@ static void launch_m(int M, const TIN *in, float *out, const Dims &d, cudaStream
     }
 }
 
-bool col32_supported(int nz) { return nz >= 32 && nz <= 512; }
+// L = 2 nz = 32 M with M a power of two, 2..32
+bool col32_supported(int nz) { return nz == 32 || nz == 64 || nz == 128 || nz == 256 || nz == 512; }
 
 template <typename TIN>
 void columns32(const Dims &d, cudaStream_t st, int mode, const TIN *in, float *out, const double *k2l2, float dz,
