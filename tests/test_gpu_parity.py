@@ -158,12 +158,13 @@ def test_one_step_matches_oracle(stepper):
 def test_multi_step_parity_per_step():
     """Per-step relative L2 of each vorticity component and the energy /
     enstrophy / helicity series over 200 steps at 32^3 against the oracle,
-    measured against a rounding floor (tests.parity_util.multi_step_parity);
-    the worst ratio of GPU error to floor is printed.  (128^3 over 200 steps:
+    measured against a shadow oracle run that carries the GPU's own per-step
+    rounding differences (tests.parity_util.multi_step_parity); the worst
+    ratio of GPU error to shadow is printed.  (128^3 over 200 steps:
     test_gpu_parity_config2.py.)"""
     from tests.parity_util import multi_step_parity
     ratio, at, series, eps = multi_step_parity(32, 200, check_every=10)
-    print(f"32^3 x 200 steps: one-step difference {eps:.3g}; worst GPU/floor ratio {ratio:.3g} at "
+    print(f"32^3 x 200 steps: worst local (one-step) error {eps:.3g}; worst GPU/shadow ratio {ratio:.3g} at "
           f"(step, comp, err, floor) {at}; worst series error {series:.3g}")
 
 
