@@ -61,7 +61,7 @@ extern "C" {
  * (src/utils/options.f90:11-96) and the box (src/utils/parameters.f90).
  * The first 17 members match the oracle's ps3o_config field for field. */
 typedef struct {
-    int nx, ny, nz;             /* cells; nx, ny, nz powers of two, 8..2048  */
+    int nx, ny, nz;             /* cells; even, factors 2, 3, 5; 8..2048     */
     int nnu;                    /* vor_visc%nnu                              */
     double lower[3];            /* box lower corner                          */
     double extent[3];           /* box extent                                */
@@ -112,7 +112,9 @@ typedef struct ps3d_gpu_ctx ps3d_gpu_ctx;
 
 /* ---- lifetime ----------------------------------------------------------
  * create: init_inversion (inversion_utils.f90:222-372) + initialise_fft
- * (sta3dfft.f90:53-110) + field_alloc (fields.f90:45-84). */
+ * (sta3dfft.f90:53-110) + field_alloc (fields.f90:45-84).  nx, ny, nz:
+ * even, 8..2048 (nz up to 1024 in the FP64 form), prime factors 2, 3 and 5
+ * only (factorisen, stafft.f90:128-187); otherwise PS3D_ERR_UNSUPPORTED_SIZE. */
 int ps3d_gpu_create(const ps3d_gpu_config *cfg, ps3d_gpu_ctx **ctx);
 int ps3d_gpu_destroy(ps3d_gpu_ctx *ctx);
 const char *ps3d_gpu_strerror(int status);
@@ -167,7 +169,10 @@ int ps3d_gpu_init_diffusion(ps3d_gpu_ctx *ctx, double te, double en);
 /* vor2vel (inversion.f90:23-226) */
 int ps3d_gpu_vor2vel(ps3d_gpu_ctx *ctx);
 /* source (inversion.f90:376-388): buoyancy_tendency (:232-292) on buoyancy
- * contexts, then vorticity_tendency (:298-371) */
+ * contexts, then vorticity_tendency (:298-371).  svorts is left
+ * unprojected, as the reference leaves it; the mixed form also keeps the z
+ * part of the tendency's solenoidal projection, which its stage updates
+ * use to project each source term as they apply it. */
 int ps3d_gpu_source(ps3d_gpu_ctx *ctx);
 /* adapt (advance.f90:109-377) incl. set_diffusion of the stepper */
 int ps3d_gpu_adapt(ps3d_gpu_ctx *ctx, double t, double *dt, ps3d_gpu_diag *diag);
@@ -255,10 +260,16 @@ int ps3d_gpu_host_free(void *ptr);
  * (PS3D_ERR_NONFINITE / PS3D_ERR_DEVICE_LIMIT; the state is then invalid).
  * PS3D_ERR_INVALID_ARG for the FP64 form, cn2, a held source or buoyancy. */
 int ps3d_gpu_advance_graph(ps3d_gpu_ctx *ctx, double *t, int nsteps, ps3d_gpu_diag *diag, double *ms);
-/* Batching (no reference counterpart): nsteps captured steps of n independent
- * contexts (any grid sizes, one device), the runs' graphs interleaved on
- * their own streams so they execute concurrently.  t[n] in/out; ms = device
- * time of the whole batch. */
+/* Batching (no reference counterpart): nsteps steps of n independent
+ * contexts (any grid sizes, one device; the conditions of
+ * ps3d_gpu_advance_graph), each step one CUDA graph for the whole batch:
+ * every run's right-hand sides on the run's own stream, and each of the
+ * four stage updates one persistent launch over the (run, partner orbit)
+ * work items of all runs.  The graph is captured on the first call and
+ * kept (by ctx[0]) while the same contexts come in the same order.  The
+ * states equal those of the runs stepped alone, bitwise.  t[n] in/out; ms =
+ * device time of the whole batch.  A context listed twice is
+ * PS3D_ERR_INVALID_ARG. */
 int ps3d_gpu_batch_advance(ps3d_gpu_ctx *const *ctx, int n, double *t, int nsteps, double *ms);
 
 /* Line-FFT autotuner (no reference counterpart): at creation the mixed form
