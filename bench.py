@@ -117,11 +117,6 @@ class ClockSampler:
 
 
 # ------------------------------------------------------------ workloads
-# DRAM bytes (read + write) per launch of k_xy32 at 512^3, from the ncu
-# capture summarised in profiles/k_xy32_512.md (None until measured)
-XY32_TRAFFIC_512 = None
-
-
 def make_ic(n, seed=1):
     from ps3d_gb300 import ic
     if n >= 1024:  # 26 GB per vector field: build it slab by slab
@@ -365,15 +360,12 @@ def run_gpu(args, rank, world, dist):
     clocks = clk.summary()
 
     # dominant kernel probe inside real steps (same stream, CUDA events).
-    # The horizontal transforms (one launch per transform on square planes,
-    # k_xy32: both line passes, the intermediate in L2; otherwise two
-    # k_lines32 passes) and the k_colz column-kernel family are the
-    # candidates; y and x line passes are also reported apart where they run.
+    # k_lines32 (the line FFT, both directions) and the k_colz column-kernel
+    # family are the candidates; y and x lines are also reported apart.
     probe_steps = max(1, min(3, args.steps))
     best = None
     probes = []
-    kinds = ((4, "horizontal transforms (k_xy32 / k_lines32)", True), (3, "k_colz (column transforms)", True),
-             (5, "k_xy32 (one launch per horizontal transform)", False),
+    kinds = ((4, "k_lines32 (x and y lines)", True), (3, "k_colz (column transforms)", True),
              (1, "k_lines32 (y lines)", False), (2, "k_lines32 (x lines)", False))
     for kind, name, candidate in kinds:
         gm.probe(kind)
@@ -389,15 +381,14 @@ def run_gpu(args, rank, world, dist):
     peak, peak_kind = peaks()
     krec = best[0]
     achieved = krec["bytes_per_launch"] / (krec["ms_per_launch"] * 1e-3) / 1e9
-    # DRAM traffic per launch of the one-launch horizontal transform from
-    # the committed ncu capture (profiles/k_xy32_512.md): read + write per
-    # launch at 512 x 512 x 128 (5 z-tiles of 32), scaled to 512^3 by the
-    # z-tiles processed (17); not measured for other kernels or sizes
-    traffic = XY32_TRAFFIC_512 if (best[2] == 4 and n == 512 and XY32_TRAFFIC_512) else None
+    # DRAM traffic per launch from the committed ncu capture of the same
+    # kernel at 512^3 (profiles/k_lines32_512.md: read + write, mean of four
+    # launches); not measured for other kernels or sizes
+    traffic = 1.04e9 if (best[2] == 4 and n == 512) else None
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                 "frac": achieved / peak, "traffic": traffic, "traffic_unit": "bytes per launch",
-                "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum at 512x512x128, scaled by "
-                                  "z-tiles (profiles/k_xy32_512.md)" if traffic else None,
+                "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum, profiles/k_lines32_512.md"
+                if traffic else None,
                 "kernel": krec["kernel"],
                 "algorithmic_bytes_per_launch": krec["bytes_per_launch"],
                 "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured" else peak_kind,
@@ -464,14 +455,10 @@ def run_gpu(args, rank, world, dist):
     cufft = None
     if rank == 0:
         cufft = cufft_comparator(n, dev)
-        lp = {p["kernel"]: (p["ms_per_launch"], p["launches_per_step"]) for p in roofline["probes"]}
-        fused = lp.get("k_xy32 (one launch per horizontal transform)", (0.0, 0))
-        if fused[1] > 0:
-            ours = fused[0]
-        else:
-            ours = lp.get("k_lines32 (y lines)", (0.0, 0))[0] + lp.get("k_lines32 (x lines)", (0.0, 0))[0]
+        lp = {p["kernel"]: p["ms_per_launch"] for p in roofline["probes"]}
+        ours = lp.get("k_lines32 (y lines)", 0.0) + lp.get("k_lines32 (x lines)", 0.0)
         if isinstance(cufft, dict) and "forward_xy_ms" in cufft:
-            cufft["ours_xy_transform_ms"] = ours
+            cufft["ours_xy_pass_pair_ms"] = ours
 
     closure = closure_timing(dev) if rank == 0 and not args.skip_closure else None
     batch = batch_timing(args.batch_steps) if rank == 0 and not args.skip_batch else None

@@ -28,9 +28,7 @@ enum { COL_DST = 0, COL_DCT = 1, COL_DECOMP = 2, COL_COMBINE = 3 };
 // events on the launching stream (used by the benchmark to time the dominant
 // kernel inside a real step).  kind: 0 off, 1 y lines, 2 x lines, 3 columns.
 // PROBE_LINES brackets the line transforms of both directions
-// PROBE_XYFUSED brackets the one-launch horizontal transforms (both passes;
-// PROBE_LINES brackets them too)
-enum { PROBE_OFF = 0, PROBE_YLINES = 1, PROBE_XLINES = 2, PROBE_COLUMNS = 3, PROBE_LINES = 4, PROBE_XYFUSED = 5 };
+enum { PROBE_OFF = 0, PROBE_YLINES = 1, PROBE_XLINES = 2, PROBE_COLUMNS = 3, PROBE_LINES = 4 };
 struct Probe {
     static constexpr int MAXP = 8192;
     int kind = PROBE_OFF;
@@ -40,7 +38,7 @@ struct Probe {
     double bytes = 0.0;         // algorithmic bytes of the bracketed launches
     bool match(int k) const
     {
-        return k == kind || (kind == PROBE_LINES && (k == PROBE_YLINES || k == PROBE_XLINES || k == PROBE_XYFUSED));
+        return k == kind || (kind == PROBE_LINES && (k == PROBE_YLINES || k == PROBE_XLINES));
     }
     void begin(int k, cudaStream_t st)
     {
@@ -58,14 +56,12 @@ struct Probe {
 
 // transforms.cu
 void transforms_init();
-// xyctl: the control block of the one-launch FP32 transform (launch_xy32),
-// or null for two line passes
 template <typename T>
 void xy_forward(const Dims &d, cudaStream_t st, const T *in, T *out, const typename cplx<T>::type *twx,
-                const typename cplx<T>::type *twy, Probe *pr, void *xyctl = nullptr);
+                const typename cplx<T>::type *twy, Probe *pr);
 template <typename T>
 void xy_inverse(const Dims &d, cudaStream_t st, const T *in, T *out, const typename cplx<T>::type *twx,
-                const typename cplx<T>::type *twy, Probe *pr, void *xyctl = nullptr);
+                const typename cplx<T>::type *twy, Probe *pr);
 template <typename T>
 void columns(const Dims &d, cudaStream_t st, int mode, const T *in, T *out, const T *phim,
              const T *phip, const typename cplx<T>::type *twz2, Probe *pr);
@@ -79,16 +75,6 @@ void launch_lines32(cudaStream_t st, const float *in, float *out, int n, int P, 
                     long long nbatch, long long batch_stride, bool inverse, const float2 *tw, int shape = -1);
 // number of block shapes the autotuner can choose from at line length n
 int lines32_shapes(int n);
-// both passes of one horizontal transform in one launch, the intermediate
-// kept in L2 (square planes nx = ny = n, lines32_supported(n), at most
-// XY_MAX_ZTILES tiles of 32 z); ctl: a device control block of
-// xy_control_bytes() per stream, zeroed once; its first word becomes
-// non-zero if a wait ran out and stays so until the host clears it
-constexpr int XY_MAX_ZTILES = 40;
-size_t xy_control_bytes();
-bool xy32_supported(int nx, int ny, int P);
-void launch_xy32(cudaStream_t st, const float *in, float *out, int n, int P, int zv, bool inverse, const float2 *tw,
-                 void *ctl);
 // FP32 half-length warp z transforms (colz.cu), nz = 64..1024
 bool colz_supported(int nz);
 void colz_init();

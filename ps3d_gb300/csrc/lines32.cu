@@ -15,8 +15,6 @@
 // the Hermitian rows k and N - k as it loads them (one lane per thread
 // there, to bound the registers).  N (the line length) is a compile-time
 // constant: 64..1024.
-#include <cstddef>
-
 #include "kernels.h"
 
 namespace ps3d {
@@ -52,7 +50,7 @@ template <int R, bool INV> __device__ __forceinline__ void dftR(float2 *v) { dft
 // one radix-R Stockham pass with span NS over N points: inputs x[j + r N/R]
 // of butterfly j, outputs at (j - k) R + k + r NS, k = j mod NS; each thread
 // applies it to its two lanes
-template <int N, int R, int NS, bool INV, int W, bool FROM_GLOBAL, bool TO_GLOBAL, bool CG = false>
+template <int N, int R, int NS, bool INV, int W, bool FROM_GLOBAL, bool TO_GLOBAL>
 __device__ __forceinline__ void pass(float4 *sm, const float4 *__restrict__ gin, float4 *__restrict__ gout,
                                      long long gstride, bool valid, float scale, const float2 *__restrict__ tw,
                                      int nval = 4)
@@ -71,8 +69,7 @@ __device__ __forceinline__ void pass(float4 *sm, const float4 *__restrict__ gin,
                 const int row = j + r * NB;
                 float4 x;
                 if (FROM_GLOBAL) {
-                    x = valid ? (CG ? __ldcg(&gin[row * gstride]) : gin[row * gstride])
-                              : make_float4(0.f, 0.f, 0.f, 0.f);
+                    x = valid ? gin[row * gstride] : make_float4(0.f, 0.f, 0.f, 0.f);
                     // z rows beyond the top wall (padding) enter as zero: the
                     // paired real line must not pick up leftover content
                     if (nval < 4) {
@@ -133,7 +130,7 @@ __device__ __forceinline__ float2 herm_high(float2 lo, float2 hi) { return make_
 // butterflies (slot s: s and N/8 - s; slot 0: butterflies 0 and N/16, each
 // its own mirror) for one lane, so every row is loaded once and used for
 // both C_k and C_{N-k}.  Items: slots x 16 lanes over the block's threads.
-template <int N, int W, bool CG = false>
+template <int N, int W>
 __device__ __forceinline__ void herm_first_pass(float2 *sm2, const float2 *__restrict__ gin2, long long gs2,
                                                 int z0, int P, int zv)
 {
@@ -150,8 +147,8 @@ __device__ __forceinline__ void herm_first_pass(float2 *sm2, const float2 *__res
         float2 h1[8], h2[8];
 #pragma unroll
         for (int r = 0; r < 8; ++r) {
-            h1[r] = valid ? (CG ? __ldcg(&g[(j1 + r * NB) * gs2]) : g[(j1 + r * NB) * gs2]) : make_float2(0.f, 0.f);
-            h2[r] = valid ? (CG ? __ldcg(&g[(j2 + r * NB) * gs2]) : g[(j2 + r * NB) * gs2]) : make_float2(0.f, 0.f);
+            h1[r] = valid ? g[(j1 + r * NB) * gs2] : make_float2(0.f, 0.f);
+            h2[r] = valid ? g[(j2 + r * NB) * gs2] : make_float2(0.f, 0.f);
         }
         // padding rows (z >= zv) enter as zero
         const int nv = zv - (z0 + 2 * lane);
@@ -227,24 +224,23 @@ __device__ __forceinline__ void later_passes(float4 *sm, float4 *gout, long long
     }
 }
 
-// one tile: z-tile zt (32 consecutive z) of line set `batch`; CG: load
-// through L2 only (the input was written by other blocks of this launch)
-template <int N, bool INV, int W, bool CG>
-__device__ __forceinline__ void line_tile(float4 *smL, const float *__restrict__ in, float *__restrict__ out, int P,
-                                          int zv, long long line_stride, long long batch_stride,
-                                          const float2 *__restrict__ tw, int zt, long long batch)
+template <int N, bool INV, int W>
+__global__ void __launch_bounds__(LinePlan<N, INV, W>::T, LinePlan<N, INV, W>::MINB)
+    k_lines32(const float *__restrict__ in, float *__restrict__ out, int P, int zv, long long line_stride,
+              long long batch_stride, const float2 *__restrict__ tw)
 {
+    extern __shared__ __align__(16) float4 smL[];
     constexpr int T = LinePlan<N, INV, W>::T;
     const int p = threadIdx.x & (PAIRS - 1);
-    const int z0 = zt * 2 * LANES;
+    const int z0 = blockIdx.x * 2 * LANES;
     const bool valid = z0 + 4 * p < P;  // P is a multiple of 8: both lanes or neither
-    const long long base = batch * batch_stride + z0;  // floats
+    const long long base = (long long)blockIdx.y * batch_stride + z0;  // floats
     const float s = rsqrtf((float)N);
     constexpr int H = N / 2;
     if (!INV) {
         const long long gs = line_stride >> 2;  // float4 units
         const float4 *gin = reinterpret_cast<const float4 *>(in + base) + p;
-        pass<N, 8, 1, false, W, true, false, CG>(smL, gin, nullptr, gs, valid, 1.0f, tw, zv - (z0 + 4 * p));
+        pass<N, 8, 1, false, W, true, false>(smL, gin, nullptr, gs, valid, 1.0f, tw, zv - (z0 + 4 * p));
         later_passes<N, false, W, false>(smL, nullptr, gs, valid, 1.0f, tw);
         // split the two packed real transforms of each lane and store the
         // Hermitian rows k and N - k
@@ -263,94 +259,11 @@ __device__ __forceinline__ void line_tile(float4 *smL, const float *__restrict__
                                                   0.5f * (ck.w - cn.w) * s, -0.5f * (ck.z - cn.z) * s);
         }
     } else {
-        herm_first_pass<N, W, CG>(reinterpret_cast<float2 *>(smL), reinterpret_cast<const float2 *>(in + base),
-                                  line_stride >> 1, z0, P, zv);
+        herm_first_pass<N, W>(reinterpret_cast<float2 *>(smL), reinterpret_cast<const float2 *>(in + base),
+                              line_stride >> 1, z0, P, zv);
         const long long gs = line_stride >> 2;
         float4 *gout = reinterpret_cast<float4 *>(out + base) + p;
         later_passes<N, true, W, true>(smL, gout, gs, valid, s, tw);
-    }
-}
-
-template <int N, bool INV, int W>
-__global__ void __launch_bounds__(LinePlan<N, INV, W>::T, LinePlan<N, INV, W>::MINB)
-    k_lines32(const float *__restrict__ in, float *__restrict__ out, int P, int zv, long long line_stride,
-              long long batch_stride, const float2 *__restrict__ tw)
-{
-    extern __shared__ __align__(16) float4 smL[];
-    line_tile<N, INV, W, false>(smL, in, out, P, zv, line_stride, batch_stride, tw, blockIdx.x, blockIdx.y);
-}
-
-// ------------------------------------------------------------------------
-// Both passes of one horizontal transform in one launch (square planes,
-// nx = ny = N), with the intermediate kept in L2.  The tiles of the first
-// pass (A: y lines forward, x lines inverse) and of the second (B) are
-// numbered z-tile by z-tile with the second pass one z-tile behind:
-//   A(0), A(1), B(0), A(2), B(1), ..., A(Z-1), B(Z-2), B(Z-1),
-// and taken in that order from a ticket counter, so a z-tile's intermediate
-// (32 levels of the plane, 32 MB at 512^2) is read back by the second pass
-// while it is still in L2.  A tile of B needs every tile of A of its
-// z-tile: the A tiles count themselves done (every thread fences its
-// stores, then one atomic increment) and a B tile waits for the count.
-// Tickets are taken by running blocks only, in order, and A tiles wait for
-// nothing, so every wait ends whatever the number of resident blocks.  The
-// wait is bounded (a few seconds); if it runs out the block sets the
-// control block's error word and goes on (the host reports
-// PS3D_ERR_DEVICE_LIMIT).  B tiles load through L2 only (ld.global.cg): an
-// L1 may hold lines of the buffer from before the first pass.
-struct XyControl {
-    unsigned int err;  // sticky: cleared by the host after reporting
-    unsigned int ticket;
-    unsigned int done[XY_MAX_ZTILES];
-};
-
-template <int N, bool INV, int W>
-__global__ void __launch_bounds__(LinePlan<N, INV, W>::T, LinePlan<N, INV, W>::MINB)
-    k_xy32(const float *__restrict__ in, float *__restrict__ out, int P, int zv, int ztiles,
-           const float2 *__restrict__ twa, const float2 *__restrict__ twb, XyControl *__restrict__ ctl)
-{
-    extern __shared__ __align__(16) float4 smL[];
-    __shared__ unsigned int item;
-    // A: lines of stride P (y lines, batches x, stride N P) for the forward
-    // transform, lines of stride N P (x lines, batches y, stride P) for the
-    // inverse; B the other direction
-    const long long sy = P, sx = (long long)N * P;
-    const long long lsA = INV ? sx : sy, bsA = INV ? sy : sx, lsB = INV ? sy : sx, bsB = INV ? sx : sy;
-    const unsigned int per = 2u * N, total = (unsigned)ztiles * per;
-    for (;;) {
-        __syncthreads();
-        if (threadIdx.x == 0) item = atomicAdd(&ctl->ticket, 1u);
-        __syncthreads();
-        const unsigned int t = item;
-        if (t >= total) break;
-        // decode: group 0 = A(0); group g (1..Z-1) = A(g), B(g-1); group Z = B(Z-1)
-        int zt;
-        unsigned int batch;
-        bool first;
-        if (t < (unsigned)N) {
-            zt = 0, batch = t, first = true;
-        } else {
-            const unsigned int u = t - N, g = 1 + u / per, r = u % per;
-            if (g < (unsigned)ztiles && r < (unsigned)N) zt = (int)g, batch = r, first = true;
-            else zt = (int)g - 1, batch = (g < (unsigned)ztiles) ? r - N : r, first = false;
-        }
-        if (first) {
-            line_tile<N, INV, W, false>(smL, in, out, P, zv, lsA, bsA, twa, zt, batch);
-            __threadfence();
-            __syncthreads();
-            if (threadIdx.x == 0) asm volatile("red.release.gpu.global.add.u32 [%0], 1;" ::"l"(&ctl->done[zt]) : "memory");
-        } else {
-            if (threadIdx.x == 0) {
-                unsigned int seen = 0;
-                for (int it = 0; it < (1 << 22); ++it) {
-                    asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(seen) : "l"(&ctl->done[zt]) : "memory");
-                    if (seen >= (unsigned)N) break;
-                    __nanosleep(256);
-                }
-                if (seen < (unsigned)N) atomicOr(&ctl->err, 1u);
-            }
-            __syncthreads();
-            line_tile<N, INV, W, true>(smL, out, out, P, zv, lsB, bsB, twb, zt, batch);
-        }
     }
 }
 
@@ -382,83 +295,12 @@ void launch32(cudaStream_t st, const float *in, float *out, int P, int zv, long 
     else launch32w<N, false, 0>(st, in, out, P, zv, ls, nbatch, bs, tw);
 }
 
-template <int N, bool INV, int W>
-void launch_xy_w(cudaStream_t st, const float *in, float *out, int P, int zv, const float2 *twa, const float2 *twb,
-                 XyControl *ctl)
-{
-    static int blocks = 0;  // resident blocks (the same on every GB300)
-    const size_t sm = (size_t)N * LANES * sizeof(float2);
-    if (!blocks) {
-        int dev = 0, sms = 1, per = 1;
-        cudaGetDevice(&dev);
-        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_xy32<N, INV, W>, LinePlan<N, INV, W>::T, sm);
-        blocks = sms * (per > 0 ? per : 1);
-    }
-    const int ztiles = (P + 2 * LANES - 1) / (2 * LANES);
-    // the ticket and the done counts start at zero; the error word is kept
-    cudaMemsetAsync(&ctl->ticket, 0, sizeof(XyControl) - offsetof(XyControl, ticket), st);
-    k_xy32<N, INV, W><<<blocks, LinePlan<N, INV, W>::T, sm, st>>>(in, out, P, zv, ztiles, twa, twb, ctl);
-}
-
 }  // namespace
-
-size_t xy_control_bytes() { return sizeof(XyControl); }
-
-bool xy32_supported(int nx, int ny, int P)
-{
-    return nx == ny && lines32_supported(nx) && (P + 2 * LANES - 1) / (2 * LANES) <= XY_MAX_ZTILES;
-}
-
-void launch_xy32(cudaStream_t st, const float *in, float *out, int n, int P, int zv, bool inverse,
-                 const float2 *tw, void *ctl)
-{
-    XyControl *c = reinterpret_cast<XyControl *>(ctl);
-    // forward passes take the 512-thread shape at n = 512, inverse ones the
-    // 256-thread shape (the autotuner's choice for every pass at 512^3)
-    switch (n) {
-    case 64:
-        if (inverse) launch_xy_w<64, true, 0>(st, in, out, P, zv, tw, tw, c);
-        else launch_xy_w<64, false, 0>(st, in, out, P, zv, tw, tw, c);
-        break;
-    case 128:
-        if (inverse) launch_xy_w<128, true, 0>(st, in, out, P, zv, tw, tw, c);
-        else launch_xy_w<128, false, 0>(st, in, out, P, zv, tw, tw, c);
-        break;
-    case 256:
-        if (inverse) launch_xy_w<256, true, 0>(st, in, out, P, zv, tw, tw, c);
-        else launch_xy_w<256, false, 0>(st, in, out, P, zv, tw, tw, c);
-        break;
-    case 512:
-        if (inverse) launch_xy_w<512, true, 1>(st, in, out, P, zv, tw, tw, c);
-        else launch_xy_w<512, false, 0>(st, in, out, P, zv, tw, tw, c);
-        break;
-    default:
-        if (inverse) launch_xy_w<1024, true, 0>(st, in, out, P, zv, tw, tw, c);
-        else launch_xy_w<1024, false, 0>(st, in, out, P, zv, tw, tw, c);
-        break;
-    }
-}
 
 bool lines32_supported(int n) { return n == 64 || n == 128 || n == 256 || n == 512 || n == 1024; }
 
-template <int N, bool INV, int W> void xy_attr()
-{
-    cudaFuncSetAttribute(k_xy32<N, INV, W>, cudaFuncAttributeMaxDynamicSharedMemorySize, N * LANES * 8);
-}
-
 void lines32_init()
 {
-    xy_attr<64, false, 0>();
-    xy_attr<64, true, 0>();
-    xy_attr<128, false, 0>();
-    xy_attr<128, true, 0>();
-    xy_attr<256, false, 0>();
-    xy_attr<256, true, 0>();
-    xy_attr<512, false, 0>();
-    xy_attr<512, true, 1>();
-    xy_attr<1024, false, 0>();
-    xy_attr<1024, true, 0>();
     cudaFuncSetAttribute(k_lines32<1024, false, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, 1024 * LANES * 8);
     cudaFuncSetAttribute(k_lines32<1024, true, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, 1024 * LANES * 8);
     cudaFuncSetAttribute(k_lines32<512, false, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, 512 * LANES * 8);

@@ -96,9 +96,6 @@ struct ps3d_gpu_ctx {
     float *es_src = nullptr;
     double *mf64 = nullptr;
     const double *mf_a = nullptr;
-    // control block of the one-launch FP32 horizontal transforms (mixed
-    // form; null where the grid takes two line passes)
-    unsigned int *xyctl = nullptr;
     // transient fields (storage type T)
     void *vor = nullptr, *vel = nullptr, *svel = nullptr, *svorts = nullptr, *held = nullptr;
     void *tmp = nullptr;         // NTMP consecutive fields
@@ -198,18 +195,6 @@ int sync_check(ps3d_gpu_ctx *c, const char *where)
     return PS3D_OK;
 }
 
-// the one-launch horizontal transforms' error word (a wait that ran out),
-// read after a synchronisation; cleared once reported
-int xy_error(ps3d_gpu_ctx *c)
-{
-    if (!c->xyctl) return PS3D_OK;
-    unsigned int e = 0;
-    cudaMemcpy(&e, c->xyctl, sizeof(e), cudaMemcpyDeviceToHost);
-    if (!e) return PS3D_OK;
-    cudaMemset(c->xyctl, 0, sizeof(e));
-    return fail(c, PS3D_ERR_DEVICE_LIMIT, "horizontal transform: a wait for its first pass ran out");
-}
-
 template <typename P> bool dalloc(ps3d_gpu_ctx *c, P **p, size_t bytes)
 {
     void *q = nullptr;
@@ -280,13 +265,13 @@ int download(ps3d_gpu_ctx *c, const void *src, bool src_is_fp64, int ncomp, doub
 // ------------------------------------------------------------- primitives
 template <typename T> void xyf(ps3d_gpu_ctx *c, const T *in, T *out)
 {
-    xy_forward<T>(c->d, c->st, in, out, tf<CT<T>>(c->twx), tf<CT<T>>(c->twy), &c->probe, c->xyctl);
-    c->launches += (sizeof(T) == sizeof(float) && c->xyctl) ? 1 : NL_XY;
+    xy_forward<T>(c->d, c->st, in, out, tf<CT<T>>(c->twx), tf<CT<T>>(c->twy), &c->probe);
+    c->launches += NL_XY;
 }
 template <typename T> void xyi(ps3d_gpu_ctx *c, const T *in, T *out)
 {
-    xy_inverse<T>(c->d, c->st, in, out, tf<CT<T>>(c->twx), tf<CT<T>>(c->twy), &c->probe, c->xyctl);
-    c->launches += (sizeof(T) == sizeof(float) && c->xyctl) ? 1 : NL_XY;
+    xy_inverse<T>(c->d, c->st, in, out, tf<CT<T>>(c->twx), tf<CT<T>>(c->twy), &c->probe);
+    c->launches += NL_XY;
 }
 template <typename T, typename TIN> void col_any(ps3d_gpu_ctx *c, int mode, const TIN *in, T *out)
 {
@@ -749,7 +734,6 @@ template <typename T> int adapt(ps3d_gpu_ctx *c, double t, double *dt_out, ps3d_
     cudaMemcpyAsync(r2, c->res2, RED2_N * sizeof(double), cudaMemcpyDeviceToHost, c->st);
     cudaMemcpyAsync(&hflag, c->flag, sizeof(int), cudaMemcpyDeviceToHost, c->st);
     rc = sync_check(c, "adapt");
-    if (!rc) rc = xy_error(c);
     if (rc) return rc;
     if (hflag) return fail(c, PS3D_ERR_DEVICE_LIMIT, "adapt: Jacobi sweep limit reached");
     const double small = 1.0e-12;
@@ -1274,7 +1258,6 @@ int graph_finish(ps3d_gpu_ctx *c, double *t, ps3d_gpu_diag *diag)
     cudaMemcpyAsync(c->roll.hist.data(), c->roll_dev, c->roll.hist.size() * sizeof(double),
                     cudaMemcpyDeviceToHost, c->st);
     int rc = sync_check(c, "graph_finish");
-    if (!rc) rc = xy_error(c);
     if (rc) return rc;
     c->roll.sma = h.sma;
     c->roll.inew = h.inew;
@@ -1830,7 +1813,6 @@ template <typename T> int allocate_fields(ps3d_gpu_ctx *c)
     }
     if (ok && !c->fp64)
         ok = dalloc(c, &c->svor32, 3 * N * sizeof(float)) && dalloc(c, &c->es_src, N * sizeof(float)) &&
-             (!xy32_supported(d.nx, d.ny, d.P) || dalloc(c, &c->xyctl, xy_control_bytes())) &&
              dalloc(c, &c->mf64, 2 * (size_t)d.P * sizeof(double)) &&
              dalloc(c, &c->twz32, d.nz * sizeof(float2)) && dalloc(c, &c->sinz32, d.nz * sizeof(float)) &&
              dalloc(c, &c->cosz32, d.nz * sizeof(float)) &&

@@ -136,24 +136,9 @@ template <typename T> static double pass_bytes(const Dims &d)
 }
 
 template <typename T>
-static bool xy_fused(const Dims &d, void *xyctl)
-{
-    return sizeof(T) == sizeof(float) && xyctl && xy32_supported(d.nx, d.ny, d.P);
-}
-
-template <typename T>
 void xy_forward(const Dims &d, cudaStream_t st, const T *in, T *out, const typename cplx<T>::type *twx,
-                const typename cplx<T>::type *twy, Probe *pr, void *xyctl)
+                const typename cplx<T>::type *twy, Probe *pr)
 {
-    if (xy_fused<T>(d, xyctl)) {
-        // both passes in one launch (algorithmic bytes: one read and one
-        // write of the field)
-        if (pr) pr->begin(PROBE_XYFUSED, st);
-        launch_xy32(st, reinterpret_cast<const float *>(in), reinterpret_cast<float *>(out), d.nx, d.P, d.nz + 1,
-                    false, reinterpret_cast<const float2 *>(twx), xyctl);
-        if (pr) pr->end(PROBE_XYFUSED, st, pass_bytes<T>(d));
-        return;
-    }
     // y lines: line stride P (one column), batches over x (stride ny*P)
     if (pr) pr->begin(PROBE_YLINES, st);
     launch_lines<T>(st, in, out, d.ny, d.P, d.nz + 1, d.P, d.nx, (long long)d.ny * d.P, false, twy, d.line_shape[0]);
@@ -166,15 +151,8 @@ void xy_forward(const Dims &d, cudaStream_t st, const T *in, T *out, const typen
 
 template <typename T>
 void xy_inverse(const Dims &d, cudaStream_t st, const T *in, T *out, const typename cplx<T>::type *twx,
-                const typename cplx<T>::type *twy, Probe *pr, void *xyctl)
+                const typename cplx<T>::type *twy, Probe *pr)
 {
-    if (xy_fused<T>(d, xyctl)) {
-        if (pr) pr->begin(PROBE_XYFUSED, st);
-        launch_xy32(st, reinterpret_cast<const float *>(in), reinterpret_cast<float *>(out), d.nx, d.P, d.nz + 1,
-                    true, reinterpret_cast<const float2 *>(twx), xyctl);
-        if (pr) pr->end(PROBE_XYFUSED, st, pass_bytes<T>(d));
-        return;
-    }
     if (pr) pr->begin(PROBE_XLINES, st);
     launch_lines<T>(st, in, out, d.nx, d.P, d.nz + 1, (long long)d.ny * d.P, d.ny, d.P, true, twx, d.line_shape[3]);
     if (pr) pr->end(PROBE_XLINES, st, pass_bytes<T>(d));
@@ -345,13 +323,13 @@ void transforms_init()
 }
 
 template void xy_forward<double>(const Dims &, cudaStream_t, const double *, double *, const double2 *,
-                                 const double2 *, Probe *, void *);
+                                 const double2 *, Probe *);
 template void xy_forward<float>(const Dims &, cudaStream_t, const float *, float *, const float2 *,
-                                const float2 *, Probe *, void *);
+                                const float2 *, Probe *);
 template void xy_inverse<double>(const Dims &, cudaStream_t, const double *, double *, const double2 *,
-                                 const double2 *, Probe *, void *);
+                                 const double2 *, Probe *);
 template void xy_inverse<float>(const Dims &, cudaStream_t, const float *, float *, const float2 *,
-                                const float2 *, Probe *, void *);
+                                const float2 *, Probe *);
 template void columns<double>(const Dims &, cudaStream_t, int, const double *, double *, const double *,
                               const double *, const double2 *, Probe *);
 template void columns<float>(const Dims &, cudaStream_t, int, const float *, float *, const float *,

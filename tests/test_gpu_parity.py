@@ -460,11 +460,10 @@ def test_mixed_held_source_step_matches_oracle(n):
 @pytest.mark.parametrize("grid", [(64, 64, 64), (128, 128, 40), (256, 256, 8), (512, 512, 72), (1024, 1024, 8)],
                          ids=lambda g: "x".join(map(str, g)))
 @pytest.mark.parametrize("op", ["fftxyp2s", "fftxys2p", "decompose_physical", "combine_physical"])
-def test_mixed_one_launch_horizontal_transforms_match_oracle(grid, op):
-    """Square planes take both line passes in one launch (the second pass
-    one z-tile behind the first, reading its intermediate from L2): FP32
-    against the FP64 oracle within 2e-6, for one to three tiles of 32
-    levels."""
+def test_mixed_square_plane_transforms_match_oracle(grid, op):
+    """FP32 horizontal transforms of square planes (the benchmark's shape)
+    at every line length of the register-butterfly kernels, over one to
+    three tiles of 32 levels, against the FP64 oracle within 2e-6."""
     o = oracle.Oracle(*grid, [0.0, 0.0, 0.0], [2.0, 2.0, 0.5])
     g = Ps3dGpu(*grid, [0.0, 0.0, 0.0], [2.0, 2.0, 0.5], precision="mixed")
     f = np.random.default_rng(14).standard_normal(o.shape)
