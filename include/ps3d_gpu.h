@@ -273,12 +273,16 @@ int ps3d_gpu_advance_graph(ps3d_gpu_ctx *ctx, double *t, int nsteps, ps3d_gpu_di
 int ps3d_gpu_batch_advance(ps3d_gpu_ctx *const *ctx, int n, double *t, int nsteps, double *ms);
 
 /* Line-FFT autotuner (no reference counterpart): at creation the mixed form
- * times each block shape of the FP32 line FFTs where a line length has more
- * than one (512 points: 512-thread blocks, two per SM, or 256-thread blocks,
- * three per SM) for the passes forward y, forward x, inverse y, inverse x,
- * and keeps the fastest.  shape[4]: the choice per pass (-1 = the only
- * shape); ms[8]: ms per launch of shapes 0 and 1 per pass (0 = not timed). */
-int ps3d_gpu_tuning(ps3d_gpu_ctx *ctx, int shape[4], double ms[8]);
+ * times each kernel shape of the FP32 line FFTs where a line length has more
+ * than one, for the passes forward y, forward x, inverse y, inverse x, and
+ * keeps the fastest.  Shapes: 0 the default blocks (at 512 points 512
+ * threads, two per SM), 1 256-thread blocks, three per SM (512 points), 2
+ * the TMA-fed persistent kernel (128, 256 and 512 points: one block per SM
+ * with two tile buffers, tensor copies of the next tile overlapping the
+ * current one's butterflies).  shape[4]: the choice per pass (-1 = the
+ * only shape); ms[12]: ms per launch of shapes 0, 1, 2 per pass (0 = not
+ * timed). */
+int ps3d_gpu_tuning(ps3d_gpu_ctx *ctx, int shape[4], double ms[12]);
 /* Pin the line-FFT block shapes (e.g. for reproducible timings); -1 = the
  * default shape.  PS3D_ERR_INVALID_ARG for a shape the line length lacks. */
 int ps3d_gpu_set_tuning(ps3d_gpu_ctx *ctx, const int shape[4]);

@@ -68,13 +68,18 @@ void columns(const Dims &d, cudaStream_t st, int mode, const T *in, T *out, cons
 // FP32 bandwidth-tuned line FFTs (lines32.cu), n = 64..1024
 bool lines32_supported(int n);
 void lines32_init();
-// shape: -1 default, 0 512-thread blocks (two per SM), 1 256-thread blocks
-// (three per SM); the two differ only at n = 512
+// shape: -1 default, 0 the default blocks (512 threads, two per SM, at
+// n = 512), 1 256-thread blocks (three per SM, n = 512), 2 the TMA-fed
+// persistent kernel (n = 128..512); a shape the length lacks runs the default
 // zv = nz+1 valid z rows; rows zv..P-1 (padding) are read as zero
 void launch_lines32(cudaStream_t st, const float *in, float *out, int n, int P, int zv, long long line_stride,
                     long long nbatch, long long batch_stride, bool inverse, const float2 *tw, int shape = -1);
-// number of block shapes the autotuner can choose from at line length n
-int lines32_shapes(int n);
+// kernel shapes at line length n: 0 the default blocks, 1 256-thread blocks
+// (n = 512), 2 the TMA-fed persistent kernel (n = 128, 256, 512)
+bool lines32_has_shape(int n, int w);
+int lines32_shapes(int n);  // how many of them n has
+// a bounded wait of the TMA-fed kernel ran out since the last call (cleared)
+int lines32_error();
 // FP32 half-length warp z transforms (colz.cu), nz = 64..1024
 bool colz_supported(int nz);
 void colz_init();

@@ -15,6 +15,9 @@
 // the Hermitian rows k and N - k as it loads them (one lane per thread
 // there, to bound the registers).  N (the line length) is a compile-time
 // constant: 64..1024.
+#include <cuda.h>
+#include <cudaTypedefs.h>
+
 #include "kernels.h"
 
 namespace ps3d {
@@ -276,10 +279,260 @@ void launch32w(cudaStream_t st, const float *in, float *out, int P, int zv, long
     k_lines32<N, INV, W><<<grid, LinePlan<N, INV, W>::T, sm, st>>>(in, out, P, zv, ls, bs, tw);
 }
 
+
+// ------------------------------------------------------------------------
+// TMA-fed persistent form (N = 128, 256, 512).  One block per SM owns two
+// tile buffers in shared memory; while it transforms the tile in one
+// buffer, a cp.async.bulk.tensor copy brings its next tile into the other,
+// so the loads of a block overlap its arithmetic.  A tile is the same
+// 32-level slab of one line set as above, copied as N rows of 128 bytes by
+// 3-D tensor copies (z, y, x) of at most 256 rows each.  The tensor's z
+// extent is nz + 1, so the copy fills the padding rows above the top wall
+// with zeros.  The butterflies are those of the kernel above, the first
+// pass reading the tile from shared memory.  Every mbarrier wait is bounded
+// (about a second); one that runs out sets the error word and the block
+// stops taking tiles (the host reports PS3D_ERR_DEVICE_LIMIT).
+__device__ unsigned int g_lines_err;
+
+__device__ __forceinline__ uint32_t smem_addr(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ bool tma_wait(uint32_t bar, uint32_t parity)
+{
+    for (int i = 0; i < (1 << 21); ++i) {
+        uint32_t ok;
+        asm volatile(
+            "{\n.reg .pred p;\nmbarrier.test_wait.parity.shared::cta.b64 p, [%1], %2;\nselp.u32 %0, 1, 0, p;\n}\n"
+            : "=r"(ok)
+            : "r"(bar), "r"(parity)
+            : "memory");
+        if (ok) return true;
+        if (i > 32) __nanosleep(128);
+    }
+    return false;
+}
+
+// the inverse transform's first pass from the Hermitian rows of the tile in
+// shared memory (the same items as herm_first_pass; every thread holds at
+// most one item, read completely before the buffer is overwritten)
+template <int N, int W> __device__ __forceinline__ void herm_first_pass_smem(float2 *sm2)
+{
+    constexpr int T = LinePlan<N, true, W>::T, NB = N / 8, SLOTS = NB / 2;
+    constexpr int ITEMS = SLOTS * LANES;
+    static_assert(ITEMS <= T, "one item per thread");
+    const int it = threadIdx.x;
+    const bool act = it < ITEMS;
+    const int lane = it & (LANES - 1), s = it / LANES;
+    const int j1 = s == 0 ? 0 : s, j2 = s == 0 ? NB / 2 : NB - s;
+    float2 h1[8], h2[8];
+    if (act) {
+#pragma unroll
+        for (int r = 0; r < 8; ++r) {
+            h1[r] = sm2[(j1 + r * NB) * LANES + lane];
+            h2[r] = sm2[(j2 + r * NB) * LANES + lane];
+        }
+    }
+    __syncthreads();
+    if (act) {
+        float2 a[8], b[8];
+        if (s == 0) {
+#pragma unroll
+            for (int r = 0; r < 8; ++r) {
+                const int rm = (8 - r) & 7;
+                a[r] = (r == 0 || r == 4) ? h1[r] : (r < 4 ? herm_low(h1[r], h1[rm]) : herm_high(h1[rm], h1[r]));
+            }
+#pragma unroll
+            for (int r = 0; r < 8; ++r)
+                b[r] = r < 4 ? herm_low(h2[r], h2[7 - r]) : herm_high(h2[7 - r], h2[r]);
+        } else {
+#pragma unroll
+            for (int r = 0; r < 8; ++r) {
+                if (r < 4) {
+                    a[r] = herm_low(h1[r], h2[7 - r]);
+                    b[7 - r] = herm_high(h1[r], h2[7 - r]);
+                } else {
+                    a[r] = herm_high(h2[7 - r], h1[r]);
+                    b[7 - r] = herm_low(h2[7 - r], h1[r]);
+                }
+            }
+        }
+        dftR<8, true>(a);
+        dftR<8, true>(b);
+#pragma unroll
+        for (int r = 0; r < 8; ++r) {
+            sm2[(j1 * 8 + r) * LANES + lane] = a[r];
+            sm2[(j2 * 8 + r) * LANES + lane] = b[r];
+        }
+    }
+    __syncthreads();
+}
+
+// ylines: the lines run along the tensor's second dimension (y lines; tiles
+// are numbered z-tile fastest, then the x index), else along the third
+template <int N, bool INV>
+__global__ void __launch_bounds__(LinePlan<N, INV, 0>::T, 1)
+    k_lines32_tma(const __grid_constant__ CUtensorMap tmap, float *__restrict__ out, int P, long long line_stride,
+                  long long batch_stride, int ztiles, long long ntiles, int ylines, const float2 *__restrict__ tw)
+{
+    constexpr int W = 0;
+    constexpr int T = LinePlan<N, INV, W>::T;
+    constexpr int BOX = N < 256 ? N : 256;
+    constexpr uint32_t TILE_BYTES = N * 128;
+    extern __shared__ __align__(128) unsigned char smraw[];
+    __shared__ __align__(8) unsigned long long mbar[2];
+    __shared__ int stop;
+    const uint32_t bar0 = smem_addr(&mbar[0]), bar1 = smem_addr(&mbar[1]);
+    if (threadIdx.x == 0) {
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(bar0) : "memory");
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(bar1) : "memory");
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        stop = 0;
+    }
+    __syncthreads();
+    // thread 0: copy tile `tile` into buffer b
+    auto issue = [&](long long tile, int b) {
+        const int zt = (int)(tile % ztiles);
+        const int batch = (int)(tile / ztiles);
+        const uint32_t bar = b ? bar1 : bar0;
+        const uint32_t dst = smem_addr(smraw + (size_t)b * TILE_BYTES);
+        // the buffer was last read through the generic proxy
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(TILE_BYTES) : "memory");
+#pragma unroll
+        for (int r0 = 0; r0 < N; r0 += BOX) {
+            const int c0 = zt * 2 * LANES, c1 = ylines ? r0 : batch, c2 = ylines ? batch : r0;
+            asm volatile(
+                "cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], [%5];" ::"r"(
+                    dst + (uint32_t)r0 * 128u),
+                "l"(&tmap), "r"(c0), "r"(c1), "r"(c2), "r"(bar)
+                : "memory");
+        }
+    };
+    long long tile = blockIdx.x;
+    if (threadIdx.x == 0 && tile < ntiles) issue(tile, 0);
+    uint32_t ph0 = 0, ph1 = 0;
+    const int p = threadIdx.x & (PAIRS - 1);
+    const float sc = rsqrtf((float)N);
+    constexpr int H = N / 2;
+    for (int b = 0; tile < ntiles; tile += gridDim.x, b ^= 1) {
+        const long long next = tile + gridDim.x;
+        // buffer b ^ 1 was released by the barrier that ended the last tile
+        if (threadIdx.x == 0 && next < ntiles) issue(next, b ^ 1);
+        if (!tma_wait(b ? bar1 : bar0, b ? ph1 : ph0)) {
+            atomicOr(&g_lines_err, 1u);
+            stop = 1;
+        }
+        if (b) ph1 ^= 1u;
+        else ph0 ^= 1u;
+        __syncthreads();
+        if (stop) break;
+        float4 *sm = reinterpret_cast<float4 *>(smraw + (size_t)b * TILE_BYTES);
+        const int zt = (int)(tile % ztiles);
+        const long long batch = tile / ztiles;
+        const int z0 = zt * 2 * LANES;
+        const bool valid = z0 + 4 * p < P;
+        const long long base = batch * batch_stride + z0;
+        const long long gs = line_stride >> 2;
+        if (!INV) {
+            pass<N, 8, 1, false, W, false, false>(sm, nullptr, nullptr, gs, valid, 1.0f, tw);
+            later_passes<N, false, W, false>(sm, nullptr, gs, valid, 1.0f, tw);
+            float4 *o = reinterpret_cast<float4 *>(out + base);
+            for (int e = threadIdx.x; e < (H + 1) * PAIRS; e += T) {
+                const int k = e / PAIRS, q = e & (PAIRS - 1);
+                if (z0 + 4 * q >= P) continue;
+                const float4 ck = sm[k * PAIRS + q];
+                const float4 cn = sm[((N - k) & (N - 1)) * PAIRS + q];
+                const float4 re = make_float4(0.5f * (ck.x + cn.x) * sc, 0.5f * (ck.y + cn.y) * sc,
+                                              0.5f * (ck.z + cn.z) * sc, 0.5f * (ck.w + cn.w) * sc);
+                o[k * gs + q] = re;
+                if (k > 0 && k < H)
+                    o[(N - k) * gs + q] = make_float4(0.5f * (ck.y - cn.y) * sc, -0.5f * (ck.x - cn.x) * sc,
+                                                      0.5f * (ck.w - cn.w) * sc, -0.5f * (ck.z - cn.z) * sc);
+            }
+        } else {
+            herm_first_pass_smem<N, W>(reinterpret_cast<float2 *>(sm));
+            float4 *gout = reinterpret_cast<float4 *>(out + base) + p;
+            later_passes<N, true, W, true>(sm, gout, gs, valid, sc, tw);
+        }
+        __syncthreads();
+    }
+    // a copy issued for a tile this block no longer takes (after a stop):
+    // wait for it (bounded) before the block's shared memory is released
+    if (stop && threadIdx.x == 0) {
+        const long long next = tile + gridDim.x;
+        if (next < ntiles) tma_wait(bar0, ph0), tma_wait(bar1, ph1);
+    }
+}
+
+using EncodeTiled = PFN_cuTensorMapEncodeTiled_v12000;
+
+EncodeTiled tensor_encoder()
+{
+    static EncodeTiled fn = nullptr;
+    static bool tried = false;
+    if (!tried) {
+        tried = true;
+        void *f = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &f, 12000, cudaEnableDefault, &q) ==
+                cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = reinterpret_cast<EncodeTiled>(f);
+        cudaGetLastError();
+    }
+    return fn;
+}
+
+// false: no tensor map for this field (the caller takes the plain kernel)
+template <int N, bool INV>
+bool launch32tma(cudaStream_t st, const float *in, float *out, int P, int zv, long long ls, long long nbatch,
+                 long long bs, const float2 *tw)
+{
+    EncodeTiled enc = tensor_encoder();
+    if (!enc) return false;
+    // y lines: line stride P, batches over x; x lines: line stride ny P,
+    // batches over y
+    const bool ylines = ls == P;
+    const long long ny = ylines ? N : nbatch, nx = ylines ? nbatch : N;
+    cuuint64_t dims[3] = {(cuuint64_t)zv, (cuuint64_t)ny, (cuuint64_t)nx};
+    cuuint64_t strides[2] = {(cuuint64_t)P * 4, (cuuint64_t)P * 4 * (cuuint64_t)ny};
+    constexpr int BOX = N < 256 ? N : 256;
+    cuuint32_t box[3] = {32, ylines ? (cuuint32_t)BOX : 1u, ylines ? 1u : (cuuint32_t)BOX};
+    cuuint32_t es[3] = {1, 1, 1};
+    CUtensorMap map;
+    if (enc(&map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, const_cast<float *>(in), dims, strides, box, es,
+            CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+            CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
+        return false;
+    static int blocks = 0;  // resident blocks (the same on every GB300)
+    const size_t sm = 2 * (size_t)N * 128;
+    if (!blocks) {
+        int dev = 0, sms = 1, per = 1;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_lines32_tma<N, INV>, LinePlan<N, INV, 0>::T, sm);
+        blocks = sms * (per > 0 ? per : 1);
+    }
+    const int ztiles = (P + 2 * LANES - 1) / (2 * LANES);
+    const long long ntiles = (long long)ztiles * nbatch;
+    const int grid = (int)(ntiles < blocks ? ntiles : blocks);
+    k_lines32_tma<N, INV><<<grid, LinePlan<N, INV, 0>::T, sm, st>>>(map, out, P, ls, bs, ztiles, ntiles,
+                                                                    ylines ? 1 : 0, tw);
+    return true;
+}
+
 template <int N>
 void launch32(cudaStream_t st, const float *in, float *out, int P, int zv, long long ls, long long nbatch,
               long long bs, bool inverse, const float2 *tw, int shape)
 {
+    // shape 2: the TMA-fed persistent kernel (N = 128, 256, 512)
+    if constexpr (N >= 128 && N <= 512) {
+        if (shape == 2) {
+            const bool ok = inverse ? launch32tma<N, true>(st, in, out, P, zv, ls, nbatch, bs, tw)
+                                    : launch32tma<N, false>(st, in, out, P, zv, ls, nbatch, bs, tw);
+            if (ok) return;
+            shape = -1;
+        }
+    }
     if (N == 512) {
         const int w = shape < 0 ? (inverse ? 1 : 0) : shape;
         if (inverse) {
@@ -301,15 +554,50 @@ bool lines32_supported(int n) { return n == 64 || n == 128 || n == 256 || n == 5
 
 void lines32_init()
 {
+    tensor_encoder();  // resolve the driver's tensor-map encoder outside any stream capture
     cudaFuncSetAttribute(k_lines32<1024, false, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, 1024 * LANES * 8);
     cudaFuncSetAttribute(k_lines32<1024, true, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, 1024 * LANES * 8);
     cudaFuncSetAttribute(k_lines32<512, false, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, 512 * LANES * 8);
     cudaFuncSetAttribute(k_lines32<512, true, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, 512 * LANES * 8);
     cudaFuncSetAttribute(k_lines32<512, false, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, 512 * LANES * 8);
     cudaFuncSetAttribute(k_lines32<512, true, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, 512 * LANES * 8);
+    cudaFuncSetAttribute(k_lines32_tma<512, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, 2 * 512 * 128);
+    cudaFuncSetAttribute(k_lines32_tma<512, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, 2 * 512 * 128);
+    cudaFuncSetAttribute(k_lines32_tma<256, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, 2 * 256 * 128);
+    cudaFuncSetAttribute(k_lines32_tma<256, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, 2 * 256 * 128);
+    cudaFuncSetAttribute(k_lines32_tma<128, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, 2 * 128 * 128);
+    cudaFuncSetAttribute(k_lines32_tma<128, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, 2 * 128 * 128);
 }
 
-int lines32_shapes(int n) { return n == 512 ? 2 : 1; }
+// kernel shapes: 0 the default blocks, 1 the 256-thread blocks (N = 512),
+// 2 the TMA-fed persistent kernel (N = 128, 256, 512)
+bool lines32_has_shape(int n, int w)
+{
+    if (w == 0) return lines32_supported(n);
+    if (w == 1) return n == 512;
+    return w == 2 && (n == 128 || n == 256 || n == 512);
+}
+
+int lines32_shapes(int n)
+{
+    int c = 0;
+    for (int w = 0; w < 3; ++w) c += lines32_has_shape(n, w) ? 1 : 0;
+    return c;
+}
+
+int lines32_error()
+{
+    unsigned int e = 0;
+    if (cudaMemcpyFromSymbol(&e, g_lines_err, sizeof(e)) != cudaSuccess) {
+        cudaGetLastError();
+        return 0;
+    }
+    if (e) {
+        const unsigned int z = 0;
+        cudaMemcpyToSymbol(g_lines_err, &z, sizeof(z));
+    }
+    return e ? 1 : 0;
+}
 
 void launch_lines32(cudaStream_t st, const float *in, float *out, int n, int P, int zv, long long line_stride,
                     long long nbatch, long long batch_stride, bool inverse, const float2 *tw, int shape)

@@ -138,7 +138,7 @@ struct ps3d_gpu_ctx {
     unsigned long long serial = 0;
     // line-FFT autotuner: ms per launch of each block shape for the passes
     // forward y, forward x, inverse y, inverse x (0 where not timed)
-    double tune_ms[4][2] = {{0, 0}, {0, 0}, {0, 0}, {0, 0}};
+    double tune_ms[4][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
     // kinetic-energy spectrum scratch (allocated on first use): rkx, rky,
     // shell sums, shell counts
     double *spec_buf = nullptr;
@@ -736,6 +736,7 @@ template <typename T> int adapt(ps3d_gpu_ctx *c, double t, double *dt_out, ps3d_
     rc = sync_check(c, "adapt");
     if (rc) return rc;
     if (hflag) return fail(c, PS3D_ERR_DEVICE_LIMIT, "adapt: Jacobi sweep limit reached");
+    if (lines32_error()) return fail(c, PS3D_ERR_DEVICE_LIMIT, "line transform: a wait for a tile copy ran out");
     const double small = 1.0e-12;
     const double vorch = r2[1] / (small + r2[0]);
     const double ggmax = r2[2], usggmax = r2[3], lsggmax = r2[4];
@@ -1259,6 +1260,7 @@ int graph_finish(ps3d_gpu_ctx *c, double *t, ps3d_gpu_diag *diag)
                     cudaMemcpyDeviceToHost, c->st);
     int rc = sync_check(c, "graph_finish");
     if (rc) return rc;
+    if (lines32_error()) return fail(c, PS3D_ERR_DEVICE_LIMIT, "line transform: a wait for a tile copy ran out");
     c->roll.sma = h.sma;
     c->roll.inew = h.inew;
     c->roll.iold = h.iold;
@@ -1762,7 +1764,8 @@ int autotune_lines(ps3d_gpu_ctx *c)
         const long long ls = xl ? (long long)d.ny * d.P : d.P, nb = xl ? d.ny : d.nx,
                         bs = xl ? d.P : (long long)d.ny * d.P;
         int best = 0;
-        for (int w = 0; w < ns; ++w) {
+        for (int w = 0; w < 3; ++w) {
+            if (!lines32_has_shape(n, w)) continue;
             launch_lines32(c->st, a, b, n, d.P, d.nz + 1, ls, nb, bs, inv, xl ? twx : twy, w);
             cudaEventRecord(c->ev0, c->st);
             for (int r = 0; r < 3; ++r) launch_lines32(c->st, a, b, n, d.P, d.nz + 1, ls, nb, bs, inv, xl ? twx : twy, w);
@@ -2484,15 +2487,14 @@ int ps3d_gpu_batch_advance(ps3d_gpu_ctx *const *ctx, int n, double *t, int nstep
     return rc ? rc : rf;
 }
 
-int ps3d_gpu_tuning(ps3d_gpu_ctx *c, int shape[4], double ms[8])
+int ps3d_gpu_tuning(ps3d_gpu_ctx *c, int shape[4], double ms[12])
 {
     int rc = enter(c);
     if (rc) return rc;
     if (!shape || !ms) return PS3D_ERR_INVALID_ARG;
     for (int p = 0; p < 4; ++p) {
         shape[p] = c->d.line_shape[p];
-        ms[2 * p] = c->tune_ms[p][0];
-        ms[2 * p + 1] = c->tune_ms[p][1];
+        for (int w = 0; w < 3; ++w) ms[3 * p + w] = c->tune_ms[p][w];
     }
     return PS3D_OK;
 }
@@ -2504,7 +2506,7 @@ int ps3d_gpu_set_tuning(ps3d_gpu_ctx *c, const int shape[4])
     if (!shape) return PS3D_ERR_INVALID_ARG;
     for (int p = 0; p < 4; ++p) {
         const int n = (p & 1) ? c->d.nx : c->d.ny;
-        if (shape[p] < -1 || shape[p] >= lines32_shapes(n)) return PS3D_ERR_INVALID_ARG;
+        if (shape[p] < -1 || (shape[p] >= 0 && !lines32_has_shape(n, shape[p]))) return PS3D_ERR_INVALID_ARG;
     }
     if (c->graph) {  // a captured step holds the old shapes
         cudaGraphExecDestroy(c->graph);

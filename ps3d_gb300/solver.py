@@ -289,11 +289,12 @@ class Ps3dGpu:
 
     def tuning(self):
         """Line-FFT autotuner result: (shape per pass [fwd y, fwd x, inv y,
-        inv x], ms per launch of each shape per pass)."""
+        inv x], ms per launch of shapes 0, 1, 2 per pass, 0 where a shape
+        was not timed)."""
         sh = (ctypes.c_int * 4)()
-        ms = (ctypes.c_double * 8)()
+        ms = (ctypes.c_double * 12)()
         self._chk(self.L.ps3d_gpu_tuning(self._h, sh, ms))
-        return list(sh), [list(ms[2 * i:2 * i + 2]) for i in range(4)]
+        return list(sh), [list(ms[3 * i:3 * i + 3]) for i in range(4)]
 
     def set_tuning(self, shapes):
         """Pin the line-FFT block shape per pass (-1 = default)."""

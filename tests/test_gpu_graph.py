@@ -70,21 +70,29 @@ def test_graph_refused_for_fp64_form():
         m.advance_graph(0.0, 1)
 
 
-@pytest.mark.parametrize("grid", [(512, 16, 8), (16, 512, 8)], ids=lambda g: "x".join(map(str, g)))
+@pytest.mark.parametrize("grid", [(512, 16, 8), (16, 512, 8), (256, 32, 40), (32, 128, 72)],
+                         ids=lambda g: "x".join(map(str, g)))
 def test_line_fft_shapes_all_match_oracle(grid):
-    """Both block shapes of the 512-point line FFT (the autotuner's choices)
-    against the FP64 oracle, and the autotuner's record."""
+    """Every kernel shape of the FP32 line FFTs (the autotuner's choices:
+    512- and 256-thread blocks at 512 points, the TMA-fed persistent kernel
+    at 128, 256 and 512 points) against the FP64 oracle, and the
+    autotuner's record."""
     import oracle
     from tests.parity_util import rel_l2
     o = oracle.Oracle(*grid, [0.0, 0.0, 0.0], [1.0, 2.0, 0.5])
     g = Ps3dGpu(*grid, [0.0, 0.0, 0.0], [1.0, 2.0, 0.5], precision="mixed")
     shapes, ms = g.tuning()
-    timed = [p for p in range(4) if ((p & 1) and grid[0] == 512) or (not (p & 1) and grid[1] == 512)]
-    for p in timed:
-        assert shapes[p] in (0, 1) and min(ms[p]) > 0
+    # shapes per line length (0 default, 1 256-thread blocks, 2 TMA-fed)
+    have = {512: (0, 1, 2), 256: (0, 2), 128: (0, 2)}
+    lengths = [grid[1], grid[0], grid[1], grid[0]]  # fwd y, fwd x, inv y, inv x
+    for p in range(4):
+        ws = have.get(lengths[p], ())
+        if len(ws) > 1:
+            assert shapes[p] in ws and all(ms[p][w] > 0 for w in ws), (p, shapes[p], ms[p])
     f = np.random.default_rng(5).standard_normal(o.shape)
-    for w in (0, 1):
-        g.set_tuning([w if p in timed else -1 for p in range(4)])
+    for w in (0, 1, 2):
+        pin = [w if w in have.get(lengths[p], ()) else -1 for p in range(4)]
+        g.set_tuning(pin)
         for op in ("fftxyp2s", "fftxys2p"):
             err = rel_l2(getattr(g, op)(f), getattr(o, op)(f))
             assert err < 2e-6, (w, op, err)
