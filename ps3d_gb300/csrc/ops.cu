@@ -383,26 +383,46 @@ template void op_products_dz<float>(const Dims &, cudaStream_t, double, const fl
                                     float *, float *, float *, float *);
 
 // svorts = (D_y r - dq/dz, dp/dz - D_x r, D_x q - D_y p) (inversion.f90:341-367)
+// in orbit form (as k_v2v_orbit): one warp per partner orbit, so r, q and p
+// are read once each instead of once per partner that needs them; the same
+// expression per output as the per-column form.
 template <typename T>
-__global__ void k_svorts(Dims d, Deriv D, const T *__restrict__ r, const T *__restrict__ q,
-                         const T *__restrict__ p, const T *__restrict__ gq, const T *__restrict__ gp,
-                         T *__restrict__ s1, T *__restrict__ s2, T *__restrict__ s3)
+__global__ void k_svorts_orbit(Dims d, Deriv D, const T *__restrict__ r, const T *__restrict__ q,
+                               const T *__restrict__ p, const T *__restrict__ gq, const T *__restrict__ gp,
+                               T *__restrict__ s1, T *__restrict__ s2, T *__restrict__ s3)
 {
-    COLUMN_HEADER
-    PARTNERS
-    const T cx = (T)cxk, cy = (T)cyk;
+    const int hy = d.ny / 2 + 1;
+    const long long orb = (long long)blockIdx.x * COLS_PER_BLOCK + threadIdx.y;
+    if (orb >= (long long)(d.nx / 2 + 1) * hy) return;
+    const int kx = (int)(orb / hy), ky = (int)(orb - (long long)kx * hy);
+    const int x2 = xsrc(kx, d.nx), y2 = xsrc(ky, d.ny);
+    const long long o00 = ((long long)ky + (long long)d.ny * kx) * d.P, o10 = ((long long)ky + (long long)d.ny * x2) * d.P;
+    const long long o01 = ((long long)y2 + (long long)d.ny * kx) * d.P, o11 = ((long long)y2 + (long long)d.ny * x2) * d.P;
+    const bool dx = x2 != kx, dy = y2 != ky;
+    const T cxa = (T)D.cx[kx], cxb = (T)D.cx[x2], cya = (T)D.cy[ky], cyb = (T)D.cy[y2];
     for (int iz = threadIdx.x; iz <= d.nz; iz += 32) {
-        const long long i = o + iz;
-        s1[i] = cy * r[oy + iz] - gq[i];
-        s2[i] = gp[i] - cx * r[ox + iz];
-        s3[i] = cx * q[ox + iz] - cy * p[oy + iz];
+        const T r00 = r[o00 + iz], r10 = r[o10 + iz], r01 = r[o01 + iz], r11 = r[o11 + iz];
+        const T q00 = q[o00 + iz], q10 = q[o10 + iz], q01 = q[o01 + iz], q11 = q[o11 + iz];
+        const T p00 = p[o00 + iz], p10 = p[o10 + iz], p01 = p[o01 + iz], p11 = p[o11 + iz];
+        // member at offset o with its own cx, cy; rx, qx at its x partner,
+        // ry, py at its y partner
+        auto put = [&](long long o, T cx, T cy, T rx, T ry, T qx, T py) {
+            const long long i = o + iz;
+            s1[i] = cy * ry - gq[i];
+            s2[i] = gp[i] - cx * rx;
+            s3[i] = cx * qx - cy * py;
+        };
+        put(o00, cxa, cya, r10, r01, q10, p01);
+        if (dx) put(o10, cxb, cya, r00, r11, q00, p11);
+        if (dy) put(o01, cxa, cyb, r11, r00, q11, p00);
+        if (dx && dy) put(o11, cxb, cyb, r01, r10, q01, p10);
     }
 }
 template <typename T>
 void op_svorts(const Dims &d, cudaStream_t st, const Deriv &D, const T *r, const T *q, const T *p,
                const T *gq, const T *gp, T *s1, T *s2, T *s3)
 {
-    k_svorts<T><<<col_grid(d), COL_BLOCK, 0, st>>>(d, D, r, q, p, gq, gp, s1, s2, s3);
+    k_svorts_orbit<T><<<orbit_grid(d), COL_BLOCK, 0, st>>>(d, D, r, q, p, gq, gp, s1, s2, s3);
 }
 
 // spectral velocity gradients for the strain (advance.f90:193-217):
