@@ -107,57 +107,58 @@ void op_v2v_wsrc(const Dims &d, cudaStream_t st, const Deriv &D, const S *A, con
 //   a = k2l2i (D_x e + D_y f),  b = k2l2i (D_y e - D_x f),
 // D_x f at (kx, ky) reading f at (nx - kx, ky) and D_y at (kx, ny - ky).  The
 // columns (kx, ky), (nx-kx, ky), (kx, ny-ky), (nx-kx, ny-ky) read only one
-// another, so one warp takes the whole orbit: e and f are read once instead
+// another, so one block takes the whole orbit: e and f are read once instead
 // of twice.  Same expression per output as the per-column form.  MEAN: the
 // (0,0) column gets ubar, vbar; otherwise it is left as it is.
 template <typename T, typename S, bool MEAN>
-__global__ void k_v2v_orbit(Dims d, Deriv D, const double *__restrict__ k2l2i, const T *__restrict__ e,
-                            const T *__restrict__ f, const double *__restrict__ ubar,
-                            const double *__restrict__ vbar, S *__restrict__ a, S *__restrict__ b)
+__global__ void __launch_bounds__(128) k_v2v_orbit(Dims d, Deriv D, const double *__restrict__ k2l2i,
+                                                   const T *__restrict__ e, const T *__restrict__ f,
+                                                   const double *__restrict__ ubar, const double *__restrict__ vbar,
+                                                   S *__restrict__ a, S *__restrict__ b)
 {
+    // one 128-thread block per orbit, warp w on member (x partner if w & 1,
+    // y partner if w & 2); the members' e and f meet in shared memory (two
+    // buffers, alternating), next levels' loads issued before the barrier
+    __shared__ S sh_e[2][4][32], sh_f[2][4][32];
     const int hy = d.ny / 2 + 1;
-    const long long orb = (long long)blockIdx.x * COLS_PER_BLOCK + threadIdx.y;
-    if (orb >= (long long)(d.nx / 2 + 1) * hy) return;
+    const long long orb = blockIdx.x;
     const int kx = (int)(orb / hy), ky = (int)(orb - (long long)kx * hy);
     const int x2 = xsrc(kx, d.nx), y2 = xsrc(ky, d.ny);
-    const long long o00 = ((long long)ky + (long long)d.ny * kx) * d.P, o10 = ((long long)ky + (long long)d.ny * x2) * d.P;
-    const long long o01 = ((long long)y2 + (long long)d.ny * kx) * d.P, o11 = ((long long)y2 + (long long)d.ny * x2) * d.P;
-    if (o00 == 0) {
-        if (MEAN)
-            for (int iz = threadIdx.x; iz <= d.nz; iz += 32) {
+    const bool dx = x2 != kx, dy = y2 != ky;
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const bool active = (!(w & 1) || dx) && (!(w & 2) || dy);
+    const int mx = (w & 1) ? x2 : kx, my = (w & 2) ? y2 : ky;
+    const int xw = dx ? (w ^ 1) : w, yw = dy ? (w ^ 2) : w;
+    const long long col = (long long)my + (long long)d.ny * mx, o = col * d.P;
+    if (col == 0) {  // the (0,0) column: the mean flow, or left as it is
+        if (MEAN && active)
+            for (int iz = lane; iz <= d.nz; iz += 32) {
                 a[iz] = (S)ubar[iz];
                 b[iz] = (S)vbar[iz];
             }
-        return;
+        return;  // the (0,0) orbit has no other member
     }
-    const bool dx = x2 != kx, dy = y2 != ky;
-    const S cxa = (S)D.cx[kx], cxb = (S)D.cx[x2], cya = (S)D.cy[ky], cyb = (S)D.cy[y2];
-    const S k00 = (S)k2l2i[o00 / d.P], k10 = (S)k2l2i[o10 / d.P], k01 = (S)k2l2i[o01 / d.P],
-            k11 = (S)k2l2i[o11 / d.P];
-    for (int iz = threadIdx.x; iz <= d.nz; iz += 32) {
-        const S e00 = (S)e[o00 + iz], e10 = (S)e[o10 + iz], e01 = (S)e[o01 + iz], e11 = (S)e[o11 + iz];
-        const S f00 = (S)f[o00 + iz], f10 = (S)f[o10 + iz], f01 = (S)f[o01 + iz], f11 = (S)f[o11 + iz];
-        a[o00 + iz] = k00 * (cxa * e10 + cya * f01);
-        b[o00 + iz] = k00 * (cya * e01 - cxa * f10);
-        if (dx) {
-            a[o10 + iz] = k10 * (cxb * e00 + cya * f11);
-            b[o10 + iz] = k10 * (cya * e11 - cxb * f00);
+    const S cx = (S)D.cx[mx], cy = (S)D.cy[my], kk = (S)k2l2i[col];
+    auto ld = [&](const T *g, int iz) { return (active && iz <= d.nz) ? (S)g[o + iz] : (S)0; };
+    S ev = ld(e, lane), fv = ld(f, lane);
+    int buf = 0;
+    for (int z0 = 0; z0 <= d.nz; z0 += 32, buf ^= 1) {
+        const int iz = z0 + lane;
+        sh_e[buf][w][lane] = ev;
+        sh_f[buf][w][lane] = fv;
+        if (z0 + 32 <= d.nz) {
+            ev = ld(e, iz + 32);
+            fv = ld(f, iz + 32);
         }
-        if (dy) {
-            a[o01 + iz] = k01 * (cxa * e11 + cyb * f00);
-            b[o01 + iz] = k01 * (cyb * e00 - cxa * f11);
-        }
-        if (dx && dy) {
-            a[o11 + iz] = k11 * (cxb * e01 + cyb * f10);
-            b[o11 + iz] = k11 * (cyb * e10 - cxb * f01);
+        __syncthreads();
+        if (active && iz <= d.nz) {
+            a[o + iz] = kk * (cx * sh_e[buf][xw][lane] + cy * sh_f[buf][yw][lane]);
+            b[o + iz] = kk * (cy * sh_e[buf][yw][lane] - cx * sh_f[buf][xw][lane]);
         }
     }
 }
-static inline dim3 orbit_grid(const Dims &d)
-{
-    const long long norb = (long long)(d.nx / 2 + 1) * (d.ny / 2 + 1);
-    return dim3((unsigned)((norb + COLS_PER_BLOCK - 1) / COLS_PER_BLOCK));
-}
+// one block per partner orbit
+static inline unsigned orbit_blocks(const Dims &d) { return (unsigned)((long long)(d.nx / 2 + 1) * (d.ny / 2 + 1)); }
 
 // A = k2l2i (D_x es + D_y ds), B = k2l2i (D_y es - D_x ds); the (0,0) column
 // keeps its mean vorticity (inversion.f90:50-76)
@@ -165,7 +166,7 @@ template <typename T, typename S>
 void op_v2v_project(const Dims &d, cudaStream_t st, const Deriv &D, const double *k2l2i, const T *es,
                     const T *ds, S *A, S *B)
 {
-    k_v2v_orbit<T, S, false><<<orbit_grid(d), COL_BLOCK, 0, st>>>(d, D, k2l2i, es, ds, nullptr, nullptr, A, B);
+    k_v2v_orbit<T, S, false><<<orbit_blocks(d), 128, 0, st>>>(d, D, k2l2i, es, ds, nullptr, nullptr, A, B);
 }
 
 // boundary contributions and Green-function inversion for w
@@ -269,7 +270,7 @@ template <typename T>
 void op_v2v_uv(const Dims &d, cudaStream_t st, const Deriv &D, const double *k2l2i, const T *es, const T *cs,
                const double *ubar, const double *vbar, T *u, T *v)
 {
-    k_v2v_orbit<T, T, true><<<orbit_grid(d), COL_BLOCK, 0, st>>>(d, D, k2l2i, es, cs, ubar, vbar, u, v);
+    k_v2v_orbit<T, T, true><<<orbit_blocks(d), 128, 0, st>>>(d, D, k2l2i, es, cs, ubar, vbar, u, v);
 }
 
 // ------------------------------------------------------------------- source
@@ -383,90 +384,115 @@ template void op_products_dz<float>(const Dims &, cudaStream_t, double, const fl
                                     float *, float *, float *, float *);
 
 // svorts = (D_y r - dq/dz, dp/dz - D_x r, D_x q - D_y p) (inversion.f90:341-367)
-// in orbit form (as k_v2v_orbit): one warp per partner orbit, so r, q and p
-// are read once each instead of once per partner that needs them; the same
-// expression per output as the per-column form.
+// in orbit form: one 128-thread block per partner orbit {(kx,ky), (nx-kx,ky),
+// (kx,ny-ky), (nx-kx,ny-ky)}, warp w on member (x partner if w & 1, y
+// partner if w & 2), 32 levels at a time.  The members' r, q, p meet in
+// shared memory (two buffers, alternating), so every product column is read
+// once from HBM; the next 32 levels' loads are issued before the current
+// levels' barrier.  The same expression per output as the per-column form.
 template <typename T>
-__global__ void k_svorts_orbit(Dims d, Deriv D, const T *__restrict__ r, const T *__restrict__ q,
-                               const T *__restrict__ p, const T *__restrict__ gq, const T *__restrict__ gp,
-                               T *__restrict__ s1, T *__restrict__ s2, T *__restrict__ s3)
+__global__ void __launch_bounds__(128) k_svorts_orbit(Dims d, Deriv D, const T *__restrict__ r,
+                                                      const T *__restrict__ q, const T *__restrict__ p,
+                                                      const T *__restrict__ gq, const T *__restrict__ gp,
+                                                      T *__restrict__ s1, T *__restrict__ s2, T *__restrict__ s3)
 {
+    __shared__ T sh_r[2][4][32], sh_q[2][4][32], sh_p[2][4][32];
     const int hy = d.ny / 2 + 1;
-    const long long orb = (long long)blockIdx.x * COLS_PER_BLOCK + threadIdx.y;
-    if (orb >= (long long)(d.nx / 2 + 1) * hy) return;
+    const long long orb = blockIdx.x;
     const int kx = (int)(orb / hy), ky = (int)(orb - (long long)kx * hy);
     const int x2 = xsrc(kx, d.nx), y2 = xsrc(ky, d.ny);
-    const long long o00 = ((long long)ky + (long long)d.ny * kx) * d.P, o10 = ((long long)ky + (long long)d.ny * x2) * d.P;
-    const long long o01 = ((long long)y2 + (long long)d.ny * kx) * d.P, o11 = ((long long)y2 + (long long)d.ny * x2) * d.P;
     const bool dx = x2 != kx, dy = y2 != ky;
-    const T cxa = (T)D.cx[kx], cxb = (T)D.cx[x2], cya = (T)D.cy[ky], cyb = (T)D.cy[y2];
-    for (int iz = threadIdx.x; iz <= d.nz; iz += 32) {
-        const T r00 = r[o00 + iz], r10 = r[o10 + iz], r01 = r[o01 + iz], r11 = r[o11 + iz];
-        const T q00 = q[o00 + iz], q10 = q[o10 + iz], q01 = q[o01 + iz], q11 = q[o11 + iz];
-        const T p00 = p[o00 + iz], p10 = p[o10 + iz], p01 = p[o01 + iz], p11 = p[o11 + iz];
-        // member at offset o with its own cx, cy; rx, qx at its x partner,
-        // ry, py at its y partner
-        auto put = [&](long long o, T cx, T cy, T rx, T ry, T qx, T py) {
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const bool active = (!(w & 1) || dx) && (!(w & 2) || dy);
+    const int mx = (w & 1) ? x2 : kx, my = (w & 2) ? y2 : ky;
+    const int xw = dx ? (w ^ 1) : w, yw = dy ? (w ^ 2) : w;  // partner members
+    const long long o = ((long long)my + (long long)d.ny * mx) * d.P;
+    const T cx = (T)D.cx[mx], cy = (T)D.cy[my];
+    auto ld = [&](const T *f, int iz) { return (active && iz <= d.nz) ? f[o + iz] : (T)0; };
+    T rv = ld(r, lane), qv = ld(q, lane), pv = ld(p, lane), gqv = ld(gq, lane), gpv = ld(gp, lane);
+    int buf = 0;
+    for (int z0 = 0; z0 <= d.nz; z0 += 32, buf ^= 1) {
+        const int iz = z0 + lane;
+        sh_r[buf][w][lane] = rv;
+        sh_q[buf][w][lane] = qv;
+        sh_p[buf][w][lane] = pv;
+        const T gqc = gqv, gpc = gpv;
+        if (z0 + 32 <= d.nz) {
+            rv = ld(r, iz + 32);
+            qv = ld(q, iz + 32);
+            pv = ld(p, iz + 32);
+            gqv = ld(gq, iz + 32);
+            gpv = ld(gp, iz + 32);
+        }
+        __syncthreads();
+        if (active && iz <= d.nz) {
             const long long i = o + iz;
-            s1[i] = cy * ry - gq[i];
-            s2[i] = gp[i] - cx * rx;
-            s3[i] = cx * qx - cy * py;
-        };
-        put(o00, cxa, cya, r10, r01, q10, p01);
-        if (dx) put(o10, cxb, cya, r00, r11, q00, p11);
-        if (dy) put(o01, cxa, cyb, r11, r00, q11, p00);
-        if (dx && dy) put(o11, cxb, cyb, r01, r10, q01, p10);
+            s1[i] = cy * sh_r[buf][yw][lane] - gqc;
+            s2[i] = gpc - cx * sh_r[buf][xw][lane];
+            s3[i] = cx * sh_q[buf][xw][lane] - cy * sh_p[buf][yw][lane];
+        }
     }
 }
 template <typename T>
 void op_svorts(const Dims &d, cudaStream_t st, const Deriv &D, const T *r, const T *q, const T *p,
                const T *gq, const T *gp, T *s1, T *s2, T *s3)
 {
-    k_svorts_orbit<T><<<orbit_grid(d), COL_BLOCK, 0, st>>>(d, D, r, q, p, gq, gp, s1, s2, s3);
+    const unsigned norb = (unsigned)((long long)(d.nx / 2 + 1) * (d.ny / 2 + 1));
+    k_svorts_orbit<T><<<norb, 128, 0, st>>>(d, D, r, q, p, gq, gp, s1, s2, s3);
 }
 
 // spectral velocity gradients for the strain (advance.f90:193-217):
 // du/dx, du/dy, dw/dx, dv/dy, dw/dy
-// Orbit form (as k_v2v_orbit): one warp per partner orbit, each velocity
-// column read once; same products as k_strain_fields.
+// Orbit form (as k_v2v_orbit): each velocity column read once.
 template <typename T>
-__global__ void k_strain_orbit(Dims d, Deriv D, const T *__restrict__ svel, T *__restrict__ g5)
+__global__ void __launch_bounds__(128) k_strain_orbit(Dims d, Deriv D, const T *__restrict__ svel,
+                                                      T *__restrict__ g5)
 {
-    const int hy = d.ny / 2 + 1;
-    const long long orb = (long long)blockIdx.x * COLS_PER_BLOCK + threadIdx.y;
-    if (orb >= (long long)(d.nx / 2 + 1) * hy) return;
+    // one 128-thread block per orbit as k_v2v_orbit: the members' u, v, w
+    // meet in shared memory
+    __shared__ T sh_u[2][4][32], sh_v[2][4][32], sh_w[2][4][32];
     const long long N = d.nfield;
+    const int hy = d.ny / 2 + 1;
+    const long long orb = blockIdx.x;
     const int kx = (int)(orb / hy), ky = (int)(orb - (long long)kx * hy);
     const int x2 = xsrc(kx, d.nx), y2 = xsrc(ky, d.ny);
-    const long long o00 = ((long long)ky + (long long)d.ny * kx) * d.P, o10 = ((long long)ky + (long long)d.ny * x2) * d.P;
-    const long long o01 = ((long long)y2 + (long long)d.ny * kx) * d.P, o11 = ((long long)y2 + (long long)d.ny * x2) * d.P;
     const bool dx = x2 != kx, dy = y2 != ky;
-    const T cxa = (T)D.cx[kx], cxb = (T)D.cx[x2], cya = (T)D.cy[ky], cyb = (T)D.cy[y2];
+    const int wp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const bool active = (!(wp & 1) || dx) && (!(wp & 2) || dy);
+    const int mx = (wp & 1) ? x2 : kx, my = (wp & 2) ? y2 : ky;
+    const int xw = dx ? (wp ^ 1) : wp, yw = dy ? (wp ^ 2) : wp;
+    const long long o = ((long long)my + (long long)d.ny * mx) * d.P;
+    const T cx = (T)D.cx[mx], cy = (T)D.cy[my];
     const T *u = svel, *v = svel + N, *w = svel + 2 * N;
-    for (int iz = threadIdx.x; iz <= d.nz; iz += 32) {
-        const T u00 = u[o00 + iz], u10 = u[o10 + iz], u01 = u[o01 + iz], u11 = u[o11 + iz];
-        const T v00 = v[o00 + iz], v10 = v[o10 + iz], v01 = v[o01 + iz], v11 = v[o11 + iz];
-        const T w00 = w[o00 + iz], w10 = w[o10 + iz], w01 = w[o01 + iz], w11 = w[o11 + iz];
-        // member (a, b): x partner / y partner reads as in k_strain_fields
-        auto put = [&](long long o, T cx, T cy, T ux, T uy, T vy, T wx, T wy) {
-            g5[o + iz] = cx * ux;
-            g5[N + o + iz] = cy * uy;
-            g5[2 * N + o + iz] = cx * wx;
-            g5[3 * N + o + iz] = cy * vy;
-            g5[4 * N + o + iz] = cy * wy;
-        };
-        put(o00, cxa, cya, u10, u01, v01, w10, w01);
-        if (dx) put(o10, cxb, cya, u00, u11, v11, w00, w11);
-        if (dy) put(o01, cxa, cyb, u11, u00, v00, w11, w00);
-        if (dx && dy) put(o11, cxb, cyb, u01, u10, v10, w01, w10);
+    auto ld = [&](const T *g, int iz) { return (active && iz <= d.nz) ? g[o + iz] : (T)0; };
+    T uv = ld(u, lane), vv = ld(v, lane), wv = ld(w, lane);
+    int buf = 0;
+    for (int z0 = 0; z0 <= d.nz; z0 += 32, buf ^= 1) {
+        const int iz = z0 + lane;
+        sh_u[buf][wp][lane] = uv;
+        sh_v[buf][wp][lane] = vv;
+        sh_w[buf][wp][lane] = wv;
+        if (z0 + 32 <= d.nz) {
+            uv = ld(u, iz + 32);
+            vv = ld(v, iz + 32);
+            wv = ld(w, iz + 32);
+        }
+        __syncthreads();
+        if (active && iz <= d.nz) {
+            const long long i = o + iz;
+            // du/dx, du/dy, dw/dx, dv/dy, dw/dy (advance.f90:193-217)
+            g5[i] = cx * sh_u[buf][xw][lane];
+            g5[N + i] = cy * sh_u[buf][yw][lane];
+            g5[2 * N + i] = cx * sh_w[buf][xw][lane];
+            g5[3 * N + i] = cy * sh_v[buf][yw][lane];
+            g5[4 * N + i] = cy * sh_w[buf][yw][lane];
+        }
     }
 }
 template <typename T>
 void op_strain_fields(const Dims &d, cudaStream_t st, const Deriv &D, const T *svel, T *g5)
 {
-    const long long norb = (long long)(d.nx / 2 + 1) * (d.ny / 2 + 1);
-    k_strain_orbit<T><<<(unsigned)((norb + COLS_PER_BLOCK - 1) / COLS_PER_BLOCK), COL_BLOCK, 0, st>>>(d, D, svel,
-                                                                                                      g5);
+    k_strain_orbit<T><<<orbit_blocks(d), 128, 0, st>>>(d, D, svel, g5);
 }
 
 // Derived fields (fields_derived.f90:67-182, buoyancy disabled).
