@@ -107,6 +107,43 @@ struct Harm {
     }
 };
 
+// d exp(-2 pi i j / 32) for a j known at compile time (the loops that call
+// it are unrolled): the factors 1, -i, -1, i become moves and sign flips,
+// and the eighth turns two adds and two multiplies.  cos(2 pi q / 32) for
+// q = 0..8 as decimal literals.
+__device__ __forceinline__ float2 tw32(float2 d, int j)
+{
+    constexpr float C[9] = {1.0f,
+                            0.98078528040323044913f,
+                            0.92387953251128675613f,
+                            0.83146961230254523708f,
+                            0.70710678118654752440f,
+                            0.55557023301960222474f,
+                            0.38268343236508977173f,
+                            0.19509032201612826785f,
+                            0.0f};
+    j &= 31;
+    if (j == 0) return d;
+    if (j == 8) return make_float2(d.y, -d.x);
+    if (j == 16) return make_float2(-d.x, -d.y);
+    if (j == 24) return make_float2(-d.y, d.x);
+    if ((j & 7) == 4) {
+        const float r = C[4];
+        // (1 - i) / sqrt 2 rotated by the quadrant of j
+        const float2 q = (j == 4) ? make_float2(d.x + d.y, d.y - d.x)
+                       : (j == 12) ? make_float2(d.y - d.x, -d.x - d.y)
+                       : (j == 20) ? make_float2(-d.x - d.y, d.x - d.y)
+                                   : make_float2(d.x - d.y, d.x + d.y);
+        return make_float2(q.x * r, q.y * r);
+    }
+    // w = cos t - i sin t, t = 2 pi j / 32; cos and sin from the octant
+    const int o = j & 7, qd = j >> 3;
+    const float c0 = C[o], s0 = C[8 - o];  // cos, sin of the in-quadrant angle
+    const float c = (qd == 0) ? c0 : (qd == 1) ? -s0 : (qd == 2) ? -c0 : s0;
+    const float s = (qd == 0) ? s0 : (qd == 1) ? c0 : (qd == 2) ? -s0 : -c0;
+    return make_float2(d.x * c + d.y * s, d.y * c - d.x * s);
+}
+
 template <int M> __device__ __forceinline__ void dif(float2 *v)
 {
 #pragma unroll
@@ -117,8 +154,7 @@ template <int M> __device__ __forceinline__ void dif(float2 *v)
             for (int i = 0; i < h; ++i) {
                 const float2 a = v[s0 + i], b = v[s0 + i + h];
                 v[s0 + i] = make_float2(a.x + b.x, a.y + b.y);
-                const float2 d = make_float2(a.x - b.x, a.y - b.y);
-                v[s0 + i + h] = (i == 0) ? d : fm(d, c_w32z[i * (16 / h)]);
+                v[s0 + i + h] = tw32(make_float2(a.x - b.x, a.y - b.y), i * (16 / h));
             }
         }
     }
@@ -176,17 +212,19 @@ __device__ __forceinline__ void warp_fft(float2 *v, float2 *xs, const float2 *__
         for (int r = 1; r < M; ++r) v[r] = fm(v[r], c_w32z[(h * brev<M>(r)) & 31]);
         // S-point DIF across the S lanes of the group
 #pragma unroll
+        // the lower lane of a butterfly keeps v + u, the upper one takes
+        // (u - v) w: one fused multiply-add with a sign, then a multiply by
+        // w or by exactly 1
         for (int hs = S / 2; hs >= 1; hs >>= 1) {
             const bool upper = (h & hs) != 0;
-            const float2 w = c_w32z[((h & (hs - 1)) * (16 / hs)) & 31];
+            const float sg = upper ? -1.f : 1.f;
+            const float2 w = upper ? c_w32z[((h & (hs - 1)) * (16 / hs)) & 31] : make_float2(1.f, 0.f);
 #pragma unroll
             for (int r = 0; r < M; ++r) {
                 float2 u;
                 u.x = __shfl_xor_sync(0xffffffffu, v[r].x, hs);
                 u.y = __shfl_xor_sync(0xffffffffu, v[r].y, hs);
-                const float2 sum = make_float2(v[r].x + u.x, v[r].y + u.y);
-                const float2 dif2 = fm(make_float2(u.x - v[r].x, u.y - v[r].y), w);
-                v[r] = upper ? dif2 : sum;
+                v[r] = fm(make_float2(fmaf(sg, v[r].x, u.x), fmaf(sg, v[r].y, u.y)), w);
             }
         }
     }
@@ -219,36 +257,82 @@ __device__ __forceinline__ float warp_sum(float x)
 // fetched with one shuffle each where needed.
 __device__ __forceinline__ float lane_get(float par, int i) { return __shfl_sync(0xffffffffu, par, i); }
 
+__device__ __forceinline__ void st2(float *col, int k, float e, float o)
+{
+    reinterpret_cast<float2 *>(col)[k] = make_float2(e, o);
+}
+
 // Post-processing of the packed spectra in xs (stafft.f90:458-482 cosine,
-// :531-549 sine): for k = lane + 32 i calls emit(k, eA, oA, eB, oB) with the
-// transform values of both columns at levels 2k and 2k+1 (sine: the value at
-// level 0 is meaningless; cosine: x1 is the direct sum giving level 1's
-// constant).  Running sums are warp scans with a carry.
+// :531-549 sine).  At spectral index k both columns get a direct value (level
+// 2k) and a running sum (level 2k+1) over the other half of the spectrum;
+// split() gives the direct values and the running-sum addends, the running
+// sums are warp scans with a carry.  For every k, fix(k, eA, oA, eB, oB) may
+// change the two levels of both columns (mode-specific terms), then they are
+// stored.  With n >= 128 a lane takes two consecutive k (one scan for both,
+// one 16-byte store per column); sine: the value at level 0 is meaningless,
+// cosine: x1 is the direct sum that gives level 1's constant.
+template <bool COS>
+__device__ __forceinline__ void split(int k, float2 ck, float2 cn, float r2s, float &dA, float &aA, float &dB,
+                                      float &aB)
+{
+    const float ReA = 0.5f * (ck.x + cn.x), ImA = 0.5f * (ck.y - cn.y);
+    const float ReB = 0.5f * (ck.y + cn.y), ImB = -0.5f * (ck.x - cn.x);
+    if (COS) {
+        dA = r2s * ReA;
+        dB = r2s * ReB;
+        aA = (k == 0) ? 0.f : ImA;
+        aB = (k == 0) ? 0.f : ImB;
+    } else {
+        dA = -r2s * ImA;
+        dB = -r2s * ImB;
+        aA = (k == 0) ? 0.5f * ReA : ReA;
+        aB = (k == 0) ? 0.5f * ReB : ReB;
+    }
+}
+
+template <bool COS> __device__ __forceinline__ float odd_level(float run, float x1, float r2s)
+{
+    return COS ? x1 - r2s * run : r2s * run;
+}
+
 template <int M, bool COS, typename F>
-__device__ __forceinline__ void post(const float2 *xs, int lane, float r2s, float x1A, float x1B, F &&emit)
+__device__ __forceinline__ void post(const float2 *xs, int lane, float r2s, float x1A, float x1B, float *colA,
+                                     float *colB, F &&fix)
 {
     constexpr int n = 32 * M, KPL = n / 64;
-    float carryA = 0.f, carryB = 0.f;
+    if constexpr (KPL == 1) {
+        const int k = lane;
+        float dA, aA, dB, aB;
+        split<COS>(k, xs[nsw<M>(k)], xs[nsw<M>((n - k) & (n - 1))], r2s, dA, aA, dB, aB);
+        float eA = dA, oA = odd_level<COS>(warp_incl_scan(aA, lane), x1A, r2s);
+        float eB = dB, oB = odd_level<COS>(warp_incl_scan(aB, lane), x1B, r2s);
+        fix(k, eA, oA, eB, oB);
+        st2(colA, k, eA, oA);
+        st2(colB, k, eB, oB);
+    } else {
+        float carryA = 0.f, carryB = 0.f;
 #pragma unroll
-    for (int i = 0; i < KPL; ++i) {
-        const int k = lane + 32 * i;
-        const float2 ck = xs[nsw<M>(k)], cn = xs[nsw<M>((n - k) & (n - 1))];
-        const float ReA = 0.5f * (ck.x + cn.x), ImA = 0.5f * (ck.y - cn.y);
-        const float ReB = 0.5f * (ck.y + cn.y), ImB = -0.5f * (ck.x - cn.x);
-        float va, vb;
-        if (COS) {
-            va = (k == 0) ? 0.f : ImA;
-            vb = (k == 0) ? 0.f : ImB;
-        } else {
-            va = (k == 0) ? 0.5f * ReA : ReA;
-            vb = (k == 0) ? 0.5f * ReB : ReB;
+        for (int i = 0; i < KPL / 2; ++i) {
+            const int k0 = 2 * lane + 64 * i;
+            // X[k0], X[k0 + 1] share one aligned 16-byte slot pair
+            const float4 c = *reinterpret_cast<const float4 *>(xs + nsw<M>(k0));
+            const float2 m0 = xs[nsw<M>((n - k0) & (n - 1))], m1 = xs[nsw<M>(n - k0 - 1)];
+            float dA0, aA0, dB0, aB0, dA1, aA1, dB1, aB1;
+            split<COS>(k0, make_float2(c.x, c.y), m0, r2s, dA0, aA0, dB0, aB0);
+            split<COS>(k0 + 1, make_float2(c.z, c.w), m1, r2s, dA1, aA1, dB1, aB1);
+            const float ra1 = warp_incl_scan(aA0 + aA1, lane) + carryA;
+            const float rb1 = warp_incl_scan(aB0 + aB1, lane) + carryB;
+            carryA = __shfl_sync(0xffffffffu, ra1, 31);
+            carryB = __shfl_sync(0xffffffffu, rb1, 31);
+            float eA0 = dA0, oA0 = odd_level<COS>(ra1 - aA1, x1A, r2s);
+            float eB0 = dB0, oB0 = odd_level<COS>(rb1 - aB1, x1B, r2s);
+            float eA1 = dA1, oA1 = odd_level<COS>(ra1, x1A, r2s);
+            float eB1 = dB1, oB1 = odd_level<COS>(rb1, x1B, r2s);
+            fix(k0, eA0, oA0, eB0, oB0);
+            fix(k0 + 1, eA1, oA1, eB1, oB1);
+            reinterpret_cast<float4 *>(colA)[lane + 32 * i] = make_float4(eA0, oA0, eA1, oA1);
+            reinterpret_cast<float4 *>(colB)[lane + 32 * i] = make_float4(eB0, oB0, eB1, oB1);
         }
-        const float ia = warp_incl_scan(va, lane) + carryA;
-        const float ib = warp_incl_scan(vb, lane) + carryB;
-        carryA = __shfl_sync(0xffffffffu, ia, 31);
-        carryB = __shfl_sync(0xffffffffu, ib, 31);
-        if (COS) emit(k, r2s * ReA, x1A - r2s * ia, r2s * ReB, x1B - r2s * ib);
-        else emit(k, -r2s * ImA, r2s * ia, -r2s * ImB, r2s * ib);
     }
 }
 
@@ -263,40 +347,143 @@ __device__ __forceinline__ float2 pre_cosine(float xa, float ya, float xb, float
     return make_float2(0.5f * (xa + ya) - sj * (xa - ya), 0.5f * (xb + yb) - sj * (xb - yb));
 }
 
-__device__ __forceinline__ void st2(float *col, int k, float e, float o)
+// ---- staging of a column pair in shared memory
+// The two columns of a pair are adjacent (column B = column A + 1), so the
+// pair is one contiguous run of 2P floats.  One lane of the warp copies the
+// warp's next pair with a bulk copy (cp.async.bulk, completion counted on the
+// warp's mbarrier) as soon as the current pair has been read: the copy runs
+// while the warp does the FFT and the post-processing, and every read of the
+// input comes from shared memory.  Waits are bounded; a wait that runs out
+// sets g_colz_err and the warp stops.
+__device__ unsigned int g_colz_err;
+
+__device__ __forceinline__ uint32_t smem_addr(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void stage_init(uint32_t bar)
 {
-    reinterpret_cast<float2 *>(col)[k] = make_float2(e, o);
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(bar) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
 }
+
+// one lane: copy `bytes` (a multiple of 16, both addresses 16-byte aligned)
+// from global src to shared dst; the warp's earlier reads of dst are ordered
+// before the copy by the __syncwarp the caller issues and the proxy fence
+__device__ __forceinline__ void stage_copy(uint32_t dst, const void *src, uint32_t bytes, uint32_t bar)
+{
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(dst),
+                 "l"(src), "r"(bytes), "r"(bar)
+                 : "memory");
+}
+
+__device__ __forceinline__ bool stage_wait(uint32_t bar, uint32_t parity)
+{
+    for (int i = 0; i < (1 << 21); ++i) {
+        uint32_t ok;
+        asm volatile("{\n.reg .pred p;\nmbarrier.test_wait.parity.shared::cta.b64 p, [%1], %2;\nselp.u32 %0, 1, 0, p;\n}\n"
+                     : "=r"(ok)
+                     : "r"(bar), "r"(parity)
+                     : "memory");
+        if (ok) return true;
+        if (i > 32) __nanosleep(64);
+    }
+    return false;
+}
+
+// Per-warp stager: the warp's pair buffer zin (2P floats) and its mbarrier.
+struct Stager {
+    uint32_t bar, dst, bytes, phase;
+    bool stopped;
+    __device__ void start(int lane, const float *in, long long first, long long npairs, int P)
+    {
+        phase = 0;
+        stopped = false;
+        if (lane == 0) {
+            stage_init(bar);
+            if (first < npairs) stage_copy(dst, in + 2 * first * (long long)P, bytes, bar);
+        }
+        __syncwarp();
+    }
+    // wait for the current pair; false (warp-uniform) when the wait ran out
+    __device__ bool wait(int lane)
+    {
+        const bool ok = __all_sync(0xffffffffu, stage_wait(bar, phase));
+        phase ^= 1u;
+        if (!ok) {
+            if (lane == 0) atomicOr(&g_colz_err, 1u);
+            stopped = true;
+        }
+        return ok;
+    }
+    // the current pair has been read: start the copy of the next one
+    __device__ void next(int lane, const float *in, long long pr_next, long long npairs, int P)
+    {
+        __syncwarp();
+        if (lane == 0 && pr_next < npairs) stage_copy(dst, in + 2 * pr_next * (long long)P, bytes, bar);
+    }
+    // after a stop the copy that ran out may still land: wait once more
+    // (bounded) before the block's shared memory is released
+    __device__ void finish(int lane)
+    {
+        if (stopped && lane == 0) stage_wait(bar, phase ^ 1u);
+    }
+};
+
+// float inputs up to nz = 512 are staged (at nz = 1024 the buffer would
+// halve the resident warps)
+template <int M, typename TIN> constexpr bool staged() { return std::is_same<TIN, float>::value && M <= 16; }
+
+// shared memory of a block of 8 warps: 8 mbarriers, then per warp the FFT
+// buffer (n float2) and, when staged, the pair buffer (2P floats)
+constexpr size_t COLZ_BAR_BYTES = 64;
+template <int M> constexpr size_t xs_bytes() { return 32 * M * sizeof(float2); }
+__host__ __device__ inline size_t warp_bytes(size_t xsb, bool stage, int P) { return xsb + (stage ? 2 * (size_t)P * sizeof(float) : 0); }
 
 }  // namespace
 
-// resident 256-thread blocks per SM: three up to nz = 512 (85 registers, a
-// few spilled), two at nz = 1024
+// resident 256-thread blocks per SM: three up to nz = 512, two at nz = 1024
 template <int M> constexpr int col_blocks_per_sm() { return M <= 16 ? 3 : 2; }
 
 // MODE: COL_DST, COL_DCT, COL_DECOMP, COL_COMBINE (see kernels.h).  Safe in
-// place: a pair's inputs are all read before its outputs are written.
+// place: a pair's inputs are all read before its outputs are written, and a
+// staged copy only reads the warp's own next pair.
 template <int MODE, int M, typename TIN>
-__global__ void __launch_bounds__(256, col_blocks_per_sm<M>()) k_colz(const TIN *__restrict__ in, float *__restrict__ out, int P,
-                                              long long npairs, const double *__restrict__ k2l2, float dz,
-                                              float Lz, const float2 *__restrict__ twn,
-                                              const float *__restrict__ sinz, const float *__restrict__ cosz)
+__global__ void __launch_bounds__(256, col_blocks_per_sm<M>())
+    k_colz(const TIN *__restrict__ in, float *__restrict__ out, int P, long long npairs,
+           const double *__restrict__ k2l2, float dz, float Lz, const float2 *__restrict__ twn,
+           const float *__restrict__ sinz, const float *__restrict__ cosz)
 {
     constexpr int n = 32 * M;  // = nz
+    constexpr bool ST = staged<M, TIN>();
     const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
     extern __shared__ __align__(16) unsigned char smz[];
-    float2 *xs = reinterpret_cast<float2 *>(smz) + (size_t)wib * n;
+    unsigned char *wbase = smz + COLZ_BAR_BYTES + (size_t)wib * warp_bytes(xs_bytes<M>(), ST, P);
+    float2 *xs = reinterpret_cast<float2 *>(wbase);
+    const float *zin = reinterpret_cast<const float *>(wbase + xs_bytes<M>());
     const float r2s = 1.41421356237309505f * rsqrtf((float)n);
     const long long warps = (long long)gridDim.x * (blockDim.x >> 5);
-    for (long long pr = (long long)blockIdx.x * (blockDim.x >> 5) + wib; pr < npairs; pr += warps) {
+    const long long first = (long long)blockIdx.x * (blockDim.x >> 5) + wib;
+    Stager sg;
+    if (ST) {
+        sg.bar = smem_addr(smz + 8 * wib);
+        sg.dst = smem_addr(zin);
+        sg.bytes = 8u * (uint32_t)P;
+        sg.start(lane, reinterpret_cast<const float *>(in), first, npairs, P);
+    }
+    for (long long pr = first; pr < npairs; pr += warps) {
+        if (ST && !sg.wait(lane)) break;
         const long long cA = 2 * pr, cB = cA + 1;
         const long long oA = cA * P, oB = cB * P;
+        // column values at level z: from the pair buffer or from global memory
+        auto xA = [&](int z) { return ST ? zin[z] : ld(in, oA + z); };
+        auto xB = [&](int z) { return ST ? zin[P + z] : ld(in, oB + z); };
         // lanes 0..2 (column A) and 8..10 (column B): f(0), f(nz), kl
         float par = 0.f;
         if (lane < 16 && (lane & 7) < 3) {
-            const long long c = lane < 8 ? cA : cB;
             const int q = lane & 7;
-            par = q == 2 ? sqrtf((float)k2l2[c]) : ld(in, c * P + (q == 0 ? 0 : n));
+            if (q == 2) par = sqrtf((float)k2l2[lane < 8 ? cA : cB]);
+            else par = lane < 8 ? xA(q == 0 ? 0 : n) : xB(q == 0 ? 0 : n);
         }
         // ---- pre-processed sequence wk (both columns), lane l: j = l + 32 m
         float dsumA = 0.f, dsumB = 0.f;  // DCT direct sum for x(1)
@@ -314,10 +501,10 @@ __global__ void __launch_bounds__(256, col_blocks_per_sm<M>()) k_colz(const TIN 
                 const int j = lane + 32 * m;
                 float xa = 0.f, xb = 0.f, ya = 0.f, yb = 0.f;  // x(j), x(n-j)
                 if (j > 0) {
-                    xa = ld(in, oA + j);
-                    xb = ld(in, oB + j);
-                    ya = ld(in, oA + n - j);
-                    yb = ld(in, oB + n - j);
+                    xa = xA(j);
+                    xb = xB(j);
+                    ya = xA(n - j);
+                    yb = xB(n - j);
                 }
                 if (MODE == COL_DECOMP && j > 0) {
                     float pm, pp;
@@ -342,19 +529,17 @@ __global__ void __launch_bounds__(256, col_blocks_per_sm<M>()) k_colz(const TIN 
                     v[m] = (j == 0) ? make_float2(0.f, 0.f) : pre_sine(xa, ya, xb, yb, sj);
                 }
             }
+            if (ST) sg.next(lane, reinterpret_cast<const float *>(in), pr + warps, npairs, P);
             warp_fft<M>(v, xs, twn, lane);
         }
-        // ---- split the packed spectra, store levels 2k, 2k+1 as float2
+        // ---- split the packed spectra, store levels 2k, 2k+1
         float *colA = out + oA, *colB = out + oB;
         const float f0A = lane_get(par, 0), fnA = lane_get(par, 1), f0B = lane_get(par, 8),
                     fnB = lane_get(par, 9);
         if (MODE == COL_DCT) {
             const float x1A = r2s * (0.5f * f0A + warp_sum(dsumA) - 0.5f * fnA);
             const float x1B = r2s * (0.5f * f0B + warp_sum(dsumB) - 0.5f * fnB);
-            post<M, true>(xs, lane, r2s, x1A, x1B, [&](int k, float eA, float oA_, float eB, float oB_) {
-                st2(colA, k, eA, oA_);
-                st2(colB, k, eB, oB_);
-            });
+            post<M, true>(xs, lane, r2s, x1A, x1B, colA, colB, [](int, float &, float &, float &, float &) {});
             if (lane == 0) {
                 const float2 cm = xs[nsw<M>(n / 2)];
                 colA[n] = r2s * cm.x;
@@ -363,17 +548,16 @@ __global__ void __launch_bounds__(256, col_blocks_per_sm<M>()) k_colz(const TIN 
         } else if (MODE == COL_COMBINE) {
             const Harm hA = Harm::make(lane_get(par, 2), dz, Lz, n, cA == 0);
             const Harm hB = Harm::make(lane_get(par, 10), dz, Lz, n, cB == 0);
-            post<M, false>(xs, lane, r2s, 0.f, 0.f, [&](int k, float eA, float oA_, float eB, float oB_) {
-                float pm0, pp0, pm1, pp1;
-                hA.at2(2 * k, n, pm0, pp0, pm1, pp1);
-                eA = (k == 0) ? f0A : eA + f0A * pm0 + fnA * pp0;
-                oA_ += f0A * pm1 + fnA * pp1;
-                hB.at2(2 * k, n, pm0, pp0, pm1, pp1);
-                eB = (k == 0) ? f0B : eB + f0B * pm0 + fnB * pp0;
-                oB_ += f0B * pm1 + fnB * pp1;
-                st2(colA, k, eA, oA_);
-                st2(colB, k, eB, oB_);
-            });
+            post<M, false>(xs, lane, r2s, 0.f, 0.f, colA, colB,
+                           [&](int k, float &eA, float &oA_, float &eB, float &oB_) {
+                               float pm0, pp0, pm1, pp1;
+                               hA.at2(2 * k, n, pm0, pp0, pm1, pp1);
+                               eA = (k == 0) ? f0A : eA + f0A * pm0 + fnA * pp0;
+                               oA_ += f0A * pm1 + fnA * pp1;
+                               hB.at2(2 * k, n, pm0, pp0, pm1, pp1);
+                               eB = (k == 0) ? f0B : eB + f0B * pm0 + fnB * pp0;
+                               oB_ += f0B * pm1 + fnB * pp1;
+                           });
             if (lane == 0) {
                 colA[n] = fnA;
                 colB[n] = fnB;
@@ -381,10 +565,11 @@ __global__ void __launch_bounds__(256, col_blocks_per_sm<M>()) k_colz(const TIN 
         } else {
             // DST keeps the input's level 0 and zeroes level nz; DECOMP
             // keeps both boundary values
-            const float bA = f0A, bB = f0B;
-            post<M, false>(xs, lane, r2s, 0.f, 0.f, [&](int k, float eA, float oA_, float eB, float oB_) {
-                st2(colA, k, (k == 0) ? bA : eA, oA_);
-                st2(colB, k, (k == 0) ? bB : eB, oB_);
+            post<M, false>(xs, lane, r2s, 0.f, 0.f, colA, colB, [&](int k, float &eA, float &, float &eB, float &) {
+                if (k == 0) {
+                    eA = f0A;
+                    eB = f0B;
+                }
             });
             if (lane == 0) {
                 colA[n] = (MODE == COL_DST) ? 0.f : fnA;
@@ -393,6 +578,7 @@ __global__ void __launch_bounds__(256, col_blocks_per_sm<M>()) k_colz(const TIN 
         }
         __syncwarp();
     }
+    if (ST) sg.finish(lane);
 }
 
 namespace {
@@ -474,22 +660,44 @@ __global__ void __launch_bounds__(256, 2) k_colz_w(const float *__restrict__ ds,
                                                    const float *__restrict__ sinz, const float *__restrict__ cosz)
 {
     constexpr int n = 32 * M;
+    constexpr bool ST = staged<M, float>();
     const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
     extern __shared__ __align__(16) unsigned char smz[];
-    float2 *xs = reinterpret_cast<float2 *>(smz) + (size_t)wib * n;
+    unsigned char *wbase = smz + COLZ_BAR_BYTES + (size_t)wib * warp_bytes(xs_bytes<M>(), ST, P);
+    float2 *xs = reinterpret_cast<float2 *>(wbase);
+    const float *zin = reinterpret_cast<const float *>(wbase + xs_bytes<M>());
     const float r2s = 1.41421356237309505f * rsqrtf((float)n);
     const float pk = 3.14159265358979324f / Lz;  // rkz(kz) = pk kz
     const long long warps = (long long)gridDim.x * (blockDim.x >> 5);
-    for (long long pr = (long long)blockIdx.x * (blockDim.x >> 5) + wib; pr < npairs; pr += warps) {
+    const long long first = (long long)blockIdx.x * (blockDim.x >> 5) + wib;
+    Stager sg;
+    if (ST) {
+        sg.bar = smem_addr(smz + 8 * wib);
+        sg.dst = smem_addr(zin);
+        sg.bytes = 8u * (uint32_t)P;
+        sg.start(lane, ds, first, npairs, P);
+    }
+    for (long long pr = first; pr < npairs; pr += warps) {
+        if (ST && !sg.wait(lane)) break;
         const long long cA = 2 * pr, cB = cA + 1;
         const long long oA = cA * P, oB = cB * P;
+        // opaque copies of the offsets keep the compiler from hoisting the
+        // second transform's global loads above the first (register spills)
+        long long qA = oA, qB = oB;
+        asm volatile("" : "+l"(qA), "+l"(qB));
+        auto dA = [&](int z) { return ST ? zin[z] : ds[oA + z]; };
+        auto dB = [&](int z) { return ST ? zin[P + z] : ds[oB + z]; };
+        auto dA2 = [&](int z) { return ST ? zin[z] : ds[qA + z]; };
+        auto dB2 = [&](int z) { return ST ? zin[P + z] : ds[qB + z]; };
         // lanes 0..3 (column A) and 8..11 (column B): k^2+l^2, 1/(k^2+l^2),
         // ds(0), ds(nz)
         float par = 0.f;
         if (lane < 16 && (lane & 7) < 4) {
             const long long c = lane < 8 ? cA : cB;
             const int f = lane & 3;
-            par = f == 0 ? (float)k2l2[c] : f == 1 ? (float)k2l2i[c] : ds[c * P + (f == 2 ? 0 : n)];
+            if (f == 0) par = (float)k2l2[c];
+            else if (f == 1) par = (float)k2l2i[c];
+            else par = lane < 8 ? dA(f == 2 ? 0 : n) : dB(f == 2 ? 0 : n);
         }
         // ---- dst of dsg = green ds
         {
@@ -502,8 +710,8 @@ __global__ void __launch_bounds__(256, 2) k_colz_w(const float *__restrict__ ds,
                 if (j > 0) {
                     const float rj = pk * (float)j, rn = pk * (float)(n - j);
                     const float rj2 = rj * rj, rn2 = rn * rn;
-                    const float xa = __fdividef(-ds[oA + j], k2A + rj2), ya = __fdividef(-ds[oA + n - j], k2A + rn2);
-                    const float xb = __fdividef(-ds[oB + j], k2B + rj2), yb = __fdividef(-ds[oB + n - j], k2B + rn2);
+                    const float xa = __fdividef(-dA(j), k2A + rj2), ya = __fdividef(-dA(n - j), k2A + rn2);
+                    const float xb = __fdividef(-dB(j), k2B + rj2), yb = __fdividef(-dB(n - j), k2B + rn2);
                     v[m] = pre_sine(xa, ya, xb, yb, __ldg(&sinz[j]));
                 }
             }
@@ -516,12 +724,14 @@ __global__ void __launch_bounds__(256, 2) k_colz_w(const float *__restrict__ ds,
             const ThetaCol tB =
                 ThetaCol::make(false, klB, lane_get(par, 9), lane_get(par, 10), lane_get(par, 11), dz, Lz, cB == 0);
             float *wA = w + oA, *wB = w + oB;
-            post<M, false>(xs, lane, r2s, 0.f, 0.f, [&](int k, float eA, float oA_, float eB, float oB_) {
+            post<M, false>(xs, lane, r2s, 0.f, 0.f, wA, wB, [&](int k, float &eA, float &oA_, float &eB, float &oB_) {
                 float b0, b1;
                 tA.at2(2 * k, n, b0, b1);
-                st2(wA, k, (k == 0) ? 0.f : eA + b0, oA_ + b1);
+                eA = (k == 0) ? 0.f : eA + b0;
+                oA_ += b1;
                 tB.at2(2 * k, n, b0, b1);
-                st2(wB, k, (k == 0) ? 0.f : eB + b0, oB_ + b1);
+                eB = (k == 0) ? 0.f : eB + b0;
+                oB_ += b1;
             });
             if (lane == 0) {
                 wA[n] = 0.f;
@@ -533,10 +743,6 @@ __global__ void __launch_bounds__(256, 2) k_colz_w(const float *__restrict__ ds,
         float x1A, x1B;
         {
             const float k2A = lane_get(par, 0), k2B = lane_get(par, 8);
-            // opaque copies of the offsets keep the compiler from hoisting
-            // this phase's loads above the first transform (register spills)
-            long long qA = oA, qB = oB;
-            asm volatile("" : "+l"(qA), "+l"(qB));
             float2 v[M];
             float sA = 0.f, sB = 0.f;
 #pragma unroll
@@ -546,16 +752,17 @@ __global__ void __launch_bounds__(256, 2) k_colz_w(const float *__restrict__ ds,
                 if (j > 0) {
                     const float rj = pk * (float)j, rn = pk * (float)(n - j);
                     const float rj2 = rj * rj, rn2 = rn * rn;
-                    const float xa = __fdividef(-rj * ds[qA + j], k2A + rj2);
-                    const float ya = __fdividef(-rn * ds[qA + n - j], k2A + rn2);
-                    const float xb = __fdividef(-rj * ds[qB + j], k2B + rj2);
-                    const float yb = __fdividef(-rn * ds[qB + n - j], k2B + rn2);
+                    const float xa = __fdividef(-rj * dA2(j), k2A + rj2);
+                    const float ya = __fdividef(-rn * dA2(n - j), k2A + rn2);
+                    const float xb = __fdividef(-rj * dB2(j), k2B + rj2);
+                    const float yb = __fdividef(-rn * dB2(n - j), k2B + rn2);
                     const float cj = __ldg(&cosz[j]);
                     sA += xa * cj;
                     sB += xb * cj;
                     v[m] = pre_cosine(xa, ya, xb, yb, __ldg(&sinz[j]));
                 }
             }
+            if (ST) sg.next(lane, ds, pr + warps, npairs, P);
             x1A = r2s * warp_sum(sA);
             x1B = r2s * warp_sum(sB);
             warp_fft<M>(v, xs, twn, lane);
@@ -567,12 +774,14 @@ __global__ void __launch_bounds__(256, 2) k_colz_w(const float *__restrict__ ds,
             const ThetaCol tB =
                 ThetaCol::make(true, klB, lane_get(par, 9), lane_get(par, 10), lane_get(par, 11), dz, Lz, cB == 0);
             float *eA_ = es + oA, *eB_ = es + oB;
-            post<M, true>(xs, lane, r2s, x1A, x1B, [&](int k, float eA, float oA_, float eB, float oB_) {
+            post<M, true>(xs, lane, r2s, x1A, x1B, eA_, eB_, [&](int k, float &eA, float &oA_, float &eB, float &oB_) {
                 float b0, b1;
                 tA.at2(2 * k, n, b0, b1);
-                st2(eA_, k, eA + b0, oA_ + b1);
+                eA += b0;
+                oA_ += b1;
                 tB.at2(2 * k, n, b0, b1);
-                st2(eB_, k, eB + b0, oB_ + b1);
+                eB += b0;
+                oB_ += b1;
             });
             if (lane == 0) {
                 const float2 cm = xs[nsw<M>(n / 2)];
@@ -585,12 +794,8 @@ __global__ void __launch_bounds__(256, 2) k_colz_w(const float *__restrict__ ds,
         }
         __syncwarp();
     }
+    if (ST) sg.finish(lane);
 }
-
-namespace {
-__device__ __forceinline__ int zpad(int z) { return z + (z >> 4); }
-template <int M> constexpr int zbuf_floats() { return 32 * M + 1 + (32 * M + 1) / 16 + 2; }
-}  // namespace
 
 // ------------------------------------------------------------------------
 // The third tendency component's two decompositions in one kernel (mixed
@@ -598,50 +803,63 @@ template <int M> constexpr int zbuf_floats() { return 32 * M + 1 + (32 * M + 1) 
 //   out = decompose(S3)                 (the mixed-spectral tendency), and
 //   es  = decompose(central_diffz(S3))  (the z part of its solenoidal
 //                                        projection, inversion.f90:41-47),
-// one read of S3 into the warp's z buffers, two warp FFTs, one write each.
+// one read of S3 into the warp's pair buffer, two warp FFTs, one write each.
 // Safe in place (out == f): the pair is read whole before anything is
-// written.
+// written.  Up to nz = 512 the pair arrives by a staged bulk copy (prefetched
+// one pair ahead); at nz = 1024 the warp loads it itself.
 template <int M>
-__global__ void __launch_bounds__(256, 2) k_colz_dec2(const float *__restrict__ f, float *out, float *__restrict__ es,
+__global__ void __launch_bounds__(256, M <= 16 ? 3 : 2) k_colz_dec2(const float *__restrict__ f, float *out, float *__restrict__ es,
                                                       int P, long long npairs, const double *__restrict__ k2l2,
                                                       float dz, float Lz, const float2 *__restrict__ twn,
                                                       const float *__restrict__ sinz)
 {
     constexpr int n = 32 * M;
-    constexpr int ZS = zbuf_floats<M>();
+    constexpr bool ST = staged<M, float>();
     const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
     extern __shared__ __align__(16) unsigned char smz[];
-    float2 *xs = reinterpret_cast<float2 *>(smz + (size_t)wib * (n * sizeof(float2) + 2 * ZS * sizeof(float)));
-    float *zA = reinterpret_cast<float *>(xs + n);
-    float *zB = zA + ZS;
+    unsigned char *wbase = smz + COLZ_BAR_BYTES + (size_t)wib * warp_bytes(xs_bytes<M>(), true, P);
+    float2 *xs = reinterpret_cast<float2 *>(wbase);
+    float *zA = reinterpret_cast<float *>(wbase + xs_bytes<M>());
+    float *zB = zA + P;
     float *gA = reinterpret_cast<float *>(xs), *gB = gA + n;
     const float r2s = 1.41421356237309505f * rsqrtf((float)n);
     const float dzi = 1.0f / dz, hdzi = 0.5f / dz;
     const long long warps = (long long)gridDim.x * (blockDim.x >> 5);
-    for (long long pr = (long long)blockIdx.x * (blockDim.x >> 5) + wib; pr < npairs; pr += warps) {
+    const long long first = (long long)blockIdx.x * (blockDim.x >> 5) + wib;
+    Stager sg;
+    if (ST) {
+        sg.bar = smem_addr(smz + 8 * wib);
+        sg.dst = smem_addr(zA);
+        sg.bytes = 8u * (uint32_t)P;
+        sg.start(lane, f, first, npairs, P);
+    }
+    for (long long pr = first; pr < npairs; pr += warps) {
         const long long cA = 2 * pr, cB = cA + 1;
         const long long oA = cA * P, oB = cB * P;
-        // the pair into the z buffers (levels 0..n)
-        for (int iz = lane; iz <= n; iz += 32) {
-            zA[zpad(iz)] = f[oA + iz];
-            zB[zpad(iz)] = f[oB + iz];
+        if (ST) {
+            if (!sg.wait(lane)) break;
+        } else {
+            for (int iz = lane; iz <= n; iz += 32) {
+                zA[iz] = f[oA + iz];
+                zB[iz] = f[oB + iz];
+            }
+            __syncwarp();
         }
         // lanes 0 / 8: kl of columns A / B
         float par = 0.f;
         if (lane == 0 || lane == 8) par = sqrtf((float)k2l2[lane == 0 ? cA : cB]);
-        __syncwarp();
+        const float f0A = zA[0], fnA = zA[n], f0B = zB[0], fnB = zB[n];
         // ---- decompose S3: subtract the harmonic part, dst
         {
             const Harm hA = Harm::make(lane_get(par, 0), dz, Lz, n, cA == 0);
             const Harm hB = Harm::make(lane_get(par, 8), dz, Lz, n, cB == 0);
-            const float f0A = zA[zpad(0)], fnA = zA[zpad(n)], f0B = zB[zpad(0)], fnB = zB[zpad(n)];
             float2 v[M];
 #pragma unroll
             for (int m = 0; m < M; ++m) {
                 const int j = lane + 32 * m;
                 v[m] = make_float2(0.f, 0.f);
                 if (j > 0) {
-                    float xa = zA[zpad(j)], ya = zA[zpad(n - j)], xb = zB[zpad(j)], yb = zB[zpad(n - j)];
+                    float xa = zA[j], ya = zA[n - j], xb = zB[j], yb = zB[n - j];
                     float pm, pp;
                     hA.at(j, n, pm, pp);
                     xa -= f0A * pm + fnA * pp;
@@ -655,11 +873,12 @@ __global__ void __launch_bounds__(256, 2) k_colz_dec2(const float *__restrict__ 
             warp_fft<M>(v, xs, twn, lane);
         }
         {
-            const float f0A = zA[zpad(0)], fnA = zA[zpad(n)], f0B = zB[zpad(0)], fnB = zB[zpad(n)];
             float *colA = out + oA, *colB = out + oB;
-            post<M, false>(xs, lane, r2s, 0.f, 0.f, [&](int k, float eA, float oA_, float eB, float oB_) {
-                st2(colA, k, (k == 0) ? f0A : eA, oA_);
-                st2(colB, k, (k == 0) ? f0B : eB, oB_);
+            post<M, false>(xs, lane, r2s, 0.f, 0.f, colA, colB, [&](int k, float &eA, float &, float &eB, float &) {
+                if (k == 0) {
+                    eA = f0A;
+                    eB = f0B;
+                }
             });
             if (lane == 0) {
                 colA[n] = fnA;
@@ -672,12 +891,14 @@ __global__ void __launch_bounds__(256, 2) k_colz_dec2(const float *__restrict__ 
         for (int iz = lane; iz < n; iz += 32) {
             const int lo = iz == 0 ? 0 : iz - 1;
             const float sc = iz == 0 ? dzi : hdzi;
-            gA[iz] = (zA[zpad(iz + 1)] - zA[zpad(lo)]) * sc;
-            gB[iz] = (zB[zpad(iz + 1)] - zB[zpad(lo)]) * sc;
+            gA[iz] = (zA[iz + 1] - zA[lo]) * sc;
+            gB[iz] = (zB[iz + 1] - zB[lo]) * sc;
         }
-        const float gnA = dzi * (zA[zpad(n)] - zA[zpad(n - 1)]);
-        const float gnB = dzi * (zB[zpad(n)] - zB[zpad(n - 1)]);
-        __syncwarp();
+        const float gnA = dzi * (fnA - zA[n - 1]);
+        const float gnB = dzi * (fnB - zB[n - 1]);
+        // the pair buffer is free: start the next pair's copy
+        if (ST) sg.next(lane, f, pr + warps, npairs, P);
+        else __syncwarp();
         // ---- decompose the derivative
         const float g0A = gA[0], g0B = gB[0];
         {
@@ -705,9 +926,11 @@ __global__ void __launch_bounds__(256, 2) k_colz_dec2(const float *__restrict__ 
         }
         {
             float *eA_ = es + oA, *eB_ = es + oB;
-            post<M, false>(xs, lane, r2s, 0.f, 0.f, [&](int k, float eA, float oA_, float eB, float oB_) {
-                st2(eA_, k, (k == 0) ? g0A : eA, oA_);
-                st2(eB_, k, (k == 0) ? g0B : eB, oB_);
+            post<M, false>(xs, lane, r2s, 0.f, 0.f, eA_, eB_, [&](int k, float &eA, float &, float &eB, float &) {
+                if (k == 0) {
+                    eA = g0A;
+                    eB = g0B;
+                }
             });
             if (lane == 0) {
                 eA_[n] = gnA;
@@ -716,19 +939,32 @@ __global__ void __launch_bounds__(256, 2) k_colz_dec2(const float *__restrict__ 
         }
         __syncwarp();
     }
+    if (ST) sg.finish(lane);
 }
 
 namespace {
-template <int M> constexpr size_t colz_smem_per_warp() { return 32 * M * sizeof(float2); }
-template <int M> constexpr size_t proj_smem_per_warp()
-{
-    return 32 * M * sizeof(float2) + 2 * zbuf_floats<M>() * sizeof(float);
-}
+template <int M> size_t colz_smem(bool stage, int P) { return COLZ_BAR_BYTES + 8 * warp_bytes(xs_bytes<M>(), stage, P); }
 
-long long colz_blocks(long long npairs)
+// set by a launch whose pointers or pitch break the 16-byte rules (the
+// kernels store 16-byte pairs of levels, the staged copy needs 16-byte
+// runs): the launch is skipped and colz_error() reports it
+bool g_colz_host_err = false;
+
+bool aligned16(const void *p) { return ((uintptr_t)p & 15u) == 0; }
+
+// One block of 8 warps per 8 pairs, at most as many blocks as are resident
+// at once (the warps then loop over pairs, so each warp's prefetch of its
+// next pair overlaps its current one).
+template <typename K> unsigned colz_grid(K kern, size_t smem, long long npairs)
 {
-    long long nb = (npairs + 7) / 8;
-    return nb > 152 * 24 ? 152 * 24 : nb;
+    int dev = 0, sms = 1;
+    cudaGetDevice(&dev);
+    if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || sms < 1) sms = 1;
+    int per_sm = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, 256, smem) != cudaSuccess || per_sm < 1)
+        per_sm = 1;
+    const long long nb = (npairs + 7) / 8, cap = (long long)per_sm * sms;
+    return (unsigned)(nb < cap ? nb : cap);
 }
 
 template <int MODE, int M, typename TIN>
@@ -736,8 +972,9 @@ void launch_colz_m(const TIN *in, float *out, const Dims &d, cudaStream_t st, co
                    const float2 *twn, const float *sinz, const float *cosz)
 {
     const long long npairs = d.ncol / 2;
-    k_colz<MODE, M, TIN><<<(unsigned)colz_blocks(npairs), 256, 8 * colz_smem_per_warp<M>(), st>>>(
-        in, out, d.P, npairs, k2l2, dz, Lz, twn, sinz, cosz);
+    const size_t smem = colz_smem<M>(staged<M, TIN>(), d.P);
+    auto kern = k_colz<MODE, M, TIN>;
+    kern<<<colz_grid(kern, smem, npairs), 256, smem, st>>>(in, out, d.P, npairs, k2l2, dz, Lz, twn, sinz, cosz);
 }
 
 template <int MODE, typename TIN>
@@ -758,8 +995,9 @@ void launch_w_m(const Dims &d, cudaStream_t st, const float *ds, float *w, float
                 const double *k2l2i, float dz, float Lz, const float2 *twn, const float *sinz, const float *cosz)
 {
     const long long npairs = d.ncol / 2;
-    k_colz_w<M><<<(unsigned)colz_blocks(npairs), 256, 8 * colz_smem_per_warp<M>(), st>>>(
-        ds, w, es, d.P, npairs, k2l2, k2l2i, dz, Lz, twn, sinz, cosz);
+    const size_t smem = colz_smem<M>(staged<M, float>(), d.P);
+    k_colz_w<M><<<colz_grid(k_colz_w<M>, smem, npairs), 256, smem, st>>>(ds, w, es, d.P, npairs, k2l2, k2l2i, dz, Lz,
+                                                                         twn, sinz, cosz);
 }
 
 template <int M>
@@ -767,33 +1005,62 @@ void launch_dec2_m(const Dims &d, cudaStream_t st, const float *f, float *out, f
                    float dz, float Lz, const float2 *twn, const float *sinz)
 {
     const long long npairs = d.ncol / 2;
-    k_colz_dec2<M><<<(unsigned)colz_blocks(npairs), 256, 8 * proj_smem_per_warp<M>(), st>>>(
-        f, out, es, d.P, npairs, k2l2, dz, Lz, twn, sinz);
+    const size_t smem = colz_smem<M>(true, d.P);
+    k_colz_dec2<M><<<colz_grid(k_colz_dec2<M>, smem, npairs), 256, smem, st>>>(f, out, es, d.P, npairs, k2l2, dz, Lz,
+                                                                               twn, sinz);
 }
 
-template <typename K> void smem_attr(K kern, size_t bytes)
+// every column kernel may take up to the device's opt-in shared memory per
+// block (the launch asks for what its pitch needs)
+template <typename K> void smem_attr(K kern, int optin)
 {
-    if (bytes > 48 * 1024) cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+    cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
 }
-template <int M> void attr_m()
+template <int M> void attr_m(int optin)
 {
-    smem_attr(k_colz<COL_DST, M, float>, 8 * colz_smem_per_warp<M>());
-    smem_attr(k_colz<COL_DCT, M, float>, 8 * colz_smem_per_warp<M>());
-    smem_attr(k_colz<COL_DECOMP, M, float>, 8 * colz_smem_per_warp<M>());
-    smem_attr(k_colz<COL_COMBINE, M, float>, 8 * colz_smem_per_warp<M>());
-    smem_attr(k_colz<COL_DST, M, double>, 8 * colz_smem_per_warp<M>());
-    smem_attr(k_colz<COL_DCT, M, double>, 8 * colz_smem_per_warp<M>());
-    smem_attr(k_colz<COL_DECOMP, M, double>, 8 * colz_smem_per_warp<M>());
-    smem_attr(k_colz<COL_COMBINE, M, double>, 8 * colz_smem_per_warp<M>());
-    smem_attr(k_colz_w<M>, 8 * colz_smem_per_warp<M>());
-    smem_attr(k_colz_dec2<M>, 8 * proj_smem_per_warp<M>());
+    smem_attr(k_colz<COL_DST, M, float>, optin);
+    smem_attr(k_colz<COL_DCT, M, float>, optin);
+    smem_attr(k_colz<COL_DECOMP, M, float>, optin);
+    smem_attr(k_colz<COL_COMBINE, M, float>, optin);
+    smem_attr(k_colz<COL_DST, M, double>, optin);
+    smem_attr(k_colz<COL_DCT, M, double>, optin);
+    smem_attr(k_colz<COL_DECOMP, M, double>, optin);
+    smem_attr(k_colz<COL_COMBINE, M, double>, optin);
+    smem_attr(k_colz_w<M>, optin);
+    smem_attr(k_colz_dec2<M>, optin);
+}
+
+// the 16-byte rules of the column kernels: pitch a multiple of 4 floats,
+// every column pointer 16-byte aligned
+bool colz_layout_ok(const Dims &d, const void *a, const void *b, const void *c)
+{
+    const bool ok = d.P % 4 == 0 && aligned16(a) && aligned16(b) && (!c || aligned16(c));
+    if (!ok) g_colz_host_err = true;
+    return ok;
 }
 }  // namespace
+
+int colz_error()
+{
+    unsigned int e = 0;
+    if (cudaMemcpyFromSymbol(&e, g_colz_err, sizeof(e)) != cudaSuccess) {
+        cudaGetLastError();
+        e = 0;
+    }
+    if (e) {
+        const unsigned int z = 0;
+        cudaMemcpyToSymbol(g_colz_err, &z, sizeof(z));
+    }
+    const bool h = g_colz_host_err;
+    g_colz_host_err = false;
+    return (e || h) ? 1 : 0;
+}
 
 void columns_w(const Dims &d, cudaStream_t st, const float *ds, float *w, float *es, const double *k2l2,
                const double *k2l2i, float dz, float Lz, const float2 *twn, const float *sinz, const float *cosz,
                Probe *pr)
 {
+    if (!colz_layout_ok(d, ds, w, es)) return;
     if (pr) pr->begin(PROBE_COLUMNS, st);
     switch (d.nz) {
     case 64: launch_w_m<2>(d, st, ds, w, es, k2l2, k2l2i, dz, Lz, twn, sinz, cosz); break;
@@ -808,6 +1075,7 @@ void columns_w(const Dims &d, cudaStream_t st, const float *ds, float *w, float 
 void columns_dec2(const Dims &d, cudaStream_t st, const float *f, float *out, float *es, const double *k2l2,
                   float dz, float Lz, const float2 *twn, const float *sinz, Probe *pr)
 {
+    if (!colz_layout_ok(d, f, out, es)) return;
     if (pr) pr->begin(PROBE_COLUMNS, st);
     switch (d.nz) {
     case 64: launch_dec2_m<2>(d, st, f, out, es, k2l2, dz, Lz, twn, sinz); break;
@@ -835,17 +1103,21 @@ void colz_init()
         w[j] = make_float2((float)c, (float)(-sn));
     }
     cudaMemcpyToSymbol(c_w32z, w, sizeof(w));
-    attr_m<2>();
-    attr_m<4>();
-    attr_m<8>();
-    attr_m<16>();
-    attr_m<32>();
+    int dev = 0, optin = 48 * 1024;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+    attr_m<2>(optin);
+    attr_m<4>(optin);
+    attr_m<8>(optin);
+    attr_m<16>(optin);
+    attr_m<32>(optin);
 }
 
 template <typename TIN>
 void columns_z(const Dims &d, cudaStream_t st, int mode, const TIN *in, float *out, const double *k2l2, float dz,
                float Lz, const float2 *twn, const float *sinz, const float *cosz, Probe *pr)
 {
+    if (!colz_layout_ok(d, in, out, nullptr)) return;
     if (pr) pr->begin(PROBE_COLUMNS, st);
     switch (mode) {
     case COL_DST: launch_colz<COL_DST, TIN>(in, out, d, st, k2l2, dz, Lz, twn, sinz, cosz); break;

@@ -83,6 +83,9 @@ int lines32_error();
 // FP32 half-length warp z transforms (colz.cu), nz = 64..1024
 bool colz_supported(int nz);
 void colz_init();
+// 1 (and cleared) when a column kernel's bounded wait for a staged copy ran
+// out, or a launch was refused for breaking the kernels' 16-byte layout rules
+int colz_error();
 template <typename TIN>
 void columns_z(const Dims &d, cudaStream_t st, int mode, const TIN *in, float *out, const double *k2l2, float dz,
                float Lz, const float2 *twn, const float *sinz, const float *cosz, Probe *pr);

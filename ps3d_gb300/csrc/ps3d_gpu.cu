@@ -737,6 +737,7 @@ template <typename T> int adapt(ps3d_gpu_ctx *c, double t, double *dt_out, ps3d_
     if (rc) return rc;
     if (hflag) return fail(c, PS3D_ERR_DEVICE_LIMIT, "adapt: Jacobi sweep limit reached");
     if (lines32_error()) return fail(c, PS3D_ERR_DEVICE_LIMIT, "line transform: a wait for a tile copy ran out");
+    if (colz_error()) return fail(c, PS3D_ERR_DEVICE_LIMIT, "column transform: a staged copy wait ran out or a layout was refused");
     const double small = 1.0e-12;
     const double vorch = r2[1] / (small + r2[0]);
     const double ggmax = r2[2], usggmax = r2[3], lsggmax = r2[4];
@@ -1261,6 +1262,7 @@ int graph_finish(ps3d_gpu_ctx *c, double *t, ps3d_gpu_diag *diag)
     int rc = sync_check(c, "graph_finish");
     if (rc) return rc;
     if (lines32_error()) return fail(c, PS3D_ERR_DEVICE_LIMIT, "line transform: a wait for a tile copy ran out");
+    if (colz_error()) return fail(c, PS3D_ERR_DEVICE_LIMIT, "column transform: a staged copy wait ran out or a layout was refused");
     c->roll.sma = h.sma;
     c->roll.inew = h.inew;
     c->roll.iold = h.iold;
