@@ -645,15 +645,20 @@ struct ThetaCol {
 }  // namespace
 
 // ------------------------------------------------------------------------
-// Vertical velocity of vor2vel in one kernel (inversion.f90:94-139):
+// Vertical velocity of vor2vel (inversion.f90:94-139):
 //   bs = ds(0) thetam + ds(nz) thetap,  es = ds(0) dthetam + ds(nz) dthetap,
 //   dsg = green ds (interior), as = rkz dsg,
 //   w = [0, dst(dsg) + bs, 0],  dw/dz = es + dct(as),
 // with green(kz) = -1/(k^2 + l^2 + rkz^2) and the boundary-driven parts
-// evaluated in registers: one read of ds (the second transform re-reads it
-// from L2), one write each of w and dw/dz.
-template <int M>
-__global__ void __launch_bounds__(256, 2) k_colz_w(const float *__restrict__ ds, float *__restrict__ w,
+// evaluated in registers.  PART 1 computes w, PART 2 dw/dz, PART 3 both from
+// one read of ds.  Two single-part launches, each reading ds, take less time
+// than one two-part launch (51.4 against 52.0 ms per 512^3 step), and run
+// faster at two blocks per SM with 128 registers than at three with 80 and
+// spills (51.4 against 51.7 ms).
+template <int PART> constexpr int w_blocks_per_sm() { return 2; }
+
+template <int M, int PART>
+__global__ void __launch_bounds__(256, w_blocks_per_sm<PART>()) k_colz_w(const float *__restrict__ ds, float *__restrict__ w,
                                                    float *__restrict__ es, int P, long long npairs,
                                                    const double *__restrict__ k2l2, const double *__restrict__ k2l2i,
                                                    float dz, float Lz, const float2 *__restrict__ twn,
@@ -700,7 +705,7 @@ __global__ void __launch_bounds__(256, 2) k_colz_w(const float *__restrict__ ds,
             else par = lane < 8 ? dA(f == 2 ? 0 : n) : dB(f == 2 ? 0 : n);
         }
         // ---- dst of dsg = green ds
-        {
+        if (PART & 1) {
             const float k2A = lane_get(par, 0), k2B = lane_get(par, 8);
             float2 v[M];
 #pragma unroll
@@ -715,9 +720,10 @@ __global__ void __launch_bounds__(256, 2) k_colz_w(const float *__restrict__ ds,
                     v[m] = pre_sine(xa, ya, xb, yb, __ldg(&sinz[j]));
                 }
             }
+            if (ST && PART == 1) sg.next(lane, ds, pr + warps, npairs, P);
             warp_fft<M>(v, xs, twn, lane);
         }
-        {
+        if (PART & 1) {
             const float klA = sqrtf(lane_get(par, 0)), klB = sqrtf(lane_get(par, 8));
             const ThetaCol tA =
                 ThetaCol::make(false, klA, lane_get(par, 1), lane_get(par, 2), lane_get(par, 3), dz, Lz, cA == 0);
@@ -740,8 +746,8 @@ __global__ void __launch_bounds__(256, 2) k_colz_w(const float *__restrict__ ds,
         }
         __syncwarp();
         // ---- dct of as = rkz green ds (as(0) = as(nz) = 0)
-        float x1A, x1B;
-        {
+        float x1A = 0.f, x1B = 0.f;
+        if (PART & 2) {
             const float k2A = lane_get(par, 0), k2B = lane_get(par, 8);
             float2 v[M];
             float sA = 0.f, sB = 0.f;
@@ -767,7 +773,7 @@ __global__ void __launch_bounds__(256, 2) k_colz_w(const float *__restrict__ ds,
             x1B = r2s * warp_sum(sB);
             warp_fft<M>(v, xs, twn, lane);
         }
-        {
+        if (PART & 2) {
             const float klA = sqrtf(lane_get(par, 0)), klB = sqrtf(lane_get(par, 8));
             const ThetaCol tA =
                 ThetaCol::make(true, klA, lane_get(par, 1), lane_get(par, 2), lane_get(par, 3), dz, Lz, cA == 0);
@@ -996,8 +1002,10 @@ void launch_w_m(const Dims &d, cudaStream_t st, const float *ds, float *w, float
 {
     const long long npairs = d.ncol / 2;
     const size_t smem = colz_smem<M>(staged<M, float>(), d.P);
-    k_colz_w<M><<<colz_grid(k_colz_w<M>, smem, npairs), 256, smem, st>>>(ds, w, es, d.P, npairs, k2l2, k2l2i, dz, Lz,
-                                                                         twn, sinz, cosz);
+    k_colz_w<M, 1><<<colz_grid(k_colz_w<M, 1>, smem, npairs), 256, smem, st>>>(ds, w, es, d.P, npairs, k2l2, k2l2i,
+                                                                               dz, Lz, twn, sinz, cosz);
+    k_colz_w<M, 2><<<colz_grid(k_colz_w<M, 2>, smem, npairs), 256, smem, st>>>(ds, w, es, d.P, npairs, k2l2, k2l2i,
+                                                                               dz, Lz, twn, sinz, cosz);
 }
 
 template <int M>
@@ -1026,7 +1034,8 @@ template <int M> void attr_m(int optin)
     smem_attr(k_colz<COL_DCT, M, double>, optin);
     smem_attr(k_colz<COL_DECOMP, M, double>, optin);
     smem_attr(k_colz<COL_COMBINE, M, double>, optin);
-    smem_attr(k_colz_w<M>, optin);
+    smem_attr(k_colz_w<M, 1>, optin);
+    smem_attr(k_colz_w<M, 2>, optin);
     smem_attr(k_colz_dec2<M>, optin);
 }
 

@@ -425,12 +425,12 @@ template <typename T> int vor2vel_mixed(ps3d_gpu_ctx *c)
     // vertical velocity, mean flow, u, v (inversion.f90:86-213)
     op_v2v_wsrc<T, T>(d, c->st, D, A32, B32, ds);
     if (colz_supported(d.nz)) {
-        // w and dw/dz in one column kernel (theta functions and the Green
-        // function evaluated in registers)
+        // w and dw/dz in two column kernels, one per output (theta
+        // functions and the Green function evaluated in registers)
         columns_w(d, c->st, reinterpret_cast<const float *>(ds), reinterpret_cast<float *>(svel + 2 * N),
                   reinterpret_cast<float *>(es), c->k2l2, c->k2l2i, (float)c->dx[2], (float)c->cfg.extent[2],
                   c->twz32, c->sinz32, c->cosz32, &c->probe);
-        c->launches += 1;
+        c->launches += 2;
     } else {
         op_v2v_wprep<T>(d, c->st, ds, tf<T>(c->thetam), tf<T>(c->thetap), tf<T>(c->dthetam), tf<T>(c->dthetap),
                         tf<T>(c->green), c->rkz, bs, es, dsg, as);
