@@ -381,13 +381,16 @@ def run_gpu(args, rank, world, dist):
     peak, peak_kind = peaks()
     krec = best[0]
     achieved = krec["bytes_per_launch"] / (krec["ms_per_launch"] * 1e-3) / 1e9
-    # DRAM traffic per launch from the committed ncu capture of the same
-    # kernel at 512^3 (profiles/k_lines32_512.md: read + write, mean of four
-    # launches); not measured for other kernels or sizes
-    traffic = 1.04e9 if (best[2] == 4 and n == 512) else None
+    # DRAM traffic per launch of the line kernels: ncu read + write bytes of
+    # the 98 line launches of one 512 x 512 x 128 advance (mean 235.3 MB per
+    # launch; profiles/step_traffic_512x512x128.md), scaled to 512^3 by the
+    # field size ratio P(512) / P(128) = 520 / 136 (traffic grows with the
+    # column pitch at fixed nx, ny); not measured for other kernels or sizes
+    traffic = 235.3e6 * 520.0 / 136.0 if (best[2] == 4 and n == 512) else None
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                 "frac": achieved / peak, "traffic": traffic, "traffic_unit": "bytes per launch",
-                "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum, profiles/k_lines32_512.md"
+                "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of the line launches of one "
+                                  "512x512x128 advance, scaled by 520/136 (profiles/k_lines32_512.md)"
                 if traffic else None,
                 "kernel": krec["kernel"],
                 "algorithmic_bytes_per_launch": krec["bytes_per_launch"],
