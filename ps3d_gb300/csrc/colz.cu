@@ -422,6 +422,22 @@ struct Stager {
         __syncwarp();
         if (lane == 0 && pr_next < npairs) stage_copy(dst, in + 2 * pr_next * (long long)P, bytes, bar);
     }
+    // the same with the source address of the pair given (nullptr: none)
+    __device__ void start_at(int lane, const float *src)
+    {
+        phase = 0;
+        stopped = false;
+        if (lane == 0) {
+            stage_init(bar);
+            if (src) stage_copy(dst, src, bytes, bar);
+        }
+        __syncwarp();
+    }
+    __device__ void next_at(int lane, const float *src)
+    {
+        __syncwarp();
+        if (lane == 0 && src) stage_copy(dst, src, bytes, bar);
+    }
     // after a stop the copy that ran out may still land: wait once more
     // (bounded) before the block's shared memory is released
     __device__ void finish(int lane)
@@ -657,13 +673,24 @@ struct ThetaCol {
 // spills (51.4 against 51.7 ms).
 template <int PART> constexpr int w_blocks_per_sm() { return 2; }
 
-template <int M, int PART>
+//
+// SRC: the kernel also forms ds itself (the w source of inversion.f90:86-92,
+// ds = cy A(kx, -ky) - cx B(-kx, ky) with the state components A, B, the
+// partner columns as in k_v2v_wsrc): the x-partner pair of B (two adjacent
+// columns) comes by the staged copy, A's y partners are read with one batch
+// of loads, and the pair buffer is overwritten with ds.  `ds` is then B.
+// Staged lengths only (nz <= 512).
+template <int M, int PART, bool SRC = false>
 __global__ void __launch_bounds__(256, w_blocks_per_sm<PART>()) k_colz_w(const float *__restrict__ ds, float *__restrict__ w,
                                                    float *__restrict__ es, int P, long long npairs,
                                                    const double *__restrict__ k2l2, const double *__restrict__ k2l2i,
                                                    float dz, float Lz, const float2 *__restrict__ twn,
-                                                   const float *__restrict__ sinz, const float *__restrict__ cosz)
+                                                   const float *__restrict__ sinz, const float *__restrict__ cosz,
+                                                   const float *__restrict__ A = nullptr,
+                                                   const double *__restrict__ cxv = nullptr,
+                                                   const double *__restrict__ cyv = nullptr, int ny = 0)
 {
+    static_assert(!SRC || staged<M, float>(), "the fused w source needs the staged pair buffer");
     constexpr int n = 32 * M;
     constexpr bool ST = staged<M, float>();
     const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
@@ -675,17 +702,51 @@ __global__ void __launch_bounds__(256, w_blocks_per_sm<PART>()) k_colz_w(const f
     const float pk = 3.14159265358979324f / Lz;  // rkz(kz) = pk kz
     const long long warps = (long long)gridDim.x * (blockDim.x >> 5);
     const long long first = (long long)blockIdx.x * (blockDim.x >> 5) + wib;
+    // source of the staged pair (SRC: B's x-partner pair)
+    auto stage_src = [&](long long pr) -> const float * {
+        if (pr >= npairs) return nullptr;
+        if (!SRC) return ds + 2 * pr * (long long)P;
+        const long long cA = 2 * pr, kx = cA / ny, ky = cA - kx * ny, nx = (2 * npairs) / ny;
+        return ds + ((kx == 0 ? 0 : nx - kx) * ny + ky) * (long long)P;
+    };
     Stager sg;
     if (ST) {
         sg.bar = smem_addr(smz + 8 * wib);
         sg.dst = smem_addr(zin);
         sg.bytes = 8u * (uint32_t)P;
-        sg.start(lane, ds, first, npairs, P);
+        sg.start_at(lane, stage_src(first));
     }
     for (long long pr = first; pr < npairs; pr += warps) {
         if (ST && !sg.wait(lane)) break;
         const long long cA = 2 * pr, cB = cA + 1;
         const long long oA = cA * P, oB = cB * P;
+        if (SRC) {
+            // ds = cy A(y partner) - cx B(x partner), in place over the
+            // staged B pair; every load of A issued before the first is used
+            float *zw = const_cast<float *>(zin);
+            const long long kx = cA / ny;
+            const int kyA = (int)(cA - kx * ny), kyB = kyA + 1;
+            const long long aA = (kx * ny + (kyA == 0 ? 0 : ny - kyA)) * (long long)P;
+            const long long aB = (kx * ny + (ny - kyB)) * (long long)P;
+            const float cx = (float)cxv[kx], cyA = (float)cyv[kyA], cyB = (float)cyv[kyB];
+            float h[2][M];
+#pragma unroll
+            for (int b = 0; b < 2; ++b)
+#pragma unroll
+                for (int m = 0; m < M; ++m) h[b][m] = A[(b ? aB : aA) + lane + 32 * m];
+#pragma unroll
+            for (int b = 0; b < 2; ++b) {
+                float *zc = zw + b * P;
+                const float cy = b ? cyB : cyA;
+#pragma unroll
+                for (int m = 0; m < M; ++m) zc[lane + 32 * m] = cy * h[b][m] - cx * zc[lane + 32 * m];
+            }
+            if (lane < 2) {
+                float *zc = zw + lane * P;
+                zc[n] = (lane ? cyB : cyA) * A[(lane ? aB : aA) + n] - cx * zc[n];
+            }
+            __syncwarp();
+        }
         // opaque copies of the offsets keep the compiler from hoisting the
         // second transform's global loads above the first (register spills)
         long long qA = oA, qB = oB;
@@ -720,7 +781,7 @@ __global__ void __launch_bounds__(256, w_blocks_per_sm<PART>()) k_colz_w(const f
                     v[m] = pre_sine(xa, ya, xb, yb, __ldg(&sinz[j]));
                 }
             }
-            if (ST && PART == 1) sg.next(lane, ds, pr + warps, npairs, P);
+            if (ST && PART == 1) sg.next_at(lane, stage_src(pr + warps));
             warp_fft<M>(v, xs, twn, lane);
         }
         if (PART & 1) {
@@ -768,7 +829,7 @@ __global__ void __launch_bounds__(256, w_blocks_per_sm<PART>()) k_colz_w(const f
                     v[m] = pre_cosine(xa, ya, xb, yb, __ldg(&sinz[j]));
                 }
             }
-            if (ST) sg.next(lane, ds, pr + warps, npairs, P);
+            if (ST) sg.next_at(lane, stage_src(pr + warps));
             x1A = r2s * warp_sum(sA);
             x1B = r2s * warp_sum(sB);
             warp_fft<M>(v, xs, twn, lane);
@@ -948,6 +1009,234 @@ __global__ void __launch_bounds__(256, M <= 16 ? 3 : 2) k_colz_dec2(const float 
     if (ST) sg.finish(lane);
 }
 
+// ------------------------------------------------------------------------
+// The tail of the mixed source as three column kernels.  Each forms one
+// tendency component of a column pair from the transformed products of
+// vorticity_tendency (inversion.f90:298-388: spectral x / y derivatives by
+// partner columns, as the orbit kernel k_svorts_orbit forms them) and
+// decomposes it at once, so the undecomposed tendency never goes to HBM:
+//   OUT 1: S1 = cy r(kx, -ky) - gq                 -> decompose(S1)
+//   OUT 2: S2 = gp - cx r(-kx, ky)                 -> decompose(S2)
+//   OUT 3: S3 = cx q(-kx, ky) - cy p(kx, -ky)      -> decompose(S3) and
+//          es = decompose(central_diffz(S3))
+// (-k: the partner column of the Hermitian storage).  One operand (gq, gp:
+// the pair itself; q: the x-partner pair, also two adjacent columns) comes
+// into the warp's pair buffer by the staged bulk copy; the other is read
+// from global memory column by column while the buffer is overwritten with
+// the combined values (for ky = 0 the y partners of a pair are columns 0 and
+// ny - 1).  From there on OUT 1, 2 are the DECOMP column transform and
+// OUT 3 is k_colz_dec2.
+template <int M, int OUT>
+__global__ void __launch_bounds__(256, M <= 16 ? 3 : 2)
+    k_colz_src(const float *__restrict__ fs, const float *__restrict__ fh, float *__restrict__ out,
+               float *__restrict__ es, int P, int ny, long long npairs, const double *__restrict__ k2l2,
+               const double *__restrict__ cxv, const double *__restrict__ cyv, float dz, float Lz,
+               const float2 *__restrict__ twn, const float *__restrict__ sinz)
+{
+    constexpr int n = 32 * M;
+    constexpr bool ST = staged<M, float>();
+    const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+    extern __shared__ __align__(16) unsigned char smz[];
+    unsigned char *wbase = smz + COLZ_BAR_BYTES + (size_t)wib * warp_bytes(xs_bytes<M>(), true, P);
+    float2 *xs = reinterpret_cast<float2 *>(wbase);
+    float *zA = reinterpret_cast<float *>(wbase + xs_bytes<M>());
+    float *zB = zA + P;
+    float *gA = reinterpret_cast<float *>(xs), *gB = gA + n;
+    const float r2s = 1.41421356237309505f * rsqrtf((float)n);
+    const float dzi = 1.0f / dz, hdzi = 0.5f / dz;
+    const long long warps = (long long)gridDim.x * (blockDim.x >> 5);
+    const long long first = (long long)blockIdx.x * (blockDim.x >> 5) + wib;
+    // first column of the pair whose values the staged operand holds
+    auto staged_col = [&](long long pr) -> long long {
+        const long long cA = 2 * pr;
+        if (OUT != 3) return cA;
+        const long long kx = cA / ny;
+        const long long ky = cA - kx * ny;
+        const long long nx = (2 * npairs) / ny;
+        return (kx == 0 ? 0 : nx - kx) * ny + ky;
+    };
+    Stager sg;
+    if (ST) {
+        sg.bar = smem_addr(smz + 8 * wib);
+        sg.dst = smem_addr(zA);
+        sg.bytes = 8u * (uint32_t)P;
+        sg.phase = 0;
+        sg.stopped = false;
+        if (lane == 0) {
+            stage_init(sg.bar);
+            if (first < npairs) stage_copy(sg.dst, fs + staged_col(first) * (long long)P, sg.bytes, sg.bar);
+        }
+        __syncwarp();
+    }
+    for (long long pr = first; pr < npairs; pr += warps) {
+        const long long cA = 2 * pr, cB = cA + 1;
+        const long long oA = cA * P, oB = cB * P;
+        const long long sA = staged_col(pr) * (long long)P;
+        if (ST) {
+            if (!sg.wait(lane)) break;
+        } else {
+            for (int iz = lane; iz <= n; iz += 32) {
+                zA[iz] = fs[sA + iz];
+                zB[iz] = fs[sA + P + iz];
+            }
+            __syncwarp();
+        }
+        // ---- the tendency component of both columns, in place
+        {
+            const long long kx = cA / ny;
+            const int kyA = (int)(cA - kx * ny), kyB = kyA + 1;
+            const long long nx = (2 * npairs) / ny;
+            const long long xp = kx == 0 ? 0 : nx - kx;
+            // columns of the operand read from global memory
+            long long hA, hB;
+            if (OUT == 2) {
+                hA = (xp * ny + kyA) * P;
+                hB = hA + P;
+            } else {
+                hA = (kx * ny + (kyA == 0 ? 0 : ny - kyA)) * P;
+                hB = (kx * ny + (ny - kyB)) * P;
+            }
+            const float cx = (float)cxv[kx];
+            const float cyA = (float)cyv[kyA], cyB = (float)cyv[kyB];
+            auto comb = [&](float sv, float h, float cy) {
+                if (OUT == 1) return fmaf(cy, h, -sv);
+                if (OUT == 2) return fmaf(-cx, h, sv);
+                return fmaf(cx, sv, -(cy * h));
+            };
+            // levels 0..n-1: every load of a batch issued before the first
+            // is used (one memory latency per batch: both columns at once up
+            // to nz = 512, one column at a time at nz = 1024); level n by
+            // lanes 0 (column A) and 1 (column B)
+            constexpr int NB = M <= 16 ? 2 : 1;
+#pragma unroll
+            for (int b0 = 0; b0 < 2; b0 += NB) {
+                float h[NB][M];
+#pragma unroll
+                for (int b = 0; b < NB; ++b)
+#pragma unroll
+                    for (int m = 0; m < M; ++m) h[b][m] = fh[(b0 + b ? hB : hA) + lane + 32 * m];
+#pragma unroll
+                for (int b = 0; b < NB; ++b) {
+                    float *zc = b0 + b ? zB : zA;
+                    const float cy = b0 + b ? cyB : cyA;
+#pragma unroll
+                    for (int m = 0; m < M; ++m) zc[lane + 32 * m] = comb(zc[lane + 32 * m], h[b][m], cy);
+                }
+            }
+            if (lane < 2) {
+                float *zc = lane ? zB : zA;
+                zc[n] = comb(zc[n], fh[(lane ? hB : hA) + n], lane ? cyB : cyA);
+            }
+            __syncwarp();
+        }
+        // lanes 0 / 8: kl of columns A / B
+        float par = 0.f;
+        if (lane == 0 || lane == 8) par = sqrtf((float)k2l2[lane == 0 ? cA : cB]);
+        const float f0A = zA[0], fnA = zA[n], f0B = zB[0], fnB = zB[n];
+        // ---- decompose: subtract the harmonic part, dst
+        {
+            const Harm hA = Harm::make(lane_get(par, 0), dz, Lz, n, cA == 0);
+            const Harm hB = Harm::make(lane_get(par, 8), dz, Lz, n, cB == 0);
+            float2 v[M];
+#pragma unroll
+            for (int m = 0; m < M; ++m) {
+                const int j = lane + 32 * m;
+                v[m] = make_float2(0.f, 0.f);
+                if (j > 0) {
+                    float xa = zA[j], ya = zA[n - j], xb = zB[j], yb = zB[n - j];
+                    float pm, pp;
+                    hA.at(j, n, pm, pp);
+                    xa -= f0A * pm + fnA * pp;
+                    ya -= f0A * pp + fnA * pm;
+                    hB.at(j, n, pm, pp);
+                    xb -= f0B * pm + fnB * pp;
+                    yb -= f0B * pp + fnB * pm;
+                    v[m] = pre_sine(xa, ya, xb, yb, __ldg(&sinz[j]));
+                }
+            }
+            if (OUT != 3) {
+                // the pair buffer is consumed: start the next pair's copy
+                if (ST) {
+                    __syncwarp();
+                    if (lane == 0 && pr + warps < npairs)
+                        stage_copy(sg.dst, fs + staged_col(pr + warps) * (long long)P, sg.bytes, sg.bar);
+                } else {
+                    __syncwarp();
+                }
+            }
+            warp_fft<M>(v, xs, twn, lane);
+        }
+        {
+            float *colA = out + oA, *colB = out + oB;
+            post<M, false>(xs, lane, r2s, 0.f, 0.f, colA, colB, [&](int k, float &eA, float &, float &eB, float &) {
+                if (k == 0) {
+                    eA = f0A;
+                    eB = f0B;
+                }
+            });
+            if (lane == 0) {
+                colA[n] = fnA;
+                colB[n] = fnB;
+            }
+        }
+        __syncwarp();
+        if (OUT != 3) continue;
+        // ---- central_diffz (inversion_utils.f90:653-673): levels 0..n-1
+        // into gA / gB (the FFT buffer), level n in registers
+        for (int iz = lane; iz < n; iz += 32) {
+            const int lo = iz == 0 ? 0 : iz - 1;
+            const float sc = iz == 0 ? dzi : hdzi;
+            gA[iz] = (zA[iz + 1] - zA[lo]) * sc;
+            gB[iz] = (zB[iz + 1] - zB[lo]) * sc;
+        }
+        const float gnA = dzi * (fnA - zA[n - 1]);
+        const float gnB = dzi * (fnB - zB[n - 1]);
+        __syncwarp();
+        if (ST && lane == 0 && pr + warps < npairs)
+            stage_copy(sg.dst, fs + staged_col(pr + warps) * (long long)P, sg.bytes, sg.bar);
+        // ---- decompose the derivative
+        const float g0A = gA[0], g0B = gB[0];
+        {
+            const Harm hA = Harm::make(lane_get(par, 0), dz, Lz, n, cA == 0);
+            const Harm hB = Harm::make(lane_get(par, 8), dz, Lz, n, cB == 0);
+            float2 v[M];
+#pragma unroll
+            for (int m = 0; m < M; ++m) {
+                const int j = lane + 32 * m;
+                v[m] = make_float2(0.f, 0.f);
+                if (j > 0) {
+                    float xa = gA[j], ya = gA[n - j], xb = gB[j], yb = gB[n - j];
+                    float pm, pp;
+                    hA.at(j, n, pm, pp);
+                    xa -= g0A * pm + gnA * pp;
+                    ya -= g0A * pp + gnA * pm;
+                    hB.at(j, n, pm, pp);
+                    xb -= g0B * pm + gnB * pp;
+                    yb -= g0B * pp + gnB * pm;
+                    v[m] = pre_sine(xa, ya, xb, yb, __ldg(&sinz[j]));
+                }
+            }
+            __syncwarp();
+            warp_fft<M>(v, xs, twn, lane);
+        }
+        {
+            float *eA_ = es + oA, *eB_ = es + oB;
+            post<M, false>(xs, lane, r2s, 0.f, 0.f, eA_, eB_, [&](int k, float &eA, float &, float &eB, float &) {
+                if (k == 0) {
+                    eA = g0A;
+                    eB = g0B;
+                }
+            });
+            if (lane == 0) {
+                eA_[n] = gnA;
+                eB_[n] = gnB;
+            }
+        }
+        __syncwarp();
+    }
+    if (ST) sg.finish(lane);
+}
+
 namespace {
 template <int M> size_t colz_smem(bool stage, int P) { return COLZ_BAR_BYTES + 8 * warp_bytes(xs_bytes<M>(), stage, P); }
 
@@ -1009,6 +1298,21 @@ void launch_w_m(const Dims &d, cudaStream_t st, const float *ds, float *w, float
 }
 
 template <int M>
+void launch_w_src_m(const Dims &d, cudaStream_t st, const float *A, const float *B, float *w, float *es,
+                    const double *k2l2, const double *k2l2i, const double *cx, const double *cy, float dz, float Lz,
+                    const float2 *twn, const float *sinz, const float *cosz)
+{
+    if constexpr (staged<M, float>()) {
+        const long long npairs = d.ncol / 2;
+        const size_t smem = colz_smem<M>(true, d.P);
+        k_colz_w<M, 1, true><<<colz_grid(k_colz_w<M, 1, true>, smem, npairs), 256, smem, st>>>(
+            B, w, es, d.P, npairs, k2l2, k2l2i, dz, Lz, twn, sinz, cosz, A, cx, cy, d.ny);
+        k_colz_w<M, 2, true><<<colz_grid(k_colz_w<M, 2, true>, smem, npairs), 256, smem, st>>>(
+            B, w, es, d.P, npairs, k2l2, k2l2i, dz, Lz, twn, sinz, cosz, A, cx, cy, d.ny);
+    }
+}
+
+template <int M>
 void launch_dec2_m(const Dims &d, cudaStream_t st, const float *f, float *out, float *es, const double *k2l2,
                    float dz, float Lz, const float2 *twn, const float *sinz)
 {
@@ -1016,6 +1320,21 @@ void launch_dec2_m(const Dims &d, cudaStream_t st, const float *f, float *out, f
     const size_t smem = colz_smem<M>(true, d.P);
     k_colz_dec2<M><<<colz_grid(k_colz_dec2<M>, smem, npairs), 256, smem, st>>>(f, out, es, d.P, npairs, k2l2, dz, Lz,
                                                                                twn, sinz);
+}
+
+template <int M>
+void launch_src_m(const Dims &d, cudaStream_t st, const float *r, const float *q, const float *p, const float *gq,
+                  const float *gp, float *s1, float *s2, float *s3, float *es, const double *k2l2,
+                  const double *cx, const double *cy, float dz, float Lz, const float2 *twn, const float *sinz)
+{
+    const long long npairs = d.ncol / 2;
+    const size_t smem = colz_smem<M>(true, d.P);
+    k_colz_src<M, 1><<<colz_grid(k_colz_src<M, 1>, smem, npairs), 256, smem, st>>>(
+        gq, r, s1, nullptr, d.P, d.ny, npairs, k2l2, cx, cy, dz, Lz, twn, sinz);
+    k_colz_src<M, 2><<<colz_grid(k_colz_src<M, 2>, smem, npairs), 256, smem, st>>>(
+        gp, r, s2, nullptr, d.P, d.ny, npairs, k2l2, cx, cy, dz, Lz, twn, sinz);
+    k_colz_src<M, 3><<<colz_grid(k_colz_src<M, 3>, smem, npairs), 256, smem, st>>>(
+        q, p, s3, es, d.P, d.ny, npairs, k2l2, cx, cy, dz, Lz, twn, sinz);
 }
 
 // every column kernel may take up to the device's opt-in shared memory per
@@ -1036,7 +1355,14 @@ template <int M> void attr_m(int optin)
     smem_attr(k_colz<COL_COMBINE, M, double>, optin);
     smem_attr(k_colz_w<M, 1>, optin);
     smem_attr(k_colz_w<M, 2>, optin);
+    if constexpr (staged<M, float>()) {
+        smem_attr(k_colz_w<M, 1, true>, optin);
+        smem_attr(k_colz_w<M, 2, true>, optin);
+    }
     smem_attr(k_colz_dec2<M>, optin);
+    smem_attr(k_colz_src<M, 1>, optin);
+    smem_attr(k_colz_src<M, 2>, optin);
+    smem_attr(k_colz_src<M, 3>, optin);
 }
 
 // the 16-byte rules of the column kernels: pitch a multiple of 4 floats,
@@ -1081,6 +1407,24 @@ void columns_w(const Dims &d, cudaStream_t st, const float *ds, float *w, float 
     if (pr) pr->end(PROBE_COLUMNS, st, 3.0 * (double)d.ncol * (double)(d.nz + 1) * sizeof(float));
 }
 
+bool columns_w_src_supported(int nz) { return nz == 64 || nz == 128 || nz == 256 || nz == 512; }
+
+void columns_w_src(const Dims &d, cudaStream_t st, const float *A, const float *B, float *w, float *es,
+                   const double *k2l2, const double *k2l2i, const double *cx, const double *cy, float dz, float Lz,
+                   const float2 *twn, const float *sinz, const float *cosz, Probe *pr)
+{
+    if (!colz_layout_ok(d, A, B, w) || !colz_layout_ok(d, es, es, nullptr)) return;
+    if (pr) pr->begin(PROBE_COLUMNS, st);
+    switch (d.nz) {
+    case 64: launch_w_src_m<2>(d, st, A, B, w, es, k2l2, k2l2i, cx, cy, dz, Lz, twn, sinz, cosz); break;
+    case 128: launch_w_src_m<4>(d, st, A, B, w, es, k2l2, k2l2i, cx, cy, dz, Lz, twn, sinz, cosz); break;
+    case 256: launch_w_src_m<8>(d, st, A, B, w, es, k2l2, k2l2i, cx, cy, dz, Lz, twn, sinz, cosz); break;
+    default: launch_w_src_m<16>(d, st, A, B, w, es, k2l2, k2l2i, cx, cy, dz, Lz, twn, sinz, cosz); break;
+    }
+    // two launches, each reading A and B and writing one field
+    if (pr) pr->end(PROBE_COLUMNS, st, 6.0 * (double)d.ncol * (double)(d.nz + 1) * sizeof(float));
+}
+
 void columns_dec2(const Dims &d, cudaStream_t st, const float *f, float *out, float *es, const double *k2l2,
                   float dz, float Lz, const float2 *twn, const float *sinz, Probe *pr)
 {
@@ -1094,6 +1438,23 @@ void columns_dec2(const Dims &d, cudaStream_t st, const float *f, float *out, fl
     default: launch_dec2_m<32>(d, st, f, out, es, k2l2, dz, Lz, twn, sinz); break;
     }
     if (pr) pr->end(PROBE_COLUMNS, st, 3.0 * (double)d.ncol * (double)(d.nz + 1) * sizeof(float));
+}
+
+void columns_src(const Dims &d, cudaStream_t st, const float *r, const float *q, const float *p, const float *gq,
+                 const float *gp, float *s1, float *s2, float *s3, float *es, const double *k2l2, const double *cx,
+                 const double *cy, float dz, float Lz, const float2 *twn, const float *sinz, Probe *pr)
+{
+    if (!colz_layout_ok(d, r, q, p) || !colz_layout_ok(d, gq, gp, es) || !colz_layout_ok(d, s1, s2, s3)) return;
+    if (pr) pr->begin(PROBE_COLUMNS, st);
+    switch (d.nz) {
+    case 64: launch_src_m<2>(d, st, r, q, p, gq, gp, s1, s2, s3, es, k2l2, cx, cy, dz, Lz, twn, sinz); break;
+    case 128: launch_src_m<4>(d, st, r, q, p, gq, gp, s1, s2, s3, es, k2l2, cx, cy, dz, Lz, twn, sinz); break;
+    case 256: launch_src_m<8>(d, st, r, q, p, gq, gp, s1, s2, s3, es, k2l2, cx, cy, dz, Lz, twn, sinz); break;
+    case 512: launch_src_m<16>(d, st, r, q, p, gq, gp, s1, s2, s3, es, k2l2, cx, cy, dz, Lz, twn, sinz); break;
+    default: launch_src_m<32>(d, st, r, q, p, gq, gp, s1, s2, s3, es, k2l2, cx, cy, dz, Lz, twn, sinz); break;
+    }
+    // six fields read, four written (three launches)
+    if (pr) pr->end(PROBE_COLUMNS, st, 10.0 * (double)d.ncol * (double)(d.nz + 1) * sizeof(float));
 }
 
 bool colz_supported(int nz) { return nz == 64 || nz == 128 || nz == 256 || nz == 512 || nz == 1024; }

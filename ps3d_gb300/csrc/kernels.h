@@ -96,6 +96,17 @@ void columns_z(const Dims &d, cudaStream_t st, int mode, const TIN *in, float *o
 void columns_w(const Dims &d, cudaStream_t st, const float *ds, float *w, float *es, const double *k2l2,
                const double *k2l2i, float dz, float Lz, const float2 *twn, const float *sinz, const float *cosz,
                Probe *pr);
+// w and dw/dz of vor2vel with the w source ds formed inside the column
+// kernels from the state components A, B (nz = 64..512)
+bool columns_w_src_supported(int nz);
+void columns_w_src(const Dims &d, cudaStream_t st, const float *A, const float *B, float *w, float *es,
+                   const double *k2l2, const double *k2l2i, const double *cx, const double *cy, float dz, float Lz,
+                   const float2 *twn, const float *sinz, const float *cosz, Probe *pr);
+// the tail of the mixed source: tendency components from the transformed
+// products, decomposed, and es (three column kernels)
+void columns_src(const Dims &d, cudaStream_t st, const float *r, const float *q, const float *p, const float *gq,
+                 const float *gp, float *s1, float *s2, float *s3, float *es, const double *k2l2, const double *cx,
+                 const double *cy, float dz, float Lz, const float2 *twn, const float *sinz, Probe *pr);
 void columns_dec2(const Dims &d, cudaStream_t st, const float *f, float *out, float *es, const double *k2l2,
                   float dz, float Lz, const float2 *twn, const float *sinz, Probe *pr);
 // FP32 warp-per-column-pair transforms (columns32.cu), nz = 32..512

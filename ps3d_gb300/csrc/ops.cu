@@ -1021,6 +1021,103 @@ void op_stage_orbit(const Dims &d, cudaStream_t st, int sub, const Deriv &D, con
 // another) <-> the device's P-pitched columns, FP64.  The unpack raises
 // *changed when any element differs bitwise from the device state it
 // overwrites.
+//
+// The host side of these copies is page-locked memory read or written over
+// the host link (zero copy), where the link, not HBM, sets the pace.  A
+// block takes FLAT_COLS consecutive columns, one contiguous run of
+// FLAT_COLS * (nz+1) doubles on the host (16-byte aligned when the host
+// array is, FLAT_COLS being even), and moves it as 16-byte pairs, each
+// thread holding FLAT_U pairs in flight; the device side scatters each pair
+// to its one or two columns.  The per-column kernels (8-byte accesses) serve
+// host arrays that are not 16-byte aligned.
+constexpr int FLAT_COLS = 8, FLAT_U = 4, FLAT_T = 256;
+
+// (column, level) of element e of a chunk of columns of n1 levels; e <
+// FLAT_COLS * n1 < 2^24, where e + 0.5 is never within 1/(2 n1) of a
+// multiple of n1, so the single-precision quotient truncates correctly
+__device__ __forceinline__ void chunk_pos(int e, int n1, float inv_n1, int &col, int &iz)
+{
+    col = (int)(((float)e + 0.5f) * inv_n1);
+    iz = e - col * n1;
+}
+
+__global__ void __launch_bounds__(FLAT_T) k_unpack_flat(Dims d, const double2 *__restrict__ src,
+                                                        double *__restrict__ dst, long long ncols, float inv_n1,
+                                                        int *__restrict__ changed)
+{
+    const int n1 = d.nz + 1;
+    const long long c0 = (long long)blockIdx.x * FLAT_COLS;
+    const int ne = (int)min((long long)FLAT_COLS, ncols - c0) * n1;  // elements of this chunk
+    const double2 *s = src + ((c0 * n1) >> 1);                         // c0 even: whole pairs
+    double *t = dst + c0 * d.P;
+    bool diff = false;
+    for (int q0 = threadIdx.x; 2 * q0 < ne; q0 += FLAT_T * FLAT_U) {
+        double2 v[FLAT_U];
+#pragma unroll
+        for (int u = 0; u < FLAT_U; ++u) {
+            const int q = q0 + FLAT_T * u;
+            if (2 * q + 1 < ne) v[u] = s[q];
+            else if (2 * q < ne) v[u].x = reinterpret_cast<const double *>(s)[2 * q];  // odd tail
+        }
+#pragma unroll
+        for (int u = 0; u < FLAT_U; ++u) {
+            const int e = 2 * (q0 + FLAT_T * u);
+            if (e < ne) {
+                int col, iz;
+                chunk_pos(e, n1, inv_n1, col, iz);
+                double *p0 = t + (long long)col * d.P + iz;
+                diff |= __double_as_longlong(v[u].x) != __double_as_longlong(*p0);
+                *p0 = v[u].x;
+                if (e + 1 < ne) {
+                    if (++iz == n1) {
+                        iz = 0;
+                        ++col;
+                    }
+                    double *p1 = t + (long long)col * d.P + iz;
+                    diff |= __double_as_longlong(v[u].y) != __double_as_longlong(*p1);
+                    *p1 = v[u].y;
+                }
+            }
+        }
+    }
+    if (__any_sync(0xffffffffu, diff) && (threadIdx.x & 31) == 0) atomicOr(changed, 1);
+}
+
+__global__ void __launch_bounds__(FLAT_T) k_pack_flat(Dims d, const double *__restrict__ src,
+                                                      double2 *__restrict__ dst, long long ncols, float inv_n1)
+{
+    const int n1 = d.nz + 1;
+    const long long c0 = (long long)blockIdx.x * FLAT_COLS;
+    const int ne = (int)min((long long)FLAT_COLS, ncols - c0) * n1;
+    double2 *t = dst + ((c0 * n1) >> 1);
+    const double *s = src + c0 * d.P;
+    for (int q0 = threadIdx.x; 2 * q0 < ne; q0 += FLAT_T * FLAT_U) {
+        double2 v[FLAT_U];
+#pragma unroll
+        for (int u = 0; u < FLAT_U; ++u) {
+            const int e = 2 * (q0 + FLAT_T * u);
+            if (e < ne) {
+                int col, iz;
+                chunk_pos(e, n1, inv_n1, col, iz);
+                v[u].x = s[(long long)col * d.P + iz];
+                if (e + 1 < ne) {
+                    if (++iz == n1) {
+                        iz = 0;
+                        ++col;
+                    }
+                    v[u].y = s[(long long)col * d.P + iz];
+                }
+            }
+        }
+#pragma unroll
+        for (int u = 0; u < FLAT_U; ++u) {
+            const int e = 2 * (q0 + FLAT_T * u);
+            if (e + 1 < ne) t[e >> 1] = v[u];
+            else if (e < ne) reinterpret_cast<double *>(t)[e] = v[u].x;  // odd tail
+        }
+    }
+}
+
 __global__ void k_unpack_cols(Dims d, const double *__restrict__ src, double *__restrict__ dst, long long ncols,
                               int *__restrict__ changed)
 {
@@ -1046,15 +1143,28 @@ __global__ void k_pack_cols(Dims d, const double *__restrict__ src, double *__re
     double *t = dst + c * n1;
     for (int iz = threadIdx.x; iz < n1; iz += 32) t[iz] = s[iz];
 }
+
+static bool aligned16(const void *p) { return (reinterpret_cast<uintptr_t>(p) & 15u) == 0; }
+
 void op_unpack_cols(const Dims &d, cudaStream_t st, const double *src, double *dst, int ncomp, int *changed)
 {
     const long long ncols = (long long)ncomp * d.ncol;
+    if (aligned16(src)) {
+        k_unpack_flat<<<(unsigned)((ncols + FLAT_COLS - 1) / FLAT_COLS), FLAT_T, 0, st>>>(
+            d, reinterpret_cast<const double2 *>(src), dst, ncols, 1.0f / (float)(d.nz + 1), changed);
+        return;
+    }
     k_unpack_cols<<<(unsigned)((ncols + COLS_PER_BLOCK - 1) / COLS_PER_BLOCK), COL_BLOCK, 0, st>>>(d, src, dst,
                                                                                                    ncols, changed);
 }
 void op_pack_cols(const Dims &d, cudaStream_t st, const double *src, double *dst, int ncomp)
 {
     const long long ncols = (long long)ncomp * d.ncol;
+    if (aligned16(dst)) {
+        k_pack_flat<<<(unsigned)((ncols + FLAT_COLS - 1) / FLAT_COLS), FLAT_T, 0, st>>>(
+            d, src, reinterpret_cast<double2 *>(dst), ncols, 1.0f / (float)(d.nz + 1));
+        return;
+    }
     k_pack_cols<<<(unsigned)((ncols + COLS_PER_BLOCK - 1) / COLS_PER_BLOCK), COL_BLOCK, 0, st>>>(d, src, dst,
                                                                                                  ncols);
 }

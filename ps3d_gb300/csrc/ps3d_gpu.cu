@@ -423,8 +423,17 @@ template <typename T> int vor2vel_mixed(ps3d_gpu_ctx *c)
     col<T>(c, COL_COMBINE, C32, cs);
     xyi<T>(c, cs, vor + 2 * N);
     // vertical velocity, mean flow, u, v (inversion.f90:86-213)
-    op_v2v_wsrc<T, T>(d, c->st, D, A32, B32, ds);
-    if (colz_supported(d.nz)) {
+    if (columns_w_src_supported(d.nz)) {
+        // w and dw/dz in two column kernels that also form the w source ds
+        // from the partner columns of the state (ds stays on chip)
+        columns_w_src(d, c->st, reinterpret_cast<const float *>(A32), reinterpret_cast<const float *>(B32),
+                      reinterpret_cast<float *>(svel + 2 * N), reinterpret_cast<float *>(es), c->k2l2, c->k2l2i,
+                      D.cx, D.cy, (float)c->dx[2], (float)c->cfg.extent[2], c->twz32, c->sinz32, c->cosz32,
+                      &c->probe);
+        c->launches += 2;
+    } else if (colz_supported(d.nz)) {
+        op_v2v_wsrc<T, T>(d, c->st, D, A32, B32, ds);
+        c->launches += 1;
         // w and dw/dz in two column kernels, one per output (theta
         // functions and the Green function evaluated in registers)
         columns_w(d, c->st, reinterpret_cast<const float *>(ds), reinterpret_cast<float *>(svel + 2 * N),
@@ -432,18 +441,19 @@ template <typename T> int vor2vel_mixed(ps3d_gpu_ctx *c)
                   c->twz32, c->sinz32, c->cosz32, &c->probe);
         c->launches += 2;
     } else {
+        op_v2v_wsrc<T, T>(d, c->st, D, A32, B32, ds);
         op_v2v_wprep<T>(d, c->st, ds, tf<T>(c->thetam), tf<T>(c->thetap), tf<T>(c->dthetam), tf<T>(c->dthetap),
                         tf<T>(c->green), c->rkz, bs, es, dsg, as);
         col<T>(c, COL_DCT, as, as);
         col<T>(c, COL_DST, dsg, dsg);
         op_v2v_wfinish<T>(d, c->st, dsg, bs, as, svel + 2 * N, es);
-        c->launches += 2;
+        c->launches += 3;
     }
     // the (0,0) column of the stage state: FP64 (mf64) inside a step
     const double *mA = c->mf_a ? c->mf_a : A, *mB = c->mf_a ? c->mf_a + d.P : B;
     op_v2v_meanflow<double>(d, c->st, mA, mB, c->tables(), c->ubar, c->vbar);
     op_v2v_uv<T>(d, c->st, D, c->k2l2i, es, cs, c->ubar, c->vbar, svel, svel + N);
-    c->launches += 3;
+    c->launches += 2;
     for (int k = 0; k < 3; ++k) xyi<T>(c, svel + k * N, vel + k * N);
     return check(c, "vor2vel");
 }
@@ -664,6 +674,17 @@ template <typename T> int source(ps3d_gpu_ctx *c)
         // column and its x / y partners, so it commutes with D_x, D_y:
         // 3 column transforms instead of 5.
         for (int k = 0; k < 5; ++k) xyf<T>(c, f5[k], f5[k]);
+        if (!c->closure && colz_supported(d.nz)) {
+            // tendency components formed inside the column kernels that
+            // decompose them (the undecomposed tendency stays on chip)
+            const Deriv D = c->D();
+            auto f = [](T *x) { return reinterpret_cast<float *>(x); };
+            columns_src(d, c->st, f(r), f(q), f(p), f(gq), f(gp), f(svorts), f(svorts + N), f(svorts + 2 * N),
+                        reinterpret_cast<float *>(c->es_src), c->k2l2, D.cx, D.cy, (float)c->dx[2],
+                        (float)c->cfg.extent[2], c->twz32, c->sinz32, &c->probe);
+            c->launches += 3;
+            return check(c, "source");
+        }
         op_svorts<T>(d, c->st, c->D(), r, q, p, gq, gp, svorts, svorts + N, svorts + 2 * N);
         c->launches += 1;
         if (c->closure) closure_add<T>(c, svorts);
