@@ -360,13 +360,15 @@ def run_gpu(args, rank, world, dist):
     clocks = clk.summary()
 
     # dominant kernel probe inside real steps (same stream, CUDA events).
-    # k_lines32 (the line FFT, both directions) and the k_colz column-kernel
-    # family are the candidates; y and x lines are also reported apart.
+    # k_lines32 (the line FFT, both directions), the k_colz column-kernel
+    # family and the source's products-plus-forward-y-lines kernel are the
+    # candidates; y and x lines are also reported apart.
     probe_steps = max(1, min(3, args.steps))
     best = None
     probes = []
     kinds = ((4, "k_lines32 (x and y lines)", True), (3, "k_colz (column transforms)", True),
-             (1, "k_lines32 (y lines)", False), (2, "k_lines32 (x lines)", False))
+             (1, "k_lines32 (y lines)", False), (2, "k_lines32 (x lines)", False),
+             (5, "k_lines32_prod (source products + forward y lines)", True))
     for kind, name, candidate in kinds:
         gm.probe(kind)
         t_m, _ = gm.time_advance(t_m, probe_steps)

@@ -290,10 +290,11 @@ int ps3d_gpu_set_tuning(ps3d_gpu_ctx *ctx, const int shape[4]);
 /* Kernel probe: bracket every launch of one kernel class with CUDA events on
  * the context stream.  kind: 0 off, 1 y-line transforms, 2 x-line
  * transforms, 3 column (z) transforms, 4 line transforms of both
- * directions.  probe resets the counters;
+ * directions, 5 the mixed source's products formed in its forward y-line
+ * kernel.  probe resets the counters;
  * probe_result returns the summed device time, the number of bracketed
- * launches and their algorithmic bytes (one read and one write of
- * nx*ny*(nz+1) elements per launch). */
+ * launches and their algorithmic bytes (the fields each launch must read
+ * and write, nx*ny*(nz+1) elements per field: two for a transform pass). */
 int ps3d_gpu_probe(ps3d_gpu_ctx *ctx, int kind);
 int ps3d_gpu_probe_result(ps3d_gpu_ctx *ctx, double *total_ms, long long *launches, double *bytes);
 

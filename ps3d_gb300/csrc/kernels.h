@@ -28,7 +28,7 @@ enum { COL_DST = 0, COL_DCT = 1, COL_DECOMP = 2, COL_COMBINE = 3 };
 // events on the launching stream (used by the benchmark to time the dominant
 // kernel inside a real step).  kind: 0 off, 1 y lines, 2 x lines, 3 columns.
 // PROBE_LINES brackets the line transforms of both directions
-enum { PROBE_OFF = 0, PROBE_YLINES = 1, PROBE_XLINES = 2, PROBE_COLUMNS = 3, PROBE_LINES = 4 };
+enum { PROBE_OFF = 0, PROBE_YLINES = 1, PROBE_XLINES = 2, PROBE_COLUMNS = 3, PROBE_LINES = 4, PROBE_PRODUCTS = 5 };
 struct Probe {
     static constexpr int MAXP = 8192;
     int kind = PROBE_OFF;
@@ -60,6 +60,8 @@ template <typename T>
 void xy_forward(const Dims &d, cudaStream_t st, const T *in, T *out, const typename cplx<T>::type *twx,
                 const typename cplx<T>::type *twy, Probe *pr);
 template <typename T>
+void x_forward(const Dims &d, cudaStream_t st, const T *in, T *out, const typename cplx<T>::type *twx, Probe *pr);
+template <typename T>
 void xy_inverse(const Dims &d, cudaStream_t st, const T *in, T *out, const typename cplx<T>::type *twx,
                 const typename cplx<T>::type *twy, Probe *pr);
 template <typename T>
@@ -79,6 +81,12 @@ void launch_lines32(cudaStream_t st, const float *in, float *out, int n, int P, 
 bool lines32_has_shape(int n, int w);
 int lines32_shapes(int n);  // how many of them n has
 // a bounded wait of the TMA-fed kernel ran out since the last call (cleared)
+// the forward y lines of the five products of vorticity_tendency (r, q,
+// p, dq/dz, dp/dz; out holds them nfield apart) formed from the physical
+// velocity and vorticity inside the line kernel (ny = 64..1024)
+bool lines32_prod_supported(int ny);
+void lines32_prod_y(cudaStream_t st, const float *vel, const float *vor, float *out, const Dims &d, double dzi,
+                    const float2 *twy, Probe *pr);
 int lines32_error();
 // FP32 half-length warp z transforms (colz.cu), nz = 64..1024
 bool colz_supported(int nz);

@@ -281,6 +281,162 @@ void launch32w(cudaStream_t st, const float *in, float *out, int P, int zv, long
 
 
 // ------------------------------------------------------------------------
+// Forward y lines of the five products of vorticity_tendency straight from
+// the velocity and vorticity (inversion.f90:298-340, mixed form): the first
+// radix-8 pass forms, for the block's output o, the value at each of its
+// (y, z) points from the physical u, omega there,
+//   o = 0: r = u eta - v xi,  1: q = w xi - u zeta,  2: p = v zeta - w eta,
+//   3: dq/dz,  4: dp/dz  (central_diffz, inversion_utils.f90:653-673: one-
+//   sided at iz = 0 and iz = nz, centred in between),
+// so the products never go to HBM.  The z neighbours of a thread's four
+// levels come from the adjacent threads of its row by shuffles, the levels
+// just outside the block's 32 from four scalar loads.  The five blocks of a
+// tile are consecutive (blockIdx.x = 5 * tile + o), so they run together
+// and the velocity and vorticity of the tile come from DRAM about once and
+// from L2 after that.  The remaining passes and the Hermitian stores are
+// those of k_lines32; out holds the five outputs nfield apart.
+struct ProdSrc {
+    const float *vel, *vor;  // three components each, nfield apart
+    long long nfield;
+    float dzi, hdzi;
+    int nz;
+};
+
+template <int N, int W>
+__global__ void __launch_bounds__(LinePlan<N, false, W>::T, LinePlan<N, false, W>::MINB)
+    k_lines32_prod(ProdSrc ps, float *__restrict__ out, int P, long long line_stride, long long batch_stride,
+                   const float2 *__restrict__ tw)
+{
+    extern __shared__ __align__(16) float4 smL[];
+    constexpr int T = LinePlan<N, false, W>::T, G = LinePlan<N, false, W>::G;
+    constexpr int R = 8, NB = N / R, NBT = (NB + G - 1) / G;
+    // butterflies j >= NB (N <= 128) leave whole warps idle: a warp's four
+    // row groups are g = 4w..4w+3 and NB is a multiple of 4, so the
+    // shuffles below always run on full warps
+    static_assert(NB % 4 == 0 && PAIRS == 8, "warp-uniform butterfly ranges");
+    const int o = blockIdx.x % 5;
+    const int z0 = (blockIdx.x / 5) * 2 * LANES;
+    const int p = threadIdx.x & (PAIRS - 1), g = threadIdx.x / PAIRS;
+    const int zt = z0 + 4 * p;  // first of the thread's four levels
+    const bool valid = zt < P;  // P is a multiple of 8: all four or none
+    const long long base = (long long)blockIdx.y * batch_stride + z0;
+    const long long Nf = ps.nfield;
+    const float *u = ps.vel, *v = ps.vel + Nf, *w = ps.vel + 2 * Nf;
+    const float *xi = ps.vor, *eta = ps.vor + Nf, *zeta = ps.vor + 2 * Nf;
+    const int nz = ps.nz;
+    // the product of output o (q for 3, p for 4) at one point
+    auto prod = [&](long long i) -> float {
+        if (o == 0) return u[i] * eta[i] - v[i] * xi[i];
+        if (o == 1 || o == 3) return w[i] * xi[i] - u[i] * zeta[i];
+        return v[i] * zeta[i] - w[i] * eta[i];
+    };
+    auto prod4 = [&](long long i) -> float4 {
+        const float4 *U = reinterpret_cast<const float4 *>(u + i), *V = reinterpret_cast<const float4 *>(v + i),
+                     *Wv = reinterpret_cast<const float4 *>(w + i);
+        const float4 *X = reinterpret_cast<const float4 *>(xi + i), *E = reinterpret_cast<const float4 *>(eta + i),
+                     *Z = reinterpret_cast<const float4 *>(zeta + i);
+        float4 a, b, c, d;
+        if (o == 0) {
+            a = *U; b = *E; c = *V; d = *X;
+        } else if (o == 1 || o == 3) {
+            a = *Wv; b = *X; c = *U; d = *Z;
+        } else {
+            a = *V; b = *Z; c = *Wv; d = *E;
+        }
+        return make_float4(a.x * b.x - c.x * d.x, a.y * b.y - c.y * d.y, a.z * b.z - c.z * d.z,
+                           a.w * b.w - c.w * d.w);
+    };
+    // the value the line transform takes at (row, levels zt..zt+3); rows
+    // above the top wall are zero
+    auto load = [&](int row) -> float4 {
+        const long long i = base + (long long)row * line_stride + 4 * p;
+        float4 f = valid ? prod4(i) : make_float4(0.f, 0.f, 0.f, 0.f);
+        if (o >= 3) {
+            // neighbours zt - 1 and zt + 4: from the threads beside this one
+            // in the row, or loaded at the block's edges
+            float fm = __shfl_up_sync(0xffffffffu, f.w, 1);
+            float fp = __shfl_down_sync(0xffffffffu, f.x, 1);
+            if (p == 0) fm = (valid && zt > 0) ? prod(i - 1) : 0.f;
+            if (p == PAIRS - 1) fp = (valid && zt + 4 <= nz) ? prod(i + 4) : 0.f;
+            const float lv[6] = {fm, f.x, f.y, f.z, f.w, fp};
+            float dv[4];
+#pragma unroll
+            for (int c = 0; c < 4; ++c) {
+                const int iz = zt + c;
+                if (iz == 0) dv[c] = (lv[c + 2] - lv[c + 1]) * ps.dzi;
+                else if (iz == nz) dv[c] = (lv[c + 1] - lv[c]) * ps.dzi;
+                else dv[c] = (lv[c + 2] - lv[c]) * ps.hdzi;
+            }
+            f = make_float4(dv[0], dv[1], dv[2], dv[3]);
+        }
+        // levels above the top wall (padding) enter as zero
+        const int nval = nz + 1 - zt;
+        if (nval < 4) {
+            f.w = 0.f;
+            if (nval < 3) f.z = 0.f;
+            if (nval < 2) f.y = 0.f;
+            if (nval < 1) f.x = 0.f;
+        }
+        return f;
+    };
+    // first radix-8 pass (span 1): butterfly j reads rows j + r N/8 and
+    // writes rows 8 j + r
+    {
+        float2 va[NBT][R], vb[NBT][R];
+#pragma unroll
+        for (int q = 0; q < NBT; ++q) {
+            const int j = g + G * q;
+            if (NB % G == 0 || j < NB) {
+#pragma unroll
+                for (int r = 0; r < R; ++r) {
+                    const float4 x = load(j + r * NB);
+                    va[q][r] = lo2(x);
+                    vb[q][r] = hi2(x);
+                }
+            }
+        }
+#pragma unroll
+        for (int q = 0; q < NBT; ++q) {
+            const int j = g + G * q;
+            if (!(NB % G == 0 || j < NB)) continue;
+            dftR<R, false>(va[q]);
+            dftR<R, false>(vb[q]);
+#pragma unroll
+            for (int r = 0; r < R; ++r) smL[(j * R + r) * PAIRS + p] = f4(va[q][r], vb[q][r]);
+        }
+        __syncthreads();
+    }
+    const long long gs = line_stride >> 2;
+    later_passes<N, false, W, false>(smL, nullptr, gs, valid, 1.0f, tw);
+    // split the two packed real transforms of each lane, store the
+    // Hermitian rows k and N - k (as k_lines32)
+    const float s = rsqrtf((float)N);
+    constexpr int H = N / 2;
+    float4 *ob = reinterpret_cast<float4 *>(out + (long long)o * Nf + base);
+    for (int e = threadIdx.x; e < (H + 1) * PAIRS; e += T) {
+        const int k = e / PAIRS, q = e & (PAIRS - 1);
+        if (z0 + 4 * q >= P) continue;
+        const float4 ck = smL[k * PAIRS + q];
+        const float4 cn = smL[((N - k) & (N - 1)) * PAIRS + q];
+        const float4 re = make_float4(0.5f * (ck.x + cn.x) * s, 0.5f * (ck.y + cn.y) * s, 0.5f * (ck.z + cn.z) * s,
+                                      0.5f * (ck.w + cn.w) * s);
+        ob[k * gs + q] = re;
+        if (k > 0 && k < H)
+            ob[(N - k) * gs + q] = make_float4(0.5f * (ck.y - cn.y) * s, -0.5f * (ck.x - cn.x) * s,
+                                               0.5f * (ck.w - cn.w) * s, -0.5f * (ck.z - cn.z) * s);
+    }
+}
+
+template <int N, int W>
+void launch_prod(cudaStream_t st, const ProdSrc &ps, float *out, int P, int nx, int ny, const float2 *tw)
+{
+    const int ztiles = (P + 2 * LANES - 1) / (2 * LANES);
+    dim3 grid((unsigned)(5 * ztiles), (unsigned)nx);
+    const size_t sm = (size_t)N * LANES * sizeof(float2);
+    k_lines32_prod<N, W><<<grid, LinePlan<N, false, W>::T, sm, st>>>(ps, out, P, P, (long long)ny * P, tw);
+}
+
+// ------------------------------------------------------------------------
 // TMA-fed persistent form (N = 128, 256, 512).  One block per SM owns two
 // tile buffers in shared memory; while it transforms the tile in one
 // buffer, a cp.async.bulk.tensor copy brings its next tile into the other,
@@ -561,6 +717,8 @@ void lines32_init()
     cudaFuncSetAttribute(k_lines32<512, true, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, 512 * LANES * 8);
     cudaFuncSetAttribute(k_lines32<512, false, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, 512 * LANES * 8);
     cudaFuncSetAttribute(k_lines32<512, true, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, 512 * LANES * 8);
+    cudaFuncSetAttribute(k_lines32_prod<1024, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, 1024 * LANES * 8);
+    cudaFuncSetAttribute(k_lines32_prod<512, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, 512 * LANES * 8);
     cudaFuncSetAttribute(k_lines32_tma<512, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, 2 * 512 * 128);
     cudaFuncSetAttribute(k_lines32_tma<512, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, 2 * 512 * 128);
     cudaFuncSetAttribute(k_lines32_tma<256, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, 2 * 256 * 128);
@@ -609,6 +767,24 @@ void launch_lines32(cudaStream_t st, const float *in, float *out, int n, int P, 
     case 512: launch32<512>(st, in, out, P, zv, line_stride, nbatch, batch_stride, inverse, tw, shape); break;
     default: launch32<1024>(st, in, out, P, zv, line_stride, nbatch, batch_stride, inverse, tw, shape); break;
     }
+}
+
+bool lines32_prod_supported(int ny) { return ny == 64 || ny == 128 || ny == 256 || ny == 512 || ny == 1024; }
+
+void lines32_prod_y(cudaStream_t st, const float *vel, const float *vor, float *out, const Dims &d, double dzi,
+                    const float2 *twy, Probe *pr)
+{
+    ProdSrc ps{vel, vor, d.nfield, (float)dzi, (float)(0.5 * dzi), d.nz};
+    if (pr) pr->begin(PROBE_PRODUCTS, st);
+    switch (d.ny) {
+    case 64: launch_prod<64, 0>(st, ps, out, d.P, d.nx, d.ny, twy); break;
+    case 128: launch_prod<128, 0>(st, ps, out, d.P, d.nx, d.ny, twy); break;
+    case 256: launch_prod<256, 0>(st, ps, out, d.P, d.nx, d.ny, twy); break;
+    case 512: launch_prod<512, 0>(st, ps, out, d.P, d.nx, d.ny, twy); break;
+    default: launch_prod<1024, 0>(st, ps, out, d.P, d.nx, d.ny, twy); break;
+    }
+    // algorithmic bytes: six fields read, five written
+    if (pr) pr->end(PROBE_PRODUCTS, st, 11.0 * (double)d.ncol * (double)(d.nz + 1) * sizeof(float));
 }
 
 }  // namespace ps3d

@@ -651,7 +651,21 @@ template <typename T> int source(ps3d_gpu_ctx *c)
     // with the horizontal transform) the FP32 form would amplify the
     // transform's rounding by 1/dz at every level, and in 256^3 and 512^3
     // runs that seeded a growing top-boundary error within about 40 steps
-    if (sizeof(T) == sizeof(float)) {
+    T *f5[5] = {r, q, p, gq, gp};
+    const bool fused_products = sizeof(T) == sizeof(float) && !c->cfg.buoyancy && lines32_prod_supported(d.ny) &&
+                                r + N == q && q + N == p && p + N == gq && gq + N == gp;
+    if (fused_products) {
+        // the five products and their forward y lines in one launch (the
+        // products stay on chip), then the x lines of each
+        lines32_prod_y(c->st, reinterpret_cast<const float *>(vel), reinterpret_cast<const float *>(vor),
+                       reinterpret_cast<float *>(r), d, c->dzi, tf<float2>(c->twy), &c->probe);
+        c->launches += 1;
+        for (int k = 0; k < 5; ++k) {
+            x_forward<float>(d, c->st, reinterpret_cast<const float *>(f5[k]), reinterpret_cast<float *>(f5[k]),
+                             tf<float2>(c->twx), &c->probe);
+            c->launches += 1;
+        }
+    } else if (sizeof(T) == sizeof(float)) {
         op_products_dz<float>(d, c->st, c->dzi, reinterpret_cast<const float *>(vel),
                               reinterpret_cast<const float *>(vor), tf<float>(r), tf<float>(q), tf<float>(p),
                               tf<float>(gq), tf<float>(gp));
@@ -666,14 +680,14 @@ template <typename T> int source(ps3d_gpu_ctx *c)
         op_addf<T>(d, c->st, r, tf<T>(c->buoy));  // c->buoy from buoyancy_tendency
         c->launches += 1;
     }
-    T *f5[5] = {r, q, p, gq, gp};
     if (sizeof(T) == sizeof(float)) {
         // mixed: the tendency is assembled on the semi-spectral fields and
         // decomposed once per component.  The decomposition is linear per
         // column and the harmonic functions depend on |k| only, equal at a
         // column and its x / y partners, so it commutes with D_x, D_y:
         // 3 column transforms instead of 5.
-        for (int k = 0; k < 5; ++k) xyf<T>(c, f5[k], f5[k]);
+        if (!fused_products)
+            for (int k = 0; k < 5; ++k) xyf<T>(c, f5[k], f5[k]);
         if (!c->closure && colz_supported(d.nz)) {
             // tendency components formed inside the column kernels that
             // decompose them (the undecomposed tendency stays on chip)
@@ -2583,7 +2597,7 @@ int ps3d_gpu_probe(ps3d_gpu_ctx *c, int kind)
 {
     int rc = enter(c);
     if (rc) return rc;
-    if (kind < PROBE_OFF || kind > PROBE_LINES) return PS3D_ERR_INVALID_ARG;
+    if (kind < PROBE_OFF || kind > PROBE_PRODUCTS) return PS3D_ERR_INVALID_ARG;
     rc = sync_check(c, "probe");
     if (rc) return rc;
     if (kind != PROBE_OFF && !c->probe.ev) {

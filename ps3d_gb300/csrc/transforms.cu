@@ -149,6 +149,15 @@ void xy_forward(const Dims &d, cudaStream_t st, const T *in, T *out, const typen
     if (pr) pr->end(PROBE_XLINES, st, pass_bytes<T>(d));
 }
 
+// the second half of xy_forward: x lines only
+template <typename T>
+void x_forward(const Dims &d, cudaStream_t st, const T *in, T *out, const typename cplx<T>::type *twx, Probe *pr)
+{
+    if (pr) pr->begin(PROBE_XLINES, st);
+    launch_lines<T>(st, in, out, d.nx, d.P, d.nz + 1, (long long)d.ny * d.P, d.ny, d.P, false, twx, d.line_shape[1]);
+    if (pr) pr->end(PROBE_XLINES, st, pass_bytes<T>(d));
+}
+
 template <typename T>
 void xy_inverse(const Dims &d, cudaStream_t st, const T *in, T *out, const typename cplx<T>::type *twx,
                 const typename cplx<T>::type *twy, Probe *pr)
@@ -326,6 +335,7 @@ template void xy_forward<double>(const Dims &, cudaStream_t, const double *, dou
                                  const double2 *, Probe *);
 template void xy_forward<float>(const Dims &, cudaStream_t, const float *, float *, const float2 *,
                                 const float2 *, Probe *);
+template void x_forward<float>(const Dims &, cudaStream_t, const float *, float *, const float2 *, Probe *);
 template void xy_inverse<double>(const Dims &, cudaStream_t, const double *, double *, const double2 *,
                                  const double2 *, Probe *);
 template void xy_inverse<float>(const Dims &, cudaStream_t, const float *, float *, const float2 *,
