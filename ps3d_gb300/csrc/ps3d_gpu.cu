@@ -14,6 +14,7 @@
 #include <atomic>
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <string>
 #include <vector>
@@ -76,6 +77,9 @@ struct ps3d_gpu_ctx {
     ps3d_gpu_config cfg;
     Dims d;
     bool fp64 = true;
+    // mixed source: products formed inside their forward y-line kernel
+    // (set at creation, see products_fused_default)
+    bool fuse_products = false;
     cudaStream_t st = nullptr;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     std::string err;
@@ -652,8 +656,8 @@ template <typename T> int source(ps3d_gpu_ctx *c)
     // transform's rounding by 1/dz at every level, and in 256^3 and 512^3
     // runs that seeded a growing top-boundary error within about 40 steps
     T *f5[5] = {r, q, p, gq, gp};
-    const bool fused_products = sizeof(T) == sizeof(float) && !c->cfg.buoyancy && lines32_prod_supported(d.ny) &&
-                                r + N == q && q + N == p && p + N == gq && gq + N == gp;
+    const bool fused_products = sizeof(T) == sizeof(float) && c->fuse_products && !c->cfg.buoyancy &&
+                                lines32_prod_supported(d.ny) && r + N == q && q + N == p && p + N == gq && gq + N == gp;
     if (fused_products) {
         // the five products and their forward y lines in one launch (the
         // products stay on chip), then the x lines of each
@@ -1928,6 +1932,20 @@ template <typename T> int allocate_fields(ps3d_gpu_ctx *c)
 
 #define DISPATCH(c, fn, ...) ((c)->fp64 ? fn<double>(__VA_ARGS__) : fn<float>(__VA_ARGS__))
 
+// The fused products kernel saves the products' trip through HBM; while a
+// field fits comfortably in L2 (below 2^24 elements, 64 MB in FP32) there
+// is nothing to save and the plain kernels run faster (the fused first pass
+// reads four fields per output point).  PS3D_FUSE_PRODUCTS=1 or 0 in the
+// environment forces the choice; both give bitwise the same tendency.
+bool products_fused_default(const Dims &d)
+{
+    if (const char *e = getenv("PS3D_FUSE_PRODUCTS")) {
+        if (e[0] == '1') return true;
+        if (e[0] == '0') return false;
+    }
+    return d.nfield >= (1LL << 24);
+}
+
 int enter(ps3d_gpu_ctx *c)
 {
     if (!c) return PS3D_ERR_INVALID_ARG;
@@ -2012,6 +2030,7 @@ int ps3d_gpu_create(const ps3d_gpu_config *cfg, ps3d_gpu_ctx **out)
     d.P = ((nz + 1) + 7) / 8 * 8;
     d.ncol = (long long)nx * ny;
     d.nfield = (long long)d.P * d.ncol;
+    c->fuse_products = products_fused_default(d);
     const int nc[3] = {nx, ny, nz};
     for (int k = 0; k < 3; ++k) c->dx[k] = cfg->extent[k] / (double)nc[k];
     c->ncell = (long long)nx * ny * nz;

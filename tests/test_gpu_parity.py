@@ -262,36 +262,51 @@ def test_mixed_vor2vel_and_source_match_oracle(grid):
 PRODUCT_LINE_GRIDS = [(64, 64, 64), (16, 128, 64), (16, 256, 40), (8, 512, 64), (8, 1024, 64), (8, 512, 120)]
 
 
+def _mixed_source(grid, fuse, monkeypatch):
+    """svorts of the mixed source on the seeded perturbed Beltrami state,
+    with the products formed inside the forward y-line kernel (fuse "1") or
+    by the separate products kernel ("0"); the choice is read when the
+    context is created."""
+    nx, ny, nz = grid
+    lo, ex = ic.BELTRAMI_BOX["lower"], ic.BELTRAMI_BOX["extent"]
+    vor, pert = ic.beltrami_plus_perturbation(nx, ny, nz, seed=6, amplitude=1.0e-2)
+    monkeypatch.setenv("PS3D_FUSE_PRODUCTS", fuse)
+    g = Ps3dGpu(nx, ny, nz, lo, ex, precision="mixed")
+    monkeypatch.delenv("PS3D_FUSE_PRODUCTS")
+    g.setup_fields(vor, pert)
+    g.vor2vel()
+    g.source()
+    return g.get("svorts"), vor, pert
+
+
 @pytest.mark.parametrize("grid", PRODUCT_LINE_GRIDS, ids=lambda g: "x".join(map(str, g)))
-def test_mixed_source_fused_products_match_oracle(grid):
-    """For y line lengths 64..1024 the mixed source forms the five products
-    (and the z derivatives of two of them) inside the forward y-line kernel
-    and the tendency components inside the column kernels that decompose
-    them.  Against the FP64 oracle on the same state.  The tendency of a
-    near-Beltrami flow is a small difference of nearly equal products, so
-    the FP32 rounding of the products and of the line transforms shows at
-    the 1e-4 level, growing with the line length: measured on a GB300,
-    5.8e-5 (64^3), 1.5e-4 (ny = 256), 2.5e-4 (ny = 512), 5.4e-4
-    (ny = 1024), spread evenly over the levels.  On those grids the
-    separate products kernel with the plain line transforms gives bitwise
-    the same tendency, so the tolerance below (about 1.5x the measured
-    value) bounds FP32 rounding, not the fusion.  The column counts put
+def test_mixed_source_fused_products_match_oracle(grid, monkeypatch):
+    """For y line lengths 64..1024 the mixed source can form the five
+    products (and the z derivatives of two of them) inside the forward
+    y-line kernel (the default for fields of 2^24 elements and more; forced
+    here) and the tendency components inside the column kernels that
+    decompose them.  (1) The fused products give bitwise the tendency of the
+    separate products kernel with the plain line transforms.  (2) Against
+    the FP64 oracle on the same state: the tendency of a near-Beltrami flow
+    is a small difference of nearly equal products, so the FP32 rounding of
+    the products and of the line transforms shows at the 1e-4 level, growing
+    with the line length: measured on a GB300, 5.8e-5 (64^3), 1.5e-4
+    (ny = 256), 2.5e-4 (ny = 512), 5.4e-4 (ny = 1024), spread evenly over the
+    levels; the tolerance is about 1.5x that.  The column counts put
     z-derivatives across the edges of the kernel's 32-level z tiles
     (nz = 64, 120) and the top wall inside a tile (nz = 40, 120; those
     column lengths take the unfused tendency assembly)."""
     nx, ny, nz = grid
+    fused, vor, pert = _mixed_source(grid, "1", monkeypatch)
+    plain, _, _ = _mixed_source(grid, "0", monkeypatch)
+    assert np.array_equal(fused, plain)
     lo, ex = ic.BELTRAMI_BOX["lower"], ic.BELTRAMI_BOX["extent"]
-    vor, pert = ic.beltrami_plus_perturbation(nx, ny, nz, seed=6, amplitude=1.0e-2)
     o = oracle.Oracle(nx, ny, nz, lo, ex)
-    g = Ps3dGpu(nx, ny, nz, lo, ex, precision="mixed")
     o.setup_fields(vor, pert)
-    g.setup_fields(vor, pert)
     o.vor2vel()
-    g.vor2vel()
     o.source()
-    g.source()
     tol = {64: 1.0e-4, 128: 2.0e-4, 256: 2.5e-4, 512: 4.0e-4, 1024: 8.0e-4}[max(nx, ny)]
-    err = rel_l2(g.get("svorts"), o.get("svorts"))
+    err = rel_l2(fused, o.get("svorts"))
     assert err < tol, err
 
 
