@@ -188,7 +188,14 @@ int ps3d_gpu_step(ps3d_gpu_ctx *ctx, double *t, double dt);
 int ps3d_gpu_advance(ps3d_gpu_ctx *ctx, double *t, int nsteps, ps3d_gpu_diag *diag);
 /* One advance for a caller that owns the state on the host (the Fortran
  * driver's arrays): upload svor (3 fields), advance once, download svor.
- * PS3D_ERR_INVALID_ARG on a buoyancy context (its state includes sbuoy). */
+ * A state bitwise equal to the device's (the previous call's result) is
+ * taken as it is; any other state is projected first, as set_field does.
+ * Page-locked svor (ps3d_gpu_host_alloc, 16-byte aligned) is read and
+ * written over the host link by the library's kernels; in the mixed form
+ * the upload and its comparison run on a second stream beside the step's
+ * first right-hand side, which is evaluated again from the new state when
+ * the comparison finds a difference.  PS3D_ERR_INVALID_ARG on a buoyancy
+ * context (its state includes sbuoy). */
 int ps3d_gpu_advance_host(ps3d_gpu_ctx *ctx, double *svor, double *t, ps3d_gpu_diag *diag);
 /* calc_vorticity_mean / adjust_vorticity_mean (field_diagnostics.f90:584-619) */
 int ps3d_gpu_calc_vorticity_mean(ps3d_gpu_ctx *ctx, double out[2]);

@@ -256,6 +256,12 @@ void op_spec_bins(const Dims &d, cudaStream_t st, const double *rkx, const doubl
 // host-layout (nz+1)-pitched FP64 columns <-> device P-pitched columns
 void op_unpack_cols(const Dims &d, cudaStream_t st, const double *src, double *dst, int ncomp, int *changed);
 void op_pack_cols(const Dims &d, cudaStream_t st, const double *src, double *dst, int ncomp);
+// host-layout state -> staging array in the device layout, compared bitwise
+// with cmp (*changed raised on a difference); a small persistent grid meant
+// to run beside other kernels.  false (nothing launched): src not 16-byte
+// aligned.
+bool op_unpack_check(const Dims &d, cudaStream_t st, const double *src, const double *cmp, double *dst, int ncomp,
+                     int *changed);
 
 // reductions (adapt, energy series); results are FP64 partials per block
 struct RedOut {

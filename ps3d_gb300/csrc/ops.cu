@@ -1118,6 +1118,58 @@ __global__ void __launch_bounds__(FLAT_T) k_pack_flat(Dims d, const double *__re
     }
 }
 
+// The same copy for a state check that runs beside the step on a second
+// stream: the host state goes into a staging array (device layout) and is
+// compared bitwise with the state it would replace (cmp), which the step
+// reads meanwhile and nobody writes.  A small persistent grid, CHECK_U pairs
+// in flight per thread, keeps the host link busy while leaving the SMs to
+// the step's kernels.
+constexpr int CHECK_BLOCKS = 48, CHECK_U = 8;
+__global__ void __launch_bounds__(FLAT_T) k_unpack_check(Dims d, const double2 *__restrict__ src,
+                                                         const double *__restrict__ cmp, double *__restrict__ dst,
+                                                         long long ncols, float inv_n1, int *__restrict__ changed)
+{
+    const int n1 = d.nz + 1;
+    const long long nchunks = (ncols + FLAT_COLS - 1) / FLAT_COLS;
+    bool diff = false;
+    for (long long ch = blockIdx.x; ch < nchunks; ch += gridDim.x) {
+        const long long c0 = ch * FLAT_COLS;
+        const int ne = (int)min((long long)FLAT_COLS, ncols - c0) * n1;
+        const double2 *s = src + ((c0 * n1) >> 1);
+        const long long tb = c0 * d.P;
+        for (int q0 = threadIdx.x; 2 * q0 < ne; q0 += FLAT_T * CHECK_U) {
+            double2 v[CHECK_U];
+#pragma unroll
+            for (int u = 0; u < CHECK_U; ++u) {
+                const int q = q0 + FLAT_T * u;
+                if (2 * q + 1 < ne) v[u] = s[q];
+                else if (2 * q < ne) v[u].x = reinterpret_cast<const double *>(s)[2 * q];  // odd tail
+            }
+#pragma unroll
+            for (int u = 0; u < CHECK_U; ++u) {
+                const int e = 2 * (q0 + FLAT_T * u);
+                if (e < ne) {
+                    int col, iz;
+                    chunk_pos(e, n1, inv_n1, col, iz);
+                    long long o = tb + (long long)col * d.P + iz;
+                    diff |= __double_as_longlong(v[u].x) != __double_as_longlong(cmp[o]);
+                    dst[o] = v[u].x;
+                    if (e + 1 < ne) {
+                        if (++iz == n1) {
+                            iz = 0;
+                            ++col;
+                        }
+                        o = tb + (long long)col * d.P + iz;
+                        diff |= __double_as_longlong(v[u].y) != __double_as_longlong(cmp[o]);
+                        dst[o] = v[u].y;
+                    }
+                }
+            }
+        }
+    }
+    if (__any_sync(0xffffffffu, diff) && (threadIdx.x & 31) == 0) atomicOr(changed, 1);
+}
+
 __global__ void k_unpack_cols(Dims d, const double *__restrict__ src, double *__restrict__ dst, long long ncols,
                               int *__restrict__ changed)
 {
@@ -1156,6 +1208,16 @@ void op_unpack_cols(const Dims &d, cudaStream_t st, const double *src, double *d
     }
     k_unpack_cols<<<(unsigned)((ncols + COLS_PER_BLOCK - 1) / COLS_PER_BLOCK), COL_BLOCK, 0, st>>>(d, src, dst,
                                                                                                    ncols, changed);
+}
+bool op_unpack_check(const Dims &d, cudaStream_t st, const double *src, const double *cmp, double *dst, int ncomp,
+                     int *changed)
+{
+    if (!aligned16(src)) return false;
+    const long long ncols = (long long)ncomp * d.ncol;
+    const long long nchunks = (ncols + FLAT_COLS - 1) / FLAT_COLS;
+    k_unpack_check<<<(unsigned)(nchunks < CHECK_BLOCKS ? nchunks : CHECK_BLOCKS), FLAT_T, 0, st>>>(
+        d, reinterpret_cast<const double2 *>(src), cmp, dst, ncols, 1.0f / (float)(d.nz + 1), changed);
+    return true;
 }
 void op_pack_cols(const Dims &d, cudaStream_t st, const double *src, double *dst, int ncomp)
 {

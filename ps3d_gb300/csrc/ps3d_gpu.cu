@@ -80,6 +80,13 @@ struct ps3d_gpu_ctx {
     // mixed source: products formed inside their forward y-line kernel
     // (set at creation, see products_fused_default)
     bool fuse_products = false;
+    // advance_host's state check on a second stream beside the first
+    // right-hand side (mixed form): staging array svorf, flag_chk, resolved
+    // by adapt before anything persistent changes
+    cudaStream_t st_chk = nullptr;
+    cudaEvent_t ev_chk0 = nullptr, ev_chk = nullptr;
+    int *flag_chk = nullptr;
+    bool pending_check = false;
     cudaStream_t st = nullptr;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     std::string err;
@@ -745,6 +752,34 @@ double pre_factor(int pretype, double vorch, double bfmax, double rmv, double rm
 }
 
 // adapt (advance.f90:109-377)
+// internal: the state advance_host received differs from the device's;
+// the staged state has been installed and projected, and the right-hand
+// side evaluated so far must be evaluated again (never leaves the library)
+constexpr int RESTART_STATE = -1000;
+
+// Wait for advance_host's state check.  Unchanged: nothing to do (the step
+// runs on the device state, bitwise the host's).  Changed: the staged host
+// state becomes the state, projected in FP64 as set_field does, and the
+// caller starts the step over.
+int resolve_state_check(ps3d_gpu_ctx *c)
+{
+    c->pending_check = false;
+    int changed = 0;
+    cudaStreamWaitEvent(c->st, c->ev_chk, 0);
+    cudaMemcpyAsync(&changed, c->flag_chk, sizeof(int), cudaMemcpyDeviceToHost, c->st);
+    int rc = sync_check(c, "advance_host");
+    if (rc) return rc;
+    if (!changed) return PS3D_OK;
+    // levels 0..nz of every column (the staging array's padding rows hold
+    // whatever the accumulator left there)
+    const size_t pitch = (size_t)c->d.P * sizeof(double);
+    cudaMemcpy2DAsync(c->svor, pitch, c->svorf, pitch, (size_t)(c->d.nz + 1) * sizeof(double), (size_t)3 * c->d.ncol,
+                      cudaMemcpyDeviceToDevice, c->st);
+    project_state_mixed(c);
+    rc = check(c, "advance_host");
+    return rc ? rc : RESTART_STATE;
+}
+
 template <typename T> int adapt(ps3d_gpu_ctx *c, double t, double *dt_out, ps3d_gpu_diag *diag)
 {
     const Dims &d = c->d;
@@ -777,6 +812,11 @@ template <typename T> int adapt(ps3d_gpu_ctx *c, double t, double *dt_out, ps3d_
     if (hflag) return fail(c, PS3D_ERR_DEVICE_LIMIT, "adapt: Jacobi sweep limit reached");
     if (lines32_error()) return fail(c, PS3D_ERR_DEVICE_LIMIT, "line transform: a wait for a tile copy ran out");
     if (colz_error()) return fail(c, PS3D_ERR_DEVICE_LIMIT, "column transform: a staged copy wait ran out or a layout was refused");
+    if (c->pending_check) {
+        // advance_host's state check, before anything persistent changes
+        rc = resolve_state_check(c);
+        if (rc) return rc;
+    }
     const double small = 1.0e-12;
     const double vorch = r2[1] / (small + r2[0]);
     const double ggmax = r2[2], usggmax = r2[3], lsggmax = r2[4];
@@ -1060,6 +1100,12 @@ template <typename T> int advance(ps3d_gpu_ctx *c, double *t, ps3d_gpu_diag *dia
     if (rc) return rc;
     double dt;
     rc = adapt<T>(c, *t, &dt, diag);
+    if (rc == RESTART_STATE) {
+        // advance_host's state differed: evaluate from the new state
+        rc = vor2vel<T>(c);
+        if (rc) return rc;
+        rc = adapt<T>(c, *t, &dt, diag);
+    }
     if (rc) return rc;
     c->closure_fresh = true;
     rc = source<T>(c);
@@ -1880,7 +1926,7 @@ template <typename T> int allocate_fields(ps3d_gpu_ctx *c)
          dalloc(c, &c->ini, 2 * sizeof(double)) && dalloc(c, &c->savg, 2 * sizeof(double)) &&
          dalloc(c, &c->part, (size_t)red_nblocks(d) * RED1_N * sizeof(double)) &&
          dalloc(c, &c->res1, RED1_N * sizeof(double)) && dalloc(c, &c->res2, RED2_N * sizeof(double)) &&
-         dalloc(c, &c->flag, sizeof(int)) && dalloc(c, &c->sc, sizeof(StepScal)) &&
+         dalloc(c, &c->flag, sizeof(int)) && dalloc(c, &c->flag_chk, sizeof(int)) && dalloc(c, &c->sc, sizeof(StepScal)) &&
          dalloc(c, &c->roll_dev, c->roll.hist.size() * sizeof(double));
     if (!ok) return fail(c, PS3D_ERR_OUT_OF_MEMORY, "device allocation failed");
     twiddles<T>(c, c->twx, d.nx);
@@ -2021,8 +2067,11 @@ int ps3d_gpu_create(const ps3d_gpu_config *cfg, ps3d_gpu_ctx **out)
     columns32_init();
     colz_init();
     cudaStreamCreateWithFlags(&c->st, cudaStreamNonBlocking);
+    cudaStreamCreateWithFlags(&c->st_chk, cudaStreamNonBlocking);
     cudaEventCreate(&c->ev0);
     cudaEventCreate(&c->ev1);
+    cudaEventCreateWithFlags(&c->ev_chk0, cudaEventDisableTiming);
+    cudaEventCreateWithFlags(&c->ev_chk, cudaEventDisableTiming);
     Dims &d = c->d;
     d.nx = nx;
     d.ny = ny;
@@ -2064,6 +2113,12 @@ int ps3d_gpu_destroy(ps3d_gpu_ctx *c)
     }
     if (c->ev0) cudaEventDestroy(c->ev0);
     if (c->ev1) cudaEventDestroy(c->ev1);
+    if (c->ev_chk0) cudaEventDestroy(c->ev_chk0);
+    if (c->ev_chk) cudaEventDestroy(c->ev_chk);
+    if (c->st_chk) {
+        cudaStreamSynchronize(c->st_chk);
+        cudaStreamDestroy(c->st_chk);
+    }
     if (c->st) cudaStreamDestroy(c->st);
     delete c;
     return PS3D_OK;
@@ -2396,6 +2451,32 @@ int ps3d_gpu_advance_host(ps3d_gpu_ctx *c, double *svor, double *t, ps3d_gpu_dia
         cudaGetLastError();
     }
     double *stage = mapped ? mapped : c->svorf;
+    if (mapped && !c->fp64) {
+        // mixed form, page-locked state: the host state is read over the
+        // link into the staging array svorf and compared with the device
+        // state on a second stream while the first right-hand side runs
+        // from the device state (vor2vel and adapt's reductions write only
+        // transient fields); adapt waits for the check before anything
+        // persistent changes and restarts the step from the host state if
+        // it differs (resolve_state_check)
+        cudaEventRecord(c->ev_chk0, c->st);
+        cudaStreamWaitEvent(c->st_chk, c->ev_chk0, 0);
+        cudaMemsetAsync(c->flag_chk, 0, sizeof(int), c->st_chk);
+        if (op_unpack_check(d, c->st_chk, mapped, c->svor, c->svorf, 3, c->flag_chk)) {
+            cudaEventRecord(c->ev_chk, c->st_chk);
+            c->pending_check = true;
+            c->launches += 1;
+            rc = ps3d_gpu_advance(c, t, 1, diag);
+            if (c->pending_check) {  // the step stopped before adapt took the check
+                cudaEventSynchronize(c->ev_chk);
+                c->pending_check = false;
+            }
+            if (rc) return rc;
+            op_pack_cols(d, c->st, c->svor, mapped, 3);
+            c->launches += 1;
+            return sync_check(c, "advance_host");
+        }
+    }
     if (!mapped) cudaMemcpyAsync(stage, svor, bytes, cudaMemcpyHostToDevice, c->st);
     cudaMemsetAsync(c->flag, 0, sizeof(int), c->st);
     op_unpack_cols(d, c->st, stage, c->svor, 3, c->flag);
