@@ -11,6 +11,9 @@ vorticity error against it is reported.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
 
+After the headline the same workload runs once more at 1024^3 (mixed form
+only; `large_grid` in the JSON line; --skip-large leaves it out).
+
 With --impl reference the CPU restatement of the reference's algorithm
 (oracle/, FP64, OpenMP over all host cores) is timed instead, one advance at
 256^3 per step (a bounded sample of the same workload, reported per grid
@@ -384,11 +387,11 @@ def run_gpu(args, rank, world, dist):
     krec = best[0]
     achieved = krec["bytes_per_launch"] / (krec["ms_per_launch"] * 1e-3) / 1e9
     # DRAM traffic per launch of the line kernels: ncu read + write bytes of
-    # the 98 line launches of one 512 x 512 x 128 advance (mean 235.3 MB per
+    # the 78 line launches of one 512 x 512 x 128 advance (mean 238.3 MB per
     # launch; profiles/step_traffic_512x512x128.md), scaled to 512^3 by the
     # field size ratio P(512) / P(128) = 520 / 136 (traffic grows with the
     # column pitch at fixed nx, ny); not measured for other kernels or sizes
-    traffic = 235.3e6 * 520.0 / 136.0 if (best[2] == 4 and n == 512) else None
+    traffic = 238.3e6 * 520.0 / 136.0 if (best[2] == 4 and n == 512) else None
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                 "frac": achieved / peak, "traffic": traffic, "traffic_unit": "bytes per launch",
                 "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of the line launches of one "
@@ -467,6 +470,7 @@ def run_gpu(args, rank, world, dist):
 
     closure = closure_timing(dev) if rank == 0 and not args.skip_closure else None
     batch = batch_timing(args.batch_steps) if rank == 0 and not args.skip_batch else None
+    device_bytes, tuning = gm.device_bytes, dict(zip(("shape", "ms_per_launch"), gm.tuning()))
 
     cpu = None
     if rank == 0 and not args.skip_cpu:
@@ -487,14 +491,56 @@ def run_gpu(args, rank, world, dist):
                        "timed_steps": "graph-captured (ps3d_gpu_advance_graph)"},
             "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "fp64": fp64,
             "gpu_launches": launches, "clocks": clocks,
-            "device_bytes": gm.device_bytes,
-            "line_fft_autotune": dict(zip(("shape", "ms_per_launch"), gm.tuning())),
+            "device_bytes": device_bytes,
+            "line_fft_autotune": tuning,
             "cufft_comparator": cufft,
             "closure": closure,
             "batch": batch,
         }
-        print(json.dumps(line), flush=True)
     gm.close()
+    if rank == 0:
+        line["large_grid"] = None if args.skip_large or n >= args.large_n else large_grid_timing(args, dev)
+        print(json.dumps(line), flush=True)
+
+
+def large_grid_timing(args, dev):
+    """The mixed form at large_n^3 (1024^3: the context holds ~225 GB of the
+    GPU's HBM), the same workload with the perturbation built slab by slab
+    on the host; graph-captured steps timed with CUDA events after
+    `warmup` steps, as the headline.  Runs after every other context is
+    closed."""
+    from ps3d_gb300 import Ps3dGpu, ic
+    try:
+        import torch
+        torch.cuda.empty_cache()
+    except Exception:
+        pass
+    n = args.large_n
+    t0 = time.perf_counter()
+    vor, pert = make_ic(n, seed=1)
+    t_ic = time.perf_counter() - t0
+    try:
+        g = Ps3dGpu(n, n, n, ic.BELTRAMI_BOX["lower"], ic.BELTRAMI_BOX["extent"], precision="mixed", device=dev,
+                    **model_kw())
+    except Exception as e:  # not enough device memory on this GPU
+        return {"grid": [n, n, n], "skipped": str(e)[:200]}
+    try:
+        g.setup_fields(vor, pert)
+        del vor, pert
+        t = 0.0
+        for _ in range(max(args.warmup - 1, 1)):
+            t, _ = g.advance(t)
+        t, _, _ = g.advance_graph(t, 1)
+        g.synchronize()
+        with ClockSampler(dev) as clk:
+            t, _, ms = g.advance_graph(t, args.large_steps)
+        ms_step = ms / args.large_steps
+        return {"grid": [n, n, n], "value": float(n) ** 3 / (ms_step * 1e-3) / 1e6, "unit": "Mpts*steps/s",
+                "ms_per_step": ms_step, "steps": args.large_steps, "warmup": args.warmup,
+                "device_bytes": g.device_bytes, "clocks": clk.summary(), "ic_seconds": t_ic,
+                "timed_steps": "graph-captured (ps3d_gpu_advance_graph)"}
+    finally:
+        g.close()
 
 
 def pinned_like(shape):
@@ -544,6 +590,9 @@ def main():
     ap.add_argument("--skip-closure", action="store_true")
     ap.add_argument("--skip-batch", action="store_true")
     ap.add_argument("--batch-steps", type=int, default=500)
+    ap.add_argument("--skip-large", action="store_true")
+    ap.add_argument("--large-n", type=int, default=1024)
+    ap.add_argument("--large-steps", type=int, default=3)
     args = ap.parse_args()
     if args.warmup < 3:
         log("[bench] warm-up raised to 3 steps")
