@@ -282,19 +282,23 @@ void launch32w(cudaStream_t st, const float *in, float *out, int P, int zv, long
 
 // ------------------------------------------------------------------------
 // Forward y lines of the five products of vorticity_tendency straight from
-// the velocity and vorticity (inversion.f90:298-340, mixed form): the first
-// radix-8 pass forms, for the block's output o, the value at each of its
-// (y, z) points from the physical u, omega there,
-//   o = 0: r = u eta - v xi,  1: q = w xi - u zeta,  2: p = v zeta - w eta,
-//   3: dq/dz,  4: dp/dz  (central_diffz, inversion_utils.f90:653-673: one-
-//   sided at iz = 0 and iz = nz, centred in between),
-// so the products never go to HBM.  The z neighbours of a thread's four
-// levels come from the adjacent threads of its row by shuffles, the levels
-// just outside the block's 32 from four scalar loads.  The five blocks of a
-// tile are consecutive (blockIdx.x = 5 * tile + o), so they run together
-// and the velocity and vorticity of the tile come from DRAM about once and
-// from L2 after that.  The remaining passes and the Hermitian stores are
-// those of k_lines32; out holds the five outputs nfield apart.
+// the velocity and vorticity (inversion.f90:298-340, mixed form).  Three
+// blocks per 32-level tile of an x column (blockIdx.x = 3 * tile + o):
+//   o = 0: r = u eta - v xi,
+//   o = 1: q = w xi - u zeta  and dq/dz,
+//   o = 2: p = v zeta - w eta and dp/dz
+// (central_diffz, inversion_utils.f90:653-673: one-sided at iz = 0 and
+// iz = nz, centred in between).  The first radix-8 pass forms the product at
+// each of the block's (y, z) points from the physical u, omega there, so the
+// products never go to HBM; blocks 1 and 2 also form the z derivative from
+// the same values (the z neighbours of a thread's four levels come from the
+// adjacent threads of its row by shuffles, the levels just outside the
+// block's 32 from scalar loads) and park it in the derivative's output tile,
+// which the same threads read back for its own line transform once the
+// product's is stored (the tile is still in L2).  The three blocks of a tile
+// are consecutive, so the tile's velocity and vorticity come from DRAM
+// about once and from L2 after that.  The passes and the Hermitian stores
+// are those of k_lines32; out holds r, q, p, dq/dz, dp/dz nfield apart.
 struct ProdSrc {
     const float *vel, *vor;  // three components each, nfield apart
     long long nfield;
@@ -314,8 +318,8 @@ __global__ void __launch_bounds__(LinePlan<N, false, W>::T, LinePlan<N, false, W
     // row groups are g = 4w..4w+3 and NB is a multiple of 4, so the
     // shuffles below always run on full warps
     static_assert(NB % 4 == 0 && PAIRS == 8, "warp-uniform butterfly ranges");
-    const int o = blockIdx.x % 5;
-    const int z0 = (blockIdx.x / 5) * 2 * LANES;
+    const int o = blockIdx.x % 3;
+    const int z0 = (blockIdx.x / 3) * 2 * LANES;
     const int p = threadIdx.x & (PAIRS - 1), g = threadIdx.x / PAIRS;
     const int zt = z0 + 4 * p;  // first of the thread's four levels
     const bool valid = zt < P;  // P is a multiple of 8: all four or none
@@ -324,10 +328,12 @@ __global__ void __launch_bounds__(LinePlan<N, false, W>::T, LinePlan<N, false, W
     const float *u = ps.vel, *v = ps.vel + Nf, *w = ps.vel + 2 * Nf;
     const float *xi = ps.vor, *eta = ps.vor + Nf, *zeta = ps.vor + 2 * Nf;
     const int nz = ps.nz;
-    // the product of output o (q for 3, p for 4) at one point
+    const int nval = nz + 1 - zt;  // levels of the thread's four below the top wall
+    float *dout = o ? out + (long long)(o + 2) * Nf : nullptr;  // dq/dz or dp/dz
+    // the product of block o at one point
     auto prod = [&](long long i) -> float {
         if (o == 0) return u[i] * eta[i] - v[i] * xi[i];
-        if (o == 1 || o == 3) return w[i] * xi[i] - u[i] * zeta[i];
+        if (o == 1) return w[i] * xi[i] - u[i] * zeta[i];
         return v[i] * zeta[i] - w[i] * eta[i];
     };
     auto prod4 = [&](long long i) -> float4 {
@@ -338,7 +344,7 @@ __global__ void __launch_bounds__(LinePlan<N, false, W>::T, LinePlan<N, false, W
         float4 a, b, c, d;
         if (o == 0) {
             a = *U; b = *E; c = *V; d = *X;
-        } else if (o == 1 || o == 3) {
+        } else if (o == 1) {
             a = *Wv; b = *X; c = *U; d = *Z;
         } else {
             a = *V; b = *Z; c = *Wv; d = *E;
@@ -346,12 +352,22 @@ __global__ void __launch_bounds__(LinePlan<N, false, W>::T, LinePlan<N, false, W
         return make_float4(a.x * b.x - c.x * d.x, a.y * b.y - c.y * d.y, a.z * b.z - c.z * d.z,
                            a.w * b.w - c.w * d.w);
     };
-    // the value the line transform takes at (row, levels zt..zt+3); rows
-    // above the top wall are zero
+    // levels above the top wall (padding) enter as zero
+    auto mask = [&](float4 f) {
+        if (nval < 4) {
+            f.w = 0.f;
+            if (nval < 3) f.z = 0.f;
+            if (nval < 2) f.y = 0.f;
+            if (nval < 1) f.x = 0.f;
+        }
+        return f;
+    };
+    // the product at (row, levels zt..zt+3); blocks 1, 2 write its z
+    // derivative there to their derivative's output tile
     auto load = [&](int row) -> float4 {
         const long long i = base + (long long)row * line_stride + 4 * p;
-        float4 f = valid ? prod4(i) : make_float4(0.f, 0.f, 0.f, 0.f);
-        if (o >= 3) {
+        const float4 f = valid ? prod4(i) : make_float4(0.f, 0.f, 0.f, 0.f);
+        if (o) {
             // neighbours zt - 1 and zt + 4: from the threads beside this one
             // in the row, or loaded at the block's edges
             float fm = __shfl_up_sync(0xffffffffu, f.w, 1);
@@ -367,20 +383,32 @@ __global__ void __launch_bounds__(LinePlan<N, false, W>::T, LinePlan<N, false, W
                 else if (iz == nz) dv[c] = (lv[c + 1] - lv[c]) * ps.dzi;
                 else dv[c] = (lv[c + 2] - lv[c]) * ps.hdzi;
             }
-            f = make_float4(dv[0], dv[1], dv[2], dv[3]);
+            if (valid) *reinterpret_cast<float4 *>(dout + i) = mask(make_float4(dv[0], dv[1], dv[2], dv[3]));
         }
-        // levels above the top wall (padding) enter as zero
-        const int nval = nz + 1 - zt;
-        if (nval < 4) {
-            f.w = 0.f;
-            if (nval < 3) f.z = 0.f;
-            if (nval < 2) f.y = 0.f;
-            if (nval < 1) f.x = 0.f;
-        }
-        return f;
+        return mask(f);
     };
-    // first radix-8 pass (span 1): butterfly j reads rows j + r N/8 and
-    // writes rows 8 j + r
+    const long long gs = line_stride >> 2;
+    const float s = rsqrtf((float)N);
+    constexpr int H = N / 2;
+    // split the two packed real transforms of each lane, store the
+    // Hermitian rows k and N - k (as k_lines32)
+    auto store = [&](float *dst) {
+        float4 *ob = reinterpret_cast<float4 *>(dst + base);
+        for (int e = threadIdx.x; e < (H + 1) * PAIRS; e += T) {
+            const int k = e / PAIRS, q = e & (PAIRS - 1);
+            if (z0 + 4 * q >= P) continue;
+            const float4 ck = smL[k * PAIRS + q];
+            const float4 cn = smL[((N - k) & (N - 1)) * PAIRS + q];
+            const float4 re = make_float4(0.5f * (ck.x + cn.x) * s, 0.5f * (ck.y + cn.y) * s,
+                                          0.5f * (ck.z + cn.z) * s, 0.5f * (ck.w + cn.w) * s);
+            ob[k * gs + q] = re;
+            if (k > 0 && k < H)
+                ob[(N - k) * gs + q] = make_float4(0.5f * (ck.y - cn.y) * s, -0.5f * (ck.x - cn.x) * s,
+                                                   0.5f * (ck.w - cn.w) * s, -0.5f * (ck.z - cn.z) * s);
+        }
+    };
+    // first radix-8 pass (span 1) of the product: butterfly j reads rows
+    // j + r N/8 and writes rows 8 j + r
     {
         float2 va[NBT][R], vb[NBT][R];
 #pragma unroll
@@ -406,32 +434,23 @@ __global__ void __launch_bounds__(LinePlan<N, false, W>::T, LinePlan<N, false, W
         }
         __syncthreads();
     }
-    const long long gs = line_stride >> 2;
     later_passes<N, false, W, false>(smL, nullptr, gs, valid, 1.0f, tw);
-    // split the two packed real transforms of each lane, store the
-    // Hermitian rows k and N - k (as k_lines32)
-    const float s = rsqrtf((float)N);
-    constexpr int H = N / 2;
-    float4 *ob = reinterpret_cast<float4 *>(out + (long long)o * Nf + base);
-    for (int e = threadIdx.x; e < (H + 1) * PAIRS; e += T) {
-        const int k = e / PAIRS, q = e & (PAIRS - 1);
-        if (z0 + 4 * q >= P) continue;
-        const float4 ck = smL[k * PAIRS + q];
-        const float4 cn = smL[((N - k) & (N - 1)) * PAIRS + q];
-        const float4 re = make_float4(0.5f * (ck.x + cn.x) * s, 0.5f * (ck.y + cn.y) * s, 0.5f * (ck.z + cn.z) * s,
-                                      0.5f * (ck.w + cn.w) * s);
-        ob[k * gs + q] = re;
-        if (k > 0 && k < H)
-            ob[(N - k) * gs + q] = make_float4(0.5f * (ck.y - cn.y) * s, -0.5f * (ck.x - cn.x) * s,
-                                               0.5f * (ck.w - cn.w) * s, -0.5f * (ck.z - cn.z) * s);
-    }
+    store(out + (long long)o * Nf);
+    if (!o) return;
+    // the derivative: each thread reads back the values it parked (its own
+    // rows and levels), then the same transform in place
+    __syncthreads();
+    const float4 *gin = reinterpret_cast<const float4 *>(dout + base) + p;
+    pass<N, 8, 1, false, W, true, false>(smL, gin, nullptr, gs, valid, 1.0f, tw, nval);
+    later_passes<N, false, W, false>(smL, nullptr, gs, valid, 1.0f, tw);
+    store(dout);
 }
 
 template <int N, int W>
 void launch_prod(cudaStream_t st, const ProdSrc &ps, float *out, int P, int nx, int ny, const float2 *tw)
 {
     const int ztiles = (P + 2 * LANES - 1) / (2 * LANES);
-    dim3 grid((unsigned)(5 * ztiles), (unsigned)nx);
+    dim3 grid((unsigned)(3 * ztiles), (unsigned)nx);
     const size_t sm = (size_t)N * LANES * sizeof(float2);
     k_lines32_prod<N, W><<<grid, LinePlan<N, false, W>::T, sm, st>>>(ps, out, P, P, (long long)ny * P, tw);
 }
