@@ -386,16 +386,22 @@ def run_gpu(args, rank, world, dist):
     peak, peak_kind = peaks()
     krec = best[0]
     achieved = krec["bytes_per_launch"] / (krec["ms_per_launch"] * 1e-3) / 1e9
-    # DRAM traffic per launch of the line kernels: ncu read + write bytes of
-    # the 78 line launches of one 512 x 512 x 128 advance (mean 238.3 MB per
-    # launch; profiles/step_traffic_512x512x128.md), scaled to 512^3 by the
-    # field size ratio P(512) / P(128) = 520 / 136 (traffic grows with the
-    # column pitch at fixed nx, ny); not measured for other kernels or sizes
-    traffic = 238.3e6 * 520.0 / 136.0 if (best[2] == 4 and n == 512) else None
+    # DRAM traffic of the line kernels per field pass: ncu read + write bytes
+    # of the plain line launches of one 512 x 512 x 128 advance (mean 238.3 MB
+    # per field pass; profiles/step_traffic_512x512x128.md), scaled to 512^3
+    # by the field size ratio P(512) / P(128) = 520 / 136 (traffic grows with
+    # the column pitch at fixed nx, ny), times the field passes per launch (a
+    # launch transforms up to five fields); not measured for other kernels or
+    # sizes
+    traffic = None
+    if best[2] == 4 and n == 512:
+        field_pass = 2.0 * n * n * (n + 1) * 4.0
+        traffic = 238.3e6 * 520.0 / 136.0 * (krec["bytes_per_launch"] / field_pass)
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                 "frac": achieved / peak, "traffic": traffic, "traffic_unit": "bytes per launch",
                 "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of the line launches of one "
-                                  "512x512x128 advance, scaled by 520/136 (profiles/k_lines32_512.md)"
+                                  "512x512x128 advance, per field pass, scaled by 520/136 and by the field "
+                                  "passes per launch (profiles/k_lines32_512.md)"
                 if traffic else None,
                 "kernel": krec["kernel"],
                 "algorithmic_bytes_per_launch": krec["bytes_per_launch"],
@@ -463,7 +469,11 @@ def run_gpu(args, rank, world, dist):
     cufft = None
     if rank == 0:
         cufft = cufft_comparator(n, dev)
-        lp = {p["kernel"]: p["ms_per_launch"] for p in roofline["probes"]}
+        # our time per field for one y pass plus one x pass (a launch may
+        # transform several fields: time per launch over field passes)
+        fp_bytes = 2.0 * n * n * (n + 1) * 4.0
+        lp = {p["kernel"]: p["ms_per_launch"] * fp_bytes / max(p["bytes_per_launch"], 1.0)
+              for p in roofline["probes"]}
         ours = lp.get("k_lines32 (y lines)", 0.0) + lp.get("k_lines32 (x lines)", 0.0)
         if isinstance(cufft, dict) and "forward_xy_ms" in cufft:
             cufft["ours_xy_pass_pair_ms"] = ours

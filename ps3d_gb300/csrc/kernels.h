@@ -56,14 +56,23 @@ struct Probe {
 
 // transforms.cu
 void transforms_init();
+// horizontal transforms of nf consecutive fields (nfield apart), one launch
+// per pass where the FP32 line kernels serve the length
 template <typename T>
 void xy_forward(const Dims &d, cudaStream_t st, const T *in, T *out, const typename cplx<T>::type *twx,
-                const typename cplx<T>::type *twy, Probe *pr);
+                const typename cplx<T>::type *twy, Probe *pr, int nf = 1);
 template <typename T>
-void x_forward(const Dims &d, cudaStream_t st, const T *in, T *out, const typename cplx<T>::type *twx, Probe *pr);
+void x_forward(const Dims &d, cudaStream_t st, const T *in, T *out, const typename cplx<T>::type *twx, Probe *pr,
+               int nf = 1);
+template <typename T>
+void x_inverse(const Dims &d, cudaStream_t st, const T *in, T *out, const typename cplx<T>::type *twx, Probe *pr,
+               int nf = 1);
+template <typename T>
+void y_inverse(const Dims &d, cudaStream_t st, const T *in, T *out, const typename cplx<T>::type *twy, Probe *pr,
+               int nf = 1);
 template <typename T>
 void xy_inverse(const Dims &d, cudaStream_t st, const T *in, T *out, const typename cplx<T>::type *twx,
-                const typename cplx<T>::type *twy, Probe *pr);
+                const typename cplx<T>::type *twy, Probe *pr, int nf = 1);
 template <typename T>
 void columns(const Dims &d, cudaStream_t st, int mode, const T *in, T *out, const T *phim,
              const T *phip, const typename cplx<T>::type *twz2, Probe *pr);
@@ -74,8 +83,10 @@ void lines32_init();
 // n = 512), 1 256-thread blocks (three per SM, n = 512), 2 the TMA-fed
 // persistent kernel (n = 128..512); a shape the length lacks runs the default
 // zv = nz+1 valid z rows; rows zv..P-1 (padding) are read as zero
+// nf fields per launch: field f at in + f fs_in, out + f fs_out
 void launch_lines32(cudaStream_t st, const float *in, float *out, int n, int P, int zv, long long line_stride,
-                    long long nbatch, long long batch_stride, bool inverse, const float2 *tw, int shape = -1);
+                    long long nbatch, long long batch_stride, bool inverse, const float2 *tw, int shape = -1,
+                    int nf = 1, long long fs_in = 0, long long fs_out = 0);
 // kernel shapes at line length n: 0 the default blocks, 1 256-thread blocks
 // (n = 512), 2 the TMA-fed persistent kernel (n = 128, 256, 512)
 bool lines32_has_shape(int n, int w);

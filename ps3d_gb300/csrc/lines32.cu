@@ -230,9 +230,12 @@ __device__ __forceinline__ void later_passes(float4 *sm, float4 *gout, long long
 template <int N, bool INV, int W>
 __global__ void __launch_bounds__(LinePlan<N, INV, W>::T, LinePlan<N, INV, W>::MINB)
     k_lines32(const float *__restrict__ in, float *__restrict__ out, int P, int zv, long long line_stride,
-              long long batch_stride, const float2 *__restrict__ tw)
+              long long batch_stride, const float2 *__restrict__ tw, long long fs_in, long long fs_out)
 {
     extern __shared__ __align__(16) float4 smL[];
+    // several fields per launch: field blockIdx.z at in + z fs_in, out + z fs_out
+    in += blockIdx.z * fs_in;
+    out += blockIdx.z * fs_out;
     constexpr int T = LinePlan<N, INV, W>::T;
     const int p = threadIdx.x & (PAIRS - 1);
     const int z0 = blockIdx.x * 2 * LANES;
@@ -272,11 +275,11 @@ __global__ void __launch_bounds__(LinePlan<N, INV, W>::T, LinePlan<N, INV, W>::M
 
 template <int N, bool INV, int W>
 void launch32w(cudaStream_t st, const float *in, float *out, int P, int zv, long long ls, long long nbatch,
-               long long bs, const float2 *tw)
+               long long bs, const float2 *tw, int nf, long long fs_in, long long fs_out)
 {
-    dim3 grid((P + 2 * LANES - 1) / (2 * LANES), (unsigned)nbatch);
+    dim3 grid((P + 2 * LANES - 1) / (2 * LANES), (unsigned)nbatch, (unsigned)nf);
     const size_t sm = (size_t)N * LANES * sizeof(float2);
-    k_lines32<N, INV, W><<<grid, LinePlan<N, INV, W>::T, sm, st>>>(in, out, P, zv, ls, bs, tw);
+    k_lines32<N, INV, W><<<grid, LinePlan<N, INV, W>::T, sm, st>>>(in, out, P, zv, ls, bs, tw, fs_in, fs_out);
 }
 
 
@@ -697,13 +700,24 @@ bool launch32tma(cudaStream_t st, const float *in, float *out, int P, int zv, lo
 
 template <int N>
 void launch32(cudaStream_t st, const float *in, float *out, int P, int zv, long long ls, long long nbatch,
-              long long bs, bool inverse, const float2 *tw, int shape)
+              long long bs, bool inverse, const float2 *tw, int shape, int nf, long long fs_in, long long fs_out)
 {
-    // shape 2: the TMA-fed persistent kernel (N = 128, 256, 512)
+    // shape 2: the TMA-fed persistent kernel (N = 128, 256, 512), one launch
+    // per field (its tensor map covers one field)
     if constexpr (N >= 128 && N <= 512) {
         if (shape == 2) {
-            const bool ok = inverse ? launch32tma<N, true>(st, in, out, P, zv, ls, nbatch, bs, tw)
-                                    : launch32tma<N, false>(st, in, out, P, zv, ls, nbatch, bs, tw);
+            bool ok = true;
+            for (int f = 0; f < nf && ok; ++f) {
+                const float *fi = in + f * fs_in;
+                float *fo = out + f * fs_out;
+                ok = inverse ? launch32tma<N, true>(st, fi, fo, P, zv, ls, nbatch, bs, tw)
+                             : launch32tma<N, false>(st, fi, fo, P, zv, ls, nbatch, bs, tw);
+                if (!ok && f > 0) {  // the remaining fields with the plain kernel
+                    in = fi;
+                    out = fo;
+                    nf -= f;
+                }
+            }
             if (ok) return;
             shape = -1;
         }
@@ -711,16 +725,16 @@ void launch32(cudaStream_t st, const float *in, float *out, int P, int zv, long 
     if (N == 512) {
         const int w = shape < 0 ? (inverse ? 1 : 0) : shape;
         if (inverse) {
-            if (w) launch32w<N, true, 1>(st, in, out, P, zv, ls, nbatch, bs, tw);
-            else launch32w<N, true, 0>(st, in, out, P, zv, ls, nbatch, bs, tw);
+            if (w) launch32w<N, true, 1>(st, in, out, P, zv, ls, nbatch, bs, tw, nf, fs_in, fs_out);
+            else launch32w<N, true, 0>(st, in, out, P, zv, ls, nbatch, bs, tw, nf, fs_in, fs_out);
         } else {
-            if (w) launch32w<N, false, 1>(st, in, out, P, zv, ls, nbatch, bs, tw);
-            else launch32w<N, false, 0>(st, in, out, P, zv, ls, nbatch, bs, tw);
+            if (w) launch32w<N, false, 1>(st, in, out, P, zv, ls, nbatch, bs, tw, nf, fs_in, fs_out);
+            else launch32w<N, false, 0>(st, in, out, P, zv, ls, nbatch, bs, tw, nf, fs_in, fs_out);
         }
         return;
     }
-    if (inverse) launch32w<N, true, 0>(st, in, out, P, zv, ls, nbatch, bs, tw);
-    else launch32w<N, false, 0>(st, in, out, P, zv, ls, nbatch, bs, tw);
+    if (inverse) launch32w<N, true, 0>(st, in, out, P, zv, ls, nbatch, bs, tw, nf, fs_in, fs_out);
+    else launch32w<N, false, 0>(st, in, out, P, zv, ls, nbatch, bs, tw, nf, fs_in, fs_out);
 }
 
 }  // namespace
@@ -777,14 +791,15 @@ int lines32_error()
 }
 
 void launch_lines32(cudaStream_t st, const float *in, float *out, int n, int P, int zv, long long line_stride,
-                    long long nbatch, long long batch_stride, bool inverse, const float2 *tw, int shape)
+                    long long nbatch, long long batch_stride, bool inverse, const float2 *tw, int shape, int nf,
+                    long long fs_in, long long fs_out)
 {
     switch (n) {
-    case 64: launch32<64>(st, in, out, P, zv, line_stride, nbatch, batch_stride, inverse, tw, shape); break;
-    case 128: launch32<128>(st, in, out, P, zv, line_stride, nbatch, batch_stride, inverse, tw, shape); break;
-    case 256: launch32<256>(st, in, out, P, zv, line_stride, nbatch, batch_stride, inverse, tw, shape); break;
-    case 512: launch32<512>(st, in, out, P, zv, line_stride, nbatch, batch_stride, inverse, tw, shape); break;
-    default: launch32<1024>(st, in, out, P, zv, line_stride, nbatch, batch_stride, inverse, tw, shape); break;
+    case 64: launch32<64>(st, in, out, P, zv, line_stride, nbatch, batch_stride, inverse, tw, shape, nf, fs_in, fs_out); break;
+    case 128: launch32<128>(st, in, out, P, zv, line_stride, nbatch, batch_stride, inverse, tw, shape, nf, fs_in, fs_out); break;
+    case 256: launch32<256>(st, in, out, P, zv, line_stride, nbatch, batch_stride, inverse, tw, shape, nf, fs_in, fs_out); break;
+    case 512: launch32<512>(st, in, out, P, zv, line_stride, nbatch, batch_stride, inverse, tw, shape, nf, fs_in, fs_out); break;
+    default: launch32<1024>(st, in, out, P, zv, line_stride, nbatch, batch_stride, inverse, tw, shape, nf, fs_in, fs_out); break;
     }
 }
 

@@ -225,7 +225,7 @@ template <typename T> T *tmpf(ps3d_gpu_ctx *c, int i) { return tf<T>(c->tmp) + (
 template <typename T> using CT = typename cplx<T>::type;
 
 // launch-count bookkeeping (kernels per host-side operation)
-constexpr int NL_XY = 2, NL_COL = 1, NL_EW = 1;
+constexpr int NL_COL = 1;
 
 // ---------------------------------------------------------------- transfers
 // host (nz+1)-pitched columns <-> device P-pitched columns
@@ -274,15 +274,22 @@ int download(ps3d_gpu_ctx *c, const void *src, bool src_is_fp64, int ncomp, doub
 }
 
 // ------------------------------------------------------------- primitives
-template <typename T> void xyf(ps3d_gpu_ctx *c, const T *in, T *out)
+// launches of one line pass over nf fields: one for the FP32 line kernels,
+// one per field otherwise
+template <typename T> int line_launches(const ps3d_gpu_ctx *c, int n, int nf)
 {
-    xy_forward<T>(c->d, c->st, in, out, tf<CT<T>>(c->twx), tf<CT<T>>(c->twy), &c->probe);
-    c->launches += NL_XY;
+    return (sizeof(T) == sizeof(float) && lines32_supported(n)) ? 1 : nf;
 }
-template <typename T> void xyi(ps3d_gpu_ctx *c, const T *in, T *out)
+// horizontal transforms of nf consecutive fields (nfield apart)
+template <typename T> void xyf(ps3d_gpu_ctx *c, const T *in, T *out, int nf = 1)
 {
-    xy_inverse<T>(c->d, c->st, in, out, tf<CT<T>>(c->twx), tf<CT<T>>(c->twy), &c->probe);
-    c->launches += NL_XY;
+    xy_forward<T>(c->d, c->st, in, out, tf<CT<T>>(c->twx), tf<CT<T>>(c->twy), &c->probe, nf);
+    c->launches += line_launches<T>(c, c->d.ny, nf) + line_launches<T>(c, c->d.nx, nf);
+}
+template <typename T> void xyi(ps3d_gpu_ctx *c, const T *in, T *out, int nf = 1)
+{
+    xy_inverse<T>(c->d, c->st, in, out, tf<CT<T>>(c->twx), tf<CT<T>>(c->twy), &c->probe, nf);
+    c->launches += line_launches<T>(c, c->d.ny, nf) + line_launches<T>(c, c->d.nx, nf);
 }
 template <typename T, typename TIN> void col_any(ps3d_gpu_ctx *c, int mode, const TIN *in, T *out)
 {
@@ -426,13 +433,17 @@ template <typename T> int vor2vel_mixed(ps3d_gpu_ctx *c)
     T *vor = tf<T>(c->vor), *vel = tf<T>(c->vel), *svel = tf<T>(c->svel);
     const Deriv D = c->D();
     // vorticity in physical space (field_combine_physical x3) from the FP32
-    // copy of the state
-    col<T>(c, COL_COMBINE, A32, bs);
-    xyi<T>(c, bs, vor);
-    col<T>(c, COL_COMBINE, B32, bs);
-    xyi<T>(c, bs, vor + N);
+    // copy of the state: the first two components combined straight into
+    // vor, the third into cs (which the horizontal inversion reads below);
+    // x lines of the first two in place and of the third into vor, then the
+    // y lines of all three in one launch
+    col<T>(c, COL_COMBINE, A32, vor);
+    col<T>(c, COL_COMBINE, B32, vor + N);
     col<T>(c, COL_COMBINE, C32, cs);
-    xyi<T>(c, cs, vor + 2 * N);
+    x_inverse<T>(d, c->st, vor, vor, tf<CT<T>>(c->twx), &c->probe, 2);
+    x_inverse<T>(d, c->st, cs, vor + 2 * N, tf<CT<T>>(c->twx), &c->probe, 1);
+    y_inverse<T>(d, c->st, vor, vor, tf<CT<T>>(c->twy), &c->probe, 3);
+    c->launches += line_launches<T>(c, d.nx, 2) + line_launches<T>(c, d.nx, 1) + line_launches<T>(c, d.ny, 3);
     // vertical velocity, mean flow, u, v (inversion.f90:86-213)
     if (columns_w_src_supported(d.nz)) {
         // w and dw/dz in two column kernels that also form the w source ds
@@ -465,7 +476,7 @@ template <typename T> int vor2vel_mixed(ps3d_gpu_ctx *c)
     op_v2v_meanflow<double>(d, c->st, mA, mB, c->tables(), c->ubar, c->vbar);
     op_v2v_uv<T>(d, c->st, D, c->k2l2i, es, cs, c->ubar, c->vbar, svel, svel + N);
     c->launches += 2;
-    for (int k = 0; k < 3; ++k) xyi<T>(c, svel + k * N, vel + k * N);
+    xyi<T>(c, svel, vel, 3);
     return check(c, "vor2vel");
 }
 
@@ -671,11 +682,9 @@ template <typename T> int source(ps3d_gpu_ctx *c)
         lines32_prod_y(c->st, reinterpret_cast<const float *>(vel), reinterpret_cast<const float *>(vor),
                        reinterpret_cast<float *>(r), d, c->dzi, tf<float2>(c->twy), &c->probe);
         c->launches += 1;
-        for (int k = 0; k < 5; ++k) {
-            x_forward<float>(d, c->st, reinterpret_cast<const float *>(f5[k]), reinterpret_cast<float *>(f5[k]),
-                             tf<float2>(c->twx), &c->probe);
-            c->launches += 1;
-        }
+        x_forward<float>(d, c->st, reinterpret_cast<const float *>(r), reinterpret_cast<float *>(r),
+                         tf<float2>(c->twx), &c->probe, 5);
+        c->launches += line_launches<float>(c, d.nx, 5);
     } else if (sizeof(T) == sizeof(float)) {
         op_products_dz<float>(d, c->st, c->dzi, reinterpret_cast<const float *>(vel),
                               reinterpret_cast<const float *>(vor), tf<float>(r), tf<float>(q), tf<float>(p),
@@ -697,8 +706,11 @@ template <typename T> int source(ps3d_gpu_ctx *c)
         // column and the harmonic functions depend on |k| only, equal at a
         // column and its x / y partners, so it commutes with D_x, D_y:
         // 3 column transforms instead of 5.
-        if (!fused_products)
-            for (int k = 0; k < 5; ++k) xyf<T>(c, f5[k], f5[k]);
+        if (!fused_products) {
+            if (r + N == q && q + N == p && p + N == gq && gq + N == gp) xyf<T>(c, r, r, 5);
+            else
+                for (int k = 0; k < 5; ++k) xyf<T>(c, f5[k], f5[k]);
+        }
         if (!c->closure && colz_supported(d.nz)) {
             // tendency components formed inside the column kernels that
             // decompose them (the undecomposed tendency stays on chip)
@@ -783,7 +795,6 @@ int resolve_state_check(ps3d_gpu_ctx *c)
 template <typename T> int adapt(ps3d_gpu_ctx *c, double t, double *dt_out, ps3d_gpu_diag *diag)
 {
     const Dims &d = c->d;
-    const long long N = d.nfield;
     double bfmax = 0.0;
     int rc;
     if (c->cfg.buoyancy) {
@@ -799,7 +810,7 @@ template <typename T> int adapt(ps3d_gpu_ctx *c, double t, double *dt_out, ps3d_
     T *g5 = tmpf<T>(c, 0);
     op_strain_fields<T>(d, c->st, c->D(), tf<T>(c->svel), g5);
     c->launches += 1;
-    for (int k = 0; k < 5; ++k) xyi<T>(c, g5 + k * N, g5 + k * N);
+    xyi<T>(c, g5, g5, 5);
     cudaMemsetAsync(c->flag, 0, sizeof(int), c->st);
     red_pass2<T>(d, c->st, tf<T>(c->vor), g5, vortrms, c->part, c->res2, c->flag);
     c->launches += 2;

@@ -107,15 +107,19 @@ int lines_lanes(int n)
     return B;
 }
 
+// nf fields (field f at in + f fs_in, out + f fs_out): one launch for the
+// FP32 line kernels, one per field otherwise
 template <typename T>
 void launch_lines(cudaStream_t st, const T *in, T *out, int n, int P, int zv, long long line_stride,
                   long long nbatch, long long batch_stride, bool inverse,
-                  const typename cplx<T>::type *tw, int shape = -1)
+                  const typename cplx<T>::type *tw, int shape = -1, int nf = 1, long long fs_in = 0,
+                  long long fs_out = 0)
 {
     if constexpr (sizeof(T) == sizeof(float)) {
         if (lines32_supported(n)) {
             launch_lines32(st, reinterpret_cast<const float *>(in), reinterpret_cast<float *>(out), n, P, zv,
-                           line_stride, nbatch, batch_stride, inverse, reinterpret_cast<const float2 *>(tw), shape);
+                           line_stride, nbatch, batch_stride, inverse, reinterpret_cast<const float2 *>(tw), shape,
+                           nf, fs_in, fs_out);
             return;
         }
     }
@@ -123,10 +127,14 @@ void launch_lines(cudaStream_t st, const T *in, T *out, int n, int P, int zv, lo
     const int logB = ilog2(B);
     dim3 grid((P + 2 * B - 1) / (2 * B), (unsigned)nbatch);
     const size_t sm = 2 * (size_t)n * B * sizeof(typename cplx<T>::type);
-    if (inverse)
-        k_lines<T, true><<<grid, 256, sm, st>>>(in, out, n, logB, P, zv, line_stride, batch_stride, tw);
-    else
-        k_lines<T, false><<<grid, 256, sm, st>>>(in, out, n, logB, P, zv, line_stride, batch_stride, tw);
+    for (int f = 0; f < nf; ++f) {
+        const T *fi = in + f * fs_in;
+        T *fo = out + f * fs_out;
+        if (inverse)
+            k_lines<T, true><<<grid, 256, sm, st>>>(fi, fo, n, logB, P, zv, line_stride, batch_stride, tw);
+        else
+            k_lines<T, false><<<grid, 256, sm, st>>>(fi, fo, n, logB, P, zv, line_stride, batch_stride, tw);
+    }
 }
 
 // algorithmic bytes of one pass over a field: read + write nx*ny*(nz+1)
@@ -135,39 +143,63 @@ template <typename T> static double pass_bytes(const Dims &d)
     return 2.0 * (double)d.ncol * (double)(d.nz + 1) * sizeof(T);
 }
 
+// The horizontal transforms of nf consecutive fields (nfield apart) in one
+// launch per pass.  y lines: line stride P (one column), batches over x
+// (stride ny P); x lines: line stride ny P, batches over y (stride P).
 template <typename T>
-void xy_forward(const Dims &d, cudaStream_t st, const T *in, T *out, const typename cplx<T>::type *twx,
-                const typename cplx<T>::type *twy, Probe *pr)
+void y_forward(const Dims &d, cudaStream_t st, const T *in, T *out, const typename cplx<T>::type *twy, Probe *pr,
+               int nf)
 {
-    // y lines: line stride P (one column), batches over x (stride ny*P)
     if (pr) pr->begin(PROBE_YLINES, st);
-    launch_lines<T>(st, in, out, d.ny, d.P, d.nz + 1, d.P, d.nx, (long long)d.ny * d.P, false, twy, d.line_shape[0]);
-    if (pr) pr->end(PROBE_YLINES, st, pass_bytes<T>(d));
-    // x lines: line stride ny*P, batches over y (stride P)
-    if (pr) pr->begin(PROBE_XLINES, st);
-    launch_lines<T>(st, out, out, d.nx, d.P, d.nz + 1, (long long)d.ny * d.P, d.ny, d.P, false, twx, d.line_shape[1]);
-    if (pr) pr->end(PROBE_XLINES, st, pass_bytes<T>(d));
+    launch_lines<T>(st, in, out, d.ny, d.P, d.nz + 1, d.P, d.nx, (long long)d.ny * d.P, false, twy, d.line_shape[0],
+                    nf, d.nfield, d.nfield);
+    if (pr) pr->end(PROBE_YLINES, st, nf * pass_bytes<T>(d));
 }
 
-// the second half of xy_forward: x lines only
 template <typename T>
-void x_forward(const Dims &d, cudaStream_t st, const T *in, T *out, const typename cplx<T>::type *twx, Probe *pr)
+void x_forward(const Dims &d, cudaStream_t st, const T *in, T *out, const typename cplx<T>::type *twx, Probe *pr,
+               int nf)
 {
     if (pr) pr->begin(PROBE_XLINES, st);
-    launch_lines<T>(st, in, out, d.nx, d.P, d.nz + 1, (long long)d.ny * d.P, d.ny, d.P, false, twx, d.line_shape[1]);
-    if (pr) pr->end(PROBE_XLINES, st, pass_bytes<T>(d));
+    launch_lines<T>(st, in, out, d.nx, d.P, d.nz + 1, (long long)d.ny * d.P, d.ny, d.P, false, twx, d.line_shape[1],
+                    nf, d.nfield, d.nfield);
+    if (pr) pr->end(PROBE_XLINES, st, nf * pass_bytes<T>(d));
+}
+
+template <typename T>
+void x_inverse(const Dims &d, cudaStream_t st, const T *in, T *out, const typename cplx<T>::type *twx, Probe *pr,
+               int nf)
+{
+    if (pr) pr->begin(PROBE_XLINES, st);
+    launch_lines<T>(st, in, out, d.nx, d.P, d.nz + 1, (long long)d.ny * d.P, d.ny, d.P, true, twx, d.line_shape[3],
+                    nf, d.nfield, d.nfield);
+    if (pr) pr->end(PROBE_XLINES, st, nf * pass_bytes<T>(d));
+}
+
+template <typename T>
+void y_inverse(const Dims &d, cudaStream_t st, const T *in, T *out, const typename cplx<T>::type *twy, Probe *pr,
+               int nf)
+{
+    if (pr) pr->begin(PROBE_YLINES, st);
+    launch_lines<T>(st, in, out, d.ny, d.P, d.nz + 1, d.P, d.nx, (long long)d.ny * d.P, true, twy, d.line_shape[2],
+                    nf, d.nfield, d.nfield);
+    if (pr) pr->end(PROBE_YLINES, st, nf * pass_bytes<T>(d));
+}
+
+template <typename T>
+void xy_forward(const Dims &d, cudaStream_t st, const T *in, T *out, const typename cplx<T>::type *twx,
+                const typename cplx<T>::type *twy, Probe *pr, int nf)
+{
+    y_forward<T>(d, st, in, out, twy, pr, nf);
+    x_forward<T>(d, st, out, out, twx, pr, nf);
 }
 
 template <typename T>
 void xy_inverse(const Dims &d, cudaStream_t st, const T *in, T *out, const typename cplx<T>::type *twx,
-                const typename cplx<T>::type *twy, Probe *pr)
+                const typename cplx<T>::type *twy, Probe *pr, int nf)
 {
-    if (pr) pr->begin(PROBE_XLINES, st);
-    launch_lines<T>(st, in, out, d.nx, d.P, d.nz + 1, (long long)d.ny * d.P, d.ny, d.P, true, twx, d.line_shape[3]);
-    if (pr) pr->end(PROBE_XLINES, st, pass_bytes<T>(d));
-    if (pr) pr->begin(PROBE_YLINES, st);
-    launch_lines<T>(st, out, out, d.ny, d.P, d.nz + 1, d.P, d.nx, (long long)d.ny * d.P, true, twy, d.line_shape[2]);
-    if (pr) pr->end(PROBE_YLINES, st, pass_bytes<T>(d));
+    x_inverse<T>(d, st, in, out, twx, pr, nf);
+    y_inverse<T>(d, st, out, out, twy, pr, nf);
 }
 
 // ------------------------------------------------------------------------
@@ -332,14 +364,16 @@ void transforms_init()
 }
 
 template void xy_forward<double>(const Dims &, cudaStream_t, const double *, double *, const double2 *,
-                                 const double2 *, Probe *);
+                                 const double2 *, Probe *, int);
 template void xy_forward<float>(const Dims &, cudaStream_t, const float *, float *, const float2 *,
-                                const float2 *, Probe *);
-template void x_forward<float>(const Dims &, cudaStream_t, const float *, float *, const float2 *, Probe *);
+                                const float2 *, Probe *, int);
 template void xy_inverse<double>(const Dims &, cudaStream_t, const double *, double *, const double2 *,
-                                 const double2 *, Probe *);
+                                 const double2 *, Probe *, int);
 template void xy_inverse<float>(const Dims &, cudaStream_t, const float *, float *, const float2 *,
-                                const float2 *, Probe *);
+                                const float2 *, Probe *, int);
+template void x_forward<float>(const Dims &, cudaStream_t, const float *, float *, const float2 *, Probe *, int);
+template void x_inverse<float>(const Dims &, cudaStream_t, const float *, float *, const float2 *, Probe *, int);
+template void y_inverse<float>(const Dims &, cudaStream_t, const float *, float *, const float2 *, Probe *, int);
 template void columns<double>(const Dims &, cudaStream_t, int, const double *, double *, const double *,
                               const double *, const double2 *, Probe *);
 template void columns<float>(const Dims &, cudaStream_t, int, const float *, float *, const float *,
