@@ -82,7 +82,7 @@ struct ps3d_gpu_ctx {
     bool fuse_products = false;
     // advance_host's state check on a second stream beside the first
     // right-hand side (mixed form): staging array svorf, flag_chk, resolved
-    // by adapt before anything persistent changes
+    // by advance before the stage updates
     cudaStream_t st_chk = nullptr;
     cudaEvent_t ev_chk0 = nullptr, ev_chk = nullptr;
     int *flag_chk = nullptr;
@@ -765,8 +765,8 @@ double pre_factor(int pretype, double vorch, double bfmax, double rmv, double rm
 
 // adapt (advance.f90:109-377)
 // internal: the state advance_host received differs from the device's;
-// the staged state has been installed and projected, and the right-hand
-// side evaluated so far must be evaluated again (never leaves the library)
+// the staged state has been installed and projected, and the first
+// right-hand side must be evaluated again (never leaves the library)
 constexpr int RESTART_STATE = -1000;
 
 // Wait for advance_host's state check.  Unchanged: nothing to do (the step
@@ -823,11 +823,6 @@ template <typename T> int adapt(ps3d_gpu_ctx *c, double t, double *dt_out, ps3d_
     if (hflag) return fail(c, PS3D_ERR_DEVICE_LIMIT, "adapt: Jacobi sweep limit reached");
     if (lines32_error()) return fail(c, PS3D_ERR_DEVICE_LIMIT, "line transform: a wait for a tile copy ran out");
     if (colz_error()) return fail(c, PS3D_ERR_DEVICE_LIMIT, "column transform: a staged copy wait ran out or a layout was refused");
-    if (c->pending_check) {
-        // advance_host's state check, before anything persistent changes
-        rc = resolve_state_check(c);
-        if (rc) return rc;
-    }
     const double small = 1.0e-12;
     const double vorch = r2[1] / (small + r2[0]);
     const double ggmax = r2[2], usggmax = r2[3], lsggmax = r2[4];
@@ -1107,20 +1102,36 @@ template <typename T> int step(ps3d_gpu_ctx *c, double *t, double dt)
 // advance (advance.f90:77-104)
 template <typename T> int advance(ps3d_gpu_ctx *c, double *t, ps3d_gpu_diag *diag)
 {
-    int rc = vor2vel<T>(c);
-    if (rc) return rc;
-    double dt;
-    rc = adapt<T>(c, *t, &dt, diag);
-    if (rc == RESTART_STATE) {
-        // advance_host's state differed: evaluate from the new state
-        rc = vor2vel<T>(c);
+    // advance_host's state check runs beside the first right-hand side
+    // (vor2vel, adapt, source), which writes transient fields and, on the
+    // host, adapt's rolling means (kept here to be put back) and the
+    // diffusion tables (rebuilt by a second adapt); it is resolved before the
+    // stage updates touch the state
+    Rolling keep_roll, keep_roll_b;
+    if (c->pending_check) {
+        keep_roll = c->roll;
+        keep_roll_b = c->roll_b;
+    }
+    double dt = 0.0;
+    for (int pass = 0; pass < 2; ++pass) {
+        int rc = vor2vel<T>(c);
         if (rc) return rc;
         rc = adapt<T>(c, *t, &dt, diag);
+        if (rc) return rc;
+        c->closure_fresh = true;
+        rc = source<T>(c);
+        if (rc) return rc;
+        if (!c->pending_check) break;
+        rc = resolve_state_check(c);
+        if (rc != RESTART_STATE) {
+            if (rc) return rc;
+            break;
+        }
+        // the host state differed: it is installed and projected; evaluate
+        // the right-hand side again from it
+        c->roll = keep_roll;
+        c->roll_b = keep_roll_b;
     }
-    if (rc) return rc;
-    c->closure_fresh = true;
-    rc = source<T>(c);
-    if (rc) return rc;
     return step<T>(c, t, dt);
 }
 
@@ -2466,10 +2477,9 @@ int ps3d_gpu_advance_host(ps3d_gpu_ctx *c, double *svor, double *t, ps3d_gpu_dia
         // mixed form, page-locked state: the host state is read over the
         // link into the staging array svorf and compared with the device
         // state on a second stream while the first right-hand side runs
-        // from the device state (vor2vel and adapt's reductions write only
-        // transient fields); adapt waits for the check before anything
-        // persistent changes and restarts the step from the host state if
-        // it differs (resolve_state_check)
+        // from the device state; advance waits for the check before the
+        // stage updates and evaluates the right-hand side again from the
+        // host state if it differs (resolve_state_check)
         cudaEventRecord(c->ev_chk0, c->st);
         cudaStreamWaitEvent(c->st_chk, c->ev_chk0, 0);
         cudaMemsetAsync(c->flag_chk, 0, sizeof(int), c->st_chk);

@@ -394,8 +394,11 @@ def test_mixed_advance_host_matches_resident_and_projects_changes():
 @pytest.mark.parametrize("precision", ["fp64", "mixed"])
 def test_advance_host_page_locked_equals_pageable(precision):
     """A state buffer from ps3d_gpu_host_alloc is read and written in place by
-    the device (zero copy); a plain numpy buffer goes through the staging
-    copies.  Both give the same state bitwise, including a host-side change."""
+    the device (zero copy; in the mixed form the read and its comparison run
+    beside the first right-hand side); a plain numpy buffer goes through the
+    staging copies.  Both give the same state bitwise, including a host-side
+    change (which makes the mixed form evaluate the first right-hand side
+    again)."""
     from ps3d_gb300.solver import PinnedArray
     lo, ex, vor, pert = beltrami_case(32, seed=12)
     a = Ps3dGpu(32, 32, 32, lo, ex, precision=precision)
@@ -415,7 +418,9 @@ def test_advance_host_page_locked_equals_pageable(precision):
             t_a, da = a.advance_host(plain, t_a)
             t_b, db = b.advance_host(locked.array, t_b)
             assert np.array_equal(plain, locked.array)
-            assert t_a == t_b and da["ke"] == db["ke"]
+            # rmv: adapt's rolling mean, which a changed state's second
+            # evaluation of the first right-hand side must not advance twice
+            assert t_a == t_b and da["ke"] == db["ke"] and da["rmv"] == db["rmv"]
     finally:
         locked.close()
 
@@ -451,7 +456,7 @@ def test_advance_host_page_locked_unaligned_equals_aligned(grid):
             t_a, da = a.advance_host(al.array, t_a)
             t_b, db = b.advance_host(un, t_b)
             assert np.array_equal(al.array, un)
-            assert t_a == t_b and da["ke"] == db["ke"]
+            assert t_a == t_b and da["ke"] == db["ke"] and da["rmv"] == db["rmv"]
         assert np.array_equal(a.get("svor"), al.array)
     finally:
         al.close()
