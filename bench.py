@@ -387,8 +387,9 @@ def run_gpu(args, rank, world, dist):
     krec = best[0]
     achieved = krec["bytes_per_launch"] / (krec["ms_per_launch"] * 1e-3) / 1e9
     # DRAM traffic of the line kernels per field pass: ncu read + write bytes
-    # of the plain line launches of one 512 x 512 x 128 advance (mean 238.3 MB
-    # per field pass; profiles/step_traffic_512x512x128.md), scaled to 512^3
+    # of the plain line launches of one 512 x 512 x 128 advance (21.0 GB over
+    # 78 field passes, 269.3 MB each; profiles/step_traffic_512x512x128.md),
+    # scaled to 512^3
     # by the field size ratio P(512) / P(128) = 520 / 136 (traffic grows with
     # the column pitch at fixed nx, ny), times the field passes per launch (a
     # launch transforms up to five fields); not measured for other kernels or
@@ -396,7 +397,7 @@ def run_gpu(args, rank, world, dist):
     traffic = None
     if best[2] == 4 and n == 512:
         field_pass = 2.0 * n * n * (n + 1) * 4.0
-        traffic = 238.3e6 * 520.0 / 136.0 * (krec["bytes_per_launch"] / field_pass)
+        traffic = 269.3e6 * 520.0 / 136.0 * (krec["bytes_per_launch"] / field_pass)
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                 "frac": achieved / peak, "traffic": traffic, "traffic_unit": "bytes per launch",
                 "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of the line launches of one "
