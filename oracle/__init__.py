@@ -2,7 +2,8 @@
 
 The oracle is a plain-C FP64 restatement of the reference Fortran hot path
 (matt-frey/ps3d).  Only the tests, the smoke entry point and the benchmark's
-CPU-baseline leg use it, as the checker; the GPU product path never calls it.
+CPU-baseline leg use it, to check results and to time the CPU; the GPU
+product path never calls it.
 Parity pinning: see tests/test_oracle_kat.py (the reference's own known-answer
 unit tests, ported).
 """
