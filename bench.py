@@ -198,7 +198,8 @@ def closure_timing(dev, n=64):
     """The learned closure's forward pass (four BF16 tensor-core 3x3x3
     convolutions, closure.cu) at n^3 against the measured bf16 peak, and its
     cost inside a coarse step: one captured impl-diff-rk4 advance at n^3 with
-    and without a network evaluated at every stage."""
+    and without a network evaluated at every stage, each also per unit of
+    model time against the fine (4n)^3 mixed run (the closure's bar: 1/20)."""
     try:
         from ps3d_gb300 import Ps3dGpu, ic
         from ps3d_gb300.closure import Closure, attach, forward_flops, param_views
@@ -230,27 +231,37 @@ def closure_timing(dev, n=64):
                 pk, src = float(json.load(f)["bf16_tflops"]), "measured (MEASURED_PEAKS.json bf16_tflops)"
         except (OSError, KeyError, ValueError):
             pk, src = 1900.0, "fallback"
-        vor, pert = ic.beltrami_plus_perturbation(n, n, n, seed=1, amplitude=1.0e-2)
-        steps = {}
-        for name, net in (("plain", None), ("closure_every_stage", cl)):
-            m = Ps3dGpu(n, n, n, ic.BELTRAMI_BOX["lower"], ic.BELTRAMI_BOX["extent"], precision="mixed",
+        def timed_run(nn, net=None):
+            # 20 captured advances after 3; ms per step and the mean dt
+            vv, pp = ic.beltrami_plus_perturbation(nn, nn, nn, seed=1, amplitude=1.0e-2)
+            m = Ps3dGpu(nn, nn, nn, ic.BELTRAMI_BOX["lower"], ic.BELTRAMI_BOX["extent"], precision="mixed",
                         device=dev, **model_kw())
-            m.setup_fields(vor, pert)
+            m.setup_fields(vv, pp)
             if net is not None:
                 attach(m, net, every_stage=True)
-            t, _, _ = m.advance_graph(0.0, 3)
-            _, _, mss = m.advance_graph(t, 20)
-            steps[name] = mss / 20
+            t0, _, _ = m.advance_graph(0.0, 3)
+            t1, _, mss = m.advance_graph(t0, 20)
             if net is not None:
                 attach(m, None)
             m.close()
+            return mss / 20, (t1 - t0) / 20
+        steps, dts = {}, {}
+        for name, net in (("plain", None), ("closure_every_stage", cl)):
+            steps[name], dts[name] = timed_run(n, net)
         cl.close()
+        # the cost of a unit of model time against the fine (4n)^3 run of the
+        # mixed form that the closure stands in for
+        nf = 4 * n
+        fine_ms, fine_dt = timed_run(nf)
+        per_time = {k: (steps[k] / dts[k]) / (fine_ms / fine_dt) for k in steps}
         return {"grid": [n, n, n], "engine": eng_best, "ms_per_forward_by_engine": engines,
                 "ms_per_forward": ms, "flops_per_forward": forward_flops(npts),
                 "roofline": {"bound": "tensor", "achieved": tf, "peak": pk, "unit": "TFLOP/s", "frac": tf / pk,
                              "peak_source": src},
                 "tflops_padded_channels": forward_flops(npts, True) / (ms * 1e9),
-                "step_ms": steps}
+                "step_ms": steps, "mean_dt": dts,
+                "fine_mixed": {"grid": [nf, nf, nf], "ms_per_step": fine_ms, "mean_dt": fine_dt},
+                "cost_per_model_time_vs_fine_mixed": per_time}
     except Exception as e:
         return {"unavailable": str(e)[:200]}
 
