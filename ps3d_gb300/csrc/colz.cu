@@ -1031,7 +1031,7 @@ __global__ void __launch_bounds__(256, M <= 16 ? 3 : 2)
     k_colz_src(const float *__restrict__ fs, const float *__restrict__ fh, float *__restrict__ out,
                float *__restrict__ es, int P, int ny, long long npairs, const double *__restrict__ k2l2,
                const double *__restrict__ cxv, const double *__restrict__ cyv, float dz, float Lz,
-               const float2 *__restrict__ twn, const float *__restrict__ sinz)
+               const float2 *__restrict__ twn, const float *__restrict__ sinz, const float *__restrict__ corr)
 {
     constexpr int n = 32 * M;
     constexpr bool ST = staged<M, float>();
@@ -1126,6 +1126,17 @@ __global__ void __launch_bounds__(256, M <= 16 ? 3 : 2)
             if (lane < 2) {
                 float *zc = lane ? zB : zA;
                 zc[n] = comb(zc[n], fh[(lane ? hB : hA) + n], lane ? cyB : cyA);
+            }
+            if (corr) {
+                // an attached closure's correction of this component (the
+                // pair's own columns), added as the separate add would
+                __syncwarp();
+                for (int i = lane; i < 2 * (n + 1); i += 32) {
+                    const bool b = i > n;
+                    const int z = b ? i - (n + 1) : i;
+                    float *zp = (b ? zB : zA) + z;
+                    *zp = *zp + corr[(b ? oB : oA) + z];
+                }
             }
             __syncwarp();
         }
@@ -1325,16 +1336,18 @@ void launch_dec2_m(const Dims &d, cudaStream_t st, const float *f, float *out, f
 template <int M>
 void launch_src_m(const Dims &d, cudaStream_t st, const float *r, const float *q, const float *p, const float *gq,
                   const float *gp, float *s1, float *s2, float *s3, float *es, const double *k2l2,
-                  const double *cx, const double *cy, float dz, float Lz, const float2 *twn, const float *sinz)
+                  const double *cx, const double *cy, float dz, float Lz, const float2 *twn, const float *sinz,
+                  const float *corr)
 {
     const long long npairs = d.ncol / 2;
+    const long long N = d.nfield;
     const size_t smem = colz_smem<M>(true, d.P);
     k_colz_src<M, 1><<<colz_grid(k_colz_src<M, 1>, smem, npairs), 256, smem, st>>>(
-        gq, r, s1, nullptr, d.P, d.ny, npairs, k2l2, cx, cy, dz, Lz, twn, sinz);
+        gq, r, s1, nullptr, d.P, d.ny, npairs, k2l2, cx, cy, dz, Lz, twn, sinz, corr);
     k_colz_src<M, 2><<<colz_grid(k_colz_src<M, 2>, smem, npairs), 256, smem, st>>>(
-        gp, r, s2, nullptr, d.P, d.ny, npairs, k2l2, cx, cy, dz, Lz, twn, sinz);
+        gp, r, s2, nullptr, d.P, d.ny, npairs, k2l2, cx, cy, dz, Lz, twn, sinz, corr ? corr + N : nullptr);
     k_colz_src<M, 3><<<colz_grid(k_colz_src<M, 3>, smem, npairs), 256, smem, st>>>(
-        q, p, s3, es, d.P, d.ny, npairs, k2l2, cx, cy, dz, Lz, twn, sinz);
+        q, p, s3, es, d.P, d.ny, npairs, k2l2, cx, cy, dz, Lz, twn, sinz, corr ? corr + 2 * N : nullptr);
 }
 
 // every column kernel may take up to the device's opt-in shared memory per
@@ -1442,16 +1455,17 @@ void columns_dec2(const Dims &d, cudaStream_t st, const float *f, float *out, fl
 
 void columns_src(const Dims &d, cudaStream_t st, const float *r, const float *q, const float *p, const float *gq,
                  const float *gp, float *s1, float *s2, float *s3, float *es, const double *k2l2, const double *cx,
-                 const double *cy, float dz, float Lz, const float2 *twn, const float *sinz, Probe *pr)
+                 const double *cy, float dz, float Lz, const float2 *twn, const float *sinz, Probe *pr,
+                 const float *corr)
 {
     if (!colz_layout_ok(d, r, q, p) || !colz_layout_ok(d, gq, gp, es) || !colz_layout_ok(d, s1, s2, s3)) return;
     if (pr) pr->begin(PROBE_COLUMNS, st);
     switch (d.nz) {
-    case 64: launch_src_m<2>(d, st, r, q, p, gq, gp, s1, s2, s3, es, k2l2, cx, cy, dz, Lz, twn, sinz); break;
-    case 128: launch_src_m<4>(d, st, r, q, p, gq, gp, s1, s2, s3, es, k2l2, cx, cy, dz, Lz, twn, sinz); break;
-    case 256: launch_src_m<8>(d, st, r, q, p, gq, gp, s1, s2, s3, es, k2l2, cx, cy, dz, Lz, twn, sinz); break;
-    case 512: launch_src_m<16>(d, st, r, q, p, gq, gp, s1, s2, s3, es, k2l2, cx, cy, dz, Lz, twn, sinz); break;
-    default: launch_src_m<32>(d, st, r, q, p, gq, gp, s1, s2, s3, es, k2l2, cx, cy, dz, Lz, twn, sinz); break;
+    case 64: launch_src_m<2>(d, st, r, q, p, gq, gp, s1, s2, s3, es, k2l2, cx, cy, dz, Lz, twn, sinz, corr); break;
+    case 128: launch_src_m<4>(d, st, r, q, p, gq, gp, s1, s2, s3, es, k2l2, cx, cy, dz, Lz, twn, sinz, corr); break;
+    case 256: launch_src_m<8>(d, st, r, q, p, gq, gp, s1, s2, s3, es, k2l2, cx, cy, dz, Lz, twn, sinz, corr); break;
+    case 512: launch_src_m<16>(d, st, r, q, p, gq, gp, s1, s2, s3, es, k2l2, cx, cy, dz, Lz, twn, sinz, corr); break;
+    default: launch_src_m<32>(d, st, r, q, p, gq, gp, s1, s2, s3, es, k2l2, cx, cy, dz, Lz, twn, sinz, corr); break;
     }
     // six fields read, four written (three launches)
     if (pr) pr->end(PROBE_COLUMNS, st, 10.0 * (double)d.ncol * (double)(d.nz + 1) * sizeof(float));

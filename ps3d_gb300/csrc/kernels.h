@@ -122,10 +122,13 @@ void columns_w_src(const Dims &d, cudaStream_t st, const float *A, const float *
                    const double *k2l2, const double *k2l2i, const double *cx, const double *cy, float dz, float Lz,
                    const float2 *twn, const float *sinz, const float *cosz, Probe *pr);
 // the tail of the mixed source: tendency components from the transformed
-// products, decomposed, and es (three column kernels)
+// products, decomposed, and es (three column kernels); corr (nullable): an
+// attached closure's semi-spectral correction, three fields nfield apart,
+// added to the components before their decomposition
 void columns_src(const Dims &d, cudaStream_t st, const float *r, const float *q, const float *p, const float *gq,
                  const float *gp, float *s1, float *s2, float *s3, float *es, const double *k2l2, const double *cx,
-                 const double *cy, float dz, float Lz, const float2 *twn, const float *sinz, Probe *pr);
+                 const double *cy, float dz, float Lz, const float2 *twn, const float *sinz, Probe *pr,
+                 const float *corr = nullptr);
 void columns_dec2(const Dims &d, cudaStream_t st, const float *f, float *out, float *es, const double *k2l2,
                   float dz, float Lz, const float2 *twn, const float *sinz, Probe *pr);
 // FP32 warp-per-column-pair transforms (columns32.cu), nz = 32..512

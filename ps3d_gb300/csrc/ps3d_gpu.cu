@@ -634,9 +634,13 @@ template <typename T> int closure_correction(ps3d_gpu_ctx *c)
         closure_apply<T>(c->closure, c->st, tf<T>(c->vor), tf<T>(c->vel), N, c->d.P, corr, N, c->closure_flags);
     c->launches += CLOSURE_LAUNCHES;
     if (rc) return check(c, "closure");
-    for (int k = 0; k < 3; ++k) {
-        xyf<T>(c, corr + k * N, corr + k * N);
-        if (sizeof(T) == sizeof(double)) col<T>(c, COL_DECOMP, corr + k * N, corr + k * N);
+    if (sizeof(T) == sizeof(float)) {
+        xyf<T>(c, corr, corr, 3);  // the three components in one launch per pass
+    } else {
+        for (int k = 0; k < 3; ++k) {
+            xyf<T>(c, corr + k * N, corr + k * N);
+            col<T>(c, COL_DECOMP, corr + k * N, corr + k * N);
+        }
     }
     c->closure_fresh = false;
     return PS3D_OK;
@@ -711,14 +715,16 @@ template <typename T> int source(ps3d_gpu_ctx *c)
             else
                 for (int k = 0; k < 5; ++k) xyf<T>(c, f5[k], f5[k]);
         }
-        if (!c->closure && colz_supported(d.nz)) {
+        if (colz_supported(d.nz)) {
             // tendency components formed inside the column kernels that
-            // decompose them (the undecomposed tendency stays on chip)
+            // decompose them (the undecomposed tendency stays on chip), an
+            // attached closure's correction added there
             const Deriv D = c->D();
             auto f = [](T *x) { return reinterpret_cast<float *>(x); };
             columns_src(d, c->st, f(r), f(q), f(p), f(gq), f(gp), f(svorts), f(svorts + N), f(svorts + 2 * N),
                         reinterpret_cast<float *>(c->es_src), c->k2l2, D.cx, D.cy, (float)c->dx[2],
-                        (float)c->cfg.extent[2], c->twz32, c->sinz32, &c->probe);
+                        (float)c->cfg.extent[2], c->twz32, c->sinz32, &c->probe,
+                        c->closure ? reinterpret_cast<const float *>(c->corr) : nullptr);
             c->launches += 3;
             return check(c, "source");
         }
